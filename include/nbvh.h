@@ -1,0 +1,449 @@
+/*
+ * nbvh.h -- C ABI of the GB300-native N-BVH ray-query library (libnbvh.so).
+ *
+ * This header is the drop-in boundary for the neural ray-query path of the N-BVH renderer
+ * (WeiPhil/nbvh). The reference exposes that path as C++ classes whose state lives in CUDA
+ * __constant__ globals; every entry point below replaces one member of that surface and cites it.
+ *
+ *   reference surface                                          entry point here
+ *   --------------------------------------------------------   --------------------------------------
+ *   NeuralBVHModule ctor / reinitialise_neural_model            nbvh_create
+ *     (include/cuda/neural/neural_bvh_module.h:144-241,
+ *      src/cuda/neural/neural_bvh_module.cu:118-263)
+ *   CudaBackend::load_scene / build_blas                        nbvh_set_mesh, nbvh_build_classic
+ *     (src/cuda/cuda_backend.cpp:138-310)
+ *   NeuralBVHRenderer::build_and_upload_neural_bvh              nbvh_build_neural_cut
+ *     (src/cuda/neural/neural_bvh_renderer_accel.cpp:504-557)
+ *   non_neural_bvh_intersection -> CudaBVH2::intersect<false>   nbvh_query_closest_classic
+ *     (src/cuda/neural/path/path_inference_kernels.cu:195-222,
+ *      include/cuda/accel/bvh2.cuh:12-88)
+ *   CudaBVH2::intersect<true> (shadow rays)                     nbvh_query_any_classic
+ *   neural_bvh_traversal + process_neural_bvh_traversal_step    nbvh_query_closest_neural
+ *     (src/cuda/neural/path/path_module.cu:54-137,
+ *      src/cuda/neural/path/path_inference_kernels.cu:61-131)
+ *   neural_node_traversal(visibility_query_only = true)         nbvh_query_visibility_neural
+ *     (include/cuda/neural/neural_bvh_module_common.cuh:160-209)
+ *   NeuralBVHRendererConstants::ignore_neural_blas              nbvh_set_ignore_neural_blas
+ *     (include/cuda/neural/neural_bvh_renderer_constants.cuh:19,
+ *      include/cuda/neural/neural_bvh_module_common.cuh:323)
+ *   NeuralBVHRenderer::render, m_run_optimisation branch        nbvh_run_optimisation
+ *     (src/cuda/neural/neural_bvh_renderer.cu:141-288)
+ *   NeuralBVHRenderer::render, m_run_inference branch           nbvh_run_inference
+ *     (src/cuda/neural/neural_bvh_renderer.cu:299-379)
+ *   trainer->serialize / deserialize, save/load of .nbvh        nbvh_save, nbvh_load
+ *     (src/cuda/neural/neural_bvh_renderer_init.cu:385-404,
+ *      src/cuda/neural/neural_bvh_renderer_accel.cpp:170-254)
+ *
+ * Conventions.
+ *  - Every call returns an nbvh_status; nothing throws or exits across this boundary. The
+ *    reference throws (CUDA_CHECK, src/ntwr.h:30-39) or calls exit(2) (CUDA_SYNC_CHECK,
+ *    src/ntwr.h:46-54); here the message of the last failure is kept per handle and returned by
+ *    nbvh_last_error.
+ *  - Buffers named d_* are device pointers on the handle's device; h_* are host pointers. Query
+ *    calls are asynchronous on the given stream (NULL = the legacy default stream) unless stated.
+ *  - A handle serialises its calls with an internal mutex: it is safe to call from several host
+ *    threads, and two handles share no state (the reference keeps its state in __constant__
+ *    globals, which allows one model per process).
+ *  - The library has no CPU fallback: when the CUDA device is missing every call that needs it
+ *    returns NBVH_EDEVICE.
+ */
+#ifndef NBVH_H
+#define NBVH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBVH_ABI_VERSION 1u
+
+typedef struct nbvh_handle nbvh_handle;
+typedef struct CUstream_st *nbvh_stream; /* identical to cudaStream_t */
+
+typedef enum nbvh_status {
+    NBVH_OK        = 0,
+    NBVH_EINVAL    = 1, /* bad argument, size or configuration */
+    NBVH_ENOMEM    = 2, /* device or pinned-host allocation failed */
+    NBVH_EDEVICE   = 3, /* CUDA runtime error or no usable device */
+    NBVH_ETIMEOUT  = 4, /* a bounded device-side loop gave up (step cap reached) */
+    NBVH_EOVERFLOW = 5, /* a traversal stack overflowed on the device */
+    NBVH_ESTATE    = 6, /* call order violated (e.g. query before build) */
+    NBVH_EIO       = 7  /* checkpoint file could not be read or written, or is malformed */
+} nbvh_status;
+
+/* ---------------------------------------------------------------------------------------------
+ * Ray and hit records
+ * ------------------------------------------------------------------------------------------- */
+
+/* Ray3f (include/cuda/base/ray.cuh:65-77): origin, tmin (default 1e-4), direction, tmax
+ * (default FLT_MAX). 32 bytes, 16-byte aligned arrays are loaded with two 128-bit loads. */
+typedef struct nbvh_ray {
+    float o[3];
+    float tmin;
+    float d[3];
+    float tmax;
+} nbvh_ray;
+
+/* PreliminaryItsData (include/cuda/base/ray.cuh:22-35) without mesh_idx: t = FLT_MAX and
+ * prim = 0xFFFFFFFF when the ray misses. u, v are the barycentrics of the reference's
+ * Moller-Trumbore test (include/cuda/accel/bvh.cuh:98-136). 16 bytes. */
+typedef struct nbvh_hit {
+    float t;
+    float u;
+    float v;
+    uint32_t prim;
+} nbvh_hit;
+
+#define NBVH_HIT_VALID 0x1u            /* the query found a surface */
+#define NBVH_HIT_CLASSIC_FALLBACK 0x2u /* the answer came from the classic BLAS */
+#define NBVH_HIT_STEP_CAP 0x4u         /* the neural loop hit max_traversal_steps for this ray */
+
+/* NeuralTraversalResult (src/cuda/neural/path/path_inference_kernels.cu:14-32) plus the network
+ * visibility of the accepted segment and the number of leaf segments inferred. 48 bytes. */
+typedef struct nbvh_neural_hit {
+    float t;          /* FLT_MAX when no hit */
+    float normal[3];  /* normalize(2 * o[2:5] - 1) of the accepted segment */
+    float albedo[3];  /* o[5:8] of the accepted segment */
+    float visibility; /* sigmoid visibility output of the accepted segment (0 if none) */
+    uint32_t flags;   /* NBVH_HIT_* */
+    uint32_t segments;
+    uint32_t prim;    /* classic prim id when NBVH_HIT_CLASSIC_FALLBACK, else 0xFFFFFFFF */
+    uint32_t reserved;
+} nbvh_neural_hit;
+
+/* ---------------------------------------------------------------------------------------------
+ * Configuration (keys mirror the reference JSON: bvh_constants, pt_output_constants,
+ * bvh_module_constants, segment_encoding.hashgrid_options, network, optimizer)
+ * ------------------------------------------------------------------------------------------- */
+
+typedef enum nbvh_loss_type { /* loss_types, include/cuda/neural/utils/tcnn_config.h:23-36 */
+    NBVH_LOSS_RELATIVE_L2 = 0,
+    NBVH_LOSS_L2          = 1,
+    NBVH_LOSS_RELATIVE_L1 = 2,
+    NBVH_LOSS_L1          = 3,
+    NBVH_LOSS_BCE         = 5,
+    NBVH_LOSS_LOG_L2      = 6,
+    NBVH_LOSS_L_HALF      = 7
+} nbvh_loss_type;
+
+typedef enum nbvh_segment_distribution { /* neural_bvh_module.h:23-25 */
+    NBVH_SEGMENT_EQUIDISTANT_INTERIOR = 0,
+    NBVH_SEGMENT_EQUIDISTANT_EXTERIOR = 1,
+    NBVH_SEGMENT_UNIFORM              = 2
+} nbvh_segment_distribution;
+
+typedef enum nbvh_precision {
+    NBVH_PRECISION_FP16 = 0, /* MLP operands FP16, FP32 accumulation */
+    NBVH_PRECISION_BF16 = 1, /* MLP operands BF16, FP32 accumulation */
+    NBVH_PRECISION_FP8  = 2  /* hidden layers FP8-E4M3 (per-tensor scale), first/last layer FP16 */
+} nbvh_precision;
+
+/* HashGridOptions, include/cuda/neural/utils/tcnn_config.h:69-78. n_features_per_level must be 2;
+ * input_segment_points * n_levels * 2 must be a multiple of 16 and at most 128. */
+typedef struct nbvh_hashgrid_options {
+    int32_t n_levels;
+    int32_t n_features_per_level;
+    int32_t log2_hashmap_size;
+    int32_t base_resolution;
+    float per_level_scale;
+} nbvh_hashgrid_options;
+
+/* NetworkOptions, tcnn_config.h:221-233: ReLU hidden layers, Sigmoid output, no biases.
+ * n_neurons must be 64; n_hidden_layers in [1, 8]. */
+typedef struct nbvh_network_options {
+    int32_t n_neurons;
+    int32_t n_hidden_layers;
+    int32_t precision; /* nbvh_precision */
+} nbvh_network_options;
+
+/* OptimizerOptions (Adam wrapped in ExponentialDecay), tcnn_config.h:150-166 and
+ * neural_bvh_module.cu:146-168. loss_scale multiplies the output gradient before the FP16
+ * backward pass and is divided out in the Adam step. */
+typedef struct nbvh_optimizer_options {
+    float learning_rate;
+    float beta1;
+    float beta2;
+    float epsilon;
+    float l2_reg;
+    int32_t decay_start;
+    int32_t decay_interval;
+    float decay_base;
+    float loss_scale;
+} nbvh_optimizer_options;
+
+/* NeuralBVHRendererConstants, include/cuda/neural/neural_bvh_renderer_constants.cuh:13-46. */
+typedef struct nbvh_bvh_constants {
+    float inference_mint_epsilon;
+    float inference_maxt_epsilon;
+    float learning_mint_epsilon;
+    float learning_maxt_epsilon;
+    float sampling_bbox_scaling;
+    float fixed_node_dilation;
+    float node_extent_dilation;
+    float leaf_boundary_sampling_ratio;
+    int32_t ignore_neural_blas;
+    int32_t max_training_bounces;
+    int32_t sample_cosine_weighted;
+    int32_t backface_bounce_training;
+    int32_t log2_bvh_max_traversals;
+} nbvh_bvh_constants;
+
+/* PathTracingOutputConstants, include/cuda/neural/neural_bvh_module.h:243-302. The output
+ * layout is fixed at visibility(1), LocalT depth(1), normal(3), albedo(3), padded to 16. */
+typedef struct nbvh_output_constants {
+    int32_t visibility_loss; /* nbvh_loss_type */
+    float visibility_loss_scale;
+    int32_t depth_loss;
+    float depth_loss_scale;
+    int32_t normal_loss;
+    float normal_loss_scale;
+    int32_t albedo_loss;
+    float albedo_loss_scale;
+    int32_t output_normal_linear_activation;
+    int32_t output_albedo_linear_activation;
+    int32_t visibility_masking_loss;
+    float primary_visibility_threshold;
+    float secondary_visibility_threshold;
+    float depth_epsilon;
+    float fixed_depth_epsilon;
+    int32_t learn_normal; /* output_normal_dim == 3 */
+    int32_t learn_albedo; /* output_albedo_dim == 3 */
+} nbvh_output_constants;
+
+/* NeuralBVHModuleConstants, include/cuda/neural/neural_bvh_module.h:79-131 (no direction input). */
+typedef struct nbvh_module_constants {
+    int32_t input_segment_points;
+    int32_t segment_distribution; /* nbvh_segment_distribution */
+} nbvh_module_constants;
+
+typedef struct nbvh_config {
+    uint32_t abi_version; /* NBVH_ABI_VERSION */
+    nbvh_hashgrid_options hashgrid;
+    nbvh_network_options network;
+    nbvh_optimizer_options optimizer;
+    nbvh_bvh_constants bvh;
+    nbvh_output_constants output;
+    nbvh_module_constants module;
+    uint32_t batch_size;           /* training rays per step, power of two (renderer.h:193) */
+    uint32_t neural_bvh_max_depth; /* fixed cut depth, m_neural_bvh_min_depth */
+    uint32_t max_traversal_steps;  /* neural_bvh_module.h:200 (1000) */
+    uint32_t seed;                 /* parameter initialisation and training-ray seed */
+    float fallback_margin;         /* |visibility - threshold| < margin -> classic answer; 0 = off */
+    uint32_t reserved[7];
+} nbvh_config;
+
+/* Fills the defaults of the reference (the tcnn_config.h / renderer-constant defaults) with the
+ * hot-path network shape: 4 stratified points, 16 levels x 2 features x 2^19 entries,
+ * resolution 16..2048, 64 x 4 ReLU MLP in FP16, batch 2^18, cut depth 10. */
+nbvh_status nbvh_config_default(nbvh_config *cfg);
+
+/* ---------------------------------------------------------------------------------------------
+ * Lifetime, scene and acceleration structures
+ * ------------------------------------------------------------------------------------------- */
+
+nbvh_status nbvh_create(const nbvh_config *cfg, int device, nbvh_handle **out);
+nbvh_status nbvh_destroy(nbvh_handle *h);
+const char *nbvh_last_error(const nbvh_handle *h);
+const char *nbvh_status_string(nbvh_status s);
+uint32_t nbvh_abi_version(void);
+
+/* Triangle mesh (host arrays; copied). albedo is per triangle (3 floats) or NULL for the
+ * reference's default base colour 0.9 (include/base/material.h:54). */
+nbvh_status nbvh_set_mesh(nbvh_handle *h, const float *h_vertices, uint32_t n_vertices,
+                          const uint32_t *h_indices, uint32_t n_triangles, const float *h_albedo);
+
+/* Builds the classic BVH2 on the host (binned SAH, leaves of 1-2 triangles, flat-axis boxes padded
+ * by 1e-4 as cuda_backend.cpp:212-223) and uploads nodes plus pre-gathered triangle records. */
+nbvh_status nbvh_build_classic(nbvh_handle *h);
+
+/* Copies the classic BVH out (host): nodes as 8 x 32-bit words per node in the reference layout
+ * {min.xyz, prim_count, max.xyz, left_or_prim_offset} (include/base/accel/bvh.h:66-72), and the
+ * primitive index list. Pass NULL buffers to query the counts. */
+nbvh_status nbvh_get_classic_bvh(const nbvh_handle *h, uint32_t *h_nodes, uint32_t *n_nodes,
+                                 uint32_t *h_prim_indices, uint32_t *n_prim_indices);
+
+/* Fixed tree cut of the classic BVH at max_depth (traverse_and_build_neural_bvh,
+ * neural_bvh_renderer_accel.cpp:25-88): nodes with prim_count 0 (interior),
+ * 1 (final leaf) or 8 (LoD-6 leaf). Also sets the neural scene box to the BVH root box. */
+nbvh_status nbvh_build_neural_cut(nbvh_handle *h, uint32_t max_depth);
+nbvh_status nbvh_get_neural_bvh(const nbvh_handle *h, uint32_t *h_nodes, uint32_t *n_nodes,
+                                float *h_scene_bbox /* 6 floats: min, max */);
+
+/* Marks neural leaves whose queries are answered by the classic BLAS (flag != 0). */
+nbvh_status nbvh_set_non_neural_leaves(nbvh_handle *h, const uint32_t *h_node_ids, uint32_t n,
+                                       int flag);
+nbvh_status nbvh_set_ignore_neural_blas(nbvh_handle *h, int ignore);
+
+/* ---------------------------------------------------------------------------------------------
+ * Queries (device buffers, asynchronous on stream)
+ * ------------------------------------------------------------------------------------------- */
+
+nbvh_status nbvh_query_closest_classic(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n,
+                                       nbvh_hit *d_hits, nbvh_stream stream);
+nbvh_status nbvh_query_any_classic(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n,
+                                   nbvh_hit *d_hits, nbvh_stream stream);
+
+/* Neural closest hit. Rays with tmin != 1e-4 are accepted; the neural traversal always restarts
+ * from -FLT_MAX as the reference does (neural_bvh2.cuh:185-189). depth: 1 = primary ray
+ * (primary_visibility_threshold), > 1 = secondary. When ignore_neural_blas is set the call
+ * answers from the classic BLAS and sets NBVH_HIT_CLASSIC_FALLBACK on every valid hit. */
+nbvh_status nbvh_query_closest_neural(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n,
+                                      uint32_t depth, nbvh_neural_hit *d_hits, nbvh_stream stream);
+nbvh_status nbvh_query_visibility_neural(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n,
+                                         uint32_t depth, nbvh_neural_hit *d_hits,
+                                         nbvh_stream stream);
+
+/* Same queries from host buffers: the library stages the rays through pinned memory in chunks on
+ * two internal streams so that copies overlap the kernels, and returns when h_hits is filled. */
+nbvh_status nbvh_query_closest_neural_host(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n,
+                                           uint32_t depth, nbvh_neural_hit *h_hits);
+nbvh_status nbvh_query_closest_classic_host(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n,
+                                            nbvh_hit *h_hits);
+
+/* Leaf segments each ray enters, in traversal order, with current_maxt = FLT_MAX (the N-BVH
+ * traversal alone, NeuralBVH2::intersect, neural_bvh2.cuh:170-292). Per ray up to max_segments
+ * records {mint, maxt, node}; d_counts receives the total number entered. */
+typedef struct nbvh_segment {
+    float mint;
+    float maxt;
+    uint32_t node;
+    uint32_t reserved;
+} nbvh_segment;
+nbvh_status nbvh_query_segments(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n,
+                                uint32_t max_segments, nbvh_segment *d_segments,
+                                uint32_t *d_counts, nbvh_stream stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Network: parameters, forward/backward kernels, optimisation
+ * ------------------------------------------------------------------------------------------- */
+
+/* Parameter layout (one flat FP32 vector, network first as tcnn orders it):
+ *   W_0   [n_neurons][n_inputs]     n_inputs = input_segment_points * n_levels * 2
+ *   W_1.. [n_neurons][n_neurons]    (n_hidden_layers - 1 matrices)
+ *   W_out [16][n_neurons]           rows 8..15 are padding and stay zero
+ *   grid  [n_grid_entries][2]       levels concatenated; level offsets from nbvh_grid_layout
+ */
+typedef struct nbvh_param_layout {
+    uint32_t n_inputs;
+    uint32_t n_network_params;
+    uint32_t n_grid_entries;
+    uint32_t n_params; /* n_network_params + 2 * n_grid_entries */
+    uint32_t n_levels;
+    uint32_t level_offset[32];     /* in entries */
+    uint32_t level_size[32];       /* entries in the level (hashed levels: 2^log2_hashmap_size) */
+    uint32_t level_resolution[32]; /* grid points per axis */
+    float level_scale[32];         /* position scale: pos = scale * x + 0.5 */
+} nbvh_param_layout;
+nbvh_status nbvh_get_param_layout(const nbvh_handle *h, nbvh_param_layout *out);
+
+/* FP32 master parameters; set also refreshes the FP16 (or BF16/FP8) copies and resets Adam. */
+nbvh_status nbvh_get_params(nbvh_handle *h, float *h_params);
+nbvh_status nbvh_set_params(nbvh_handle *h, const float *h_params);
+
+/* Network inference on explicit inputs: d_positions holds n x points x 3 encoded positions in
+ * [0,1]^3; d_outputs receives n x 8 sigmoid outputs. (Hash-grid encoding + fused MLP.) */
+nbvh_status nbvh_network_inference(nbvh_handle *h, const float *d_positions, uint32_t n,
+                                   float *d_outputs, nbvh_stream stream);
+
+/* Hash-grid encoding alone: n x points x 3 positions -> n x n_inputs features (FP32 values of the
+ * FP16 features fed to the MLP). */
+nbvh_status nbvh_encode(nbvh_handle *h, const float *d_positions, uint32_t n, float *d_features,
+                        nbvh_stream stream);
+
+/* One forward + loss + backward pass on an explicit batch without the optimiser: writes the FP32
+ * gradient of the mean loss w.r.t. every parameter (n_params floats, loss scale removed) and the
+ * mean loss. targets: n x 8. */
+nbvh_status nbvh_compute_gradients(nbvh_handle *h, const float *d_positions, const float *d_targets,
+                                   uint32_t n, float *d_gradients, float *h_loss,
+                                   nbvh_stream stream);
+
+/* One Adam + ExponentialDecay step from an explicit FP32 gradient (n_params floats). */
+nbvh_status nbvh_adam_step(nbvh_handle *h, const float *d_gradients, nbvh_stream stream);
+
+/* Training rays generated and labelled on the device for a training step
+ * (granular_sample_bvh_network_input_data, src/cuda/neural/neural_bvh_module_kernels.cu:119-264
+ * with n_sub_batch = 2^log2_bvh_max_traversals). d_positions: n x points x 3, d_targets: n x 8,
+ * d_nodes: sampled neural node per sample (may be NULL). */
+nbvh_status nbvh_generate_training_batch(nbvh_handle *h, uint32_t training_step, uint32_t n,
+                                         float *d_positions, float *d_targets, uint32_t *d_nodes,
+                                         nbvh_stream stream);
+
+typedef struct nbvh_train_stats {
+    uint32_t steps_done;
+    uint32_t training_step; /* total steps after the call */
+    float last_loss;        /* mean loss of the last step */
+    float mean_loss;        /* mean over the steps of this call */
+    float learning_rate;    /* effective rate of the last step */
+    float ms_per_step;      /* device time per step */
+} nbvh_train_stats;
+
+/* run-optimisation: `steps` training steps on device-generated, classic-labelled rays
+ * (sample generation -> fused forward/loss/backward -> Adam). Synchronous; stats may be NULL. */
+nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_stats *stats);
+uint32_t nbvh_training_step(const nbvh_handle *h);
+
+/* run-inference: renders one frame of primary rays from a pinhole camera (camera_raygen,
+ * include/cuda/neural/neural_bvh_renderer_kernels.cuh:74-79; CudaBackend::update_camera,
+ * src/cuda/cuda_backend.cpp:595-611) through the neural query, into a headless buffer. */
+typedef struct nbvh_render_request {
+    uint32_t width, height;
+    uint32_t sample_idx; /* get_lcg_rng(sample_idx, sample_offset, pixel) jitter */
+    uint32_t sample_offset;
+    float origin[3];
+    float target[3];
+    float up[3];
+    float yfov_degrees;
+} nbvh_render_request;
+/* d_image: width*height nbvh_neural_hit records (row-major, y down). */
+nbvh_status nbvh_run_inference(nbvh_handle *h, const nbvh_render_request *req,
+                               nbvh_neural_hit *d_image, nbvh_stream stream);
+/* The primary rays run_inference traces (for checking against a host restatement). */
+nbvh_status nbvh_camera_rays(nbvh_handle *h, const nbvh_render_request *req, nbvh_ray *d_rays,
+                             nbvh_stream stream);
+
+/* Checkpoint: config, mesh, both BVHs, FP32 parameters, Adam moments and step (own format). */
+nbvh_status nbvh_save(nbvh_handle *h, const char *path);
+nbvh_status nbvh_load(nbvh_handle *h, const char *path);
+
+/* Counters of the last query call (device-side step caps and stack overflows). */
+typedef struct nbvh_query_stats {
+    uint32_t rays;
+    uint32_t segments;       /* leaf segments inferred */
+    uint32_t step_capped;    /* rays stopped by max_traversal_steps */
+    uint32_t stack_overflow; /* rays whose traversal stack overflowed */
+    uint32_t fallback;       /* rays answered by the classic BLAS */
+} nbvh_query_stats;
+nbvh_status nbvh_last_query_stats(nbvh_handle *h, nbvh_query_stats *out);
+
+/* Device time (ms, CUDA events on the launching stream) of the dominant kernel of the last query
+ * or training call, and the number of kernels that call launched. */
+nbvh_status nbvh_last_kernel_time(nbvh_handle *h, float *ms, uint32_t *launches);
+
+/* ---------------------------------------------------------------------------------------------
+ * Host-only utilities (no CUDA device needed)
+ * ------------------------------------------------------------------------------------------- */
+
+/* The classic BVH builder of nbvh_build_classic, run on host arrays. h_nodes receives
+ * 8 words per node (capacity 2 * n_triangles nodes), h_prim_indices n_triangles entries. */
+nbvh_status nbvh_build_bvh2_host(const float *h_vertices, uint32_t n_vertices, const uint32_t *h_indices,
+                                 uint32_t n_triangles, uint32_t *h_nodes, uint32_t *n_nodes,
+                                 uint32_t *h_prim_indices);
+/* The fixed neural cut of nbvh_build_neural_cut; *n_neural_nodes is the capacity on input. */
+nbvh_status nbvh_build_neural_cut_host(const uint32_t *h_nodes, uint32_t n_nodes, uint32_t max_depth,
+                                       uint32_t *h_neural_nodes, uint32_t *n_neural_nodes);
+/* Parameter layout and seeded initial parameters (Xavier-uniform matrices, grid U(-1e-4, 1e-4))
+ * that nbvh_create would produce for cfg. */
+nbvh_status nbvh_param_layout_host(const nbvh_config *cfg, nbvh_param_layout *out);
+nbvh_status nbvh_init_params_host(const nbvh_config *cfg, float *h_params);
+
+/* Page-locked host memory for the *_host queries (cudaHostAlloc / cudaFreeHost). */
+nbvh_status nbvh_host_alloc(size_t bytes, void **out);
+nbvh_status nbvh_host_free(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBVH_H */

@@ -1,0 +1,437 @@
+"""nbvh_gb300 -- Python bindings of libnbvh, the GB300-native N-BVH ray-query library.
+
+The product is the C ABI in include/nbvh.h (host C++ over sm_103a CUDA kernels); this module is a
+thin ctypes layer over it for tests, benchmarks and Python callers. Device buffers are torch CUDA
+tensors (only their data pointers cross the boundary); host buffers are numpy arrays.
+
+There is no CPU fallback: without the compiled library importing works, but every call raises,
+and without a GPU the library answers NBVH_EDEVICE.
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import Config, ParamLayout, QueryStats, RenderRequest, TrainStats
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnbvh.so")
+
+RAY_DTYPE = np.dtype([("o", np.float32, 3), ("tmin", np.float32), ("d", np.float32, 3), ("tmax", np.float32)])
+HIT_DTYPE = np.dtype([("t", np.float32), ("u", np.float32), ("v", np.float32), ("prim", np.uint32)])
+NEURAL_HIT_DTYPE = np.dtype([("t", np.float32), ("normal", np.float32, 3), ("albedo", np.float32, 3),
+                             ("visibility", np.float32), ("flags", np.uint32), ("segments", np.uint32),
+                             ("prim", np.uint32), ("reserved", np.uint32)])
+SEGMENT_DTYPE = np.dtype([("mint", np.float32), ("maxt", np.float32), ("node", np.uint32), ("reserved", np.uint32)])
+FLT_MAX = np.float32(3.4028234663852886e38)
+
+_lib = None
+
+
+class NBVHError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (abi.STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+def load_library(path=None):
+    """Loads libnbvh.so (built in-tree by nbvh_gb300.build) and binds every prototype."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise NBVHError(abi.NBVH_EDEVICE, "libnbvh.so not built (run nbvh_gb300.build.build())")
+    lib = C.CDLL(p)
+    for name, (res, args) in abi.PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def default_config(**overrides):
+    """nbvh_config_default() with keyword overrides using dotted names, e.g.
+    default_config(**{"hashgrid.n_levels": 8, "batch_size": 1 << 16})."""
+    lib = load_library()
+    cfg = Config()
+    _check(lib.nbvh_config_default(C.byref(cfg)), None)
+    for key, val in overrides.items():
+        obj = cfg
+        parts = key.split(".")
+        for part in parts[:-1]:
+            obj = getattr(obj, part)
+        setattr(obj, parts[-1], val)
+    return cfg
+
+
+def config_from_reference_json(js, base=None):
+    """Builds a config from a reference-style JSON dict (neural_bvh_renderer section keys:
+    bvh_constants, neural_module.{pt_output_constants, bvh_module_constants, network, optimizer,
+    segment_encoding.hashgrid_options}, batch_size, neural_bvh_min_depth)."""
+    cfg = base if base is not None else default_config()
+    r = js.get("neural_bvh_renderer", js)
+    nm = r.get("neural_module", {})
+    bc = r.get("bvh_constants", {})
+    for k in ("inference_mint_epsilon", "inference_maxt_epsilon", "learning_mint_epsilon", "learning_maxt_epsilon",
+              "sampling_bbox_scaling", "fixed_node_dilation", "node_extent_dilation", "leaf_boundary_sampling_ratio"):
+        if k in bc:
+            setattr(cfg.bvh, k, float(bc[k]))
+    for k in ("ignore_neural_blas", "max_training_bounces", "sample_cosine_weighted", "backface_bounce_training",
+              "log2_bvh_max_traversals"):
+        if k in bc:
+            setattr(cfg.bvh, k, int(bc[k]))
+    pt = nm.get("pt_output_constants", {})
+    for k in ("visibility_loss", "depth_loss", "normal_loss", "albedo_loss"):
+        if k in pt:
+            setattr(cfg.output, k, abi.LOSS[pt[k]])
+    for k in ("visibility_loss_scale", "depth_loss_scale", "normal_loss_scale", "albedo_loss_scale",
+              "primary_visibility_threshold", "secondary_visibility_threshold", "depth_epsilon",
+              "fixed_depth_epsilon"):
+        if k in pt:
+            setattr(cfg.output, k, float(pt[k]))
+    for k in ("output_normal_linear_activation", "output_albedo_linear_activation", "visibility_masking_loss"):
+        if k in pt:
+            setattr(cfg.output, k, int(bool(pt[k])))
+    if "output_normal_dim" in pt:
+        cfg.output.learn_normal = int(pt["output_normal_dim"] == 3)
+    if "output_albedo_dim" in pt:
+        cfg.output.learn_albedo = int(pt["output_albedo_dim"] == 3)
+    mc = nm.get("bvh_module_constants", {})
+    if "input_segment_points" in mc:
+        cfg.module.input_segment_points = int(mc["input_segment_points"])
+    if "segment_distribution" in mc:
+        cfg.module.segment_distribution = abi.SEGMENT[mc["segment_distribution"]]
+    net = nm.get("network", {})
+    if "n_neurons" in net:
+        cfg.network.n_neurons = int(net["n_neurons"])
+    if "n_hidden_layers" in net:
+        cfg.network.n_hidden_layers = int(net["n_hidden_layers"])
+    opt = nm.get("optimizer", {})
+    for k in ("learning_rate", "beta1", "beta2", "epsilon", "l2_reg", "decay_base"):
+        if k in opt:
+            setattr(cfg.optimizer, k, float(opt[k]))
+    for k in ("decay_start", "decay_interval"):
+        if k in opt:
+            setattr(cfg.optimizer, k, int(opt[k]))
+    hg = nm.get("segment_encoding", {}).get("hashgrid_options", {})
+    for k in ("n_levels", "n_features_per_level", "log2_hashmap_size", "base_resolution"):
+        if k in hg:
+            setattr(cfg.hashgrid, k, int(hg[k]))
+    if "per_level_scale" in hg:
+        cfg.hashgrid.per_level_scale = float(hg["per_level_scale"])
+    if "batch_size" in r:
+        cfg.batch_size = int(r["batch_size"])
+    if "neural_bvh_min_depth" in r:
+        cfg.neural_bvh_max_depth = int(r["neural_bvh_min_depth"])
+    return cfg
+
+
+def _check(status, handle, lib=None):
+    if status != abi.NBVH_OK:
+        lib = lib or load_library()
+        msg = lib.nbvh_last_error(handle).decode() if handle else lib.nbvh_status_string(status).decode()
+        raise NBVHError(status, msg)
+
+
+def _ptr(x):
+    """Data pointer of a torch tensor (device or host) or a numpy array."""
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data_as(C.c_void_p)
+    return C.c_void_p(x.data_ptr())
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(stream.cuda_stream)
+
+
+def param_layout(cfg):
+    lib = load_library()
+    L = ParamLayout()
+    _check(lib.nbvh_param_layout_host(C.byref(cfg), C.byref(L)), None)
+    return L
+
+
+def init_params(cfg):
+    L = param_layout(cfg)
+    p = np.empty(L.n_params, np.float32)
+    _check(load_library().nbvh_init_params_host(C.byref(cfg), _ptr(p)), None)
+    return p
+
+
+def build_bvh2_host(vertices, indices):
+    """Host BVH2 build (no device needed): returns (nodes uint32 [n, 8], prim_indices uint32)."""
+    lib = load_library()
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+    nodes = np.empty((2 * len(t), 8), np.uint32)
+    n = C.c_uint32(0)
+    prims = np.empty(len(t), np.uint32)
+    _check(lib.nbvh_build_bvh2_host(_ptr(v), len(v), _ptr(t), len(t), _ptr(nodes), C.byref(n), _ptr(prims)), None)
+    return nodes[: n.value].copy(), prims
+
+
+def build_neural_cut_host(nodes, max_depth):
+    lib = load_library()
+    nodes = np.ascontiguousarray(nodes, np.uint32)
+    out = np.empty((max(1, 2 * len(nodes)), 8), np.uint32)
+    n = C.c_uint32(len(out))
+    _check(lib.nbvh_build_neural_cut_host(_ptr(nodes), len(nodes), max_depth, _ptr(out), C.byref(n)), None)
+    return out[: n.value].copy()
+
+
+def nodes_to_float(nodes):
+    """Bounding boxes of uint32 [n, 8] node records: (min [n,3], max [n,3]) float32."""
+    f = nodes.view(np.float32)
+    return f[:, 0:3].copy(), f[:, 4:7].copy()
+
+
+class NBVH:
+    """One library handle: scene, classic BVH, neural cut, network parameters and workspaces."""
+
+    def __init__(self, config=None, device=0):
+        self.lib = load_library()
+        self.cfg = config if config is not None else default_config()
+        h = C.c_void_p()
+        _check(self.lib.nbvh_create(C.byref(self.cfg), device, C.byref(h)), None, self.lib)
+        self.h = h
+        self.device = device
+        L = ParamLayout()
+        self._check(self.lib.nbvh_get_param_layout(self.h, C.byref(L)))
+        self.layout = L
+
+    def _check(self, st):
+        _check(st, self.h, self.lib)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nbvh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- scene ----
+    def set_mesh(self, vertices, indices, albedo=None):
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+        a = None if albedo is None else np.ascontiguousarray(albedo, np.float32).reshape(-1, 3)
+        self._keep = (v, t, a)
+        self._check(self.lib.nbvh_set_mesh(self.h, _ptr(v), len(v), _ptr(t), len(t), _ptr(a)))
+
+    def build_classic(self):
+        self._check(self.lib.nbvh_build_classic(self.h))
+
+    def classic_bvh(self):
+        nn, np_ = C.c_uint32(0), C.c_uint32(0)
+        self._check(self.lib.nbvh_get_classic_bvh(self.h, None, C.byref(nn), None, C.byref(np_)))
+        nodes = np.empty((nn.value, 8), np.uint32)
+        prims = np.empty(np_.value, np.uint32)
+        self._check(self.lib.nbvh_get_classic_bvh(self.h, _ptr(nodes), C.byref(nn), _ptr(prims), C.byref(np_)))
+        return nodes, prims
+
+    def build_neural_cut(self, max_depth=None):
+        self._check(self.lib.nbvh_build_neural_cut(self.h, self.cfg.neural_bvh_max_depth if max_depth is None else max_depth))
+
+    def neural_bvh(self):
+        nn = C.c_uint32(0)
+        self._check(self.lib.nbvh_get_neural_bvh(self.h, None, C.byref(nn), None))
+        nodes = np.empty((nn.value, 8), np.uint32)
+        bbox = np.empty(6, np.float32)
+        self._check(self.lib.nbvh_get_neural_bvh(self.h, _ptr(nodes), C.byref(nn), _ptr(bbox)))
+        return nodes, bbox
+
+    def set_non_neural_leaves(self, node_ids, flag=True):
+        ids = np.ascontiguousarray(node_ids, np.uint32)
+        self._check(self.lib.nbvh_set_non_neural_leaves(self.h, _ptr(ids), len(ids), int(bool(flag))))
+
+    def set_ignore_neural_blas(self, ignore):
+        self._check(self.lib.nbvh_set_ignore_neural_blas(self.h, int(bool(ignore))))
+
+    # ---- queries on device tensors ----
+    def _out(self, like, n, words):
+        import torch
+        return torch.empty((n, words), dtype=torch.int32, device=like.device)
+
+    def query_closest_classic(self, rays, out=None, stream=None):
+        n = rays.shape[0]
+        out = self._out(rays, n, 4) if out is None else out
+        self._check(self.lib.nbvh_query_closest_classic(self.h, _ptr(rays), n, _ptr(out), _stream(stream)))
+        return out
+
+    def query_any_classic(self, rays, out=None, stream=None):
+        n = rays.shape[0]
+        out = self._out(rays, n, 4) if out is None else out
+        self._check(self.lib.nbvh_query_any_classic(self.h, _ptr(rays), n, _ptr(out), _stream(stream)))
+        return out
+
+    def query_closest_neural(self, rays, depth=1, out=None, stream=None):
+        n = rays.shape[0]
+        out = self._out(rays, n, 12) if out is None else out
+        self._check(self.lib.nbvh_query_closest_neural(self.h, _ptr(rays), n, depth, _ptr(out), _stream(stream)))
+        return out
+
+    def query_visibility_neural(self, rays, depth=1, out=None, stream=None):
+        n = rays.shape[0]
+        out = self._out(rays, n, 12) if out is None else out
+        self._check(self.lib.nbvh_query_visibility_neural(self.h, _ptr(rays), n, depth, _ptr(out), _stream(stream)))
+        return out
+
+    def query_segments(self, rays, max_segments, stream=None):
+        import torch
+        n = rays.shape[0]
+        segs = torch.empty((n, max_segments, 4), dtype=torch.int32, device=rays.device)
+        counts = torch.empty(n, dtype=torch.int32, device=rays.device)
+        self._check(self.lib.nbvh_query_segments(self.h, _ptr(rays), n, max_segments, _ptr(segs), _ptr(counts),
+                                                 _stream(stream)))
+        return segs, counts
+
+    # ---- queries on host arrays (pinned or pageable) ----
+    @staticmethod
+    def _host_rays(rays_np):
+        rays_np = np.ascontiguousarray(rays_np)
+        return rays_np, rays_np.nbytes // 32
+
+    def query_closest_neural_host(self, rays_np, depth=1, out=None):
+        rays_np, n = self._host_rays(rays_np)
+        out = np.empty(n, NEURAL_HIT_DTYPE) if out is None else out
+        self._check(self.lib.nbvh_query_closest_neural_host(self.h, _ptr(rays_np), n, depth, _ptr(out)))
+        return out
+
+    def query_closest_classic_host(self, rays_np, out=None):
+        rays_np, n = self._host_rays(rays_np)
+        out = np.empty(n, HIT_DTYPE) if out is None else out
+        self._check(self.lib.nbvh_query_closest_classic_host(self.h, _ptr(rays_np), n, _ptr(out)))
+        return out
+
+    # ---- network ----
+    def params(self):
+        p = np.empty(self.layout.n_params, np.float32)
+        self._check(self.lib.nbvh_get_params(self.h, _ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.layout.n_params
+        self._check(self.lib.nbvh_set_params(self.h, _ptr(p)))
+
+    def network_inference(self, positions, stream=None):
+        import torch
+        n = positions.shape[0]
+        out = torch.empty((n, 8), dtype=torch.float32, device=positions.device)
+        self._check(self.lib.nbvh_network_inference(self.h, _ptr(positions), n, _ptr(out), _stream(stream)))
+        return out
+
+    def encode(self, positions, stream=None):
+        import torch
+        n = positions.shape[0]
+        out = torch.empty((n, self.layout.n_inputs), dtype=torch.float32, device=positions.device)
+        self._check(self.lib.nbvh_encode(self.h, _ptr(positions), n, _ptr(out), _stream(stream)))
+        return out
+
+    def compute_gradients(self, positions, targets, stream=None):
+        import torch
+        n = positions.shape[0]
+        g = torch.empty(self.layout.n_params, dtype=torch.float32, device=positions.device)
+        loss = C.c_float(0)
+        self._check(self.lib.nbvh_compute_gradients(self.h, _ptr(positions), _ptr(targets), n, _ptr(g),
+                                                    C.byref(loss), _stream(stream)))
+        return g, loss.value
+
+    def adam_step(self, gradients, stream=None):
+        self._check(self.lib.nbvh_adam_step(self.h, _ptr(gradients), _stream(stream)))
+
+    def generate_training_batch(self, training_step, n, stream=None):
+        import torch
+        P = self.cfg.module.input_segment_points
+        dev = torch.device("cuda", self.device)
+        pos = torch.empty((n, P, 3), dtype=torch.float32, device=dev)
+        tgt = torch.empty((n, 8), dtype=torch.float32, device=dev)
+        nodes = torch.empty(n, dtype=torch.int32, device=dev)
+        self._check(self.lib.nbvh_generate_training_batch(self.h, training_step, n, _ptr(pos), _ptr(tgt),
+                                                          _ptr(nodes), _stream(stream)))
+        return pos, tgt, nodes
+
+    def run_optimisation(self, steps):
+        st = TrainStats()
+        self._check(self.lib.nbvh_run_optimisation(self.h, steps, C.byref(st)))
+        return st
+
+    @property
+    def training_step(self):
+        return self.lib.nbvh_training_step(self.h)
+
+    # ---- run-inference ----
+    def camera_rays(self, req, stream=None):
+        import torch
+        rays = torch.empty((req.width * req.height, 8), dtype=torch.float32, device=torch.device("cuda", self.device))
+        self._check(self.lib.nbvh_camera_rays(self.h, C.byref(req), _ptr(rays), _stream(stream)))
+        return rays
+
+    def run_inference(self, req, stream=None):
+        import torch
+        img = torch.empty((req.width * req.height, 12), dtype=torch.int32, device=torch.device("cuda", self.device))
+        self._check(self.lib.nbvh_run_inference(self.h, C.byref(req), _ptr(img), _stream(stream)))
+        return img
+
+    # ---- checkpoints, stats ----
+    def save(self, path):
+        self._check(self.lib.nbvh_save(self.h, path.encode()))
+
+    def load(self, path):
+        self._check(self.lib.nbvh_load(self.h, path.encode()))
+        L = ParamLayout()
+        self._check(self.lib.nbvh_get_param_layout(self.h, C.byref(L)))
+        self.layout = L
+
+    def query_stats(self):
+        s = QueryStats()
+        self._check(self.lib.nbvh_last_query_stats(self.h, C.byref(s)))
+        return s
+
+    def last_kernel_time(self):
+        ms = C.c_float(0)
+        launches = C.c_uint32(0)
+        self._check(self.lib.nbvh_last_kernel_time(self.h, C.byref(ms), C.byref(launches)))
+        return ms.value, launches.value
+
+
+def render_request(width, height, origin, target, up=(0.0, 1.0, 0.0), yfov_degrees=45.0, sample_idx=0,
+                   sample_offset=0):
+    r = RenderRequest()
+    r.width, r.height = width, height
+    r.sample_idx, r.sample_offset = sample_idx, sample_offset
+    for k in range(3):
+        r.origin[k] = float(origin[k])
+        r.target[k] = float(target[k])
+        r.up[k] = float(up[k])
+    r.yfov_degrees = float(yfov_degrees)
+    return r
+
+
+__all__ = [
+    "NBVH", "NBVHError", "Config", "ParamLayout", "RenderRequest", "TrainStats", "QueryStats", "abi",
+    "load_library", "default_config", "config_from_reference_json", "param_layout", "init_params",
+    "build_bvh2_host", "build_neural_cut_host", "nodes_to_float", "render_request", "RAY_DTYPE", "HIT_DTYPE",
+    "NEURAL_HIT_DTYPE", "SEGMENT_DTYPE", "FLT_MAX",
+]

@@ -1,0 +1,270 @@
+// bvh_builder.cpp -- host construction of the classic BVH2 and of the fixed neural tree cut.
+//
+// The reference builds its BLAS with madmann91/bvh v2 DefaultBuilder (Quality::High, leaves of
+// 1..2 primitives; src/cuda/cuda_backend.cpp:270-310), converts it to 32-byte BVH2Node records
+// whose two children are adjacent (include/base/accel/bvh.h:66-72, src/base/accel/bvh.cpp:133-151)
+// and pads flat boxes by 1e-4 (src/cuda/cuda_backend.cpp:212-223). That library is not part of the
+// reference tree, so this file is an own binned-SAH builder producing the same node format and
+// leaf size. Closest-hit results depend on the topology only through exact distance ties.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "nbvh_internal.h"
+
+namespace nbvh {
+
+namespace {
+
+constexpr int kBins = 32;
+constexpr int kMaxDepth = 31; // the traversal stack has 32 entries
+constexpr float kBoxRegularisation = 1e-4f; // BBOX_REGULARISATION, include/cuda/cuda_backend.h:14
+
+struct Box {
+    float mn[3], mx[3];
+    void reset()
+    {
+        for (int k = 0; k < 3; k++) {
+            mn[k] = INFINITY;
+            mx[k] = -INFINITY;
+        }
+    }
+    void grow(const Box &b)
+    {
+        for (int k = 0; k < 3; k++) {
+            mn[k] = std::min(mn[k], b.mn[k]);
+            mx[k] = std::max(mx[k], b.mx[k]);
+        }
+    }
+    void grow(const float *p)
+    {
+        for (int k = 0; k < 3; k++) {
+            mn[k] = std::min(mn[k], p[k]);
+            mx[k] = std::max(mx[k], p[k]);
+        }
+    }
+    double half_area() const
+    {
+        double dx = std::max(0.0, (double)mx[0] - mn[0]), dy = std::max(0.0, (double)mx[1] - mn[1]),
+               dz = std::max(0.0, (double)mx[2] - mn[2]);
+        return dx * dy + dy * dz + dz * dx;
+    }
+};
+
+struct Builder {
+    const std::vector<Box> &boxes;
+    const std::vector<float> &centroids; // 3 per primitive
+    std::vector<uint32_t> &prims;
+    std::vector<BVHNode> &nodes;
+    int max_depth_seen = 0;
+
+    void set_box(uint32_t ni, const Box &b)
+    {
+        for (int k = 0; k < 3; k++) {
+            nodes[ni].min[k] = b.mn[k];
+            nodes[ni].max[k] = b.mx[k];
+        }
+    }
+
+    // Builds node `ni` over prims[begin, end). Iterative over an explicit stack.
+    void build(uint32_t root_begin, uint32_t root_end)
+    {
+        struct Task {
+            uint32_t ni, begin, end;
+            int depth;
+        };
+        std::vector<Task> stack;
+        stack.push_back({0u, root_begin, root_end, 0});
+        while (!stack.empty()) {
+            Task t = stack.back();
+            stack.pop_back();
+            max_depth_seen = std::max(max_depth_seen, t.depth);
+            Box nb, cb;
+            nb.reset();
+            cb.reset();
+            for (uint32_t i = t.begin; i < t.end; i++) {
+                nb.grow(boxes[prims[i]]);
+                cb.grow(&centroids[3u * prims[i]]);
+            }
+            set_box(t.ni, nb);
+            const uint32_t count = t.end - t.begin;
+            if (count <= 2u) {
+                nodes[t.ni].prim_count = count;
+                nodes[t.ni].left_or_prim_offset = t.begin;
+                continue;
+            }
+            uint32_t mid = t.begin + count / 2u;
+            // With the remaining depth budget a balanced split must still fit: beyond half of the
+            // budget's capacity fall back to an object-median split.
+            const int levels_left = kMaxDepth - t.depth;
+            const bool force_median = levels_left < 31 && (double)count > std::ldexp(1.0, levels_left);
+            bool split_found = false;
+            if (!force_median) {
+                double best_cost = INFINITY;
+                int best_axis = -1, best_bin = -1;
+                for (int axis = 0; axis < 3; axis++) {
+                    const float lo = cb.mn[axis], hi = cb.mx[axis];
+                    if (!(hi > lo))
+                        continue;
+                    const float scale = (float)kBins / (hi - lo);
+                    Box bb[kBins];
+                    uint32_t bc[kBins];
+                    for (int b = 0; b < kBins; b++) {
+                        bb[b].reset();
+                        bc[b] = 0;
+                    }
+                    for (uint32_t i = t.begin; i < t.end; i++) {
+                        int b = (int)((centroids[3u * prims[i] + axis] - lo) * scale);
+                        b = std::min(std::max(b, 0), kBins - 1);
+                        bb[b].grow(boxes[prims[i]]);
+                        bc[b]++;
+                    }
+                    double right_area[kBins];
+                    uint32_t right_count[kBins];
+                    Box acc;
+                    acc.reset();
+                    uint32_t cnt = 0;
+                    for (int b = kBins - 1; b > 0; b--) {
+                        acc.grow(bb[b]);
+                        cnt += bc[b];
+                        right_area[b] = acc.half_area();
+                        right_count[b] = cnt;
+                    }
+                    acc.reset();
+                    cnt = 0;
+                    for (int b = 0; b < kBins - 1; b++) {
+                        acc.grow(bb[b]);
+                        cnt += bc[b];
+                        if (cnt == 0 || right_count[b + 1] == 0)
+                            continue;
+                        double cost = acc.half_area() * cnt + right_area[b + 1] * right_count[b + 1];
+                        if (cost < best_cost) {
+                            best_cost = cost;
+                            best_axis = axis;
+                            best_bin = b;
+                        }
+                    }
+                }
+                if (best_axis >= 0) {
+                    const float lo = cb.mn[best_axis], hi = cb.mx[best_axis];
+                    const float scale = (float)kBins / (hi - lo);
+                    auto it = std::partition(prims.begin() + t.begin, prims.begin() + t.end, [&](uint32_t p) {
+                        int b = (int)((centroids[3u * p + best_axis] - lo) * scale);
+                        b = std::min(std::max(b, 0), kBins - 1);
+                        return b <= best_bin;
+                    });
+                    mid = (uint32_t)(it - prims.begin());
+                    split_found = mid > t.begin && mid < t.end;
+                }
+            }
+            if (!split_found) {
+                // object median along the largest centroid extent
+                int axis = 0;
+                float ext = cb.mx[0] - cb.mn[0];
+                for (int k = 1; k < 3; k++)
+                    if (cb.mx[k] - cb.mn[k] > ext) {
+                        ext = cb.mx[k] - cb.mn[k];
+                        axis = k;
+                    }
+                mid = t.begin + count / 2u;
+                std::nth_element(prims.begin() + t.begin, prims.begin() + mid, prims.begin() + t.end,
+                                 [&](uint32_t a, uint32_t b) {
+                                     float ca = centroids[3u * a + axis], cb2 = centroids[3u * b + axis];
+                                     return ca < cb2 || (ca == cb2 && a < b);
+                                 });
+            }
+            const uint32_t left = (uint32_t)nodes.size();
+            nodes.push_back(BVHNode{});
+            nodes.push_back(BVHNode{});
+            nodes[t.ni].prim_count = 0;
+            nodes[t.ni].left_or_prim_offset = left;
+            // right first on the stack so that the left subtree is finished first
+            stack.push_back({left + 1u, mid, t.end, t.depth + 1});
+            stack.push_back({left, t.begin, mid, t.depth + 1});
+        }
+    }
+};
+
+} // namespace
+
+bool build_bvh2(const std::vector<float> &vertices, const std::vector<uint32_t> &indices, std::vector<BVHNode> &nodes,
+                std::vector<uint32_t> &prim_indices, std::string &err)
+{
+    const uint32_t nt = (uint32_t)(indices.size() / 3u);
+    if (nt == 0) {
+        err = "mesh has no triangles";
+        return false;
+    }
+    std::vector<Box> boxes(nt);
+    std::vector<float> centroids(3u * (size_t)nt);
+    for (uint32_t p = 0; p < nt; p++) {
+        Box b;
+        b.reset();
+        for (int k = 0; k < 3; k++)
+            b.grow(&vertices[3u * (size_t)indices[3u * (size_t)p + k]]);
+        boxes[p] = b;
+        for (int k = 0; k < 3; k++)
+            centroids[3u * (size_t)p + k] = 0.5f * (b.mn[k] + b.mx[k]);
+    }
+    prim_indices.resize(nt);
+    for (uint32_t p = 0; p < nt; p++)
+        prim_indices[p] = p;
+    nodes.clear();
+    nodes.reserve(2u * (size_t)nt);
+    nodes.push_back(BVHNode{});
+    Builder b{boxes, centroids, prim_indices, nodes};
+    b.build(0u, nt);
+    if (b.max_depth_seen > kMaxDepth) {
+        err = "BVH deeper than the 32-entry traversal stack";
+        return false;
+    }
+    // flat-box regularisation, src/cuda/cuda_backend.cpp:212-223
+    for (auto &n : nodes)
+        for (int k = 0; k < 3; k++)
+            if (n.max[k] - n.min[k] <= kBoxRegularisation) {
+                n.min[k] -= kBoxRegularisation * 0.5f;
+                n.max[k] += kBoxRegularisation * 0.5f;
+            }
+    return true;
+}
+
+// traverse_and_build_neural_bvh, src/cuda/neural/neural_bvh_renderer_accel.cpp:25-88: copy the
+// classic BVH down to max_depth; leaves become LEAF_FINAL (1) when they are classic leaves and
+// LEAF_LOD(6) (= 8, the coarsest LoD, assigned first when building the cut) otherwise.
+void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std::vector<BVHNode> &neural)
+{
+    constexpr uint32_t kLeafFinal = 1u, kLeafLod6 = 8u;
+    neural.assign(1, BVHNode{});
+    struct Task {
+        uint32_t bvh_idx, neural_idx, depth;
+    };
+    // recursion order of the reference: a node's two children are allocated, then the left
+    // subtree is built completely before the right one
+    std::vector<Task> stack;
+    stack.push_back({0u, 0u, 0u});
+    while (!stack.empty()) {
+        Task t = stack.back();
+        stack.pop_back();
+        const BVHNode &src = nodes[t.bvh_idx];
+        BVHNode &dst = neural[t.neural_idx];
+        std::memcpy(dst.min, src.min, sizeof(dst.min));
+        std::memcpy(dst.max, src.max, sizeof(dst.max));
+        if (src.prim_count > 0u || t.depth == max_depth) {
+            dst.prim_count = src.prim_count > 0u ? kLeafFinal : kLeafLod6;
+            dst.left_or_prim_offset = kNoNeuralChild;
+            continue;
+        }
+        const uint32_t left = (uint32_t)neural.size();
+        neural.push_back(BVHNode{});
+        neural.push_back(BVHNode{});
+        BVHNode &d2 = neural[t.neural_idx];
+        d2.prim_count = 0u;
+        d2.left_or_prim_offset = left;
+        stack.push_back({src.left_or_prim_offset + 1u, left + 1u, t.depth + 1u});
+        stack.push_back({src.left_or_prim_offset, left, t.depth + 1u});
+    }
+}
+
+} // namespace nbvh

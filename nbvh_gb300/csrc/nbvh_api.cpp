@@ -1,0 +1,1294 @@
+// nbvh_api.cpp -- the C ABI of libnbvh (include/nbvh.h): handle lifetime, scene and BVH upload,
+// parameter management, query dispatch, run-optimisation / run-inference loops and checkpoints.
+//
+// Host-side counterpart of the reference's NeuralBVHModule / NeuralPathModule / NeuralBVHRenderer
+// surface (include/cuda/neural/neural_bvh_module.h:144-241, src/cuda/neural/path/path_module.cu,
+// src/cuda/neural/neural_bvh_renderer.cu). State is per handle instead of __constant__ globals;
+// errors are status codes instead of exceptions or exit().
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <fstream>
+#include <new>
+
+#include "nbvh_internal.h"
+
+using namespace nbvh;
+
+namespace {
+
+struct Fail {
+    nbvh_status status;
+    std::string msg;
+};
+
+[[noreturn]] void fail(nbvh_status s, const std::string &m) { throw Fail{s, m}; }
+
+void cuda_check(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) {
+        if (e == cudaErrorMemoryAllocation)
+            fail(NBVH_ENOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+        fail(NBVH_EDEVICE, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+template <typename F>
+nbvh_status guarded(nbvh_handle *h, F &&f)
+{
+    if (!h)
+        return NBVH_EINVAL;
+    std::lock_guard<std::mutex> lock(h->mu);
+    try {
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        f();
+        h->last_error.clear();
+        return NBVH_OK;
+    } catch (const Fail &e) {
+        h->last_error = e.msg;
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        h->last_error = "host allocation failed";
+        return NBVH_ENOMEM;
+    } catch (const std::exception &e) {
+        h->last_error = e.what();
+        return NBVH_EINVAL;
+    }
+}
+
+template <typename F>
+nbvh_status guarded_free(F &&f)
+{
+    try {
+        f();
+        return NBVH_OK;
+    } catch (const Fail &e) {
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        return NBVH_ENOMEM;
+    } catch (...) {
+        return NBVH_EINVAL;
+    }
+}
+
+// -------- configuration --------
+
+uint32_t n_inputs_of(const nbvh_config &c)
+{
+    return (uint32_t)c.module.input_segment_points * (uint32_t)c.hashgrid.n_levels * 2u;
+}
+
+void validate_config(const nbvh_config &c)
+{
+    if (c.abi_version != NBVH_ABI_VERSION)
+        fail(NBVH_EINVAL, "config abi_version mismatch");
+    if (c.hashgrid.n_features_per_level != 2)
+        fail(NBVH_EINVAL, "n_features_per_level must be 2");
+    if (c.hashgrid.n_levels < 1 || c.hashgrid.n_levels > (int)kMaxLevels)
+        fail(NBVH_EINVAL, "n_levels must be in [1, 32]");
+    if (c.hashgrid.log2_hashmap_size < 4 || c.hashgrid.log2_hashmap_size > 24)
+        fail(NBVH_EINVAL, "log2_hashmap_size must be in [4, 24]");
+    if (c.hashgrid.base_resolution < 2 || !(c.hashgrid.per_level_scale >= 1.0f))
+        fail(NBVH_EINVAL, "bad grid resolution options");
+    if (c.module.input_segment_points < 1 || c.module.input_segment_points > (int)kMaxPoints)
+        fail(NBVH_EINVAL, "input_segment_points must be in [1, 16]");
+    if (c.module.segment_distribution < 0 || c.module.segment_distribution > 2)
+        fail(NBVH_EINVAL, "bad segment_distribution");
+    const uint32_t ni = n_inputs_of(c);
+    if (ni % 16u != 0u || ni > kMaxInputs)
+        fail(NBVH_EINVAL, "points * levels * 2 must be a multiple of 16 and at most 128");
+    if (c.network.n_neurons != (int)kNeurons)
+        fail(NBVH_EINVAL, "n_neurons must be 64");
+    if (c.network.n_hidden_layers < 1 || c.network.n_hidden_layers > (int)kMaxHiddenLayers)
+        fail(NBVH_EINVAL, "n_hidden_layers must be in [1, 8]");
+    if (c.network.precision != NBVH_PRECISION_FP16)
+        fail(NBVH_EINVAL, "only the FP16 network precision is implemented");
+    if (c.batch_size == 0 || (c.batch_size & (c.batch_size - 1u)) != 0)
+        fail(NBVH_EINVAL, "batch_size must be a power of two");
+    if (c.bvh.log2_bvh_max_traversals != 0)
+        fail(NBVH_EINVAL, "log2_bvh_max_traversals must be 0");
+    if (c.optimizer.loss_scale <= 0.f)
+        fail(NBVH_EINVAL, "loss_scale must be positive");
+}
+
+// Grid geometry: scale_l = base * per_level_scale^l - 1 (power by repeated double
+// multiplication), res = ceil(scale) + 1, entries = min(roundup8(res^3), 2^log2T).
+void compute_layout(const nbvh_config &c, nbvh_param_layout &L, GridParams &g)
+{
+    std::memset(&L, 0, sizeof(L));
+    std::memset(&g, 0, sizeof(g));
+    const uint32_t nl = (uint32_t)c.hashgrid.n_levels;
+    const uint64_t hashmap = 1ull << c.hashgrid.log2_hashmap_size;
+    uint64_t off = 0;
+    double p = 1.0;
+    for (uint32_t l = 0; l < nl; l++) {
+        float s = (float)((double)c.hashgrid.base_resolution * p - 1.0);
+        uint32_t res = (uint32_t)std::ceil(s) + 1u;
+        uint64_t dense = (uint64_t)res * res * res;
+        uint64_t dense8 = (dense + 7u) & ~7ull;
+        uint64_t sz = dense8 < hashmap ? dense8 : hashmap;
+        L.level_offset[l] = (uint32_t)off;
+        L.level_size[l] = (uint32_t)sz;
+        L.level_resolution[l] = res;
+        L.level_scale[l] = s;
+        g.offset[l] = (uint32_t)off;
+        g.size[l] = (uint32_t)sz;
+        g.res[l] = res;
+        g.scale[l] = s;
+        g.hashed[l] = dense > sz ? 1u : 0u;
+        off += sz;
+        p *= (double)c.hashgrid.per_level_scale;
+    }
+    L.n_levels = nl;
+    L.n_inputs = n_inputs_of(c);
+    const uint32_t H = (uint32_t)c.network.n_hidden_layers;
+    L.n_network_params = kNeurons * L.n_inputs + (H - 1u) * kNeurons * kNeurons + kOutputsPadded * kNeurons;
+    L.n_grid_entries = (uint32_t)off;
+    L.n_params = L.n_network_params + 2u * L.n_grid_entries;
+    g.n_levels = nl;
+    g.n_points = (uint32_t)c.module.input_segment_points;
+    g.n_inputs = L.n_inputs;
+    g.segment_distribution = (uint32_t)c.module.segment_distribution;
+}
+
+// seeded initial parameters: Xavier-uniform matrices (rows 8..15 of the output matrix zero),
+// hash-grid entries uniform in [-1e-4, 1e-4]
+void init_params(const nbvh_config &c, const nbvh_param_layout &L, float *out)
+{
+    uint64_t state = 0x9E3779B97F4A7C15ull ^ ((uint64_t)c.seed * 0xD1B54A32D192ED03ull);
+    auto next = [&]() -> double { // splitmix64 -> [0, 1)
+        state += 0x9E3779B97F4A7C15ull;
+        uint64_t z = state;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * 0x1p-53;
+    };
+    const uint32_t H = (uint32_t)c.network.n_hidden_layers;
+    uint32_t o = 0;
+    for (uint32_t m = 0; m <= H; m++) {
+        const uint32_t rows = (m == H) ? kOutputsPadded : kNeurons;
+        const uint32_t cols = (m == 0) ? L.n_inputs : kNeurons;
+        const uint32_t fan_out = (m == H) ? kOutputs : kNeurons;
+        const double s = std::sqrt(6.0 / (double)(cols + fan_out));
+        for (uint32_t r = 0; r < rows; r++)
+            for (uint32_t k = 0; k < cols; k++)
+                out[o + r * cols + k] = (m == H && r >= kOutputs) ? 0.0f : (float)((2.0 * next() - 1.0) * s);
+        o += rows * cols;
+    }
+    for (uint32_t i = 0; i < 2u * L.n_grid_entries; i++)
+        out[L.n_network_params + i] = (float)((2.0 * next() - 1.0) * 1e-4);
+}
+
+NeuralConsts make_neural_consts(const nbvh_handle *h, uint32_t depth, bool visibility_only)
+{
+    const nbvh_config &c = h->cfg;
+    NeuralConsts nc;
+    std::memset(&nc, 0, sizeof(nc));
+    nc.inference_mint_epsilon = c.bvh.inference_mint_epsilon;
+    nc.inference_maxt_epsilon = c.bvh.inference_maxt_epsilon;
+    nc.learning_mint_epsilon = c.bvh.learning_mint_epsilon;
+    nc.learning_maxt_epsilon = c.bvh.learning_maxt_epsilon;
+    nc.sampling_bbox_scaling = c.bvh.sampling_bbox_scaling;
+    nc.fixed_node_dilation = c.bvh.fixed_node_dilation;
+    nc.node_extent_dilation = c.bvh.node_extent_dilation;
+    nc.leaf_boundary_sampling_ratio = c.bvh.leaf_boundary_sampling_ratio;
+    nc.visibility_threshold =
+        depth == 1u ? c.output.primary_visibility_threshold : c.output.secondary_visibility_threshold;
+    nc.depth_epsilon = c.output.depth_epsilon;
+    nc.fixed_depth_epsilon = c.output.fixed_depth_epsilon;
+    nc.fallback_margin = c.fallback_margin;
+    for (int k = 0; k < 3; k++) {
+        nc.scene_min[k] = h->scene_min[k];
+        nc.scene_max[k] = h->scene_max[k];
+    }
+    nc.bvh_lod = 0u; // rendered_lod
+    nc.max_traversal_steps = c.max_traversal_steps;
+    nc.visibility_only = visibility_only ? 1u : 0u;
+    return nc;
+}
+
+LossConsts make_loss_consts(const nbvh_config &c, uint32_t n)
+{
+    LossConsts lc;
+    lc.visibility_loss = c.output.visibility_loss;
+    lc.depth_loss = c.output.depth_loss;
+    lc.normal_loss = c.output.normal_loss;
+    lc.albedo_loss = c.output.albedo_loss;
+    lc.visibility_loss_scale = c.output.visibility_loss_scale;
+    lc.depth_loss_scale = c.output.depth_loss_scale;
+    lc.normal_loss_scale = c.output.normal_loss_scale;
+    lc.albedo_loss_scale = c.output.albedo_loss_scale;
+    lc.normal_linear = c.output.output_normal_linear_activation;
+    lc.albedo_linear = c.output.output_albedo_linear_activation;
+    lc.masking = c.output.visibility_masking_loss;
+    lc.learn_normal = c.output.learn_normal;
+    lc.learn_albedo = c.output.learn_albedo;
+    lc.loss_scale = c.optimizer.loss_scale;
+    const uint32_t dims = 2u + (c.output.learn_normal ? 3u : 0u) + (c.output.learn_albedo ? 3u : 0u);
+    lc.inv_n_total = 1.0f / (float)((double)n * dims);
+    return lc;
+}
+
+// Adam step size of step `step` (0-based): ExponentialDecay then the bias corrections.
+float adam_step_size(const nbvh_config &c, uint32_t step)
+{
+    double lr = c.optimizer.learning_rate;
+    if ((int64_t)step >= (int64_t)c.optimizer.decay_start && c.optimizer.decay_interval > 0)
+        lr *= std::pow((double)c.optimizer.decay_base,
+                       (double)(((int64_t)step - c.optimizer.decay_start) / c.optimizer.decay_interval));
+    const double t = (double)step + 1.0;
+    return (float)(lr * std::sqrt(1.0 - std::pow((double)c.optimizer.beta2, t)) /
+                   (1.0 - std::pow((double)c.optimizer.beta1, t)));
+}
+
+void require(bool cond, nbvh_status s, const char *msg)
+{
+    if (!cond)
+        fail(s, msg);
+}
+
+void upload_bvh(nbvh_handle *h)
+{
+    // nodes: two float4 per node in the reference layout
+    cuda_check(h->d_nodes.resize(2u * h->nodes.size()), "alloc nodes");
+    cuda_check(cudaMemcpy(h->d_nodes.ptr, h->nodes.data(), h->nodes.size() * sizeof(BVHNode), cudaMemcpyHostToDevice),
+               "upload nodes");
+    // pre-gathered triangle records in leaf order: {v0 | prim}, {e1 | 0}, {e2 | 0}
+    const size_t nt = h->prim_indices.size();
+    std::vector<float> rec(12u * nt);
+    for (size_t j = 0; j < nt; j++) {
+        const uint32_t p = h->prim_indices[j];
+        const float *v0 = &h->vertices[3u * (size_t)h->indices[3u * p]];
+        const float *v1 = &h->vertices[3u * (size_t)h->indices[3u * p + 1u]];
+        const float *v2 = &h->vertices[3u * (size_t)h->indices[3u * p + 2u]];
+        float *r = &rec[12u * j];
+        r[0] = v0[0];
+        r[1] = v0[1];
+        r[2] = v0[2];
+        std::memcpy(&r[3], &p, 4);
+        r[4] = v1[0] - v0[0];
+        r[5] = v1[1] - v0[1];
+        r[6] = v1[2] - v0[2];
+        r[7] = 0.f;
+        r[8] = v2[0] - v0[0];
+        r[9] = v2[1] - v0[1];
+        r[10] = v2[2] - v0[2];
+        r[11] = 0.f;
+    }
+    cuda_check(h->d_tris.resize(3u * nt), "alloc triangles");
+    cuda_check(cudaMemcpy(h->d_tris.ptr, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice),
+               "upload triangles");
+    if (!h->albedo.empty()) {
+        cuda_check(h->d_albedo.resize(h->albedo.size()), "alloc albedo");
+        cuda_check(cudaMemcpy(h->d_albedo.ptr, h->albedo.data(), h->albedo.size() * sizeof(float), cudaMemcpyHostToDevice),
+                   "upload albedo");
+    } else {
+        h->d_albedo.release();
+    }
+}
+
+void upload_neural(nbvh_handle *h)
+{
+    cuda_check(h->d_neural_nodes.resize(2u * h->neural_nodes.size()), "alloc neural nodes");
+    cuda_check(cudaMemcpy(h->d_neural_nodes.ptr, h->neural_nodes.data(), h->neural_nodes.size() * sizeof(BVHNode),
+                          cudaMemcpyHostToDevice),
+               "upload neural nodes");
+    h->non_neural.assign(h->neural_nodes.size(), 0u);
+    h->any_non_neural = false;
+    h->d_non_neural.release();
+}
+
+void upload_params(nbvh_handle *h, const float *params, bool reset_adam)
+{
+    const uint32_t n = h->layout.n_params;
+    cuda_check(h->d_params.resize(n), "alloc params");
+    cuda_check(h->d_params_h.resize(n), "alloc fp16 params");
+    cuda_check(cudaMemcpy(h->d_params.ptr, params, (size_t)n * sizeof(float), cudaMemcpyHostToDevice), "upload params");
+    cuda_check(launch_params_to_half(h->d_params.ptr, h->d_params_h.ptr, n, nullptr), "to half");
+    if (reset_adam) {
+        cuda_check(h->d_adam_m.resize(n), "alloc adam m");
+        cuda_check(h->d_adam_v.resize(n), "alloc adam v");
+        cuda_check(cudaMemset(h->d_adam_m.ptr, 0, (size_t)n * sizeof(float)), "zero m");
+        cuda_check(cudaMemset(h->d_adam_v.ptr, 0, (size_t)n * sizeof(float)), "zero v");
+        h->training_step = 0;
+    }
+    cuda_check(cudaDeviceSynchronize(), "sync");
+}
+
+void ensure_train_workspace(nbvh_handle *h, uint32_t n)
+{
+    const uint32_t P = h->grid.n_points, ni = h->layout.n_inputs, H = (uint32_t)h->cfg.network.n_hidden_layers;
+    if (h->d_train_pos.count < (size_t)n * P * 3u)
+        cuda_check(h->d_train_pos.resize((size_t)n * P * 3u), "alloc train positions");
+    if (h->d_train_tgt.count < (size_t)n * 8u)
+        cuda_check(h->d_train_tgt.resize((size_t)n * 8u), "alloc train targets");
+    if (h->d_train_nodes.count < n)
+        cuda_check(h->d_train_nodes.resize(n), "alloc train nodes");
+    if (h->d_train_acts.count < (size_t)n * (ni + H * kNeurons))
+        cuda_check(h->d_train_acts.resize((size_t)n * (ni + H * kNeurons)), "alloc activations");
+    if (h->d_train_dz.count < (size_t)n * (H * kNeurons + kOutputsPadded))
+        cuda_check(h->d_train_dz.resize((size_t)n * (H * kNeurons + kOutputsPadded)), "alloc gradients");
+    if (h->d_grad.count < h->layout.n_params)
+        cuda_check(h->d_grad.resize(h->layout.n_params), "alloc grad");
+}
+
+void ensure_query_workspace(nbvh_handle *h, uint32_t n, int ctx)
+{
+    if (h->d_counters.count < 3u)
+        cuda_check(h->d_counters.resize(3u), "alloc counters");
+    auto &list = ctx == 0 ? h->d_fallback_list : h->d_pipe_fallback[ctx - 1];
+    if (list.count < n)
+        cuda_check(list.resize(n), "alloc fallback list");
+}
+
+// The neural query on device buffers with query context ctx (0: API calls, 1-2: host pipeline).
+void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t depth, bool vis_only,
+                  nbvh_neural_hit *d_hits, cudaStream_t s, int ctx, bool timed)
+{
+    require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
+    require(h->neural_built, NBVH_ESTATE, "neural cut not built");
+    ensure_query_workspace(h, n, ctx);
+    QueryCounters *counters = h->d_counters.ptr + ctx;
+    uint32_t *list = ctx == 0 ? h->d_fallback_list.ptr : h->d_pipe_fallback[ctx - 1].ptr;
+    cuda_check(cudaMemsetAsync(counters, 0, sizeof(QueryCounters), s), "reset counters");
+    if (h->cfg.bvh.ignore_neural_blas) {
+        // the non-neural BLAS switch: the mesh goes to the classic traversal
+        // (include/cuda/neural/neural_bvh_module_common.cuh:323)
+        if (timed)
+            cuda_check(cudaEventRecord(h->ev0, s), "event");
+        cuda_check(launch_classic_as_neural(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, vis_only, s), "classic");
+        if (timed)
+            cuda_check(cudaEventRecord(h->ev1, s), "event");
+        h->last_launches = 1;
+        return;
+    }
+    const NeuralConsts nc = make_neural_consts(h, depth, vis_only);
+    if (timed)
+        cuda_check(cudaEventRecord(h->ev0, s), "event");
+    cuda_check(launch_neural_query(h->d_neural_nodes.ptr, h->any_non_neural ? h->d_non_neural.ptr : nullptr,
+                                   h->d_params_h.ptr, h->grid, nc, (uint32_t)h->cfg.network.n_hidden_layers, d_rays, n,
+                                   d_hits, counters, list, h->num_sms, s),
+               "neural query");
+    if (timed)
+        cuda_check(cudaEventRecord(h->ev1, s), "event");
+    h->last_launches = 1;
+    if (h->any_non_neural || h->cfg.fallback_margin > 0.f) {
+        cuda_check(launch_classic_fallback(h->d_nodes.ptr, h->d_tris.ptr, d_rays, list, counters, n, d_hits, vis_only,
+                                           h->num_sms, s),
+                   "fallback");
+        h->last_launches = 2;
+    }
+    h->last_rays = n;
+}
+
+} // namespace
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+
+extern "C" {
+
+uint32_t nbvh_abi_version(void) { return NBVH_ABI_VERSION; }
+
+const char *nbvh_status_string(nbvh_status s)
+{
+    switch (s) {
+    case NBVH_OK: return "ok";
+    case NBVH_EINVAL: return "invalid argument";
+    case NBVH_ENOMEM: return "out of memory";
+    case NBVH_EDEVICE: return "CUDA device error";
+    case NBVH_ETIMEOUT: return "device loop step cap reached";
+    case NBVH_EOVERFLOW: return "traversal stack overflow";
+    case NBVH_ESTATE: return "call order violated";
+    case NBVH_EIO: return "checkpoint i/o error";
+    }
+    return "unknown status";
+}
+
+const char *nbvh_last_error(const nbvh_handle *h) { return h ? h->last_error.c_str() : "null handle"; }
+
+nbvh_status nbvh_config_default(nbvh_config *c)
+{
+    if (!c)
+        return NBVH_EINVAL;
+    std::memset(c, 0, sizeof(*c));
+    c->abi_version = NBVH_ABI_VERSION;
+    c->hashgrid.n_levels = 16;
+    c->hashgrid.n_features_per_level = 2;
+    c->hashgrid.log2_hashmap_size = 19;
+    c->hashgrid.base_resolution = 16;
+    c->hashgrid.per_level_scale = (float)std::pow(2048.0 / 16.0, 1.0 / 15.0);
+    c->network.n_neurons = 64;
+    c->network.n_hidden_layers = 4;
+    c->network.precision = NBVH_PRECISION_FP16;
+    c->optimizer.learning_rate = 1e-2f;
+    c->optimizer.beta1 = 0.9f;
+    c->optimizer.beta2 = 0.999f;
+    c->optimizer.epsilon = 1e-8f;
+    c->optimizer.l2_reg = 1e-8f;
+    c->optimizer.decay_start = 10000;
+    c->optimizer.decay_interval = 2000;
+    c->optimizer.decay_base = 0.33f;
+    c->optimizer.loss_scale = 128.0f;
+    c->bvh.inference_mint_epsilon = 1e-4f;
+    c->bvh.inference_maxt_epsilon = 1e-3f;
+    c->bvh.learning_mint_epsilon = 1e-3f;
+    c->bvh.learning_maxt_epsilon = 1e-3f;
+    c->bvh.sampling_bbox_scaling = 1.5f;
+    c->bvh.fixed_node_dilation = 1e-5f;
+    c->bvh.node_extent_dilation = 1e-4f;
+    c->bvh.leaf_boundary_sampling_ratio = 0.0f;
+    c->bvh.ignore_neural_blas = 0;
+    c->bvh.max_training_bounces = 1;
+    c->bvh.sample_cosine_weighted = 1;
+    c->bvh.backface_bounce_training = 0;
+    c->bvh.log2_bvh_max_traversals = 0;
+    c->output.visibility_loss = NBVH_LOSS_BCE;
+    c->output.visibility_loss_scale = 1.f;
+    c->output.depth_loss = NBVH_LOSS_L1;
+    c->output.depth_loss_scale = 1.f;
+    c->output.normal_loss = NBVH_LOSS_L1;
+    c->output.normal_loss_scale = 1.f;
+    c->output.albedo_loss = NBVH_LOSS_RELATIVE_L2;
+    c->output.albedo_loss_scale = 1.f;
+    c->output.output_normal_linear_activation = 1;
+    c->output.output_albedo_linear_activation = 0;
+    c->output.visibility_masking_loss = 1;
+    c->output.primary_visibility_threshold = 0.5f;
+    c->output.secondary_visibility_threshold = 0.5f;
+    c->output.depth_epsilon = 0.2f;
+    c->output.fixed_depth_epsilon = 1e-5f;
+    c->output.learn_normal = 1;
+    c->output.learn_albedo = 1;
+    c->module.input_segment_points = 4;
+    c->module.segment_distribution = NBVH_SEGMENT_EQUIDISTANT_INTERIOR;
+    c->batch_size = 1u << 18;
+    c->neural_bvh_max_depth = 10;
+    c->max_traversal_steps = 1000;
+    c->seed = 1337;
+    c->fallback_margin = 0.0f;
+    return NBVH_OK;
+}
+
+nbvh_status nbvh_create(const nbvh_config *cfg, int device, nbvh_handle **out)
+{
+    if (!cfg || !out)
+        return NBVH_EINVAL;
+    *out = nullptr;
+    nbvh_handle *h = nullptr;
+    try {
+        h = new nbvh_handle();
+    } catch (...) {
+        return NBVH_ENOMEM;
+    }
+    h->device = device;
+    nbvh_status st = guarded_free([&]() {
+        validate_config(*cfg);
+        h->cfg = *cfg;
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+            fail(NBVH_EDEVICE, "no CUDA device");
+        if (device < 0 || device >= count)
+            fail(NBVH_EINVAL, "bad device index");
+        cuda_check(cudaSetDevice(device), "cudaSetDevice");
+        cuda_check(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device), "SM count");
+        cuda_check(cudaEventCreate(&h->ev0), "event");
+        cuda_check(cudaEventCreate(&h->ev1), "event");
+        for (int k = 0; k < 2; k++)
+            cuda_check(cudaStreamCreateWithFlags(&h->pipe_stream[k], cudaStreamNonBlocking), "stream");
+        cuda_check(h->d_counters.resize(3u), "alloc counters");
+        cuda_check(cudaMemset(h->d_counters.ptr, 0, 3u * sizeof(QueryCounters)), "zero counters");
+        cuda_check(h->d_loss_sum.resize(1u), "alloc loss");
+        compute_layout(h->cfg, h->layout, h->grid);
+        std::vector<float> p(h->layout.n_params);
+        init_params(h->cfg, h->layout, p.data());
+        upload_params(h, p.data(), true);
+    });
+    if (st != NBVH_OK) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    return NBVH_OK;
+}
+
+nbvh_status nbvh_destroy(nbvh_handle *h)
+{
+    if (!h)
+        return NBVH_EINVAL;
+    cudaSetDevice(h->device);
+    cudaDeviceSynchronize();
+    for (int k = 0; k < 2; k++) {
+        if (h->pipe_stream[k])
+            cudaStreamDestroy(h->pipe_stream[k]);
+    }
+    if (h->ev0)
+        cudaEventDestroy(h->ev0);
+    if (h->ev1)
+        cudaEventDestroy(h->ev1);
+    delete h;
+    return NBVH_OK;
+}
+
+nbvh_status nbvh_set_mesh(nbvh_handle *h, const float *v, uint32_t nv, const uint32_t *idx, uint32_t nt,
+                          const float *albedo)
+{
+    return guarded(h, [&]() {
+        require(v && idx && nv > 0 && nt > 0, NBVH_EINVAL, "empty mesh");
+        for (size_t i = 0; i < 3u * (size_t)nt; i++)
+            require(idx[i] < nv, NBVH_EINVAL, "triangle index out of range");
+        h->vertices.assign(v, v + 3u * (size_t)nv);
+        h->indices.assign(idx, idx + 3u * (size_t)nt);
+        if (albedo)
+            h->albedo.assign(albedo, albedo + 3u * (size_t)nt);
+        else
+            h->albedo.clear();
+        h->classic_built = false;
+        h->neural_built = false;
+    });
+}
+
+nbvh_status nbvh_build_classic(nbvh_handle *h)
+{
+    return guarded(h, [&]() {
+        require(!h->indices.empty(), NBVH_ESTATE, "no mesh");
+        std::string err;
+        if (!build_bvh2(h->vertices, h->indices, h->nodes, h->prim_indices, err))
+            fail(NBVH_EINVAL, err);
+        upload_bvh(h);
+        for (int k = 0; k < 3; k++) {
+            h->scene_min[k] = h->nodes[0].min[k];
+            h->scene_max[k] = h->nodes[0].max[k];
+        }
+        h->classic_built = true;
+        h->neural_built = false;
+        cuda_check(cudaDeviceSynchronize(), "sync");
+    });
+}
+
+nbvh_status nbvh_get_classic_bvh(const nbvh_handle *hc, uint32_t *h_nodes, uint32_t *n_nodes, uint32_t *h_prims,
+                                 uint32_t *n_prims)
+{
+    nbvh_handle *h = const_cast<nbvh_handle *>(hc);
+    return guarded(h, [&]() {
+        require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
+        if (n_nodes)
+            *n_nodes = (uint32_t)h->nodes.size();
+        if (n_prims)
+            *n_prims = (uint32_t)h->prim_indices.size();
+        if (h_nodes)
+            std::memcpy(h_nodes, h->nodes.data(), h->nodes.size() * sizeof(BVHNode));
+        if (h_prims)
+            std::memcpy(h_prims, h->prim_indices.data(), h->prim_indices.size() * sizeof(uint32_t));
+    });
+}
+
+nbvh_status nbvh_build_neural_cut(nbvh_handle *h, uint32_t max_depth)
+{
+    return guarded(h, [&]() {
+        require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
+        build_neural_cut(h->nodes, max_depth, h->neural_nodes);
+        upload_neural(h);
+        h->neural_built = true;
+        cuda_check(cudaDeviceSynchronize(), "sync");
+    });
+}
+
+nbvh_status nbvh_get_neural_bvh(const nbvh_handle *hc, uint32_t *h_nodes, uint32_t *n_nodes, float *bbox)
+{
+    nbvh_handle *h = const_cast<nbvh_handle *>(hc);
+    return guarded(h, [&]() {
+        require(h->neural_built, NBVH_ESTATE, "neural cut not built");
+        if (n_nodes)
+            *n_nodes = (uint32_t)h->neural_nodes.size();
+        if (h_nodes)
+            std::memcpy(h_nodes, h->neural_nodes.data(), h->neural_nodes.size() * sizeof(BVHNode));
+        if (bbox) {
+            for (int k = 0; k < 3; k++) {
+                bbox[k] = h->scene_min[k];
+                bbox[3 + k] = h->scene_max[k];
+            }
+        }
+    });
+}
+
+nbvh_status nbvh_set_non_neural_leaves(nbvh_handle *h, const uint32_t *ids, uint32_t n, int flag)
+{
+    return guarded(h, [&]() {
+        require(h->neural_built, NBVH_ESTATE, "neural cut not built");
+        require(ids || n == 0, NBVH_EINVAL, "null ids");
+        for (uint32_t i = 0; i < n; i++) {
+            require(ids[i] < h->neural_nodes.size(), NBVH_EINVAL, "node id out of range");
+            h->non_neural[ids[i]] = flag ? 1u : 0u;
+        }
+        h->any_non_neural = false;
+        for (uint8_t f : h->non_neural)
+            h->any_non_neural |= f != 0u;
+        cuda_check(h->d_non_neural.resize(h->non_neural.size()), "alloc flags");
+        cuda_check(cudaMemcpy(h->d_non_neural.ptr, h->non_neural.data(), h->non_neural.size(), cudaMemcpyHostToDevice),
+                   "upload flags");
+    });
+}
+
+nbvh_status nbvh_set_ignore_neural_blas(nbvh_handle *h, int ignore)
+{
+    return guarded(h, [&]() { h->cfg.bvh.ignore_neural_blas = ignore ? 1 : 0; });
+}
+
+nbvh_status nbvh_query_closest_classic(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, nbvh_hit *d_hits,
+                                       nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
+        require((d_rays && d_hits) || n == 0, NBVH_EINVAL, "null buffers");
+        cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        cuda_check(cudaEventRecord(h->ev0, s), "event");
+        cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, false, nullptr, s), "classic");
+        cuda_check(cudaEventRecord(h->ev1, s), "event");
+        h->last_launches = 1;
+        h->last_rays = n;
+    });
+}
+
+nbvh_status nbvh_query_any_classic(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, nbvh_hit *d_hits,
+                                   nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
+        require((d_rays && d_hits) || n == 0, NBVH_EINVAL, "null buffers");
+        cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        cuda_check(cudaEventRecord(h->ev0, s), "event");
+        cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, true, nullptr, s), "classic");
+        cuda_check(cudaEventRecord(h->ev1, s), "event");
+        h->last_launches = 1;
+        h->last_rays = n;
+    });
+}
+
+nbvh_status nbvh_query_closest_neural(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t depth,
+                                      nbvh_neural_hit *d_hits, nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require((d_rays && d_hits) || n == 0, NBVH_EINVAL, "null buffers");
+        neural_query(h, d_rays, n, depth, false, d_hits, reinterpret_cast<cudaStream_t>(stream), 0, true);
+    });
+}
+
+nbvh_status nbvh_query_visibility_neural(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t depth,
+                                         nbvh_neural_hit *d_hits, nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require((d_rays && d_hits) || n == 0, NBVH_EINVAL, "null buffers");
+        neural_query(h, d_rays, n, depth, true, d_hits, reinterpret_cast<cudaStream_t>(stream), 0, true);
+    });
+}
+
+} // extern "C"
+
+namespace {
+
+// Host-buffer queries: chunks alternate between two streams; each chunk is copied in, queried and
+// copied out on its stream, so the copies of one chunk overlap the kernel of the other.
+template <typename Rec, typename Q>
+void pipelined(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, Rec *h_out, Q &&query)
+{
+    const uint32_t chunk = 1u << 20;
+    const size_t in_bytes = (size_t)chunk * sizeof(nbvh_ray), out_bytes = (size_t)chunk * sizeof(Rec);
+    for (int k = 0; k < 2; k++) {
+        if (h->d_pipe_in[k].count < in_bytes)
+            cuda_check(h->d_pipe_in[k].resize(in_bytes), "alloc pipeline in");
+        if (h->d_pipe_out[k].count < out_bytes)
+            cuda_check(h->d_pipe_out[k].resize(out_bytes), "alloc pipeline out");
+    }
+    uint32_t launches = 0;
+    for (uint32_t c0 = 0, ci = 0; c0 < n; c0 += chunk, ci++) {
+        const int k = (int)(ci & 1u);
+        const uint32_t cnt = (n - c0) < chunk ? (n - c0) : chunk;
+        cudaStream_t s = h->pipe_stream[k];
+        auto *din = reinterpret_cast<nbvh_ray *>(h->d_pipe_in[k].ptr);
+        auto *dout = reinterpret_cast<Rec *>(h->d_pipe_out[k].ptr);
+        cuda_check(cudaMemcpyAsync(din, h_rays + c0, (size_t)cnt * sizeof(nbvh_ray), cudaMemcpyHostToDevice, s), "H2D");
+        query(din, cnt, dout, s, 1 + k);
+        launches += h->last_launches;
+        cuda_check(cudaMemcpyAsync(h_out + c0, dout, (size_t)cnt * sizeof(Rec), cudaMemcpyDeviceToHost, s), "D2H");
+    }
+    for (int k = 0; k < 2; k++)
+        cuda_check(cudaStreamSynchronize(h->pipe_stream[k]), "sync pipeline");
+    h->last_launches = launches;
+    h->last_rays = n;
+}
+
+} // namespace
+
+extern "C" {
+
+nbvh_status nbvh_query_closest_neural_host(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, uint32_t depth,
+                                           nbvh_neural_hit *h_hits)
+{
+    return guarded(h, [&]() {
+        require((h_rays && h_hits) || n == 0, NBVH_EINVAL, "null buffers");
+        pipelined(h, h_rays, n, h_hits, [&](const nbvh_ray *din, uint32_t cnt, nbvh_neural_hit *dout, cudaStream_t s, int ctx) {
+            neural_query(h, din, cnt, depth, false, dout, s, ctx, false);
+        });
+    });
+}
+
+nbvh_status nbvh_query_closest_classic_host(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, nbvh_hit *h_hits)
+{
+    return guarded(h, [&]() {
+        require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
+        require((h_rays && h_hits) || n == 0, NBVH_EINVAL, "null buffers");
+        pipelined(h, h_rays, n, h_hits, [&](const nbvh_ray *din, uint32_t cnt, nbvh_hit *dout, cudaStream_t s, int) {
+            cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, din, cnt, dout, false, nullptr, s), "classic");
+            h->last_launches = 1;
+        });
+    });
+}
+
+nbvh_status nbvh_query_segments(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t max_segments,
+                                nbvh_segment *d_segments, uint32_t *d_counts, nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require(h->neural_built, NBVH_ESTATE, "neural cut not built");
+        require((d_rays && d_counts && (d_segments || max_segments == 0)) || n == 0, NBVH_EINVAL, "null buffers");
+        const NeuralConsts nc = make_neural_consts(h, 1u, false);
+        cuda_check(launch_segments(h->d_neural_nodes.ptr, nc, d_rays, n, max_segments, d_segments, d_counts,
+                                   reinterpret_cast<cudaStream_t>(stream)),
+                   "segments");
+        h->last_launches = 1;
+    });
+}
+
+nbvh_status nbvh_get_param_layout(const nbvh_handle *hc, nbvh_param_layout *out)
+{
+    nbvh_handle *h = const_cast<nbvh_handle *>(hc);
+    return guarded(h, [&]() {
+        require(out != nullptr, NBVH_EINVAL, "null output");
+        *out = h->layout;
+    });
+}
+
+nbvh_status nbvh_get_params(nbvh_handle *h, float *h_params)
+{
+    return guarded(h, [&]() {
+        require(h_params != nullptr, NBVH_EINVAL, "null output");
+        cuda_check(cudaDeviceSynchronize(), "sync");
+        cuda_check(cudaMemcpy(h_params, h->d_params.ptr, (size_t)h->layout.n_params * sizeof(float),
+                              cudaMemcpyDeviceToHost),
+                   "download params");
+    });
+}
+
+nbvh_status nbvh_set_params(nbvh_handle *h, const float *h_params)
+{
+    return guarded(h, [&]() {
+        require(h_params != nullptr, NBVH_EINVAL, "null input");
+        upload_params(h, h_params, true);
+    });
+}
+
+nbvh_status nbvh_network_inference(nbvh_handle *h, const float *d_positions, uint32_t n, float *d_outputs,
+                                   nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require((d_positions && d_outputs) || n == 0, NBVH_EINVAL, "null buffers");
+        cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        cuda_check(cudaEventRecord(h->ev0, s), "event");
+        cuda_check(launch_network_inference(h->d_params_h.ptr, h->grid, (uint32_t)h->cfg.network.n_hidden_layers,
+                                            d_positions, n, d_outputs, h->num_sms, s),
+                   "network inference");
+        cuda_check(cudaEventRecord(h->ev1, s), "event");
+        h->last_launches = 1;
+    });
+}
+
+nbvh_status nbvh_encode(nbvh_handle *h, const float *d_positions, uint32_t n, float *d_features, nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require((d_positions && d_features) || n == 0, NBVH_EINVAL, "null buffers");
+        cuda_check(launch_encode(h->d_params_h.ptr, h->grid, (uint32_t)h->cfg.network.n_hidden_layers, d_positions, n,
+                                 d_features, reinterpret_cast<cudaStream_t>(stream)),
+                   "encode");
+        h->last_launches = 1;
+    });
+}
+
+} // extern "C"
+
+namespace {
+
+// forward + loss + backward of one batch into h->d_grad (scaled by the loss scale) and loss_sum
+void gradients_into_workspace(nbvh_handle *h, const float *d_pos, const float *d_tgt, uint32_t n, cudaStream_t s,
+                              float *loss_slot)
+{
+    ensure_train_workspace(h, n);
+    const uint32_t H = (uint32_t)h->cfg.network.n_hidden_layers;
+    cuda_check(cudaMemsetAsync(h->d_grad.ptr, 0, (size_t)h->layout.n_params * sizeof(float), s), "zero grad");
+    cuda_check(launch_train_forward_backward(h->d_params_h.ptr, h->grid, H, make_loss_consts(h->cfg, n), d_pos, d_tgt, n,
+                                             h->d_train_acts.ptr, h->d_train_dz.ptr, h->d_grad.ptr, loss_slot,
+                                             h->num_sms, s),
+               "forward/backward");
+    cuda_check(launch_weight_gradients(h->grid, H, h->d_train_acts.ptr, h->d_train_dz.ptr, n, h->d_grad.ptr, h->num_sms,
+                                       s),
+               "weight gradients");
+}
+
+} // namespace
+
+extern "C" {
+
+nbvh_status nbvh_compute_gradients(nbvh_handle *h, const float *d_positions, const float *d_targets, uint32_t n,
+                                   float *d_gradients, float *h_loss, nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require(d_positions && d_targets && d_gradients && n > 0, NBVH_EINVAL, "null buffers");
+        cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        cuda_check(cudaMemsetAsync(h->d_loss_sum.ptr, 0, sizeof(float), s), "zero loss");
+        gradients_into_workspace(h, d_positions, d_targets, n, s, h->d_loss_sum.ptr);
+        cuda_check(cudaMemcpyAsync(d_gradients, h->d_grad.ptr, (size_t)h->layout.n_params * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, s),
+                   "copy grad");
+        cuda_check(launch_scale(d_gradients, h->layout.n_params, 1.0f / h->cfg.optimizer.loss_scale, s), "unscale");
+        float loss = 0.f;
+        cuda_check(cudaMemcpyAsync(&loss, h->d_loss_sum.ptr, sizeof(float), cudaMemcpyDeviceToHost, s), "loss");
+        cuda_check(cudaStreamSynchronize(s), "sync");
+        if (h_loss)
+            *h_loss = loss;
+        h->last_launches = 4;
+    });
+}
+
+nbvh_status nbvh_adam_step(nbvh_handle *h, const float *d_gradients, nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require(d_gradients != nullptr, NBVH_EINVAL, "null gradient");
+        const nbvh_config &c = h->cfg;
+        cuda_check(launch_adam(h->d_params.ptr, h->d_params_h.ptr, h->d_adam_m.ptr, h->d_adam_v.ptr, d_gradients,
+                               h->layout.n_params, adam_step_size(c, h->training_step), c.optimizer.beta1,
+                               c.optimizer.beta2, c.optimizer.epsilon, c.optimizer.l2_reg, 1.0f,
+                               reinterpret_cast<cudaStream_t>(stream)),
+                   "adam");
+        h->training_step++;
+        h->last_launches = 1;
+    });
+}
+
+nbvh_status nbvh_generate_training_batch(nbvh_handle *h, uint32_t training_step, uint32_t n, float *d_positions,
+                                         float *d_targets, uint32_t *d_nodes, nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require(h->neural_built, NBVH_ESTATE, "neural cut not built");
+        require((d_positions && d_targets) || n == 0, NBVH_EINVAL, "null buffers");
+        const NeuralConsts nc = make_neural_consts(h, 1u, false);
+        cuda_check(launch_training_samples(h->d_neural_nodes.ptr, h->d_nodes.ptr, h->d_tris.ptr,
+                                           h->albedo.empty() ? nullptr : h->d_albedo.ptr, nc, h->grid, training_step,
+                                           h->cfg.batch_size, n, d_positions, d_targets, d_nodes,
+                                           reinterpret_cast<cudaStream_t>(stream)),
+                   "training samples");
+        h->last_launches = 1;
+    });
+}
+
+nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_stats *stats)
+{
+    return guarded(h, [&]() {
+        require(h->neural_built, NBVH_ESTATE, "neural cut not built");
+        const nbvh_config &c = h->cfg;
+        const uint32_t n = c.batch_size;
+        ensure_train_workspace(h, n);
+        if (h->d_loss_sum.count < (size_t)steps + 1u)
+            cuda_check(h->d_loss_sum.resize((size_t)steps + 1u), "alloc loss");
+        cudaStream_t s = h->pipe_stream[0];
+        cuda_check(cudaMemsetAsync(h->d_loss_sum.ptr, 0, ((size_t)steps + 1u) * sizeof(float), s), "zero loss");
+        const NeuralConsts nc = make_neural_consts(h, 1u, false);
+        const uint32_t first = h->training_step;
+        float lr_t = 0.f;
+        cuda_check(cudaEventRecord(h->ev0, s), "event");
+        for (uint32_t i = 0; i < steps; i++) {
+            cuda_check(launch_training_samples(h->d_neural_nodes.ptr, h->d_nodes.ptr, h->d_tris.ptr,
+                                               h->albedo.empty() ? nullptr : h->d_albedo.ptr, nc, h->grid,
+                                               h->training_step, n, n, h->d_train_pos.ptr, h->d_train_tgt.ptr,
+                                               h->d_train_nodes.ptr, s),
+                       "training samples");
+            gradients_into_workspace(h, h->d_train_pos.ptr, h->d_train_tgt.ptr, n, s, h->d_loss_sum.ptr + i);
+            lr_t = adam_step_size(c, h->training_step);
+            cuda_check(launch_adam(h->d_params.ptr, h->d_params_h.ptr, h->d_adam_m.ptr, h->d_adam_v.ptr, h->d_grad.ptr,
+                                   h->layout.n_params, lr_t, c.optimizer.beta1, c.optimizer.beta2, c.optimizer.epsilon,
+                                   c.optimizer.l2_reg, 1.0f / c.optimizer.loss_scale, s),
+                       "adam");
+            h->training_step++;
+        }
+        cuda_check(cudaEventRecord(h->ev1, s), "event");
+        std::vector<float> losses(steps > 0 ? steps : 1u);
+        if (steps > 0)
+            cuda_check(cudaMemcpyAsync(losses.data(), h->d_loss_sum.ptr, steps * sizeof(float), cudaMemcpyDeviceToHost, s),
+                       "losses");
+        cuda_check(cudaStreamSynchronize(s), "sync");
+        float ms = 0.f;
+        cuda_check(cudaEventElapsedTime(&ms, h->ev0, h->ev1), "elapsed");
+        h->last_kernel_ms = ms;
+        h->last_launches = 4u * steps;
+        if (stats) {
+            double sum = 0.0;
+            for (uint32_t i = 0; i < steps; i++)
+                sum += losses[i];
+            stats->steps_done = steps;
+            stats->training_step = h->training_step;
+            stats->last_loss = steps ? losses[steps - 1u] : 0.f;
+            stats->mean_loss = steps ? (float)(sum / steps) : 0.f;
+            stats->learning_rate = lr_t;
+            stats->ms_per_step = steps ? ms / (float)steps : 0.f;
+        }
+        (void)first;
+    });
+}
+
+uint32_t nbvh_training_step(const nbvh_handle *h) { return h ? h->training_step : 0u; }
+
+} // extern "C"
+
+namespace {
+
+void camera_params(const nbvh_render_request *r, float du[3], float dv[3], float tl[3])
+{
+    // CudaBackend::update_camera, src/cuda/cuda_backend.cpp:595-611 (FP32, glm's order)
+    auto sub = [](const float *a, const float *b, float *o) {
+        for (int k = 0; k < 3; k++)
+            o[k] = a[k] - b[k];
+    };
+    auto dot = [](const float *a, const float *b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; };
+    auto cross = [](const float *a, const float *b, float *o) {
+        o[0] = a[1] * b[2] - b[1] * a[2];
+        o[1] = a[2] * b[0] - b[2] * a[0];
+        o[2] = a[0] * b[1] - b[0] * a[1];
+    };
+    auto normalize = [&](float *v) {
+        float s = 1.0f / std::sqrt(dot(v, v));
+        for (int k = 0; k < 3; k++)
+            v[k] = v[k] * s;
+    };
+    const float ipy = 2.0f * std::tan((0.5f * r->yfov_degrees) * 0.0174532925199432958f);
+    const float aspect = (float)r->width / (float)r->height;
+    const float ipx = ipy * aspect;
+    float dir[3], up[3] = {r->up[0], r->up[1], r->up[2]};
+    sub(r->target, r->origin, dir);
+    normalize(dir);
+    normalize(up);
+    float t[3];
+    cross(dir, up, t);
+    normalize(t);
+    for (int k = 0; k < 3; k++)
+        du[k] = t[k] * ipx;
+    cross(du, dir, t);
+    normalize(t);
+    for (int k = 0; k < 3; k++)
+        dv[k] = t[k] * -ipy;
+    for (int k = 0; k < 3; k++)
+        tl[k] = (dir[k] - du[k] * 0.5f) - dv[k] * 0.5f;
+}
+
+} // namespace
+
+extern "C" {
+
+nbvh_status nbvh_camera_rays(nbvh_handle *h, const nbvh_render_request *req, nbvh_ray *d_rays, nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require(req && d_rays && req->width > 0 && req->height > 0, NBVH_EINVAL, "bad request");
+        float du[3], dv[3], tl[3];
+        camera_params(req, du, dv, tl);
+        cuda_check(launch_camera_rays(req->width, req->height, req->sample_idx, req->sample_offset, req->origin, du, dv, tl,
+                                      d_rays, reinterpret_cast<cudaStream_t>(stream)),
+                   "camera rays");
+    });
+}
+
+nbvh_status nbvh_run_inference(nbvh_handle *h, const nbvh_render_request *req, nbvh_neural_hit *d_image,
+                               nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require(req && d_image && req->width > 0 && req->height > 0, NBVH_EINVAL, "bad request");
+        const uint32_t n = req->width * req->height;
+        if (h->d_pipe_in[0].count < (size_t)n * sizeof(nbvh_ray))
+            cuda_check(h->d_pipe_in[0].resize((size_t)n * sizeof(nbvh_ray)), "alloc camera rays");
+        auto *rays = reinterpret_cast<nbvh_ray *>(h->d_pipe_in[0].ptr);
+        cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        float du[3], dv[3], tl[3];
+        camera_params(req, du, dv, tl);
+        cuda_check(launch_camera_rays(req->width, req->height, req->sample_idx, req->sample_offset, req->origin, du, dv, tl,
+                                      rays, s),
+                   "camera rays");
+        neural_query(h, rays, n, 1u, false, d_image, s, 0, true);
+        cuda_check(cudaStreamSynchronize(s), "sync");
+    });
+}
+
+nbvh_status nbvh_last_query_stats(nbvh_handle *h, nbvh_query_stats *out)
+{
+    return guarded(h, [&]() {
+        require(out != nullptr, NBVH_EINVAL, "null output");
+        cuda_check(cudaDeviceSynchronize(), "sync");
+        QueryCounters c[3];
+        cuda_check(cudaMemcpy(c, h->d_counters.ptr, sizeof(c), cudaMemcpyDeviceToHost), "counters");
+        std::memset(out, 0, sizeof(*out));
+        out->rays = h->last_rays;
+        for (int k = 0; k < 3; k++) {
+            out->segments += c[k].segments;
+            out->step_capped += c[k].step_capped;
+            out->stack_overflow += c[k].stack_overflow;
+            out->fallback += c[k].fallback;
+        }
+    });
+}
+
+nbvh_status nbvh_last_kernel_time(nbvh_handle *h, float *ms, uint32_t *launches)
+{
+    return guarded(h, [&]() {
+        cuda_check(cudaEventSynchronize(h->ev1), "event sync");
+        float t = 0.f;
+        cuda_check(cudaEventElapsedTime(&t, h->ev0, h->ev1), "elapsed");
+        if (ms)
+            *ms = t;
+        if (launches)
+            *launches = h->last_launches;
+    });
+}
+
+} // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Checkpoints: own binary format "NBVHCKP1"
+// ---------------------------------------------------------------------------------------------
+
+namespace {
+
+constexpr char kMagic[8] = {'N', 'B', 'V', 'H', 'C', 'K', 'P', '1'};
+
+template <typename T>
+void wr_vec(std::ofstream &f, const std::vector<T> &v)
+{
+    uint64_t n = v.size();
+    f.write(reinterpret_cast<const char *>(&n), 8);
+    if (n)
+        f.write(reinterpret_cast<const char *>(v.data()), (std::streamsize)(n * sizeof(T)));
+}
+
+template <typename T>
+void rd_vec(std::ifstream &f, std::vector<T> &v, uint64_t max_elems)
+{
+    uint64_t n = 0;
+    f.read(reinterpret_cast<char *>(&n), 8);
+    if (!f || n > max_elems)
+        fail(NBVH_EIO, "malformed checkpoint");
+    v.resize(n);
+    if (n)
+        f.read(reinterpret_cast<char *>(v.data()), (std::streamsize)(n * sizeof(T)));
+    if (!f)
+        fail(NBVH_EIO, "truncated checkpoint");
+}
+
+} // namespace
+
+extern "C" {
+
+nbvh_status nbvh_save(nbvh_handle *h, const char *path)
+{
+    return guarded(h, [&]() {
+        require(path != nullptr, NBVH_EINVAL, "null path");
+        std::ofstream f(path, std::ios::binary);
+        if (!f)
+            fail(NBVH_EIO, "cannot open checkpoint for writing");
+        cuda_check(cudaDeviceSynchronize(), "sync");
+        const uint32_t np = h->layout.n_params;
+        std::vector<float> p(np), m(np), v(np);
+        cuda_check(cudaMemcpy(p.data(), h->d_params.ptr, np * sizeof(float), cudaMemcpyDeviceToHost), "params");
+        cuda_check(cudaMemcpy(m.data(), h->d_adam_m.ptr, np * sizeof(float), cudaMemcpyDeviceToHost), "adam m");
+        cuda_check(cudaMemcpy(v.data(), h->d_adam_v.ptr, np * sizeof(float), cudaMemcpyDeviceToHost), "adam v");
+        f.write(kMagic, 8);
+        f.write(reinterpret_cast<const char *>(&h->cfg), sizeof(nbvh_config));
+        f.write(reinterpret_cast<const char *>(&h->training_step), 4);
+        uint32_t flags = (h->classic_built ? 1u : 0u) | (h->neural_built ? 2u : 0u);
+        f.write(reinterpret_cast<const char *>(&flags), 4);
+        wr_vec(f, h->vertices);
+        wr_vec(f, h->indices);
+        wr_vec(f, h->albedo);
+        wr_vec(f, h->nodes);
+        wr_vec(f, h->prim_indices);
+        wr_vec(f, h->neural_nodes);
+        wr_vec(f, h->non_neural);
+        f.write(reinterpret_cast<const char *>(h->scene_min), 12);
+        f.write(reinterpret_cast<const char *>(h->scene_max), 12);
+        wr_vec(f, p);
+        wr_vec(f, m);
+        wr_vec(f, v);
+        if (!f)
+            fail(NBVH_EIO, "checkpoint write failed");
+    });
+}
+
+nbvh_status nbvh_load(nbvh_handle *h, const char *path)
+{
+    return guarded(h, [&]() {
+        require(path != nullptr, NBVH_EINVAL, "null path");
+        std::ifstream f(path, std::ios::binary);
+        if (!f)
+            fail(NBVH_EIO, "cannot open checkpoint");
+        char magic[8];
+        f.read(magic, 8);
+        if (!f || std::memcmp(magic, kMagic, 8) != 0)
+            fail(NBVH_EIO, "not an nbvh checkpoint");
+        nbvh_config cfg;
+        f.read(reinterpret_cast<char *>(&cfg), sizeof(cfg));
+        uint32_t step = 0, flags = 0;
+        f.read(reinterpret_cast<char *>(&step), 4);
+        f.read(reinterpret_cast<char *>(&flags), 4);
+        if (!f)
+            fail(NBVH_EIO, "truncated checkpoint");
+        validate_config(cfg);
+        const uint64_t lim = 1ull << 31;
+        std::vector<float> verts, albedo, p, m, v;
+        std::vector<uint32_t> idx, prims;
+        std::vector<BVHNode> nodes, neural;
+        std::vector<uint8_t> non_neural;
+        rd_vec(f, verts, lim);
+        rd_vec(f, idx, lim);
+        rd_vec(f, albedo, lim);
+        rd_vec(f, nodes, lim);
+        rd_vec(f, prims, lim);
+        rd_vec(f, neural, lim);
+        rd_vec(f, non_neural, lim);
+        float smin[3], smax[3];
+        f.read(reinterpret_cast<char *>(smin), 12);
+        f.read(reinterpret_cast<char *>(smax), 12);
+        rd_vec(f, p, lim);
+        rd_vec(f, m, lim);
+        rd_vec(f, v, lim);
+        nbvh_param_layout L;
+        GridParams g;
+        compute_layout(cfg, L, g);
+        if (p.size() != L.n_params || m.size() != L.n_params || v.size() != L.n_params)
+            fail(NBVH_EIO, "checkpoint parameters do not match its configuration");
+        if (idx.size() % 3u != 0u || verts.size() % 3u != 0u || non_neural.size() != neural.size())
+            fail(NBVH_EIO, "malformed checkpoint mesh");
+        for (uint32_t i : idx)
+            if (i >= verts.size() / 3u)
+                fail(NBVH_EIO, "checkpoint triangle index out of range");
+        // commit
+        h->cfg = cfg;
+        h->layout = L;
+        h->grid = g;
+        h->vertices.swap(verts);
+        h->indices.swap(idx);
+        h->albedo.swap(albedo);
+        h->nodes.swap(nodes);
+        h->prim_indices.swap(prims);
+        h->neural_nodes.swap(neural);
+        std::memcpy(h->scene_min, smin, 12);
+        std::memcpy(h->scene_max, smax, 12);
+        h->classic_built = (flags & 1u) && !h->nodes.empty();
+        h->neural_built = (flags & 2u) && !h->neural_nodes.empty();
+        if (h->classic_built)
+            upload_bvh(h);
+        if (h->neural_built) {
+            upload_neural(h);
+            h->non_neural = non_neural;
+            h->any_non_neural = false;
+            for (uint8_t x : h->non_neural)
+                h->any_non_neural |= x != 0u;
+            if (h->any_non_neural) {
+                cuda_check(h->d_non_neural.resize(h->non_neural.size()), "alloc flags");
+                cuda_check(cudaMemcpy(h->d_non_neural.ptr, h->non_neural.data(), h->non_neural.size(),
+                                      cudaMemcpyHostToDevice),
+                           "upload flags");
+            }
+        }
+        upload_params(h, p.data(), true);
+        cuda_check(cudaMemcpy(h->d_adam_m.ptr, m.data(), m.size() * sizeof(float), cudaMemcpyHostToDevice), "adam m");
+        cuda_check(cudaMemcpy(h->d_adam_v.ptr, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice), "adam v");
+        h->training_step = step;
+    });
+}
+
+// ---------------------------------------------------------------------------------------------
+// Host-only utilities
+// ---------------------------------------------------------------------------------------------
+
+nbvh_status nbvh_build_bvh2_host(const float *v, uint32_t nv, const uint32_t *idx, uint32_t nt, uint32_t *h_nodes,
+                                 uint32_t *n_nodes, uint32_t *h_prims)
+{
+    return guarded_free([&]() {
+        require(v && idx && nv > 0 && nt > 0 && h_nodes && n_nodes && h_prims, NBVH_EINVAL, "bad arguments");
+        for (size_t i = 0; i < 3u * (size_t)nt; i++)
+            require(idx[i] < nv, NBVH_EINVAL, "triangle index out of range");
+        std::vector<float> verts(v, v + 3u * (size_t)nv);
+        std::vector<uint32_t> ind(idx, idx + 3u * (size_t)nt);
+        std::vector<BVHNode> nodes;
+        std::vector<uint32_t> prims;
+        std::string err;
+        if (!build_bvh2(verts, ind, nodes, prims, err))
+            fail(NBVH_EINVAL, err);
+        std::memcpy(h_nodes, nodes.data(), nodes.size() * sizeof(BVHNode));
+        *n_nodes = (uint32_t)nodes.size();
+        std::memcpy(h_prims, prims.data(), prims.size() * sizeof(uint32_t));
+    });
+}
+
+nbvh_status nbvh_build_neural_cut_host(const uint32_t *h_nodes, uint32_t n_nodes, uint32_t max_depth,
+                                       uint32_t *h_neural, uint32_t *n_neural)
+{
+    return guarded_free([&]() {
+        require(h_nodes && n_nodes > 0 && h_neural && n_neural, NBVH_EINVAL, "bad arguments");
+        std::vector<BVHNode> nodes(n_nodes);
+        std::memcpy(nodes.data(), h_nodes, (size_t)n_nodes * sizeof(BVHNode));
+        std::vector<BVHNode> neural;
+        build_neural_cut(nodes, max_depth, neural);
+        require(neural.size() <= *n_neural, NBVH_EINVAL, "neural node buffer too small");
+        std::memcpy(h_neural, neural.data(), neural.size() * sizeof(BVHNode));
+        *n_neural = (uint32_t)neural.size();
+    });
+}
+
+nbvh_status nbvh_param_layout_host(const nbvh_config *cfg, nbvh_param_layout *out)
+{
+    return guarded_free([&]() {
+        require(cfg && out, NBVH_EINVAL, "null argument");
+        validate_config(*cfg);
+        GridParams g;
+        compute_layout(*cfg, *out, g);
+    });
+}
+
+nbvh_status nbvh_init_params_host(const nbvh_config *cfg, float *h_params)
+{
+    return guarded_free([&]() {
+        require(cfg && h_params, NBVH_EINVAL, "null argument");
+        validate_config(*cfg);
+        nbvh_param_layout L;
+        GridParams g;
+        compute_layout(*cfg, L, g);
+        init_params(*cfg, L, h_params);
+    });
+}
+
+nbvh_status nbvh_host_alloc(size_t bytes, void **out)
+{
+    if (!out)
+        return NBVH_EINVAL;
+    *out = nullptr;
+    cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+    if (e == cudaErrorMemoryAllocation)
+        return NBVH_ENOMEM;
+    return e == cudaSuccess ? NBVH_OK : NBVH_EDEVICE;
+}
+
+nbvh_status nbvh_host_free(void *ptr)
+{
+    if (!ptr)
+        return NBVH_OK;
+    return cudaFreeHost(ptr) == cudaSuccess ? NBVH_OK : NBVH_EDEVICE;
+}
+
+} // extern "C"

@@ -1,0 +1,245 @@
+// nbvh_internal.h -- host-side internals of libnbvh (handle, device layouts, kernel launchers).
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/nbvh.h"
+
+namespace nbvh {
+
+constexpr uint32_t kNeuralStackSize = 24;  // NEURAL_STACK_SIZE, include/cuda/neural/accel/neural_bvh.cuh:22
+constexpr uint32_t kClassicStackSize = 32; // CudaBVH2::intersect stack, include/cuda/accel/bvh2.cuh:22
+constexpr uint32_t kNoNeuralChild = 0xFFFFFFFFu;
+constexpr uint32_t kMaxLevels = 32;
+constexpr uint32_t kMaxPoints = 16;
+constexpr uint32_t kOutputs = 8;      // visibility, depth, normal(3), albedo(3)
+constexpr uint32_t kOutputsPadded = 16;
+constexpr uint32_t kNeurons = 64;
+constexpr uint32_t kMaxInputs = 128;
+constexpr uint32_t kMaxHiddenLayers = 8;
+
+// 32-byte BVH2 node in the reference layout (include/base/accel/bvh.h:66-72).
+struct BVHNode {
+    float min[3];
+    uint32_t prim_count;
+    float max[3];
+    uint32_t left_or_prim_offset;
+};
+static_assert(sizeof(BVHNode) == 32, "node layout");
+
+// Hash-grid geometry shared by every kernel (copied into shared memory at kernel start).
+struct GridParams {
+    uint32_t n_levels;
+    uint32_t n_points;
+    uint32_t n_inputs;
+    uint32_t segment_distribution;
+    uint32_t offset[kMaxLevels];
+    uint32_t size[kMaxLevels];
+    uint32_t res[kMaxLevels];
+    uint32_t hashed[kMaxLevels];
+    float scale[kMaxLevels];
+};
+
+// Constants of the neural traversal and decode (NeuralBVHRendererConstants /
+// PathTracingOutputConstants subsets).
+struct NeuralConsts {
+    float inference_mint_epsilon, inference_maxt_epsilon;
+    float learning_mint_epsilon, learning_maxt_epsilon;
+    float sampling_bbox_scaling;
+    float fixed_node_dilation, node_extent_dilation;
+    float leaf_boundary_sampling_ratio;
+    float visibility_threshold; // primary or secondary, chosen per call
+    float depth_epsilon, fixed_depth_epsilon;
+    float fallback_margin;
+    float scene_min[3], scene_max[3];
+    uint32_t bvh_lod;
+    uint32_t max_traversal_steps;
+    uint32_t visibility_only;
+};
+
+struct LossConsts {
+    int32_t visibility_loss, depth_loss, normal_loss, albedo_loss;
+    float visibility_loss_scale, depth_loss_scale, normal_loss_scale, albedo_loss_scale;
+    int32_t normal_linear, albedo_linear, masking, learn_normal, learn_albedo;
+    float loss_scale;
+    float inv_n_total; // 1 / (n * dims)
+};
+
+// Device counters of one query (nbvh_query_stats) plus the work queue head.
+struct QueryCounters {
+    uint32_t queue_head;
+    uint32_t segments;
+    uint32_t step_capped;
+    uint32_t stack_overflow;
+    uint32_t fallback;
+    uint32_t fallback_count; // entries written to the fallback list
+    uint32_t pad[2];
+};
+
+template <typename T>
+struct DeviceBuffer {
+    T *ptr = nullptr;
+    size_t count = 0;
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer &) = delete;
+    DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+    ~DeviceBuffer() { release(); }
+    void release()
+    {
+        if (ptr)
+            cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+    cudaError_t resize(size_t n)
+    {
+        if (n == count && ptr)
+            return cudaSuccess;
+        release();
+        if (n == 0)
+            return cudaSuccess;
+        cudaError_t e = cudaMalloc(&ptr, n * sizeof(T));
+        if (e == cudaSuccess)
+            count = n;
+        else
+            ptr = nullptr;
+        return e;
+    }
+};
+
+} // namespace nbvh
+
+struct nbvh_handle {
+    std::mutex mu;
+    std::string last_error;
+    nbvh_config cfg{};
+    int device = 0;
+
+    // scene (host)
+    std::vector<float> vertices;
+    std::vector<uint32_t> indices;
+    std::vector<float> albedo;
+    std::vector<nbvh::BVHNode> nodes;
+    std::vector<uint32_t> prim_indices;
+    std::vector<nbvh::BVHNode> neural_nodes;
+    std::vector<uint8_t> non_neural;
+    float scene_min[3] = {0, 0, 0}, scene_max[3] = {0, 0, 0};
+    bool classic_built = false, neural_built = false;
+
+    // scene (device)
+    nbvh::DeviceBuffer<float4> d_nodes;        // 2 float4 per node
+    nbvh::DeviceBuffer<float4> d_tris;         // 3 float4 per triangle record (v0|prim, e1, e2)
+    nbvh::DeviceBuffer<float> d_albedo;        // 3 per triangle (original order)
+    nbvh::DeviceBuffer<float4> d_neural_nodes; // 2 float4 per node
+    nbvh::DeviceBuffer<uint8_t> d_non_neural;
+    bool any_non_neural = false;
+
+    // parameters
+    nbvh_param_layout layout{};
+    nbvh::GridParams grid{};
+    std::vector<float> h_params; // FP32 master (host mirror, refreshed on demand)
+    nbvh::DeviceBuffer<float> d_params;   // FP32 master
+    nbvh::DeviceBuffer<__half> d_params_h; // FP16 copy used by the kernels
+    nbvh::DeviceBuffer<float> d_adam_m, d_adam_v;
+    nbvh::DeviceBuffer<float> d_grad;
+    uint32_t training_step = 0;
+
+    // training workspace
+    nbvh::DeviceBuffer<float> d_train_pos, d_train_tgt;
+    nbvh::DeviceBuffer<uint32_t> d_train_nodes;
+    nbvh::DeviceBuffer<__half> d_train_acts; // per row activations of every layer input
+    nbvh::DeviceBuffer<__half> d_train_dz;   // per row pre-activation gradients of every layer
+    nbvh::DeviceBuffer<float> d_loss_sum;
+
+    // query workspace
+    nbvh::DeviceBuffer<nbvh::QueryCounters> d_counters;
+    nbvh::DeviceBuffer<uint32_t> d_fallback_list;
+    nbvh::QueryCounters last_counters{};
+    uint32_t last_rays = 0;
+    float last_kernel_ms = 0.f;
+    uint32_t last_launches = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    // host-buffer query pipeline
+    cudaStream_t pipe_stream[2] = {nullptr, nullptr};
+    void *pinned_in[2] = {nullptr, nullptr};
+    void *pinned_out[2] = {nullptr, nullptr};
+    size_t pinned_chunk = 0;
+    nbvh::DeviceBuffer<uint8_t> d_pipe_in[2], d_pipe_out[2];
+    nbvh::DeviceBuffer<uint32_t> d_pipe_fallback[2];
+
+    int num_sms = 0;
+};
+
+namespace nbvh {
+
+// ---- kernel launchers (defined in the .cu files) ----
+cudaError_t launch_classic(const float4 *nodes, const float4 *tris, const nbvh_ray *rays, uint32_t n,
+                           nbvh_hit *hits, bool any_hit, const uint32_t *ray_list, cudaStream_t s);
+
+// Fallback pass: rays listed in `list` (count read on the device from counters) are answered by
+// the classic BLAS and written into neural hit records.
+cudaError_t launch_classic_fallback(const float4 *nodes, const float4 *tris, const nbvh_ray *rays,
+                                    const uint32_t *list, const QueryCounters *counters,
+                                    uint32_t max_list, nbvh_neural_hit *hits, bool any_hit, int num_sms,
+                                    cudaStream_t s);
+
+cudaError_t launch_classic_as_neural(const float4 *nodes, const float4 *tris, const nbvh_ray *rays,
+                                     uint32_t n, nbvh_neural_hit *hits, bool any_hit, cudaStream_t s);
+
+cudaError_t launch_neural_query(const float4 *neural_nodes, const uint8_t *non_neural, const __half *params_h,
+                                const GridParams &grid, const NeuralConsts &nc, uint32_t n_hidden_layers,
+                                const nbvh_ray *rays, uint32_t n, nbvh_neural_hit *hits, QueryCounters *counters,
+                                uint32_t *fallback_list, int num_sms, cudaStream_t s);
+
+cudaError_t launch_segments(const float4 *neural_nodes, const NeuralConsts &nc, const nbvh_ray *rays, uint32_t n,
+                            uint32_t max_segments, nbvh_segment *segs, uint32_t *counts, cudaStream_t s);
+
+cudaError_t launch_network_inference(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
+                                     const float *positions, uint32_t n, float *outputs, int num_sms,
+                                     cudaStream_t s);
+
+cudaError_t launch_encode(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
+                          const float *positions, uint32_t n, float *features, cudaStream_t s);
+
+cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *nodes, const float4 *tris,
+                                    const float *albedo, const NeuralConsts &nc, const GridParams &grid,
+                                    uint32_t training_step, uint32_t batch_size, uint32_t n, float *positions,
+                                    float *targets, uint32_t *sample_nodes, cudaStream_t s);
+
+// forward + loss + backward: writes per-row activations / gradients for the weight-gradient pass,
+// scatters the grid gradient into grad + n_network_params, accumulates the loss sum.
+cudaError_t launch_train_forward_backward(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
+                                          const LossConsts &lc, const float *positions, const float *targets,
+                                          uint32_t n, __half *acts, __half *dz, float *grad,
+                                          float *loss_sum, int num_sms, cudaStream_t s);
+
+cudaError_t launch_weight_gradients(const GridParams &grid, uint32_t n_hidden_layers, const __half *acts,
+                                    const __half *dz, uint32_t n, float *grad, int num_sms, cudaStream_t s);
+
+cudaError_t launch_scale(float *data, size_t n, float scale, cudaStream_t s);
+
+cudaError_t launch_adam(float *params, __half *params_h, float *m, float *v, const float *grad, uint32_t n,
+                        float lr_t, float beta1, float beta2, float eps, float l2_reg, float grad_scale,
+                        cudaStream_t s);
+
+cudaError_t launch_params_to_half(const float *params, __half *params_h, uint32_t n, cudaStream_t s);
+
+cudaError_t launch_camera_rays(uint32_t width, uint32_t height, uint32_t sample_idx, uint32_t sample_offset,
+                               const float *origin, const float *du, const float *dv, const float *top_left,
+                               nbvh_ray *rays, cudaStream_t s);
+
+// ---- host builders (bvh_builder.cpp) ----
+// Binned-SAH BVH2 with leaves of 1..2 triangles; children of a node are adjacent; returns false
+// when the tree depth exceeds the traversal stack.
+bool build_bvh2(const std::vector<float> &vertices, const std::vector<uint32_t> &indices,
+                std::vector<BVHNode> &nodes, std::vector<uint32_t> &prim_indices, std::string &err);
+void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std::vector<BVHNode> &neural);
+
+} // namespace nbvh

@@ -1,0 +1,216 @@
+// net_device.cuh -- multiresolution hash-grid encoding and the fused MLP, warp-level building
+// blocks shared by the inference and training kernels.
+//
+// The encoding follows the tcnn HashGrid behaviour the reference configures
+// (src/cuda/neural/neural_bvh_module.cu:170-191): per level, position = x * scale + 0.5, trilinear
+// weights over the 8 corners, dense indexing while res^3 fits the level, coherent prime hash
+// (x * 1 ^ y * 2654435761 ^ z * 805459861) otherwise; one grid shared by all segment points
+// (RepeatedComposite), features concatenated point-major then level-major.
+//
+// The MLP is tcnn's FullyFusedMLP shape (64 neurons, ReLU, Sigmoid output, no biases, output
+// padded to 16). Warp tiles of 16 rows are computed with mma.sync m16n8k16 (FP16 in, FP32
+// accumulate); hidden activations never leave registers: the FP32 accumulator fragment of one
+// layer, after ReLU and rounding to FP16, is exactly the A-operand fragment of the next layer.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "device_math.cuh"
+#include "nbvh_internal.h"
+
+namespace nbvh {
+
+constexpr uint32_t kHiddenLd = kNeurons + 8; // padded smem row stride (halves) of 64-wide matrices
+
+// offsets (in halves) of the network matrices inside the padded shared-memory copy
+struct SmemNetLayout {
+    uint32_t ld0;       // n_inputs + 8
+    uint32_t hidden_off; // first 64x64 matrix
+    uint32_t out_off;    // 16x64 output matrix
+    uint32_t total;      // halves
+};
+
+__host__ __device__ inline SmemNetLayout smem_net_layout(uint32_t n_inputs, uint32_t n_hidden_layers)
+{
+    SmemNetLayout L;
+    L.ld0 = n_inputs + 8u;
+    L.hidden_off = kNeurons * L.ld0;
+    L.out_off = L.hidden_off + (n_hidden_layers - 1u) * kNeurons * kHiddenLd;
+    L.total = L.out_off + kOutputsPadded * kHiddenLd;
+    return L;
+}
+
+// Copies the FP16 network matrices (packed [rows][cols], network-first parameter layout) into
+// the padded shared-memory layout. Whole block participates.
+__device__ __forceinline__ void load_weights_to_smem(const __half *__restrict__ w, __half *sw, uint32_t n_inputs,
+                                                     uint32_t n_hidden_layers)
+{
+    SmemNetLayout L = smem_net_layout(n_inputs, n_hidden_layers);
+    const uint32_t *w32 = reinterpret_cast<const uint32_t *>(w);
+    // matrix 0: 64 x n_inputs
+    uint32_t words0 = kNeurons * n_inputs / 2u;
+    for (uint32_t i = threadIdx.x; i < words0; i += blockDim.x) {
+        uint32_t r = (2u * i) / n_inputs, c = (2u * i) % n_inputs;
+        *reinterpret_cast<uint32_t *>(sw + r * L.ld0 + c) = __ldg(w32 + i);
+    }
+    // hidden 64x64 matrices and the 16x64 output matrix
+    uint32_t rows_rest = (n_hidden_layers - 1u) * kNeurons + kOutputsPadded;
+    uint32_t words_rest = rows_rest * kNeurons / 2u;
+    const uint32_t *wr = w32 + words0;
+    for (uint32_t i = threadIdx.x; i < words_rest; i += blockDim.x) {
+        uint32_t r = (2u * i) / kNeurons, c = (2u * i) % kNeurons;
+        *reinterpret_cast<uint32_t *>(sw + L.hidden_off + r * kHiddenLd + c) = __ldg(wr + i);
+    }
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_half2(float lo, float hi)
+{
+    __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+__device__ __forceinline__ float2 unpack_half2(uint32_t u)
+{
+    __half2 h = *reinterpret_cast<__half2 *>(&u);
+    return __half22float2(h);
+}
+
+// Features of one point at one level: 2 values, FMA accumulation over corners c = 0..7 (bit d of
+// c selects the upper corner along axis d), identical operation order to the CPU restatement.
+__device__ __forceinline__ float2 encode_level(const uint32_t *__restrict__ table, const GridParams &gp, uint32_t l,
+                                               V3 p)
+{
+    const float s = gp.scale[l];
+    const float px = __fmaf_rn(p.x, s, 0.5f), py = __fmaf_rn(p.y, s, 0.5f), pz = __fmaf_rn(p.z, s, 0.5f);
+    const float flx = floorf(px), fly = floorf(py), flz = floorf(pz);
+    const uint32_t gx = (uint32_t)(int32_t)flx, gy = (uint32_t)(int32_t)fly, gz = (uint32_t)(int32_t)flz;
+    const float rx = __fsub_rn(px, flx), ry = __fsub_rn(py, fly), rz = __fsub_rn(pz, flz);
+    const uint32_t res = gp.res[l], size = gp.size[l], off = gp.offset[l];
+    const bool hashed = gp.hashed[l] != 0u;
+    uint32_t v[8];
+#pragma unroll
+    for (uint32_t c = 0; c < 8; c++) {
+        uint32_t x = gx + (c & 1u), y = gy + ((c >> 1) & 1u), z = gz + ((c >> 2) & 1u);
+        uint32_t idx;
+        if (hashed) {
+            idx = (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (size - 1u);
+        } else {
+            idx = x + y * res + z * res * res;
+            if (idx >= size)
+                idx %= size;
+        }
+        v[c] = __ldg(table + off + idx);
+    }
+    const float wx0 = __fsub_rn(1.0f, rx), wy0 = __fsub_rn(1.0f, ry), wz0 = __fsub_rn(1.0f, rz);
+    float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+    for (uint32_t c = 0; c < 8; c++) {
+        float w = __fmul_rn(__fmul_rn((c & 1u) ? rx : wx0, (c & 2u) ? ry : wy0), (c & 4u) ? rz : wz0);
+        float2 f = unpack_half2(v[c]);
+        a0 = __fmaf_rn(w, f.x, a0);
+        a1 = __fmaf_rn(w, f.y, a1);
+    }
+    return make_float2(a0, a1);
+}
+
+// Rebuilds the FP16 A fragments of the next layer from the FP32 accumulators (after ReLU).
+__device__ __forceinline__ void relu_pack(const float (&acc)[8][4], uint32_t (&a)[4][4])
+{
+#pragma unroll
+    for (int kb = 0; kb < 4; kb++) {
+        a[kb][0] = pack_half2(fmaxf(acc[2 * kb][0], 0.f), fmaxf(acc[2 * kb][1], 0.f));
+        a[kb][1] = pack_half2(fmaxf(acc[2 * kb][2], 0.f), fmaxf(acc[2 * kb][3], 0.f));
+        a[kb][2] = pack_half2(fmaxf(acc[2 * kb + 1][0], 0.f), fmaxf(acc[2 * kb + 1][1], 0.f));
+        a[kb][3] = pack_half2(fmaxf(acc[2 * kb + 1][2], 0.f), fmaxf(acc[2 * kb + 1][3], 0.f));
+    }
+}
+
+// Forward of one 16-row tile. make_a(kb, a) fills the layer-0 A fragment of k-block kb (16
+// inputs). On return o[0..1] are the sigmoid outputs (row g, cols 2*tig, 2*tig+1) and o[2..3]
+// those of row g + 8 (g = lane / 4, tig = lane % 4), for output columns 0..7.
+template <typename AMaker>
+__device__ __forceinline__ void mlp_forward_tile(const __half *sw, uint32_t n_inputs, uint32_t n_hidden_layers,
+                                                 AMaker &&make_a, float (&o)[4])
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+    const SmemNetLayout L = smem_net_layout(n_inputs, n_hidden_layers);
+    float acc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++)
+        acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+    const uint32_t nkb = n_inputs / 16u;
+    for (uint32_t kb = 0; kb < nkb; kb++) {
+        uint32_t a[4];
+        make_a(kb, a);
+        const __half *wrow = sw + g * L.ld0 + kb * 16u + tig * 2;
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+            uint32_t b0 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * L.ld0);
+            uint32_t b1 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * L.ld0 + 8);
+            mma16816(acc[nt], a, b0, b1);
+        }
+    }
+    const __half *wl = sw + L.hidden_off;
+    for (uint32_t layer = 1; layer < n_hidden_layers; layer++) {
+        uint32_t a[4][4];
+        relu_pack(acc, a);
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++)
+            acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+#pragma unroll
+        for (int kb = 0; kb < 4; kb++) {
+            const __half *wrow = wl + g * kHiddenLd + kb * 16 + tig * 2;
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) {
+                uint32_t b0 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * kHiddenLd);
+                uint32_t b1 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * kHiddenLd + 8);
+                mma16816(acc[nt], a[kb], b0, b1);
+            }
+        }
+        wl += kNeurons * kHiddenLd;
+    }
+    uint32_t a[4][4];
+    relu_pack(acc, a);
+    float oc[4] = {0.f, 0.f, 0.f, 0.f};
+    const __half *wo = sw + L.out_off + g * kHiddenLd + tig * 2;
+#pragma unroll
+    for (int kb = 0; kb < 4; kb++) {
+        uint32_t b0 = *reinterpret_cast<const uint32_t *>(wo + kb * 16);
+        uint32_t b1 = *reinterpret_cast<const uint32_t *>(wo + kb * 16 + 8);
+        mma16816(oc, a[kb], b0, b1);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        o[i] = 1.0f / (1.0f + expf(-oc[i]));
+}
+
+// Encoded segment points along [po, pi] (neural_bvh_module_kernels.cu:57-96).
+__device__ __forceinline__ float segment_t(uint32_t k, uint32_t n_points, uint32_t distribution, uint32_t &rng)
+{
+    if (distribution == NBVH_SEGMENT_UNIFORM)
+        return lcg_randomf(rng);
+    float delta, offset;
+    if (distribution == NBVH_SEGMENT_EQUIDISTANT_EXTERIOR) {
+        delta = n_points == 1u ? 1.0f : __fdiv_rn(1.0f, (float)(n_points - 1u));
+        offset = 0.0f;
+    } else {
+        delta = __fdiv_rn(1.0f, (float)n_points);
+        offset = 0.5f;
+    }
+    return __fmul_rn(delta, __fadd_rn((float)k, offset));
+}
+
+__device__ __forceinline__ V3 segment_point(V3 epo, V3 epi, float t)
+{
+    return add3(scale3(epo, __fsub_rn(1.0f, t)), scale3(epi, t));
+}
+
+} // namespace nbvh

@@ -1,0 +1,278 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes bindings of the CPU oracle (oracle/nbvh_oracle.c).
+
+Imported by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg; never by the
+product. Parity status of the oracle: unpinned (see nbvh_oracle.h).
+"""
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "nbvh_oracle.c")
+LIB = os.path.join(HERE, "liboracle.so")
+FLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=c11"]
+
+
+def build(force=False):
+    """Compiles the oracle with gcc (no FMA contraction, no fast math)."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "nbvh_oracle.h"))):
+        return LIB
+    subprocess.run(["gcc"] + FLAGS + ["-o", LIB, SRC, "-lm", "-lpthread"], check=True)
+    return LIB
+
+
+class ClassicScene(C.Structure):
+    _fields_ = [("nodes", C.c_void_p), ("n_nodes", C.c_uint32), ("prim_indices", C.c_void_p),
+                ("vertices", C.c_void_p), ("indices", C.c_void_p), ("n_triangles", C.c_uint32)]
+
+
+class NeuralConsts(C.Structure):
+    _fields_ = [("inference_mint_epsilon", C.c_float), ("inference_maxt_epsilon", C.c_float),
+                ("learning_mint_epsilon", C.c_float), ("learning_maxt_epsilon", C.c_float),
+                ("sampling_bbox_scaling", C.c_float), ("fixed_node_dilation", C.c_float),
+                ("node_extent_dilation", C.c_float), ("leaf_boundary_sampling_ratio", C.c_float),
+                ("primary_visibility_threshold", C.c_float), ("secondary_visibility_threshold", C.c_float),
+                ("depth_epsilon", C.c_float), ("fixed_depth_epsilon", C.c_float),
+                ("input_segment_points", C.c_int32), ("segment_distribution", C.c_int32),
+                ("bvh_lod", C.c_uint32), ("max_traversal_steps", C.c_uint32)]
+
+
+class Network(C.Structure):
+    _fields_ = [("n_levels", C.c_uint32), ("n_points", C.c_uint32), ("n_inputs", C.c_uint32),
+                ("n_neurons", C.c_uint32), ("n_hidden_layers", C.c_uint32), ("level_offset", C.c_void_p),
+                ("level_size", C.c_void_p), ("level_resolution", C.c_void_p), ("level_scale", C.c_void_p),
+                ("grid_f16", C.c_void_p), ("weights_f16", C.c_void_p), ("exact", C.c_int32),
+                ("grid_f32", C.c_void_p), ("weights_f32", C.c_void_p)]
+
+
+class NeuralScene(C.Structure):
+    _fields_ = [("neural_nodes", C.c_void_p), ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3),
+                ("non_neural", C.c_void_p)]
+
+
+class LossConsts(C.Structure):
+    _fields_ = [("visibility_loss", C.c_int32), ("depth_loss", C.c_int32), ("normal_loss", C.c_int32),
+                ("albedo_loss", C.c_int32), ("visibility_loss_scale", C.c_float), ("depth_loss_scale", C.c_float),
+                ("normal_loss_scale", C.c_float), ("albedo_loss_scale", C.c_float),
+                ("output_normal_linear_activation", C.c_int32), ("output_albedo_linear_activation", C.c_int32),
+                ("visibility_masking_loss", C.c_int32), ("learn_normal", C.c_int32), ("learn_albedo", C.c_int32)]
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """Owns the oracle library plus the arrays referenced by the structs handed to it."""
+
+    def __init__(self, path=None):
+        self.lib = C.CDLL(path or build())
+        L = self.lib
+        L.orc_murmur_mix.restype = C.c_uint32
+        L.orc_murmur_mix.argtypes = [C.c_uint32, C.c_uint32]
+        L.orc_murmur_finalize.restype = C.c_uint32
+        L.orc_murmur_finalize.argtypes = [C.c_uint32]
+        L.orc_lcg_seed.restype = C.c_uint32
+        L.orc_lcg_seed.argtypes = [C.c_uint32] * 3
+        L.orc_lcg_randomf.restype = C.c_float
+        L.orc_lcg_randomf.argtypes = [C.POINTER(C.c_uint32)]
+        L.orc_sincos_turns.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.orc_f32_to_f16.restype = C.c_uint16
+        L.orc_f32_to_f16.argtypes = [C.c_float]
+        L.orc_f16_to_f32.restype = C.c_float
+        L.orc_f16_to_f32.argtypes = [C.c_uint16]
+        self._keep = []
+
+    # ---- RNG ----
+    def lcg_seed(self, index, frame, linear):
+        return self.lib.orc_lcg_seed(index, frame, linear)
+
+    def lcg_stream(self, index, frame, linear, n):
+        s = C.c_uint32(self.lcg_seed(index, frame, linear))
+        return np.array([self.lib.orc_lcg_randomf(C.byref(s)) for _ in range(n)], np.float32)
+
+    def sincos_turns(self, u):
+        s, c = C.c_float(), C.c_float()
+        self.lib.orc_sincos_turns(u, C.byref(s), C.byref(c))
+        return s.value, c.value
+
+    # ---- scenes ----
+    def classic_scene(self, nodes, prims, vertices, indices):
+        nodes = np.ascontiguousarray(nodes, np.uint32)
+        prims = np.ascontiguousarray(prims, np.uint32)
+        v = np.ascontiguousarray(vertices, np.float32)
+        t = np.ascontiguousarray(indices, np.uint32)
+        self._keep += [nodes, prims, v, t]
+        return ClassicScene(_p(nodes).value, len(nodes), _p(prims).value, _p(v).value, _p(t).value, len(t))
+
+    def neural_scene(self, neural_nodes, bbox, non_neural=None):
+        nn = np.ascontiguousarray(neural_nodes, np.uint32)
+        self._keep.append(nn)
+        s = NeuralScene()
+        s.neural_nodes = _p(nn).value
+        for k in range(3):
+            s.scene_min[k] = float(bbox[k])
+            s.scene_max[k] = float(bbox[3 + k])
+        if non_neural is not None:
+            f = np.ascontiguousarray(non_neural, np.uint8)
+            self._keep.append(f)
+            s.non_neural = _p(f).value
+        return s
+
+    @staticmethod
+    def neural_consts(cfg):
+        c = NeuralConsts()
+        for k in ("inference_mint_epsilon", "inference_maxt_epsilon", "learning_mint_epsilon",
+                  "learning_maxt_epsilon", "sampling_bbox_scaling", "fixed_node_dilation", "node_extent_dilation",
+                  "leaf_boundary_sampling_ratio"):
+            setattr(c, k, getattr(cfg.bvh, k))
+        for k in ("primary_visibility_threshold", "secondary_visibility_threshold", "depth_epsilon",
+                  "fixed_depth_epsilon"):
+            setattr(c, k, getattr(cfg.output, k))
+        c.input_segment_points = cfg.module.input_segment_points
+        c.segment_distribution = cfg.module.segment_distribution
+        c.bvh_lod = 0
+        c.max_traversal_steps = cfg.max_traversal_steps
+        return c
+
+    @staticmethod
+    def loss_consts(cfg):
+        lc = LossConsts()
+        o = cfg.output
+        for k in ("visibility_loss", "depth_loss", "normal_loss", "albedo_loss", "visibility_loss_scale",
+                  "depth_loss_scale", "normal_loss_scale", "albedo_loss_scale", "output_normal_linear_activation",
+                  "output_albedo_linear_activation", "visibility_masking_loss", "learn_normal", "learn_albedo"):
+            setattr(lc, k, getattr(o, k))
+        return lc
+
+    def network(self, cfg, layout, params, exact=False):
+        """Network struct over FP32 parameters (rounded to FP16 unless exact)."""
+        params = np.ascontiguousarray(params, np.float32)
+        nl = layout.n_levels
+        off = np.array(layout.level_offset[:nl], np.uint32)
+        size = np.array(layout.level_size[:nl], np.uint32)
+        res = np.array(layout.level_resolution[:nl], np.uint32)
+        scale = np.array(layout.level_scale[:nl], np.float32)
+        nnet = layout.n_network_params
+        w32 = np.ascontiguousarray(params[:nnet])
+        g32 = np.ascontiguousarray(params[nnet:])
+        w16 = w32.astype(np.float16).view(np.uint16)
+        g16 = g32.astype(np.float16).view(np.uint16)
+        self._keep += [off, size, res, scale, w32, g32, w16, g16]
+        net = Network()
+        net.n_levels = nl
+        net.n_points = cfg.module.input_segment_points
+        net.n_inputs = layout.n_inputs
+        net.n_neurons = cfg.network.n_neurons
+        net.n_hidden_layers = cfg.network.n_hidden_layers
+        net.level_offset, net.level_size = _p(off).value, _p(size).value
+        net.level_resolution, net.level_scale = _p(res).value, _p(scale).value
+        net.grid_f16, net.weights_f16 = _p(g16).value, _p(w16).value
+        net.exact = 1 if exact else 0
+        net.grid_f32, net.weights_f32 = _p(g32).value, _p(w32).value
+        return net
+
+    # ---- queries ----
+    def classic_query(self, scene, rays, any_hit=False, threads=1, stats=False):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = len(rays)
+        hits = np.empty((n, 4), np.uint32)
+        st = np.empty((n, 2), np.uint32) if stats else None
+        self.lib.orc_classic_query(C.byref(scene), _p(rays), C.c_uint32(n), C.c_int(int(any_hit)), _p(hits), _p(st),
+                                   C.c_int(threads))
+        return (hits, st) if stats else hits
+
+    def fp64_closest(self, scene, rays):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = len(rays)
+        t = np.empty(n, np.float64)
+        prim = np.empty(n, np.uint32)
+        self.lib.orc_fp64_closest(C.byref(scene), _p(rays), C.c_uint32(n), _p(t), _p(prim))
+        return t, prim
+
+    def neural_segments(self, neural_nodes, consts, rays, max_segments):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        nn = np.ascontiguousarray(neural_nodes, np.uint32)
+        n = len(rays)
+        segs = np.zeros((n, max_segments, 4), np.uint32)
+        counts = np.empty(n, np.uint32)
+        self.lib.orc_neural_segments(_p(nn), C.byref(consts), _p(rays), C.c_uint32(n), C.c_uint32(max_segments),
+                                     _p(segs), _p(counts))
+        return segs, counts
+
+    def encode(self, net, positions):
+        pos = np.ascontiguousarray(positions, np.float32)
+        n = pos.shape[0]
+        out = np.empty((n, net.n_inputs), np.float32)
+        self.lib.orc_encode(C.byref(net), _p(pos), C.c_uint32(n), _p(out))
+        return out
+
+    def network_inference(self, net, positions, threads=1):
+        pos = np.ascontiguousarray(positions, np.float32)
+        n = pos.shape[0]
+        out = np.empty((n, 16), np.float32)
+        self.lib.orc_network_inference(C.byref(net), _p(pos), C.c_uint32(n), _p(out), C.c_int(threads))
+        return out
+
+    def neural_query(self, nscene, net, consts, rays, depth=1, visibility_only=False, classic=None,
+                     fallback_margin=0.0, threads=1):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = len(rays)
+        hits = np.empty((n, 12), np.uint32)
+        self.lib.orc_neural_query(C.byref(nscene), C.byref(net), C.byref(consts),
+                                  C.byref(classic) if classic is not None else None, C.c_float(fallback_margin),
+                                  _p(rays), C.c_uint32(n), C.c_uint32(depth), C.c_int(int(visibility_only)),
+                                  _p(hits), C.c_int(threads))
+        return hits
+
+    def training_batch(self, nscene, cscene, albedo, consts, training_step, batch_size, n):
+        P = consts.input_segment_points
+        pos = np.empty((n, P, 3), np.float32)
+        tgt = np.empty((n, 8), np.float32)
+        nodes = np.empty(n, np.uint32)
+        alb = None if albedo is None else np.ascontiguousarray(albedo, np.float32)
+        self.lib.orc_generate_training_batch(C.byref(nscene), C.byref(cscene), _p(alb), C.byref(consts),
+                                             C.c_uint32(training_step), C.c_uint32(batch_size), C.c_uint32(n),
+                                             _p(pos), _p(tgt), _p(nodes))
+        return pos, tgt, nodes
+
+    def composite_loss(self, lc, predictions, targets, loss_scale=1.0):
+        pred = np.ascontiguousarray(predictions, np.float32).reshape(-1, 16)
+        tgt = np.ascontiguousarray(targets, np.float32).reshape(-1, 8)
+        n = len(pred)
+        vals = np.empty((n, 16), np.float32)
+        grads = np.empty((n, 16), np.float32)
+        self.lib.orc_composite_loss(C.byref(lc), _p(pred), _p(tgt), C.c_uint32(n), C.c_float(loss_scale), _p(vals),
+                                    _p(grads))
+        return vals, grads
+
+    def compute_gradients(self, net, lc, positions, targets, n_params, loss_scale=128.0, fp16_backward=True):
+        pos = np.ascontiguousarray(positions, np.float32)
+        tgt = np.ascontiguousarray(targets, np.float32)
+        g = np.empty(n_params, np.float64)
+        loss = C.c_double(0)
+        self.lib.orc_compute_gradients(C.byref(net), C.byref(lc), _p(pos), _p(tgt), C.c_uint32(len(pos)),
+                                       C.c_float(loss_scale), _p(g), C.byref(loss), C.c_int(int(fp16_backward)))
+        return g, loss.value
+
+    def adam_step(self, params, m, v, grad, step, cfg):
+        o = cfg.optimizer
+        self.lib.orc_adam_step(_p(params), _p(m), _p(v), _p(np.ascontiguousarray(grad, np.float32)),
+                               C.c_uint32(len(params)), C.c_uint32(step), C.c_float(o.learning_rate),
+                               C.c_float(o.beta1), C.c_float(o.beta2), C.c_float(o.epsilon), C.c_float(o.l2_reg),
+                               C.c_int32(o.decay_start), C.c_int32(o.decay_interval), C.c_float(o.decay_base))
+
+    def camera_rays(self, req):
+        n = req.width * req.height
+        rays = np.empty((n, 8), np.float32)
+        o = np.array(req.origin[:], np.float32)
+        t = np.array(req.target[:], np.float32)
+        u = np.array(req.up[:], np.float32)
+        self.lib.orc_camera_rays(C.c_uint32(req.width), C.c_uint32(req.height), C.c_uint32(req.sample_idx),
+                                 C.c_uint32(req.sample_offset), _p(o), _p(t), _p(u), C.c_float(req.yfov_degrees),
+                                 _p(rays))
+        return rays

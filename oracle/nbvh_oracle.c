@@ -1,0 +1,1384 @@
+/*
+ * nbvh_oracle.c -- TEST INFRASTRUCTURE ONLY (see nbvh_oracle.h).
+ *
+ * CPU restatement of the reference's N-BVH ray-query path. Each function cites the reference
+ * file:line it follows (paths relative to the reference project root). Parity: UNPINNED -- the
+ * reference has no golden vectors and cannot be built here; see nbvh_oracle.h.
+ *
+ * Compile with -ffp-contract=off -fno-fast-math: every FP32 operation below is rounded on its
+ * own, in the order written, which is the order glm evaluates the reference expressions in
+ * (dot = (x*x' + y*y') + z*z', cross = (a.y*b.z - b.y*a.z, ...), min(a,b) = b < a ? b : a,
+ * max(a,b) = a < b ? b : a, normalize(v) = v * (1 / sqrt(dot(v, v)))).
+ */
+#include "nbvh_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------------------------ */
+/* glm-semantics FP32 vector helpers                                                          */
+/* ------------------------------------------------------------------------------------------ */
+
+typedef struct {
+    float x, y, z;
+} v3;
+
+static inline v3 mk(float x, float y, float z)
+{
+    v3 r = {x, y, z};
+    return r;
+}
+static inline v3 vadd(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 vsub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 vmul(v3 a, v3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline v3 vdiv(v3 a, v3 b) { return mk(a.x / b.x, a.y / b.y, a.z / b.z); }
+static inline v3 vscale(v3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+static inline v3 vadds(v3 a, float s) { return mk(a.x + s, a.y + s, a.z + s); }
+static inline float vdot(v3 a, v3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+static inline v3 vcross(v3 a, v3 b)
+{
+    return mk(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+static inline float gmin(float a, float b) { return (b < a) ? b : a; }
+static inline float gmax(float a, float b) { return (a < b) ? b : a; }
+static inline v3 vmin(v3 a, v3 b) { return mk(gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z)); }
+static inline v3 vmax(v3 a, v3 b) { return mk(gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z)); }
+static inline float cmax(v3 v) { return gmax(gmax(v.x, v.y), v.z); } /* common.cuh:38-41 */
+static inline float cmin(v3 v) { return gmin(gmin(v.x, v.y), v.z); } /* common.cuh:43-46 */
+static inline v3 vnormalize(v3 v) { return vscale(v, 1.0f / sqrtf(vdot(v, v))); }
+static inline float vlength(v3 v) { return sqrtf(vdot(v, v)); }
+static inline float gclamp01(float x) { return gmin(gmax(x, 0.0f), 1.0f); }
+
+static inline v3 load3(const float *p) { return mk(p[0], p[1], p[2]); }
+static inline float u2f(uint32_t u)
+{
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+static inline uint32_t f2u(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* RNG: include/cuda/utils/lcg_rng.cuh                                                        */
+/* ------------------------------------------------------------------------------------------ */
+
+uint32_t orc_murmur_mix(uint32_t hash, uint32_t k) /* lcg_rng.cuh:12-29 */
+{
+    k *= 0xcc9e2d51u;
+    k = (k << 15) | (k >> 17);
+    k *= 0x1b873593u;
+    hash ^= k;
+    hash = ((hash << 13) | (hash >> 19)) * 5u + 0xe6546b64u;
+    return hash;
+}
+
+uint32_t orc_murmur_finalize(uint32_t hash) /* lcg_rng.cuh:31-40 */
+{
+    hash ^= hash >> 16;
+    hash *= 0x85ebca6bu;
+    hash ^= hash >> 13;
+    hash *= 0xc2b2ae35u;
+    hash ^= hash >> 16;
+    return hash;
+}
+
+uint32_t orc_lcg_seed(uint32_t index, uint32_t frame, uint32_t linear) /* lcg_rng.cuh:65-72 */
+{
+    uint32_t s = orc_murmur_mix(0u, linear);
+    s = orc_murmur_mix(s, 512u * frame + index);
+    return orc_murmur_finalize(s);
+}
+
+float orc_lcg_randomf(uint32_t *state) /* lcg_rng.cuh:42-53: ldexp((float)u32, -32) */
+{
+    *state = *state * 1664525u + 1013904223u;
+    return (float)(*state) * 0x1p-32f;
+}
+
+/* sin(2 pi u), cos(2 pi u): octant reduction on u (exact in FP32), then Taylor series of degree
+ * 11 (sin) and 12 (cos) on [0, pi/4] evaluated with fused multiply-adds. The reference calls
+ * sin/cos of 2*PI*u (sampling.cuh:8-14); this is a deterministic replacement that the device code
+ * evaluates with the same operations, so oracle and GPU agree bit for bit. */
+void orc_sincos_turns(float u, float *s, float *c)
+{
+    float y = u * 8.0f;
+    float o = floorf(y);
+    float f = y - o;
+    int oct = ((int)o) & 7;
+    float g = (oct & 1) ? (1.0f - f) : f;
+    float x = g * 0.785398163397448310f;
+    float x2 = x * x;
+    float ps = fmaf(x2, -2.50521084e-08f, 2.75573192e-06f);
+    ps = fmaf(x2, ps, -1.98412698e-04f);
+    ps = fmaf(x2, ps, 8.33333333e-03f);
+    ps = fmaf(x2, ps, -1.66666667e-01f);
+    ps = fmaf(x2, ps, 1.0f);
+    float sn = x * ps;
+    float pc = fmaf(x2, 2.08767570e-09f, -2.75573192e-07f);
+    pc = fmaf(x2, pc, 2.48015873e-05f);
+    pc = fmaf(x2, pc, -1.38888889e-03f);
+    pc = fmaf(x2, pc, 4.16666667e-02f);
+    pc = fmaf(x2, pc, -0.5f);
+    float cs = fmaf(x2, pc, 1.0f);
+    float rs, rc;
+    switch (oct) {
+    case 0: rs = sn; rc = cs; break;
+    case 1: rs = cs; rc = sn; break;
+    case 2: rs = cs; rc = -sn; break;
+    case 3: rs = sn; rc = -cs; break;
+    case 4: rs = -sn; rc = -cs; break;
+    case 5: rs = -cs; rc = -sn; break;
+    case 6: rs = -cs; rc = sn; break;
+    default: rs = -sn; rc = cs; break;
+    }
+    *s = rs;
+    *c = rc;
+}
+
+/* square_to_uniform_sphere, include/cuda/utils/sampling.cuh:8-14 */
+static v3 uniform_sphere(float sx, float sy)
+{
+    float sp, cp;
+    orc_sincos_turns(sx, &sp, &cp);
+    float cos_theta = sy * 2.0f - 1.0f;
+    float sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+    return mk(sin_theta * cp, sin_theta * sp, cos_theta);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Classic BVH2: include/base/accel/bvh.h:66-154, include/cuda/accel/bvh.cuh:98-136,           */
+/* include/cuda/accel/bvh2.cuh:12-88                                                           */
+/* ------------------------------------------------------------------------------------------ */
+
+typedef struct {
+    v3 o;
+    float mint;
+    v3 d;
+    float maxt;
+} ray3;
+
+static inline ray3 load_ray(const float *r)
+{
+    ray3 ray;
+    ray.o = load3(r);
+    ray.mint = r[3];
+    ray.d = load3(r + 4);
+    ray.maxt = r[7];
+    return ray;
+}
+
+static inline v3 node_min(const uint32_t *node) { return mk(u2f(node[0]), u2f(node[1]), u2f(node[2])); }
+static inline v3 node_max(const uint32_t *node) { return mk(u2f(node[4]), u2f(node[5]), u2f(node[6])); }
+
+/* BVH2Node::intersect, bvh.h:121-133: entry distance inside (ray.mint, ray.maxt) or FLT_MAX */
+static inline float box_entry(v3 bmin, v3 bmax, const ray3 *ray)
+{
+    v3 t0 = vdiv(vsub(bmin, ray->o), ray->d);
+    v3 t1 = vdiv(vsub(bmax, ray->o), ray->d);
+    v3 ts = vmin(t0, t1);
+    v3 tb = vmax(t0, t1);
+    float mint = gmax(ray->mint, cmax(ts));
+    float maxt = gmin(ray->maxt, cmin(tb));
+    return (mint <= maxt) ? mint : FLT_MAX;
+}
+
+/* BaseCudaBLAS::intersect_triangle, bvh.cuh:98-136 (Moller-Trumbore). Returns 1 on hit. */
+static inline int tri_intersect(const orc_classic_scene *s, const ray3 *ray, uint32_t prim, float *t_out,
+                                float *u_out, float *v_out)
+{
+    const uint32_t *ix = s->indices + 3u * prim;
+    v3 v0 = load3(s->vertices + 3u * ix[0]);
+    v3 v1 = load3(s->vertices + 3u * ix[1]);
+    v3 v2 = load3(s->vertices + 3u * ix[2]);
+    v3 e1 = vsub(v1, v0);
+    v3 e2 = vsub(v2, v0);
+    v3 pvec = vcross(ray->d, e2);
+    float det = vdot(e1, pvec);
+    if (det > -1e-8f && det < 1e-8f)
+        return 0;
+    float inv_det = 1.0f / det;
+    v3 tvec = vsub(ray->o, v0);
+    float u = vdot(tvec, pvec) * inv_det;
+    if (u < 0.0f || u > 1.0f)
+        return 0;
+    v3 qvec = vcross(tvec, e1);
+    float v = vdot(ray->d, qvec) * inv_det;
+    if (v < 0.0f || (u + v) > 1.0f)
+        return 0;
+    float t = vdot(e2, qvec) * inv_det;
+    if (t < ray->mint || t >= ray->maxt)
+        return 0;
+    *t_out = t;
+    *u_out = u;
+    *v_out = v;
+    return 1;
+}
+
+/* CudaBVH2::intersect<ShadowRay>, bvh2.cuh:12-88. Fills t,u,v,prim (prim = UINT32_MAX on miss). */
+static void classic_intersect(const orc_classic_scene *s, ray3 ray, int any_hit, float *t_o, float *u_o,
+                              float *v_o, uint32_t *prim_o, uint32_t *boxes, uint32_t *tris)
+{
+    float best_t = FLT_MAX, best_u = 0.f, best_v = 0.f;
+    uint32_t best_prim = 0xFFFFFFFFu;
+    uint32_t stack[32];
+    int sp = 0;
+    uint32_t node_idx = 0;
+    uint32_t nb = 0, nt = 0;
+    for (;;) {
+        const uint32_t *node = s->nodes + 8u * node_idx;
+        if (node[3] > 0u) { /* leaf */
+            uint32_t start = node[7], end = node[7] + node[3];
+            int done = 0;
+            for (uint32_t pid = start; pid < end; pid++) {
+                uint32_t prim = s->prim_indices[pid];
+                float t, u, v;
+                nt++;
+                if (tri_intersect(s, &ray, prim, &t, &u, &v) && t < ray.maxt) {
+                    best_t = t;
+                    best_u = u;
+                    best_v = v;
+                    best_prim = prim;
+                    if (any_hit) {
+                        done = 1;
+                        break;
+                    }
+                    ray.maxt = t;
+                }
+            }
+            if (done || sp == 0)
+                break;
+            node_idx = stack[--sp];
+            continue;
+        }
+        uint32_t c1 = node[7], c2 = node[7] + 1u;
+        const uint32_t *n1 = s->nodes + 8u * c1;
+        const uint32_t *n2 = s->nodes + 8u * c2;
+        float d1 = box_entry(node_min(n1), node_max(n1), &ray);
+        float d2 = box_entry(node_min(n2), node_max(n2), &ray);
+        nb += 2;
+        if (d1 > d2) {
+            float td = d1;
+            d1 = d2;
+            d2 = td;
+            uint32_t tc = c1;
+            c1 = c2;
+            c2 = tc;
+        }
+        if (d1 == FLT_MAX) {
+            if (sp == 0)
+                break;
+            node_idx = stack[--sp];
+        } else {
+            node_idx = c1;
+            if (d2 != FLT_MAX)
+                stack[sp++] = c2; /* depth of the build is below 32 (checked by the builder) */
+        }
+    }
+    *t_o = best_t;
+    *u_o = best_u;
+    *v_o = best_v;
+    *prim_o = best_prim;
+    if (boxes)
+        *boxes = nb;
+    if (tris)
+        *tris = nt;
+}
+
+typedef struct {
+    const orc_classic_scene *scene;
+    const float *rays;
+    uint32_t begin, end;
+    int any_hit;
+    uint32_t *hits;
+    uint32_t *stats;
+} classic_job;
+
+static void *classic_worker(void *arg)
+{
+    classic_job *j = (classic_job *)arg;
+    for (uint32_t i = j->begin; i < j->end; i++) {
+        float t, u, v;
+        uint32_t prim, nb, nt;
+        classic_intersect(j->scene, load_ray(j->rays + 8u * i), j->any_hit, &t, &u, &v, &prim, &nb, &nt);
+        j->hits[4u * i + 0] = f2u(t);
+        j->hits[4u * i + 1] = f2u(u);
+        j->hits[4u * i + 2] = f2u(v);
+        j->hits[4u * i + 3] = prim;
+        if (j->stats) {
+            j->stats[2u * i] = nb;
+            j->stats[2u * i + 1] = nt;
+        }
+    }
+    return NULL;
+}
+
+void orc_classic_query(const orc_classic_scene *scene, const float *rays, uint32_t n, int any_hit,
+                       uint32_t *hits, uint32_t *stats, int n_threads)
+{
+    if (n_threads < 1)
+        n_threads = 1;
+    if (n_threads > 256)
+        n_threads = 256;
+    pthread_t th[256];
+    classic_job jobs[256];
+    uint32_t chunk = (n + (uint32_t)n_threads - 1u) / (uint32_t)n_threads;
+    for (int k = 0; k < n_threads; k++) {
+        uint32_t b = (uint32_t)k * chunk, e = b + chunk;
+        if (b > n)
+            b = n;
+        if (e > n)
+            e = n;
+        jobs[k] = (classic_job){scene, rays, b, e, any_hit, hits, stats};
+        if (n_threads == 1)
+            classic_worker(&jobs[k]);
+        else
+            pthread_create(&th[k], NULL, classic_worker, &jobs[k]);
+    }
+    if (n_threads > 1)
+        for (int k = 0; k < n_threads; k++)
+            pthread_join(th[k], NULL);
+}
+
+void orc_fp64_closest(const orc_classic_scene *s, const float *rays, uint32_t n, double *t_out,
+                      uint32_t *prim_out)
+{
+    for (uint32_t i = 0; i < n; i++) {
+        const float *r = rays + 8u * i;
+        double o[3] = {r[0], r[1], r[2]}, d[3] = {r[4], r[5], r[6]};
+        double tmin = r[3], tmax = r[7];
+        double best = 1e300;
+        uint32_t bp = 0xFFFFFFFFu;
+        for (uint32_t p = 0; p < s->n_triangles; p++) {
+            const uint32_t *ix = s->indices + 3u * p;
+            double v0[3], e1[3], e2[3];
+            for (int k = 0; k < 3; k++) {
+                v0[k] = s->vertices[3u * ix[0] + k];
+                e1[k] = s->vertices[3u * ix[1] + k] - v0[k];
+                e2[k] = s->vertices[3u * ix[2] + k] - v0[k];
+            }
+            double pv[3] = {d[1] * e2[2] - e2[1] * d[2], d[2] * e2[0] - e2[2] * d[0], d[0] * e2[1] - e2[0] * d[1]};
+            double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
+            if (det == 0.0)
+                continue;
+            double tv[3] = {o[0] - v0[0], o[1] - v0[1], o[2] - v0[2]};
+            double u = (tv[0] * pv[0] + tv[1] * pv[1] + tv[2] * pv[2]) / det;
+            if (u < 0.0 || u > 1.0)
+                continue;
+            double qv[3] = {tv[1] * e1[2] - e1[1] * tv[2], tv[2] * e1[0] - e1[2] * tv[0], tv[0] * e1[1] - e1[0] * tv[1]};
+            double v = (d[0] * qv[0] + d[1] * qv[1] + d[2] * qv[2]) / det;
+            if (v < 0.0 || u + v > 1.0)
+                continue;
+            double t = (e2[0] * qv[0] + e2[1] * qv[1] + e2[2] * qv[2]) / det;
+            if (t < tmin || t >= tmax)
+                continue;
+            if (t < best || (t == best && p < bp)) {
+                best = t;
+                bp = p;
+            }
+        }
+        t_out[i] = best;
+        prim_out[i] = bp;
+    }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Neural BVH2: include/cuda/neural/accel/neural_bvh2.cuh                                      */
+/* ------------------------------------------------------------------------------------------ */
+
+#define ORC_NEURAL_STACK 24 /* NEURAL_STACK_SIZE, neural_bvh.cuh:22 */
+#define NO_NEURAL_CHILD 0xFFFFFFFFu
+
+/* dilated box: BVH2Node::bbox_center = min + extent * 0.5 (bvh.h:235-243) and
+ * neural_bvh2.cuh:80-86 */
+static inline void dilated_box(const uint32_t *node, float dil, v3 *bmin, v3 *bmax)
+{
+    v3 mn = node_min(node), mx = node_max(node);
+    if (dil != 0.0f) {
+        v3 ext = vsub(mx, mn);
+        v3 center = vadd(mn, vscale(ext, 0.5f));
+        v3 next = vscale(ext, 1.0f + dil);
+        *bmin = vsub(center, vscale(next, 0.5f));
+        *bmax = vadd(center, vscale(next, 0.5f));
+    } else {
+        *bmin = mn;
+        *bmax = mx;
+    }
+}
+
+/* intersect_bbox_min_max without ray bounds (ray.cuh:111-132 / bvh.h:137-154) */
+static inline int slab_min_max(v3 bmin, v3 bmax, v3 o, v3 d, float *mint, float *maxt)
+{
+    v3 t0 = vdiv(vsub(bmin, o), d);
+    v3 t1 = vdiv(vsub(bmax, o), d);
+    *mint = cmax(vmin(t0, t1));
+    *maxt = cmin(vmax(t0, t1));
+    return *mint <= *maxt;
+}
+
+/* intersect_traversal_bbox, neural_bvh2.cuh:94-115 (check_ray_bounds = true) */
+static inline float traversal_entry(const uint32_t *node, float dil, v3 o, v3 d, float rmint, float rmaxt)
+{
+    v3 bmin, bmax;
+    dilated_box(node, dil, &bmin, &bmax);
+    v3 t0 = vdiv(vsub(bmin, o), d);
+    v3 t1 = vdiv(vsub(bmax, o), d);
+    float mint = gmax(rmint, cmax(vmin(t0, t1)));
+    float maxt = gmin(rmaxt, cmin(vmax(t0, t1)));
+    return (mint <= maxt) ? mint : FLT_MAX;
+}
+
+static inline int is_leaf_at_lod(const uint32_t *node, uint32_t lod) /* neural_bvh2.cuh:124-128 */
+{
+    return node[3] > 0u && node[3] <= 2u + lod;
+}
+
+/* NeuralBVH2::intersect, neural_bvh2.cuh:170-292. Returns 1 with the next entered leaf segment,
+ * 0 when the stack is exhausted, -1 on stack overflow (the reference prints and returns false). */
+static int neural_intersect(const uint32_t *nodes, uint32_t lod, v3 o, v3 d, uint32_t *stack, int *sp,
+                            int inference, const orc_neural_consts *c, float current_maxt, float dil,
+                            float *seg_mint, float *seg_maxt, uint32_t *seg_node)
+{
+    const float rmint = -FLT_MAX, rmaxt = current_maxt;
+    uint32_t node_idx = stack[--(*sp)];
+    for (;;) {
+        const uint32_t *node = nodes + 8u * node_idx;
+        if (is_leaf_at_lod(node, lod) || node[7] == NO_NEURAL_CHILD) {
+            v3 bmin, bmax;
+            float mint, maxt;
+            dilated_box(node, dil, &bmin, &bmax);
+            if (slab_min_max(bmin, bmax, o, d, &mint, &maxt)) {
+                float maxt_eps = inference ? c->inference_maxt_epsilon : c->learning_maxt_epsilon;
+                float mint_eps = inference ? c->inference_mint_epsilon : c->learning_mint_epsilon;
+                int valid = mint < rmaxt;
+                if (mint < 0.0f)
+                    valid &= maxt > maxt_eps;
+                else
+                    valid &= mint > mint_eps;
+                if (valid) {
+                    *seg_mint = mint;
+                    *seg_maxt = maxt;
+                    *seg_node = node_idx;
+                    return 1;
+                }
+            }
+            if (*sp == 0)
+                return 0;
+            node_idx = stack[--(*sp)];
+            continue;
+        }
+        uint32_t c1 = node[7], c2 = node[7] + 1u;
+        float d1 = traversal_entry(nodes + 8u * c1, dil, o, d, rmint, rmaxt);
+        float d2 = traversal_entry(nodes + 8u * c2, dil, o, d, rmint, rmaxt);
+        if (d1 > d2) {
+            float td = d1;
+            d1 = d2;
+            d2 = td;
+            uint32_t tc = c1;
+            c1 = c2;
+            c2 = tc;
+        }
+        if (d1 == FLT_MAX) {
+            if (*sp == 0)
+                return 0;
+            node_idx = stack[--(*sp)];
+        } else {
+            node_idx = c1;
+            if (d2 != FLT_MAX) {
+                stack[(*sp)++] = c2;
+                if (*sp >= ORC_NEURAL_STACK)
+                    return -1;
+            }
+        }
+    }
+}
+
+void orc_neural_segments(const uint32_t *nodes, const orc_neural_consts *c, const float *rays, uint32_t n,
+                         uint32_t max_segments, uint32_t *segs, uint32_t *counts)
+{
+    for (uint32_t i = 0; i < n; i++) {
+        ray3 r = load_ray(rays + 8u * i);
+        uint32_t stack[ORC_NEURAL_STACK];
+        int sp = 1;
+        stack[0] = 0;
+        uint32_t cnt = 0;
+        while (sp > 0) {
+            float mint, maxt;
+            uint32_t nd;
+            int res = neural_intersect(nodes, c->bvh_lod, r.o, r.d, stack, &sp, 1, c, FLT_MAX,
+                                       c->fixed_node_dilation, &mint, &maxt, &nd);
+            if (res != 1)
+                break;
+            if (cnt < max_segments) {
+                uint32_t *s = segs + 4u * ((size_t)i * max_segments + cnt);
+                s[0] = f2u(mint);
+                s[1] = f2u(maxt);
+                s[2] = nd;
+                s[3] = 0;
+            }
+            cnt++;
+        }
+        counts[i] = cnt;
+    }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* FP16                                                                                       */
+/* ------------------------------------------------------------------------------------------ */
+
+uint16_t orc_f32_to_f16(float f) /* IEEE binary16, round to nearest even */
+{
+    uint32_t x = f2u(f);
+    uint32_t sign = (x >> 16) & 0x8000u;
+    uint32_t absx = x & 0x7FFFFFFFu;
+    if (absx >= 0x7F800000u) /* inf or nan */
+        return (uint16_t)(sign | 0x7C00u | (absx > 0x7F800000u ? 0x200u : 0u));
+    if (absx >= 0x477FF000u) /* >= 65520 rounds to inf */
+        return (uint16_t)(sign | 0x7C00u);
+    if (absx < 0x38800000u) { /* below the smallest normal 2^-14: subnormal or zero */
+        if (absx < 0x33000000u) /* < 2^-25 rounds to zero */
+            return (uint16_t)sign;
+        uint32_t mant = (absx & 0x7FFFFFu) | 0x800000u;
+        int e = (int)(absx >> 23); /* biased */
+        int shift = 126 - e;       /* value = mant * 2^(e-150); half subnormal unit 2^-24 */
+        /* result = mant * 2^(e-150) / 2^-24 = mant >> (126 - e) */
+        uint32_t q = mant >> shift;
+        uint32_t rem = mant & ((1u << shift) - 1u);
+        uint32_t halfway = 1u << (shift - 1);
+        if (rem > halfway || (rem == halfway && (q & 1u)))
+            q++;
+        return (uint16_t)(sign | q);
+    }
+    uint32_t e = (absx >> 23) - 112u; /* rebias 127 -> 15 */
+    uint32_t mant = absx & 0x7FFFFFu;
+    uint32_t q = (e << 10) | (mant >> 13);
+    uint32_t rem = mant & 0x1FFFu;
+    if (rem > 0x1000u || (rem == 0x1000u && (q & 1u)))
+        q++;
+    return (uint16_t)(sign | q);
+}
+
+float orc_f16_to_f32(uint16_t h)
+{
+    uint32_t sign = ((uint32_t)h & 0x8000u) << 16;
+    uint32_t e = ((uint32_t)h >> 10) & 0x1Fu;
+    uint32_t m = (uint32_t)h & 0x3FFu;
+    if (e == 0) {
+        float v = (float)m * 0x1p-24f;
+        return sign ? -v : v;
+    }
+    if (e == 31)
+        return u2f(sign | 0x7F800000u | (m << 13));
+    return u2f(sign | ((e + 112u) << 23) | (m << 13));
+}
+
+static inline float round_f16(float x) { return orc_f16_to_f32(orc_f32_to_f16(x)); }
+static inline float net_round(const orc_network *net, float x) { return net->exact ? x : round_f16(x); }
+static inline float net_w(const orc_network *net, size_t i)
+{
+    return net->exact ? net->weights_f32[i] : orc_f16_to_f32(net->weights_f16[i]);
+}
+static inline float net_g(const orc_network *net, size_t i)
+{
+    return net->exact ? net->grid_f32[i] : orc_f16_to_f32(net->grid_f16[i]);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Multiresolution hash grid (tcnn GridEncoding behaviour; Muller et al. 2022, Instant NGP)    */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Level l: scale = base_resolution * per_level_scale^l - 1 (per_level_scale^l by repeated
+ * double multiplication), resolution = ceil(scale) + 1, entries = min(roundup8(res^3), 2^log2T). */
+void orc_grid_layout(uint32_t n_levels, uint32_t log2_hashmap_size, uint32_t base_resolution,
+                     float per_level_scale, uint32_t *offset, uint32_t *size, uint32_t *resolution,
+                     float *scale, uint32_t *total_entries)
+{
+    uint64_t off = 0;
+    double p = 1.0;
+    uint64_t hashmap = 1ull << log2_hashmap_size;
+    for (uint32_t l = 0; l < n_levels; l++) {
+        float s = (float)((double)base_resolution * p - 1.0);
+        uint32_t res = (uint32_t)ceilf(s) + 1u;
+        uint64_t dense = (uint64_t)res * res * res;
+        dense = (dense + 7u) & ~7ull;
+        uint64_t sz = dense < hashmap ? dense : hashmap;
+        offset[l] = (uint32_t)off;
+        size[l] = (uint32_t)sz;
+        resolution[l] = res;
+        scale[l] = s;
+        off += sz;
+        p *= (double)per_level_scale;
+    }
+    *total_entries = (uint32_t)off;
+}
+
+/* grid_index: dense index x + y*res + z*res^2 while res^3 fits the level, else the coherent prime
+ * hash x*1 ^ y*2654435761 ^ z*805459861; both modulo the level size. */
+static inline uint32_t grid_index(uint32_t level_size, uint32_t res, uint32_t x, uint32_t y, uint32_t z)
+{
+    uint64_t dense = (uint64_t)res * res * res;
+    uint32_t idx;
+    if (dense <= (uint64_t)level_size)
+        idx = x + y * res + z * res * res;
+    else
+        idx = x ^ (y * 2654435761u) ^ (z * 805459861u);
+    return idx % level_size;
+}
+
+/* features of one point for one level (2 values), fused multiply-add accumulation over the 8
+ * corners in order c = 0..7 (bit d of c selects the upper corner along axis d) */
+static void encode_level(const orc_network *net, uint32_t l, v3 p, float *f0, float *f1, uint32_t *cidx,
+                         float *cw)
+{
+    float s = net->level_scale[l];
+    float pos[3] = {fmaf(p.x, s, 0.5f), fmaf(p.y, s, 0.5f), fmaf(p.z, s, 0.5f)};
+    uint32_t g[3];
+    float fr[3];
+    for (int d = 0; d < 3; d++) {
+        float fl = floorf(pos[d]);
+        g[d] = (uint32_t)(int32_t)fl;
+        fr[d] = pos[d] - fl;
+    }
+    float a0 = 0.f, a1 = 0.f;
+    for (uint32_t c = 0; c < 8; c++) {
+        float wx = (c & 1u) ? fr[0] : 1.0f - fr[0];
+        float wy = (c & 2u) ? fr[1] : 1.0f - fr[1];
+        float wz = (c & 4u) ? fr[2] : 1.0f - fr[2];
+        float w = (wx * wy) * wz;
+        uint32_t idx = grid_index(net->level_size[l], net->level_resolution[l], g[0] + (c & 1u),
+                                  g[1] + ((c >> 1) & 1u), g[2] + ((c >> 2) & 1u));
+        uint32_t e = net->level_offset[l] + idx;
+        a0 = fmaf(w, net_g(net, 2u * e), a0);
+        a1 = fmaf(w, net_g(net, 2u * e + 1u), a1);
+        if (cidx) {
+            cidx[c] = e;
+            cw[c] = w;
+        }
+    }
+    *f0 = a0;
+    *f1 = a1;
+}
+
+void orc_encode(const orc_network *net, const float *positions, uint32_t n, float *features)
+{
+    for (uint32_t i = 0; i < n; i++)
+        for (uint32_t k = 0; k < net->n_points; k++) {
+            v3 p = load3(positions + 3u * ((size_t)i * net->n_points + k));
+            for (uint32_t l = 0; l < net->n_levels; l++) {
+                float *f = features + (size_t)i * net->n_inputs + (size_t)k * net->n_levels * 2u + 2u * l;
+                encode_level(net, l, p, &f[0], &f[1], NULL, NULL);
+            }
+        }
+}
+
+/* offsets of the network matrices in the parameter vector */
+static void matrix_offsets(const orc_network *net, uint32_t *off, uint32_t *rows, uint32_t *cols, uint32_t *n_mat)
+{
+    uint32_t nm = net->n_hidden_layers + 1u, o = 0;
+    for (uint32_t m = 0; m < nm; m++) {
+        rows[m] = (m == nm - 1u) ? 16u : net->n_neurons;
+        cols[m] = (m == 0) ? net->n_inputs : net->n_neurons;
+        off[m] = o;
+        o += rows[m] * cols[m];
+    }
+    *n_mat = nm;
+}
+
+/* forward of one row: x (FP16-rounded features) -> outputs (16, sigmoid). acts (optional) receives
+ * the FP16 activations entering every layer (n_mat x 128 max) and pre (optional) the output
+ * pre-activations. */
+static void mlp_row(const orc_network *net, const float *x_in, float *out, float *acts, double *pre_out)
+{
+    uint32_t off[16], rows[16], cols[16], nm;
+    matrix_offsets(net, off, rows, cols, &nm);
+    float a[128], b[128];
+    for (uint32_t i = 0; i < net->n_inputs; i++)
+        a[i] = net_round(net, x_in[i]);
+    for (uint32_t m = 0; m < nm; m++) {
+        if (acts)
+            memcpy(acts + 128u * m, a, sizeof(float) * cols[m]);
+        for (uint32_t r = 0; r < rows[m]; r++) {
+            double acc = 0.0;
+            const size_t wo = off[m] + (size_t)r * cols[m];
+            for (uint32_t k = 0; k < cols[m]; k++)
+                acc += (double)net_w(net, wo + k) * (double)a[k];
+            if (m == nm - 1u) {
+                if (pre_out)
+                    pre_out[r] = acc;
+                out[r] = (float)(1.0 / (1.0 + exp(-acc)));
+            } else {
+                b[r] = net_round(net, acc > 0.0 ? (float)acc : 0.0f);
+            }
+        }
+        if (m != nm - 1u)
+            memcpy(a, b, sizeof(float) * rows[m]);
+    }
+}
+
+typedef struct {
+    const orc_network *net;
+    const float *positions;
+    float *outputs;
+    uint32_t begin, end;
+} infer_job;
+
+static void *infer_worker(void *arg)
+{
+    infer_job *j = (infer_job *)arg;
+    float feat[128];
+    for (uint32_t i = j->begin; i < j->end; i++) {
+        orc_encode(j->net, j->positions + (size_t)i * j->net->n_points * 3u, 1, feat);
+        mlp_row(j->net, feat, j->outputs + 16u * (size_t)i, NULL, NULL);
+    }
+    return NULL;
+}
+
+void orc_network_inference(const orc_network *net, const float *positions, uint32_t n, float *outputs,
+                           int n_threads)
+{
+    if (n_threads < 1)
+        n_threads = 1;
+    if (n_threads > 256)
+        n_threads = 256;
+    pthread_t th[256];
+    infer_job jobs[256];
+    uint32_t chunk = (n + (uint32_t)n_threads - 1u) / (uint32_t)n_threads;
+    for (int k = 0; k < n_threads; k++) {
+        uint32_t b = (uint32_t)k * chunk, e = b + chunk;
+        if (b > n)
+            b = n;
+        if (e > n)
+            e = n;
+        jobs[k] = (infer_job){net, positions, outputs, b, e};
+        if (n_threads == 1)
+            infer_worker(&jobs[k]);
+        else
+            pthread_create(&th[k], NULL, infer_worker, &jobs[k]);
+    }
+    if (n_threads > 1)
+        for (int k = 0; k < n_threads; k++)
+            pthread_join(th[k], NULL);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Segment encoding: src/cuda/neural/neural_bvh_module_kernels.cu:10-97, 266-303              */
+/* ------------------------------------------------------------------------------------------ */
+
+static void encode_segment(const orc_neural_scene *sc, const orc_neural_consts *c, v3 wpo, v3 wpi,
+                           uint32_t *rng, float *pts)
+{
+    v3 smin = load3(sc->scene_min), smax = load3(sc->scene_max);
+    float dilation = 1.0f + c->node_extent_dilation + c->fixed_node_dilation;
+    v3 ext = vscale(vsub(smax, smin), dilation);
+    v3 center = vscale(vadd(smax, smin), 0.5f);
+    v3 epo = vadds(vdiv(vsub(wpo, center), ext), 0.5f);
+    v3 epi = vadds(vdiv(vsub(wpi, center), ext), 0.5f);
+    int np = c->input_segment_points;
+    float delta, offset;
+    if (c->segment_distribution == 1) { /* EquidistantExterior */
+        delta = 1.0f / (float)(np - 1);
+        offset = 0.0f;
+        if (np == 1)
+            delta = 1.0f;
+    } else {
+        delta = 1.0f / (float)np;
+        offset = 0.5f;
+    }
+    for (int k = 0; k < np; k++) {
+        float t = (c->segment_distribution == 2) ? orc_lcg_randomf(rng) : delta * ((float)k + offset);
+        v3 p = vadd(vscale(epo, 1.0f - t), vscale(epi, t));
+        pts[3 * k + 0] = p.x;
+        pts[3 * k + 1] = p.y;
+        pts[3 * k + 2] = p.z;
+    }
+}
+
+static inline v3 ray_at(v3 o, v3 d, float t) { return vadd(o, vscale(d, t)); }
+
+/* decode_depth_estimate, LocalT branch, neural_bvh_module_common.cuh:23-58 */
+static float decode_local_t(const orc_neural_consts *c, float out_depth, float mint, float maxt, int inside)
+{
+    float seg_len = maxt - mint;
+    float u = gclamp01(out_depth);
+    float depth = FLT_MAX;
+    if (inside) {
+        if (c->depth_epsilon != 1.0f) {
+            float inward = (float)((double)u * ((double)seg_len + 1e-3));
+            if (inward < maxt - seg_len * c->depth_epsilon - c->fixed_depth_epsilon)
+                depth = maxt - inward;
+        }
+    } else {
+        depth = (float)((double)u * ((double)seg_len + 1e-3) + (double)mint);
+    }
+    return depth;
+}
+
+float orc_decode_local_t(float out_depth, float mint, float maxt, int inside, float depth_epsilon,
+                         float fixed_depth_epsilon)
+{
+    orc_neural_consts c;
+    memset(&c, 0, sizeof(c));
+    c.depth_epsilon = depth_epsilon;
+    c.fixed_depth_epsilon = fixed_depth_epsilon;
+    return decode_local_t(&c, out_depth, mint, maxt, inside);
+}
+
+typedef struct {
+    const orc_neural_scene *scene;
+    const orc_network *net;
+    const orc_neural_consts *c;
+    const orc_classic_scene *classic;
+    float margin;
+    const float *rays;
+    uint32_t begin, end, depth;
+    int vis_only;
+    uint32_t *hits;
+} nq_job;
+
+static void neural_query_one(const nq_job *j, uint32_t i)
+{
+    const orc_neural_consts *c = j->c;
+    ray3 r = load_ray(j->rays + 8u * i);
+    uint32_t *h = j->hits + 12u * (size_t)i;
+    float best_t = r.maxt; /* init_neural_traversal_result(current_t) */
+    int valid = 0;
+    v3 normal = mk(0, 0, 0), albedo = mk(0, 0, 0);
+    float vis_acc = 0.0f;
+    uint32_t flags = 0, segments = 0;
+    int fallback = 0;
+    uint32_t rng = orc_lcg_seed(0u, 0u, i);
+
+    uint32_t stack[ORC_NEURAL_STACK];
+    int sp = 1;
+    stack[0] = 0;
+    float mint, maxt;
+    uint32_t node;
+    int res = neural_intersect(j->scene->neural_nodes, c->bvh_lod, r.o, r.d, stack, &sp, 1, c, FLT_MAX,
+                               c->fixed_node_dilation, &mint, &maxt, &node);
+    float thr = j->depth == 1u ? c->primary_visibility_threshold : c->secondary_visibility_threshold;
+    uint32_t step = 0;
+    while (res == 1) {
+        if (j->scene->non_neural && j->scene->non_neural[node]) {
+            fallback = 1;
+            break;
+        }
+        if (step > c->max_traversal_steps) {
+            flags |= 0x4u;
+            break;
+        }
+        step++;
+        /* encode_bvh_network_input_data: swap for a negative mint (kernels.cu:281-286) */
+        float a = mint, b = maxt;
+        if (a < 0.0f) {
+            float t = a;
+            a = b;
+            b = t;
+        }
+        float pts[3 * 16], feat[128], out[16];
+        encode_segment(j->scene, c, ray_at(r.o, r.d, a), ray_at(r.o, r.d, b), &rng, pts);
+        for (int k = 0; k < c->input_segment_points; k++) {
+            v3 p = load3(pts + 3 * k);
+            for (uint32_t l = 0; l < j->net->n_levels; l++)
+                encode_level(j->net, l, p, &feat[(size_t)k * j->net->n_levels * 2u + 2u * l],
+                             &feat[(size_t)k * j->net->n_levels * 2u + 2u * l + 1u], NULL, NULL);
+        }
+        mlp_row(j->net, feat, out, NULL, NULL);
+        segments++;
+        if (j->margin > 0.0f && fabsf(out[0] - thr) < j->margin) {
+            fallback = 1;
+            break;
+        }
+        /* process_neural_bvh_traversal_step, path_inference_kernels.cu:61-131 */
+        float new_depth = best_t;
+        int stop = 0;
+        if (out[0] > thr) {
+            int inside = mint < 0.0f;
+            if (j->vis_only && !inside) {
+                valid = 1;
+                vis_acc = out[0];
+                stop = 1;
+            } else {
+                float de = decode_local_t(c, out[1], mint, maxt, inside);
+                if (de != FLT_MAX) {
+                    if (j->vis_only) {
+                        valid = 1;
+                        vis_acc = out[0];
+                        stop = 1;
+                    } else if (de < best_t) {
+                        valid = 1;
+                        best_t = de;
+                        new_depth = de;
+                        vis_acc = out[0];
+                        normal = vnormalize(mk(out[2] * 2.0f - 1.0f, out[3] * 2.0f - 1.0f, out[4] * 2.0f - 1.0f));
+                        albedo = mk(out[5], out[6], out[7]);
+                    }
+                }
+            }
+        }
+        if (stop)
+            break;
+        /* process_bvh_network_output_and_intersect_neural_bvh, common.cuh:496-550 */
+        if (sp == 0)
+            break;
+        res = neural_intersect(j->scene->neural_nodes, c->bvh_lod, r.o, r.d, stack, &sp, 1, c, new_depth,
+                               c->fixed_node_dilation, &mint, &maxt, &node);
+    }
+    if (res == -1)
+        flags |= 0x8u;
+    if (fallback && j->classic) {
+        float t, u, v;
+        uint32_t prim;
+        ray3 cr = r;
+        classic_intersect(j->classic, cr, j->vis_only, &t, &u, &v, &prim, NULL, NULL);
+        h[0] = f2u(t);
+        for (int k = 1; k < 8; k++)
+            h[k] = 0;
+        h[8] = (prim != 0xFFFFFFFFu ? 0x1u : 0u) | 0x2u | flags;
+        h[9] = segments;
+        h[10] = prim;
+        h[11] = 0;
+        return;
+    }
+    if (!valid)
+        best_t = FLT_MAX;
+    h[0] = f2u(valid ? best_t : FLT_MAX);
+    h[1] = f2u(normal.x);
+    h[2] = f2u(normal.y);
+    h[3] = f2u(normal.z);
+    h[4] = f2u(albedo.x);
+    h[5] = f2u(albedo.y);
+    h[6] = f2u(albedo.z);
+    h[7] = f2u(valid ? vis_acc : 0.0f);
+    h[8] = (valid ? 0x1u : 0u) | flags;
+    h[9] = segments;
+    h[10] = 0xFFFFFFFFu;
+    h[11] = 0;
+}
+
+static void *nq_worker(void *arg)
+{
+    nq_job *j = (nq_job *)arg;
+    for (uint32_t i = j->begin; i < j->end; i++)
+        neural_query_one(j, i);
+    return NULL;
+}
+
+void orc_neural_query(const orc_neural_scene *scene, const orc_network *net, const orc_neural_consts *c,
+                      const orc_classic_scene *classic, float fallback_margin, const float *rays, uint32_t n,
+                      uint32_t depth, int visibility_only, uint32_t *hits, int n_threads)
+{
+    if (n_threads < 1)
+        n_threads = 1;
+    if (n_threads > 256)
+        n_threads = 256;
+    pthread_t th[256];
+    nq_job jobs[256];
+    uint32_t chunk = (n + (uint32_t)n_threads - 1u) / (uint32_t)n_threads;
+    for (int k = 0; k < n_threads; k++) {
+        uint32_t b = (uint32_t)k * chunk, e = b + chunk;
+        if (b > n)
+            b = n;
+        if (e > n)
+            e = n;
+        jobs[k] = (nq_job){scene, net, c, classic, fallback_margin, rays, b, e, depth, visibility_only, hits};
+        if (n_threads == 1)
+            nq_worker(&jobs[k]);
+        else
+            pthread_create(&th[k], NULL, nq_worker, &jobs[k]);
+    }
+    if (n_threads > 1)
+        for (int k = 0; k < n_threads; k++)
+            pthread_join(th[k], NULL);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Training samples: neural_bvh_module_kernels.cu:119-264 (n_sub_batch = 1),                  */
+/* stack_based_sample_uniform_bvh_density common.cuh:703-781, sample_bbox_position 635-660,    */
+/* generate_single_bvh_network_output_reference 783-861, compute_depth_or_position_output      */
+/* 586-629 (LocalT)                                                                             */
+/* ------------------------------------------------------------------------------------------ */
+
+static v3 cube_pos_on_face(int face, float u, float v) /* sampling.cuh:85-94 */
+{
+    switch (face) {
+    case 0: return mk(1.0f, u, v);
+    case 1: return mk(0.0f, u, v);
+    case 2: return mk(u, 1.0f, v);
+    case 3: return mk(u, 0.0f, v);
+    case 4: return mk(u, v, 1.0f);
+    default: return mk(u, v, 0.0f);
+    }
+}
+
+void orc_generate_training_batch(const orc_neural_scene *sc, const orc_classic_scene *classic,
+                                 const float *albedo, const orc_neural_consts *c, uint32_t training_step,
+                                 uint32_t batch_size, uint32_t n, float *positions, float *targets,
+                                 uint32_t *nodes_out)
+{
+    v3 smin = load3(sc->scene_min), smax = load3(sc->scene_max);
+    const uint32_t *nodes = sc->neural_nodes;
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t rng = orc_lcg_seed(training_step * batch_size, 0u, i);
+        /* stack_based_sample_uniform_bvh_density */
+        float sx = orc_lcg_randomf(&rng);
+        float sy = orc_lcg_randomf(&rng);
+        v3 dir = uniform_sphere(sx, sy);
+        (void)orc_lcg_randomf(&rng); /* sampled LoD draw (single learned LoD for a fixed cut) */
+        float dil = c->fixed_node_dilation + orc_lcg_randomf(&rng) * c->node_extent_dilation;
+        uint32_t stack[ORC_NEURAL_STACK];
+        int sp = 0;
+        int valid = 0;
+        v3 o = mk(0, 0, 0), d = dir;
+        float mint = 0.f, maxt = 0.f;
+        uint32_t node = 0;
+        uint32_t guard = 0;
+        do {
+            if (!valid) {
+                stack[0] = 0;
+                sp = 1;
+                float px = orc_lcg_randomf(&rng);
+                float py = orc_lcg_randomf(&rng);
+                float pz = orc_lcg_randomf(&rng);
+                v3 ps = vsub(vscale(mk(px, py, pz), c->sampling_bbox_scaling),
+                             mk((c->sampling_bbox_scaling - 1.0f) * 0.5f, (c->sampling_bbox_scaling - 1.0f) * 0.5f,
+                                (c->sampling_bbox_scaling - 1.0f) * 0.5f));
+                o = vadd(vmul(ps, vsub(smax, smin)), smin); /* Bbox::local_to_bbox, bbox.h:93-97 */
+                d = dir;
+            }
+            int res = neural_intersect(nodes, c->bvh_lod, o, d, stack, &sp, 0, c, FLT_MAX, dil, &mint, &maxt, &node);
+            valid = (res == 1);
+            if (res == -1)
+                sp = 0;
+        } while (!valid && ++guard < 100000u);
+        if (c->leaf_boundary_sampling_ratio != 0.0f &&
+            orc_lcg_randomf(&rng) <= c->leaf_boundary_sampling_ratio) {
+            /* sample_bbox_position, common.cuh:635-660 */
+            int f1 = (int)(orc_lcg_randomf(&rng) * 6.0f);
+            f1 = f1 < 5 ? f1 : 5;
+            int f2;
+            do {
+                f2 = (int)(orc_lcg_randomf(&rng) * 6.0f);
+                f2 = f2 < 5 ? f2 : 5;
+            } while (f1 == f2);
+            float u1 = orc_lcg_randomf(&rng), v1 = orc_lcg_randomf(&rng);
+            v3 lp1 = cube_pos_on_face(f1, u1, v1);
+            float u2 = orc_lcg_randomf(&rng), v2 = orc_lcg_randomf(&rng);
+            v3 lp2 = cube_pos_on_face(f2, u2, v2);
+            const uint32_t *nd = nodes + 8u * node;
+            v3 mn = node_min(nd), mx = node_max(nd);
+            v3 ext = vsub(mx, mn);
+            v3 center = vadd(mn, vscale(ext, 0.5f));
+            v3 next = vscale(ext, 1.0f + dil);
+            v3 nmin = vsub(center, vscale(next, 0.5f));
+            v3 entry = vadd(nmin, vmul(lp1, next));
+            v3 exitp = vadd(nmin, vmul(lp2, next));
+            o = entry;
+            d = vnormalize(vsub(exitp, entry));
+            mint = 0.0f;
+            maxt = vlength(vsub(exitp, entry));
+        }
+        if (nodes_out)
+            nodes_out[i] = node;
+        float pts[48];
+        encode_segment(sc, c, ray_at(o, d, mint), ray_at(o, d, maxt), &rng, pts);
+        memcpy(positions + (size_t)i * 3u * (uint32_t)c->input_segment_points, pts,
+               sizeof(float) * 3u * (uint32_t)c->input_segment_points);
+        /* labels from the classic BLAS on [mint, maxt] */
+        ray3 lr;
+        lr.o = o;
+        lr.d = d;
+        lr.mint = mint;
+        lr.maxt = maxt;
+        float t, u, v;
+        uint32_t prim;
+        classic_intersect(classic, lr, 0, &t, &u, &v, &prim, NULL, NULL);
+        float *tg = targets + 8u * (size_t)i;
+        int hit = t != FLT_MAX;
+        tg[0] = hit ? 1.0f : 0.0f;
+        tg[1] = hit ? (float)((double)(t - mint) / ((double)(maxt - mint) + 1e-3)) : 0.0f;
+        if (hit) {
+            const uint32_t *ix = classic->indices + 3u * prim;
+            v3 v0 = load3(classic->vertices + 3u * ix[0]);
+            v3 va = load3(classic->vertices + 3u * ix[1]);
+            v3 vb = load3(classic->vertices + 3u * ix[2]);
+            v3 gn = vnormalize(vcross(vsub(va, v0), vsub(vb, v0))); /* compute_its_data, bvh.cuh:69 */
+            v3 nn = vscale(vadds(gn, 1.0f), 0.5f);
+            tg[2] = nn.x;
+            tg[3] = nn.y;
+            tg[4] = nn.z;
+            if (albedo) {
+                tg[5] = albedo[3u * prim];
+                tg[6] = albedo[3u * prim + 1u];
+                tg[7] = albedo[3u * prim + 2u];
+            } else {
+                tg[5] = tg[6] = tg[7] = 0.9f;
+            }
+        } else {
+            for (int k = 2; k < 8; k++)
+                tg[k] = 0.0f;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Loss: include/cuda/neural/utils/loss_gradient.cuh:25-94, pt_composite_loss.cuh:18-123       */
+/* ------------------------------------------------------------------------------------------ */
+
+static void loss_and_gradient(int type, float target, float pred, float *loss, float *grad)
+{
+    switch (type) {
+    case 0: { /* RelativeL2 */
+        float diff = pred - target;
+        float denom = pred * pred + 1e-2f;
+        *loss = diff * diff / denom;
+        *grad = 2.0f * diff / denom;
+        break;
+    }
+    case 2: { /* RelativeL1 */
+        float scale = 1.0f / (fabsf(pred) + 1e-2f);
+        float diff = pred - target;
+        *loss = fabsf(diff) * scale;
+        *grad = copysignf(scale, diff);
+        break;
+    }
+    case 3: { /* L1 */
+        float diff = pred - target;
+        *loss = fabsf(diff);
+        *grad = copysignf(1.0f, diff);
+        break;
+    }
+    case 5: { /* BinaryCrossEntropy */
+        const float eps = 1e-5f;
+        float p = fminf(fmaxf(pred, eps), 1.0f - eps);
+        *loss = -(target * logf(p) + (1.0f - target) * logf(1.0f - p));
+        *grad = -(target - p) / (p - (p * p));
+        break;
+    }
+    case 6: { /* LogL2 */
+        float diff = logf(1.0f + pred) - logf(1.0f + target);
+        *loss = diff * diff;
+        *grad = 2.0f * diff / (pred + 1.0f);
+        break;
+    }
+    case 7: { /* LHalf */
+        float sd = sqrtf(fabsf(pred - target));
+        *loss = sd;
+        *grad = 1.0f / (2.0f * sd + 1e-5f);
+        break;
+    }
+    default: { /* L2 */
+        float diff = pred - target;
+        *loss = diff * diff;
+        *grad = 2.0f * diff;
+        break;
+    }
+    }
+}
+
+void orc_composite_loss(const orc_loss_consts *lc, const float *predictions, const float *targets, uint32_t n,
+                        float loss_scale, float *values, float *gradients)
+{
+    uint32_t dims = 2u + (lc->learn_normal ? 3u : 0u) + (lc->learn_albedo ? 3u : 0u);
+    float n_total = (float)(n * dims);
+    for (uint32_t i = 0; i < n; i++)
+        for (uint32_t ch = 0; ch < 16; ch++) {
+            float pred = predictions[16u * i + ch];
+            float loss = 0.f, grad = 0.f;
+            const float *tg = targets + 8u * i;
+            int ignore = lc->visibility_masking_loss ? (tg[0] < 0.5f) : 0;
+            if (ch == 0) {
+                loss_and_gradient(lc->visibility_loss, tg[0], pred, &loss, &grad);
+                loss *= lc->visibility_loss_scale;
+                grad *= lc->visibility_loss_scale;
+            } else if (ch == 1 && !ignore) {
+                loss_and_gradient(lc->depth_loss, tg[1], pred, &loss, &grad);
+                loss *= lc->depth_loss_scale;
+                grad *= lc->depth_loss_scale;
+            } else if (ch >= 2 && ch < 5 && !ignore && lc->learn_normal) {
+                if (lc->output_normal_linear_activation) {
+                    float n_length = 0.1f;
+                    float n_axis = (pred * 2.0f - 1.0f) / n_length;
+                    float lin = n_axis * 0.5f + 0.5f;
+                    loss_and_gradient(lc->normal_loss, tg[ch], lin, &loss, &grad);
+                    grad *= 1.0f / n_length;
+                } else {
+                    loss_and_gradient(lc->normal_loss, tg[ch], pred, &loss, &grad);
+                }
+                loss *= lc->normal_loss_scale;
+                grad *= lc->normal_loss_scale;
+            } else if (ch >= 5 && ch < 8 && !ignore && lc->learn_albedo) {
+                if (lc->output_albedo_linear_activation) {
+                    float n_length = 0.1f;
+                    float lin = pred / n_length;
+                    loss_and_gradient(lc->albedo_loss, tg[ch], lin, &loss, &grad);
+                    grad *= 1.0f / n_length;
+                } else {
+                    loss_and_gradient(lc->albedo_loss, tg[ch], pred, &loss, &grad);
+                }
+                loss *= lc->albedo_loss_scale;
+                grad *= lc->albedo_loss_scale;
+            }
+            values[16u * i + ch] = loss / n_total;
+            gradients[16u * i + ch] = loss_scale * grad / n_total;
+        }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Backward pass (gradient of the mean loss), FP64 accumulation                               */
+/* ------------------------------------------------------------------------------------------ */
+
+void orc_compute_gradients(const orc_network *net, const orc_loss_consts *lc, const float *positions,
+                           const float *targets, uint32_t n, float loss_scale, double *gradients,
+                           double *mean_loss, int fp16_backward)
+{
+    uint32_t off[16], rows[16], cols[16], nm;
+    matrix_offsets(net, off, rows, cols, &nm);
+    uint32_t n_net = off[nm - 1u] + rows[nm - 1u] * cols[nm - 1u];
+    uint32_t n_grid = net->level_offset[net->n_levels - 1u] + net->level_size[net->n_levels - 1u];
+    memset(gradients, 0, sizeof(double) * ((size_t)n_net + 2u * (size_t)n_grid));
+    double total_loss = 0.0;
+    float *acts = (float *)malloc(sizeof(float) * 128u * 16u);
+    double dz[128], da[128];
+    for (uint32_t i = 0; i < n; i++) {
+        float feat[128], out[16], vals[16], grads[16];
+        double pre[16];
+        const float *pos = positions + (size_t)i * net->n_points * 3u;
+        /* forward, keeping the corner indices and weights for the grid backward */
+        uint32_t cidx[16][32][8];
+        float cw[16][32][8];
+        for (uint32_t k = 0; k < net->n_points; k++) {
+            v3 p = load3(pos + 3u * k);
+            for (uint32_t l = 0; l < net->n_levels; l++)
+                encode_level(net, l, p, &feat[k * net->n_levels * 2u + 2u * l],
+                             &feat[k * net->n_levels * 2u + 2u * l + 1u], cidx[k][l], cw[k][l]);
+        }
+        mlp_row(net, feat, out, acts, pre);
+        orc_composite_loss(lc, out, targets + 8u * (size_t)i, 1, loss_scale, vals, grads);
+        /* the per-row loss values are normalised by n_total of a batch of one; rescale to n */
+        for (uint32_t ch = 0; ch < 16; ch++) {
+            total_loss += (double)vals[ch] / (double)n;
+            float g = grads[ch] / (float)n;
+            if (fp16_backward)
+                g = round_f16(g);
+            double s = 1.0 / (1.0 + exp(-pre[ch]));
+            dz[ch] = (double)g * s * (1.0 - s);
+            if (fp16_backward)
+                dz[ch] = (double)round_f16((float)dz[ch]);
+        }
+        /* layers backward */
+        for (int m = (int)nm - 1; m >= 0; m--) {
+            const float *a = acts + 128u * (uint32_t)m;
+            double *gw = gradients + off[m];
+            for (uint32_t r = 0; r < rows[m]; r++) {
+                if (dz[r] == 0.0)
+                    continue;
+                for (uint32_t k = 0; k < cols[m]; k++)
+                    gw[(size_t)r * cols[m] + k] += dz[r] * (double)a[k];
+            }
+            for (uint32_t k = 0; k < cols[m]; k++) {
+                double s = 0.0;
+                for (uint32_t r = 0; r < rows[m]; r++)
+                    s += dz[r] * (double)net_w(net, off[m] + (size_t)r * cols[m] + k);
+                da[k] = s;
+            }
+            if (m > 0) {
+                for (uint32_t k = 0; k < cols[m]; k++) {
+                    double g = a[k] > 0.0f ? da[k] : 0.0; /* ReLU of the previous layer */
+                    if (fp16_backward)
+                        g = (double)round_f16((float)g);
+                    dz[k] = g;
+                }
+            }
+        }
+        /* grid backward: d feature = da (input gradient of the first layer) */
+        double *gg = gradients + n_net;
+        for (uint32_t k = 0; k < net->n_points; k++)
+            for (uint32_t l = 0; l < net->n_levels; l++) {
+                double g0 = da[k * net->n_levels * 2u + 2u * l];
+                double g1 = da[k * net->n_levels * 2u + 2u * l + 1u];
+                if (fp16_backward) {
+                    g0 = (double)round_f16((float)g0);
+                    g1 = (double)round_f16((float)g1);
+                }
+                for (uint32_t cc = 0; cc < 8; cc++) {
+                    gg[2u * cidx[k][l][cc]] += (double)cw[k][l][cc] * g0;
+                    gg[2u * cidx[k][l][cc] + 1u] += (double)cw[k][l][cc] * g1;
+                }
+            }
+    }
+    free(acts);
+    for (size_t p = 0; p < (size_t)n_net + 2u * (size_t)n_grid; p++)
+        gradients[p] /= (double)loss_scale;
+    *mean_loss = total_loss;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Adam with ExponentialDecay (Kingma & Ba 2015, Algorithm 1, bias correction folded into the  */
+/* step size); decay as configured at neural_bvh_module.cu:146-150                             */
+/* ------------------------------------------------------------------------------------------ */
+
+void orc_adam_step(float *params, float *m, float *v, const float *grad, uint32_t n, uint32_t step, float lr,
+                   float beta1, float beta2, float eps, float l2_reg, int32_t decay_start, int32_t decay_interval,
+                   float decay_base)
+{
+    double lr_s = (double)lr;
+    if ((int64_t)step >= (int64_t)decay_start && decay_interval > 0)
+        lr_s *= pow((double)decay_base, (double)(((int64_t)step - decay_start) / decay_interval));
+    double t = (double)step + 1.0;
+    float lr_t = (float)(lr_s * sqrt(1.0 - pow((double)beta2, t)) / (1.0 - pow((double)beta1, t)));
+    float omb1 = 1.0f - beta1, omb2 = 1.0f - beta2;
+    for (uint32_t i = 0; i < n; i++) {
+        float w = params[i];
+        float g = grad[i] + l2_reg * w;
+        float mi = beta1 * m[i] + omb1 * g;
+        float vi = beta2 * v[i] + omb2 * (g * g);
+        m[i] = mi;
+        v[i] = vi;
+        params[i] = w - lr_t * (mi / (sqrtf(vi) + eps));
+    }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Camera rays: CudaBackend::update_camera cuda_backend.cpp:595-611, camera_raygen             */
+/* renderer_kernels.cuh:74-79, jitter from get_lcg_rng(sample_idx, offset, pixel)              */
+/* neural_bvh_module_common.cuh:222-228                                                         */
+/* ------------------------------------------------------------------------------------------ */
+
+void orc_camera_rays(uint32_t width, uint32_t height, uint32_t sample_idx, uint32_t sample_offset,
+                     const float *origin, const float *target, const float *up, float yfov_degrees, float *rays)
+{
+    float ipy = 2.0f * tanf((0.5f * yfov_degrees) * 0.0174532925199432958f);
+    float aspect = (float)width / (float)height;
+    float ipx = ipy * aspect;
+    v3 org = load3(origin);
+    v3 dir = vnormalize(vsub(load3(target), org));
+    v3 upv = vnormalize(load3(up));
+    v3 du = vscale(vnormalize(vcross(dir, upv)), ipx);
+    v3 dv = vscale(vnormalize(vcross(du, dir)), -ipy);
+    v3 tl = vsub(vsub(dir, vscale(du, 0.5f)), vscale(dv, 0.5f));
+    for (uint32_t p = 0; p < width * height; p++) {
+        uint32_t px = p % width, py = p / width;
+        uint32_t rng = orc_lcg_seed(sample_idx, sample_offset, p);
+        float jx = orc_lcg_randomf(&rng);
+        float jy = orc_lcg_randomf(&rng);
+        float xf = ((float)px + jx) / (float)width;
+        float yf = ((float)py + jy) / (float)height;
+        v3 d = vnormalize(vadd(vadd(vscale(du, xf), vscale(dv, yf)), tl));
+        float *r = rays + 8u * (size_t)p;
+        r[0] = org.x;
+        r[1] = org.y;
+        r[2] = org.z;
+        r[3] = 1e-4f;
+        r[4] = d.x;
+        r[5] = d.y;
+        r[6] = d.z;
+        r[7] = FLT_MAX;
+    }
+}

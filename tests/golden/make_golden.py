@@ -1,0 +1,116 @@
+"""Generates tests/golden/golden.npz: golden vectors of the N-BVH ray-query path computed by the
+independent pure-Python restatement in pyref.py (not by the C oracle), on small seeded inputs.
+
+    python tests/golden/make_golden.py
+
+The BVH topologies fed to both restatements come from the library's host builder (its output is an
+input here; the traversal results are what the vectors pin).
+"""
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import pyref  # noqa: E402
+import nbvh_gb300 as nb  # noqa: E402
+from nbvh_gb300 import scenes  # noqa: E402
+
+F = np.float32
+
+
+def main():
+    out = {}
+    # RNG streams: get_lcg_rng(index, frame, linear) then 6 draws
+    seeds = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [7 * 262144, 0, 12345], [3, 2, 99999],
+                      [0xFFFFFFFF, 5, 77]], np.uint64)
+    streams = []
+    for s in seeds:
+        r = pyref.Rng(pyref.lcg_seed(int(s[0]) & 0xFFFFFFFF, int(s[1]), int(s[2])))
+        streams.append([r.f() for _ in range(6)])
+    out["rng_seeds"] = seeds.astype(np.uint32)
+    out["rng_streams"] = np.array(streams, np.float32)
+    # sin/cos of 2 pi u
+    us = np.concatenate([np.linspace(0, 1, 97, dtype=np.float32), np.array([1e-7, 0.124999, 0.875001], F)])
+    out["sincos_u"] = us
+    out["sincos"] = np.array([pyref.sincos_turns(u) for u in us], np.float32)
+
+    # classic traversal on a 1,024-triangle sphere
+    v, f = scenes.fbm_sphere(4, seed=9)
+    nodes, prims = nb.build_bvh2_host(v, f)
+    mn, mx = nb.nodes_to_float(nodes[:1])
+    rays = scenes.uniform_rays(200, mn[0], mx[0], seed=9)
+    rays[:5, 3] = np.array([-0.5, 0.0, 1e-4, 0.3, 0.6], F)
+    rays[5:10, 7] = np.array([0.1, 0.2, 0.5, 1.0, 2.0], F)
+    hits = np.zeros((len(rays), 4), np.uint32)
+    any_hits = np.zeros((len(rays), 4), np.uint32)
+    for i, r in enumerate(rays):
+        for arr, flag in ((hits, False), (any_hits, True)):
+            t, u, vv, p = pyref.classic_intersect(nodes, prims, v, f, r, flag)
+            arr[i] = [F(t).view(np.uint32), F(u).view(np.uint32), F(vv).view(np.uint32), p]
+    out.update(mesh_v=v, mesh_f=f, bvh_nodes=nodes, bvh_prims=prims, classic_rays=rays, classic_hits=hits,
+               any_hits=any_hits)
+
+    # neural segments with the cut at depth 4 (inference epsilons and dilation)
+    neural = nb.build_neural_cut_host(nodes, 4)
+    nrays = rays[:120].copy()
+    nrays[:, 3] = F(1e-4)
+    segs = np.zeros((len(nrays), 32, 4), np.uint32)
+    counts = np.zeros(len(nrays), np.uint32)
+    for i, r in enumerate(nrays):
+        ss = pyref.neural_segments(neural, r, F(1e-5), F(1e-4), F(1e-3))
+        counts[i] = len(ss)
+        for k, (a, b, nd) in enumerate(ss[:32]):
+            segs[i, k] = [F(a).view(np.uint32), F(b).view(np.uint32), nd, 0]
+    out.update(neural_nodes=neural, neural_rays=nrays, neural_segments=segs, neural_counts=counts)
+
+    # hash-grid levels: 4 levels, 2^8 entries, base 4, scale 2 (two dense, two hashed)
+    offs, sizes, res, scl = [], [], [], []
+    o, p = 0, 1.0
+    for level in range(4):
+        s = F(4.0 * p - 1.0)
+        rr = int(np.ceil(s)) + 1
+        dense = rr ** 3
+        sz = min((dense + 7) // 8 * 8, 256)
+        offs.append(o)
+        sizes.append(sz)
+        res.append(rr)
+        scl.append(s)
+        o += sz
+        p *= 2.0
+    rng = np.random.default_rng(5)
+    grid = rng.uniform(-1, 1, (o, 2)).astype(np.float16).astype(np.float32)
+    pts = rng.uniform(-0.01, 1.01, (60, 3)).astype(np.float32)
+    feats = np.array([[pyref.encode_level(grid, offs[lv], sizes[lv], res[lv], scl[lv], q) for lv in range(4)]
+                      for q in pts], np.float32).reshape(60, 8)
+    out.update(grid_offsets=np.array(offs, np.uint32), grid_sizes=np.array(sizes, np.uint32),
+               grid_res=np.array(res, np.uint32), grid_scale=np.array(scl, np.float32), grid_values=grid,
+               grid_points=pts, grid_features=feats)
+
+    # LocalT depth decode
+    cases = rng.uniform(0, 1, (50, 3)).astype(np.float32)
+    dec = []
+    for k, (u, a, b) in enumerate(cases):
+        mint = F(a - 0.5) if k % 2 else F(a)
+        maxt = F(mint + F(b * 0.5) + F(0.01))
+        dec.append([u, mint, maxt, pyref.decode_local_t(u, mint, maxt, mint < 0)])
+    out["decode"] = np.array(dec, np.float32)
+
+    # losses: (kind, target, prediction) -> (loss, gradient)
+    kinds = ["L1", "L2", "RelativeL2", "BinaryCrossEntropy"]
+    lrows = []
+    for ki, kind in enumerate(kinds):
+        for t, pr in rng.uniform(0, 1, (25, 2)).astype(np.float32):
+            l, g = pyref.loss_and_gradient(kind, t, pr)
+            lrows.append([ki, t, pr, l, g])
+    out["losses"] = np.array(lrows, np.float32)
+    np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
+    print("wrote", os.path.join(HERE, "golden.npz"))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,312 @@
+"""Independent pure-Python restatement of reference functions on the N-BVH ray-query path, used
+only to generate the golden vectors in golden.npz (make_golden.py) that pin the C oracle.
+
+Every FP32 operation is a numpy float32 scalar operation (IEEE single, rounded per operation, no
+contraction); fused multiply-adds are evaluated in double and rounded to float32. Citations are
+file:line in the reference project.
+"""
+
+import numpy as np
+
+F = np.float32
+FLT_MAX = F(3.4028234663852886e38)
+M32 = 0xFFFFFFFF
+
+
+# ---- include/cuda/utils/lcg_rng.cuh:12-72 ----
+def murmur_mix(h, k):
+    k = (k * 0xCC9E2D51) & M32
+    k = ((k << 15) | (k >> 17)) & M32
+    k = (k * 0x1B873593) & M32
+    h ^= k
+    h = ((((h << 13) | (h >> 19)) & M32) * 5 + 0xE6546B64) & M32
+    return h
+
+
+def murmur_finalize(h):
+    h ^= h >> 16
+    h = (h * 0x85EBCA6B) & M32
+    h ^= h >> 13
+    h = (h * 0xC2B2AE35) & M32
+    h ^= h >> 16
+    return h
+
+
+def lcg_seed(index, frame, linear):
+    s = murmur_mix(0, linear)
+    s = murmur_mix(s, (512 * frame + index) & M32)
+    return murmur_finalize(s)
+
+
+class Rng:
+    def __init__(self, state):
+        self.state = state
+
+    def f(self):
+        self.state = (self.state * 1664525 + 1013904223) & M32
+        return F(F(self.state) * F(2.0 ** -32))
+
+
+def fma(a, b, c):
+    return F(float(a) * float(b) + float(c))
+
+
+def sincos_turns(u):
+    y = F(F(u) * F(8.0))
+    o = F(np.floor(y))
+    f = F(y - o)
+    oct_ = int(o) & 7
+    g = F(F(1.0) - f) if (oct_ & 1) else f
+    x = F(g * F(0.785398163397448310))
+    x2 = F(x * x)
+    ps = fma(x2, F(-2.50521084e-08), F(2.75573192e-06))
+    ps = fma(x2, ps, F(-1.98412698e-04))
+    ps = fma(x2, ps, F(8.33333333e-03))
+    ps = fma(x2, ps, F(-1.66666667e-01))
+    ps = fma(x2, ps, F(1.0))
+    sn = F(x * ps)
+    pc = fma(x2, F(2.08767570e-09), F(-2.75573192e-07))
+    pc = fma(x2, pc, F(2.48015873e-05))
+    pc = fma(x2, pc, F(-1.38888889e-03))
+    pc = fma(x2, pc, F(4.16666667e-02))
+    pc = fma(x2, pc, F(-0.5))
+    cs = fma(x2, pc, F(1.0))
+    table = {0: (sn, cs), 1: (cs, sn), 2: (cs, -sn), 3: (sn, -cs), 4: (-sn, -cs), 5: (-cs, -sn), 6: (-cs, sn),
+             7: (-sn, cs)}
+    s, c = table[oct_]
+    return F(s), F(c)
+
+
+# ---- glm-order vector helpers ----
+def sub(a, b):
+    return [F(a[i] - b[i]) for i in range(3)]
+
+
+def add(a, b):
+    return [F(a[i] + b[i]) for i in range(3)]
+
+
+def div(a, b):
+    with np.errstate(all="ignore"):
+        return [F(a[i] / b[i]) for i in range(3)]
+
+
+def scale(a, s):
+    return [F(a[i] * s) for i in range(3)]
+
+
+def dot(a, b):
+    return F(F(F(a[0] * b[0]) + F(a[1] * b[1])) + F(a[2] * b[2]))
+
+
+def cross(a, b):
+    return [F(F(a[1] * b[2]) - F(b[1] * a[2])), F(F(a[2] * b[0]) - F(b[2] * a[0])), F(F(a[0] * b[1]) - F(b[0] * a[1]))]
+
+
+def gmin(a, b):
+    return b if b < a else a
+
+
+def gmax(a, b):
+    return b if a < b else a
+
+
+def cmax(v):
+    return gmax(gmax(v[0], v[1]), v[2])
+
+
+def cmin(v):
+    return gmin(gmin(v[0], v[1]), v[2])
+
+
+def node_box(nodes, i):
+    f = nodes[i].view(np.float32)
+    return [F(f[0]), F(f[1]), F(f[2])], int(nodes[i][3]), [F(f[4]), F(f[5]), F(f[6])], int(nodes[i][7])
+
+
+# ---- include/base/accel/bvh.h:121-133, include/cuda/accel/bvh.cuh:98-136, bvh2.cuh:12-88 ----
+def box_entry(bmin, bmax, o, d, rmint, rmaxt):
+    t0 = div(sub(bmin, o), d)
+    t1 = div(sub(bmax, o), d)
+    mint = gmax(rmint, cmax([gmin(t0[i], t1[i]) for i in range(3)]))
+    maxt = gmin(rmaxt, cmin([gmax(t0[i], t1[i]) for i in range(3)]))
+    return mint if mint <= maxt else FLT_MAX
+
+
+def tri_intersect(verts, idx, prim, o, d, rmint, rmaxt):
+    ix = idx[prim]
+    v0 = [F(x) for x in verts[ix[0]]]
+    v1 = [F(x) for x in verts[ix[1]]]
+    v2 = [F(x) for x in verts[ix[2]]]
+    e1, e2 = sub(v1, v0), sub(v2, v0)
+    pvec = cross(d, e2)
+    det = dot(e1, pvec)
+    if F(-1e-8) < det < F(1e-8):
+        return None
+    inv = F(F(1.0) / det)
+    tvec = sub(o, v0)
+    u = F(dot(tvec, pvec) * inv)
+    if u < 0 or u > 1:
+        return None
+    qvec = cross(tvec, e1)
+    v = F(dot(d, qvec) * inv)
+    if v < 0 or F(u + v) > 1:
+        return None
+    t = F(dot(e2, qvec) * inv)
+    if t < rmint or t >= rmaxt:
+        return None
+    return t, u, v
+
+
+def classic_intersect(nodes, prims, verts, idx, ray, any_hit=False):
+    o = [F(x) for x in ray[0:3]]
+    d = [F(x) for x in ray[4:7]]
+    rmint, rmaxt = F(ray[3]), F(ray[7])
+    best = (FLT_MAX, F(0), F(0), M32)
+    stack = []
+    ni = 0
+    while True:
+        mn, cnt, mx, off = node_box(nodes, ni)
+        if cnt > 0:
+            done = False
+            for pid in range(off, off + cnt):
+                r = tri_intersect(verts, idx, int(prims[pid]), o, d, rmint, rmaxt)
+                if r is not None and r[0] < rmaxt:
+                    best = (r[0], r[1], r[2], int(prims[pid]))
+                    if any_hit:
+                        done = True
+                        break
+                    rmaxt = r[0]
+            if done or not stack:
+                return best
+            ni = stack.pop()
+            continue
+        c1, c2 = off, off + 1
+        m1, _, x1, _ = node_box(nodes, c1)
+        m2, _, x2, _ = node_box(nodes, c2)
+        d1 = box_entry(m1, x1, o, d, rmint, rmaxt)
+        d2 = box_entry(m2, x2, o, d, rmint, rmaxt)
+        if d1 > d2:
+            d1, d2, c1, c2 = d2, d1, c2, c1
+        if d1 == FLT_MAX:
+            if not stack:
+                return best
+            ni = stack.pop()
+        else:
+            ni = c1
+            if d2 != FLT_MAX:
+                stack.append(c2)
+
+
+# ---- include/cuda/neural/accel/neural_bvh2.cuh:80-86, 170-292 ----
+def dilated(nodes, i, dil):
+    mn, cnt, mx, off = node_box(nodes, i)
+    if dil != 0:
+        ext = sub(mx, mn)
+        c = add(mn, scale(ext, F(0.5)))
+        ne = scale(ext, F(F(1.0) + dil))
+        return sub(c, scale(ne, F(0.5))), add(c, scale(ne, F(0.5))), cnt, off
+    return mn, mx, cnt, off
+
+
+def neural_segments(nodes, ray, dil, mint_eps, maxt_eps, lod=0, stack_size=24):
+    o = [F(x) for x in ray[0:3]]
+    d = [F(x) for x in ray[4:7]]
+    rmint, rmaxt = -FLT_MAX, FLT_MAX
+    stack = [0]
+    out = []
+    while stack:
+        ni = stack.pop()
+        found = None
+        while True:
+            bmin, bmax, cnt, off = dilated(nodes, ni, dil)
+            if (0 < cnt <= 2 + lod) or off == M32:
+                t0 = div(sub(bmin, o), d)
+                t1 = div(sub(bmax, o), d)
+                mint = cmax([gmin(t0[i], t1[i]) for i in range(3)])
+                maxt = cmin([gmax(t0[i], t1[i]) for i in range(3)])
+                if mint <= maxt:
+                    valid = mint < rmaxt
+                    valid = valid and (maxt > maxt_eps if mint < 0 else mint > mint_eps)
+                    if valid:
+                        found = (mint, maxt, ni)
+                        break
+                if not stack:
+                    break
+                ni = stack.pop()
+                continue
+            c1, c2 = off, off + 1
+            b1 = dilated(nodes, c1, dil)
+            b2 = dilated(nodes, c2, dil)
+            d1 = box_entry(b1[0], b1[1], o, d, rmint, rmaxt)
+            d2 = box_entry(b2[0], b2[1], o, d, rmint, rmaxt)
+            if d1 > d2:
+                d1, d2, c1, c2 = d2, d1, c2, c1
+            if d1 == FLT_MAX:
+                if not stack:
+                    break
+                ni = stack.pop()
+            else:
+                ni = c1
+                if d2 != FLT_MAX:
+                    stack.append(c2)
+                    assert len(stack) < stack_size
+        if found is None:
+            break
+        out.append(found)
+    return out
+
+
+# ---- hash-grid level (tcnn HashGrid behaviour, coherent prime hash) ----
+def encode_level(grid, offset, size, res, scale_l, p):
+    pos = [fma(F(p[i]), F(scale_l), F(0.5)) for i in range(3)]
+    g = [int(np.floor(x)) for x in pos]
+    fr = [F(pos[i] - F(np.floor(pos[i]))) for i in range(3)]
+    a0, a1 = F(0), F(0)
+    dense = res ** 3 <= size
+    for c in range(8):
+        x, y, z = (g[0] + (c & 1)) & M32, (g[1] + ((c >> 1) & 1)) & M32, (g[2] + ((c >> 2) & 1)) & M32
+        if dense:
+            idx = (x + y * res + z * res * res) & M32
+        else:
+            idx = x ^ ((y * 2654435761) & M32) ^ ((z * 805459861) & M32)
+        idx %= size
+        w = F(F((fr[0] if c & 1 else F(F(1) - fr[0])) * (fr[1] if c & 2 else F(F(1) - fr[1]))) *
+              (fr[2] if c & 4 else F(F(1) - fr[2])))
+        a0 = fma(w, grid[offset + idx, 0], a0)
+        a1 = fma(w, grid[offset + idx, 1], a1)
+    return a0, a1
+
+
+# ---- include/cuda/neural/neural_bvh_module_common.cuh:23-58 (LocalT) ----
+def decode_local_t(out_depth, mint, maxt, inside, depth_epsilon=F(0.2), fixed_depth_epsilon=F(1e-5)):
+    seg_len = F(F(maxt) - F(mint))
+    u = gmin(gmax(F(out_depth), F(0)), F(1))
+    if inside:
+        if depth_epsilon != 1:
+            inward = F(float(u) * (float(seg_len) + 1e-3))
+            if inward < F(F(F(maxt) - F(seg_len * depth_epsilon)) - fixed_depth_epsilon):
+                return F(F(maxt) - inward)
+        return FLT_MAX
+    return F(float(u) * (float(seg_len) + 1e-3) + float(mint))
+
+
+# ---- include/cuda/neural/utils/loss_gradient.cuh:25-94 ----
+def loss_and_gradient(kind, target, pred):
+    target, pred = F(target), F(pred)
+    if kind == "L1":
+        diff = F(pred - target)
+        return F(abs(diff)), F(np.copysign(F(1), diff))
+    if kind == "L2":
+        diff = F(pred - target)
+        return F(diff * diff), F(F(2) * diff)
+    if kind == "RelativeL2":
+        diff = F(pred - target)
+        den = F(F(pred * pred) + F(1e-2))
+        return F(F(diff * diff) / den), F(F(F(2) * diff) / den)
+    if kind == "BinaryCrossEntropy":
+        p = min(max(pred, F(1e-5)), F(F(1) - F(1e-5)))
+        loss = -(float(target) * np.log(float(p)) + (1 - float(target)) * np.log(1 - float(p)))
+        grad = F(-F(target - p) / F(p - F(p * p)))
+        return F(loss), grad
+    raise KeyError(kind)

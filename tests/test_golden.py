@@ -1,0 +1,89 @@
+"""Pins the C oracle to the golden vectors of the independent Python restatement
+(tests/golden/pyref.py -> golden.npz): RNG, sin/cos, classic closest/any hit, neural segments,
+hash-grid features, LocalT decode and the composite-loss terms."""
+
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from oracle.bindings import Network
+
+G = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden.npz"))
+
+
+def test_rng_streams(oracle):
+    for seed, stream in zip(G["rng_seeds"], G["rng_streams"]):
+        got = oracle.lcg_stream(int(seed[0]), int(seed[1]), int(seed[2]), 6)
+        assert np.array_equal(got.view(np.uint32), stream.view(np.uint32))
+
+
+def test_sincos(oracle):
+    for u, (s, c) in zip(G["sincos_u"], G["sincos"]):
+        gs, gc = oracle.sincos_turns(float(u))
+        assert abs(gs - s) <= 1e-7 and abs(gc - c) <= 1e-7
+        assert abs(gs - np.sin(2 * np.pi * float(u))) < 2e-7
+        assert abs(gc - np.cos(2 * np.pi * float(u))) < 2e-7
+
+
+def test_classic(oracle):
+    cs = oracle.classic_scene(G["bvh_nodes"], G["bvh_prims"], G["mesh_v"], G["mesh_f"])
+    assert np.array_equal(oracle.classic_query(cs, G["classic_rays"]), G["classic_hits"])
+    assert np.array_equal(oracle.classic_query(cs, G["classic_rays"], any_hit=True), G["any_hits"])
+    assert (G["classic_hits"][:, 3] != 0xFFFFFFFF).sum() > 30
+
+
+def test_neural_segments(oracle):
+    import nbvh_gb300 as nb
+    consts = oracle.neural_consts(nb.default_config())
+    segs, counts = oracle.neural_segments(G["neural_nodes"], consts, G["neural_rays"], 32)
+    assert np.array_equal(counts, G["neural_counts"])
+    for i, c in enumerate(counts):
+        assert np.array_equal(segs[i, :c, :3], G["neural_segments"][i, :c, :3])
+    assert counts.max() >= 2
+
+
+def test_grid_features(oracle):
+    off, size, res, scl = G["grid_offsets"], G["grid_sizes"], G["grid_res"], G["grid_scale"]
+    g16 = np.ascontiguousarray(G["grid_values"].astype(np.float16).view(np.uint16))
+    w16 = np.zeros(16, np.uint16)
+    net = Network()
+    net.n_levels, net.n_points, net.n_inputs, net.n_neurons, net.n_hidden_layers = 4, 1, 8, 64, 1
+    keep = [off, size, res, scl, g16, w16]
+    net.level_offset, net.level_size = off.ctypes.data, size.ctypes.data
+    net.level_resolution, net.level_scale = res.ctypes.data, scl.ctypes.data
+    net.grid_f16, net.weights_f16 = g16.ctypes.data, w16.ctypes.data
+    feats = oracle.encode(net, G["grid_points"].reshape(-1, 1, 3))
+    assert np.array_equal(feats.view(np.uint32), G["grid_features"].view(np.uint32))
+    del keep
+
+
+def test_decode_local_t(oracle):
+    lib = oracle.lib
+    # the oracle's decode is internal; exercise it through a one-segment neural query is heavy, so
+    # the decode golden values are checked against the C restatement compiled into a helper
+    fn = getattr(lib, "orc_decode_local_t", None)
+    if fn is None:
+        pytest.skip("decode helper not exported")
+    fn.restype = C.c_float
+    fn.argtypes = [C.c_float, C.c_float, C.c_float, C.c_int, C.c_float, C.c_float]
+    for u, a, b, ref in G["decode"]:
+        got = fn(float(u), float(a), float(b), int(a < 0), 0.2, 1e-5)
+        assert np.float32(got).view(np.uint32) == np.float32(ref).view(np.uint32)
+
+
+def test_losses(oracle):
+    import nbvh_gb300 as nb
+    kinds = {0: 3, 1: 1, 2: 0, 3: 5}  # golden kind index -> nbvh loss enum (L1, L2, RelativeL2, BCE)
+    cfg = nb.default_config()
+    for ki, t, p, loss, grad in G["losses"]:
+        lc = oracle.loss_consts(cfg)
+        lc.visibility_loss = kinds[int(ki)]
+        pred = np.zeros((1, 16), np.float32)
+        tgt = np.zeros((1, 8), np.float32)
+        pred[0, 0], tgt[0, 0] = p, t
+        vals, grads = oracle.composite_loss(lc, pred, tgt)
+        dims = 8.0
+        assert abs(vals[0, 0] * dims - loss) <= 2e-6 * max(1.0, abs(loss))
+        assert abs(grads[0, 0] * dims - grad) <= 2e-6 * max(1.0, abs(grad))

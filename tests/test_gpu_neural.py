@@ -1,0 +1,205 @@
+"""K2/K3/K4 inference on the GPU against the CPU oracle.
+
+* N-BVH traversal (NeuralBVH2::intersect, include/cuda/neural/accel/neural_bvh2.cuh:170-292):
+  entered segments bit-identical.
+* Hash-grid encoding: features bit-identical (same FMA order).
+* Fused MLP: outputs within 5e-3 absolute of the FP64-accumulated oracle with the same FP16
+  rounding of features and hidden activations.
+* Full neural query (path_module.cu:54-137, path_inference_kernels.cu:61-131): hit decisions equal
+  except on rays where a visibility output lies within 1e-2 of the threshold; depth within 1e-3
+  relative on rays that hit in both.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import nbvh_gb300 as nb
+from helpers import as_u32, handle
+from nbvh_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _cuda(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _spread_params(h, seed=0):
+    """Parameters with outputs spread over (0, 1): larger grid entries and weights."""
+    rng = np.random.default_rng(seed)
+    p = h.params()
+    nn = h.layout.n_network_params
+    p[:nn] *= 2.5
+    p[nn:] = rng.uniform(-1.0, 1.0, p.size - nn).astype(np.float32)
+    h.set_params(p)
+    return p
+
+
+@pytest.fixture(scope="module")
+def scene(built):
+    h, s = handle(kind="sphere65k", seed=1, albedo=True)
+    s["params"] = _spread_params(h)
+    yield h, s
+    h.close()
+
+
+def test_segments_bit_exact(scene, oracle):
+    h, s = scene
+    rays = scenes.uniform_rays(1 << 15, s["bbox"][:3], s["bbox"][3:], seed=31)
+    segs, counts = h.query_segments(_cuda(rays), 64)
+    consts = oracle.neural_consts(h.cfg)
+    rsegs, rcounts = oracle.neural_segments(s["neural"], consts, rays, 64)
+    counts = counts.cpu().numpy().view(np.uint32)
+    assert np.array_equal(counts, rcounts)
+    segs = as_u32(segs)
+    for i in range(len(rays)):
+        k = min(counts[i], 64)
+        assert np.array_equal(segs[i, :k, :3], rsegs[i, :k, :3])
+    assert rcounts.max() > 1
+
+
+def test_encoding_bit_exact(scene, oracle):
+    h, s = scene
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(-0.01, 1.01, (4096, h.cfg.module.input_segment_points, 3)).astype(np.float32)
+    got = h.encode(_cuda(pos)).cpu().numpy()
+    net = oracle.network(h.cfg, h.layout, s["params"])
+    ref = oracle.encode(net, pos)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_network_inference(scene, oracle):
+    h, s = scene
+    rng = np.random.default_rng(4)
+    pos = rng.uniform(0.0, 1.0, (8192, h.cfg.module.input_segment_points, 3)).astype(np.float32)
+    got = h.network_inference(_cuda(pos)).cpu().numpy()
+    net = oracle.network(h.cfg, h.layout, s["params"])
+    ref = oracle.network_inference(net, pos, threads=8)[:, :8]
+    assert ref.std() > 0.05
+    assert np.max(np.abs(got - ref)) < 5e-3
+
+
+def _compare_queries(got, ref, thr_margin_rays):
+    flags_g, flags_r = got[:, 8] & 1, ref[:, 8] & 1
+    differ = flags_g != flags_r
+    # decisions may differ where a visibility output was borderline in the oracle; elsewhere only
+    # through a decoded depth sitting on the inside-node acceptance bound (rare)
+    assert (differ & ~thr_margin_rays).mean() < 1e-3, np.where(differ & ~thr_margin_rays)[0][:10]
+    assert differ.mean() < 2e-3
+    both = (flags_g == 1) & (flags_r == 1) & ~thr_margin_rays
+    tg, tr = got[both, 0].view(np.float32), ref[both, 0].view(np.float32)
+    rel = np.abs(tg - tr) / np.maximum(np.abs(tr), 1e-6)
+    assert np.mean(rel <= 1e-3) > 0.998
+    return both
+
+
+def _borderline(h, oracle, s, rays, margin=1e-2):
+    """Rays for which any evaluated segment's visibility lies within margin of the threshold
+    (computed by re-running the oracle query with the fallback margin)."""
+    net = oracle.network(h.cfg, h.layout, s["params"])
+    consts = oracle.neural_consts(h.cfg)
+    nscene = oracle.neural_scene(s["neural"], s["bbox"])
+    cs = oracle.classic_scene(s["nodes"], s["prims"], s["v"], s["f"])
+    fb = oracle.neural_query(nscene, net, consts, rays, classic=cs, fallback_margin=margin, threads=8)
+    return (fb[:, 8] & 2) != 0
+
+
+def test_neural_query_matches_oracle(scene, oracle):
+    h, s = scene
+    rays = scenes.uniform_rays(1 << 15, s["bbox"][:3], s["bbox"][3:], seed=32)
+    got = as_u32(h.query_closest_neural(_cuda(rays)))
+    net = oracle.network(h.cfg, h.layout, s["params"])
+    consts = oracle.neural_consts(h.cfg)
+    nscene = oracle.neural_scene(s["neural"], s["bbox"])
+    ref = oracle.neural_query(nscene, net, consts, rays, threads=8)
+    border = _borderline(h, oracle, s, rays)
+    both = _compare_queries(got, ref, border)
+    assert both.sum() > 100
+    same = ~border
+    assert np.mean(got[same, 9] == ref[same, 9]) > 0.998  # segments evaluated
+    st = h.query_stats()
+    assert st.segments == int(got[:, 9].astype(np.int64).sum())
+    assert st.step_capped == 0 and st.stack_overflow == 0
+
+
+def test_visibility_query_and_secondary_threshold(scene, oracle):
+    h, s = scene
+    rays = scenes.uniform_rays(1 << 14, s["bbox"][:3], s["bbox"][3:], seed=33)
+    net = oracle.network(h.cfg, h.layout, s["params"])
+    consts = oracle.neural_consts(h.cfg)
+    nscene = oracle.neural_scene(s["neural"], s["bbox"])
+    border = _borderline(h, oracle, s, rays)
+    got = as_u32(h.query_visibility_neural(_cuda(rays)))
+    ref = oracle.neural_query(nscene, net, consts, rays, visibility_only=True, threads=8)
+    differ = (got[:, 8] & 1) != (ref[:, 8] & 1)
+    assert np.all(~differ | border)
+    got2 = as_u32(h.query_closest_neural(_cuda(rays), depth=2))
+    ref2 = oracle.neural_query(nscene, net, consts, rays, depth=2, threads=8)
+    _compare_queries(got2, ref2, border)
+
+
+def test_ignore_neural_blas_switch(scene, oracle):
+    h, s = scene
+    rays = scenes.uniform_rays(1 << 14, s["bbox"][:3], s["bbox"][3:], seed=34)
+    h.set_ignore_neural_blas(True)
+    try:
+        got = as_u32(h.query_closest_neural(_cuda(rays)))
+    finally:
+        h.set_ignore_neural_blas(False)
+    cs = oracle.classic_scene(s["nodes"], s["prims"], s["v"], s["f"])
+    ref = oracle.classic_query(cs, rays)
+    assert np.array_equal(got[:, 0], ref[:, 0])
+    assert np.array_equal(got[:, 10], ref[:, 3])
+    hit = ref[:, 3] != 0xFFFFFFFF
+    assert np.all((got[hit, 8] & 3) == 3) and np.all((got[~hit, 8] & 1) == 0)
+
+
+def test_confidence_fallback_and_non_neural_leaves(built, oracle):
+    cfg = nb.default_config(fallback_margin=0.05)
+    h, s = handle(cfg, kind="sphere65k", seed=1)
+    try:
+        s["params"] = _spread_params(h, seed=5)
+        leaves = np.where(s["neural"][:, 3] > 0)[0]
+        marked = leaves[::7]
+        h.set_non_neural_leaves(marked)
+        flags = np.zeros(len(s["neural"]), np.uint8)
+        flags[marked] = 1
+        rays = scenes.uniform_rays(1 << 14, s["bbox"][:3], s["bbox"][3:], seed=35)
+        got = as_u32(h.query_closest_neural(_cuda(rays)))
+        net = oracle.network(h.cfg, h.layout, s["params"])
+        consts = oracle.neural_consts(h.cfg)
+        nscene = oracle.neural_scene(s["neural"], s["bbox"], flags)
+        cs = oracle.classic_scene(s["nodes"], s["prims"], s["v"], s["f"])
+        ref = oracle.neural_query(nscene, net, consts, rays, classic=cs, fallback_margin=0.05, threads=8)
+        fb_g, fb_r = (got[:, 8] & 2) != 0, (ref[:, 8] & 2) != 0
+        assert fb_r.sum() > 100
+        assert np.mean(fb_g == fb_r) > 0.995
+        both = fb_g & fb_r
+        # classic answers are bit-exact
+        assert np.array_equal(got[both, 0], ref[both, 0])
+        assert np.array_equal(got[both, 10], ref[both, 10])
+        assert h.query_stats().fallback == int(fb_g.sum())
+    finally:
+        h.close()
+
+
+def test_host_pipeline_matches_device(scene):
+    h, s = scene
+    rays = scenes.uniform_rays((1 << 20) + 12345, s["bbox"][:3], s["bbox"][3:], seed=36)
+    dev = as_u32(h.query_closest_neural(_cuda(rays)))
+    host = h.query_closest_neural_host(rays)
+    assert np.array_equal(host.view(np.uint32).reshape(-1, 12), dev)
+
+
+def test_run_inference_camera(scene, oracle):
+    h, s = scene
+    org, tgt, up = scenes.orbit_camera(s["bbox"][:3], s["bbox"][3:], seed=6)
+    req = nb.render_request(128, 96, org, tgt, up, 45.0, sample_idx=3, sample_offset=1)
+    rays = h.camera_rays(req).cpu().numpy()
+    ref_rays = oracle.camera_rays(req)
+    assert np.array_equal(rays.view(np.uint32), ref_rays.view(np.uint32))
+    img = as_u32(h.run_inference(req))
+    q = as_u32(h.query_closest_neural(_cuda(ref_rays)))
+    assert np.array_equal(img, q)
+    assert (img[:, 8] & 1).sum() > 100
