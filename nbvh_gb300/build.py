@@ -21,7 +21,10 @@ SOURCES = [
     "bvh_builder.cpp",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "-I", os.path.join(HERE, "..", "include")]
+# host code: no FMA contraction (aarch64 GCC contracts a*b+c by default), so that host-side
+# precomputation (dilated boxes, camera frames) rounds exactly like the device intrinsics
+COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O3,-ffp-contract=off",
+          "-I", os.path.join(HERE, "..", "include")]
 
 
 def _nvcc():

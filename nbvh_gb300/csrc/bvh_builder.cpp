@@ -267,4 +267,71 @@ void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std
     }
 }
 
+bool coords_in_fast_div_domain(const float *c, size_t n)
+{
+    for (size_t i = 0; i < n; i++) {
+        uint32_t bits;
+        std::memcpy(&bits, &c[i], 4);
+        if (bits == 0u)
+            continue; // +0
+        const float a = std::fabs(c[i]);
+        if (!(a >= 0x1p-60f && a <= 0x1p11f))
+            return false; // -0, tiny, huge, inf or nan
+    }
+    return true;
+}
+
+bool nodes_in_fast_div_domain(const std::vector<BVHNode> &nodes)
+{
+    for (const BVHNode &n : nodes)
+        if (!coords_in_fast_div_domain(n.min, 3) || !coords_in_fast_div_domain(n.max, 3))
+            return false;
+    return true;
+}
+
+// Inference copy of the neural cut: every node box dilated once by `dil` with the FP32 operations
+// of intersect_primitive_min_max / intersect_traversal_bbox (include/cuda/neural/accel/
+// neural_bvh2.cuh:80-86, 101-107; centre = min + extent * 0.5, extent * (1 + dil)), and per node the
+// union of the dilated boxes of the leaves below it (the traversal culls a subtree whose union is
+// entirely behind the origin or beyond the current closest hit; such a subtree holds no leaf the
+// reference would accept, so the accepted segments and their order are unchanged).
+void build_inference_nodes(const std::vector<BVHNode> &neural, float dil, std::vector<BVHNode> &dilated,
+                           std::vector<float> &bounds)
+{
+    const size_t n = neural.size();
+    dilated = neural;
+    if (dil != 0.0f) {
+        const float scale = 1.0f + dil;
+        for (size_t i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) {
+                const float mn = neural[i].min[k], mx = neural[i].max[k];
+                const float ext = mx - mn;
+                const float center = mn + ext * 0.5f;
+                const float next = ext * scale;
+                dilated[i].min[k] = center - next * 0.5f;
+                dilated[i].max[k] = center + next * 0.5f;
+            }
+    }
+    bounds.assign(8u * n, 0.0f);
+    // children are allocated after their parent: a reverse sweep sees children first
+    for (size_t ii = n; ii-- > 0;) {
+        float *b = &bounds[8u * ii];
+        const BVHNode &d = dilated[ii];
+        const bool leaf = neural[ii].prim_count > 0u || neural[ii].left_or_prim_offset == kNoNeuralChild;
+        if (leaf) {
+            for (int k = 0; k < 3; k++) {
+                b[k] = d.min[k];
+                b[4 + k] = d.max[k];
+            }
+        } else {
+            const float *l = &bounds[8u * neural[ii].left_or_prim_offset];
+            const float *r = &bounds[8u * (neural[ii].left_or_prim_offset + 1u)];
+            for (int k = 0; k < 3; k++) {
+                b[k] = std::min(l[k], r[k]);
+                b[4 + k] = std::max(l[4 + k], r[4 + k]);
+            }
+        }
+    }
+}
+
 } // namespace nbvh

@@ -139,11 +139,68 @@ __device__ __forceinline__ NodeBox load_node(const float4 *nodes, uint32_t idx)
     return n;
 }
 
+// Ray prepared for slab tests: the direction, its correctly rounded reciprocal and whether the
+// divisions (b - o) / d may use Markstein's correctly rounded division from a correctly rounded
+// reciprocal (P. Markstein, "IA-64 and Elementary Functions", 2000: with y = RN(1/d),
+// q0 = RN(a*y), r = a - d*q0 (exact by FMA), RN(q0 + r*y) = RN(a/d) when nothing overflows or
+// underflows). It holds here when |d_i| is in [2^-60, 2^4], o_i is 0 or |o_i| in [2^-60, 2^11]
+// and every box coordinate is +0 or has magnitude in [2^-60, 2^11] (checked on the host for
+// the scene): then a = b - o is +0 or |a| in [2^-83, 2^12], and the quotient is normal. Outside
+// that domain the IEEE division is used. Both give the bits of the IEEE quotient.
+struct RayDiv {
+    V3 d, inv;
+    bool fast;
+};
+
+__device__ __forceinline__ bool coord_ok(float x)
+{
+    const float ax = fabsf(x);
+    return x == 0.0f || (ax >= 0x1p-60f && ax <= 0x1p11f);
+}
+
+__device__ __forceinline__ RayDiv make_raydiv(V3 o, V3 d, bool scene_ok)
+{
+    RayDiv r;
+    r.d = d;
+    auto dir_ok = [](float x) {
+        const float ax = fabsf(x);
+        return ax >= 0x1p-60f && ax <= 0x1p4f;
+    };
+    r.fast = scene_ok && dir_ok(d.x) && dir_ok(d.y) && dir_ok(d.z) && coord_ok(o.x) && coord_ok(o.y) && coord_ok(o.z);
+    r.inv = r.fast ? mk3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z)) : mk3(0.f, 0.f, 0.f);
+    return r;
+}
+
+__device__ __forceinline__ float markstein_div(float a, float b, float y)
+{
+    const float q0 = __fmul_rn(a, y);
+    const float r = __fmaf_rn(-q0, b, a);
+    return __fmaf_rn(r, y, q0);
+}
+
+__device__ __forceinline__ V3 div3r(V3 a, const RayDiv &r)
+{
+    if (r.fast)
+        return mk3(markstein_div(a.x, r.d.x, r.inv.x), markstein_div(a.y, r.d.y, r.inv.y),
+                   markstein_div(a.z, r.d.z, r.inv.z));
+    return div3(a, r.d);
+}
+
 // BVH2Node::intersect, include/base/accel/bvh.h:121-133
 __device__ __forceinline__ float box_entry(V3 bmin, V3 bmax, V3 o, V3 d, float rmint, float rmaxt)
 {
     V3 t0 = div3(sub3(bmin, o), d);
     V3 t1 = div3(sub3(bmax, o), d);
+    float mint = gmax(rmint, cmax3(min3(t0, t1)));
+    float maxt = gmin(rmaxt, cmin3(max3(t0, t1)));
+    return (mint <= maxt) ? mint : FLT_MAX;
+}
+
+// BVH2Node::intersect with the prepared-ray division (bit-identical quotients)
+__device__ __forceinline__ float box_entry(V3 bmin, V3 bmax, V3 o, const RayDiv &rd, float rmint, float rmaxt)
+{
+    V3 t0 = div3r(sub3(bmin, o), rd);
+    V3 t1 = div3r(sub3(bmax, o), rd);
     float mint = gmax(rmint, cmax3(min3(t0, t1)));
     float maxt = gmin(rmaxt, cmin3(max3(t0, t1)));
     return (mint <= maxt) ? mint : FLT_MAX;
@@ -207,12 +264,14 @@ __device__ __forceinline__ bool tri_intersect(V3 v0, V3 e1, V3 e2, V3 o, V3 d, f
 template <bool ANY_HIT>
 __device__ __forceinline__ void classic_traverse(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, V3 o,
                                                  V3 d, float rmint, float rmaxt, float &best_t, float &best_u,
-                                                 float &best_v, uint32_t &best_prim, uint32_t *best_rec = nullptr)
+                                                 float &best_v, uint32_t &best_prim, uint32_t *best_rec = nullptr,
+                                                 bool scene_fast_div = false)
 {
     best_t = FLT_MAX;
     best_u = 0.f;
     best_v = 0.f;
     best_prim = 0xFFFFFFFFu;
+    const RayDiv rd = make_raydiv(o, d, scene_fast_div);
     uint32_t stack[32];
     int sp = 0;
     NodeBox node = load_node(nodes, 0);
@@ -249,8 +308,8 @@ __device__ __forceinline__ void classic_traverse(const float4 *__restrict__ node
         // both children are adjacent: four 128-bit loads
         NodeBox n1 = load_node(nodes, c1);
         NodeBox n2 = load_node(nodes, c2);
-        float d1 = box_entry(n1.mn, n1.mx, o, d, rmint, rmaxt);
-        float d2 = box_entry(n2.mn, n2.mx, o, d, rmint, rmaxt);
+        float d1 = box_entry(n1.mn, n1.mx, o, rd, rmint, rmaxt);
+        float d2 = box_entry(n2.mn, n2.mx, o, rd, rmint, rmaxt);
         if (d1 > d2) {
             float td = d1;
             d1 = d2;
@@ -338,6 +397,184 @@ __device__ __forceinline__ int neural_intersect(const float4 *__restrict__ nodes
                 if (sp >= 24)
                     return -1;
             }
+        }
+    }
+}
+
+// Raw slab of a box: entry = max_i min(t0_i, t1_i), exit = min_i max(t0_i, t1_i) with the
+// glm operation order of Ray3f::intersect_bbox_min_max (include/cuda/base/ray.cuh:111-132).
+__device__ __forceinline__ void slab_raw(V3 bmin, V3 bmax, V3 o, V3 d, float &entry, float &exit_)
+{
+    V3 t0 = div3(sub3(bmin, o), d);
+    V3 t1 = div3(sub3(bmax, o), d);
+    entry = cmax3(min3(t0, t1));
+    exit_ = cmin3(max3(t0, t1));
+}
+
+__device__ __forceinline__ void slab_raw(V3 bmin, V3 bmax, V3 o, const RayDiv &rd, float &entry, float &exit_)
+{
+    V3 t0 = div3r(sub3(bmin, o), rd);
+    V3 t1 = div3r(sub3(bmax, o), rd);
+    entry = cmax3(min3(t0, t1));
+    exit_ = cmin3(max3(t0, t1));
+}
+
+// Leaf acceptance of NeuralBVH2::intersect (neural_bvh2.cuh:199-215) from the raw slab.
+__device__ __forceinline__ bool leaf_accepts(float entry, float exit_, float rmaxt, float mint_eps, float maxt_eps)
+{
+    if (!(entry <= exit_))
+        return false;
+    bool valid = entry < rmaxt;
+    if (entry < 0.0f)
+        valid &= exit_ > maxt_eps;
+    else
+        valid &= entry > mint_eps;
+    return valid;
+}
+
+// NeuralBVH2::intersect for inference on a pre-dilated copy of the cut (`nodes` boxes already
+// dilated by fixed_node_dilation with the reference's operations). Returns the same accepted leaf
+// segments in the same order as the reference; it differs only in work skipped:
+//  * the slab of the child it descends into is carried over instead of recomputed;
+//  * a child is not pushed / entered when nothing below it can be accepted: a leaf that fails the
+//    acceptance test now (the bound rmaxt only shrinks later), or an interior node whose union of
+//    dilated leaf boxes (`bounds`) lies entirely at t <= min(mint_eps, maxt_eps), beyond rmaxt, or
+//    is missed. The slab is monotone in the box bounds for non-zero direction components, so a leaf
+//    inside the union exits no later and enters no earlier than the union (`cull_ok` is false for
+//    rays with a zero direction component).
+// Node sources of the inference traversal: the pre-dilated cut and its subtree bounds, read from
+// global memory (read-only cache) or from a shared-memory copy staged at kernel start.
+struct GlobalCut {
+    const float4 *nodes;  // 2 float4 per node
+    const float4 *bounds; // 2 float4 per node: {min, 0}, {max, 0}
+    __device__ __forceinline__ NodeBox node(uint32_t i) const { return load_node(nodes, i); }
+    __device__ __forceinline__ void bound(uint32_t i, V3 &mn, V3 &mx) const
+    {
+        const float4 a = __ldg(bounds + 2u * i), b = __ldg(bounds + 2u * i + 1u);
+        mn = mk3(a.x, a.y, a.z);
+        mx = mk3(b.x, b.y, b.z);
+    }
+};
+
+struct SharedCut {
+    const float4 *nodes;  // shared memory, 2 float4 per node
+    const float2 *bounds; // shared memory, 3 float2 per node: min.xy, min.z max.x, max.yz
+    __device__ __forceinline__ NodeBox node(uint32_t i) const
+    {
+        const float4 a = nodes[2u * i], b = nodes[2u * i + 1u];
+        NodeBox n;
+        n.mn = mk3(a.x, a.y, a.z);
+        n.count = __float_as_uint(a.w);
+        n.mx = mk3(b.x, b.y, b.z);
+        n.offset = __float_as_uint(b.w);
+        return n;
+    }
+    __device__ __forceinline__ void bound(uint32_t i, V3 &mn, V3 &mx) const
+    {
+        const float2 a = bounds[3u * i], b = bounds[3u * i + 1u], c = bounds[3u * i + 2u];
+        mn = mk3(a.x, a.y, b.x);
+        mx = mk3(b.y, c.x, c.y);
+    }
+};
+
+template <typename Src, typename Stack>
+__device__ __forceinline__ int neural_intersect_inference(const Src &src, uint32_t lod, V3 o, const RayDiv &d,
+                                                          bool cull_ok, Stack &stack, int &sp, float mint_eps,
+                                                          float maxt_eps, float current_maxt, float &seg_mint,
+                                                          float &seg_maxt, uint32_t &seg_node)
+{
+    const float rmint = -FLT_MAX, rmaxt = current_maxt;
+    const float cull_eps = gmin(mint_eps, maxt_eps);
+    uint32_t node_idx = stack[--sp];
+    NodeBox node = src.node(node_idx);
+    bool have_slab = false;
+    float cur_e = 0.f, cur_x = 0.f;
+    for (;;) {
+        const bool leaf = (node.count > 0u && node.count <= 2u + lod) || node.offset == 0xFFFFFFFFu;
+        if (leaf) {
+            if (!have_slab)
+                slab_raw(node.mn, node.mx, o, d, cur_e, cur_x);
+            if (leaf_accepts(cur_e, cur_x, rmaxt, mint_eps, maxt_eps)) {
+                seg_mint = cur_e;
+                seg_maxt = cur_x;
+                seg_node = node_idx;
+                return 1;
+            }
+            if (sp == 0)
+                return 0;
+            node_idx = stack[--sp];
+            node = src.node(node_idx);
+            have_slab = false;
+            continue;
+        }
+        uint32_t c1 = node.offset, c2 = node.offset + 1u;
+        NodeBox n1 = src.node(c1);
+        NodeBox n2 = src.node(c2);
+        float e1, x1, e2, x2;
+        slab_raw(n1.mn, n1.mx, o, d, e1, x1);
+        slab_raw(n2.mn, n2.mx, o, d, e2, x2);
+        // intersect_traversal_bbox with check_ray_bounds (neural_bvh2.cuh:94-115)
+        float m1 = gmax(rmint, e1), m2 = gmax(rmint, e2);
+        float d1 = (m1 <= gmin(rmaxt, x1)) ? m1 : FLT_MAX;
+        float d2 = (m2 <= gmin(rmaxt, x2)) ? m2 : FLT_MAX;
+        if (d1 > d2) {
+            float t = d1;
+            d1 = d2;
+            d2 = t;
+            uint32_t tc = c1;
+            c1 = c2;
+            c2 = tc;
+            NodeBox tn = n1;
+            n1 = n2;
+            n2 = tn;
+            t = e1;
+            e1 = e2;
+            e2 = t;
+            t = x1;
+            x1 = x2;
+            x2 = t;
+        }
+        auto alive = [&](const NodeBox &nb, uint32_t ci, float e, float x, float dd) -> bool {
+            if (dd == FLT_MAX)
+                return false;
+            const bool cleaf = (nb.count > 0u && nb.count <= 2u + lod) || nb.offset == 0xFFFFFFFFu;
+            if (cleaf)
+                return leaf_accepts(e, x, rmaxt, mint_eps, maxt_eps);
+            if (cull_ok && x <= cull_eps) {
+                V3 umn, umx;
+                src.bound(ci, umn, umx);
+                float ue, ux;
+                slab_raw(umn, umx, o, d, ue, ux);
+                if (!(ue <= ux) || ux <= cull_eps || ue >= rmaxt)
+                    return false;
+            }
+            return true;
+        };
+        const bool a1 = alive(n1, c1, e1, x1, d1);
+        const bool a2 = alive(n2, c2, e2, x2, d2);
+        if (a1) {
+            node_idx = c1;
+            node = n1;
+            cur_e = e1;
+            cur_x = x1;
+            have_slab = true;
+            if (a2) {
+                stack[sp++] = c2;
+                if (sp >= 24)
+                    return -1;
+            }
+        } else if (a2) {
+            node_idx = c2;
+            node = n2;
+            cur_e = e2;
+            cur_x = x2;
+            have_slab = true;
+        } else {
+            if (sp == 0)
+                return 0;
+            node_idx = stack[--sp];
+            node = src.node(node_idx);
+            have_slab = false;
         }
     }
 }

@@ -206,6 +206,7 @@ NeuralConsts make_neural_consts(const nbvh_handle *h, uint32_t depth, bool visib
     nc.bvh_lod = 0u; // rendered_lod
     nc.max_traversal_steps = c.max_traversal_steps;
     nc.visibility_only = visibility_only ? 1u : 0u;
+    nc.fast_div_ok = h->neural_fast_div ? 1u : 0u;
     return nc;
 }
 
@@ -252,6 +253,7 @@ void require(bool cond, nbvh_status s, const char *msg)
 void upload_bvh(nbvh_handle *h)
 {
     // nodes: two float4 per node in the reference layout
+    h->classic_fast_div = nodes_in_fast_div_domain(h->nodes);
     cuda_check(h->d_nodes.resize(2u * h->nodes.size()), "alloc nodes");
     cuda_check(cudaMemcpy(h->d_nodes.ptr, h->nodes.data(), h->nodes.size() * sizeof(BVHNode), cudaMemcpyHostToDevice),
                "upload nodes");
@@ -295,6 +297,17 @@ void upload_neural(nbvh_handle *h)
     cuda_check(cudaMemcpy(h->d_neural_nodes.ptr, h->neural_nodes.data(), h->neural_nodes.size() * sizeof(BVHNode),
                           cudaMemcpyHostToDevice),
                "upload neural nodes");
+    std::vector<BVHNode> dilated;
+    std::vector<float> bounds;
+    build_inference_nodes(h->neural_nodes, h->cfg.bvh.fixed_node_dilation, dilated, bounds);
+    h->neural_fast_div = nodes_in_fast_div_domain(dilated) && coords_in_fast_div_domain(bounds.data(), bounds.size());
+    cuda_check(h->d_neural_dilated.resize(2u * dilated.size()), "alloc dilated nodes");
+    cuda_check(cudaMemcpy(h->d_neural_dilated.ptr, dilated.data(), dilated.size() * sizeof(BVHNode),
+                          cudaMemcpyHostToDevice),
+               "upload dilated nodes");
+    cuda_check(h->d_neural_bounds.resize(bounds.size() / 4u), "alloc bounds");
+    cuda_check(cudaMemcpy(h->d_neural_bounds.ptr, bounds.data(), bounds.size() * sizeof(float), cudaMemcpyHostToDevice),
+               "upload bounds");
     h->non_neural.assign(h->neural_nodes.size(), 0u);
     h->any_non_neural = false;
     h->d_non_neural.release();
@@ -358,7 +371,9 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
         // (include/cuda/neural/neural_bvh_module_common.cuh:323)
         if (timed)
             cuda_check(cudaEventRecord(h->ev0, s), "event");
-        cuda_check(launch_classic_as_neural(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, vis_only, s), "classic");
+        cuda_check(launch_classic_as_neural(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, vis_only,
+                                            h->classic_fast_div, s),
+                   "classic");
         if (timed)
             cuda_check(cudaEventRecord(h->ev1, s), "event");
         h->last_launches = 1;
@@ -367,7 +382,8 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
     const NeuralConsts nc = make_neural_consts(h, depth, vis_only);
     if (timed)
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-    cuda_check(launch_neural_query(h->d_neural_nodes.ptr, h->any_non_neural ? h->d_non_neural.ptr : nullptr,
+    cuda_check(launch_neural_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),
+                                   h->any_non_neural ? h->d_non_neural.ptr : nullptr,
                                    h->d_params_h.ptr, h->grid, nc, (uint32_t)h->cfg.network.n_hidden_layers, d_rays, n,
                                    d_hits, counters, list, h->num_sms, s),
                "neural query");
@@ -376,6 +392,7 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
     h->last_launches = 1;
     if (h->any_non_neural || h->cfg.fallback_margin > 0.f) {
         cuda_check(launch_classic_fallback(h->d_nodes.ptr, h->d_tris.ptr, d_rays, list, counters, n, d_hits, vis_only,
+                                           h->classic_fast_div,
                                            h->num_sms, s),
                    "fallback");
         h->last_launches = 2;
@@ -646,7 +663,8 @@ nbvh_status nbvh_query_closest_classic(nbvh_handle *h, const nbvh_ray *d_rays, u
         require((d_rays && d_hits) || n == 0, NBVH_EINVAL, "null buffers");
         cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-        cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, false, nullptr, s), "classic");
+        cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, false, nullptr, h->classic_fast_div, s),
+                   "classic");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
         h->last_launches = 1;
         h->last_rays = n;
@@ -661,7 +679,8 @@ nbvh_status nbvh_query_any_classic(nbvh_handle *h, const nbvh_ray *d_rays, uint3
         require((d_rays && d_hits) || n == 0, NBVH_EINVAL, "null buffers");
         cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-        cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, true, nullptr, s), "classic");
+        cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, true, nullptr, h->classic_fast_div, s),
+                   "classic");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
         h->last_launches = 1;
         h->last_rays = n;
@@ -742,7 +761,9 @@ nbvh_status nbvh_query_closest_classic_host(nbvh_handle *h, const nbvh_ray *h_ra
         require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
         require((h_rays && h_hits) || n == 0, NBVH_EINVAL, "null buffers");
         pipelined(h, h_rays, n, h_hits, [&](const nbvh_ray *din, uint32_t cnt, nbvh_hit *dout, cudaStream_t s, int) {
-            cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, din, cnt, dout, false, nullptr, s), "classic");
+            cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, din, cnt, dout, false, nullptr,
+                                      h->classic_fast_div, s),
+                       "classic");
             h->last_launches = 1;
         });
     });
@@ -755,7 +776,8 @@ nbvh_status nbvh_query_segments(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t
         require(h->neural_built, NBVH_ESTATE, "neural cut not built");
         require((d_rays && d_counts && (d_segments || max_segments == 0)) || n == 0, NBVH_EINVAL, "null buffers");
         const NeuralConsts nc = make_neural_consts(h, 1u, false);
-        cuda_check(launch_segments(h->d_neural_nodes.ptr, nc, d_rays, n, max_segments, d_segments, d_counts,
+        cuda_check(launch_segments(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, nc, d_rays, n, max_segments,
+                                   d_segments, d_counts,
                                    reinterpret_cast<cudaStream_t>(stream)),
                    "segments");
         h->last_launches = 1;

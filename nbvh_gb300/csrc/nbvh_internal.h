@@ -61,6 +61,7 @@ struct NeuralConsts {
     uint32_t bvh_lod;
     uint32_t max_traversal_steps;
     uint32_t visibility_only;
+    uint32_t fast_div_ok; // every box coordinate of the cut is +0 or has magnitude in [2^-60, 2^11]
 };
 
 struct LossConsts {
@@ -137,8 +138,12 @@ struct nbvh_handle {
     nbvh::DeviceBuffer<float4> d_tris;         // 3 float4 per triangle record (v0|prim, e1, e2)
     nbvh::DeviceBuffer<float> d_albedo;        // 3 per triangle (original order)
     nbvh::DeviceBuffer<float4> d_neural_nodes; // 2 float4 per node
+    nbvh::DeviceBuffer<float4> d_neural_dilated; // inference copy: boxes dilated by fixed_node_dilation
+    nbvh::DeviceBuffer<float4> d_neural_bounds;  // union of the dilated leaf boxes below each node
     nbvh::DeviceBuffer<uint8_t> d_non_neural;
     bool any_non_neural = false;
+    bool neural_fast_div = false;  // box coordinates of the cut inside the fast-division domain
+    bool classic_fast_div = false; // same for the classic BVH
 
     // parameters
     nbvh_param_layout layout{};
@@ -181,25 +186,27 @@ namespace nbvh {
 
 // ---- kernel launchers (defined in the .cu files) ----
 cudaError_t launch_classic(const float4 *nodes, const float4 *tris, const nbvh_ray *rays, uint32_t n,
-                           nbvh_hit *hits, bool any_hit, const uint32_t *ray_list, cudaStream_t s);
+                           nbvh_hit *hits, bool any_hit, const uint32_t *ray_list, bool fast_div, cudaStream_t s);
 
 // Fallback pass: rays listed in `list` (count read on the device from counters) are answered by
 // the classic BLAS and written into neural hit records.
 cudaError_t launch_classic_fallback(const float4 *nodes, const float4 *tris, const nbvh_ray *rays,
                                     const uint32_t *list, const QueryCounters *counters,
-                                    uint32_t max_list, nbvh_neural_hit *hits, bool any_hit, int num_sms,
-                                    cudaStream_t s);
+                                    uint32_t max_list, nbvh_neural_hit *hits, bool any_hit, bool fast_div,
+                                    int num_sms, cudaStream_t s);
 
 cudaError_t launch_classic_as_neural(const float4 *nodes, const float4 *tris, const nbvh_ray *rays,
-                                     uint32_t n, nbvh_neural_hit *hits, bool any_hit, cudaStream_t s);
+                                     uint32_t n, nbvh_neural_hit *hits, bool any_hit, bool fast_div, cudaStream_t s);
 
-cudaError_t launch_neural_query(const float4 *neural_nodes, const uint8_t *non_neural, const __half *params_h,
-                                const GridParams &grid, const NeuralConsts &nc, uint32_t n_hidden_layers,
-                                const nbvh_ray *rays, uint32_t n, nbvh_neural_hit *hits, QueryCounters *counters,
-                                uint32_t *fallback_list, int num_sms, cudaStream_t s);
+cudaError_t launch_neural_query(const float4 *dilated_nodes, const float4 *bounds, uint32_t n_cut_nodes,
+                                const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
+                                const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
+                                nbvh_neural_hit *hits, QueryCounters *counters, uint32_t *fallback_list, int num_sms,
+                                cudaStream_t s);
 
-cudaError_t launch_segments(const float4 *neural_nodes, const NeuralConsts &nc, const nbvh_ray *rays, uint32_t n,
-                            uint32_t max_segments, nbvh_segment *segs, uint32_t *counts, cudaStream_t s);
+cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, const NeuralConsts &nc,
+                            const nbvh_ray *rays, uint32_t n, uint32_t max_segments, nbvh_segment *segs,
+                            uint32_t *counts, cudaStream_t s);
 
 cudaError_t launch_network_inference(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                                      const float *positions, uint32_t n, float *outputs, int num_sms,
@@ -241,5 +248,11 @@ cudaError_t launch_camera_rays(uint32_t width, uint32_t height, uint32_t sample_
 bool build_bvh2(const std::vector<float> &vertices, const std::vector<uint32_t> &indices,
                 std::vector<BVHNode> &nodes, std::vector<uint32_t> &prim_indices, std::string &err);
 void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std::vector<BVHNode> &neural);
+void build_inference_nodes(const std::vector<BVHNode> &neural, float dil, std::vector<BVHNode> &dilated,
+                           std::vector<float> &bounds);
+// true when every coordinate is +0 or has magnitude in [2^-60, 2^11] (no -0, no subnormal range),
+// the box-coordinate precondition of the fast slab division
+bool coords_in_fast_div_domain(const float *c, size_t n);
+bool nodes_in_fast_div_domain(const std::vector<BVHNode> &nodes);
 
 } // namespace nbvh

@@ -1,0 +1,103 @@
+"""The oracle's network restatement on its own (no GPU): forward against a numpy implementation,
+backward against central finite differences of its own forward (FP32 exact mode, smooth losses),
+and the composite-loss masking / linear-activation rules of
+include/cuda/neural/utils/pt_composite_loss.cuh:18-123."""
+
+import numpy as np
+import pytest
+
+import nbvh_gb300 as nb
+
+
+def small_cfg(**kw):
+    base = {"hashgrid.n_levels": 4, "hashgrid.log2_hashmap_size": 8, "hashgrid.base_resolution": 4,
+            "hashgrid.per_level_scale": 2.0, "network.n_hidden_layers": 2, "module.input_segment_points": 2}
+    base.update(kw)
+    return nb.default_config(**base)
+
+
+def random_params(cfg, seed=0):
+    L = nb.param_layout(cfg)
+    rng = np.random.default_rng(seed)
+    p = nb.init_params(cfg) * 2.0
+    p[L.n_network_params:] = rng.uniform(-1, 1, p.size - L.n_network_params).astype(np.float32)
+    return L, p
+
+
+def numpy_forward(cfg, L, p, feats):
+    H = cfg.network.n_hidden_layers
+    off = 0
+    x = feats.astype(np.float64)
+    for m in range(H + 1):
+        rows = 16 if m == H else 64
+        cols = L.n_inputs if m == 0 else 64
+        W = p[off:off + rows * cols].reshape(rows, cols).astype(np.float64)
+        off += rows * cols
+        x = x @ W.T
+        if m < H:
+            x = np.maximum(x, 0)
+    return 1.0 / (1.0 + np.exp(-x))
+
+
+def test_forward_matches_numpy(oracle, built):
+    cfg = small_cfg()
+    L, p = random_params(cfg)
+    net = oracle.network(cfg, L, p, exact=True)
+    pos = np.random.default_rng(1).uniform(0, 1, (64, 2, 3)).astype(np.float32)
+    feats = oracle.encode(net, pos)
+    out = oracle.network_inference(net, pos)
+    ref = numpy_forward(cfg, L, p, feats)
+    assert np.max(np.abs(out - ref)) < 1e-6
+    # FP16 mode rounds features / activations / parameters: close but not equal
+    out16 = oracle.network_inference(oracle.network(cfg, L, p), pos)
+    assert 0 < np.max(np.abs(out16 - ref)) < 2e-2
+
+
+def test_backward_matches_finite_differences(oracle, built):
+    cfg = small_cfg(**{"output.visibility_loss": nb.abi.LOSS["L2"], "output.depth_loss": nb.abi.LOSS["L2"],
+                       "output.normal_loss": nb.abi.LOSS["L2"], "output.albedo_loss": nb.abi.LOSS["L2"],
+                       "output.visibility_masking_loss": 0, "output.output_normal_linear_activation": 0})
+    L, p = random_params(cfg, seed=3)
+    rng = np.random.default_rng(4)
+    n = 32
+    pos = rng.uniform(0.05, 0.95, (n, 2, 3)).astype(np.float32)
+    tgt = rng.uniform(0, 1, (n, 8)).astype(np.float32)
+    lc = oracle.loss_consts(cfg)
+
+    def loss_at(params):
+        net = oracle.network(cfg, L, params, exact=True)
+        return oracle.compute_gradients(net, lc, pos, tgt, L.n_params, loss_scale=1.0, fp16_backward=False)
+
+    g, _ = loss_at(p)
+    # network weights (first, hidden, output rows 0..7) and grid entries with non-zero gradient
+    cand = list(rng.choice(64 * L.n_inputs, 12, replace=False))
+    cand += list(64 * L.n_inputs + rng.choice(64 * 64, 8, replace=False))
+    cand += list(L.n_network_params - 16 * 64 + rng.choice(8 * 64, 8, replace=False))
+    grid_nz = np.where(np.abs(g[L.n_network_params:]) > 1e-6)[0]
+    cand += list(L.n_network_params + rng.choice(grid_nz, 12, replace=False))
+    for i in cand:
+        h = 1e-3 * max(1.0, abs(float(p[i])))
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (loss_at(pp)[1] - loss_at(pm)[1]) / (float(pp[i]) - float(pm[i]))
+        assert abs(fd - g[i]) <= 2e-3 * max(abs(g[i]), 1e-3) + 1e-6, (i, fd, g[i])
+
+
+def test_composite_loss_rules(oracle, built):
+    cfg = nb.default_config()
+    lc = oracle.loss_consts(cfg)
+    pred = np.full((2, 16), 0.6, np.float32)
+    tgt = np.array([[0.0, 0.3, 0.5, 0.5, 1.0, 0.2, 0.2, 0.2], [1.0, 0.3, 0.5, 0.5, 1.0, 0.2, 0.2, 0.2]], np.float32)
+    vals, grads = oracle.composite_loss(lc, pred, tgt, loss_scale=1.0)
+    # masked row: only visibility contributes; padding channels never do
+    assert np.all(vals[0, 1:] == 0) and np.all(grads[0, 1:] == 0) and vals[0, 0] > 0
+    assert np.all(vals[1, :8] != 0) and np.all(vals[:, 8:] == 0)
+    # linearised-sigmoid normal: L1 on ((p*2-1)/0.1)*0.5+0.5, gradient scaled by 1/0.1
+    lin = ((0.6 * 2 - 1) / 0.1) * 0.5 + 0.5
+    n_total = 2 * 8
+    assert abs(vals[1, 2] - abs(lin - 0.5) / n_total) < 1e-6
+    assert abs(grads[1, 2] - 10.0 / n_total) < 1e-5
+    # loss scale multiplies the gradient only
+    v2, g2 = oracle.composite_loss(lc, pred, tgt, loss_scale=128.0)
+    assert np.array_equal(v2, vals) and np.allclose(g2, grads * 128.0)
