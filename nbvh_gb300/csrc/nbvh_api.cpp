@@ -351,9 +351,29 @@ void ensure_query_workspace(nbvh_handle *h, uint32_t n, int ctx)
 {
     if (h->d_counters.count < 3u)
         cuda_check(h->d_counters.resize(3u), "alloc counters");
-    auto &list = ctx == 0 ? h->d_fallback_list : h->d_pipe_fallback[ctx - 1];
-    if (list.count < n)
-        cuda_check(list.resize(n), "alloc fallback list");
+    QueryContext &q = h->qctx[ctx];
+    if (q.fallback_list.count < n)
+        cuda_check(q.fallback_list.resize(n), "alloc fallback list");
+    if (q.wave_counts.count < 4u)
+        cuda_check(q.wave_counts.resize(4u), "alloc wave counters");
+    if (!q.h_count) {
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&q.h_count), sizeof(uint32_t), cudaHostAllocDefault),
+                   "pinned counter");
+        *q.h_count = 0;
+    }
+    if (!q.ev)
+        cuda_check(cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming), "event");
+    if (q.capacity < n) {
+        for (int k = 0; k < 2; k++) {
+            cuda_check(q.od0[k].resize(n), "alloc wave state");
+            cuda_check(q.od1[k].resize(n), "alloc wave state");
+            cuda_check(q.nv[k].resize(n), "alloc wave state");
+            cuda_check(q.ar[k].resize(n), "alloc wave state");
+            cuda_check(q.meta[k].resize(n), "alloc wave state");
+            cuda_check(q.stack[k].resize((size_t)kNeuralStackSize * n), "alloc wave stacks");
+        }
+        q.capacity = n;
+    }
 }
 
 // The neural query on device buffers with query context ctx (0: API calls, 1-2: host pipeline).
@@ -363,8 +383,9 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
     require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
     require(h->neural_built, NBVH_ESTATE, "neural cut not built");
     ensure_query_workspace(h, n, ctx);
+    QueryContext &q = h->qctx[ctx];
     QueryCounters *counters = h->d_counters.ptr + ctx;
-    uint32_t *list = ctx == 0 ? h->d_fallback_list.ptr : h->d_pipe_fallback[ctx - 1].ptr;
+    uint32_t *list = q.fallback_list.ptr;
     cuda_check(cudaMemsetAsync(counters, 0, sizeof(QueryCounters), s), "reset counters");
     if (h->cfg.bvh.ignore_neural_blas) {
         // the non-neural BLAS switch: the mesh goes to the classic traversal
@@ -382,20 +403,24 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
     const NeuralConsts nc = make_neural_consts(h, depth, vis_only);
     if (timed)
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-    cuda_check(launch_neural_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),
-                                   h->any_non_neural ? h->d_non_neural.ptr : nullptr,
-                                   h->d_params_h.ptr, h->grid, nc, (uint32_t)h->cfg.network.n_hidden_layers, d_rays, n,
-                                   d_hits, counters, list, h->num_sms, s),
+    WaveList lists[2];
+    for (int k = 0; k < 2; k++)
+        lists[k] = WaveList{q.od0[k].ptr, q.od1[k].ptr, q.nv[k].ptr, q.ar[k].ptr, q.meta[k].ptr, q.stack[k].ptr, q.capacity};
+    uint32_t launches = 0;
+    cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),
+                                 h->any_non_neural ? h->d_non_neural.ptr : nullptr, h->d_params_h.ptr, h->grid, nc,
+                                 (uint32_t)h->cfg.network.n_hidden_layers, d_rays, n, d_hits, counters, list, lists,
+                                 q.wave_counts.ptr, q.h_count, q.ev, h->num_sms, s, &launches),
                "neural query");
     if (timed)
         cuda_check(cudaEventRecord(h->ev1, s), "event");
-    h->last_launches = 1;
+    h->last_launches = launches;
     if (h->any_non_neural || h->cfg.fallback_margin > 0.f) {
         cuda_check(launch_classic_fallback(h->d_nodes.ptr, h->d_tris.ptr, d_rays, list, counters, n, d_hits, vis_only,
                                            h->classic_fast_div,
                                            h->num_sms, s),
                    "fallback");
-        h->last_launches = 2;
+        h->last_launches = launches + 1u;
     }
     h->last_rays = n;
 }

@@ -80,7 +80,19 @@ struct QueryCounters {
     uint32_t stack_overflow;
     uint32_t fallback;
     uint32_t fallback_count; // entries written to the fallback list
-    uint32_t pad[2];
+    uint32_t work_count;     // rays that enter at least one leaf (compacted by the first pass)
+    uint32_t pad;
+};
+
+// One state list of the wavefront neural query (structure of arrays, `capacity` rays):
+// od0 = {o, best_t}, od1 = {d, seg_mint}, meta = {seg_maxt bits, seg_node, ray id,
+// segments | stack size << 16 | flags << 24}, nv = {normal, visibility}, ar = {albedo, rng bits},
+// stack = [kNeuralStackSize][capacity] node indices.
+struct WaveList {
+    float4 *od0, *od1, *nv, *ar;
+    uint4 *meta;
+    uint32_t *stack;
+    uint32_t capacity;
 };
 
 template <typename T>
@@ -111,6 +123,26 @@ struct DeviceBuffer {
         else
             ptr = nullptr;
         return e;
+    }
+};
+
+// Buffers of one query context: the two wavefront state lists, the rotating list counters, the
+// fallback list and a pinned word for the host's end-of-loop check.
+struct QueryContext {
+    DeviceBuffer<float4> od0[2], od1[2], nv[2], ar[2];
+    DeviceBuffer<uint4> meta[2];
+    DeviceBuffer<uint32_t> stack[2];
+    DeviceBuffer<uint32_t> wave_counts;
+    DeviceBuffer<uint32_t> fallback_list;
+    uint32_t capacity = 0;
+    uint32_t *h_count = nullptr;
+    cudaEvent_t ev = nullptr;
+    ~QueryContext()
+    {
+        if (h_count)
+            cudaFreeHost(h_count);
+        if (ev)
+            cudaEventDestroy(ev);
     }
 };
 
@@ -177,7 +209,7 @@ struct nbvh_handle {
     void *pinned_out[2] = {nullptr, nullptr};
     size_t pinned_chunk = 0;
     nbvh::DeviceBuffer<uint8_t> d_pipe_in[2], d_pipe_out[2];
-    nbvh::DeviceBuffer<uint32_t> d_pipe_fallback[2];
+    nbvh::QueryContext qctx[3]; // 0: device-buffer calls, 1-2: the host-buffer pipeline streams
 
     int num_sms = 0;
 };
@@ -198,11 +230,14 @@ cudaError_t launch_classic_fallback(const float4 *nodes, const float4 *tris, con
 cudaError_t launch_classic_as_neural(const float4 *nodes, const float4 *tris, const nbvh_ray *rays,
                                      uint32_t n, nbvh_neural_hit *hits, bool any_hit, bool fast_div, cudaStream_t s);
 
-cudaError_t launch_neural_query(const float4 *dilated_nodes, const float4 *bounds, uint32_t n_cut_nodes,
-                                const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
-                                const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
-                                nbvh_neural_hit *hits, QueryCounters *counters, uint32_t *fallback_list, int num_sms,
-                                cudaStream_t s);
+// Wavefront neural query (k_query.cu): first-leaf pass, then device steps checked by the host
+// every few launches through h_count (pinned). Returns when the loop has finished.
+cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds, uint32_t n_cut_nodes,
+                              const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
+                              const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
+                              nbvh_neural_hit *hits, QueryCounters *counters, uint32_t *fallback_list,
+                              const WaveList lists[2], uint32_t *wave_counts, uint32_t *h_count, cudaEvent_t ev,
+                              int num_sms, cudaStream_t s, uint32_t *launches);
 
 cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, const NeuralConsts &nc,
                             const nbvh_ray *rays, uint32_t n, uint32_t max_segments, nbvh_segment *segs,

@@ -98,7 +98,7 @@ __device__ __forceinline__ float2 encode_level(const uint32_t *__restrict__ tabl
     uint32_t v[8];
 #pragma unroll
     for (uint32_t c = 0; c < 8; c++) {
-        uint32_t x = gx + (c & 1u), y = gy + ((c >> 1) & 1u), z = gz + ((c >> 2) & 1u);
+        const uint32_t x = gx + (c & 1u), y = gy + ((c >> 1) & 1u), z = gz + ((c >> 2) & 1u);
         uint32_t idx;
         if (hashed) {
             idx = (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (size - 1u);
@@ -190,6 +190,49 @@ __device__ __forceinline__ void mlp_forward_tile(const __half *sw, uint32_t n_in
 #pragma unroll
     for (int i = 0; i < 4; i++)
         o[i] = 1.0f / (1.0f + expf(-oc[i]));
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p)
+{
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+// Encode phase of a 16-row tile: FP16 features of every (row, point, level) written to the warp's
+// feature tile feat[16][ld] (ld = n_inputs + 8 halves); rows not in active_mask16 are zero. Lane j
+// handles the (point, level) pairs j, j + 32, ... for all rows, four rows at a time so that 32
+// independent gathers are in flight per lane; no MLP accumulator is live here.
+template <typename PosFn>
+__device__ __forceinline__ void encode_tile_to_smem(const uint32_t *__restrict__ table, const GridParams &gp,
+                                                    PosFn &&pos, uint32_t active_mask16, __half *feat, uint32_t ld)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t L = gp.n_levels, PL = gp.n_points * gp.n_levels;
+    for (uint32_t j = (uint32_t)lane; j < PL; j += 32u) {
+        const uint32_t p = j / L, l = j - p * L;
+#pragma unroll 4
+        for (uint32_t r = 0; r < 16u; r++) {
+            uint32_t v = 0u;
+            if ((active_mask16 >> r) & 1u) {
+                const float2 f = encode_level(table, gp, l, pos(r, p));
+                v = pack_half2(f.x, f.y);
+            }
+            *reinterpret_cast<uint32_t *>(feat + r * ld + 2u * j) = v;
+        }
+    }
+    __syncwarp();
+}
+
+// MLP phase of a 16-row tile whose FP16 features are in feat[16][ld]; outputs as mlp_forward_tile.
+__device__ __forceinline__ void mlp_tile_from_smem(const __half *sw, const __half *feat, uint32_t ld,
+                                                   uint32_t n_inputs, uint32_t n_hidden_layers, float (&o)[4])
+{
+    const int lane = threadIdx.x & 31;
+    const __half *arow = feat + ((lane & 7) + ((lane >> 3) & 1) * 8) * ld + (lane >> 4) * 8;
+    auto make_a = [&](uint32_t kb, uint32_t(&a)[4]) { ldsm_x4(a, arow + kb * 16u); };
+    mlp_forward_tile(sw, n_inputs, n_hidden_layers, make_a, o);
 }
 
 // Encoded segment points along [po, pi] (neural_bvh_module_kernels.cu:57-96).
