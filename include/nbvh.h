@@ -288,7 +288,10 @@ nbvh_status nbvh_query_any_classic(nbvh_handle *h, const nbvh_ray *d_rays, uint3
 /* Neural closest hit. Rays with tmin != 1e-4 are accepted; the neural traversal always restarts
  * from -FLT_MAX as the reference does (neural_bvh2.cuh:185-189). depth: 1 = primary ray
  * (primary_visibility_threshold), > 1 = secondary. When ignore_neural_blas is set the call
- * answers from the classic BLAS and sets NBVH_HIT_CLASSIC_FALLBACK on every valid hit. */
+ * answers from the classic BLAS and sets NBVH_HIT_CLASSIC_FALLBACK on every valid hit.
+ * The neural queries are wavefronts whose length depends on the data: the host reads the count of
+ * rays still traversing every few steps, so these two calls return after the work is done on the
+ * stream (like the reference's host loop, path_module.cu:54-137), not asynchronously. */
 nbvh_status nbvh_query_closest_neural(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n,
                                       uint32_t depth, nbvh_neural_hit *d_hits, nbvh_stream stream);
 nbvh_status nbvh_query_visibility_neural(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n,
