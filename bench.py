@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--train-steps", type=int, default=20000)
     ap.add_argument("--cpu-sample", type=int, default=1 << 14)
+    ap.add_argument("--log2-rays", type=int, default=22,
+                    help="rays per step; smaller values are for profiling captures, not bench lines")
     return ap.parse_args()
 
 
@@ -342,7 +344,9 @@ def run_ours(args):
 
 
 def main():
+    global N_RAYS
     args = parse()
+    N_RAYS = 1 << args.log2_rays
     if args.impl == "reference":
         run_reference(args)
     else:

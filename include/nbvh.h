@@ -425,6 +425,32 @@ nbvh_status nbvh_last_query_stats(nbvh_handle *h, nbvh_query_stats *out);
 nbvh_status nbvh_last_kernel_time(nbvh_handle *h, float *ms, uint32_t *launches);
 
 /* ---------------------------------------------------------------------------------------------
+ * Allocation-free neural query. This entry point has no counterpart in the reference.
+ *
+ * Same result as nbvh_query_closest_neural, for callers that must not allocate memory while they
+ * trace: a renderer whose GPU memory is reserved up front and must not grow mid-frame, or a host
+ * thread that may not take the device-wide synchronisation an allocation can cause. The ordinary
+ * query grows per-handle buffers to the largest batch seen; this one allocates nothing. Its
+ * scratch (the per-ray traversal state, the fallback list and the counters, about 356 bytes per
+ * ray) is one fixed buffer of NBVH_NOALLOC_MAX_RAYS rays compiled into the library, one copy per
+ * device, created when the library's device code is loaded.
+ *  - n must be at most NBVH_NOALLOC_MAX_RAYS; a larger n returns NBVH_EINVAL and launches nothing.
+ *    Split larger batches into several calls.
+ *  - The first call on each device looks up the buffer's address (setup). Make one call, n = 0 is
+ *    enough, before capturing a stream.
+ *  - Each call zeroes the counters it uses before its first kernel; nothing relies on the buffer's
+ *    contents from an earlier call.
+ *  - There is one buffer per device, shared by every handle on it. Calls that overlap in time on
+ *    the same device (several host threads, or several handles) race on it: serialise them. A call
+ *    returns only after its work on the stream is complete, so consecutive calls are safe.
+ *  - nbvh_last_query_stats and nbvh_last_kernel_time do not report this call.
+ * ------------------------------------------------------------------------------------------- */
+#define NBVH_NOALLOC_MAX_RAYS 16384u
+nbvh_status nbvh_query_closest_neural_noalloc(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n,
+                                              uint32_t depth, nbvh_neural_hit *d_hits,
+                                              nbvh_stream stream);
+
+/* ---------------------------------------------------------------------------------------------
  * Host-only utilities (no CUDA device needed)
  * ------------------------------------------------------------------------------------------- */
 

@@ -116,6 +116,7 @@ PROTOTYPES = {
     "nbvh_query_closest_classic": (ST, [P, P, U32, P, P]),
     "nbvh_query_any_classic": (ST, [P, P, U32, P, P]),
     "nbvh_query_closest_neural": (ST, [P, P, U32, U32, P, P]),
+    "nbvh_query_closest_neural_noalloc": (ST, [P, P, U32, U32, P, P]),
     "nbvh_query_visibility_neural": (ST, [P, P, U32, U32, P, P]),
     "nbvh_query_closest_neural_host": (ST, [P, P, U32, U32, P]),
     "nbvh_query_closest_classic_host": (ST, [P, P, U32, P]),

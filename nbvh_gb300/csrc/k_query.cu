@@ -423,10 +423,14 @@ cudaError_t run_steps(const WaveArgs &a, size_t smem, int num_sms, uint32_t max_
         e = cudaMemcpyAsync(h_count, &a.wave_counts[it % 3u], sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         if (e != cudaSuccess)
             return e;
-        e = cudaEventRecord(ev, s);
-        if (e != cudaSuccess)
-            return e;
-        e = cudaEventSynchronize(ev);
+        if (ev) {
+            e = cudaEventRecord(ev, s);
+            if (e != cudaSuccess)
+                return e;
+            e = cudaEventSynchronize(ev);
+        } else {
+            e = cudaStreamSynchronize(s);
+        }
         if (e != cudaSuccess)
             return e;
         if (*h_count == 0u)
@@ -480,6 +484,54 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
         return run_steps<true>(a, smem_cut, num_sms, nc.max_traversal_steps, h_count, ev, s, *launches);
     return run_steps<false>(a, step_smem(grid.n_inputs, n_hidden_layers, grid.n_points, 0u), num_sms,
                             nc.max_traversal_steps, h_count, ev, s, *launches);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Fixed scratch of the allocation-free query: a file-scope device array, so the CUDA runtime
+// creates one copy per device when it loads this module and no call allocates it.
+// ---------------------------------------------------------------------------------------------
+
+namespace {
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+constexpr int kNoallocMaxDevices = 64;
+} // namespace
+
+cudaError_t noalloc_scratch(int device, NoallocScratch *out)
+{
+    static std::mutex mu;
+    static unsigned char *base[kNoallocMaxDevices] = {};
+    if (device < 0 || device >= kNoallocMaxDevices)
+        return cudaErrorInvalidDevice;
+    unsigned char *p;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!base[device]) {
+            void *addr = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+            if (e != cudaSuccess)
+                return e;
+            base[device] = static_cast<unsigned char *>(addr);
+        }
+        p = base[device];
+    }
+    const size_t n = kNoallocRays;
+    for (int k = 0; k < 2; k++) {
+        WaveList &L = out->lists[k];
+        L.od0 = reinterpret_cast<float4 *>(p);
+        L.od1 = L.od0 + n;
+        L.nv = L.od1 + n;
+        L.ar = L.nv + n;
+        L.meta = reinterpret_cast<uint4 *>(L.ar + n);
+        L.stack = reinterpret_cast<uint32_t *>(L.meta + n);
+        L.capacity = (uint32_t)n;
+        p += kNoallocListBytes;
+    }
+    out->fallback_list = reinterpret_cast<uint32_t *>(p);
+    p += n * 4u;
+    out->counters = reinterpret_cast<QueryCounters *>(p);
+    p += 256u;
+    out->wave_counts = reinterpret_cast<uint32_t *>(p);
+    return cudaSuccess;
 }
 
 } // namespace nbvh

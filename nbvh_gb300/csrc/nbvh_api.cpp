@@ -425,6 +425,43 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
     h->last_rays = n;
 }
 
+// The closest-hit neural query on the fixed per-device scratch (noalloc_scratch): the same
+// kernels as neural_query, with no allocation. Returns after the stream's work is complete, so
+// the shared scratch is free again when the call returns.
+void neural_query_noalloc(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t depth,
+                          nbvh_neural_hit *d_hits, cudaStream_t s)
+{
+    if (n > NBVH_NOALLOC_MAX_RAYS)
+        fail(NBVH_EINVAL, "n = " + std::to_string(n) + " exceeds NBVH_NOALLOC_MAX_RAYS = " +
+                              std::to_string(NBVH_NOALLOC_MAX_RAYS) + "; split the batch");
+    require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
+    require(h->neural_built, NBVH_ESTATE, "neural cut not built");
+    NoallocScratch sc;
+    cuda_check(noalloc_scratch(h->device, &sc), "fixed scratch address");
+    if (n == 0)
+        return;
+    cuda_check(cudaMemsetAsync(sc.counters, 0, sizeof(QueryCounters), s), "reset counters");
+    if (h->cfg.bvh.ignore_neural_blas) {
+        cuda_check(launch_classic_as_neural(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, false,
+                                            h->classic_fast_div, s),
+                   "classic");
+    } else {
+        const NeuralConsts nc = make_neural_consts(h, depth, false);
+        uint32_t host_count = 0, launches = 0;
+        cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr,
+                                     (uint32_t)h->neural_nodes.size(), h->any_non_neural ? h->d_non_neural.ptr : nullptr,
+                                     h->d_params_h.ptr, h->grid, nc, (uint32_t)h->cfg.network.n_hidden_layers, d_rays,
+                                     n, d_hits, sc.counters, sc.fallback_list, sc.lists, sc.wave_counts, &host_count,
+                                     nullptr, h->num_sms, s, &launches),
+                   "neural query");
+        if (h->any_non_neural || h->cfg.fallback_margin > 0.f)
+            cuda_check(launch_classic_fallback(h->d_nodes.ptr, h->d_tris.ptr, d_rays, sc.fallback_list, sc.counters,
+                                               n, d_hits, false, h->classic_fast_div, h->num_sms, s),
+                       "fallback");
+    }
+    cuda_check(cudaStreamSynchronize(s), "stream sync");
+}
+
 } // namespace
 
 // =============================================================================================
@@ -727,6 +764,15 @@ nbvh_status nbvh_query_visibility_neural(nbvh_handle *h, const nbvh_ray *d_rays,
     return guarded(h, [&]() {
         require((d_rays && d_hits) || n == 0, NBVH_EINVAL, "null buffers");
         neural_query(h, d_rays, n, depth, true, d_hits, reinterpret_cast<cudaStream_t>(stream), 0, true);
+    });
+}
+
+nbvh_status nbvh_query_closest_neural_noalloc(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t depth,
+                                              nbvh_neural_hit *d_hits, nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require((d_rays && d_hits) || n == 0, NBVH_EINVAL, "null buffers");
+        neural_query_noalloc(h, d_rays, n, depth, d_hits, reinterpret_cast<cudaStream_t>(stream));
     });
 }
 

@@ -230,8 +230,27 @@ cudaError_t launch_classic_fallback(const float4 *nodes, const float4 *tris, con
 cudaError_t launch_classic_as_neural(const float4 *nodes, const float4 *tris, const nbvh_ray *rays,
                                      uint32_t n, nbvh_neural_hit *hits, bool any_hit, bool fast_div, cudaStream_t s);
 
+// Scratch of the allocation-free neural query: one static device buffer per device holding, for
+// NBVH_NOALLOC_MAX_RAYS rays, both wave lists, the fallback list, the counters and the wave
+// counters. Every region starts on a 256-byte boundary.
+struct NoallocScratch {
+    WaveList lists[2];
+    uint32_t *fallback_list;
+    QueryCounters *counters;
+    uint32_t *wave_counts;
+};
+constexpr size_t kNoallocRays = NBVH_NOALLOC_MAX_RAYS;
+static_assert(kNoallocRays % 64u == 0u, "regions must stay 256-byte aligned");
+constexpr size_t kNoallocListBytes = kNoallocRays * (4u * sizeof(float4) + sizeof(uint4) + kNeuralStackSize * 4u);
+constexpr size_t kNoallocBytes = 2u * kNoallocListBytes + kNoallocRays * 4u + 256u + 256u;
+// The buffer's address on `device` (which must be current): looked up on the first call for that
+// device and cached. Fails with cudaErrorInvalidDevice for device ids beyond the cache.
+cudaError_t noalloc_scratch(int device, NoallocScratch *out);
+
 // Wavefront neural query (k_query.cu): first-leaf pass, then device steps checked by the host
-// every few launches through h_count (pinned). Returns when the loop has finished.
+// every few launches through h_count (pinned, with ev recorded after the copy; when ev is null,
+// h_count may be pageable and the host waits on the stream instead). Returns when the loop has
+// finished.
 cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds, uint32_t n_cut_nodes,
                               const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
                               const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
