@@ -350,6 +350,14 @@ nbvh_status nbvh_set_params(nbvh_handle *h, const float *h_params);
 nbvh_status nbvh_network_inference(nbvh_handle *h, const float *d_positions, uint32_t n,
                                    float *d_outputs, nbvh_stream stream);
 
+/* The fully fused MLP alone on encoded inputs (tcnn FullyFusedMLP::inference, configured at
+ * src/cuda/neural/neural_bvh_module.cu:232-238; the network half of the reference's
+ * NetworkWithInputEncoding): d_features holds n rows of n_inputs FP16 values (row-major, 16-byte
+ * aligned); d_outputs receives n x 8 sigmoid outputs. Runs on the tcgen05 tensor cores with
+ * TMA-fed tiles; returns after the kernel has finished (it reads back the kernel's status word). */
+nbvh_status nbvh_mlp_inference(nbvh_handle *h, const uint16_t *d_features, uint32_t n, float *d_outputs,
+                               nbvh_stream stream);
+
 /* Hash-grid encoding alone: n x points x 3 positions -> n x n_inputs features (FP32 values of the
  * FP16 features fed to the MLP). */
 nbvh_status nbvh_encode(nbvh_handle *h, const float *d_positions, uint32_t n, float *d_features,

@@ -342,6 +342,15 @@ class NBVH:
         self._check(self.lib.nbvh_network_inference(self.h, _ptr(positions), n, _ptr(out), _stream(stream)))
         return out
 
+    def mlp_inference(self, features, stream=None):
+        """tcgen05 MLP on FP16 encoded inputs (torch.float16 [n, n_inputs], contiguous)."""
+        import torch
+        assert features.dtype == torch.float16 and features.is_contiguous()
+        n = features.shape[0]
+        out = torch.empty((n, 8), dtype=torch.float32, device=features.device)
+        self._check(self.lib.nbvh_mlp_inference(self.h, _ptr(features), n, _ptr(out), _stream(stream)))
+        return out
+
     def encode(self, positions, stream=None):
         import torch
         n = positions.shape[0]

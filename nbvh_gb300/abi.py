@@ -125,6 +125,7 @@ PROTOTYPES = {
     "nbvh_get_params": (ST, [P, P]),
     "nbvh_set_params": (ST, [P, P]),
     "nbvh_network_inference": (ST, [P, P, U32, P, P]),
+    "nbvh_mlp_inference": (ST, [P, P, U32, P, P]),
     "nbvh_encode": (ST, [P, P, U32, P, P]),
     "nbvh_compute_gradients": (ST, [P, P, P, U32, P, PF, P]),
     "nbvh_adam_step": (ST, [P, P, P]),

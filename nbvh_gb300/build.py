@@ -17,6 +17,7 @@ SOURCES = [
     "k_neural.cu",
     "k_train.cu",
     "k_misc.cu",
+    "k_mlp_tc.cu",
     "k_query.cu",
     "nbvh_api.cpp",
     "bvh_builder.cpp",

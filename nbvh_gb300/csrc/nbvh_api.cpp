@@ -898,6 +898,36 @@ nbvh_status nbvh_network_inference(nbvh_handle *h, const float *d_positions, uin
     });
 }
 
+nbvh_status nbvh_mlp_inference(nbvh_handle *h, const uint16_t *d_features, uint32_t n, float *d_outputs,
+                               nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require((d_features && d_outputs) || n == 0, NBVH_EINVAL, "null buffers");
+        require((reinterpret_cast<uintptr_t>(d_features) & 15u) == 0u, NBVH_EINVAL,
+                "d_features must be 16-byte aligned");
+        require(h->cfg.network.precision == NBVH_PRECISION_FP16, NBVH_EINVAL, "tensor-core MLP needs FP16 weights");
+        cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        const uint32_t ni = h->layout.n_inputs, H = (uint32_t)h->cfg.network.n_hidden_layers;
+        const uint32_t wb = packed_weight_bytes(ni, H);
+        if (h->d_wpacked.count < wb / 2u)
+            cuda_check(h->d_wpacked.resize(wb / 2u), "alloc packed weights");
+        if (h->d_status.count < 1u)
+            cuda_check(h->d_status.resize(1u), "alloc status");
+        cuda_check(cudaMemsetAsync(h->d_status.ptr, 0, sizeof(uint32_t), s), "reset status");
+        cuda_check(launch_pack_weights(h->d_params_h.ptr, ni, H, h->d_wpacked.ptr, s), "pack weights");
+        cuda_check(cudaEventRecord(h->ev0, s), "event");
+        cuda_check(launch_mlp_tc(h->d_wpacked.ptr, ni, H, reinterpret_cast<const __half *>(d_features), n, d_outputs,
+                                 h->d_status.ptr, h->num_sms, s),
+                   "tensor-core MLP");
+        cuda_check(cudaEventRecord(h->ev1, s), "event");
+        h->last_launches = 2;
+        uint32_t status = 0;
+        cuda_check(cudaMemcpyAsync(&status, h->d_status.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "status");
+        cuda_check(cudaStreamSynchronize(s), "sync");
+        require(status == 0u, NBVH_ETIMEOUT, "tensor-core MLP: a bounded wait gave up");
+    });
+}
+
 nbvh_status nbvh_encode(nbvh_handle *h, const float *d_positions, uint32_t n, float *d_features, nbvh_stream stream)
 {
     return guarded(h, [&]() {

@@ -183,6 +183,8 @@ struct nbvh_handle {
     std::vector<float> h_params; // FP32 master (host mirror, refreshed on demand)
     nbvh::DeviceBuffer<float> d_params;   // FP32 master
     nbvh::DeviceBuffer<__half> d_params_h; // FP16 copy used by the kernels
+    nbvh::DeviceBuffer<__half> d_wpacked;  // network matrices in the tensor-core operand layout
+    nbvh::DeviceBuffer<uint32_t> d_status; // error word of kernels with bounded waits
     nbvh::DeviceBuffer<float> d_adam_m, d_adam_v;
     nbvh::DeviceBuffer<float> d_grad;
     uint32_t training_step = 0;
@@ -265,6 +267,15 @@ cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, c
 cudaError_t launch_network_inference(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                                      const float *positions, uint32_t n, float *outputs, int num_sms,
                                      cudaStream_t s);
+
+// tcgen05 fully fused MLP (k_mlp_tc.cu): weights packed into the tensor-core operand layout, then
+// 128-row tiles of FP16 inputs (row-major [n][n_inputs], 16-byte aligned) fed by TMA. status
+// receives a nonzero word if a bounded wait inside the kernel gave up.
+uint32_t packed_weight_bytes(uint32_t n_inputs, uint32_t n_hidden_layers);
+cudaError_t launch_pack_weights(const __half *params_h, uint32_t n_inputs, uint32_t n_hidden_layers, __half *packed,
+                                cudaStream_t s);
+cudaError_t launch_mlp_tc(const __half *wpacked, uint32_t n_inputs, uint32_t n_hidden_layers, const __half *features,
+                          uint32_t n, float *outputs, uint32_t *status, int num_sms, cudaStream_t s);
 
 cudaError_t launch_encode(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                           const float *positions, uint32_t n, float *features, cudaStream_t s);

@@ -1,0 +1,88 @@
+"""The tcgen05 fully fused MLP (K4 forward, TMA-fed, accumulators in tensor memory).
+
+Checked against a plain PyTorch FP32 restatement of the same network (FP16 weights, hidden
+activations rounded to FP16 between layers, sigmoid output) and against the mma.sync network path
+of nbvh_network_inference on the same encoded positions. The paths differ only in FP32
+accumulation order, which can move a hidden activation by one FP16 ulp; with the deliberately
+spread test weights such a flip moves an output by a few 1e-3. Tolerance: every sigmoid output
+within 1e-2 absolute (the visibility bar of the neural path), and 99.9% within 1e-3.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from helpers import handle
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-2
+TOL_TIGHT, FRAC_TIGHT = 1e-3, 0.999
+
+
+def check_close(a, b):
+    d = (a - b).abs()
+    worst, frac = float(d.max()), float((d <= TOL_TIGHT).float().mean())
+    assert worst <= TOL and frac >= FRAC_TIGHT, (worst, frac)
+
+
+@pytest.fixture(scope="module")
+def net(built):
+    h, s = handle(kind="sphere4k", seed=2)
+    rng = np.random.default_rng(8)
+    p = h.params()
+    nn = h.layout.n_network_params
+    p[:nn] *= 2.5
+    p[nn:] = rng.uniform(-1.0, 1.0, p.size - nn).astype(np.float32)
+    h.set_params(p)
+    yield h, p
+    h.close()
+
+
+def torch_mlp(h, p, feats):
+    ni, H = h.layout.n_inputs, h.cfg.network.n_hidden_layers
+    w = torch.from_numpy(p[: h.layout.n_network_params].astype(np.float16).astype(np.float32)).cuda()
+    x = feats.float()
+    o = 0
+    mats = [(64, ni)] + [(64, 64)] * (H - 1) + [(16, 64)]
+    for i, (r, c) in enumerate(mats):
+        W = w[o:o + r * c].view(r, c)
+        o += r * c
+        x = x @ W.t()
+        if i < len(mats) - 1:
+            x = torch.relu(x).half().float()
+    return torch.sigmoid(x[:, :8])
+
+
+@pytest.mark.parametrize("n", [5003, 4096, 1, 129])
+def test_mlp_tc_matches_torch_and_mma_path(net, n):
+    h, p = net
+    g = torch.Generator(device="cuda").manual_seed(n)
+    pos = torch.rand((n, h.cfg.module.input_segment_points, 3), device="cuda", generator=g)
+    feats = h.encode(pos).half().contiguous()
+    out = h.mlp_inference(feats)
+    ref = torch_mlp(h, p, feats)
+    check_close(out, ref)
+    fused = h.network_inference(pos)
+    check_close(out, fused)
+    # the outputs are spread: the check is not passing on a constant
+    assert float(out[:, 0].std()) > 0.02 if n > 100 else True
+
+
+def test_mlp_tc_large_batch_and_repeat(net):
+    h, p = net
+    n = (1 << 18) + 77
+    g = torch.Generator(device="cuda").manual_seed(3)
+    pos = torch.rand((n, h.cfg.module.input_segment_points, 3), device="cuda", generator=g)
+    feats = h.encode(pos).half().contiguous()
+    a = h.mlp_inference(feats)
+    b = h.mlp_inference(feats)
+    assert torch.equal(a, b)
+    ref = torch_mlp(h, p, feats)
+    check_close(a, ref)
+
+
+def test_mlp_tc_zero_rows(net):
+    h, _ = net
+    feats = torch.empty((0, h.layout.n_inputs), dtype=torch.float16, device="cuda")
+    assert h.mlp_inference(feats).shape == (0, 8)
