@@ -442,6 +442,9 @@ __device__ __forceinline__ bool leaf_accepts(float entry, float exit_, float rma
 //    is missed. The slab is monotone in the box bounds for non-zero direction components, so a leaf
 //    inside the union exits no later and enters no earlier than the union (`cull_ok` is false for
 //    rays with a zero direction component).
+// Returns 1 with the next accepted leaf, 0 when the stack runs empty, -1 on stack overflow, and 2
+// when `budget` node visits are used up before either (the traversal then resumes on the next
+// call with the same stack).
 // Node sources of the inference traversal: the pre-dilated cut and its subtree bounds, read from
 // global memory (read-only cache) or from a shared-memory copy staged at kernel start.
 struct GlobalCut {
@@ -481,7 +484,8 @@ template <typename Src, typename Stack>
 __device__ __forceinline__ int neural_intersect_inference(const Src &src, uint32_t lod, V3 o, const RayDiv &d,
                                                           bool cull_ok, Stack &stack, int &sp, float mint_eps,
                                                           float maxt_eps, float current_maxt, float &seg_mint,
-                                                          float &seg_maxt, uint32_t &seg_node)
+                                                          float &seg_maxt, uint32_t &seg_node,
+                                                          int budget = 0x7FFFFFFF)
 {
     const float rmint = -FLT_MAX, rmaxt = current_maxt;
     const float cull_eps = gmin(mint_eps, maxt_eps);
@@ -489,7 +493,14 @@ __device__ __forceinline__ int neural_intersect_inference(const Src &src, uint32
     NodeBox node = src.node(node_idx);
     bool have_slab = false;
     float cur_e = 0.f, cur_x = 0.f;
-    for (;;) {
+    for (;; budget--) {
+        if (budget <= 0) {
+            // out of node visits: put the current node back and report "not finished" (2); the next
+            // call pops it and recomputes its slab, so the traversal resumes exactly where it
+            // stopped. sp <= 23 here (a push that reached 24 returned -1), so the push fits.
+            stack[sp++] = node_idx;
+            return 2;
+        }
         const bool leaf = (node.count > 0u && node.count <= 2u + lod) || node.offset == 0xFFFFFFFFu;
         if (leaf) {
             if (!have_slab)

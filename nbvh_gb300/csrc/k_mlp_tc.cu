@@ -18,6 +18,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstring>
 #include <mutex>
 
 #include "nbvh_internal.h"
@@ -63,7 +64,8 @@ struct MlpTcArgs {
     uint32_t wbytes;
     uint32_t n_inputs;
     uint32_t n_hidden_layers;
-    uint32_t n;
+    uint32_t n;              // rows of the tensor map
+    const uint32_t *d_count; // optional row count produced on the device (min with n)
     float *outputs;
     uint32_t *status;
 };
@@ -117,6 +119,14 @@ __global__ void __launch_bounds__(kMlpThreads, 3) k_mlp_tc(const __grid_constant
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const uint32_t K = a.n_inputs, H = a.n_hidden_layers;
+    uint32_t n = a.n;
+    if (a.d_count) {
+        const uint32_t c = *reinterpret_cast<volatile const uint32_t *>(a.d_count);
+        n = c < n ? c : n;
+    }
+    const uint32_t n_tiles = (n + kTileRows - 1u) / kTileRows;
+    if (blockIdx.x >= n_tiles)
+        return; // no tile for this CTA: skip TMEM and the weight copy
     const uint32_t tile_off = (a.wbytes + 1023u) & ~1023u;
     unsigned char *tile = smem + tile_off;
     uint64_t *bars = reinterpret_cast<uint64_t *>(tile + kTileRows * K * 2u);
@@ -140,7 +150,6 @@ __global__ void __launch_bounds__(kMlpThreads, 3) k_mlp_tc(const __grid_constant
     const uint32_t tmem = *slot;
     const uint32_t tmem_row = tmem + ((32u * warp) << 16);
 
-    const uint32_t n_tiles = (a.n + kTileRows - 1u) / kTileRows;
     auto load_tile = [&](uint32_t t) {
         tc::mbar_expect_tx(bar_load, kTileRows * K * 2u);
         for (uint32_t c = 0; c < K / 8u; c++)
@@ -202,7 +211,7 @@ __global__ void __launch_bounds__(kMlpThreads, 3) k_mlp_tc(const __grid_constant
                 float o[8];
                 epilogue_out(tmem_row, o);
                 const uint32_t r = t * kTileRows + row;
-                if (r < a.n) {
+                if (r < n) {
                     float4 *dst = reinterpret_cast<float4 *>(a.outputs + (size_t)r * 8u);
                     dst[0] = make_float4(o[0], o[1], o[2], o[3]);
                     dst[1] = make_float4(o[4], o[5], o[6], o[7]);
@@ -259,38 +268,49 @@ cudaError_t launch_pack_weights(const __half *params_h, uint32_t n_inputs, uint3
     return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_tc(const __half *wpacked, uint32_t n_inputs, uint32_t n_hidden_layers, const __half *features,
-                          uint32_t n, float *outputs, uint32_t *status, int num_sms, cudaStream_t s)
+cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t rows, TensorMapBytes *out)
 {
-    if (n == 0)
-        return cudaSuccess;
-    if ((reinterpret_cast<uintptr_t>(features) & 15u) != 0u || n_inputs % 16u != 0u || n_inputs > 128u)
+    static_assert(sizeof(CUtensorMap) == sizeof(TensorMapBytes), "tensor map size");
+    if ((reinterpret_cast<uintptr_t>(features) & 15u) != 0u || n_inputs % 16u != 0u || n_inputs > 128u || rows == 0u)
         return cudaErrorInvalidValue;
     PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
     if (!encode)
         return cudaErrorNotSupported;
     CUtensorMap fmap;
-    const cuuint64_t dims[2] = {n_inputs, n};
+    const cuuint64_t dims[2] = {n_inputs, rows};
     const cuuint64_t strides[1] = {(cuuint64_t)n_inputs * 2u};
-    const cuuint32_t box[2] = {8u, kTileRows};
+    const cuuint32_t box[2] = {8u, kTileRows}; // 16 bytes x 128 rows: one K column of core matrices
     const cuuint32_t estr[2] = {1u, 1u};
     if (encode(&fmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<__half *>(features), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
+    memcpy(out->bytes, &fmap, sizeof(fmap));
+    return cudaSuccess;
+}
+
+cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
+                          uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
+                          uint32_t *status, int num_sms, cudaStream_t s)
+{
+    if (rows == 0)
+        return cudaSuccess;
+    CUtensorMap fmap;
+    memcpy(&fmap, feature_map.bytes, sizeof(fmap));
     MlpTcArgs a;
     a.wpacked = wpacked;
     a.wbytes = packed_weight_bytes(n_inputs, n_hidden_layers);
     a.n_inputs = n_inputs;
     a.n_hidden_layers = n_hidden_layers;
-    a.n = n;
+    a.n = rows;
+    a.d_count = d_count;
     a.outputs = outputs;
     a.status = status;
     const size_t smem = ((a.wbytes + 1023u) & ~1023u) + kTileRows * n_inputs * 2u + 32u;
     cudaError_t e = cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
-    const uint32_t tiles = (n + kTileRows - 1u) / kTileRows;
+    const uint32_t tiles = (rows + kTileRows - 1u) / kTileRows;
     uint32_t blocks = (uint32_t)num_sms * 3u;
     if (blocks > tiles)
         blocks = tiles;

@@ -4,17 +4,19 @@
 // 54-137) runs, per traversal step, an encode kernel, tcnn inference, a process kernel and a
 // compaction kernel, then copies the active count to the host and synchronises. Here:
 //
-//   k_wave_first  one thread per ray: the first entered leaf (K2). Rays that enter none are
-//                 answered at once; the others are appended (warp-aggregated) to state list 0.
-//   k_wave_step   persistent over the listed rays, 32 rows per warp: the segment's encoded points,
-//                 hash-grid features gathered straight into the tensor-core A fragments (K3), the
-//                 fused FP16 MLP (K4), the LocalT decode and closest-hit update, then the next
-//                 entered leaf (K2) for the rays that continue, appended to the other list.
+//   k_wave_first   one thread per ray: the first entered leaf (K2). Rays that enter none are
+//                  answered at once; the others are appended (warp-aggregated) to state list 0.
+//   then per step, over the rays listed by the previous step:
+//   k_wave_encode  K3: segment points and hash-grid features, one thread per (ray, point, level),
+//                  FP16 rows written in the layout the tensor-core MLP loads by TMA;
+//   k_mlp_tc       K4: the fused MLP on tcgen05 tensor cores (k_mlp_tc.cu), 128-row tiles;
+//   k_wave_decode  K2: LocalT decode and closest-hit update, then the next entered leaf for the
+//                  rays that continue, appended to the other list.
 //
-// Every row of a tile is a live ray, so the tensor cores and the gathers work on full tiles, and
-// the two kernels stay small. Per-ray state (~120 bytes plus the live part of the stack) moves
-// through HBM once per step in coalesced structure-of-arrays form. The host checks the list
-// count once per batch of steps (one 4-byte copy), instead of once per step.
+// Splitting the step lets each phase run at the occupancy it needs: the gathers of K3 with 64
+// warps per SM, the MLP with its accumulators in tensor memory, the divergent traversal with the
+// cut staged in shared memory. Every kernel reads the list length from device memory, so the host
+// checks it only once per batch of steps (one 16-byte copy).
 #include <type_traits>
 
 #include "device_math.cuh"
@@ -27,8 +29,13 @@ namespace {
 
 constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 constexpr unsigned kFull = 0xFFFFFFFFu;
-constexpr int kStepWarps = 16;
-constexpr int kStepThreads = kStepWarps * 32;
+constexpr uint32_t kEncodeThreads = 256;
+constexpr uint32_t kFirstThreads = 256;
+constexpr int kVisitsPerRound = 8; // node visits of the next-leaf search between refills
+// decode: the shared-memory cut variant runs one 768-thread block per SM, the global-memory
+// variant two 384-thread blocks; both leave 85 registers per thread (the traversal stack stays in
+// registers and local memory without spilling)
+constexpr uint32_t decode_threads(bool smem_cut) { return smem_cut ? 768u : 384u; }
 
 struct WaveArgs {
     GridParams grid;
@@ -37,13 +44,14 @@ struct WaveArgs {
     const float4 *bounds; // union of dilated leaf boxes per node
     const uint8_t *non_neural;
     const uint32_t *table;
-    const __half *weights;
     const nbvh_ray *rays;
     nbvh_neural_hit *hits;
     QueryCounters *counters;
     uint32_t *fallback_list;
     WaveList lists[2];
-    uint32_t *wave_counts; // 3 rotating list counters
+    uint32_t *wave_counts; // 3 rotating list counters + the MLP's error word
+    __half *features;      // [capacity][n_inputs] FP16 rows of the current step
+    float *outputs;        // [capacity][8] network outputs of the current step
     uint32_t n_hidden_layers;
     uint32_t n;
     uint32_t n_cut_nodes;
@@ -119,89 +127,182 @@ __device__ __forceinline__ uint32_t warp_append(bool want, uint32_t *counter)
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(256) k_wave_first(const __grid_constant__ WaveArgs a)
+// K2 first pass: the first entered leaf of every ray (the first leaf is searched with an unbounded
+// current_maxt, include/cuda/neural/neural_bvh_module_common.cuh:332-343). Rays that enter none
+// are answered at once; the others are appended to state list 0. Persistent warps take rays from
+// a work counter and refill lanes between rounds of kVisitsPerRound node visits, as the decode
+// kernel does, so the warp's lanes stay busy while the traversal lengths differ.
+__global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_constant__ WaveArgs a)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool listed = false;
+    const int lane = threadIdx.x & 31;
+    uint32_t *head = &a.wave_counts[7];
     RayState s;
     uint32_t stack[kNeuralStackSize];
-    if (i < a.n) {
-        const float4 *r = reinterpret_cast<const float4 *>(a.rays + i);
-        const float4 ra = __ldg(r), rb = __ldg(r + 1);
-        s.o = mk3(ra.x, ra.y, ra.z);
-        s.d = mk3(rb.x, rb.y, rb.z);
-        const bool cull_ok = s.d.x != 0.0f && s.d.y != 0.0f && s.d.z != 0.0f;
-        const RayDiv rdiv = make_raydiv(s.o, s.d, a.nc.fast_div_ok != 0u);
-        s.sp = 1;
-        stack[0] = 0;
-        const GlobalCut cut{a.nodes, a.bounds};
-        // the first leaf is searched with an unbounded current_maxt (common.cuh:332-343)
-        const int res = neural_intersect_inference(cut, a.nc.bvh_lod, s.o, rdiv, cull_ok, stack, s.sp,
-                                                   a.nc.inference_mint_epsilon, a.nc.inference_maxt_epsilon, FLT_MAX,
-                                                   s.seg_mint, s.seg_maxt, s.seg_node);
-        if (res == 1) {
-            if (a.non_neural && a.non_neural[s.seg_node]) {
-                write_hit(a.hits, i, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, 0u, 0u);
-                const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
-                a.fallback_list[slot] = i;
-                atomicAdd(&a.counters->fallback, 1u);
-            } else {
-                listed = true;
-                s.best_t = rb.w; // the ray's tmax plays the role of the current closest hit
-                s.vis = 0.f;
-                s.nrm = mk3(0, 0, 0);
-                s.alb = mk3(0, 0, 0);
+    RayDiv rdiv;
+    bool cull_ok = false, active = false, exhausted = false;
+    float tmax = 0.f;
+    const GlobalCut cut{a.nodes, a.bounds};
+    for (;;) {
+        const unsigned idle = __ballot_sync(kFull, !active);
+        if (idle != 0u && !exhausted) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader)
+                base = atomicAdd(head, (uint32_t)__popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            exhausted = base + (uint32_t)__popc(idle) >= a.n;
+            const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
+            if (!active && i < a.n) {
+                const float4 *r = reinterpret_cast<const float4 *>(a.rays + i);
+                const float4 ra = __ldg(r), rb = __ldg(r + 1);
+                s.o = mk3(ra.x, ra.y, ra.z);
+                s.d = mk3(rb.x, rb.y, rb.z);
+                tmax = rb.w;
+                cull_ok = s.d.x != 0.0f && s.d.y != 0.0f && s.d.z != 0.0f;
+                rdiv = make_raydiv(s.o, s.d, a.nc.fast_div_ok != 0u);
+                s.sp = 1;
+                stack[0] = 0;
                 s.ray_id = i;
-                s.segments = 0;
-                s.flags = 0;
-                s.rng = lcg_seed(0u, 0u, i);
+                active = true;
             }
-        } else {
-            if (res < 0)
-                atomicAdd(&a.counters->stack_overflow, 1u);
-            write_hit(a.hits, i, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, res < 0 ? 0x8u : 0u, 0u);
         }
+        if (!__any_sync(kFull, active)) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        bool listed = false;
+        if (active) {
+            const int res = neural_intersect_inference(cut, a.nc.bvh_lod, s.o, rdiv, cull_ok, stack, s.sp,
+                                                       a.nc.inference_mint_epsilon, a.nc.inference_maxt_epsilon,
+                                                       FLT_MAX, s.seg_mint, s.seg_maxt, s.seg_node, kVisitsPerRound);
+            if (res != 2) {
+                active = false;
+                const uint32_t i = s.ray_id;
+                if (res == 1) {
+                    if (a.non_neural && a.non_neural[s.seg_node]) {
+                        write_hit(a.hits, i, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, 0u, 0u);
+                        const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
+                        a.fallback_list[slot] = i;
+                        atomicAdd(&a.counters->fallback, 1u);
+                    } else {
+                        listed = true;
+                        s.best_t = tmax; // the ray's tmax plays the role of the current closest hit
+                        s.vis = 0.f;
+                        s.nrm = mk3(0, 0, 0);
+                        s.alb = mk3(0, 0, 0);
+                        s.segments = 0;
+                        s.flags = 0;
+                        s.rng = lcg_seed(0u, 0u, i);
+                    }
+                } else {
+                    if (res < 0)
+                        atomicAdd(&a.counters->stack_overflow, 1u);
+                    write_hit(a.hits, i, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, res < 0 ? 0x8u : 0u, 0u);
+                }
+            }
+        }
+        const uint32_t pos = warp_append(listed, &a.wave_counts[0]);
+        if (listed)
+            store_state(a.lists[0], pos, s, stack);
     }
-    const uint32_t pos = warp_append(listed, &a.wave_counts[0]);
-    if (listed)
-        store_state(a.lists[0], pos, s, stack);
 }
 
-template <bool SMEM_CUT>
-__global__ void __launch_bounds__(kStepThreads, 1) k_wave_step(const __grid_constant__ WaveArgs a, uint32_t it)
+// K3 of one step: the FP16 hash-grid features of every listed ray's current leaf segment, one
+// thread per (ray, point) looping over the levels, written row-major to features[row][n_inputs]
+// (point-major, then level, 2 features per level). Points follow encode_bvh_network_input_data
+// (src/cuda/neural/neural_bvh_module_kernels.cu:266-303): the segment ends are swapped for a
+// negative mint, then encoded into the dilated scene box. The point is computed once for all its
+// levels, so the kernel's instructions go to the gathers and their interpolation; it holds no
+// MLP state and runs at high occupancy to hide the gather latency.
+__global__ void __launch_bounds__(kEncodeThreads) k_wave_encode(const __grid_constant__ WaveArgs a, uint32_t it)
 {
-    const uint32_t count_in = *reinterpret_cast<volatile const uint32_t *>(&a.wave_counts[it % 3u]);
-    uint32_t *count_out = &a.wave_counts[(it + 1u) % 3u];
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        a.wave_counts[(it + 2u) % 3u] = 0u; // output counter of the next step (last read a step ago)
-    const uint32_t n_tiles = (count_in + 31u) / 32u;
-    if (blockIdx.x * kStepWarps >= n_tiles)
-        return; // nothing for this block: skip staging the network
-
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    GridParams &gp = *reinterpret_cast<GridParams *>(smem_raw);
-    const uint32_t n_inputs = a.grid.n_inputs, P = a.grid.n_points, L = a.grid.n_levels;
-    const SmemNetLayout SL = smem_net_layout(n_inputs, a.n_hidden_layers);
-    __half *sw = reinterpret_cast<__half *>(smem_raw + sizeof(GridParams));
-    unsigned char *after_net = reinterpret_cast<unsigned char *>(sw + SL.total);
-    const uint32_t cut_bytes = SMEM_CUT ? a.n_cut_nodes * 56u : 0u;
-    float *warp_area = reinterpret_cast<float *>(after_net + cut_bytes);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float *pts = warp_area + (size_t)warp * 32u * (P * 3u + 8u); // [32][P*3]
-    float *outs = pts + 32u * P * 3u;                            // [32][8]
-    const uint32_t fld = n_inputs + 8u;
-    __half *feat = reinterpret_cast<__half *>(warp_area + (size_t)kStepWarps * 32u * (P * 3u + 8u)) +
-                   (size_t)warp * 16u * fld; // per-warp 16-row feature tile
-    (void)L;
+    __shared__ GridParams gp;
     {
         const uint32_t *src = reinterpret_cast<const uint32_t *>(&a.grid);
         uint32_t *dst = reinterpret_cast<uint32_t *>(&gp);
         for (uint32_t i = threadIdx.x; i < sizeof(GridParams) / 4u; i += blockDim.x)
             dst[i] = src[i];
     }
-    load_weights_to_smem(a.weights, sw, n_inputs, a.n_hidden_layers);
-    float4 *s_nodes = reinterpret_cast<float4 *>(after_net);
-    float2 *s_bounds = reinterpret_cast<float2 *>(after_net + a.n_cut_nodes * 32u);
+    __syncthreads();
+    const uint32_t count_in = *reinterpret_cast<volatile const uint32_t *>(&a.wave_counts[it % 3u]);
+    const uint32_t L = gp.n_levels, P = gp.n_points;
+    const WaveList &in = a.lists[it & 1u];
+    const NeuralConsts &nc = a.nc;
+    const V3 smin = mk3(nc.scene_min[0], nc.scene_min[1], nc.scene_min[2]);
+    const V3 smax = mk3(nc.scene_max[0], nc.scene_max[1], nc.scene_max[2]);
+    const float dilation = __fadd_rn(__fadd_rn(1.0f, nc.node_extent_dilation), nc.fixed_node_dilation);
+    const V3 ext = scale3(sub3(smax, smin), dilation);
+    const V3 center = scale3(add3(smax, smin), 0.5f);
+    const bool vec_store = (L & 3u) == 0u; // each point's block of L words starts 16-byte aligned
+    uint32_t *feat = reinterpret_cast<uint32_t *>(a.features);
+    const uint32_t total = count_in * P; // at most 2^22 rays x 16 points
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const uint32_t row = g / P, p = g - row * P;
+        const float4 od0 = in.od0[row], od1 = in.od1[row];
+        const V3 o = mk3(od0.x, od0.y, od0.z), d = mk3(od1.x, od1.y, od1.z);
+        float ta = od1.w, tb = __uint_as_float(in.meta[row].x);
+        if (ta < 0.0f) { // swap for a negative mint (neural_bvh_module_kernels.cu:281-286)
+            const float t = ta;
+            ta = tb;
+            tb = t;
+        }
+        const V3 epo = encode_world(ray_at(o, d, ta), center, ext);
+        const V3 epi = encode_world(ray_at(o, d, tb), center, ext);
+        float t;
+        if (gp.segment_distribution == NBVH_SEGMENT_UNIFORM) {
+            uint32_t rng = __float_as_uint(in.ar[row].w);
+            for (uint32_t k = 0; k <= p; k++)
+                t = lcg_randomf(rng);
+        } else {
+            uint32_t unused = 0;
+            t = segment_t(p, P, gp.segment_distribution, unused);
+        }
+        const V3 pos = segment_point(epo, epi, t);
+        uint32_t *dst = feat + (size_t)g * L; // row * (P * L) + p * L
+        if (vec_store) {
+            for (uint32_t l = 0; l < L; l += 4u) {
+                uint4 q;
+                float2 f = encode_level(a.table, gp, l, pos);
+                q.x = pack_half2(f.x, f.y);
+                f = encode_level(a.table, gp, l + 1u, pos);
+                q.y = pack_half2(f.x, f.y);
+                f = encode_level(a.table, gp, l + 2u, pos);
+                q.z = pack_half2(f.x, f.y);
+                f = encode_level(a.table, gp, l + 3u, pos);
+                q.w = pack_half2(f.x, f.y);
+                *reinterpret_cast<uint4 *>(dst + l) = q;
+            }
+        } else {
+            for (uint32_t l = 0; l < L; l++) {
+                const float2 f = encode_level(a.table, gp, l, pos);
+                dst[l] = pack_half2(f.x, f.y);
+            }
+        }
+    }
+}
+
+// K2 of one step: decode the network outputs of each listed ray's segment (process step,
+// src/cuda/neural/path/path_inference_kernels.cu:61-131), keep the closest hit, then find the
+// next entered leaf (process_bvh_network_output_and_intersect_neural_bvh,
+// include/cuda/neural/neural_bvh_module_common.cuh:496-550) and append the ray to the next list,
+// or write its final record. One thread per listed ray.
+template <bool SMEM_CUT>
+__global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_wave_decode(const __grid_constant__ WaveArgs a,
+                                                                                   uint32_t it)
+{
+    const uint32_t count_in = *reinterpret_cast<volatile const uint32_t *>(&a.wave_counts[it % 3u]);
+    uint32_t *count_out = &a.wave_counts[(it + 1u) % 3u];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.wave_counts[(it + 2u) % 3u] = 0u;      // output counter of the next step (last read a step ago)
+        a.wave_counts[4u + (it + 1u) % 3u] = 0u; // work counter of the next step
+    }
+    if (blockIdx.x * blockDim.x >= count_in)
+        return; // nothing for this block: skip staging the cut
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4 *s_nodes = reinterpret_cast<float4 *>(smem_raw);
+    float2 *s_bounds = reinterpret_cast<float2 *>(smem_raw + a.n_cut_nodes * 32u);
     if (SMEM_CUT) {
         for (uint32_t i = threadIdx.x; i < 2u * a.n_cut_nodes; i += blockDim.x)
             s_nodes[i] = __ldg(a.nodes + i);
@@ -211,8 +312,8 @@ __global__ void __launch_bounds__(kStepThreads, 1) k_wave_step(const __grid_cons
             s_bounds[3u * i + 1u] = make_float2(u.z, v.x);
             s_bounds[3u * i + 2u] = make_float2(v.y, v.z);
         }
+        __syncthreads();
     }
-    __syncthreads();
     using Cut = typename std::conditional<SMEM_CUT, SharedCut, GlobalCut>::type;
     Cut cut;
     if constexpr (SMEM_CUT) {
@@ -224,148 +325,136 @@ __global__ void __launch_bounds__(kStepThreads, 1) k_wave_step(const __grid_cons
     }
 
     const NeuralConsts &nc = a.nc;
-    const V3 smin = mk3(nc.scene_min[0], nc.scene_min[1], nc.scene_min[2]);
-    const V3 smax = mk3(nc.scene_max[0], nc.scene_max[1], nc.scene_max[2]);
-    const float dilation = __fadd_rn(__fadd_rn(1.0f, nc.node_extent_dilation), nc.fixed_node_dilation);
-    const V3 ext = scale3(sub3(smax, smin), dilation);
-    const V3 center = scale3(add3(smax, smin), 0.5f);
     const float thr = nc.visibility_threshold;
+    const uint32_t P = a.grid.n_points;
     const WaveList &in = a.lists[it & 1u];
     const WaveList &out = a.lists[(it + 1u) & 1u];
+    const int lane = threadIdx.x & 31;
     uint32_t st_segments = 0, st_capped = 0, st_overflow = 0, st_fallback = 0;
 
-    for (uint32_t tile = blockIdx.x * kStepWarps + warp; tile < n_tiles; tile += gridDim.x * kStepWarps) {
-        const uint32_t row = tile * 32u + (uint32_t)lane;
-        bool active = row < count_in;
-        RayState s;
-        uint32_t stack[kNeuralStackSize];
-        if (active) {
-            load_state(in, row, s, stack);
-            if (s.segments > nc.max_traversal_steps) { // step cap (path_module.cu:68, last_inference)
-                s.flags |= NBVH_HIT_STEP_CAP;
-                st_capped++;
-                const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
-                write_hit(a.hits, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f, s.flags,
-                          s.segments);
-                active = false;
-            }
-        }
-        if (active) {
-            float ta = s.seg_mint, tb = s.seg_maxt;
-            if (ta < 0.0f) { // encode_bvh_network_input_data swaps for a negative mint (kernels.cu:281-286)
-                const float t = ta;
-                ta = tb;
-                tb = t;
-            }
-            const V3 epo = encode_world(ray_at(s.o, s.d, ta), center, ext);
-            const V3 epi = encode_world(ray_at(s.o, s.d, tb), center, ext);
-            for (uint32_t k = 0; k < P; k++) {
-                const V3 p = segment_point(epo, epi, segment_t(k, P, a.grid.segment_distribution, s.rng));
-                float *dst = pts + (lane * P + k) * 3u;
-                dst[0] = p.x;
-                dst[1] = p.y;
-                dst[2] = p.z;
-            }
-        }
-        const unsigned act_mask = __ballot_sync(kFull, active);
-        __syncwarp();
-#pragma unroll 1
-        for (int half = 0; half < 2; half++) {
-            const uint32_t mask = (act_mask >> (half * 16)) & 0xFFFFu;
-            if (mask == 0u)
-                continue;
-            const int g = lane >> 2, tig = lane & 3;
-            const int r0 = half * 16 + g, r1 = r0 + 8;
-            auto pos = [&](uint32_t r, uint32_t p) -> V3 {
-                const float *src = pts + ((half * 16u + r) * P + p) * 3u;
-                return mk3(src[0], src[1], src[2]);
-            };
-            encode_tile_to_smem(a.table, gp, pos, mask, feat, fld);
-            float o4[4];
-            mlp_tile_from_smem(sw, feat, fld, n_inputs, a.n_hidden_layers, o4);
-            outs[r0 * 8 + tig * 2] = o4[0];
-            outs[r0 * 8 + tig * 2 + 1] = o4[1];
-            outs[r1 * 8 + tig * 2] = o4[2];
-            outs[r1 * 8 + tig * 2 + 1] = o4[3];
-            __syncwarp();
-        }
-        __syncwarp();
-
-        bool keep = false;
-        if (active) {
-            float o8[8];
-#pragma unroll
-            for (int k = 0; k < 8; k++)
-                o8[k] = outs[lane * 8 + k];
-            s.segments++;
-            st_segments++;
-            bool done = false;
-            if (nc.fallback_margin > 0.0f && fabsf(__fsub_rn(o8[0], thr)) < nc.fallback_margin) {
-                write_hit(a.hits, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, s.flags & ~NBVH_HIT_VALID,
-                          s.segments);
-                const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
-                a.fallback_list[slot] = s.ray_id;
-                st_fallback++;
-                done = true;
-            } else {
-                // process_neural_bvh_traversal_step, src/cuda/neural/path/path_inference_kernels.cu:61-131
-                float new_depth = s.best_t;
-                bool stop = false;
-                if (o8[0] > thr) {
-                    const bool inside = s.seg_mint < 0.0f;
-                    if (nc.visibility_only && !inside) {
-                        s.flags |= NBVH_HIT_VALID;
-                        s.vis = o8[0];
-                        stop = true;
+    // Persistent warps with per-lane refill (after Aila and Laine, "Understanding the efficiency of
+    // ray traversal on GPUs", HPG 2009): the next-leaf search takes a different number of node
+    // visits per ray, so each round runs at most kVisitsPerRound visits, after which lanes whose ray
+    // is done take a new row from the step's work counter. Lanes stay busy instead of waiting for
+    // the longest traversal of their warp. All lanes run every round (warp_append needs all 32).
+    uint32_t *head = &a.wave_counts[4u + it % 3u];
+    RayState s;
+    uint32_t stack[kNeuralStackSize];
+    RayDiv rdiv;
+    bool cull_ok = false, active = false, exhausted = false;
+    for (;;) {
+        const unsigned idle = __ballot_sync(kFull, !active);
+        if (idle != 0u && !exhausted) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader)
+                base = atomicAdd(head, (uint32_t)__popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            exhausted = base + (uint32_t)__popc(idle) >= count_in;
+            const uint32_t row = base + __popc(idle & ((1u << lane) - 1u));
+            if (!active && row < count_in) {
+                load_state(in, row, s, stack);
+                bool traverse = false;
+                if (s.segments > nc.max_traversal_steps) { // step cap (path_module.cu:68, last_inference)
+                    s.flags |= NBVH_HIT_STEP_CAP;
+                    st_capped++;
+                    const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
+                    write_hit(a.hits, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f,
+                              s.flags, s.segments);
+                } else {
+                    if (a.grid.segment_distribution == NBVH_SEGMENT_UNIFORM)
+                        for (uint32_t k = 0; k < P; k++) // the draws the encoder made for this segment
+                            (void)lcg_randomf(s.rng);
+                    const float4 *src = reinterpret_cast<const float4 *>(a.outputs + (size_t)row * 8u);
+                    const float4 oa = src[0], ob = src[1];
+                    const float o8[8] = {oa.x, oa.y, oa.z, oa.w, ob.x, ob.y, ob.z, ob.w};
+                    s.segments++;
+                    st_segments++;
+                    if (nc.fallback_margin > 0.0f && fabsf(__fsub_rn(o8[0], thr)) < nc.fallback_margin) {
+                        write_hit(a.hits, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, s.flags & ~NBVH_HIT_VALID,
+                                  s.segments);
+                        const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
+                        a.fallback_list[slot] = s.ray_id;
+                        st_fallback++;
                     } else {
-                        const float de = decode_local_t(o8[1], s.seg_mint, s.seg_maxt, inside, nc.depth_epsilon,
-                                                        nc.fixed_depth_epsilon);
-                        if (de != FLT_MAX) {
-                            if (nc.visibility_only) {
+                        // process_neural_bvh_traversal_step, path_inference_kernels.cu:61-131
+                        bool stop = false;
+                        if (o8[0] > thr) {
+                            const bool inside = s.seg_mint < 0.0f;
+                            if (nc.visibility_only && !inside) {
                                 s.flags |= NBVH_HIT_VALID;
                                 s.vis = o8[0];
                                 stop = true;
-                            } else if (de < s.best_t) {
-                                s.flags |= NBVH_HIT_VALID;
-                                s.best_t = de;
-                                new_depth = de;
-                                s.vis = o8[0];
-                                s.nrm = normalize3(mk3(__fsub_rn(__fmul_rn(o8[2], 2.0f), 1.0f),
-                                                       __fsub_rn(__fmul_rn(o8[3], 2.0f), 1.0f),
-                                                       __fsub_rn(__fmul_rn(o8[4], 2.0f), 1.0f)));
-                                s.alb = mk3(o8[5], o8[6], o8[7]);
+                            } else {
+                                const float de = decode_local_t(o8[1], s.seg_mint, s.seg_maxt, inside, nc.depth_epsilon,
+                                                                nc.fixed_depth_epsilon);
+                                if (de != FLT_MAX) {
+                                    if (nc.visibility_only) {
+                                        s.flags |= NBVH_HIT_VALID;
+                                        s.vis = o8[0];
+                                        stop = true;
+                                    } else if (de < s.best_t) {
+                                        s.flags |= NBVH_HIT_VALID;
+                                        s.best_t = de;
+                                        s.vis = o8[0];
+                                        s.nrm = normalize3(mk3(__fsub_rn(__fmul_rn(o8[2], 2.0f), 1.0f),
+                                                               __fsub_rn(__fmul_rn(o8[3], 2.0f), 1.0f),
+                                                               __fsub_rn(__fmul_rn(o8[4], 2.0f), 1.0f)));
+                                        s.alb = mk3(o8[5], o8[6], o8[7]);
+                                    }
+                                }
                             }
                         }
+                        traverse = !stop && s.sp > 0;
+                        if (!traverse) {
+                            const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
+                            write_hit(a.hits, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f,
+                                      s.flags, s.segments);
+                        }
                     }
                 }
-                // process_bvh_network_output_and_intersect_neural_bvh, common.cuh:496-550
-                if (!stop && s.sp > 0) {
-                    const bool cull_ok = s.d.x != 0.0f && s.d.y != 0.0f && s.d.z != 0.0f;
-                    const RayDiv rdiv = make_raydiv(s.o, s.d, nc.fast_div_ok != 0u);
-                    const int res = neural_intersect_inference(cut, nc.bvh_lod, s.o, rdiv, cull_ok, stack, s.sp,
-                                                               nc.inference_mint_epsilon, nc.inference_maxt_epsilon,
-                                                               new_depth, s.seg_mint, s.seg_maxt, s.seg_node);
-                    if (res == 1) {
-                        if (a.non_neural && a.non_neural[s.seg_node]) {
-                            write_hit(a.hits, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f,
-                                      s.flags & ~NBVH_HIT_VALID, s.segments);
-                            const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
-                            a.fallback_list[slot] = s.ray_id;
-                            st_fallback++;
-                            done = true;
-                        } else {
-                            keep = true;
-                        }
-                    } else if (res < 0) {
-                        s.flags |= 0x8u;
-                        st_overflow++;
-                    }
+                if (traverse) {
+                    active = true;
+                    cull_ok = s.d.x != 0.0f && s.d.y != 0.0f && s.d.z != 0.0f;
+                    rdiv = make_raydiv(s.o, s.d, nc.fast_div_ok != 0u);
                 }
             }
-            if (!keep && !done) {
-                const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
-                write_hit(a.hits, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f, s.flags,
-                          s.segments);
+        }
+        if (!__any_sync(kFull, active)) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        bool keep = false;
+        if (active) {
+            // process_bvh_network_output_and_intersect_neural_bvh, common.cuh:496-550; the closest
+            // hit so far (best_t) bounds the search
+            const int res = neural_intersect_inference(cut, nc.bvh_lod, s.o, rdiv, cull_ok, stack, s.sp,
+                                                       nc.inference_mint_epsilon, nc.inference_maxt_epsilon, s.best_t,
+                                                       s.seg_mint, s.seg_maxt, s.seg_node, kVisitsPerRound);
+            if (res != 2) {
+                active = false;
+                bool done = false;
+                if (res == 1) {
+                    if (a.non_neural && a.non_neural[s.seg_node]) {
+                        write_hit(a.hits, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, s.flags & ~NBVH_HIT_VALID,
+                                  s.segments);
+                        const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
+                        a.fallback_list[slot] = s.ray_id;
+                        st_fallback++;
+                        done = true;
+                    } else {
+                        keep = true;
+                    }
+                } else if (res < 0) {
+                    s.flags |= 0x8u;
+                    st_overflow++;
+                }
+                if (!keep && !done) {
+                    const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
+                    write_hit(a.hits, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f, s.flags,
+                              s.segments);
+                }
             }
         }
         const uint32_t pos = warp_append(keep, count_out);
@@ -391,49 +480,56 @@ __global__ void __launch_bounds__(kStepThreads, 1) k_wave_step(const __grid_cons
     }
 }
 
-size_t step_smem(uint32_t n_inputs, uint32_t n_hidden, uint32_t n_points, uint32_t cut_nodes)
-{
-    return sizeof(GridParams) + smem_net_layout(n_inputs, n_hidden).total * sizeof(__half) + (size_t)cut_nodes * 56u +
-           (size_t)kStepWarps * 32u * (n_points * 3u + 8u) * sizeof(float) +
-           (size_t)kStepWarps * 16u * (n_inputs + 8u) * sizeof(__half);
-}
-
 constexpr size_t kSmemLimit = 227u * 1024u;
 constexpr uint32_t kStepsPerCheck = 4;
 
+// One batch of steps per host check; each step is K3 -> K4 -> K2 on the stream.
 template <bool SMEM_CUT>
-cudaError_t run_steps(const WaveArgs &a, size_t smem, int num_sms, uint32_t max_steps, uint32_t *h_count,
-                      cudaEvent_t ev, cudaStream_t s, uint32_t &launches)
+cudaError_t run_steps(const WaveArgs &a, const StepResources &r, size_t dec_smem, int num_sms, uint32_t max_steps,
+                      cudaStream_t s, uint32_t &launches)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_wave_step<SMEM_CUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_wave_decode<SMEM_CUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)dec_smem);
     if (e != cudaSuccess)
         return e;
+    const uint32_t enc_blocks = (uint32_t)num_sms * (2048u / kEncodeThreads);
+    const uint32_t dec_blocks = (uint32_t)num_sms * (SMEM_CUT ? 1u : 2u);
     // every listed ray advances one leaf per step; the loop ends when a list comes out empty or the
     // step cap (each ray at most max_traversal_steps + 1 segments) plus the final capping step is reached
     const uint32_t limit = max_steps + 2u;
     for (uint32_t it = 0; it < limit;) {
         const uint32_t batch = (limit - it) < kStepsPerCheck ? (limit - it) : kStepsPerCheck;
         for (uint32_t b = 0; b < batch; b++, it++) {
-            k_wave_step<SMEM_CUT><<<num_sms, kStepThreads, smem, s>>>(a, it);
+            k_wave_encode<<<enc_blocks, kEncodeThreads, 0, s>>>(a, it);
             e = cudaGetLastError();
             if (e != cudaSuccess)
                 return e;
-            launches++;
-        }
-        e = cudaMemcpyAsync(h_count, &a.wave_counts[it % 3u], sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        if (e != cudaSuccess)
-            return e;
-        if (ev) {
-            e = cudaEventRecord(ev, s);
+            e = launch_mlp_tc(r.feature_map, r.wpacked, a.grid.n_inputs, a.n_hidden_layers, a.lists[0].capacity,
+                              &a.wave_counts[it % 3u], a.outputs, &a.wave_counts[3], num_sms, s);
             if (e != cudaSuccess)
                 return e;
-            e = cudaEventSynchronize(ev);
+            k_wave_decode<SMEM_CUT><<<dec_blocks, decode_threads(SMEM_CUT), dec_smem, s>>>(a, it);
+            e = cudaGetLastError();
+            if (e != cudaSuccess)
+                return e;
+            launches += 3u;
+        }
+        e = cudaMemcpyAsync(r.h_words, a.wave_counts, 4u * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess)
+            return e;
+        if (r.ev) {
+            e = cudaEventRecord(r.ev, s);
+            if (e != cudaSuccess)
+                return e;
+            e = cudaEventSynchronize(r.ev);
         } else {
             e = cudaStreamSynchronize(s);
         }
         if (e != cudaSuccess)
             return e;
-        if (*h_count == 0u)
+        if (r.h_words[3] != 0u)
+            return cudaErrorTimeout; // a bounded wait inside the tensor-core MLP gave up
+        if (r.h_words[it % 3u] == 0u)
             break;
     }
     return cudaSuccess;
@@ -445,8 +541,8 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
                               const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
                               const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
                               nbvh_neural_hit *hits, QueryCounters *counters, uint32_t *fallback_list,
-                              const WaveList lists[2], uint32_t *wave_counts, uint32_t *h_count, cudaEvent_t ev,
-                              int num_sms, cudaStream_t s, uint32_t *launches)
+                              const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, int num_sms,
+                              cudaStream_t s, uint32_t *launches)
 {
     *launches = 0;
     if (n == 0)
@@ -460,7 +556,6 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     const uint32_t n_network_params =
         kNeurons * grid.n_inputs + (n_hidden_layers - 1u) * kNeurons * kNeurons + kOutputsPadded * kNeurons;
     a.table = reinterpret_cast<const uint32_t *>(params_h + n_network_params);
-    a.weights = params_h;
     a.rays = rays;
     a.hits = hits;
     a.counters = counters;
@@ -468,22 +563,32 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     a.lists[0] = lists[0];
     a.lists[1] = lists[1];
     a.wave_counts = wave_counts;
+    a.features = res.features;
+    a.outputs = res.outputs;
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
     a.n_cut_nodes = n_cut_nodes;
-    cudaError_t e = cudaMemsetAsync(wave_counts, 0, 3u * sizeof(uint32_t), s);
+    // words 0-2: rotating list lengths; 3: the MLP's error word; 4-6: rotating work counters of
+    // the decode kernel; 7: work counter of the first pass
+    cudaError_t e = cudaMemsetAsync(wave_counts, 0, 8u * sizeof(uint32_t), s);
     if (e != cudaSuccess)
         return e;
-    k_wave_first<<<(n + 255u) / 256u, 256, 0, s>>>(a);
+    e = launch_pack_weights(params_h, grid.n_inputs, n_hidden_layers, res.wpacked, s);
+    if (e != cudaSuccess)
+        return e;
+    uint32_t first_blocks = (n + kFirstThreads - 1u) / kFirstThreads;
+    const uint32_t first_cap = (uint32_t)num_sms * 4u; // resident blocks (64 registers a thread)
+    if (first_blocks > first_cap)
+        first_blocks = first_cap;
+    k_wave_first<<<first_blocks, kFirstThreads, 0, s>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
-    *launches = 1;
-    const size_t smem_cut = step_smem(grid.n_inputs, n_hidden_layers, grid.n_points, n_cut_nodes);
+    *launches = 2;
+    const size_t smem_cut = (size_t)n_cut_nodes * 56u;
     if (smem_cut <= kSmemLimit)
-        return run_steps<true>(a, smem_cut, num_sms, nc.max_traversal_steps, h_count, ev, s, *launches);
-    return run_steps<false>(a, step_smem(grid.n_inputs, n_hidden_layers, grid.n_points, 0u), num_sms,
-                            nc.max_traversal_steps, h_count, ev, s, *launches);
+        return run_steps<true>(a, res, smem_cut, num_sms, nc.max_traversal_steps, s, *launches);
+    return run_steps<false>(a, res, 0, num_sms, nc.max_traversal_steps, s, *launches);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -526,6 +631,12 @@ cudaError_t noalloc_scratch(int device, NoallocScratch *out)
         L.capacity = (uint32_t)n;
         p += kNoallocListBytes;
     }
+    out->features = reinterpret_cast<__half *>(p);
+    p += kNoallocFeatureBytes;
+    out->outputs = reinterpret_cast<float *>(p);
+    p += kNoallocOutputBytes;
+    out->wpacked = reinterpret_cast<__half *>(p);
+    p += kNoallocWeightBytes;
     out->fallback_list = reinterpret_cast<uint32_t *>(p);
     p += n * 4u;
     out->counters = reinterpret_cast<QueryCounters *>(p);

@@ -30,6 +30,8 @@ void cuda_check(cudaError_t e, const char *what)
     if (e != cudaSuccess) {
         if (e == cudaErrorMemoryAllocation)
             fail(NBVH_ENOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+        if (e == cudaErrorTimeout)
+            fail(NBVH_ETIMEOUT, std::string(what) + ": a bounded device-side wait gave up");
         fail(NBVH_EDEVICE, std::string(what) + ": " + cudaGetErrorString(e));
     }
 }
@@ -354,13 +356,17 @@ void ensure_query_workspace(nbvh_handle *h, uint32_t n, int ctx)
     QueryContext &q = h->qctx[ctx];
     if (q.fallback_list.count < n)
         cuda_check(q.fallback_list.resize(n), "alloc fallback list");
-    if (q.wave_counts.count < 4u)
-        cuda_check(q.wave_counts.resize(4u), "alloc wave counters");
-    if (!q.h_count) {
-        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&q.h_count), sizeof(uint32_t), cudaHostAllocDefault),
-                   "pinned counter");
-        *q.h_count = 0;
+    if (q.wave_counts.count < 8u)
+        cuda_check(q.wave_counts.resize(8u), "alloc wave counters");
+    if (!q.h_words) {
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&q.h_words), 4u * sizeof(uint32_t), cudaHostAllocDefault),
+                   "pinned counters");
+        for (int k = 0; k < 4; k++)
+            q.h_words[k] = 0;
     }
+    const uint32_t wb = packed_weight_bytes(h->layout.n_inputs, (uint32_t)h->cfg.network.n_hidden_layers);
+    if (q.wpacked.count < wb / 2u)
+        cuda_check(q.wpacked.resize(wb / 2u), "alloc packed weights");
     if (!q.ev)
         cuda_check(cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming), "event");
     if (q.capacity < n) {
@@ -372,6 +378,8 @@ void ensure_query_workspace(nbvh_handle *h, uint32_t n, int ctx)
             cuda_check(q.meta[k].resize(n), "alloc wave state");
             cuda_check(q.stack[k].resize((size_t)kNeuralStackSize * n), "alloc wave stacks");
         }
+        cuda_check(q.features.resize((size_t)n * h->layout.n_inputs), "alloc feature rows");
+        cuda_check(q.outputs.resize((size_t)n * kOutputs), "alloc network outputs");
         q.capacity = n;
     }
 }
@@ -407,10 +415,17 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
     for (int k = 0; k < 2; k++)
         lists[k] = WaveList{q.od0[k].ptr, q.od1[k].ptr, q.nv[k].ptr, q.ar[k].ptr, q.meta[k].ptr, q.stack[k].ptr, q.capacity};
     uint32_t launches = 0;
+    StepResources res;
+    res.features = q.features.ptr;
+    res.outputs = q.outputs.ptr;
+    res.wpacked = q.wpacked.ptr;
+    res.h_words = q.h_words;
+    res.ev = q.ev;
+    cuda_check(make_feature_map(q.features.ptr, h->layout.n_inputs, q.capacity, &res.feature_map), "feature map");
     cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),
                                  h->any_non_neural ? h->d_non_neural.ptr : nullptr, h->d_params_h.ptr, h->grid, nc,
                                  (uint32_t)h->cfg.network.n_hidden_layers, d_rays, n, d_hits, counters, list, lists,
-                                 q.wave_counts.ptr, q.h_count, q.ev, h->num_sms, s, &launches),
+                                 q.wave_counts.ptr, res, h->num_sms, s, &launches),
                "neural query");
     if (timed)
         cuda_check(cudaEventRecord(h->ev1, s), "event");
@@ -447,12 +462,20 @@ void neural_query_noalloc(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, ui
                    "classic");
     } else {
         const NeuralConsts nc = make_neural_consts(h, depth, false);
-        uint32_t host_count = 0, launches = 0;
+        uint32_t host_words[4] = {0, 0, 0, 0}, launches = 0;
+        StepResources res;
+        res.features = sc.features;
+        res.outputs = sc.outputs;
+        res.wpacked = sc.wpacked;
+        res.h_words = host_words;
+        res.ev = nullptr;
+        cuda_check(make_feature_map(sc.features, h->layout.n_inputs, (uint32_t)kNoallocRays, &res.feature_map),
+                   "feature map");
         cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr,
                                      (uint32_t)h->neural_nodes.size(), h->any_non_neural ? h->d_non_neural.ptr : nullptr,
                                      h->d_params_h.ptr, h->grid, nc, (uint32_t)h->cfg.network.n_hidden_layers, d_rays,
-                                     n, d_hits, sc.counters, sc.fallback_list, sc.lists, sc.wave_counts, &host_count,
-                                     nullptr, h->num_sms, s, &launches),
+                                     n, d_hits, sc.counters, sc.fallback_list, sc.lists, sc.wave_counts, res,
+                                     h->num_sms, s, &launches),
                    "neural query");
         if (h->any_non_neural || h->cfg.fallback_margin > 0.f)
             cuda_check(launch_classic_fallback(h->d_nodes.ptr, h->d_tris.ptr, d_rays, sc.fallback_list, sc.counters,
@@ -915,9 +938,12 @@ nbvh_status nbvh_mlp_inference(nbvh_handle *h, const uint16_t *d_features, uint3
             cuda_check(h->d_status.resize(1u), "alloc status");
         cuda_check(cudaMemsetAsync(h->d_status.ptr, 0, sizeof(uint32_t), s), "reset status");
         cuda_check(launch_pack_weights(h->d_params_h.ptr, ni, H, h->d_wpacked.ptr, s), "pack weights");
+        if (n == 0)
+            return;
+        TensorMapBytes map;
+        cuda_check(make_feature_map(reinterpret_cast<const __half *>(d_features), ni, n, &map), "feature map");
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-        cuda_check(launch_mlp_tc(h->d_wpacked.ptr, ni, H, reinterpret_cast<const __half *>(d_features), n, d_outputs,
-                                 h->d_status.ptr, h->num_sms, s),
+        cuda_check(launch_mlp_tc(map, h->d_wpacked.ptr, ni, H, n, nullptr, d_outputs, h->d_status.ptr, h->num_sms, s),
                    "tensor-core MLP");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
         h->last_launches = 2;

@@ -127,20 +127,24 @@ struct DeviceBuffer {
 };
 
 // Buffers of one query context: the two wavefront state lists, the rotating list counters, the
-// fallback list and a pinned word for the host's end-of-loop check.
+// fallback list, the feature rows / outputs of a step, the packed weights, and pinned words for
+// the host's end-of-batch check.
 struct QueryContext {
     DeviceBuffer<float4> od0[2], od1[2], nv[2], ar[2];
     DeviceBuffer<uint4> meta[2];
     DeviceBuffer<uint32_t> stack[2];
     DeviceBuffer<uint32_t> wave_counts;
     DeviceBuffer<uint32_t> fallback_list;
+    DeviceBuffer<__half> features; // [capacity][n_inputs]
+    DeviceBuffer<float> outputs;   // [capacity][8]
+    DeviceBuffer<__half> wpacked;
     uint32_t capacity = 0;
-    uint32_t *h_count = nullptr;
+    uint32_t *h_words = nullptr; // 4 pinned words
     cudaEvent_t ev = nullptr;
     ~QueryContext()
     {
-        if (h_count)
-            cudaFreeHost(h_count);
+        if (h_words)
+            cudaFreeHost(h_words);
         if (ev)
             cudaEventDestroy(ev);
     }
@@ -232,11 +236,34 @@ cudaError_t launch_classic_fallback(const float4 *nodes, const float4 *tris, con
 cudaError_t launch_classic_as_neural(const float4 *nodes, const float4 *tris, const nbvh_ray *rays,
                                      uint32_t n, nbvh_neural_hit *hits, bool any_hit, bool fast_div, cudaStream_t s);
 
+// Opaque 128-byte CUDA tensor map (CUtensorMap) built on the host for TMA copies.
+struct alignas(64) TensorMapBytes {
+    unsigned char bytes[128];
+};
+
+// Per-query resources of the step loop besides the state lists: the FP16 feature rows and the
+// network outputs of the current step, the packed weights, the tensor map over the feature rows,
+// and the host words the end-of-batch check copies the 4 wave counters into (pinned, with ev
+// recorded after the copy; when ev is null, h_words may be pageable and the host waits on the
+// stream instead).
+struct StepResources {
+    __half *features;
+    float *outputs;
+    __half *wpacked;
+    TensorMapBytes feature_map;
+    uint32_t *h_words;
+    cudaEvent_t ev;
+};
+
 // Scratch of the allocation-free neural query: one static device buffer per device holding, for
-// NBVH_NOALLOC_MAX_RAYS rays, both wave lists, the fallback list, the counters and the wave
-// counters. Every region starts on a 256-byte boundary.
+// NBVH_NOALLOC_MAX_RAYS rays, both wave lists, the feature rows and outputs of a step, the packed
+// weights, the fallback list, the counters and the wave counters. Every region starts on a
+// 256-byte boundary.
 struct NoallocScratch {
     WaveList lists[2];
+    __half *features;
+    float *outputs;
+    __half *wpacked;
     uint32_t *fallback_list;
     QueryCounters *counters;
     uint32_t *wave_counts;
@@ -244,21 +271,26 @@ struct NoallocScratch {
 constexpr size_t kNoallocRays = NBVH_NOALLOC_MAX_RAYS;
 static_assert(kNoallocRays % 64u == 0u, "regions must stay 256-byte aligned");
 constexpr size_t kNoallocListBytes = kNoallocRays * (4u * sizeof(float4) + sizeof(uint4) + kNeuralStackSize * 4u);
-constexpr size_t kNoallocBytes = 2u * kNoallocListBytes + kNoallocRays * 4u + 256u + 256u;
+constexpr size_t kNoallocFeatureBytes = kNoallocRays * kMaxInputs * 2u;
+constexpr size_t kNoallocOutputBytes = kNoallocRays * kOutputs * 4u;
+constexpr size_t kNoallocWeightBytes = // W0 at most 64 x 128, at most 7 more 64 x 64, output 16 x 64
+    ((kNeurons * kMaxInputs + (kMaxHiddenLayers - 1u) * kNeurons * kNeurons + kOutputsPadded * kNeurons) * 2u + 255u) &
+    ~size_t(255);
+constexpr size_t kNoallocBytes = 2u * kNoallocListBytes + kNoallocFeatureBytes + kNoallocOutputBytes +
+                                 kNoallocWeightBytes + kNoallocRays * 4u + 256u + 256u;
 // The buffer's address on `device` (which must be current): looked up on the first call for that
 // device and cached. Fails with cudaErrorInvalidDevice for device ids beyond the cache.
 cudaError_t noalloc_scratch(int device, NoallocScratch *out);
 
-// Wavefront neural query (k_query.cu): first-leaf pass, then device steps checked by the host
-// every few launches through h_count (pinned, with ev recorded after the copy; when ev is null,
-// h_count may be pageable and the host waits on the stream instead). Returns when the loop has
-// finished.
+// Wavefront neural query (k_query.cu): first-leaf pass, then batches of K3 -> K4 -> K2 steps,
+// the list length checked by the host after each batch. Returns when the loop has finished;
+// cudaErrorTimeout if a bounded wait inside the tensor-core MLP gave up.
 cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds, uint32_t n_cut_nodes,
                               const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
                               const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
                               nbvh_neural_hit *hits, QueryCounters *counters, uint32_t *fallback_list,
-                              const WaveList lists[2], uint32_t *wave_counts, uint32_t *h_count, cudaEvent_t ev,
-                              int num_sms, cudaStream_t s, uint32_t *launches);
+                              const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, int num_sms,
+                              cudaStream_t s, uint32_t *launches);
 
 cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, const NeuralConsts &nc,
                             const nbvh_ray *rays, uint32_t n, uint32_t max_segments, nbvh_segment *segs,
@@ -269,13 +301,17 @@ cudaError_t launch_network_inference(const __half *params_h, const GridParams &g
                                      cudaStream_t s);
 
 // tcgen05 fully fused MLP (k_mlp_tc.cu): weights packed into the tensor-core operand layout, then
-// 128-row tiles of FP16 inputs (row-major [n][n_inputs], 16-byte aligned) fed by TMA. status
-// receives a nonzero word if a bounded wait inside the kernel gave up.
+// 128-row tiles of FP16 inputs (row-major [rows][n_inputs], 16-byte aligned) fed by TMA through
+// the tensor map of make_feature_map. The rows processed are min(*d_count, rows) when d_count is
+// given (a length produced on the device), else rows. status receives a nonzero word if a bounded
+// wait inside the kernel gave up.
 uint32_t packed_weight_bytes(uint32_t n_inputs, uint32_t n_hidden_layers);
 cudaError_t launch_pack_weights(const __half *params_h, uint32_t n_inputs, uint32_t n_hidden_layers, __half *packed,
                                 cudaStream_t s);
-cudaError_t launch_mlp_tc(const __half *wpacked, uint32_t n_inputs, uint32_t n_hidden_layers, const __half *features,
-                          uint32_t n, float *outputs, uint32_t *status, int num_sms, cudaStream_t s);
+cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t rows, TensorMapBytes *out);
+cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
+                          uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
+                          uint32_t *status, int num_sms, cudaStream_t s);
 
 cudaError_t launch_encode(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                           const float *positions, uint32_t n, float *features, cudaStream_t s);
