@@ -9,7 +9,13 @@ timing (weights of the reference are not available). A step is one neural closes
 the 2^22 resident rays; the classic BVH kernel answers the same rays for the "vs classic" figure and
 judges depth / visibility.
 
+The same comparison is repeated on the 4,194,304-triangle sphere (key "mesh_4m"), where the
+classic traversal is deeper while the neural query still works on a 1,024-leaf cut. The tcgen05
+MLP kernel is also timed alone on 2^22 rows ("roofline_kernels.mlp_tc"), and the CPU restatements
+of the neural and classic queries run on the host cores ("cpu_baseline").
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--train-steps T]
+                    [--mesh4m-train-steps T4 | -1] [--log2-rays R]
 """
 
 import argparse
@@ -43,6 +49,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--train-steps", type=int, default=20000)
     ap.add_argument("--cpu-sample", type=int, default=1 << 14)
+    ap.add_argument("--mesh4m-train-steps", type=int, default=10000,
+                    help="training steps for the 4M-triangle comparison; -1 skips it")
     ap.add_argument("--log2-rays", type=int, default=22,
                     help="rays per step; smaller values are for profiling captures, not bench lines")
     return ap.parse_args()
@@ -126,14 +134,107 @@ def profiled_traffic():
     return None
 
 
-def build_scene(nb, scenes, cfg):
-    v, f = scenes.fbm_sphere(SUBDIV, seed=1)
+def build_scene(nb, scenes, cfg, subdiv=SUBDIV):
+    v, f = scenes.fbm_sphere(subdiv, seed=1)
     alb = scenes.palette_albedo(len(f), 1)
     h = nb.NBVH(cfg)
     h.set_mesh(v, f, alb)
     h.build_classic()
     h.build_neural_cut(CUT_DEPTH)
     return h, v, f, alb
+
+
+def time_queries(h, rays, hits, chits, steps, warmup, nvtx_name):
+    """Device times (ms) of `steps` neural and classic queries over resident rays, L2 flushed
+    between steps, CUDA events on the launching stream."""
+    import torch
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for _ in range(warmup):
+        h.query_closest_neural(rays, 1, hits)
+        neural_launches = h.last_kernel_time()[1]
+        h.query_closest_classic(rays, chits)
+        classic_launches = h.last_kernel_time()[1]
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push(nvtx_name)  # ncu --nvtx --nvtx-include "timed/" selects these launches
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        h.query_closest_neural(rays, 1, hits)
+        ev[i][1].record(stream)
+    for i in range(steps):
+        flush.zero_()
+        cev[i][0].record(stream)
+        h.query_closest_classic(rays, chits)
+        cev[i][1].record(stream)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    times = np.array([a.elapsed_time(b) for a, b in ev])
+    ctimes = np.array([a.elapsed_time(b) for a, b in cev])
+    return times, ctimes, neural_launches, classic_launches
+
+
+def accuracy(hits, chits):
+    """Visibility agreement and depth error of the neural hits against the classic kernel."""
+    g = hits.cpu().numpy().view(np.uint32)
+    c = chits.cpu().numpy().view(np.uint32)
+    nvalid = (g[:, 8] & 1) != 0
+    cvalid = c[:, 3] != 0xFFFFFFFF
+    vis_agree = float(np.mean(nvalid == cvalid))
+    both = nvalid & cvalid
+    tn, tc = g[both, 0].view(np.float32), c[both, 0].view(np.float32)
+    err = np.abs(tn - tc).astype(np.float64)
+    rel = err / np.maximum(tc, 1e-6)
+    # relative error is ill-conditioned for rays starting on the surface (t -> 0): the headline
+    # mean floors the denominator at 1% of the unit scene; the raw mean is reported beside it
+    any_ = bool(both.any())
+    depth = {"mean_rel_floor1pct": float(np.mean(err / np.maximum(tc, 1e-2))) if any_ else None,
+             "mean_rel_raw": float(rel.mean()) if any_ else None,
+             "median_rel": float(np.median(rel)) if any_ else None,
+             "p90_rel": float(np.percentile(rel, 90)) if any_ else None,
+             "p99_rel": float(np.percentile(rel, 99)) if any_ else None,
+             "within_1pct": float(np.mean(rel <= 0.01)) if any_ else None}
+    return vis_agree, depth, float(g[:, 9].astype(np.float64).mean())
+
+
+def mlp_roofline(h, peak, rows=1 << 22, reps=10):
+    """The tcgen05 MLP kernel alone on `rows` FP16 input rows resident in HBM."""
+    import torch
+    feats = (torch.rand((rows, h.layout.n_inputs), device="cuda") * 0.2 - 0.1).half().contiguous()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        h.mlp_inference(feats)
+    ks = []
+    for _ in range(reps):
+        flush.zero_()
+        h.mlp_inference(feats)
+        ks.append(h.last_kernel_time()[0])
+    ms = float(np.median(ks))
+    achieved = FLOP_PER_SEGMENT * rows / (ms * 1e-3) / 1e12
+    return {"kernel": "k_mlp_tc", "bound": "tensor", "rows": rows, "ms": ms, "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak,
+            "input_read_gbs": rows * h.layout.n_inputs * 2 / (ms * 1e-3) / 1e9}
+
+
+def cpu_classic_baseline(h, v, f, rays, sample_all, sample_one):
+    """The CPU restatement of CudaBVH2::intersect (closest hit, include/cuda/accel/bvh2.cuh:12-88)
+    over the same BVH, at all host threads and at 1 thread, on the first rays of the batch."""
+    from oracle.bindings import Oracle
+    orc = Oracle()
+    nodes, prims = h.classic_bvh()
+    scene = orc.classic_scene(nodes, prims, v, f)
+    threads = os.cpu_count() or 1
+    out = {}
+    for n_thr, n in ((threads, sample_all), (1, sample_one)):
+        sub = rays[:n]
+        orc.classic_query(scene, sub[:256], threads=n_thr)
+        t0 = time.perf_counter()
+        orc.classic_query(scene, sub, threads=n_thr)
+        out[n_thr] = n / (time.perf_counter() - t0) / 1e6
+    return {"kind": "port", "unit": "Mrays/s", "cores": threads, "value": out[threads], "single_thread": out[1],
+            "sample": "%d rays (all threads) and %d rays (1 thread) of the batch" % (sample_all, sample_one)}
 
 
 def cpu_neural_baseline(nb, cfg, h_or_none, v, f, rays, params, threads, sample):
@@ -225,64 +326,20 @@ def run_ours(args):
     rays = torch.from_numpy(rays_np).cuda()
     hits = torch.empty((N_RAYS, 12), dtype=torch.int32, device="cuda")
     chits = torch.empty((N_RAYS, 4), dtype=torch.int32, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
-    stream = torch.cuda.current_stream()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
 
-    for _ in range(args.warmup):
-        h.query_closest_neural(rays, 1, hits)
-        neural_launches = h.last_kernel_time()[1]
-        h.query_closest_classic(rays, chits)
-        classic_launches = h.last_kernel_time()[1]
-    torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
     torch.cuda.synchronize()
     wall0 = time.perf_counter()
-    torch.cuda.nvtx.range_push("timed")  # ncu --nvtx --nvtx-include "timed/" selects these launches
-    for i in range(args.steps):
-        flush.zero_()
-        ev[i][0].record(stream)
-        h.query_closest_neural(rays, 1, hits)
-        ev[i][1].record(stream)
-    for i in range(args.steps):
-        flush.zero_()
-        cev[i][0].record(stream)
-        h.query_closest_classic(rays, chits)
-        cev[i][1].record(stream)
-    torch.cuda.synchronize()
-    torch.cuda.nvtx.range_pop()
+    times, ctimes, neural_launches, classic_launches = time_queries(h, rays, hits, chits, args.steps, args.warmup,
+                                                                     "timed")
     barrier()
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
-    times = np.array([a.elapsed_time(b) for a, b in ev])
-    ctimes = np.array([a.elapsed_time(b) for a, b in cev])
-    ms = float(times.mean())
-    cms = float(ctimes.mean())
-    ms, cms = max_over_ranks([ms, cms])
+    ms, cms = max_over_ranks([float(times.mean()), float(ctimes.mean())])
     stats = h.query_stats()
-
-    # accuracy against the classic judge
-    g = hits.cpu().numpy().view(np.uint32)
-    c = chits.cpu().numpy().view(np.uint32)
-    nvalid = (g[:, 8] & 1) != 0
-    cvalid = c[:, 3] != 0xFFFFFFFF
-    vis_agree = float(np.mean(nvalid == cvalid))
-    both = nvalid & cvalid
-    tn, tc = g[both, 0].view(np.float32), c[both, 0].view(np.float32)
-    err = np.abs(tn - tc).astype(np.float64)
-    rel = err / np.maximum(tc, 1e-6)
-    # relative error is ill-conditioned for rays starting on the surface (t -> 0): the headline
-    # mean floors the denominator at 1% of the unit scene; the raw mean is reported beside it
-    depth_err = float(np.mean(err / np.maximum(tc, 1e-2))) if both.any() else None
-    depth_stats = {"mean_rel_floor1pct": depth_err, "mean_rel_raw": float(rel.mean()) if both.any() else None,
-                   "median_rel": float(np.median(rel)) if both.any() else None,
-                   "p90_rel": float(np.percentile(rel, 90)) if both.any() else None,
-                   "p99_rel": float(np.percentile(rel, 99)) if both.any() else None,
-                   "within_1pct": float(np.mean(rel <= 0.01)) if both.any() else None}
-    segs_per_ray = float(g[:, 9].astype(np.float64).mean())
+    vis_agree, depth_stats, segs_per_ray = accuracy(hits, chits)
 
     # e2e through the host-buffer C-ABI call: pinned host rays in, hits out, copies timed
     pin_in = torch.from_numpy(rays_np).pin_memory()
@@ -300,47 +357,138 @@ def run_ours(args):
     e2e_ms = max_over_ranks([float(np.mean(e2e_times)) * 1e3])[0]
 
     peaks, peak_kind = measured_peaks()
+    peak = float(peaks.get("bf16_tflops", 1900.0))
     flops = FLOP_PER_SEGMENT * stats.segments
     achieved = flops / (ms * 1e-3) / 1e12
-    peak = float(peaks.get("bf16_tflops", 1900.0))
     value = world * N_RAYS / (ms * 1e-3) / 1e6
     line = {
         "metric": "neural vs classic Mrays/s at <=1% depth err on 1 GB300; p50/p99 batch latency",
         "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16",
         "data": "synthetic (seeded mesh and rays; weights trained on device by this library)",
-        "config": {"workload": WORKLOAD, "rays_per_step": N_RAYS, "triangles": int(len(f)), "neural_leaves": int((nn[:, 3] > 0).sum()),
-                   "points_per_segment": 4, "grid": "16 levels x 2 x 2^19 FP16, res 16-2048", "mlp": "64x4 ReLU FP16",
+        "config": {"workload": WORKLOAD, "rays_per_step": N_RAYS, "triangles": int(len(f)),
+                   "neural_leaves": int((nn[:, 3] > 0).sum()), "points_per_segment": 4,
+                   "grid": "16 levels x 2 x 2^19 FP16, res 16-2048", "mlp": "64x4 ReLU FP16",
                    "train_steps": args.train_steps, "train_batch": cfg.batch_size,
                    "l2": "flushed between timed steps (256 MB write); inputs 128 MB + outputs 192 MB",
                    "parallelism": "rays sharded per rank, no collective"},
         "classic_mrays": world * N_RAYS / (cms * 1e-3) / 1e6, "classic_ms_per_step": cms,
         "neural_over_classic": cms / ms,
         "p50_ms": float(np.percentile(times, 50)), "p99_ms": float(np.percentile(times, 99)),
-        "depth_rel_err_mean": depth_err, "depth_error": depth_stats, "visibility_agreement": vis_agree,
-        "segments_per_ray": segs_per_ray,
+        "depth_rel_err_mean": depth_stats["mean_rel_floor1pct"], "depth_error": depth_stats,
+        "visibility_agreement": vis_agree, "segments_per_ray": segs_per_ray,
         "train": {"steps": args.train_steps, "seconds": train_s,
                   "last_loss": (st.last_loss if st else None), "ms_per_step": (st.ms_per_step if st else None)},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_kind": peak_kind + " bf16 dense burst (FP16 MMA shares the rate)",
                      "traffic": profiled_traffic(),
-                     "algorithmic": "43,008 FLOP per inferred leaf segment x %d segments per launch" % stats.segments},
+                     "algorithmic": "43,008 FLOP per inferred leaf segment x %d segments per query" % stats.segments,
+                     "scope": "whole neural query (first pass + all steps); the per-kernel figures are in "
+                              "roofline_kernels"},
         "e2e": {"value": world * N_RAYS / (e2e_ms * 1e-3) / 1e6, "unit": "Mrays/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": N_RAYS * 32, "d2h_bytes_per_step": N_RAYS * 48},
         "gpu_launches": args.steps * (neural_launches + classic_launches),
         "clocks": clk,
         "wall_s_timed": wall,
     }
+    line["roofline_kernels"] = {
+        "mlp_tc": mlp_roofline(h, peak),
+        "encode_gather": {"kernel": "k_wave_encode", "bound": "L1->L2 miss requests (table L2-resident)",
+                          "algorithmic_bytes_per_segment": 2048,
+                          "note": "4 points x 16 levels x 8 corners x 4 B gathered per segment"},
+    }
     if rank == 0:
         params = h.params()
         threads = os.cpu_count() or 1
         mr, _ = cpu_neural_baseline(nb, cfg, h, v, f, rays_np, params, threads, args.cpu_sample)
         line["cpu_baseline"] = {"value": mr, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                                "sample": "%d of the 2^22 rays, trained weights, CPU restatement" % args.cpu_sample}
-        print(json.dumps(line))
+                                "sample": "%d of the 2^22 rays, trained weights, CPU restatement of the neural "
+                                          "query" % args.cpu_sample}
+        line["cpu_baseline"]["classic"] = cpu_classic_baseline(h, v, f, rays_np, 1 << 18, 1 << 16)
+        line["classic_config1"] = run_classic_config1(h, v, f, bbox, scenes, args.steps, args.warmup, 1 << 17)
     h.close()
+    del rays, hits, chits, pin_in, pin_out
+    torch.cuda.empty_cache()
+
+    if args.mesh4m_train_steps >= 0:
+        line["mesh_4m"] = run_mesh_4m(args, nb, scenes, cfg, max_over_ranks, rank)
+    if rank == 0:
+        print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_classic_config1(h, v, f, bbox, scenes, steps, warmup, cpu_sample):
+    """Classic closest hit on 512x512 pinhole rays from a seeded orbit camera plus one cosine bounce
+    per hit (the plain method's own workload): device time of the combined batch, bit-exact check
+    of a sample against the CPU restatement, and that restatement's throughput on the host cores."""
+    import torch
+    from oracle.bindings import Oracle
+    org, tgt, up = scenes.orbit_camera(bbox[:3], bbox[3:], seed=4)
+    prim = scenes.camera_rays(512, 512, org, tgt, up, seed=4)
+    prim_hits = h.query_closest_classic_host(prim)
+    bounce = scenes.bounce_rays(prim, prim_hits.view(np.uint32).reshape(-1, 4), v, f, seed=4)
+    rays_np = np.ascontiguousarray(np.concatenate([prim, bounce]), np.float32)
+    n = len(rays_np)
+    rays = torch.from_numpy(rays_np).cuda()
+    out = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        h.query_closest_classic(rays, out)
+    ts = []
+    for _ in range(steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        h.query_closest_classic(rays, out)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    ms = float(np.mean(ts))
+    orc = Oracle()
+    nodes, prims = h.classic_bvh()
+    scene = orc.classic_scene(nodes, prims, v, f)
+    idx = np.random.default_rng(5).choice(n, size=min(cpu_sample, n), replace=False)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref = orc.classic_query(scene, rays_np[idx], threads=threads)
+    cpu_s = time.perf_counter() - t0
+    got = out.cpu().numpy().view(np.uint32)[idx]
+    return {"rays": n, "primary": len(prim), "bounce": len(bounce), "ms_per_step": ms,
+            "mrays": n / (ms * 1e-3) / 1e6, "bit_exact_sample": bool(np.array_equal(got, ref)),
+            "sample": len(idx), "cpu_mrays": len(idx) / cpu_s / 1e6, "cpu_threads": threads}
+
+
+def run_mesh_4m(args, nb, scenes, cfg, max_over_ranks, rank):
+    """The same query on the 4,194,304-triangle fBm sphere: the neural cost depends on the cut
+    (1,024 leaves), not on the triangle count, while the classic traversal deepens."""
+    import torch
+    t0 = time.perf_counter()
+    h, v, f, _ = build_scene(nb, scenes, cfg, subdiv=10)
+    build_s = time.perf_counter() - t0
+    nn, bbox = h.neural_bvh()
+    t0 = time.perf_counter()
+    st = h.run_optimisation(args.mesh4m_train_steps) if args.mesh4m_train_steps > 0 else None
+    train_s = time.perf_counter() - t0
+    rays_np = scenes.uniform_rays(N_RAYS, bbox[:3], bbox[3:], seed=4048 + rank)
+    rays = torch.from_numpy(rays_np).cuda()
+    hits = torch.empty((N_RAYS, 12), dtype=torch.int32, device="cuda")
+    chits = torch.empty((N_RAYS, 4), dtype=torch.int32, device="cuda")
+    times, ctimes, _, _ = time_queries(h, rays, hits, chits, args.steps, args.warmup, "timed_4m")
+    ms, cms = max_over_ranks([float(times.mean()), float(ctimes.mean())])
+    vis_agree, depth_stats, segs_per_ray = accuracy(hits, chits)
+    out = {"triangles": int(len(f)), "classic_nodes": int(len(h.classic_bvh()[0])), "rays_per_step": N_RAYS,
+           "neural_mrays": N_RAYS / (ms * 1e-3) / 1e6, "neural_ms_per_step": ms,
+           "classic_mrays": N_RAYS / (cms * 1e-3) / 1e6, "classic_ms_per_step": cms,
+           "neural_over_classic": cms / ms, "p50_ms": float(np.percentile(times, 50)),
+           "p99_ms": float(np.percentile(times, 99)), "visibility_agreement": vis_agree,
+           "depth_error": depth_stats, "segments_per_ray": segs_per_ray,
+           "train": {"steps": args.mesh4m_train_steps, "seconds": train_s,
+                     "last_loss": (st.last_loss if st else None)},
+           "build_seconds": build_s}
+    h.close()
+    return out
 
 
 def main():
