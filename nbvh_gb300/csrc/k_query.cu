@@ -31,6 +31,9 @@ constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr uint32_t kEncodeThreads = 256;
 constexpr uint32_t kFirstThreads = 256;
+constexpr uint32_t kSortThreads = 1024;
+// Lists shorter than this are walked in list order: the sort would cost more than the locality it buys.
+constexpr uint32_t kSortMinRows = 1u << 16;
 constexpr int kVisitsPerRound = 8; // node visits of the next-leaf search between refills
 // decode: the shared-memory cut variant runs one 768-thread block per SM, the global-memory
 // variant two 384-thread blocks; both leave 85 registers per thread (the traversal stack stays in
@@ -52,6 +55,10 @@ struct WaveArgs {
     uint32_t *wave_counts; // 3 rotating list counters + the MLP's error word
     __half *features;      // [capacity][n_inputs] FP16 rows of the current step
     float *outputs;        // [capacity][8] network outputs of the current step
+    uint32_t *perm;        // list rows in leaf-node order (nullptr: rows in list order)
+    uint32_t *node_bins;   // [2][n_sort_nodes] rows per leaf node of the current / next list
+    uint32_t *node_cursor; // [2][n_sort_nodes] placement cursors of the sort
+    uint32_t n_sort_nodes;
     uint32_t n_hidden_layers;
     uint32_t n;
     uint32_t n_cut_nodes;
@@ -125,6 +132,18 @@ __device__ __forceinline__ uint32_t warp_append(bool want, uint32_t *counter)
         base = __shfl_sync(kFull, base, leader);
     }
     return base + __popc(m & ((1u << lane) - 1u));
+}
+
+// Counts the rows a warp appends per leaf node (one atomic per distinct node in the warp); all 32
+// lanes take part.
+__device__ __forceinline__ void count_nodes(uint32_t *bins, bool want, uint32_t node)
+{
+    const unsigned m = __ballot_sync(kFull, want);
+    if (!want)
+        return;
+    const unsigned same = __match_any_sync(m, node);
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(same) - 1))
+        atomicAdd(&bins[node], (uint32_t)__popc(same));
 }
 
 // K2 first pass: the first entered leaf of every ray (the first leaf is searched with an unbounded
@@ -205,6 +224,8 @@ __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_co
         const uint32_t pos = warp_append(listed, &a.wave_counts[0]);
         if (listed)
             store_state(a.lists[0], pos, s, stack);
+        if (a.perm)
+            count_nodes(a.node_bins, listed, s.seg_node);
     }
 }
 
@@ -236,9 +257,15 @@ __global__ void __launch_bounds__(kEncodeThreads) k_wave_encode(const __grid_con
     const V3 center = scale3(add3(smax, smin), 0.5f);
     const bool vec_store = (L & 3u) == 0u; // each point's block of L words starts 16-byte aligned
     uint32_t *feat = reinterpret_cast<uint32_t *>(a.features);
+    const bool sorted = a.perm != nullptr && count_in >= kSortMinRows;
     const uint32_t total = count_in * P; // at most 2^22 rays x 16 points
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
-        const uint32_t row = g / P, p = g - row * P;
+    // each block takes one contiguous range of the (node-sorted) rows, so an SM's L1 serves the
+    // grid cells of a few leaf regions at a time
+    const uint32_t per_block = (total + gridDim.x - 1u) / gridDim.x;
+    const uint32_t g_end = min(total, blockIdx.x * per_block + per_block);
+    for (uint32_t g = blockIdx.x * per_block + threadIdx.x; g < g_end; g += blockDim.x) {
+        const uint32_t i = g / P, p = g - i * P;
+        const uint32_t row = sorted ? a.perm[i] : i;
         const float4 od0 = in.od0[row], od1 = in.od1[row];
         const V3 o = mk3(od0.x, od0.y, od0.z), d = mk3(od1.x, od1.y, od1.z);
         float ta = od1.w, tb = __uint_as_float(in.meta[row].x);
@@ -279,6 +306,78 @@ __global__ void __launch_bounds__(kEncodeThreads) k_wave_encode(const __grid_con
                 dst[l] = pack_half2(f.x, f.y);
             }
         }
+    }
+}
+
+// Counting sort of the listed rays by their current leaf node (the per-node compaction of the
+// segments). The per-node counts were gathered when the list was written. Each block takes one
+// contiguous chunk of the list: it scans the counts in shared memory, counts its own rows per node
+// with shared-memory atomics, reserves one range per non-empty node with a global atomic, then
+// places its rows. The encoder, MLP and decoder then walk the list in node order, so rays of the
+// same leaf region are encoded together and the grid cells of the coarser levels are served from
+// L1. Also clears the next step's counts and cursors.
+__global__ void __launch_bounds__(kSortThreads) k_wave_sort(const __grid_constant__ WaveArgs a, uint32_t it)
+{
+    extern __shared__ uint32_t sort_smem[];
+    const uint32_t NB = a.n_sort_nodes;
+    uint32_t *scan = sort_smem, *cnt = sort_smem + NB, *base = sort_smem + 2u * NB;
+    const uint32_t *bins = a.node_bins + (it & 1u) * NB;
+    uint32_t *cursor = a.node_cursor + (it & 1u) * NB;
+    {
+        uint32_t *next_bins = a.node_bins + ((it + 1u) & 1u) * NB;
+        uint32_t *next_cursor = a.node_cursor + ((it + 1u) & 1u) * NB;
+        for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < NB; k += gridDim.x * blockDim.x) {
+            next_bins[k] = 0u;
+            next_cursor[k] = 0u;
+        }
+    }
+    const uint32_t count_in = *reinterpret_cast<volatile const uint32_t *>(&a.wave_counts[it % 3u]);
+    const uint32_t per_block = (count_in + gridDim.x - 1u) / gridDim.x;
+    const uint32_t r0 = blockIdx.x * per_block, r1 = min(count_in, r0 + per_block);
+    if (count_in < kSortMinRows || r0 >= r1)
+        return;
+    // exclusive scan of the node counts: contiguous runs per thread, then a scan of the run sums
+    const uint32_t per = (NB + blockDim.x - 1u) / blockDim.x;
+    const uint32_t k0 = min(NB, threadIdx.x * per), k1 = min(NB, k0 + per);
+    uint32_t run = 0;
+    for (uint32_t k = k0; k < k1; k++) {
+        run += bins[k];
+        cnt[k] = 0u;
+    }
+    __shared__ uint32_t warp_sums[kSortThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t v = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off)
+            incl += v;
+    }
+    if (lane == 31)
+        warp_sums[warp] = incl;
+    __syncthreads();
+    uint32_t acc = incl - run;
+    for (int w = 0; w < warp; w++)
+        acc += warp_sums[w];
+    for (uint32_t k = k0; k < k1; k++) {
+        scan[k] = acc;
+        acc += bins[k];
+    }
+    const WaveList &in = a.lists[it & 1u];
+    for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
+        atomicAdd(&cnt[in.meta[r].y], 1u);
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < NB; k += blockDim.x) {
+        const uint32_t c = cnt[k];
+        base[k] = c ? atomicAdd(&cursor[k], c) : 0u;
+        cnt[k] = 0u;
+    }
+    __syncthreads();
+    for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const uint32_t node = in.meta[r].y;
+        const uint32_t slot = scan[node] + base[node] + atomicAdd(&cnt[node], 1u);
+        if (slot < count_in) // the counts match the list; the check only keeps a stray row in bounds
+            a.perm[slot] = r;
     }
 }
 
@@ -338,6 +437,7 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
     // is done take a new row from the step's work counter. Lanes stay busy instead of waiting for
     // the longest traversal of their warp. All lanes run every round (warp_append needs all 32).
     uint32_t *head = &a.wave_counts[4u + it % 3u];
+    const bool sorted = a.perm != nullptr && count_in >= kSortMinRows;
     RayState s;
     uint32_t stack[kNeuralStackSize];
     RayDiv rdiv;
@@ -351,9 +451,9 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
                 base = atomicAdd(head, (uint32_t)__popc(idle));
             base = __shfl_sync(kFull, base, leader);
             exhausted = base + (uint32_t)__popc(idle) >= count_in;
-            const uint32_t row = base + __popc(idle & ((1u << lane) - 1u));
-            if (!active && row < count_in) {
-                load_state(in, row, s, stack);
+            const uint32_t i = base + __popc(idle & ((1u << lane) - 1u)); // position in node order
+            if (!active && i < count_in) {
+                load_state(in, sorted ? a.perm[i] : i, s, stack);
                 bool traverse = false;
                 if (s.segments > nc.max_traversal_steps) { // step cap (path_module.cu:68, last_inference)
                     s.flags |= NBVH_HIT_STEP_CAP;
@@ -365,7 +465,7 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
                     if (a.grid.segment_distribution == NBVH_SEGMENT_UNIFORM)
                         for (uint32_t k = 0; k < P; k++) // the draws the encoder made for this segment
                             (void)lcg_randomf(s.rng);
-                    const float4 *src = reinterpret_cast<const float4 *>(a.outputs + (size_t)row * 8u);
+                    const float4 *src = reinterpret_cast<const float4 *>(a.outputs + (size_t)i * 8u);
                     const float4 oa = src[0], ob = src[1];
                     const float o8[8] = {oa.x, oa.y, oa.z, oa.w, ob.x, ob.y, ob.z, ob.w};
                     s.segments++;
@@ -460,6 +560,8 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
         const uint32_t pos = warp_append(keep, count_out);
         if (keep)
             store_state(out, pos, s, stack);
+        if (a.perm)
+            count_nodes(a.node_bins + ((it + 1u) & 1u) * a.n_sort_nodes, keep, s.seg_node);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -490,6 +592,9 @@ cudaError_t run_steps(const WaveArgs &a, const StepResources &r, size_t dec_smem
 {
     cudaError_t e = cudaFuncSetAttribute(k_wave_decode<SMEM_CUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)dec_smem);
+    if (e == cudaSuccess && a.perm)
+        e = cudaFuncSetAttribute(k_wave_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(3u * a.n_sort_nodes * 4u));
     if (e != cudaSuccess)
         return e;
     const uint32_t enc_blocks = (uint32_t)num_sms * (2048u / kEncodeThreads);
@@ -500,6 +605,13 @@ cudaError_t run_steps(const WaveArgs &a, const StepResources &r, size_t dec_smem
     for (uint32_t it = 0; it < limit;) {
         const uint32_t batch = (limit - it) < kStepsPerCheck ? (limit - it) : kStepsPerCheck;
         for (uint32_t b = 0; b < batch; b++, it++) {
+            if (a.perm) {
+                k_wave_sort<<<(uint32_t)num_sms, kSortThreads, 3u * a.n_sort_nodes * 4u, s>>>(a, it);
+                e = cudaGetLastError();
+                if (e != cudaSuccess)
+                    return e;
+                launches++;
+            }
             k_wave_encode<<<enc_blocks, kEncodeThreads, 0, s>>>(a, it);
             e = cudaGetLastError();
             if (e != cudaSuccess)
@@ -565,6 +677,11 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     a.wave_counts = wave_counts;
     a.features = res.features;
     a.outputs = res.outputs;
+    a.n_sort_nodes = n_cut_nodes;
+    const bool sort = res.perm != nullptr && n_cut_nodes <= kMaxSortNodes;
+    a.perm = sort ? res.perm : nullptr;
+    a.node_bins = res.node_bins;
+    a.node_cursor = res.node_cursor;
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
     a.n_cut_nodes = n_cut_nodes;
@@ -573,6 +690,13 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     cudaError_t e = cudaMemsetAsync(wave_counts, 0, 8u * sizeof(uint32_t), s);
     if (e != cudaSuccess)
         return e;
+    if (sort) {
+        e = cudaMemsetAsync(res.node_bins, 0, 2u * n_cut_nodes * sizeof(uint32_t), s);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(res.node_cursor, 0, 2u * n_cut_nodes * sizeof(uint32_t), s);
+        if (e != cudaSuccess)
+            return e;
+    }
     e = launch_pack_weights(params_h, grid.n_inputs, n_hidden_layers, res.wpacked, s);
     if (e != cudaSuccess)
         return e;
@@ -637,6 +761,10 @@ cudaError_t noalloc_scratch(int device, NoallocScratch *out)
     p += kNoallocOutputBytes;
     out->wpacked = reinterpret_cast<__half *>(p);
     p += kNoallocWeightBytes;
+    out->perm = reinterpret_cast<uint32_t *>(p);
+    out->node_bins = out->perm + n;
+    out->node_cursor = out->node_bins + 2u * kMaxSortNodes;
+    p += kNoallocSortBytes;
     out->fallback_list = reinterpret_cast<uint32_t *>(p);
     p += n * 4u;
     out->counters = reinterpret_cast<QueryCounters *>(p);

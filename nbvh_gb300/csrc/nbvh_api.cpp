@@ -364,6 +364,11 @@ void ensure_query_workspace(nbvh_handle *h, uint32_t n, int ctx)
         for (int k = 0; k < 4; k++)
             q.h_words[k] = 0;
     }
+    const size_t cut = h->neural_nodes.size();
+    if (q.node_bins.count < 2u * cut) {
+        cuda_check(q.node_bins.resize(2u * cut), "alloc node counts");
+        cuda_check(q.node_cursor.resize(2u * cut), "alloc node cursors");
+    }
     const uint32_t wb = packed_weight_bytes(h->layout.n_inputs, (uint32_t)h->cfg.network.n_hidden_layers);
     if (q.wpacked.count < wb / 2u)
         cuda_check(q.wpacked.resize(wb / 2u), "alloc packed weights");
@@ -380,6 +385,7 @@ void ensure_query_workspace(nbvh_handle *h, uint32_t n, int ctx)
         }
         cuda_check(q.features.resize((size_t)n * h->layout.n_inputs), "alloc feature rows");
         cuda_check(q.outputs.resize((size_t)n * kOutputs), "alloc network outputs");
+        cuda_check(q.perm.resize(n), "alloc node order");
         q.capacity = n;
     }
 }
@@ -419,6 +425,9 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
     res.features = q.features.ptr;
     res.outputs = q.outputs.ptr;
     res.wpacked = q.wpacked.ptr;
+    res.perm = q.perm.ptr;
+    res.node_bins = q.node_bins.ptr;
+    res.node_cursor = q.node_cursor.ptr;
     res.h_words = q.h_words;
     res.ev = q.ev;
     cuda_check(make_feature_map(q.features.ptr, h->layout.n_inputs, q.capacity, &res.feature_map), "feature map");
@@ -467,6 +476,9 @@ void neural_query_noalloc(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, ui
         res.features = sc.features;
         res.outputs = sc.outputs;
         res.wpacked = sc.wpacked;
+        res.perm = sc.perm;
+        res.node_bins = sc.node_bins;
+        res.node_cursor = sc.node_cursor;
         res.h_words = host_words;
         res.ev = nullptr;
         cuda_check(make_feature_map(sc.features, h->layout.n_inputs, (uint32_t)kNoallocRays, &res.feature_map),

@@ -138,6 +138,8 @@ struct QueryContext {
     DeviceBuffer<__half> features; // [capacity][n_inputs]
     DeviceBuffer<float> outputs;   // [capacity][8]
     DeviceBuffer<__half> wpacked;
+    DeviceBuffer<uint32_t> perm;                   // [capacity]
+    DeviceBuffer<uint32_t> node_bins, node_cursor; // [2][cut nodes]
     uint32_t capacity = 0;
     uint32_t *h_words = nullptr; // 4 pinned words
     cudaEvent_t ev = nullptr;
@@ -236,6 +238,10 @@ cudaError_t launch_classic_fallback(const float4 *nodes, const float4 *tris, con
 cudaError_t launch_classic_as_neural(const float4 *nodes, const float4 *tris, const nbvh_ray *rays,
                                      uint32_t n, nbvh_neural_hit *hits, bool any_hit, bool fast_div, cudaStream_t s);
 
+// Cuts with more nodes than this are not sorted by node between steps (the sort scans the node
+// counts in shared memory).
+constexpr uint32_t kMaxSortNodes = 8192;
+
 // Opaque 128-byte CUDA tensor map (CUtensorMap) built on the host for TMA copies.
 struct alignas(64) TensorMapBytes {
     unsigned char bytes[128];
@@ -250,6 +256,9 @@ struct StepResources {
     __half *features;
     float *outputs;
     __half *wpacked;
+    uint32_t *perm;        // [capacity] rows in leaf-node order (nullptr: no sorting)
+    uint32_t *node_bins;   // [2][n_cut_nodes]
+    uint32_t *node_cursor; // [2][n_cut_nodes]
     TensorMapBytes feature_map;
     uint32_t *h_words;
     cudaEvent_t ev;
@@ -257,13 +266,16 @@ struct StepResources {
 
 // Scratch of the allocation-free neural query: one static device buffer per device holding, for
 // NBVH_NOALLOC_MAX_RAYS rays, both wave lists, the feature rows and outputs of a step, the packed
-// weights, the fallback list, the counters and the wave counters. Every region starts on a
+// weights, the node-sort buffers, the fallback list, the counters and the wave counters. Every region starts on a
 // 256-byte boundary.
 struct NoallocScratch {
     WaveList lists[2];
     __half *features;
     float *outputs;
     __half *wpacked;
+    uint32_t *perm;
+    uint32_t *node_bins;
+    uint32_t *node_cursor;
     uint32_t *fallback_list;
     QueryCounters *counters;
     uint32_t *wave_counts;
@@ -276,8 +288,9 @@ constexpr size_t kNoallocOutputBytes = kNoallocRays * kOutputs * 4u;
 constexpr size_t kNoallocWeightBytes = // W0 at most 64 x 128, at most 7 more 64 x 64, output 16 x 64
     ((kNeurons * kMaxInputs + (kMaxHiddenLayers - 1u) * kNeurons * kNeurons + kOutputsPadded * kNeurons) * 2u + 255u) &
     ~size_t(255);
+constexpr size_t kNoallocSortBytes = kNoallocRays * 4u + 4u * kMaxSortNodes * 4u; // perm, bins, cursors
 constexpr size_t kNoallocBytes = 2u * kNoallocListBytes + kNoallocFeatureBytes + kNoallocOutputBytes +
-                                 kNoallocWeightBytes + kNoallocRays * 4u + 256u + 256u;
+                                 kNoallocWeightBytes + kNoallocSortBytes + kNoallocRays * 4u + 256u + 256u;
 // The buffer's address on `device` (which must be current): looked up on the first call for that
 // device and cached. Fails with cudaErrorInvalidDevice for device ids beyond the cache.
 cudaError_t noalloc_scratch(int device, NoallocScratch *out);
