@@ -439,9 +439,10 @@ nbvh_status nbvh_last_kernel_time(nbvh_handle *h, float *ms, uint32_t *launches)
  * trace: a renderer whose GPU memory is reserved up front and must not grow mid-frame, or a host
  * thread that may not take the device-wide synchronisation an allocation can cause. The ordinary
  * query grows per-handle buffers to the largest batch seen; this one allocates nothing. Its
- * scratch (the per-ray traversal state, the fallback list and the counters, about 356 bytes per
- * ray) is one fixed buffer of NBVH_NOALLOC_MAX_RAYS rays compiled into the library, one copy per
- * device, created when the library's device code is loaded.
+ * scratch (the per-ray traversal state, the network inputs and outputs of a step, the node order,
+ * the fallback list and the counters: about 660 bytes per ray, 10.8 MB in all) is one fixed buffer
+ * of NBVH_NOALLOC_MAX_RAYS rays compiled into the library, one copy per device, created when the
+ * library's device code is loaded.
  *  - n must be at most NBVH_NOALLOC_MAX_RAYS; a larger n returns NBVH_EINVAL and launches nothing.
  *    Split larger batches into several calls.
  *  - The first call on each device looks up the buffer's address (setup). Make one call, n = 0 is
