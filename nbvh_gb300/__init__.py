@@ -343,9 +343,11 @@ class NBVH:
         return out
 
     def mlp_inference(self, features, stream=None):
-        """tcgen05 MLP on FP16 encoded inputs (torch.float16 [n, n_inputs], contiguous)."""
+        """tcgen05 MLP on 16-bit encoded inputs ([n, n_inputs], contiguous): torch.float16, or
+        torch.bfloat16 when the network precision is BF16."""
         import torch
-        assert features.dtype == torch.float16 and features.is_contiguous()
+        want = torch.bfloat16 if int(self.cfg.network.precision) == 1 else torch.float16
+        assert features.dtype == want and features.is_contiguous()
         n = features.shape[0]
         out = torch.empty((n, 8), dtype=torch.float32, device=features.device)
         self._check(self.lib.nbvh_mlp_inference(self.h, _ptr(features), n, _ptr(out), _stream(stream)))

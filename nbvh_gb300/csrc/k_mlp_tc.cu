@@ -83,10 +83,12 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, uint
     }
 }
 
-// Hidden-layer epilogue for this thread's row: 64 accumulator columns -> ReLU -> FP16 -> the next
-// layer's A operand (128 x 64) at act.
+// Hidden-layer epilogue for this thread's row: 64 accumulator columns -> ReLU -> 16-bit (FP16 or
+// BF16) -> the next layer's A operand (128 x 64) at act.
+template <bool BF16>
 __device__ __forceinline__ void epilogue_hidden(uint32_t tmem_row, unsigned char *act, uint32_t row)
 {
+    using Pr = MlpPrec<BF16>;
     uint32_t v[4][16];
 #pragma unroll
     for (int q = 0; q < 4; q++)
@@ -96,10 +98,10 @@ __device__ __forceinline__ void epilogue_hidden(uint32_t tmem_row, unsigned char
     for (int c = 0; c < 8; c++) {
         const uint32_t *s = &v[c >> 1][(c & 1) * 8];
         uint4 q;
-        q.x = pack_half2(fmaxf(__uint_as_float(s[0]), 0.f), fmaxf(__uint_as_float(s[1]), 0.f));
-        q.y = pack_half2(fmaxf(__uint_as_float(s[2]), 0.f), fmaxf(__uint_as_float(s[3]), 0.f));
-        q.z = pack_half2(fmaxf(__uint_as_float(s[4]), 0.f), fmaxf(__uint_as_float(s[5]), 0.f));
-        q.w = pack_half2(fmaxf(__uint_as_float(s[6]), 0.f), fmaxf(__uint_as_float(s[7]), 0.f));
+        q.x = Pr::pack(fmaxf(__uint_as_float(s[0]), 0.f), fmaxf(__uint_as_float(s[1]), 0.f));
+        q.y = Pr::pack(fmaxf(__uint_as_float(s[2]), 0.f), fmaxf(__uint_as_float(s[3]), 0.f));
+        q.z = Pr::pack(fmaxf(__uint_as_float(s[4]), 0.f), fmaxf(__uint_as_float(s[5]), 0.f));
+        q.w = Pr::pack(fmaxf(__uint_as_float(s[6]), 0.f), fmaxf(__uint_as_float(s[7]), 0.f));
         *reinterpret_cast<uint4 *>(act + tc::operand_offset(row, 8u * c, kTileRows)) = q;
     }
 }
@@ -115,6 +117,7 @@ __device__ __forceinline__ void epilogue_out(uint32_t tmem_row, float (&o)[8])
         o[i] = 1.0f / (1.0f + expf(-__uint_as_float(v[i])));
 }
 
+template <bool BF16>
 __global__ void __launch_bounds__(kMlpThreads, 3) k_mlp_tc(const __grid_constant__ CUtensorMap fmap, const MlpTcArgs a)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -170,8 +173,8 @@ __global__ void __launch_bounds__(kMlpThreads, 3) k_mlp_tc(const __grid_constant
     if (ok && t < n_tiles && tid == 0)
         load_tile(t);
     load_pending = ok && t < n_tiles;
-    const uint32_t id_hidden = tc::idesc_f16(kTileRows, kNeurons, false);
-    const uint32_t id_out = tc::idesc_f16(kTileRows, kOutputsPadded, false);
+    const uint32_t id_hidden = tc::idesc_f16(kTileRows, kNeurons, BF16);
+    const uint32_t id_out = tc::idesc_f16(kTileRows, kOutputsPadded, BF16);
     for (; ok && t < n_tiles; t += gridDim.x) {
         ok = tc::mbar_wait(bar_load, ph_load);
         ok = __syncthreads_and(ok);
@@ -201,7 +204,7 @@ __global__ void __launch_bounds__(kMlpThreads, 3) k_mlp_tc(const __grid_constant
             mma_pending = false;
             tc::fence_after_sync();
             if (layer < H) {
-                epilogue_hidden(tmem_row, tile, row);
+                epilogue_hidden<BF16>(tmem_row, tile, row);
                 tc::fence_async_shared();
             } else {
                 // the tile buffer is free: start the next tile's copy under this epilogue
@@ -281,6 +284,7 @@ cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t
     const cuuint64_t strides[1] = {(cuuint64_t)n_inputs * 2u};
     const cuuint32_t box[2] = {8u, kTileRows}; // 16 bytes x 128 rows: one K column of core matrices
     const cuuint32_t estr[2] = {1u, 1u};
+    // 16-bit rows; the element type of the map only sizes the copy (FP16 and BF16 move the same bits)
     if (encode(&fmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<__half *>(features), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
@@ -291,7 +295,7 @@ cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t
 
 cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
                           uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
-                          uint32_t *status, int num_sms, cudaStream_t s)
+                          uint32_t *status, bool bf16, int num_sms, cudaStream_t s)
 {
     if (rows == 0)
         return cudaSuccess;
@@ -307,14 +311,18 @@ cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpack
     a.outputs = outputs;
     a.status = status;
     const size_t smem = ((a.wbytes + 1023u) & ~1023u) + kTileRows * n_inputs * 2u + 32u;
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = bf16 ? cudaFuncSetAttribute(k_mlp_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                         : cudaFuncSetAttribute(k_mlp_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
     const uint32_t tiles = (rows + kTileRows - 1u) / kTileRows;
     uint32_t blocks = (uint32_t)num_sms * 3u;
     if (blocks > tiles)
         blocks = tiles;
-    k_mlp_tc<<<blocks, kMlpThreads, smem, s>>>(fmap, a);
+    if (bf16)
+        k_mlp_tc<true><<<blocks, kMlpThreads, smem, s>>>(fmap, a);
+    else
+        k_mlp_tc<false><<<blocks, kMlpThreads, smem, s>>>(fmap, a);
     return cudaGetLastError();
 }
 

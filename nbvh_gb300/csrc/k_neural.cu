@@ -71,7 +71,8 @@ struct InferArgs {
     uint32_t n;
 };
 
-// Network inference on explicit encoded positions: one warp per 32-row tile, grid-stride.
+// Network inference on explicit encoded positions: one warp per 16-row tile, grid-stride.
+template <bool BF16>
 __global__ void __launch_bounds__(kThreads, 2) k_network_inference(const __grid_constant__ InferArgs args)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -97,9 +98,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_network_inference(const __grid_
             const float *src = args.positions + ((size_t)(tile * 16u + r) * P + p) * 3u;
             return mk3(__ldg(src), __ldg(src + 1), __ldg(src + 2));
         };
-        encode_tile_to_smem(args.table, gp, pos, mask, feat, fld);
+        encode_tile_to_smem<BF16>(args.table, gp, pos, mask, feat, fld);
         float o4[4];
-        mlp_tile_from_smem(sw, feat, fld, n_inputs, args.n_hidden_layers, o4);
+        mlp_tile_from_smem<BF16>(sw, feat, fld, n_inputs, args.n_hidden_layers, o4);
         __syncwarp();
         if (act0) {
             args.outputs[(size_t)r0 * 8u + tig * 2] = o4[0];
@@ -148,7 +149,8 @@ cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, c
 }
 
 cudaError_t launch_network_inference(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
-                                     const float *positions, uint32_t n, float *outputs, int num_sms, cudaStream_t s)
+                                     const float *positions, uint32_t n, float *outputs, bool bf16, int num_sms,
+                                     cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
@@ -164,7 +166,7 @@ cudaError_t launch_network_inference(const __half *params_h, const GridParams &g
     a.n = n;
     size_t smem = sizeof(GridParams) + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half) +
                   (size_t)kWarps * 16u * (grid.n_inputs + 8u) * sizeof(__half);
-    cudaError_t e = prepare_smem(k_network_inference, smem);
+    cudaError_t e = bf16 ? prepare_smem(k_network_inference<true>, smem) : prepare_smem(k_network_inference<false>, smem);
     if (e != cudaSuccess)
         return e;
     uint32_t tiles = (n + 15u) / 16u;
@@ -172,7 +174,10 @@ cudaError_t launch_network_inference(const __half *params_h, const GridParams &g
     uint32_t cap = (uint32_t)num_sms * 2u;
     if (blocks > cap)
         blocks = cap;
-    k_network_inference<<<blocks, kThreads, smem, s>>>(a);
+    if (bf16)
+        k_network_inference<true><<<blocks, kThreads, smem, s>>>(a);
+    else
+        k_network_inference<false><<<blocks, kThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -62,6 +62,7 @@ struct WaveArgs {
     uint32_t n_hidden_layers;
     uint32_t n;
     uint32_t n_cut_nodes;
+    uint32_t bf16; // MLP inputs in BF16 (else FP16)
 };
 
 __device__ __forceinline__ void write_hit(nbvh_neural_hit *hits, uint32_t id, float t, V3 nrm, V3 alb, float vis,
@@ -256,6 +257,8 @@ __global__ void __launch_bounds__(kEncodeThreads) k_wave_encode(const __grid_con
     const V3 ext = scale3(sub3(smax, smin), dilation);
     const V3 center = scale3(add3(smax, smin), 0.5f);
     const bool vec_store = (L & 3u) == 0u; // each point's block of L words starts 16-byte aligned
+    const bool bf16 = a.bf16 != 0u;
+    auto pack16 = [bf16](float lo, float hi) { return bf16 ? pack_bf162(lo, hi) : pack_half2(lo, hi); };
     uint32_t *feat = reinterpret_cast<uint32_t *>(a.features);
     const bool sorted = a.perm != nullptr && count_in >= kSortMinRows;
     const uint32_t total = count_in * P; // at most 2^22 rays x 16 points
@@ -291,19 +294,19 @@ __global__ void __launch_bounds__(kEncodeThreads) k_wave_encode(const __grid_con
             for (uint32_t l = 0; l < L; l += 4u) {
                 uint4 q;
                 float2 f = encode_level(a.table, gp, l, pos);
-                q.x = pack_half2(f.x, f.y);
+                q.x = pack16(f.x, f.y);
                 f = encode_level(a.table, gp, l + 1u, pos);
-                q.y = pack_half2(f.x, f.y);
+                q.y = pack16(f.x, f.y);
                 f = encode_level(a.table, gp, l + 2u, pos);
-                q.z = pack_half2(f.x, f.y);
+                q.z = pack16(f.x, f.y);
                 f = encode_level(a.table, gp, l + 3u, pos);
-                q.w = pack_half2(f.x, f.y);
+                q.w = pack16(f.x, f.y);
                 *reinterpret_cast<uint4 *>(dst + l) = q;
             }
         } else {
             for (uint32_t l = 0; l < L; l++) {
                 const float2 f = encode_level(a.table, gp, l, pos);
-                dst[l] = pack_half2(f.x, f.y);
+                dst[l] = pack16(f.x, f.y);
             }
         }
     }
@@ -617,7 +620,7 @@ cudaError_t run_steps(const WaveArgs &a, const StepResources &r, size_t dec_smem
             if (e != cudaSuccess)
                 return e;
             e = launch_mlp_tc(r.feature_map, r.wpacked, a.grid.n_inputs, a.n_hidden_layers, a.lists[0].capacity,
-                              &a.wave_counts[it % 3u], a.outputs, &a.wave_counts[3], num_sms, s);
+                              &a.wave_counts[it % 3u], a.outputs, &a.wave_counts[3], a.bf16 != 0u, num_sms, s);
             if (e != cudaSuccess)
                 return e;
             k_wave_decode<SMEM_CUT><<<dec_blocks, decode_threads(SMEM_CUT), dec_smem, s>>>(a, it);
@@ -653,8 +656,8 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
                               const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
                               const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
                               nbvh_neural_hit *hits, QueryCounters *counters, uint32_t *fallback_list,
-                              const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, int num_sms,
-                              cudaStream_t s, uint32_t *launches)
+                              const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, bool bf16,
+                              int num_sms, cudaStream_t s, uint32_t *launches)
 {
     *launches = 0;
     if (n == 0)
@@ -678,6 +681,7 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     a.features = res.features;
     a.outputs = res.outputs;
     a.n_sort_nodes = n_cut_nodes;
+    a.bf16 = bf16 ? 1u : 0u;
     const bool sort = res.perm != nullptr && n_cut_nodes <= kMaxSortNodes;
     a.perm = sort ? res.perm : nullptr;
     a.node_bins = res.node_bins;

@@ -289,8 +289,10 @@ struct TrainArgs {
 constexpr int kTrainWarps = 8;
 constexpr int kTrainThreads = kTrainWarps * 32;
 
+template <bool BF16>
 __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid_constant__ TrainArgs a)
 {
+    using Pr = MlpPrec<BF16>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     GridParams &gp = *reinterpret_cast<GridParams *>(smem_raw);
     const uint32_t n_in = a.grid.n_inputs, P = a.grid.n_points, L = a.grid.n_levels, H = a.n_hidden_layers;
@@ -331,7 +333,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
                     return 0u;
                 uint32_t p = j / L, l = j - p * L;
                 float2 f = encode_level(a.table, gp, l, pos_of(row, p));
-                return pack_half2(f.x, f.y);
+                return Pr::pack(f.x, f.y);
             };
             af[0] = feat(act0, r0, j0);
             af[1] = feat(act1, r1, j0);
@@ -350,12 +352,12 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
             for (int nt = 0; nt < 8; nt++) {
                 uint32_t b0 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * SL.ld0);
                 uint32_t b1 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * SL.ld0 + 8);
-                mma16816(acc[nt], af, b0, b1);
+                Pr::mma(acc[nt], af, b0, b1);
             }
         }
         uint32_t ah[4][4];
         for (uint32_t layer = 1; layer <= H; layer++) {
-            relu_pack(acc, ah);
+            relu_pack<BF16>(acc, ah);
             // store x_layer (input of matrix `layer`)
             __half *dst0 = a.acts + (size_t)r0 * acts_stride + n_in + (layer - 1u) * kNeurons;
             __half *dst1 = a.acts + (size_t)r1 * acts_stride + n_in + (layer - 1u) * kNeurons;
@@ -383,7 +385,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
                 for (int nt = 0; nt < 8; nt++) {
                     uint32_t b0 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * kHiddenLd);
                     uint32_t b1 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * kHiddenLd + 8);
-                    mma16816(acc[nt], ah[kb], b0, b1);
+                    Pr::mma(acc[nt], ah[kb], b0, b1);
                 }
             }
         }
@@ -395,7 +397,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
             for (int kb = 0; kb < 4; kb++) {
                 uint32_t b0 = *reinterpret_cast<const uint32_t *>(wo + kb * 16);
                 uint32_t b1 = *reinterpret_cast<const uint32_t *>(wo + kb * 16 + 8);
-                mma16816(oc, ah[kb], b0, b1);
+                Pr::mma(oc, ah[kb], b0, b1);
             }
         }
         // ---------------- loss ----------------
@@ -411,14 +413,14 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
                 const float tgt = __ldg(a.targets + (size_t)row * 8u + ch);
                 const float tvis = __ldg(a.targets + (size_t)row * 8u);
                 composite_loss(a.lc, ch, y, tgt, tvis, value, gr);
-                gr = __half2float(__float2half_rn(gr)); // FP16 output gradient
+                gr = Pr::round(gr); // 16-bit output gradient
             }
             loss_acc += value;
             dzo[e] = gr * y * (1.0f - y); // sigmoid backward
         }
         // dz_out (cols 0..7; 8..15 stay zero)
         {
-            uint32_t lo = pack_half2(dzo[0], dzo[1]), hi = pack_half2(dzo[2], dzo[3]);
+            uint32_t lo = Pr::pack(dzo[0], dzo[1]), hi = Pr::pack(dzo[2], dzo[3]);
             if (act0) {
                 __half *dst = a.dz + (size_t)r0 * dz_stride + H * kNeurons;
                 *reinterpret_cast<uint32_t *>(dst + tig * 2) = lo;
@@ -433,8 +435,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
         // ---------------- backward ----------------
         // dx_H = dz_out . W_out (K = 16 outputs, only 0..7 non-zero)
         uint32_t adz[4][4]; // A fragments of the current dz (k = out channel)
-        adz[0][0] = pack_half2(dzo[0], dzo[1]);
-        adz[0][1] = pack_half2(dzo[2], dzo[3]);
+        adz[0][0] = Pr::pack(dzo[0], dzo[1]);
+        adz[0][1] = Pr::pack(dzo[2], dzo[3]);
         adz[0][2] = 0u;
         adz[0][3] = 0u;
         uint32_t n_kb = 1;
@@ -451,8 +453,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
                     uint32_t b[4];
                     const __half *addr = wmat + (kb * 16u + (lane & 15)) * wld + np * 16 + (lane >> 4) * 8;
                     ldsm_x4_trans(b, addr);
-                    mma16816(acc[2 * np], adz[kb], b[0], b[1]);
-                    mma16816(acc[2 * np + 1], adz[kb], b[2], b[3]);
+                    Pr::mma(acc[2 * np], adz[kb], b[0], b[1]);
+                    Pr::mma(acc[2 * np + 1], adz[kb], b[2], b[3]);
                 }
             }
             // dz_layer = dx_layer * (x_layer > 0), x_layer = input activation of matrix `layer`
@@ -462,9 +464,9 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
             __half *dzw1 = a.dz + (size_t)r1 * dz_stride + (uint32_t)(layer - 1) * kNeurons;
 #pragma unroll
             for (int nt = 0; nt < 8; nt++) {
-                float2 m0 = act0 ? unpack_half2(*reinterpret_cast<const uint32_t *>(x0 + nt * 8 + tig * 2))
+                float2 m0 = act0 ? Pr::unpack(*reinterpret_cast<const uint32_t *>(x0 + nt * 8 + tig * 2))
                                  : make_float2(0.f, 0.f);
-                float2 m1 = act1 ? unpack_half2(*reinterpret_cast<const uint32_t *>(x1 + nt * 8 + tig * 2))
+                float2 m1 = act1 ? Pr::unpack(*reinterpret_cast<const uint32_t *>(x1 + nt * 8 + tig * 2))
                                  : make_float2(0.f, 0.f);
                 acc[nt][0] = m0.x > 0.f ? acc[nt][0] : 0.f;
                 acc[nt][1] = m0.y > 0.f ? acc[nt][1] : 0.f;
@@ -473,10 +475,10 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
             }
 #pragma unroll
             for (int kb = 0; kb < 4; kb++) {
-                adz[kb][0] = pack_half2(acc[2 * kb][0], acc[2 * kb][1]);
-                adz[kb][1] = pack_half2(acc[2 * kb][2], acc[2 * kb][3]);
-                adz[kb][2] = pack_half2(acc[2 * kb + 1][0], acc[2 * kb + 1][1]);
-                adz[kb][3] = pack_half2(acc[2 * kb + 1][2], acc[2 * kb + 1][3]);
+                adz[kb][0] = Pr::pack(acc[2 * kb][0], acc[2 * kb][1]);
+                adz[kb][1] = Pr::pack(acc[2 * kb][2], acc[2 * kb][3]);
+                adz[kb][2] = Pr::pack(acc[2 * kb + 1][0], acc[2 * kb + 1][1]);
+                adz[kb][3] = Pr::pack(acc[2 * kb + 1][2], acc[2 * kb + 1][3]);
                 if (act0) {
                     *reinterpret_cast<uint32_t *>(dzw0 + kb * 16 + tig * 2) = adz[kb][0];
                     *reinterpret_cast<uint32_t *>(dzw0 + kb * 16 + tig * 2 + 8) = adz[kb][2];
@@ -499,7 +501,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
                 // x2 is enough here; reuse the x4 form with the upper half pointing at the same tile
                 const __half *addr = sw + (kb * 16u + (lane & 15)) * SL.ld0 + nt * 8u;
                 ldsm_x4_trans(b, addr);
-                mma16816(dx, adz[kb], b[0], b[1]);
+                Pr::mma(dx, adz[kb], b[0], b[1]);
             }
             // feature pair j = nt * 4 + tig (both features) for rows r0, r1
             const uint32_t j = nt * 4u + (uint32_t)tig;
@@ -510,8 +512,8 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
                 if (!act)
                     continue;
                 const uint32_t row = rr ? r1 : r0;
-                const float g0 = __half2float(__float2half_rn(dx[2 * rr]));
-                const float g1 = __half2float(__float2half_rn(dx[2 * rr + 1]));
+                const float g0 = Pr::round(dx[2 * rr]);
+                const float g1 = Pr::round(dx[2 * rr + 1]);
                 if (g0 == 0.f && g1 == 0.f)
                     continue;
                 // corner indices / weights of this (row, point, level), as encode_level
@@ -594,7 +596,7 @@ __device__ __forceinline__ void tile_info(uint32_t t, uint32_t n_in, uint32_t H,
     nt = t;
 }
 
-template <int TPW>
+template <int TPW, bool BF16>
 __global__ void __launch_bounds__(kWgThreads, 1) k_weight_grads(const __grid_constant__ WgArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -648,7 +650,7 @@ __global__ void __launch_bounds__(kWgThreads, 1) k_weight_grads(const __grid_con
                 // B = x (k = row, n = in channel): ldmatrix.trans of the [row][in] tile
                 const __half *pb = sa + (kb * 16u + (lane & 15)) * sa_ld + xoff;
                 ldsm_x4_trans(bf, pb);
-                mma16816(acc[i], af, bf[0], bf[1]);
+                MlpPrec<BF16>::mma(acc[i], af, bf[0], bf[1]);
             }
         }
     }
@@ -681,10 +683,21 @@ __global__ void __launch_bounds__(kWgThreads, 1) k_weight_grads(const __grid_con
 // FP32 master weights, m and v; writes the FP16 copy the kernels read.
 // ---------------------------------------------------------------------------------------------
 
+// 16-bit copy of parameter i: the first n_bf16 parameters (the network matrices in BF16 mode) as
+// BF16, the rest (or all, in FP16 mode) as FP16.
+__device__ __forceinline__ __half to_param16(float x, uint32_t i, uint32_t n_bf16)
+{
+    if (i < n_bf16) {
+        const __nv_bfloat16 b = __float2bfloat16_rn(x);
+        return *reinterpret_cast<const __half *>(&b);
+    }
+    return __float2half_rn(x);
+}
+
 __global__ void __launch_bounds__(256) k_adam(float *__restrict__ params, __half *__restrict__ params_h,
                                               float *__restrict__ m, float *__restrict__ v,
                                               const float *__restrict__ grad, uint32_t n, float lr_t, float beta1,
-                                              float beta2, float eps, float l2_reg, float grad_scale)
+                                              float beta2, float eps, float l2_reg, float grad_scale, uint32_t n_bf16)
 {
     const float omb1 = __fsub_rn(1.0f, beta1), omb2 = __fsub_rn(1.0f, beta2);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -696,14 +709,14 @@ __global__ void __launch_bounds__(256) k_adam(float *__restrict__ params, __half
         v[i] = vi;
         const float nw = __fsub_rn(w, __fmul_rn(lr_t, __fdiv_rn(mi, __fadd_rn(__fsqrt_rn(vi), eps))));
         params[i] = nw;
-        params_h[i] = __float2half_rn(nw);
+        params_h[i] = to_param16(nw, i, n_bf16);
     }
 }
 
-__global__ void k_to_half(const float *__restrict__ p, __half *__restrict__ h, uint32_t n)
+__global__ void k_to_half(const float *__restrict__ p, __half *__restrict__ h, uint32_t n, uint32_t n_bf16)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        h[i] = __float2half_rn(p[i]);
+        h[i] = to_param16(p[i], i, n_bf16);
 }
 
 __global__ void k_scale(float *__restrict__ p, size_t n, float s)
@@ -741,7 +754,7 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
 cudaError_t launch_train_forward_backward(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                                           const LossConsts &lc, const float *positions, const float *targets,
                                           uint32_t n, __half *acts, __half *dz, float *grad, float *loss_sum,
-                                          int num_sms, cudaStream_t s)
+                                          bool bf16, int num_sms, cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
@@ -761,7 +774,8 @@ cudaError_t launch_train_forward_backward(const __half *params_h, const GridPara
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
     const size_t smem = sizeof(GridParams) + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half);
-    cudaError_t e = cudaFuncSetAttribute(k_train_fwd_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = bf16 ? cudaFuncSetAttribute(k_train_fwd_bwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                         : cudaFuncSetAttribute(k_train_fwd_bwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
     const uint32_t tiles = (n + 15u) / 16u;
@@ -769,12 +783,26 @@ cudaError_t launch_train_forward_backward(const __half *params_h, const GridPara
     const uint32_t cap = (uint32_t)num_sms * 2u;
     if (blocks > cap)
         blocks = cap;
-    k_train_fwd_bwd<<<blocks, kTrainThreads, smem, s>>>(a);
+    if (bf16)
+        k_train_fwd_bwd<true><<<blocks, kTrainThreads, smem, s>>>(a);
+    else
+        k_train_fwd_bwd<false><<<blocks, kTrainThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int TPW, bool BF16>
+cudaError_t run_weight_grads(const WgArgs &a, uint32_t blocks, size_t smem, cudaStream_t s)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_weight_grads<TPW, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    k_weight_grads<TPW, BF16><<<blocks, kWgThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_weight_gradients(const GridParams &grid, uint32_t n_hidden_layers, const __half *acts,
-                                    const __half *dz, uint32_t n, float *grad, int num_sms, cudaStream_t s)
+                                    const __half *dz, uint32_t n, float *grad, bool bf16, int num_sms, cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
@@ -795,27 +823,14 @@ cudaError_t launch_weight_gradients(const GridParams &grid, uint32_t n_hidden_la
     const size_t smem = (size_t)kWgRows * ((acts_stride + 8u) + (dz_stride + 8u)) * sizeof(__half);
     const uint32_t n_tiles = 4u * (grid.n_inputs / 8u) + 32u * (n_hidden_layers - 1u) + 8u;
     const uint32_t tpw = (n_tiles + kWgWarps - 1u) / kWgWarps;
-    cudaError_t e;
-    if (tpw <= 16) {
-        e = cudaFuncSetAttribute(k_weight_grads<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess)
-            return e;
-        k_weight_grads<16><<<blocks, kWgThreads, smem, s>>>(a);
-    } else if (tpw <= 24) {
-        e = cudaFuncSetAttribute(k_weight_grads<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess)
-            return e;
-        k_weight_grads<24><<<blocks, kWgThreads, smem, s>>>(a);
-    } else if (tpw <= kMaxTilesPerWarp) {
-        e = cudaFuncSetAttribute(k_weight_grads<kMaxTilesPerWarp>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-        if (e != cudaSuccess)
-            return e;
-        k_weight_grads<kMaxTilesPerWarp><<<blocks, kWgThreads, smem, s>>>(a);
-    } else {
-        return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
+    if (tpw <= 16)
+        return bf16 ? run_weight_grads<16, true>(a, blocks, smem, s) : run_weight_grads<16, false>(a, blocks, smem, s);
+    if (tpw <= 24)
+        return bf16 ? run_weight_grads<24, true>(a, blocks, smem, s) : run_weight_grads<24, false>(a, blocks, smem, s);
+    if (tpw <= kMaxTilesPerWarp)
+        return bf16 ? run_weight_grads<kMaxTilesPerWarp, true>(a, blocks, smem, s)
+                    : run_weight_grads<kMaxTilesPerWarp, false>(a, blocks, smem, s);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_scale(float *data, size_t n, float scale, cudaStream_t s)
@@ -827,25 +842,26 @@ cudaError_t launch_scale(float *data, size_t n, float scale, cudaStream_t s)
 }
 
 cudaError_t launch_adam(float *params, __half *params_h, float *m, float *v, const float *grad, uint32_t n, float lr_t,
-                        float beta1, float beta2, float eps, float l2_reg, float grad_scale, cudaStream_t s)
+                        float beta1, float beta2, float eps, float l2_reg, float grad_scale, uint32_t n_bf16,
+                        cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
     uint32_t blocks = (n + 255u) / 256u;
     if (blocks > 8192u)
         blocks = 8192u;
-    k_adam<<<blocks, 256, 0, s>>>(params, params_h, m, v, grad, n, lr_t, beta1, beta2, eps, l2_reg, grad_scale);
+    k_adam<<<blocks, 256, 0, s>>>(params, params_h, m, v, grad, n, lr_t, beta1, beta2, eps, l2_reg, grad_scale, n_bf16);
     return cudaGetLastError();
 }
 
-cudaError_t launch_params_to_half(const float *params, __half *params_h, uint32_t n, cudaStream_t s)
+cudaError_t launch_params_to_half(const float *params, __half *params_h, uint32_t n, uint32_t n_bf16, cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
     uint32_t blocks = (n + 255u) / 256u;
     if (blocks > 8192u)
         blocks = 8192u;
-    k_to_half<<<blocks, 256, 0, s>>>(params, params_h, n);
+    k_to_half<<<blocks, 256, 0, s>>>(params, params_h, n, n_bf16);
     return cudaGetLastError();
 }
 

@@ -104,8 +104,8 @@ void validate_config(const nbvh_config &c)
         fail(NBVH_EINVAL, "n_neurons must be 64");
     if (c.network.n_hidden_layers < 1 || c.network.n_hidden_layers > (int)kMaxHiddenLayers)
         fail(NBVH_EINVAL, "n_hidden_layers must be in [1, 8]");
-    if (c.network.precision != NBVH_PRECISION_FP16)
-        fail(NBVH_EINVAL, "only the FP16 network precision is implemented");
+    if (c.network.precision != NBVH_PRECISION_FP16 && c.network.precision != NBVH_PRECISION_BF16)
+        fail(NBVH_EINVAL, "network precision must be NBVH_PRECISION_FP16 or NBVH_PRECISION_BF16");
     if (c.batch_size == 0 || (c.batch_size & (c.batch_size - 1u)) != 0)
         fail(NBVH_EINVAL, "batch_size must be a power of two");
     if (c.bvh.log2_bvh_max_traversals != 0)
@@ -315,13 +315,17 @@ void upload_neural(nbvh_handle *h)
     h->d_non_neural.release();
 }
 
+// The MLP runs in BF16 (else FP16); its matrices are the first n_network_params parameters.
+bool mlp_bf16(const nbvh_handle *h) { return h->cfg.network.precision == NBVH_PRECISION_BF16; }
+uint32_t n_bf16_params(const nbvh_handle *h) { return mlp_bf16(h) ? h->layout.n_network_params : 0u; }
+
 void upload_params(nbvh_handle *h, const float *params, bool reset_adam)
 {
     const uint32_t n = h->layout.n_params;
     cuda_check(h->d_params.resize(n), "alloc params");
     cuda_check(h->d_params_h.resize(n), "alloc fp16 params");
     cuda_check(cudaMemcpy(h->d_params.ptr, params, (size_t)n * sizeof(float), cudaMemcpyHostToDevice), "upload params");
-    cuda_check(launch_params_to_half(h->d_params.ptr, h->d_params_h.ptr, n, nullptr), "to half");
+    cuda_check(launch_params_to_half(h->d_params.ptr, h->d_params_h.ptr, n, n_bf16_params(h), nullptr), "to half");
     if (reset_adam) {
         cuda_check(h->d_adam_m.resize(n), "alloc adam m");
         cuda_check(h->d_adam_v.resize(n), "alloc adam v");
@@ -434,7 +438,7 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
     cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),
                                  h->any_non_neural ? h->d_non_neural.ptr : nullptr, h->d_params_h.ptr, h->grid, nc,
                                  (uint32_t)h->cfg.network.n_hidden_layers, d_rays, n, d_hits, counters, list, lists,
-                                 q.wave_counts.ptr, res, h->num_sms, s, &launches),
+                                 q.wave_counts.ptr, res, mlp_bf16(h), h->num_sms, s, &launches),
                "neural query");
     if (timed)
         cuda_check(cudaEventRecord(h->ev1, s), "event");
@@ -487,7 +491,7 @@ void neural_query_noalloc(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, ui
                                      (uint32_t)h->neural_nodes.size(), h->any_non_neural ? h->d_non_neural.ptr : nullptr,
                                      h->d_params_h.ptr, h->grid, nc, (uint32_t)h->cfg.network.n_hidden_layers, d_rays,
                                      n, d_hits, sc.counters, sc.fallback_list, sc.lists, sc.wave_counts, res,
-                                     h->num_sms, s, &launches),
+                                     mlp_bf16(h), h->num_sms, s, &launches),
                    "neural query");
         if (h->any_non_neural || h->cfg.fallback_margin > 0.f)
             cuda_check(launch_classic_fallback(h->d_nodes.ptr, h->d_tris.ptr, d_rays, sc.fallback_list, sc.counters,
@@ -926,7 +930,7 @@ nbvh_status nbvh_network_inference(nbvh_handle *h, const float *d_positions, uin
         cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
         cuda_check(cudaEventRecord(h->ev0, s), "event");
         cuda_check(launch_network_inference(h->d_params_h.ptr, h->grid, (uint32_t)h->cfg.network.n_hidden_layers,
-                                            d_positions, n, d_outputs, h->num_sms, s),
+                                            d_positions, n, d_outputs, mlp_bf16(h), h->num_sms, s),
                    "network inference");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
         h->last_launches = 1;
@@ -940,7 +944,6 @@ nbvh_status nbvh_mlp_inference(nbvh_handle *h, const uint16_t *d_features, uint3
         require((d_features && d_outputs) || n == 0, NBVH_EINVAL, "null buffers");
         require((reinterpret_cast<uintptr_t>(d_features) & 15u) == 0u, NBVH_EINVAL,
                 "d_features must be 16-byte aligned");
-        require(h->cfg.network.precision == NBVH_PRECISION_FP16, NBVH_EINVAL, "tensor-core MLP needs FP16 weights");
         cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
         const uint32_t ni = h->layout.n_inputs, H = (uint32_t)h->cfg.network.n_hidden_layers;
         const uint32_t wb = packed_weight_bytes(ni, H);
@@ -955,7 +958,8 @@ nbvh_status nbvh_mlp_inference(nbvh_handle *h, const uint16_t *d_features, uint3
         TensorMapBytes map;
         cuda_check(make_feature_map(reinterpret_cast<const __half *>(d_features), ni, n, &map), "feature map");
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-        cuda_check(launch_mlp_tc(map, h->d_wpacked.ptr, ni, H, n, nullptr, d_outputs, h->d_status.ptr, h->num_sms, s),
+        cuda_check(launch_mlp_tc(map, h->d_wpacked.ptr, ni, H, n, nullptr, d_outputs, h->d_status.ptr, mlp_bf16(h),
+                                 h->num_sms, s),
                    "tensor-core MLP");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
         h->last_launches = 2;
@@ -990,10 +994,10 @@ void gradients_into_workspace(nbvh_handle *h, const float *d_pos, const float *d
     cuda_check(cudaMemsetAsync(h->d_grad.ptr, 0, (size_t)h->layout.n_params * sizeof(float), s), "zero grad");
     cuda_check(launch_train_forward_backward(h->d_params_h.ptr, h->grid, H, make_loss_consts(h->cfg, n), d_pos, d_tgt, n,
                                              h->d_train_acts.ptr, h->d_train_dz.ptr, h->d_grad.ptr, loss_slot,
-                                             h->num_sms, s),
+                                             mlp_bf16(h), h->num_sms, s),
                "forward/backward");
-    cuda_check(launch_weight_gradients(h->grid, H, h->d_train_acts.ptr, h->d_train_dz.ptr, n, h->d_grad.ptr, h->num_sms,
-                                       s),
+    cuda_check(launch_weight_gradients(h->grid, H, h->d_train_acts.ptr, h->d_train_dz.ptr, n, h->d_grad.ptr,
+                                       mlp_bf16(h), h->num_sms, s),
                "weight gradients");
 }
 
@@ -1029,7 +1033,7 @@ nbvh_status nbvh_adam_step(nbvh_handle *h, const float *d_gradients, nbvh_stream
         const nbvh_config &c = h->cfg;
         cuda_check(launch_adam(h->d_params.ptr, h->d_params_h.ptr, h->d_adam_m.ptr, h->d_adam_v.ptr, d_gradients,
                                h->layout.n_params, adam_step_size(c, h->training_step), c.optimizer.beta1,
-                               c.optimizer.beta2, c.optimizer.epsilon, c.optimizer.l2_reg, 1.0f,
+                               c.optimizer.beta2, c.optimizer.epsilon, c.optimizer.l2_reg, 1.0f, n_bf16_params(h),
                                reinterpret_cast<cudaStream_t>(stream)),
                    "adam");
         h->training_step++;
@@ -1078,7 +1082,7 @@ nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_sta
             lr_t = adam_step_size(c, h->training_step);
             cuda_check(launch_adam(h->d_params.ptr, h->d_params_h.ptr, h->d_adam_m.ptr, h->d_adam_v.ptr, h->d_grad.ptr,
                                    h->layout.n_params, lr_t, c.optimizer.beta1, c.optimizer.beta2, c.optimizer.epsilon,
-                                   c.optimizer.l2_reg, 1.0f / c.optimizer.loss_scale, s),
+                                   c.optimizer.l2_reg, 1.0f / c.optimizer.loss_scale, n_bf16_params(h), s),
                        "adam");
             h->training_step++;
         }

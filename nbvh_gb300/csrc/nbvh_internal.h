@@ -188,7 +188,7 @@ struct nbvh_handle {
     nbvh::GridParams grid{};
     std::vector<float> h_params; // FP32 master (host mirror, refreshed on demand)
     nbvh::DeviceBuffer<float> d_params;   // FP32 master
-    nbvh::DeviceBuffer<__half> d_params_h; // FP16 copy used by the kernels
+    nbvh::DeviceBuffer<__half> d_params_h; // 16-bit copy used by the kernels (MLP part FP16 or BF16, grid FP16)
     nbvh::DeviceBuffer<__half> d_wpacked;  // network matrices in the tensor-core operand layout
     nbvh::DeviceBuffer<uint32_t> d_status; // error word of kernels with bounded waits
     nbvh::DeviceBuffer<float> d_adam_m, d_adam_v;
@@ -302,15 +302,15 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
                               const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
                               const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
                               nbvh_neural_hit *hits, QueryCounters *counters, uint32_t *fallback_list,
-                              const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, int num_sms,
-                              cudaStream_t s, uint32_t *launches);
+                              const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, bool bf16,
+                              int num_sms, cudaStream_t s, uint32_t *launches);
 
 cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, const NeuralConsts &nc,
                             const nbvh_ray *rays, uint32_t n, uint32_t max_segments, nbvh_segment *segs,
                             uint32_t *counts, cudaStream_t s);
 
 cudaError_t launch_network_inference(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
-                                     const float *positions, uint32_t n, float *outputs, int num_sms,
+                                     const float *positions, uint32_t n, float *outputs, bool bf16, int num_sms,
                                      cudaStream_t s);
 
 // tcgen05 fully fused MLP (k_mlp_tc.cu): weights packed into the tensor-core operand layout, then
@@ -324,7 +324,7 @@ cudaError_t launch_pack_weights(const __half *params_h, uint32_t n_inputs, uint3
 cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t rows, TensorMapBytes *out);
 cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
                           uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
-                          uint32_t *status, int num_sms, cudaStream_t s);
+                          uint32_t *status, bool bf16, int num_sms, cudaStream_t s);
 
 cudaError_t launch_encode(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                           const float *positions, uint32_t n, float *features, cudaStream_t s);
@@ -339,18 +339,20 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
 cudaError_t launch_train_forward_backward(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                                           const LossConsts &lc, const float *positions, const float *targets,
                                           uint32_t n, __half *acts, __half *dz, float *grad,
-                                          float *loss_sum, int num_sms, cudaStream_t s);
+                                          float *loss_sum, bool bf16, int num_sms, cudaStream_t s);
 
 cudaError_t launch_weight_gradients(const GridParams &grid, uint32_t n_hidden_layers, const __half *acts,
-                                    const __half *dz, uint32_t n, float *grad, int num_sms, cudaStream_t s);
+                                    const __half *dz, uint32_t n, float *grad, bool bf16, int num_sms, cudaStream_t s);
 
 cudaError_t launch_scale(float *data, size_t n, float scale, cudaStream_t s);
 
 cudaError_t launch_adam(float *params, __half *params_h, float *m, float *v, const float *grad, uint32_t n,
                         float lr_t, float beta1, float beta2, float eps, float l2_reg, float grad_scale,
-                        cudaStream_t s);
+                        uint32_t n_bf16, cudaStream_t s);
 
-cudaError_t launch_params_to_half(const float *params, __half *params_h, uint32_t n, cudaStream_t s);
+// 16-bit copy of the FP32 parameters: the first n_bf16 (the network matrices when the MLP runs in
+// BF16) as BF16, the rest as FP16.
+cudaError_t launch_params_to_half(const float *params, __half *params_h, uint32_t n, uint32_t n_bf16, cudaStream_t s);
 
 cudaError_t launch_camera_rays(uint32_t width, uint32_t height, uint32_t sample_idx, uint32_t sample_offset,
                                const float *origin, const float *du, const float *dv, const float *top_left,

@@ -13,6 +13,7 @@
 // layer, after ReLU and rounding to FP16, is exactly the A-operand fragment of the next layer.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include "device_math.cuh"
@@ -83,6 +84,47 @@ __device__ __forceinline__ float2 unpack_half2(uint32_t u)
     return __half22float2(h);
 }
 
+__device__ __forceinline__ uint32_t pack_bf162(float lo, float hi)
+{
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+// Element type of the MLP operands (network weights, encoded inputs, hidden activations and the
+// backward pass's activation gradients): FP16, the reference's network precision, or BF16. Both
+// are 16-bit values multiplied on the tensor cores with FP32 accumulation; the hash-grid table
+// itself stays FP16 in either case.
+template <bool BF16>
+struct MlpPrec;
+
+template <>
+struct MlpPrec<false> {
+    __device__ static __forceinline__ uint32_t pack(float lo, float hi) { return pack_half2(lo, hi); }
+    __device__ static __forceinline__ float2 unpack(uint32_t u) { return unpack_half2(u); }
+    __device__ static __forceinline__ float round(float x) { return __half2float(__float2half_rn(x)); }
+    __device__ static __forceinline__ void mma(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+    {
+        mma16816(d, a, b0, b1);
+    }
+};
+
+template <>
+struct MlpPrec<true> {
+    __device__ static __forceinline__ uint32_t pack(float lo, float hi) { return pack_bf162(lo, hi); }
+    __device__ static __forceinline__ float2 unpack(uint32_t u)
+    {
+        return make_float2(__uint_as_float(u << 16), __uint_as_float(u & 0xFFFF0000u));
+    }
+    __device__ static __forceinline__ float round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+    __device__ static __forceinline__ void mma(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+    {
+        asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                     "{%0,%1,%2,%3};\n"
+                     : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                     : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+    }
+};
+
 // Features of one point at one level: 2 values, FMA accumulation over corners c = 0..7 (bit d of
 // c selects the upper corner along axis d), identical operation order to the CPU restatement.
 __device__ __forceinline__ float2 encode_level(const uint32_t *__restrict__ table, const GridParams &gp, uint32_t l,
@@ -121,25 +163,28 @@ __device__ __forceinline__ float2 encode_level(const uint32_t *__restrict__ tabl
     return make_float2(a0, a1);
 }
 
-// Rebuilds the FP16 A fragments of the next layer from the FP32 accumulators (after ReLU).
+// Rebuilds the 16-bit A fragments of the next layer from the FP32 accumulators (after ReLU).
+template <bool BF16>
 __device__ __forceinline__ void relu_pack(const float (&acc)[8][4], uint32_t (&a)[4][4])
 {
+    using Pr = MlpPrec<BF16>;
 #pragma unroll
     for (int kb = 0; kb < 4; kb++) {
-        a[kb][0] = pack_half2(fmaxf(acc[2 * kb][0], 0.f), fmaxf(acc[2 * kb][1], 0.f));
-        a[kb][1] = pack_half2(fmaxf(acc[2 * kb][2], 0.f), fmaxf(acc[2 * kb][3], 0.f));
-        a[kb][2] = pack_half2(fmaxf(acc[2 * kb + 1][0], 0.f), fmaxf(acc[2 * kb + 1][1], 0.f));
-        a[kb][3] = pack_half2(fmaxf(acc[2 * kb + 1][2], 0.f), fmaxf(acc[2 * kb + 1][3], 0.f));
+        a[kb][0] = Pr::pack(fmaxf(acc[2 * kb][0], 0.f), fmaxf(acc[2 * kb][1], 0.f));
+        a[kb][1] = Pr::pack(fmaxf(acc[2 * kb][2], 0.f), fmaxf(acc[2 * kb][3], 0.f));
+        a[kb][2] = Pr::pack(fmaxf(acc[2 * kb + 1][0], 0.f), fmaxf(acc[2 * kb + 1][1], 0.f));
+        a[kb][3] = Pr::pack(fmaxf(acc[2 * kb + 1][2], 0.f), fmaxf(acc[2 * kb + 1][3], 0.f));
     }
 }
 
 // Forward of one 16-row tile. make_a(kb, a) fills the layer-0 A fragment of k-block kb (16
 // inputs). On return o[0..1] are the sigmoid outputs (row g, cols 2*tig, 2*tig+1) and o[2..3]
 // those of row g + 8 (g = lane / 4, tig = lane % 4), for output columns 0..7.
-template <typename AMaker>
+template <bool BF16, typename AMaker>
 __device__ __forceinline__ void mlp_forward_tile(const __half *sw, uint32_t n_inputs, uint32_t n_hidden_layers,
                                                  AMaker &&make_a, float (&o)[4])
 {
+    using Pr = MlpPrec<BF16>;
     const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
     const SmemNetLayout L = smem_net_layout(n_inputs, n_hidden_layers);
     float acc[8][4];
@@ -155,13 +200,13 @@ __device__ __forceinline__ void mlp_forward_tile(const __half *sw, uint32_t n_in
         for (int nt = 0; nt < 8; nt++) {
             uint32_t b0 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * L.ld0);
             uint32_t b1 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * L.ld0 + 8);
-            mma16816(acc[nt], a, b0, b1);
+            Pr::mma(acc[nt], a, b0, b1);
         }
     }
     const __half *wl = sw + L.hidden_off;
     for (uint32_t layer = 1; layer < n_hidden_layers; layer++) {
         uint32_t a[4][4];
-        relu_pack(acc, a);
+        relu_pack<BF16>(acc, a);
 #pragma unroll
         for (int nt = 0; nt < 8; nt++)
             acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
@@ -172,20 +217,20 @@ __device__ __forceinline__ void mlp_forward_tile(const __half *sw, uint32_t n_in
             for (int nt = 0; nt < 8; nt++) {
                 uint32_t b0 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * kHiddenLd);
                 uint32_t b1 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * kHiddenLd + 8);
-                mma16816(acc[nt], a[kb], b0, b1);
+                Pr::mma(acc[nt], a[kb], b0, b1);
             }
         }
         wl += kNeurons * kHiddenLd;
     }
     uint32_t a[4][4];
-    relu_pack(acc, a);
+    relu_pack<BF16>(acc, a);
     float oc[4] = {0.f, 0.f, 0.f, 0.f};
     const __half *wo = sw + L.out_off + g * kHiddenLd + tig * 2;
 #pragma unroll
     for (int kb = 0; kb < 4; kb++) {
         uint32_t b0 = *reinterpret_cast<const uint32_t *>(wo + kb * 16);
         uint32_t b1 = *reinterpret_cast<const uint32_t *>(wo + kb * 16 + 8);
-        mma16816(oc, a[kb], b0, b1);
+        Pr::mma(oc, a[kb], b0, b1);
     }
 #pragma unroll
     for (int i = 0; i < 4; i++)
@@ -204,7 +249,7 @@ __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p)
 // feature tile feat[16][ld] (ld = n_inputs + 8 halves); rows not in active_mask16 are zero. Lane j
 // handles the (point, level) pairs j, j + 32, ... for all rows, four rows at a time so that 32
 // independent gathers are in flight per lane; no MLP accumulator is live here.
-template <typename PosFn>
+template <bool BF16, typename PosFn>
 __device__ __forceinline__ void encode_tile_to_smem(const uint32_t *__restrict__ table, const GridParams &gp,
                                                     PosFn &&pos, uint32_t active_mask16, __half *feat, uint32_t ld)
 {
@@ -217,7 +262,7 @@ __device__ __forceinline__ void encode_tile_to_smem(const uint32_t *__restrict__
             uint32_t v = 0u;
             if ((active_mask16 >> r) & 1u) {
                 const float2 f = encode_level(table, gp, l, pos(r, p));
-                v = pack_half2(f.x, f.y);
+                v = MlpPrec<BF16>::pack(f.x, f.y);
             }
             *reinterpret_cast<uint32_t *>(feat + r * ld + 2u * j) = v;
         }
@@ -225,14 +270,15 @@ __device__ __forceinline__ void encode_tile_to_smem(const uint32_t *__restrict__
     __syncwarp();
 }
 
-// MLP phase of a 16-row tile whose FP16 features are in feat[16][ld]; outputs as mlp_forward_tile.
+// MLP phase of a 16-row tile whose 16-bit features are in feat[16][ld]; outputs as mlp_forward_tile.
+template <bool BF16>
 __device__ __forceinline__ void mlp_tile_from_smem(const __half *sw, const __half *feat, uint32_t ld,
                                                    uint32_t n_inputs, uint32_t n_hidden_layers, float (&o)[4])
 {
     const int lane = threadIdx.x & 31;
     const __half *arow = feat + ((lane & 7) + ((lane >> 3) & 1) * 8) * ld + (lane >> 4) * 8;
     auto make_a = [&](uint32_t kb, uint32_t(&a)[4]) { ldsm_x4(a, arow + kb * 16u); };
-    mlp_forward_tile(sw, n_inputs, n_hidden_layers, make_a, o);
+    mlp_forward_tile<BF16>(sw, n_inputs, n_hidden_layers, make_a, o);
 }
 
 // Encoded segment points along [po, pi] (neural_bvh_module_kernels.cu:57-96).

@@ -46,7 +46,7 @@ class Network(C.Structure):
                 ("n_neurons", C.c_uint32), ("n_hidden_layers", C.c_uint32), ("level_offset", C.c_void_p),
                 ("level_size", C.c_void_p), ("level_resolution", C.c_void_p), ("level_scale", C.c_void_p),
                 ("grid_f16", C.c_void_p), ("weights_f16", C.c_void_p), ("exact", C.c_int32),
-                ("grid_f32", C.c_void_p), ("weights_f32", C.c_void_p)]
+                ("grid_f32", C.c_void_p), ("weights_f32", C.c_void_p), ("bf16", C.c_int32)]
 
 
 class NeuralScene(C.Structure):
@@ -60,6 +60,13 @@ class LossConsts(C.Structure):
                 ("normal_loss_scale", C.c_float), ("albedo_loss_scale", C.c_float),
                 ("output_normal_linear_activation", C.c_int32), ("output_albedo_linear_activation", C.c_int32),
                 ("visibility_masking_loss", C.c_int32), ("learn_normal", C.c_int32), ("learn_albedo", C.c_int32)]
+
+
+def bf16_bits(x):
+    """bfloat16 bits of float32 values, round to nearest even (finite values)."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = u + 0x7FFF + ((u >> 16) & 1)
+    return (u >> 16).astype(np.uint16)
 
 
 def _p(a):
@@ -150,7 +157,8 @@ class Oracle:
         return lc
 
     def network(self, cfg, layout, params, exact=False):
-        """Network struct over FP32 parameters (rounded to FP16 unless exact)."""
+        """Network struct over FP32 parameters: the network matrices rounded to the configured MLP
+        precision (FP16, or BF16 when cfg.network.precision is 1) and the grid to FP16, unless exact."""
         params = np.ascontiguousarray(params, np.float32)
         nl = layout.n_levels
         off = np.array(layout.level_offset[:nl], np.uint32)
@@ -160,7 +168,8 @@ class Oracle:
         nnet = layout.n_network_params
         w32 = np.ascontiguousarray(params[:nnet])
         g32 = np.ascontiguousarray(params[nnet:])
-        w16 = w32.astype(np.float16).view(np.uint16)
+        bf16 = int(cfg.network.precision) == 1
+        w16 = bf16_bits(w32) if bf16 else w32.astype(np.float16).view(np.uint16)
         g16 = g32.astype(np.float16).view(np.uint16)
         self._keep += [off, size, res, scale, w32, g32, w16, g16]
         net = Network()
@@ -174,6 +183,7 @@ class Oracle:
         net.grid_f16, net.weights_f16 = _p(g16).value, _p(w16).value
         net.exact = 1 if exact else 0
         net.grid_f32, net.weights_f32 = _p(g32).value, _p(w32).value
+        net.bf16 = 1 if bf16 else 0
         return net
 
     # ---- queries ----

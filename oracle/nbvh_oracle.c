@@ -580,10 +580,25 @@ float orc_f16_to_f32(uint16_t h)
 }
 
 static inline float round_f16(float x) { return orc_f16_to_f32(orc_f32_to_f16(x)); }
-static inline float net_round(const orc_network *net, float x) { return net->exact ? x : round_f16(x); }
+
+/* bfloat16: the upper 16 bits of the binary32 value, rounded to nearest even (finite inputs) */
+uint16_t orc_f32_to_bf16(float f)
+{
+    uint32_t u = f2u(f);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+float orc_bf16_to_f32(uint16_t b) { return u2f((uint32_t)b << 16); }
+static inline float round_bf16(float x) { return orc_bf16_to_f32(orc_f32_to_bf16(x)); }
+
+/* rounding of an MLP operand in the network's precision */
+static inline float round_mlp(const orc_network *net, float x) { return net->bf16 ? round_bf16(x) : round_f16(x); }
+static inline float net_round(const orc_network *net, float x) { return net->exact ? x : round_mlp(net, x); }
 static inline float net_w(const orc_network *net, size_t i)
 {
-    return net->exact ? net->weights_f32[i] : orc_f16_to_f32(net->weights_f16[i]);
+    if (net->exact)
+        return net->weights_f32[i];
+    return net->bf16 ? orc_bf16_to_f32(net->weights_f16[i]) : orc_f16_to_f32(net->weights_f16[i]);
 }
 static inline float net_g(const orc_network *net, size_t i)
 {
@@ -1266,11 +1281,11 @@ void orc_compute_gradients(const orc_network *net, const orc_loss_consts *lc, co
             total_loss += (double)vals[ch] / (double)n;
             float g = grads[ch] / (float)n;
             if (fp16_backward)
-                g = round_f16(g);
+                g = round_mlp(net, g);
             double s = 1.0 / (1.0 + exp(-pre[ch]));
             dz[ch] = (double)g * s * (1.0 - s);
             if (fp16_backward)
-                dz[ch] = (double)round_f16((float)dz[ch]);
+                dz[ch] = (double)round_mlp(net, (float)dz[ch]);
         }
         /* layers backward */
         for (int m = (int)nm - 1; m >= 0; m--) {
@@ -1292,7 +1307,7 @@ void orc_compute_gradients(const orc_network *net, const orc_loss_consts *lc, co
                 for (uint32_t k = 0; k < cols[m]; k++) {
                     double g = a[k] > 0.0f ? da[k] : 0.0; /* ReLU of the previous layer */
                     if (fp16_backward)
-                        g = (double)round_f16((float)g);
+                        g = (double)round_mlp(net, (float)g);
                     dz[k] = g;
                 }
             }
@@ -1304,8 +1319,8 @@ void orc_compute_gradients(const orc_network *net, const orc_loss_consts *lc, co
                 double g0 = da[k * net->n_levels * 2u + 2u * l];
                 double g1 = da[k * net->n_levels * 2u + 2u * l + 1u];
                 if (fp16_backward) {
-                    g0 = (double)round_f16((float)g0);
-                    g1 = (double)round_f16((float)g1);
+                    g0 = (double)round_mlp(net, (float)g0);
+                    g1 = (double)round_mlp(net, (float)g1);
                 }
                 for (uint32_t cc = 0; cc < 8; cc++) {
                     gg[2u * cidx[k][l][cc]] += (double)cw[k][l][cc] * g0;

@@ -86,6 +86,10 @@ typedef struct orc_network {
     int32_t exact;
     const float *grid_f32;
     const float *weights_f32;
+    /* MLP precision: 0 = FP16 operands (weights_f16 holds FP16 bits), 1 = BF16 operands
+     * (weights_f16 holds BF16 bits; encoded features, hidden activations and backward gradients are
+     * rounded to BF16). The grid table is FP16 either way. */
+    int32_t bf16;
 } orc_network;
 
 void orc_grid_layout(uint32_t n_levels, uint32_t log2_hashmap_size, uint32_t base_resolution,
@@ -94,6 +98,8 @@ void orc_grid_layout(uint32_t n_levels, uint32_t log2_hashmap_size, uint32_t bas
 
 uint16_t orc_f32_to_f16(float f);
 float orc_f16_to_f32(uint16_t h);
+uint16_t orc_f32_to_bf16(float f);
+float orc_bf16_to_f32(uint16_t b);
 
 /* positions: n x points x 3; features: n x n_inputs (FP32 values before FP16 rounding) */
 void orc_encode(const orc_network *net, const float *positions, uint32_t n, float *features);

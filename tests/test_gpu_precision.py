@@ -1,0 +1,126 @@
+"""BF16 network precision on the GPU against the oracle in the same precision.
+
+With network.precision = BF16 the network matrices, the encoded inputs, the hidden activations
+and the backward pass's activation gradients are bfloat16 (FP32 accumulation, FP32 master
+weights); the hash-grid table stays FP16. The oracle rounds the same tensors at the same points.
+BF16 keeps 8 mantissa bits, so a one-ulp difference in a hidden activation (from FP32 vs FP64
+accumulation order) moves an output by up to a few 1e-2 with the deliberately spread test weights;
+the bars below are set accordingly: outputs within 5e-2 absolute and 99.9% within 5e-3 (one
+observed flip: 2.7e-2, with 99.99% of outputs within 5e-3); gradients within 5e-2 relative L2 per
+parameter block.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import nbvh_gb300 as nb
+from helpers import as_u32, handle
+from nbvh_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+BF16 = {"network.precision": 1}
+
+
+def _cuda(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _close(a, b, worst=5e-2, tight=5e-3, frac=0.999):
+    d = np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64))
+    assert d.max() <= worst and np.mean(d <= tight) >= frac, (d.max(), np.mean(d <= tight))
+
+
+@pytest.fixture(scope="module")
+def scene(built):
+    h, s = handle(nb.default_config(**BF16), kind="sphere65k", seed=1, albedo=True)
+    rng = np.random.default_rng(0)
+    p = h.params()
+    nn = h.layout.n_network_params
+    p[:nn] *= 2.5
+    p[nn:] = rng.uniform(-1.0, 1.0, p.size - nn).astype(np.float32)
+    h.set_params(p)
+    s["params"] = p
+    yield h, s
+    h.close()
+
+
+def test_bf16_network_inference(scene, oracle):
+    h, s = scene
+    pos = np.random.default_rng(4).uniform(0.0, 1.0, (8192, h.cfg.module.input_segment_points, 3)).astype(np.float32)
+    got = h.network_inference(_cuda(pos)).cpu().numpy()
+    ref = oracle.network_inference(oracle.network(h.cfg, h.layout, s["params"]), pos, threads=8)[:, :8]
+    assert ref.std() > 0.05
+    _close(got, ref)
+
+
+def test_bf16_tensor_core_mlp(scene, oracle):
+    h, s = scene
+    pos = np.random.default_rng(5).uniform(0.0, 1.0, (5003, h.cfg.module.input_segment_points, 3)).astype(np.float32)
+    feats = h.encode(_cuda(pos)).to(torch.bfloat16).contiguous()
+    got = h.mlp_inference(feats).cpu().numpy()
+    ref = oracle.network_inference(oracle.network(h.cfg, h.layout, s["params"]), pos, threads=8)[:, :8]
+    _close(got, ref)
+
+
+def test_bf16_query_matches_oracle(scene, oracle):
+    h, s = scene
+    rays = scenes.uniform_rays(1 << 14, s["bbox"][:3], s["bbox"][3:], seed=41)
+    got = as_u32(h.query_closest_neural(_cuda(rays)))
+    net = oracle.network(h.cfg, h.layout, s["params"])
+    consts = oracle.neural_consts(h.cfg)
+    nscene = oracle.neural_scene(s["neural"], s["bbox"])
+    ref = oracle.neural_query(nscene, net, consts, rays, threads=8)
+    cs = oracle.classic_scene(s["nodes"], s["prims"], s["v"], s["f"])
+    border = (oracle.neural_query(nscene, net, consts, rays, classic=cs, fallback_margin=2e-2, threads=8)[:, 8] & 2) != 0
+    differ = (got[:, 8] & 1) != (ref[:, 8] & 1)
+    assert (differ & ~border).mean() < 2e-3
+    both = ((got[:, 8] & 1) == 1) & ((ref[:, 8] & 1) == 1) & ~border
+    assert both.sum() > 100
+    tg, tr = got[both, 0].view(np.float32), ref[both, 0].view(np.float32)
+    rel = np.abs(tg - tr) / np.maximum(np.abs(tr), 1e-6)
+    assert np.mean(rel <= 1e-2) > 0.99
+
+
+def test_bf16_gradients_match_oracle(scene, oracle):
+    h, s = scene
+    rng = np.random.default_rng(1)
+    p = s["params"].copy()
+    nn = h.layout.n_network_params
+    p[:nn] *= 0.8
+    p[nn:] = rng.uniform(-0.5, 0.5, p.size - nn).astype(np.float32)
+    h.set_params(p)
+    try:
+        pos, tgt, _ = h.generate_training_batch(3, 2048)
+        g, loss = h.compute_gradients(pos, tgt)
+        g = g.cpu().numpy().astype(np.float64)
+        net = oracle.network(h.cfg, h.layout, p)
+        rg, rloss = oracle.compute_gradients(net, oracle.loss_consts(h.cfg), pos.cpu().numpy(), tgt.cpu().numpy(),
+                                             h.layout.n_params, loss_scale=h.cfg.optimizer.loss_scale)
+        assert abs(loss - rloss) <= 5e-3 * abs(rloss) + 1e-6
+        H = h.cfg.network.n_hidden_layers
+        off, blocks = 0, []
+        for m in range(H + 1):
+            rows = 16 if m == H else 64
+            cols = h.layout.n_inputs if m == 0 else 64
+            blocks.append((off, off + rows * cols))
+            off += rows * cols
+        blocks.append((nn, h.layout.n_params))
+        for a, b in blocks:
+            err = np.linalg.norm(g[a:b] - rg[a:b]) / max(np.linalg.norm(rg[a:b]), 1e-30)
+            assert err < 5e-2, (a, b, err)
+    finally:
+        h.set_params(s["params"])
+
+
+def test_bf16_training_lowers_loss(built):
+    cfg = nb.default_config(batch_size=1 << 14, **BF16)
+    h, s = handle(cfg, kind="sphere4k", seed=2, depth=6)
+    try:
+        first = h.run_optimisation(20).mean_loss
+        h.run_optimisation(300)
+        last = h.run_optimisation(20).mean_loss
+        assert last < 0.7 * first
+    finally:
+        h.close()

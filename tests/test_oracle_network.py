@@ -53,6 +53,38 @@ def test_forward_matches_numpy(oracle, built):
     assert 0 < np.max(np.abs(out16 - ref)) < 2e-2
 
 
+def _bf16_round(x):
+    from oracle.bindings import bf16_bits
+    return (bf16_bits(x).astype(np.uint32) << 16).view(np.float32)
+
+
+def test_bf16_forward_matches_rounded_numpy(oracle, built):
+    """BF16 mode: the network matrices, the encoded inputs and every hidden activation are rounded
+    to bfloat16 (the grid table stays FP16); accumulation stays in higher precision."""
+    cfg = small_cfg(**{"network.precision": 1})
+    L, p = random_params(cfg, seed=3)
+    net = oracle.network(cfg, L, p)
+    pos = np.random.default_rng(2).uniform(0, 1, (64, 2, 3)).astype(np.float32)
+    feats = oracle.encode(net, pos)
+    H = cfg.network.n_hidden_layers
+    x = _bf16_round(feats).astype(np.float64)
+    off = 0
+    for m in range(H + 1):
+        rows = 16 if m == H else 64
+        cols = L.n_inputs if m == 0 else 64
+        W = _bf16_round(p[off:off + rows * cols]).reshape(rows, cols).astype(np.float64)
+        off += rows * cols
+        x = x @ W.T
+        if m < H:
+            x = _bf16_round(np.maximum(x, 0).astype(np.float32)).astype(np.float64)
+    ref = 1.0 / (1.0 + np.exp(-x))
+    out = oracle.network_inference(net, pos)
+    assert np.max(np.abs(out - ref)) < 1e-5
+    # and it differs from the FP16 network on the same parameters
+    out16 = oracle.network_inference(oracle.network(small_cfg(), L, p), pos)
+    assert np.max(np.abs(out16 - out)) > 1e-4
+
+
 def test_backward_matches_finite_differences(oracle, built):
     cfg = small_cfg(**{"output.visibility_loss": nb.abi.LOSS["L2"], "output.depth_loss": nb.abi.LOSS["L2"],
                        "output.normal_loss": nb.abi.LOSS["L2"], "output.albedo_loss": nb.abi.LOSS["L2"],
