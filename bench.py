@@ -11,11 +11,12 @@ judges depth / visibility.
 
 The same comparison is repeated on the 4,194,304-triangle sphere (key "mesh_4m"), where the
 classic traversal is deeper while the neural query still works on a 1,024-leaf cut. The tcgen05
-MLP kernel is also timed alone on 2^22 rows ("roofline_kernels.mlp_tc"), and the CPU restatements
-of the neural and classic queries run on the host cores ("cpu_baseline").
+MLP kernel is also timed alone on 2^22 rows ("roofline_kernels.mlp_tc"), the network is trained in
+FP16 and in BF16 from the same seed and compared on held-out rays ("precision_sweep"), and the CPU
+restatements of the neural and classic queries run on the host cores ("cpu_baseline").
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--train-steps T]
-                    [--mesh4m-train-steps T4 | -1] [--log2-rays R]
+                    [--mesh4m-train-steps T4 | -1] [--precision-sweep-steps T3 | 0] [--log2-rays R]
 """
 
 import argparse
@@ -51,6 +52,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1 << 14)
     ap.add_argument("--mesh4m-train-steps", type=int, default=10000,
                     help="training steps for the 4M-triangle comparison; -1 skips it")
+    ap.add_argument("--precision-sweep-steps", type=int, default=5000,
+                    help="training steps per precision in the FP16/BF16 sweep; 0 skips it")
     ap.add_argument("--log2-rays", type=int, default=22,
                     help="rays per step; smaller values are for profiling captures, not bench lines")
     return ap.parse_args()
@@ -412,6 +415,8 @@ def run_ours(args):
 
     if args.mesh4m_train_steps >= 0:
         line["mesh_4m"] = run_mesh_4m(args, nb, scenes, cfg, max_over_ranks, rank)
+    if args.precision_sweep_steps > 0:
+        line["precision_sweep"] = run_precision_sweep(args, nb, scenes, args.precision_sweep_steps)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
@@ -458,6 +463,33 @@ def run_classic_config1(h, v, f, bbox, scenes, steps, warmup, cpu_sample):
     return {"rays": n, "primary": len(prim), "bounce": len(bounce), "ms_per_step": ms,
             "mrays": n / (ms * 1e-3) / 1e6, "bit_exact_sample": bool(np.array_equal(got, ref)),
             "sample": len(idx), "cpu_mrays": len(idx) / cpu_s / 1e6, "cpu_threads": threads}
+
+
+def run_precision_sweep(args, nb, scenes, steps):
+    """Config 3: the same network trained from the same seed in each MLP precision (FP16, BF16) for
+    `steps` steps of 2^18 device-labelled rays, then evaluated against the classic kernel on 2^20
+    held-out rays (visibility agreement, depth error) and timed as a query."""
+    import torch
+    out = {}
+    for name, prec in (("fp16", 0), ("bf16", 1)):
+        cfg = nb.default_config(**{"network.precision": prec})
+        h, v, f, _ = build_scene(nb, scenes, cfg)
+        nn, bbox = h.neural_bvh()
+        t0 = time.perf_counter()
+        st = h.run_optimisation(steps)
+        train_s = time.perf_counter() - t0
+        n = 1 << 20
+        rays = torch.from_numpy(scenes.uniform_rays(n, bbox[:3], bbox[3:], seed=777)).cuda()
+        hits = torch.empty((n, 12), dtype=torch.int32, device="cuda")
+        chits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+        times, _, _, _ = time_queries(h, rays, hits, chits, 5, 3, "sweep")
+        vis, depth, segs = accuracy(hits, chits)
+        out[name] = {"train_steps": steps, "train_ms_per_step": st.ms_per_step, "train_seconds": train_s,
+                     "last_loss": st.last_loss, "heldout_rays": n, "visibility_agreement": vis,
+                     "depth_error": depth, "query_ms": float(times.mean()),
+                     "query_mrays": n / (float(times.mean()) * 1e-3) / 1e6}
+        h.close()
+    return out
 
 
 def run_mesh_4m(args, nb, scenes, cfg, max_over_ranks, rank):

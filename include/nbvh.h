@@ -414,6 +414,102 @@ nbvh_status nbvh_run_inference(nbvh_handle *h, const nbvh_render_request *req,
 nbvh_status nbvh_camera_rays(nbvh_handle *h, const nbvh_render_request *req, nbvh_ray *d_rays,
                              nbvh_stream stream);
 
+/* Hybrid path tracing over the neural BLAS: the Lambertian case of the reference's path module
+ * (scatter + next traversal, src/cuda/neural/path/path_inference_kernels.cu:224-429; raygen
+ * 540-567) as a wavefront. spp camera paths per pixel (camera_raygen jitter with the sample index
+ * running over the spp samples), up to max_bounces Lambertian bounces (cosine-sampled) on neural
+ * surfaces (network albedo and normal) and on an optional classic ground plane y = ground_height,
+ * lit only by an analytic sky (horizon colour to zenith colour with the direction's height). */
+typedef struct nbvh_path_request {
+    nbvh_render_request camera;
+    uint32_t spp;
+    uint32_t max_bounces; /* bounces after the camera ray's first hit */
+    uint32_t seed;
+    int32_t has_ground;
+    float ground_height;
+    float ground_albedo[3];
+    float sky_zenith[3];
+    float sky_horizon[3];
+    uint32_t reserved[4];
+} nbvh_path_request;
+/* d_image: width*height RGBA float32 (row-major, y down), the mean over the spp paths of each
+ * pixel. rays_traced (may be NULL) receives the number of rays queried over all bounces.
+ * Synchronous: returns when the image is written. */
+nbvh_status nbvh_render_path(nbvh_handle *h, const nbvh_path_request *req, float *d_image, uint64_t *rays_traced,
+                             nbvh_stream stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Serving loop (no counterpart in the reference, which renders one model in one process).
+ *
+ * A server takes ray-query and render requests of uneven size from many client threads against
+ * several resident models and runs them with continuous batching on one GPU: n_slots worker
+ * threads, each with its own stream and buffers sized from hbm_budget_bytes, take the oldest
+ * pending work as soon as they are free; pending queries for the same model and depth are merged
+ * into one batch up to a slot's capacity, larger requests are split. Query batches are padded to
+ * power-of-two buckets whose first part runs as a captured CUDA graph; launch parameters per
+ * bucket are chosen by timing when a model is added (autotune). Models must be added before the
+ * first request; while the server holds a handle, the handle's own calls must not run.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct nbvh_server nbvh_server;
+
+typedef struct nbvh_server_config {
+    uint32_t n_slots;          /* batches in flight at once (default 4) */
+    uint32_t max_batch_rays;   /* rays (or render paths) one batch may hold (default 2^22) */
+    uint64_t hbm_budget_bytes; /* device memory all slots' buffers may take together (default 150 GiB) */
+    uint32_t use_graphs;       /* replay captured CUDA graphs per batch-size bucket (default 1) */
+    uint32_t autotune;         /* time the launch-parameter candidates per bucket (default 1) */
+    uint32_t reserved[8];
+} nbvh_server_config;
+
+typedef enum nbvh_request_kind { NBVH_REQUEST_QUERY = 0, NBVH_REQUEST_RENDER = 1 } nbvh_request_kind;
+
+typedef struct nbvh_request {
+    uint32_t kind;  /* nbvh_request_kind */
+    uint32_t model; /* id from nbvh_server_add_model */
+    /* NBVH_REQUEST_QUERY: closest-hit neural query of n_rays host rays into host hits */
+    const nbvh_ray *h_rays;
+    uint32_t n_rays;
+    uint32_t depth; /* 1 = primary threshold, > 1 secondary (0 is taken as 1) */
+    nbvh_neural_hit *h_hits;
+    /* NBVH_REQUEST_RENDER: nbvh_render_path into h_image (width * height RGBA float32) */
+    nbvh_path_request render;
+    float *h_image;
+} nbvh_request;
+
+typedef struct nbvh_request_result {
+    nbvh_status status;
+    double latency_ms; /* submit -> done */
+    double queue_ms;   /* submit -> first batch started */
+    uint64_t rays_traced;
+} nbvh_request_result;
+
+typedef struct nbvh_server_stats {
+    uint64_t requests_done;
+    uint64_t rays_traced;
+    uint64_t batches;
+    uint64_t merged_requests; /* requests that joined another request's batch */
+    uint32_t slot_capacity_rays;
+    uint64_t graphs_captured; /* query shapes running from a captured CUDA graph */
+    uint64_t graph_replays;   /* batches answered by replaying one */
+    double p50_ms, p99_ms, mean_ms, max_ms; /* request latency, submit -> done */
+    double busy_seconds;                    /* first submit -> last completion */
+} nbvh_server_stats;
+
+nbvh_status nbvh_server_config_default(nbvh_server_config *cfg);
+nbvh_status nbvh_server_create(const nbvh_server_config *cfg, int device, nbvh_server **out);
+/* Registers a built handle (scene, cuts and parameters stay on the device); sizes every slot
+ * for it and autotunes its buckets. */
+nbvh_status nbvh_server_add_model(nbvh_server *s, nbvh_handle *model, uint32_t *model_id);
+/* Queues a request (the host buffers must stay valid until it is done); returns at once. */
+nbvh_status nbvh_server_submit(nbvh_server *s, const nbvh_request *req, uint64_t *ticket);
+/* Waits up to timeout_ms for a request; NBVH_ETIMEOUT if it is not done yet (wait again). */
+nbvh_status nbvh_server_wait(nbvh_server *s, uint64_t ticket, uint32_t timeout_ms, nbvh_request_result *result);
+nbvh_status nbvh_server_get_stats(nbvh_server *s, nbvh_server_stats *out);
+nbvh_status nbvh_server_reset_stats(nbvh_server *s);
+const char *nbvh_server_last_error(nbvh_server *s);
+/* Finishes the queued work, stops the workers and frees the server (not the models). */
+nbvh_status nbvh_server_destroy(nbvh_server *s);
+
 /* Checkpoint: config, mesh, both BVHs, FP32 parameters, Adam moments and step (own format). */
 nbvh_status nbvh_save(nbvh_handle *h, const char *path);
 nbvh_status nbvh_load(nbvh_handle *h, const char *path);

@@ -14,7 +14,8 @@ import os
 import numpy as np
 
 from . import abi
-from .abi import Config, ParamLayout, QueryStats, RenderRequest, TrainStats
+from .abi import (Config, ParamLayout, PathRequest, QueryStats, RenderRequest, Request, RequestResult,
+                  ServerConfig, ServerStats, TrainStats)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libnbvh.so")
@@ -405,6 +406,15 @@ class NBVH:
         self._check(self.lib.nbvh_run_inference(self.h, C.byref(req), _ptr(img), _stream(stream)))
         return img
 
+    def render_path(self, req, stream=None):
+        """Path-traced RGBA image (float32 [height * width, 4] on the device) and the rays traced."""
+        import torch
+        cam = req.camera
+        img = torch.empty((cam.width * cam.height, 4), dtype=torch.float32, device=torch.device("cuda", self.device))
+        traced = C.c_uint64(0)
+        self._check(self.lib.nbvh_render_path(self.h, C.byref(req), _ptr(img), C.byref(traced), _stream(stream)))
+        return img, traced.value
+
     # ---- checkpoints, stats ----
     def save(self, path):
         self._check(self.lib.nbvh_save(self.h, path.encode()))
@@ -427,6 +437,21 @@ class NBVH:
         return ms.value, launches.value
 
 
+def path_request(camera, spp=1, max_bounces=4, seed=0, ground_height=None, ground_albedo=(0.5, 0.5, 0.5),
+                 sky_zenith=(0.35, 0.55, 1.0), sky_horizon=(1.0, 1.0, 1.0)):
+    """nbvh_path_request over a render_request camera (ground plane off when ground_height is None)."""
+    r = PathRequest()
+    r.camera = camera
+    r.spp, r.max_bounces, r.seed = spp, max_bounces, seed
+    r.has_ground = 0 if ground_height is None else 1
+    r.ground_height = 0.0 if ground_height is None else float(ground_height)
+    for k in range(3):
+        r.ground_albedo[k] = float(ground_albedo[k])
+        r.sky_zenith[k] = float(sky_zenith[k])
+        r.sky_horizon[k] = float(sky_horizon[k])
+    return r
+
+
 def render_request(width, height, origin, target, up=(0.0, 1.0, 0.0), yfov_degrees=45.0, sample_idx=0,
                    sample_offset=0):
     r = RenderRequest()
@@ -446,3 +471,84 @@ __all__ = [
     "build_bvh2_host", "build_neural_cut_host", "nodes_to_float", "render_request", "RAY_DTYPE", "HIT_DTYPE",
     "NEURAL_HIT_DTYPE", "SEGMENT_DTYPE", "FLT_MAX",
 ]
+
+
+class Server:
+    """The serving loop (nbvh_server_*): continuous batching of query and render requests from
+    many client threads against several resident models. Host buffers passed to submit must stay
+    alive until wait returns."""
+
+    def __init__(self, n_slots=4, hbm_budget_gb=150.0, max_batch_rays=1 << 22, use_graphs=True, autotune=True,
+                 device=0):
+        self.lib = load_library()
+        cfg = ServerConfig()
+        _check(self.lib.nbvh_server_config_default(C.byref(cfg)), None)
+        cfg.n_slots, cfg.max_batch_rays = n_slots, max_batch_rays
+        cfg.hbm_budget_bytes = int(hbm_budget_gb * (1 << 30))
+        cfg.use_graphs, cfg.autotune = int(use_graphs), int(autotune)
+        s = C.c_void_p()
+        st = self.lib.nbvh_server_create(C.byref(cfg), device, C.byref(s))
+        if st != abi.NBVH_OK:
+            raise NBVHError(st, self.lib.nbvh_status_string(st).decode())
+        self.s = s
+        self._keep = {}
+
+    def _check(self, st):
+        if st != abi.NBVH_OK:
+            raise NBVHError(st, self.lib.nbvh_server_last_error(self.s).decode())
+
+    def add_model(self, handle):
+        mid = C.c_uint32(0)
+        self._check(self.lib.nbvh_server_add_model(self.s, handle.h, C.byref(mid)))
+        return mid.value
+
+    def submit_query(self, model, rays_np, depth=1):
+        rays = np.ascontiguousarray(rays_np, np.float32).reshape(-1, 8)
+        hits = np.empty(len(rays), NEURAL_HIT_DTYPE)
+        r = Request()
+        r.kind, r.model, r.n_rays, r.depth = 0, model, len(rays), depth
+        r.h_rays, r.h_hits = rays.ctypes.data, hits.ctypes.data
+        t = C.c_uint64(0)
+        self._check(self.lib.nbvh_server_submit(self.s, C.byref(r), C.byref(t)))
+        self._keep[t.value] = (rays, hits)
+        return t.value
+
+    def submit_render(self, model, path_req):
+        cam = path_req.camera
+        img = np.empty((cam.width * cam.height, 4), np.float32)
+        r = Request()
+        r.kind, r.model = 1, model
+        r.render = path_req
+        r.h_image = img.ctypes.data
+        t = C.c_uint64(0)
+        self._check(self.lib.nbvh_server_submit(self.s, C.byref(r), C.byref(t)))
+        self._keep[t.value] = (img,)
+        return t.value
+
+    def wait(self, ticket, timeout_ms=60000):
+        """(output array, RequestResult): hits for a query, the RGBA image for a render."""
+        res = RequestResult()
+        st = self.lib.nbvh_server_wait(self.s, ticket, timeout_ms, C.byref(res))
+        if st != abi.NBVH_OK:
+            raise NBVHError(st, self.lib.nbvh_server_last_error(self.s).decode())
+        bufs = self._keep.pop(ticket)
+        return bufs[-1], res
+
+    def stats(self):
+        st = ServerStats()
+        self._check(self.lib.nbvh_server_get_stats(self.s, C.byref(st)))
+        return st
+
+    def reset_stats(self):
+        self._check(self.lib.nbvh_server_reset_stats(self.s))
+
+    def close(self):
+        if getattr(self, "s", None):
+            self.lib.nbvh_server_destroy(self.s)
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -85,6 +85,34 @@ class RenderRequest(C.Structure):
                 ("up", C.c_float * 3), ("yfov_degrees", C.c_float)]
 
 
+class PathRequest(C.Structure):
+    _fields_ = [("camera", RenderRequest), ("spp", C.c_uint32), ("max_bounces", C.c_uint32), ("seed", C.c_uint32),
+                ("has_ground", C.c_int32), ("ground_height", C.c_float), ("ground_albedo", C.c_float * 3),
+                ("sky_zenith", C.c_float * 3), ("sky_horizon", C.c_float * 3), ("reserved", C.c_uint32 * 4)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("n_slots", C.c_uint32), ("max_batch_rays", C.c_uint32), ("hbm_budget_bytes", C.c_uint64),
+                ("use_graphs", C.c_uint32), ("autotune", C.c_uint32), ("reserved", C.c_uint32 * 8)]
+
+
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("model", C.c_uint32), ("h_rays", C.c_void_p), ("n_rays", C.c_uint32),
+                ("depth", C.c_uint32), ("h_hits", C.c_void_p), ("render", PathRequest), ("h_image", C.c_void_p)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("latency_ms", C.c_double), ("queue_ms", C.c_double),
+                ("rays_traced", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("requests_done", C.c_uint64), ("rays_traced", C.c_uint64), ("batches", C.c_uint64),
+                ("merged_requests", C.c_uint64), ("slot_capacity_rays", C.c_uint32),
+                ("graphs_captured", C.c_uint64), ("graph_replays", C.c_uint64), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double), ("busy_seconds", C.c_double)]
+
+
 class QueryStats(C.Structure):
     _fields_ = [("rays", C.c_uint32), ("segments", C.c_uint32), ("step_capped", C.c_uint32),
                 ("stack_overflow", C.c_uint32), ("fallback", C.c_uint32)]
@@ -134,6 +162,16 @@ PROTOTYPES = {
     "nbvh_training_step": (U32, [P]),
     "nbvh_run_inference": (ST, [P, C.POINTER(RenderRequest), P, P]),
     "nbvh_camera_rays": (ST, [P, C.POINTER(RenderRequest), P, P]),
+    "nbvh_render_path": (ST, [P, C.POINTER(PathRequest), P, C.POINTER(C.c_uint64), P]),
+    "nbvh_server_config_default": (ST, [C.POINTER(ServerConfig)]),
+    "nbvh_server_create": (ST, [C.POINTER(ServerConfig), C.c_int, C.POINTER(C.c_void_p)]),
+    "nbvh_server_add_model": (ST, [P, P, C.POINTER(C.c_uint32)]),
+    "nbvh_server_submit": (ST, [P, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    "nbvh_server_wait": (ST, [P, C.c_uint64, C.c_uint32, C.POINTER(RequestResult)]),
+    "nbvh_server_get_stats": (ST, [P, C.POINTER(ServerStats)]),
+    "nbvh_server_reset_stats": (ST, [P]),
+    "nbvh_server_last_error": (C.c_char_p, [P]),
+    "nbvh_server_destroy": (ST, [P]),
     "nbvh_save": (ST, [P, C.c_char_p]),
     "nbvh_load": (ST, [P, C.c_char_p]),
     "nbvh_last_query_stats": (ST, [P, C.POINTER(QueryStats)]),

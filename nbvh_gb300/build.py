@@ -18,8 +18,10 @@ SOURCES = [
     "k_train.cu",
     "k_misc.cu",
     "k_mlp_tc.cu",
+    "k_path.cu",
     "k_query.cu",
     "nbvh_api.cpp",
+    "nbvh_server.cpp",
     "bvh_builder.cpp",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -295,7 +295,7 @@ cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t
 
 cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
                           uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
-                          uint32_t *status, bool bf16, int num_sms, cudaStream_t s)
+                          uint32_t *status, bool bf16, int num_sms, cudaStream_t s, bool configure)
 {
     if (rows == 0)
         return cudaSuccess;
@@ -311,10 +311,12 @@ cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpack
     a.outputs = outputs;
     a.status = status;
     const size_t smem = ((a.wbytes + 1023u) & ~1023u) + kTileRows * n_inputs * 2u + 32u;
-    cudaError_t e = bf16 ? cudaFuncSetAttribute(k_mlp_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                         : cudaFuncSetAttribute(k_mlp_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess)
-        return e;
+    if (configure) {
+        const cudaError_t e = bf16 ? allow_max_dynamic_smem(k_mlp_tc<true>)
+                                   : allow_max_dynamic_smem(k_mlp_tc<false>);
+        if (e != cudaSuccess)
+            return e;
+    }
     const uint32_t tiles = (rows + kTileRows - 1u) / kTileRows;
     uint32_t blocks = (uint32_t)num_sms * 3u;
     if (blocks > tiles)

@@ -133,7 +133,8 @@ __global__ void __launch_bounds__(128) k_encode(const __grid_constant__ GridPara
 template <typename K>
 cudaError_t prepare_smem(K kernel, size_t bytes)
 {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    (void)bytes; // every launch stays below the common limit
+    return allow_max_dynamic_smem(kernel);
 }
 
 } // namespace

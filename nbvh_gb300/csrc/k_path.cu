@@ -1,0 +1,181 @@
+// k_path.cu -- hybrid path tracing over a neural BLAS: camera paths, Lambertian bounces on the
+// surfaces the neural query returns (albedo and normal from the network), a classic analytic
+// ground plane, and an analytic sky as the only light.
+//
+// The reference's path module (src/cuda/neural/path/path_inference_kernels.cu:224-429, scatter +
+// next traversal; raygen 540-567) drives a Disney BSDF over a TLAS; this restates the Lambertian
+// case as a wavefront: raygen -> [neural query -> shade/scatter with compaction] per bounce ->
+// resolve. Paths that leave the scene collect sky radiance weighted by their throughput.
+#include "device_math.cuh"
+#include "nbvh_internal.h"
+
+namespace nbvh {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+// Duff et al., "Building an Orthonormal Basis, Revisited", JCGT 6(1), 2017.
+__device__ __forceinline__ void onb(V3 n, V3 &t, V3 &b)
+{
+    const float sign = n.z >= 0.0f ? 1.0f : -1.0f;
+    const float a = -1.0f / (sign + n.z);
+    const float c = n.x * n.y * a;
+    t = mk3(1.0f + sign * n.x * n.x * a, sign * c, -sign * n.x);
+    b = mk3(c, sign + n.y * n.y * a, -n.y);
+}
+
+// Cosine-weighted direction about n (Malley's method: uniform disk point lifted to the hemisphere).
+__device__ __forceinline__ V3 cosine_sample(V3 n, uint32_t &rng)
+{
+    const float u1 = lcg_randomf(rng), u2 = lcg_randomf(rng);
+    float sp, cp;
+    sincos_turns(u2, sp, cp);
+    const float r = sqrtf(u1), z = sqrtf(fmaxf(0.0f, 1.0f - u1));
+    V3 t, b;
+    onb(n, t, b);
+    return mk3(r * cp * t.x + r * sp * b.x + z * n.x, r * cp * t.y + r * sp * b.y + z * n.y,
+               r * cp * t.z + r * sp * b.z + z * n.z);
+}
+
+__device__ __forceinline__ uint32_t warp_append(bool want, uint32_t *counter)
+{
+    const unsigned m = __ballot_sync(kFull, want);
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (m != 0u) {
+        const int leader = __ffs(m) - 1;
+        if (lane == leader)
+            base = atomicAdd(counter, (uint32_t)__popc(m));
+        base = __shfl_sync(kFull, base, leader);
+    }
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(256) k_pt_raygen(const __grid_constant__ PathArgs a)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; // path = pixel * spp + sample
+    if (i >= a.n_paths)
+        return;
+    const uint32_t p = i / a.spp, smp = i - p * a.spp;
+    const uint32_t px = p % a.width, py = p / a.width;
+    // camera_raygen jitter (include/cuda/neural/neural_bvh_module_common.cuh:222-228) with the
+    // sample index running over the frame's samples from sample_base
+    uint32_t rng = lcg_seed(a.sample_base + smp, a.sample_offset, p);
+    const float jx = lcg_randomf(rng), jy = lcg_randomf(rng);
+    const float xf = __fdiv_rn(__fadd_rn((float)px, jx), (float)a.width);
+    const float yf = __fdiv_rn(__fadd_rn((float)py, jy), (float)a.height);
+    const V3 du = mk3(a.du[0], a.du[1], a.du[2]), dv = mk3(a.dv[0], a.dv[1], a.dv[2]),
+             tl = mk3(a.tl[0], a.tl[1], a.tl[2]);
+    const V3 d = normalize3(add3(add3(scale3(du, xf), scale3(dv, yf)), tl));
+    float4 *r = reinterpret_cast<float4 *>(a.rays_out + i);
+    r[0] = make_float4(a.origin[0], a.origin[1], a.origin[2], 1e-4f);
+    r[1] = make_float4(d.x, d.y, d.z, FLT_MAX);
+    a.ids_out[i] = i;
+    a.thr[i] = make_float4(1.f, 1.f, 1.f, __uint_as_float(rng ^ (a.seed * 0x9E3779B9u)));
+    a.rad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// One bounce: the nearer of the neural hit and the ground plane is shaded; misses collect sky
+// radiance; surviving paths (bounce < max_bounces) are appended to the next list with a
+// cosine-sampled direction about the surface normal facing the incoming ray.
+__global__ void __launch_bounds__(256) k_pt_shade(const __grid_constant__ PathArgs a, uint32_t count_in, uint32_t bounce)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = j < count_in;
+    bool keep = false;
+    uint32_t id = 0;
+    V3 o = mk3(0.f, 0.f, 0.f), nd = mk3(0.f, 0.f, 1.f);
+    float4 th = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (in) {
+        id = a.ids_in[j];
+        const float4 *r = reinterpret_cast<const float4 *>(a.rays_in + j);
+        const float4 ra = r[0], rb = r[1];
+        const V3 ro = mk3(ra.x, ra.y, ra.z), d = mk3(rb.x, rb.y, rb.z);
+        const float4 *hp = reinterpret_cast<const float4 *>(a.hits + j);
+        const float4 h0 = hp[0], h1 = hp[1], h2 = hp[2];
+        const bool nhit = (__float_as_uint(h2.x) & NBVH_HIT_VALID) != 0u;
+        float t = nhit ? h0.x : FLT_MAX;
+        V3 n = mk3(h0.y, h0.z, h0.w), alb = mk3(h1.x, h1.y, h1.z);
+        if (a.has_ground && d.y != 0.0f) {
+            const float tp = (a.ground_y - ro.y) / d.y;
+            if (tp > 1e-4f && tp < t) {
+                t = tp;
+                n = mk3(0.f, 1.f, 0.f);
+                alb = mk3(a.ground_albedo[0], a.ground_albedo[1], a.ground_albedo[2]);
+            }
+        }
+        th = a.thr[id];
+        if (t == FLT_MAX) {
+            const float w = fmaxf(d.y, 0.0f);
+            float4 rad = a.rad[id];
+            rad.x += th.x * (a.sky_horizon[0] + (a.sky_zenith[0] - a.sky_horizon[0]) * w);
+            rad.y += th.y * (a.sky_horizon[1] + (a.sky_zenith[1] - a.sky_horizon[1]) * w);
+            rad.z += th.z * (a.sky_horizon[2] + (a.sky_zenith[2] - a.sky_horizon[2]) * w);
+            a.rad[id] = rad;
+        } else if (bounce < a.max_bounces) {
+            const float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+            n = len > 0.f ? mk3(n.x / len, n.y / len, n.z / len) : mk3(-d.x, -d.y, -d.z);
+            if (n.x * d.x + n.y * d.y + n.z * d.z > 0.0f)
+                n = mk3(-n.x, -n.y, -n.z);
+            uint32_t rng = __float_as_uint(th.w);
+            nd = cosine_sample(n, rng);
+            th = make_float4(th.x * alb.x, th.y * alb.y, th.z * alb.z, __uint_as_float(rng));
+            a.thr[id] = th;
+            o = mk3(ro.x + t * d.x + 1e-3f * n.x, ro.y + t * d.y + 1e-3f * n.y, ro.z + t * d.z + 1e-3f * n.z);
+            keep = th.x + th.y + th.z > 0.0f;
+        }
+    }
+    const uint32_t pos = warp_append(keep, a.count_out);
+    if (keep) {
+        float4 *r = reinterpret_cast<float4 *>(a.rays_out + pos);
+        r[0] = make_float4(o.x, o.y, o.z, 1e-4f);
+        r[1] = make_float4(nd.x, nd.y, nd.z, FLT_MAX);
+        a.ids_out[pos] = id;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_pt_resolve(const __grid_constant__ PathArgs a, float4 *__restrict__ image)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.width * a.height)
+        return;
+    float r = 0.f, g = 0.f, b = 0.f;
+    for (uint32_t s = 0; s < a.spp; s++) {
+        const float4 v = a.rad[p * a.spp + s];
+        r += v.x;
+        g += v.y;
+        b += v.z;
+    }
+    const float inv = 1.0f / (float)a.spp;
+    image[p] = make_float4(r * inv, g * inv, b * inv, 1.0f);
+}
+
+} // namespace
+
+cudaError_t launch_path_raygen(const PathArgs &a, cudaStream_t s)
+{
+    if (a.n_paths == 0)
+        return cudaSuccess;
+    k_pt_raygen<<<(a.n_paths + 255u) / 256u, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_path_shade(const PathArgs &a, uint32_t count_in, uint32_t bounce, cudaStream_t s)
+{
+    if (count_in == 0)
+        return cudaSuccess;
+    k_pt_shade<<<(count_in + 255u) / 256u, 256, 0, s>>>(a, count_in, bounce);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_path_resolve(const PathArgs &a, float *image, cudaStream_t s)
+{
+    const uint32_t n = a.width * a.height;
+    if (n == 0)
+        return cudaSuccess;
+    k_pt_resolve<<<(n + 255u) / 256u, 256, 0, s>>>(a, reinterpret_cast<float4 *>(image));
+    return cudaGetLastError();
+}
+
+} // namespace nbvh

@@ -34,7 +34,8 @@ constexpr uint32_t kFirstThreads = 256;
 constexpr uint32_t kSortThreads = 1024;
 // Lists shorter than this are walked in list order: the sort would cost more than the locality it buys.
 constexpr uint32_t kSortMinRows = 1u << 16;
-constexpr int kVisitsPerRound = 8; // node visits of the next-leaf search between refills
+constexpr uint32_t kDefaultVisitsPerRound = 8;  // node visits of a traversal between lane refills
+constexpr uint32_t kDefaultEncodeBlocksPerSm = 8; // 2,048 resident threads
 // decode: the shared-memory cut variant runs one 768-thread block per SM, the global-memory
 // variant two 384-thread blocks; both leave 85 registers per thread (the traversal stack stays in
 // registers and local memory without spilling)
@@ -62,7 +63,8 @@ struct WaveArgs {
     uint32_t n_hidden_layers;
     uint32_t n;
     uint32_t n_cut_nodes;
-    uint32_t bf16; // MLP inputs in BF16 (else FP16)
+    uint32_t bf16;   // MLP inputs in BF16 (else FP16)
+    uint32_t visits; // node visits per traversal round between lane refills
 };
 
 __device__ __forceinline__ void write_hit(nbvh_neural_hit *hits, uint32_t id, float t, V3 nrm, V3 alb, float vis,
@@ -150,7 +152,7 @@ __device__ __forceinline__ void count_nodes(uint32_t *bins, bool want, uint32_t 
 // K2 first pass: the first entered leaf of every ray (the first leaf is searched with an unbounded
 // current_maxt, include/cuda/neural/neural_bvh_module_common.cuh:332-343). Rays that enter none
 // are answered at once; the others are appended to state list 0. Persistent warps take rays from
-// a work counter and refill lanes between rounds of kVisitsPerRound node visits, as the decode
+// a work counter and refill lanes between rounds of a.visits node visits, as the decode
 // kernel does, so the warp's lanes stay busy while the traversal lengths differ.
 __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_constant__ WaveArgs a)
 {
@@ -195,7 +197,7 @@ __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_co
         if (active) {
             const int res = neural_intersect_inference(cut, a.nc.bvh_lod, s.o, rdiv, cull_ok, stack, s.sp,
                                                        a.nc.inference_mint_epsilon, a.nc.inference_maxt_epsilon,
-                                                       FLT_MAX, s.seg_mint, s.seg_maxt, s.seg_node, kVisitsPerRound);
+                                                       FLT_MAX, s.seg_mint, s.seg_maxt, s.seg_node, (int)a.visits);
             if (res != 2) {
                 active = false;
                 const uint32_t i = s.ray_id;
@@ -436,7 +438,7 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
 
     // Persistent warps with per-lane refill (after Aila and Laine, "Understanding the efficiency of
     // ray traversal on GPUs", HPG 2009): the next-leaf search takes a different number of node
-    // visits per ray, so each round runs at most kVisitsPerRound visits, after which lanes whose ray
+    // visits per ray, so each round runs at most a.visits visits, after which lanes whose ray
     // is done take a new row from the step's work counter. Lanes stay busy instead of waiting for
     // the longest traversal of their warp. All lanes run every round (warp_append needs all 32).
     uint32_t *head = &a.wave_counts[4u + it % 3u];
@@ -534,7 +536,7 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
             // hit so far (best_t) bounds the search
             const int res = neural_intersect_inference(cut, nc.bvh_lod, s.o, rdiv, cull_ok, stack, s.sp,
                                                        nc.inference_mint_epsilon, nc.inference_maxt_epsilon, s.best_t,
-                                                       s.seg_mint, s.seg_maxt, s.seg_node, kVisitsPerRound);
+                                                       s.seg_mint, s.seg_maxt, s.seg_node, (int)a.visits);
             if (res != 2) {
                 active = false;
                 bool done = false;
@@ -585,67 +587,109 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
     }
 }
 
-constexpr size_t kSmemLimit = 227u * 1024u;
+constexpr size_t kSmemLimit = (size_t)kMaxDynamicSmem;
 constexpr uint32_t kStepsPerCheck = 4;
 
-// One batch of steps per host check; each step is K3 -> K4 -> K2 on the stream.
+// The kernels of steps [it0, it1): sort, K3, K4, K2 per step, no host synchronisation.
 template <bool SMEM_CUT>
-cudaError_t run_steps(const WaveArgs &a, const StepResources &r, size_t dec_smem, int num_sms, uint32_t max_steps,
-                      cudaStream_t s, uint32_t &launches)
+cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_smem, int num_sms, uint32_t it0,
+                          uint32_t it1, cudaStream_t s, uint32_t &launches)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_wave_decode<SMEM_CUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)dec_smem);
-    if (e == cudaSuccess && a.perm)
-        e = cudaFuncSetAttribute(k_wave_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(3u * a.n_sort_nodes * 4u));
+    cudaError_t e = cudaSuccess;
+    const uint32_t enc_per_sm = r.encode_blocks_per_sm ? r.encode_blocks_per_sm : kDefaultEncodeBlocksPerSm;
+    const uint32_t enc_blocks = (uint32_t)num_sms * enc_per_sm;
+    const uint32_t dec_blocks = (uint32_t)num_sms * (SMEM_CUT ? 1u : 2u);
+    for (uint32_t it = it0; it < it1; it++) {
+        if (a.perm) {
+            k_wave_sort<<<(uint32_t)num_sms, kSortThreads, 3u * a.n_sort_nodes * 4u, s>>>(a, it);
+            e = cudaGetLastError();
+            if (e != cudaSuccess)
+                return e;
+            launches++;
+        }
+        k_wave_encode<<<enc_blocks, kEncodeThreads, 0, s>>>(a, it);
+        e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return e;
+        e = launch_mlp_tc(r.feature_map, r.wpacked, a.grid.n_inputs, a.n_hidden_layers, a.lists[0].capacity,
+                          &a.wave_counts[it % 3u], a.outputs, &a.wave_counts[3], a.bf16 != 0u, num_sms, s,
+                          !r.capture_only);
+        if (e != cudaSuccess)
+            return e;
+        k_wave_decode<SMEM_CUT><<<dec_blocks, decode_threads(SMEM_CUT), dec_smem, s>>>(a, it);
+        e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return e;
+        launches += 3u;
+    }
+    return cudaSuccess;
+}
+
+// Copies the wave counters to the host words and waits for them; 1 if the list of step `it` is
+// empty (the query is done), 0 if not, or an error (cudaErrorTimeout if the MLP's bounded wait
+// gave up).
+cudaError_t check_done(const WaveArgs &a, const StepResources &r, uint32_t it, cudaStream_t s, bool &done)
+{
+    cudaError_t e = cudaMemcpyAsync(r.h_words, a.wave_counts, 4u * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess)
         return e;
-    const uint32_t enc_blocks = (uint32_t)num_sms * (2048u / kEncodeThreads);
-    const uint32_t dec_blocks = (uint32_t)num_sms * (SMEM_CUT ? 1u : 2u);
-    // every listed ray advances one leaf per step; the loop ends when a list comes out empty or the
-    // step cap (each ray at most max_traversal_steps + 1 segments) plus the final capping step is reached
-    const uint32_t limit = max_steps + 2u;
-    for (uint32_t it = 0; it < limit;) {
-        const uint32_t batch = (limit - it) < kStepsPerCheck ? (limit - it) : kStepsPerCheck;
-        for (uint32_t b = 0; b < batch; b++, it++) {
-            if (a.perm) {
-                k_wave_sort<<<(uint32_t)num_sms, kSortThreads, 3u * a.n_sort_nodes * 4u, s>>>(a, it);
-                e = cudaGetLastError();
-                if (e != cudaSuccess)
-                    return e;
-                launches++;
-            }
-            k_wave_encode<<<enc_blocks, kEncodeThreads, 0, s>>>(a, it);
-            e = cudaGetLastError();
-            if (e != cudaSuccess)
-                return e;
-            e = launch_mlp_tc(r.feature_map, r.wpacked, a.grid.n_inputs, a.n_hidden_layers, a.lists[0].capacity,
-                              &a.wave_counts[it % 3u], a.outputs, &a.wave_counts[3], a.bf16 != 0u, num_sms, s);
-            if (e != cudaSuccess)
-                return e;
-            k_wave_decode<SMEM_CUT><<<dec_blocks, decode_threads(SMEM_CUT), dec_smem, s>>>(a, it);
-            e = cudaGetLastError();
-            if (e != cudaSuccess)
-                return e;
-            launches += 3u;
-        }
-        e = cudaMemcpyAsync(r.h_words, a.wave_counts, 4u * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        if (e != cudaSuccess)
-            return e;
-        if (r.ev) {
-            e = cudaEventRecord(r.ev, s);
-            if (e != cudaSuccess)
-                return e;
+    if (r.ev) {
+        e = cudaEventRecord(r.ev, s);
+        if (e == cudaSuccess)
             e = cudaEventSynchronize(r.ev);
-        } else {
-            e = cudaStreamSynchronize(s);
-        }
+    } else {
+        e = cudaStreamSynchronize(s);
+    }
+    if (e != cudaSuccess)
+        return e;
+    if (r.h_words[3] != 0u)
+        return cudaErrorTimeout;
+    done = r.h_words[it % 3u] == 0u;
+    return cudaSuccess;
+}
+
+// The step loop from step `from` (after `unchecked` steps launched without a host check when from
+// is 0): batches of kStepsPerCheck steps, the host reading the list length after each batch. The
+// loop ends when a list comes out empty or at the step cap (each ray at most
+// max_traversal_steps + 1 segments) plus the final capping step. With capture_only the unchecked
+// steps and the copy of the counters are only enqueued (for stream capture) and nothing waits.
+template <bool SMEM_CUT>
+cudaError_t run_steps(const WaveArgs &a, const StepResources &r, size_t dec_smem, int num_sms, uint32_t max_steps,
+                      uint32_t from, cudaStream_t s, uint32_t &launches)
+{
+    cudaError_t e = cudaSuccess;
+    if (!r.capture_only) { // kernel attributes are set outside stream capture (an earlier run set them)
+        e = allow_max_dynamic_smem(k_wave_decode<SMEM_CUT>);
+        if (e == cudaSuccess && a.perm)
+            e = allow_max_dynamic_smem(k_wave_sort);
         if (e != cudaSuccess)
             return e;
-        if (r.h_words[3] != 0u)
-            return cudaErrorTimeout; // a bounded wait inside the tensor-core MLP gave up
-        if (r.h_words[it % 3u] == 0u)
-            break;
+    }
+    const uint32_t limit = max_steps + 2u;
+    uint32_t it = from;
+    if (from == 0u && r.unchecked_steps > 0u) {
+        const uint32_t u = r.unchecked_steps < limit ? r.unchecked_steps : limit;
+        e = enqueue_steps<SMEM_CUT>(a, r, dec_smem, num_sms, 0u, u, s, launches);
+        if (e != cudaSuccess)
+            return e;
+        it = u;
+        if (r.capture_only)
+            return cudaMemcpyAsync(r.h_words, a.wave_counts, 4u * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        bool done = false;
+        e = check_done(a, r, it, s, done);
+        if (e != cudaSuccess || done)
+            return e;
+    }
+    while (it < limit) {
+        const uint32_t batch = (limit - it) < kStepsPerCheck ? (limit - it) : kStepsPerCheck;
+        e = enqueue_steps<SMEM_CUT>(a, r, dec_smem, num_sms, it, it + batch, s, launches);
+        if (e != cudaSuccess)
+            return e;
+        it += batch;
+        bool done = false;
+        e = check_done(a, r, it, s, done);
+        if (e != cudaSuccess || done)
+            return e;
     }
     return cudaSuccess;
 }
@@ -689,6 +733,12 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
     a.n_cut_nodes = n_cut_nodes;
+    a.visits = res.visits_per_round ? res.visits_per_round : kDefaultVisitsPerRound;
+    const size_t smem_cut = (size_t)n_cut_nodes * 56u;
+    if (res.resume_from > 0u) // continue a query whose first steps ran from a captured graph
+        return smem_cut <= kSmemLimit
+                   ? run_steps<true>(a, res, smem_cut, num_sms, nc.max_traversal_steps, res.resume_from, s, *launches)
+                   : run_steps<false>(a, res, 0, num_sms, nc.max_traversal_steps, res.resume_from, s, *launches);
     // words 0-2: rotating list lengths; 3: the MLP's error word; 4-6: rotating work counters of
     // the decode kernel; 7: work counter of the first pass
     cudaError_t e = cudaMemsetAsync(wave_counts, 0, 8u * sizeof(uint32_t), s);
@@ -713,10 +763,9 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     if (e != cudaSuccess)
         return e;
     *launches = 2;
-    const size_t smem_cut = (size_t)n_cut_nodes * 56u;
     if (smem_cut <= kSmemLimit)
-        return run_steps<true>(a, res, smem_cut, num_sms, nc.max_traversal_steps, s, *launches);
-    return run_steps<false>(a, res, 0, num_sms, nc.max_traversal_steps, s, *launches);
+        return run_steps<true>(a, res, smem_cut, num_sms, nc.max_traversal_steps, 0u, s, *launches);
+    return run_steps<false>(a, res, 0, num_sms, nc.max_traversal_steps, 0u, s, *launches);
 }
 
 // ---------------------------------------------------------------------------------------------

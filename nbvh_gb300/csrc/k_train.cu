@@ -774,8 +774,8 @@ cudaError_t launch_train_forward_backward(const __half *params_h, const GridPara
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
     const size_t smem = sizeof(GridParams) + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half);
-    cudaError_t e = bf16 ? cudaFuncSetAttribute(k_train_fwd_bwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                         : cudaFuncSetAttribute(k_train_fwd_bwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = bf16 ? allow_max_dynamic_smem(k_train_fwd_bwd<true>)
+                         : allow_max_dynamic_smem(k_train_fwd_bwd<false>);
     if (e != cudaSuccess)
         return e;
     const uint32_t tiles = (n + 15u) / 16u;
@@ -793,8 +793,7 @@ cudaError_t launch_train_forward_backward(const __half *params_h, const GridPara
 template <int TPW, bool BF16>
 cudaError_t run_weight_grads(const WgArgs &a, uint32_t blocks, size_t smem, cudaStream_t s)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_weight_grads<TPW, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = allow_max_dynamic_smem(k_weight_grads<TPW, BF16>);
     if (e != cudaSuccess)
         return e;
     k_weight_grads<TPW, BF16><<<blocks, kWgThreads, smem, s>>>(a);

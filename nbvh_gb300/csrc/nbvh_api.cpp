@@ -18,23 +18,6 @@ using namespace nbvh;
 
 namespace {
 
-struct Fail {
-    nbvh_status status;
-    std::string msg;
-};
-
-[[noreturn]] void fail(nbvh_status s, const std::string &m) { throw Fail{s, m}; }
-
-void cuda_check(cudaError_t e, const char *what)
-{
-    if (e != cudaSuccess) {
-        if (e == cudaErrorMemoryAllocation)
-            fail(NBVH_ENOMEM, std::string(what) + ": " + cudaGetErrorString(e));
-        if (e == cudaErrorTimeout)
-            fail(NBVH_ETIMEOUT, std::string(what) + ": a bounded device-side wait gave up");
-        fail(NBVH_EDEVICE, std::string(what) + ": " + cudaGetErrorString(e));
-    }
-}
 
 template <typename F>
 nbvh_status guarded(nbvh_handle *h, F &&f)
@@ -246,11 +229,6 @@ float adam_step_size(const nbvh_config &c, uint32_t step)
                    (1.0 - std::pow((double)c.optimizer.beta1, t)));
 }
 
-void require(bool cond, nbvh_status s, const char *msg)
-{
-    if (!cond)
-        fail(s, msg);
-}
 
 void upload_bvh(nbvh_handle *h)
 {
@@ -357,99 +335,22 @@ void ensure_query_workspace(nbvh_handle *h, uint32_t n, int ctx)
 {
     if (h->d_counters.count < 3u)
         cuda_check(h->d_counters.resize(3u), "alloc counters");
-    QueryContext &q = h->qctx[ctx];
-    if (q.fallback_list.count < n)
-        cuda_check(q.fallback_list.resize(n), "alloc fallback list");
-    if (q.wave_counts.count < 8u)
-        cuda_check(q.wave_counts.resize(8u), "alloc wave counters");
-    if (!q.h_words) {
-        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&q.h_words), 4u * sizeof(uint32_t), cudaHostAllocDefault),
-                   "pinned counters");
-        for (int k = 0; k < 4; k++)
-            q.h_words[k] = 0;
-    }
-    const size_t cut = h->neural_nodes.size();
-    if (q.node_bins.count < 2u * cut) {
-        cuda_check(q.node_bins.resize(2u * cut), "alloc node counts");
-        cuda_check(q.node_cursor.resize(2u * cut), "alloc node cursors");
-    }
-    const uint32_t wb = packed_weight_bytes(h->layout.n_inputs, (uint32_t)h->cfg.network.n_hidden_layers);
-    if (q.wpacked.count < wb / 2u)
-        cuda_check(q.wpacked.resize(wb / 2u), "alloc packed weights");
-    if (!q.ev)
-        cuda_check(cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming), "event");
-    if (q.capacity < n) {
-        for (int k = 0; k < 2; k++) {
-            cuda_check(q.od0[k].resize(n), "alloc wave state");
-            cuda_check(q.od1[k].resize(n), "alloc wave state");
-            cuda_check(q.nv[k].resize(n), "alloc wave state");
-            cuda_check(q.ar[k].resize(n), "alloc wave state");
-            cuda_check(q.meta[k].resize(n), "alloc wave state");
-            cuda_check(q.stack[k].resize((size_t)kNeuralStackSize * n), "alloc wave stacks");
-        }
-        cuda_check(q.features.resize((size_t)n * h->layout.n_inputs), "alloc feature rows");
-        cuda_check(q.outputs.resize((size_t)n * kOutputs), "alloc network outputs");
-        cuda_check(q.perm.resize(n), "alloc node order");
-        q.capacity = n;
-    }
+    grow_query_context(h, h->qctx[ctx], n);
 }
 
-// The neural query on device buffers with query context ctx (0: API calls, 1-2: host pipeline).
+// The neural query on the given stream with the given context's buffers (the handle's own
+// contexts or a serving slot's): closest hit, or visibility when vis_only.
 void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t depth, bool vis_only,
                   nbvh_neural_hit *d_hits, cudaStream_t s, int ctx, bool timed)
 {
     require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
     require(h->neural_built, NBVH_ESTATE, "neural cut not built");
     ensure_query_workspace(h, n, ctx);
-    QueryContext &q = h->qctx[ctx];
-    QueryCounters *counters = h->d_counters.ptr + ctx;
-    uint32_t *list = q.fallback_list.ptr;
-    cuda_check(cudaMemsetAsync(counters, 0, sizeof(QueryCounters), s), "reset counters");
-    if (h->cfg.bvh.ignore_neural_blas) {
-        // the non-neural BLAS switch: the mesh goes to the classic traversal
-        // (include/cuda/neural/neural_bvh_module_common.cuh:323)
-        if (timed)
-            cuda_check(cudaEventRecord(h->ev0, s), "event");
-        cuda_check(launch_classic_as_neural(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, vis_only,
-                                            h->classic_fast_div, s),
-                   "classic");
-        if (timed)
-            cuda_check(cudaEventRecord(h->ev1, s), "event");
-        h->last_launches = 1;
-        return;
-    }
-    const NeuralConsts nc = make_neural_consts(h, depth, vis_only);
     if (timed)
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-    WaveList lists[2];
-    for (int k = 0; k < 2; k++)
-        lists[k] = WaveList{q.od0[k].ptr, q.od1[k].ptr, q.nv[k].ptr, q.ar[k].ptr, q.meta[k].ptr, q.stack[k].ptr, q.capacity};
-    uint32_t launches = 0;
-    StepResources res;
-    res.features = q.features.ptr;
-    res.outputs = q.outputs.ptr;
-    res.wpacked = q.wpacked.ptr;
-    res.perm = q.perm.ptr;
-    res.node_bins = q.node_bins.ptr;
-    res.node_cursor = q.node_cursor.ptr;
-    res.h_words = q.h_words;
-    res.ev = q.ev;
-    cuda_check(make_feature_map(q.features.ptr, h->layout.n_inputs, q.capacity, &res.feature_map), "feature map");
-    cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),
-                                 h->any_non_neural ? h->d_non_neural.ptr : nullptr, h->d_params_h.ptr, h->grid, nc,
-                                 (uint32_t)h->cfg.network.n_hidden_layers, d_rays, n, d_hits, counters, list, lists,
-                                 q.wave_counts.ptr, res, mlp_bf16(h), h->num_sms, s, &launches),
-               "neural query");
+    h->last_launches = run_neural_query(h, h->qctx[ctx], h->d_counters.ptr + ctx, d_rays, n, depth, vis_only, d_hits, s);
     if (timed)
         cuda_check(cudaEventRecord(h->ev1, s), "event");
-    h->last_launches = launches;
-    if (h->any_non_neural || h->cfg.fallback_margin > 0.f) {
-        cuda_check(launch_classic_fallback(h->d_nodes.ptr, h->d_tris.ptr, d_rays, list, counters, n, d_hits, vis_only,
-                                           h->classic_fast_div,
-                                           h->num_sms, s),
-                   "fallback");
-        h->last_launches = launches + 1u;
-    }
     h->last_rays = n;
 }
 
@@ -1115,7 +1016,7 @@ uint32_t nbvh_training_step(const nbvh_handle *h) { return h ? h->training_step 
 
 } // extern "C"
 
-namespace {
+namespace nbvh {
 
 void camera_params(const nbvh_render_request *r, float du[3], float dv[3], float tl[3])
 {
@@ -1155,7 +1056,7 @@ void camera_params(const nbvh_render_request *r, float du[3], float dv[3], float
         tl[k] = (dir[k] - du[k] * 0.5f) - dv[k] * 0.5f;
 }
 
-} // namespace
+} // namespace nbvh
 
 extern "C" {
 
@@ -1188,6 +1089,22 @@ nbvh_status nbvh_run_inference(nbvh_handle *h, const nbvh_render_request *req, n
                    "camera rays");
         neural_query(h, rays, n, 1u, false, d_image, s, 0, true);
         cuda_check(cudaStreamSynchronize(s), "sync");
+    });
+}
+
+nbvh_status nbvh_render_path(nbvh_handle *h, const nbvh_path_request *req, float *d_image, uint64_t *rays_traced,
+                             nbvh_stream stream)
+{
+    return guarded(h, [&]() {
+        require(h->classic_built && h->neural_built, NBVH_ESTATE, "scene not built");
+        if (h->d_counters.count < 3u)
+            cuda_check(h->d_counters.resize(3u), "alloc counters");
+        require(req != nullptr, NBVH_EINVAL, "null request");
+        const uint64_t traced = render_path_core(h, h->qctx[0], h->d_counters.ptr, h->path, req, d_image,
+                                                 reinterpret_cast<cudaStream_t>(stream),
+                                                 req->camera.sample_idx * req->spp);
+        if (rays_traced)
+            *rays_traced = traced;
     });
 }
 
@@ -1457,3 +1374,181 @@ nbvh_status nbvh_host_free(void *ptr)
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Query and path-tracing cores shared with the serving loop (nbvh_server.cpp)
+// ---------------------------------------------------------------------------------------------
+
+namespace nbvh {
+
+// Grows a query context to n rays for the handle's cut and network (allocates device and pinned
+// memory; no kernel runs).
+void grow_query_context(const nbvh_handle *h, QueryContext &q, uint32_t n)
+{
+    if (q.fallback_list.count < n)
+        cuda_check(q.fallback_list.resize(n), "alloc fallback list");
+    if (q.wave_counts.count < 8u)
+        cuda_check(q.wave_counts.resize(8u), "alloc wave counters");
+    if (!q.h_words) {
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&q.h_words), 4u * sizeof(uint32_t), cudaHostAllocDefault),
+                   "pinned counters");
+        for (int k = 0; k < 4; k++)
+            q.h_words[k] = 0;
+    }
+    const size_t cut = h->neural_nodes.size();
+    if (q.node_bins.count < 2u * cut) {
+        cuda_check(q.node_bins.resize(2u * cut), "alloc node counts");
+        cuda_check(q.node_cursor.resize(2u * cut), "alloc node cursors");
+    }
+    const uint32_t wb = packed_weight_bytes(h->layout.n_inputs, (uint32_t)h->cfg.network.n_hidden_layers);
+    if (q.wpacked.count < wb / 2u)
+        cuda_check(q.wpacked.resize(wb / 2u), "alloc packed weights");
+    if (!q.ev)
+        cuda_check(cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming), "event");
+    if (q.capacity < n || q.features.count < (size_t)n * h->layout.n_inputs) {
+        for (int k = 0; k < 2; k++) {
+            cuda_check(q.od0[k].resize(n), "alloc wave state");
+            cuda_check(q.od1[k].resize(n), "alloc wave state");
+            cuda_check(q.nv[k].resize(n), "alloc wave state");
+            cuda_check(q.ar[k].resize(n), "alloc wave state");
+            cuda_check(q.meta[k].resize(n), "alloc wave state");
+            cuda_check(q.stack[k].resize((size_t)kNeuralStackSize * n), "alloc wave stacks");
+        }
+        cuda_check(q.features.resize((size_t)n * h->layout.n_inputs), "alloc feature rows");
+        cuda_check(q.outputs.resize((size_t)n * kOutputs), "alloc network outputs");
+        cuda_check(q.perm.resize(n), "alloc node order");
+        q.capacity = n;
+    }
+}
+
+// The neural query itself on explicit per-call buffers (context q, counters): reads only the
+// handle's scene, cut and parameters, so several contexts may run it at once on different
+// streams. Returns the number of kernels launched.
+uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *counters, const nbvh_ray *d_rays,
+                          uint32_t n, uint32_t depth, bool vis_only, nbvh_neural_hit *d_hits, cudaStream_t s,
+                          const StepResources *tune)
+{
+    uint32_t *list = q.fallback_list.ptr;
+    if (!tune || tune->resume_from == 0u)
+        cuda_check(cudaMemsetAsync(counters, 0, sizeof(QueryCounters), s), "reset counters");
+    if (h->cfg.bvh.ignore_neural_blas) {
+        // the non-neural BLAS switch: the mesh goes to the classic traversal
+        // (include/cuda/neural/neural_bvh_module_common.cuh:323)
+        cuda_check(launch_classic_as_neural(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, vis_only,
+                                            h->classic_fast_div, s),
+                   "classic");
+        return 1u;
+    }
+    const NeuralConsts nc = make_neural_consts(h, depth, vis_only);
+    WaveList lists[2];
+    for (int k = 0; k < 2; k++)
+        lists[k] = WaveList{q.od0[k].ptr, q.od1[k].ptr, q.nv[k].ptr, q.ar[k].ptr, q.meta[k].ptr, q.stack[k].ptr, q.capacity};
+    uint32_t launches = 0;
+    StepResources res;
+    res.features = q.features.ptr;
+    res.outputs = q.outputs.ptr;
+    res.wpacked = q.wpacked.ptr;
+    res.perm = q.perm.ptr;
+    res.node_bins = q.node_bins.ptr;
+    res.node_cursor = q.node_cursor.ptr;
+    res.h_words = q.h_words;
+    res.ev = q.ev;
+    if (tune) {
+        res.visits_per_round = tune->visits_per_round;
+        res.encode_blocks_per_sm = tune->encode_blocks_per_sm;
+        res.unchecked_steps = tune->unchecked_steps;
+        res.capture_only = tune->capture_only;
+        res.resume_from = tune->resume_from;
+    }
+    cuda_check(make_feature_map(q.features.ptr, h->layout.n_inputs, q.capacity, &res.feature_map), "feature map");
+    cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),
+                                 h->any_non_neural ? h->d_non_neural.ptr : nullptr, h->d_params_h.ptr, h->grid, nc,
+                                 (uint32_t)h->cfg.network.n_hidden_layers, d_rays, n, d_hits, counters, list, lists,
+                                 q.wave_counts.ptr, res, mlp_bf16(h), h->num_sms, s, &launches),
+               "neural query");
+    if (tune && tune->capture_only)
+        return launches; // the rest runs after the captured part is replayed
+    if (h->any_non_neural || h->cfg.fallback_margin > 0.f) {
+        cuda_check(launch_classic_fallback(h->d_nodes.ptr, h->d_tris.ptr, d_rays, list, counters, n, d_hits, vis_only,
+                                           h->classic_fast_div, h->num_sms, s),
+                   "fallback");
+        launches++;
+    }
+    return launches;
+}
+
+// Path tracing on explicit buffers (the handle's or a serving slot's): raygen, then per bounce the
+// neural query of the live paths and the shade / scatter step (one host read of the surviving
+// count per bounce), then the per-pixel mean. Returns the rays queried.
+uint64_t render_path_core(const nbvh_handle *h, QueryContext &q, QueryCounters *counters, PathBuffers &pb,
+                          const nbvh_path_request *req, float *d_image, cudaStream_t s, uint32_t sample_base)
+{
+    require(req && d_image, NBVH_EINVAL, "null request or image");
+    const nbvh_render_request &cam = req->camera;
+    require(cam.width > 0 && cam.height > 0 && req->spp > 0, NBVH_EINVAL, "empty image");
+    const uint64_t n64 = (uint64_t)cam.width * cam.height * req->spp;
+    require(n64 <= (1ull << 26), NBVH_EINVAL, "width * height * spp exceeds 2^26 paths");
+    const uint32_t n = (uint32_t)n64;
+    if (pb.thr.count < n) {
+        cuda_check(pb.thr.resize(n), "alloc path throughput");
+        cuda_check(pb.rad.resize(n), "alloc path radiance");
+        for (int k = 0; k < 2; k++) {
+            cuda_check(pb.rays[k].resize(n), "alloc path rays");
+            cuda_check(pb.ids[k].resize(n), "alloc path ids");
+        }
+        cuda_check(pb.hits.resize(n), "alloc path hits");
+    }
+    if (pb.count.count < 1u)
+        cuda_check(pb.count.resize(1u), "alloc path count");
+    if (!pb.h_count)
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&pb.h_count), sizeof(uint32_t), cudaHostAllocDefault),
+                   "pinned path count");
+    grow_query_context(h, q, n);
+    PathArgs a{};
+    camera_params(&cam, a.du, a.dv, a.tl);
+    for (int k = 0; k < 3; k++) {
+        a.origin[k] = cam.origin[k];
+        a.ground_albedo[k] = req->ground_albedo[k];
+        a.sky_zenith[k] = req->sky_zenith[k];
+        a.sky_horizon[k] = req->sky_horizon[k];
+    }
+    a.width = cam.width;
+    a.height = cam.height;
+    a.spp = req->spp;
+    a.n_paths = n;
+    a.sample_base = sample_base;
+    a.sample_offset = cam.sample_offset;
+    a.seed = req->seed;
+    a.max_bounces = req->max_bounces;
+    a.has_ground = req->has_ground ? 1u : 0u;
+    a.ground_y = req->ground_height;
+    a.thr = pb.thr.ptr;
+    a.rad = pb.rad.ptr;
+    a.rays_out = pb.rays[0].ptr;
+    a.ids_out = pb.ids[0].ptr;
+    cuda_check(launch_path_raygen(a, s), "path raygen");
+    uint32_t count = n;
+    int cur = 0;
+    uint64_t traced = 0;
+    for (uint32_t bounce = 0; count > 0 && bounce <= req->max_bounces; bounce++) {
+        run_neural_query(h, q, counters, pb.rays[cur].ptr, count, bounce == 0 ? 1u : 2u, false, pb.hits.ptr, s);
+        traced += count;
+        cuda_check(cudaMemsetAsync(pb.count.ptr, 0, sizeof(uint32_t), s), "reset path count");
+        a.rays_in = pb.rays[cur].ptr;
+        a.ids_in = pb.ids[cur].ptr;
+        a.hits = pb.hits.ptr;
+        a.rays_out = pb.rays[cur ^ 1].ptr;
+        a.ids_out = pb.ids[cur ^ 1].ptr;
+        a.count_out = pb.count.ptr;
+        cuda_check(launch_path_shade(a, count, bounce, s), "path shade");
+        cuda_check(cudaMemcpyAsync(pb.h_count, pb.count.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "count");
+        cuda_check(cudaStreamSynchronize(s), "sync");
+        count = *pb.h_count;
+        cur ^= 1;
+    }
+    cuda_check(launch_path_resolve(a, d_image, s), "path resolve");
+    cuda_check(cudaStreamSynchronize(s), "sync");
+    return traced;
+}
+
+} // namespace nbvh

@@ -13,6 +13,31 @@
 
 namespace nbvh {
 
+// Host-side errors: thrown inside the library, turned into an nbvh_status at the C ABI.
+struct Fail {
+    nbvh_status status;
+    std::string msg;
+};
+
+[[noreturn]] inline void fail(nbvh_status s, const std::string &m) { throw Fail{s, m}; }
+
+inline void require(bool cond, nbvh_status s, const char *msg)
+{
+    if (!cond)
+        fail(s, msg);
+}
+
+inline void cuda_check(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) {
+        if (e == cudaErrorMemoryAllocation)
+            fail(NBVH_ENOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+        if (e == cudaErrorTimeout)
+            fail(NBVH_ETIMEOUT, std::string(what) + ": a bounded device-side wait gave up");
+        fail(NBVH_EDEVICE, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
 constexpr uint32_t kNeuralStackSize = 24;  // NEURAL_STACK_SIZE, include/cuda/neural/accel/neural_bvh.cuh:22
 constexpr uint32_t kClassicStackSize = 32; // CudaBVH2::intersect stack, include/cuda/accel/bvh2.cuh:22
 constexpr uint32_t kNoNeuralChild = 0xFFFFFFFFu;
@@ -152,6 +177,43 @@ struct QueryContext {
     }
 };
 
+// Path tracing (k_path.cu): arguments of the raygen / shade / resolve kernels and the per-render
+// buffers (per-path throughput and radiance, ping-pong ray and path-id lists, hits, list length).
+struct PathArgs {
+    float origin[3], du[3], dv[3], tl[3];
+    uint32_t width, height, spp, n_paths, sample_base, sample_offset, seed, max_bounces;
+    uint32_t has_ground;
+    float ground_y;
+    float ground_albedo[3];
+    float sky_zenith[3], sky_horizon[3];
+    float4 *thr; // rgb throughput, rng bits in w
+    float4 *rad; // rgb radiance
+    const nbvh_ray *rays_in;
+    const uint32_t *ids_in;
+    const nbvh_neural_hit *hits;
+    nbvh_ray *rays_out;
+    uint32_t *ids_out;
+    uint32_t *count_out;
+};
+
+struct PathBuffers {
+    DeviceBuffer<float4> thr, rad;
+    DeviceBuffer<nbvh_ray> rays[2];
+    DeviceBuffer<uint32_t> ids[2];
+    DeviceBuffer<nbvh_neural_hit> hits;
+    DeviceBuffer<uint32_t> count;
+    uint32_t *h_count = nullptr;
+    ~PathBuffers()
+    {
+        if (h_count)
+            cudaFreeHost(h_count);
+    }
+};
+
+cudaError_t launch_path_raygen(const PathArgs &a, cudaStream_t s);
+cudaError_t launch_path_shade(const PathArgs &a, uint32_t count_in, uint32_t bounce, cudaStream_t s);
+cudaError_t launch_path_resolve(const PathArgs &a, float *image, cudaStream_t s);
+
 } // namespace nbvh
 
 struct nbvh_handle {
@@ -202,6 +264,9 @@ struct nbvh_handle {
     nbvh::DeviceBuffer<__half> d_train_dz;   // per row pre-activation gradients of every layer
     nbvh::DeviceBuffer<float> d_loss_sum;
 
+    // path-tracing workspace
+    nbvh::PathBuffers path;
+
     // query workspace
     nbvh::DeviceBuffer<nbvh::QueryCounters> d_counters;
     nbvh::DeviceBuffer<uint32_t> d_fallback_list;
@@ -238,6 +303,24 @@ cudaError_t launch_classic_fallback(const float4 *nodes, const float4 *tris, con
 cudaError_t launch_classic_as_neural(const float4 *nodes, const float4 *tris, const nbvh_ray *rays,
                                      uint32_t n, nbvh_neural_hit *hits, bool any_hit, bool fast_div, cudaStream_t s);
 
+// Shared memory a block may take on sm_103 (static + dynamic).
+constexpr int kMaxDynamicSmem = 227 * 1024;
+
+// Every kernel with dynamic shared memory gets the same MaxDynamicSharedMemorySize attribute: the
+// block limit minus the kernel's static shared memory. A launch then only needs its own size to
+// fit, and threads launching one kernel for models of different sizes never lower the limit under
+// each other.
+template <typename K>
+inline cudaError_t allow_max_dynamic_smem(K kernel)
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                kMaxDynamicSmem - (int)fa.sharedSizeBytes);
+}
+
 // Cuts with more nodes than this are not sorted by node between steps (the sort scans the node
 // counts in shared memory).
 constexpr uint32_t kMaxSortNodes = 8192;
@@ -262,6 +345,12 @@ struct StepResources {
     TensorMapBytes feature_map;
     uint32_t *h_words;
     cudaEvent_t ev;
+    // launch parameters (0 = default) and the graph-capture split of the step loop
+    uint32_t visits_per_round = 0;     // node visits per traversal round between lane refills
+    uint32_t encode_blocks_per_sm = 0; // blocks of 256 encoder threads per SM
+    uint32_t unchecked_steps = 0;      // steps launched before the first host check
+    bool capture_only = false;         // enqueue the unchecked steps and a counter copy, then return
+    uint32_t resume_from = 0;          // > 0: skip the first pass and continue the checked loop here
 };
 
 // Scratch of the allocation-free neural query: one static device buffer per device holding, for
@@ -317,14 +406,15 @@ cudaError_t launch_network_inference(const __half *params_h, const GridParams &g
 // 128-row tiles of FP16 inputs (row-major [rows][n_inputs], 16-byte aligned) fed by TMA through
 // the tensor map of make_feature_map. The rows processed are min(*d_count, rows) when d_count is
 // given (a length produced on the device), else rows. status receives a nonzero word if a bounded
-// wait inside the kernel gave up.
+// wait inside the kernel gave up. configure = false skips setting the kernel's shared-memory
+// attribute (during stream capture, after an earlier launch set it).
 uint32_t packed_weight_bytes(uint32_t n_inputs, uint32_t n_hidden_layers);
 cudaError_t launch_pack_weights(const __half *params_h, uint32_t n_inputs, uint32_t n_hidden_layers, __half *packed,
                                 cudaStream_t s);
 cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t rows, TensorMapBytes *out);
 cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
                           uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
-                          uint32_t *status, bool bf16, int num_sms, cudaStream_t s);
+                          uint32_t *status, bool bf16, int num_sms, cudaStream_t s, bool configure = true);
 
 cudaError_t launch_encode(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                           const float *positions, uint32_t n, float *features, cudaStream_t s);
@@ -370,5 +460,30 @@ void build_inference_nodes(const std::vector<BVHNode> &neural, float dil, std::v
 // the box-coordinate precondition of the fast slab division
 bool coords_in_fast_div_domain(const float *c, size_t n);
 bool nodes_in_fast_div_domain(const std::vector<BVHNode> &nodes);
+
+} // namespace nbvh
+
+namespace nbvh {
+
+// Grows a query context to n rays for the handle's cut and network (allocates device and pinned
+// memory; no kernel runs).
+void grow_query_context(const nbvh_handle *h, QueryContext &q, uint32_t n);
+
+// The neural query on explicit per-call buffers (context q, counters): reads only the handle's
+// scene, cut and parameters, so several contexts may run it at once on different streams.
+// `tune` (may be null) carries launch parameters and the graph-capture split of the step loop.
+// Returns the kernels launched.
+uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *counters, const nbvh_ray *d_rays,
+                          uint32_t n, uint32_t depth, bool vis_only, nbvh_neural_hit *d_hits, cudaStream_t s,
+                          const StepResources *tune = nullptr);
+
+// Path tracing on explicit buffers; returns the rays queried over all bounces. Sample k of a pixel
+// (k < req->spp) uses the camera jitter of frame sample sample_base + k (a whole frame:
+// camera.sample_idx * spp; a chunk of a frame's samples starts further in).
+uint64_t render_path_core(const nbvh_handle *h, QueryContext &q, QueryCounters *counters, PathBuffers &pb,
+                          const nbvh_path_request *req, float *d_image, cudaStream_t s, uint32_t sample_base);
+
+// Pinhole camera basis of a render request (CudaBackend::update_camera, src/cuda/cuda_backend.cpp:595-611).
+void camera_params(const nbvh_render_request *r, float du[3], float dv[3], float tl[3]);
 
 } // namespace nbvh

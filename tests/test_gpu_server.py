@@ -1,0 +1,112 @@
+"""The serving loop (nbvh_server_*) on the GPU.
+
+* Every query request's hits are bit-identical alone (the handle's own nbvh_query_closest_neural_host)
+  and in the mix: several client threads submitting uneven requests against two resident models,
+  merged into shared batches, padded to graph buckets and replayed from captured CUDA graphs,
+  including a request larger than a slot (split across batches).
+* A render request equals nbvh_render_path alone; when its samples are split across batches the
+  image equals the unsplit one up to float summation order (relative 1e-5).
+* The server reports request latency percentiles and merged batches.
+"""
+
+import threading
+
+import numpy as np
+import pytest
+
+import nbvh_gb300 as nb
+from helpers import handle
+from nbvh_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def models(built):
+    h1, s1 = handle(kind="sphere4k", seed=1, depth=6)
+    h1.run_optimisation(200)
+    h2, s2 = handle(kind="terrain32k", seed=2, depth=8)
+    h2.run_optimisation(200)
+    yield [(h1, s1), (h2, s2)]
+    h1.close()
+    h2.close()
+
+
+def _requests(models, seed=0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(24):
+        m = k % 2
+        n = int(rng.choice([1, 100, 3000, 20000, 70000]))
+        bbox = models[m][1]["bbox"]
+        out.append((m, scenes.uniform_rays(n, bbox[:3], bbox[3:], seed=1000 + k), 1 + (k % 3 == 0)))
+    # one request larger than a slot (capacity 2^16 below)
+    bbox = models[0][1]["bbox"]
+    out.append((0, scenes.uniform_rays(150000, bbox[:3], bbox[3:], seed=99), 1))
+    return out
+
+
+def test_queries_same_alone_and_in_mix(models):
+    reqs = _requests(models)
+    alone = [models[m][0].query_closest_neural_host(r, depth=d) for m, r, d in reqs]
+    srv = nb.Server(n_slots=3, hbm_budget_gb=0.2, max_batch_rays=1 << 16)
+    try:
+        ids = [srv.add_model(h) for h, _ in models]
+        assert srv.stats().slot_capacity_rays == 1 << 16
+        results = [None] * len(reqs)
+
+        def client(idx):
+            tickets = [(i, srv.submit_query(ids[reqs[i][0]], reqs[i][1], reqs[i][2])) for i in idx]
+            for i, t in tickets:
+                results[i] = srv.wait(t)
+
+        threads = [threading.Thread(target=client, args=(list(range(c, len(reqs), 4)),)) for c in range(4)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        for i, (hits, res) in enumerate(results):
+            assert res.status == 0 and res.rays_traced == len(reqs[i][1])
+            assert np.array_equal(hits.view(np.uint32), alone[i].view(np.uint32)), i
+        # a second round replays the captured graphs
+        again = [srv.wait(srv.submit_query(ids[m], r, d))[0] for m, r, d in reqs[:6]]
+        for i, hits in enumerate(again):
+            assert np.array_equal(hits.view(np.uint32), alone[i].view(np.uint32)), i
+        st = srv.stats()
+        assert st.requests_done == len(reqs) + 6
+        assert 0 < st.p50_ms <= st.p99_ms <= st.max_ms
+        assert st.batches >= 1
+        assert st.graphs_captured >= 1 and st.graph_replays >= 1
+    finally:
+        srv.close()
+
+
+def test_render_same_alone_and_split(models):
+    h, s = models[0]
+    org, tgt, up = scenes.orbit_camera(s["bbox"][:3], s["bbox"][3:], seed=9)
+    cam = nb.render_request(64, 48, org, tgt, up, 45.0, sample_idx=1, sample_offset=2)
+    req = nb.path_request(cam, spp=6, max_bounces=3, seed=4, ground_height=float(s["bbox"][1]) - 0.01)
+    alone, traced = h.render_path(req)
+    alone = alone.cpu().numpy()
+    srv = nb.Server(n_slots=2, hbm_budget_gb=0.2, max_batch_rays=1 << 16)
+    try:
+        mid = srv.add_model(h)
+        img, res = srv.wait(srv.submit_render(mid, req))
+        assert res.status == 0 and res.rays_traced == traced
+        np.testing.assert_array_equal(img, alone)
+    finally:
+        srv.close()
+    # a slot of 2^12 paths holds 1 sample of 64 x 48: six chunks, averaged on the host
+    srv = nb.Server(n_slots=2, hbm_budget_gb=0.02, max_batch_rays=1 << 12, autotune=False)
+    try:
+        mid = srv.add_model(h)
+        img, res = srv.wait(srv.submit_render(mid, req))
+        assert res.status == 0 and res.rays_traced == traced
+        np.testing.assert_allclose(img, alone, rtol=1e-5, atol=1e-6)
+    finally:
+        srv.close()
+
+
+def test_budget_too_small_is_refused(built):
+    with pytest.raises(nb.NBVHError):
+        nb.Server(n_slots=4, hbm_budget_gb=1e-4)
