@@ -12,11 +12,15 @@ judges depth / visibility.
 The same comparison is repeated on the 4,194,304-triangle sphere (key "mesh_4m"), where the
 classic traversal is deeper while the neural query still works on a 1,024-leaf cut. The tcgen05
 MLP kernel is also timed alone on 2^22 rows ("roofline_kernels.mlp_tc"), the network is trained in
-FP16 and in BF16 from the same seed and compared on held-out rays ("precision_sweep"), and the CPU
-restatements of the neural and classic queries run on the host cores ("cpu_baseline").
+FP16 and in BF16 from the same seed and compared on held-out rays ("precision_sweep"), a
+1920x1080 6-bounce hybrid path trace is timed ("path_config4"), the serving loop runs a Poisson
+load of render requests against 4 resident models, beside the same load on their classic BLAS
+("serving"), and the CPU restatements of the neural and classic queries run on the host cores
+("cpu_baseline").
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--train-steps T]
-                    [--mesh4m-train-steps T4 | -1] [--precision-sweep-steps T3 | 0] [--log2-rays R]
+                    [--mesh4m-train-steps T4 | -1] [--precision-sweep-steps T3 | 0] [--serve-seconds S | 0]
+                    [--log2-rays R]
 """
 
 import argparse
@@ -54,6 +58,9 @@ def parse():
                     help="training steps for the 4M-triangle comparison; -1 skips it")
     ap.add_argument("--precision-sweep-steps", type=int, default=5000,
                     help="training steps per precision in the FP16/BF16 sweep; 0 skips it")
+    ap.add_argument("--serve-seconds", type=float, default=3.0,
+                    help="seconds of Poisson arrivals in the serving load; 0 skips it")
+    ap.add_argument("--serve-train-steps", type=int, default=1500)
     ap.add_argument("--log2-rays", type=int, default=22,
                     help="rays per step; smaller values are for profiling captures, not bench lines")
     return ap.parse_args()
@@ -409,6 +416,7 @@ def run_ours(args):
                                           "query" % args.cpu_sample}
         line["cpu_baseline"]["classic"] = cpu_classic_baseline(h, v, f, rays_np, 1 << 18, 1 << 16)
         line["classic_config1"] = run_classic_config1(h, v, f, bbox, scenes, args.steps, args.warmup, 1 << 17)
+        line["path_config4"] = run_path_config4(h, nb, scenes, bbox)
     h.close()
     del rays, hits, chits, pin_in, pin_out
     torch.cuda.empty_cache()
@@ -417,6 +425,8 @@ def run_ours(args):
         line["mesh_4m"] = run_mesh_4m(args, nb, scenes, cfg, max_over_ranks, rank)
     if args.precision_sweep_steps > 0:
         line["precision_sweep"] = run_precision_sweep(args, nb, scenes, args.precision_sweep_steps)
+    if args.serve_seconds > 0:
+        line["serving"] = run_serving(args, nb, scenes)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
@@ -463,6 +473,103 @@ def run_classic_config1(h, v, f, bbox, scenes, steps, warmup, cpu_sample):
     return {"rays": n, "primary": len(prim), "bounce": len(bounce), "ms_per_step": ms,
             "mrays": n / (ms * 1e-3) / 1e6, "bit_exact_sample": bool(np.array_equal(got, ref)),
             "sample": len(idx), "cpu_mrays": len(idx) / cpu_s / 1e6, "cpu_threads": threads}
+
+
+def run_path_config4(h, nb, scenes, bbox, reps=3):
+    """Hybrid path tracing at 1920 x 1080, 1 sample per pixel, 6 bounces: the neural BLAS plus a
+    classic ground plane under an analytic sky (one model; instancing is not built)."""
+    org, tgt, up = scenes.orbit_camera(bbox[:3], bbox[3:], seed=12)
+    cam = nb.render_request(1920, 1080, org, tgt, up, 45.0, sample_idx=0, sample_offset=0)
+    req = nb.path_request(cam, spp=1, max_bounces=6, seed=1, ground_height=float(bbox[1]) - 0.01,
+                          ground_albedo=(0.6, 0.6, 0.6))
+    h.render_path(req)  # warm
+    ts, traced = [], 0
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        _, traced = h.render_path(req)
+        ts.append(time.perf_counter() - t0)
+    t = float(np.median(ts))
+    return {"width": 1920, "height": 1080, "spp": 1, "bounces": 6, "rays_per_frame": int(traced),
+            "ms_per_frame": t * 1e3, "mrays": traced / t / 1e6, "ground_plane": True}
+
+
+def run_serving(args, nb, scenes):
+    """Serving: 4 resident models (65K / 262K / 1M / 4M-triangle spheres, config-2 network), 64
+    open-loop clients with Poisson arrivals at 200 requests/s in total, each request a render of
+    128^2..1024^2 pixels (log-uniform side), 1-8 samples and 0-4 bounces against a random model.
+    The same load then runs with every model answered by its classic BLAS (the classic-only loop)."""
+    import threading
+    models = []
+    for subdiv in (7, 8, 9, 10):
+        cfg = nb.default_config()
+        h, v, f, _ = build_scene(nb, scenes, cfg, subdiv=subdiv)
+        h.run_optimisation(args.serve_train_steps)
+        models.append((h, h.neural_bvh()[1], len(f)))
+
+    def load(srv, ids, seconds, rate, clients, seed):
+        done, lock = [], threading.Lock()
+
+        def client(c):
+            rng = np.random.default_rng(seed * 1000 + c)
+            tickets, t_end = [], time.perf_counter() + seconds
+            t_next = time.perf_counter() + rng.exponential(clients / rate)
+            while t_next < t_end:
+                delay = t_next - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                m = int(rng.integers(len(ids)))
+                side = int(2 ** rng.uniform(7, 10))
+                bbox = models[m][1]
+                org, tgt, up = scenes.orbit_camera(bbox[:3], bbox[3:], seed=int(rng.integers(1 << 30)))
+                cam = nb.render_request(side, side, org, tgt, up, 45.0, sample_idx=int(rng.integers(1000)))
+                req = nb.path_request(cam, spp=int(rng.integers(1, 9)), max_bounces=int(rng.integers(0, 5)),
+                                      seed=int(rng.integers(1 << 20)), ground_height=float(bbox[1]) - 0.01)
+                tickets.append(srv.submit_render(ids[m], req))
+                t_next += rng.exponential(clients / rate)
+            for t in tickets:
+                _, res = srv.wait(t, timeout_ms=600000)
+                with lock:
+                    done.append((res.latency_ms, res.rays_traced))
+
+        threads = [threading.Thread(target=client, args=(c,)) for c in range(clients)]
+        t0 = time.perf_counter()
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        lat = np.array([d[0] for d in done]) if done else np.zeros(1)
+        rays = np.array([max(d[1], 1) for d in done]) if done else np.ones(1)
+        per_m = lat * 1e6 / rays                      # latency per 1M rays traced
+        near_1m = lat[(rays >= 5e5) & (rays <= 2e6)]  # requests of 0.5M..2M rays
+        return {"requests": st.requests_done, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "mean_ms": st.mean_ms,
+                "max_ms": st.max_ms, "rays_traced": st.rays_traced,
+                "mrays": st.rays_traced / st.busy_seconds / 1e6 if st.busy_seconds > 0 else None,
+                "busy_seconds": st.busy_seconds, "wall_seconds": wall, "batches": st.batches,
+                "ms_per_1m_rays_p50": float(np.percentile(per_m, 50)),
+                "ms_per_1m_rays_p99": float(np.percentile(per_m, 99)),
+                "requests_0p5_to_2m_rays": int(near_1m.size),
+                "p99_ms_requests_0p5_to_2m_rays": float(np.percentile(near_1m, 99)) if near_1m.size else None,
+                "mean_rays_per_request": float(rays.mean())}
+
+    out = {"models_triangles": [m[2] for m in models], "clients": 64, "rate_req_per_s": 200.0,
+           "seconds_of_arrivals": args.serve_seconds, "hbm_budget_gb": 150}
+    srv = nb.Server(n_slots=4, hbm_budget_gb=150.0, max_batch_rays=1 << 22)
+    try:
+        ids = [srv.add_model(m[0]) for m in models]
+        out["neural"] = load(srv, ids, args.serve_seconds, 200.0, 64, 1)
+        srv.reset_stats()
+        for m in models:
+            m[0].set_ignore_neural_blas(True)
+        out["classic_only"] = load(srv, ids, args.serve_seconds, 200.0, 64, 1)
+        for m in models:
+            m[0].set_ignore_neural_blas(False)
+    finally:
+        srv.close()
+        for m in models:
+            m[0].close()
+    return out
 
 
 def run_precision_sweep(args, nb, scenes, steps):

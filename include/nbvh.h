@@ -33,6 +33,12 @@
  *   trainer->serialize / deserialize, save/load of .nbvh        nbvh_save, nbvh_load
  *     (src/cuda/neural/neural_bvh_renderer_init.cu:385-404,
  *      src/cuda/neural/neural_bvh_renderer_accel.cpp:170-254)
+ *   tcnn FullyFusedMLP::inference (the network half)            nbvh_mlp_inference
+ *     (src/cuda/neural/neural_bvh_module.cu:232-238)
+ *   path module scatter + next traversal, Lambertian case       nbvh_render_path
+ *     (src/cuda/neural/path/path_inference_kernels.cu:224-429)
+ *   (no counterpart: one model per process)                     nbvh_server_* serving loop,
+ *                                                               nbvh_query_closest_neural_noalloc
  *
  * Conventions.
  *  - Every call returns an nbvh_status; nothing throws or exits across this boundary. The
