@@ -1385,6 +1385,10 @@ namespace nbvh {
 // memory; no kernel runs).
 void grow_query_context(const nbvh_handle *h, QueryContext &q, uint32_t n)
 {
+    // record every device buffer's address: a capture of this context holds them
+    const void *before[12] = {q.fallback_list.ptr, q.wave_counts.ptr, q.node_bins.ptr, q.node_cursor.ptr,
+                              q.wpacked.ptr,       q.od0[0].ptr,       q.stack[0].ptr,  q.stack[1].ptr,
+                              q.features.ptr,      q.outputs.ptr,      q.perm.ptr,      q.meta[1].ptr};
     if (q.fallback_list.count < n)
         cuda_check(q.fallback_list.resize(n), "alloc fallback list");
     if (q.wave_counts.count < 8u)
@@ -1419,6 +1423,11 @@ void grow_query_context(const nbvh_handle *h, QueryContext &q, uint32_t n)
         cuda_check(q.perm.resize(n), "alloc node order");
         q.capacity = n;
     }
+    const void *after[12] = {q.fallback_list.ptr, q.wave_counts.ptr, q.node_bins.ptr, q.node_cursor.ptr,
+                             q.wpacked.ptr,       q.od0[0].ptr,       q.stack[0].ptr,  q.stack[1].ptr,
+                             q.features.ptr,      q.outputs.ptr,      q.perm.ptr,      q.meta[1].ptr};
+    if (std::memcmp(before, after, sizeof(before)) != 0)
+        q.generation++;
 }
 
 // The neural query itself on explicit per-call buffers (context q, counters): reads only the
@@ -1481,7 +1490,8 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
 // neural query of the live paths and the shade / scatter step (one host read of the surviving
 // count per bounce), then the per-pixel mean. Returns the rays queried.
 uint64_t render_path_core(const nbvh_handle *h, QueryContext &q, QueryCounters *counters, PathBuffers &pb,
-                          const nbvh_path_request *req, float *d_image, cudaStream_t s, uint32_t sample_base)
+                          const nbvh_path_request *req, float *d_image, cudaStream_t s, uint32_t sample_base,
+                          PathQuery *query)
 {
     require(req && d_image, NBVH_EINVAL, "null request or image");
     const nbvh_render_request &cam = req->camera;
@@ -1531,12 +1541,16 @@ uint64_t render_path_core(const nbvh_handle *h, QueryContext &q, QueryCounters *
     int cur = 0;
     uint64_t traced = 0;
     for (uint32_t bounce = 0; count > 0 && bounce <= req->max_bounces; bounce++) {
-        run_neural_query(h, q, counters, pb.rays[cur].ptr, count, bounce == 0 ? 1u : 2u, false, pb.hits.ptr, s);
+        const nbvh_neural_hit *hits = pb.hits.ptr;
+        if (query)
+            hits = (*query)(pb.rays[cur].ptr, count, bounce == 0 ? 1u : 2u);
+        else
+            run_neural_query(h, q, counters, pb.rays[cur].ptr, count, bounce == 0 ? 1u : 2u, false, pb.hits.ptr, s);
         traced += count;
         cuda_check(cudaMemsetAsync(pb.count.ptr, 0, sizeof(uint32_t), s), "reset path count");
         a.rays_in = pb.rays[cur].ptr;
         a.ids_in = pb.ids[cur].ptr;
-        a.hits = pb.hits.ptr;
+        a.hits = hits;
         a.rays_out = pb.rays[cur ^ 1].ptr;
         a.ids_out = pb.ids[cur ^ 1].ptr;
         a.count_out = pb.count.ptr;

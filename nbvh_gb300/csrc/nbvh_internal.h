@@ -166,6 +166,7 @@ struct QueryContext {
     DeviceBuffer<uint32_t> perm;                   // [capacity]
     DeviceBuffer<uint32_t> node_bins, node_cursor; // [2][cut nodes]
     uint32_t capacity = 0;
+    uint64_t generation = 0;     // incremented whenever a buffer is reallocated
     uint32_t *h_words = nullptr; // 4 pinned words
     cudaEvent_t ev = nullptr;
     ~QueryContext()
@@ -477,11 +478,20 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
                           uint32_t n, uint32_t depth, bool vis_only, nbvh_neural_hit *d_hits, cudaStream_t s,
                           const StepResources *tune = nullptr);
 
+// Neural query used by the path tracer for one bounce: answers n rays at `rays` with closest-hit
+// depth `depth` on the stream and returns where the hits are.
+struct PathQuery {
+    virtual const nbvh_neural_hit *operator()(const nbvh_ray *rays, uint32_t n, uint32_t depth) = 0;
+    virtual ~PathQuery() = default;
+};
+
 // Path tracing on explicit buffers; returns the rays queried over all bounces. Sample k of a pixel
 // (k < req->spp) uses the camera jitter of frame sample sample_base + k (a whole frame:
-// camera.sample_idx * spp; a chunk of a frame's samples starts further in).
+// camera.sample_idx * spp; a chunk of a frame's samples starts further in). `query` (may be null)
+// replaces the direct neural query of each bounce (the serving loop's graph replays).
 uint64_t render_path_core(const nbvh_handle *h, QueryContext &q, QueryCounters *counters, PathBuffers &pb,
-                          const nbvh_path_request *req, float *d_image, cudaStream_t s, uint32_t sample_base);
+                          const nbvh_path_request *req, float *d_image, cudaStream_t s, uint32_t sample_base,
+                          PathQuery *query = nullptr);
 
 // Pinhole camera basis of a render request (CudaBackend::update_camera, src/cuda/cuda_backend.cpp:595-611).
 void camera_params(const nbvh_render_request *r, float du[3], float dv[3], float tl[3]);

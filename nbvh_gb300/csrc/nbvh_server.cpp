@@ -155,63 +155,74 @@ nbvh_status server_guarded(nbvh_server *s, F &&f)
     }
 }
 
-// Runs the neural query of a padded batch on the slot: the captured graph for (model, bucket,
-// depth) when graphs are on (captured at first use), then the host-checked remainder.
+bool graphable(const nbvh_server *srv, const nbvh_handle *h)
+{
+    return srv->cfg.use_graphs && !h->cfg.bvh.ignore_neural_blas && !h->any_non_neural && h->cfg.fallback_margin <= 0.f;
+}
+
+StepResources tuning_of(const Model &m, uint32_t bucket)
+{
+    StepResources t;
+    auto it = m.tune.find(bucket);
+    if (it != m.tune.end()) {
+        t.visits_per_round = it->second.visits;
+        t.encode_blocks_per_sm = it->second.encode_blocks;
+    }
+    return t;
+}
+
+// Captures (once) the graph of a padded batch of `bucket` rays in the slot's buffers: the first-leaf
+// pass and the first kGraphSteps steps, ending with a copy of the wave counters to the host. Nothing
+// runs; the kernels' attributes must have been set by an earlier direct query. A shape whose
+// capture fails is recorded without a graph and keeps running directly.
+cudaGraphExec_t ensure_graph(nbvh_server *srv, Slot &sl, uint32_t model_id, uint32_t bucket, uint32_t depth)
+{
+    const GraphKey key{model_id, bucket, depth};
+    auto g = sl.graphs.find(key);
+    if (g != sl.graphs.end())
+        return g->second;
+    const Model &m = srv->models[model_id];
+    StepResources cap = tuning_of(m, bucket);
+    cap.unchecked_steps = kGraphSteps;
+    cap.capture_only = true;
+    cudaGraphExec_t exec = nullptr;
+    if (cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+        bool ok = true;
+        try {
+            run_neural_query(m.h, sl.q, sl.counters.ptr, sl.rays.ptr, bucket, depth, false, sl.hits.ptr, sl.stream, &cap);
+        } catch (...) {
+            ok = false;
+        }
+        cudaGraph_t graph = nullptr;
+        ok = cudaStreamEndCapture(sl.stream, &graph) == cudaSuccess && ok && graph != nullptr;
+        if (ok && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+            exec = nullptr;
+        if (graph)
+            cudaGraphDestroy(graph);
+    }
+    cudaGetLastError(); // a failed capture leaves no sticky error; clear the last one
+    sl.graphs.emplace(key, exec);
+    if (exec) {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        srv->graphs_captured++;
+    }
+    return exec;
+}
+
+// Runs the neural query of a batch of n rays already in the slot's ray buffer: padded to its
+// bucket, the captured graph replayed (when graphs are on), then the host-checked remainder.
 void slot_query(nbvh_server *srv, Slot &sl, uint32_t model_id, uint32_t n, uint32_t depth)
 {
-    Model &m = srv->models[model_id];
+    const Model &m = srv->models[model_id];
     const uint32_t bucket = std::min(bucket_of(n), sl.capacity);
     if (bucket > n) // pad the batch with rays that miss everything
         cuda_check(cudaMemcpyAsync(sl.rays.ptr + n, srv->dead, (size_t)(bucket - n) * sizeof(nbvh_ray),
                                    cudaMemcpyDeviceToDevice, sl.stream),
                    "pad batch");
-    StepResources tune;
-    auto it = m.tune.find(bucket);
-    if (it != m.tune.end()) {
-        tune.visits_per_round = it->second.visits;
-        tune.encode_blocks_per_sm = it->second.encode_blocks;
-    }
+    const StepResources tune = tuning_of(m, bucket);
     const nbvh_handle *h = m.h;
-    const bool graphable = srv->cfg.use_graphs && !h->cfg.bvh.ignore_neural_blas && !h->any_non_neural &&
-                           h->cfg.fallback_margin <= 0.f;
-    if (!graphable) {
-        run_neural_query(h, sl.q, sl.counters.ptr, sl.rays.ptr, bucket, depth, false, sl.hits.ptr, sl.stream, &tune);
-        return;
-    }
-    const GraphKey key{model_id, bucket, depth};
-    auto g = sl.graphs.find(key);
-    if (g == sl.graphs.end()) {
-        // one direct run first: it answers this batch and leaves every kernel attribute set
-        run_neural_query(h, sl.q, sl.counters.ptr, sl.rays.ptr, bucket, depth, false, sl.hits.ptr, sl.stream, &tune);
-        StepResources cap = tune;
-        cap.unchecked_steps = kGraphSteps;
-        cap.capture_only = true;
-        // capture; if the capture cannot be made, this shape keeps running without a graph
-        cudaGraphExec_t exec = nullptr;
-        if (cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
-            bool ok = true;
-            try {
-                run_neural_query(h, sl.q, sl.counters.ptr, sl.rays.ptr, bucket, depth, false, sl.hits.ptr, sl.stream,
-                                 &cap);
-            } catch (...) {
-                ok = false;
-            }
-            cudaGraph_t graph = nullptr;
-            ok = cudaStreamEndCapture(sl.stream, &graph) == cudaSuccess && ok && graph != nullptr;
-            if (ok && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
-                exec = nullptr;
-            if (graph)
-                cudaGraphDestroy(graph);
-        }
-        cudaGetLastError(); // a failed capture leaves no sticky error; clear the last one
-        sl.graphs.emplace(key, exec);
-        if (exec) {
-            std::lock_guard<std::mutex> lock(srv->mu);
-            srv->graphs_captured++;
-        }
-        return; // answered by the direct run above; later batches of this shape replay the graph
-    }
-    if (!g->second) { // no graph for this shape
+    cudaGraphExec_t exec = graphable(srv, h) ? ensure_graph(srv, sl, model_id, bucket, depth) : nullptr;
+    if (!exec) {
         run_neural_query(h, sl.q, sl.counters.ptr, sl.rays.ptr, bucket, depth, false, sl.hits.ptr, sl.stream, &tune);
         return;
     }
@@ -219,7 +230,7 @@ void slot_query(nbvh_server *srv, Slot &sl, uint32_t model_id, uint32_t n, uint3
         std::lock_guard<std::mutex> lock(srv->mu);
         srv->graph_replays++;
     }
-    cuda_check(cudaGraphLaunch(g->second, sl.stream), "graph launch");
+    cuda_check(cudaGraphLaunch(exec, sl.stream), "graph launch");
     cuda_check(cudaStreamSynchronize(sl.stream), "graph sync");
     if (sl.q.h_words[3] != 0u)
         fail(NBVH_ETIMEOUT, "tensor-core MLP: a bounded wait gave up");
@@ -229,6 +240,23 @@ void slot_query(nbvh_server *srv, Slot &sl, uint32_t model_id, uint32_t n, uint3
     rest.resume_from = kGraphSteps;
     run_neural_query(h, sl.q, sl.counters.ptr, sl.rays.ptr, bucket, depth, false, sl.hits.ptr, sl.stream, &rest);
 }
+
+// The path tracer's per-bounce query on a slot: the bounce's rays are copied into the slot's ray
+// buffer and answered like a query batch (bucket, graph), the hits read from the slot's hit buffer.
+struct SlotPathQuery : PathQuery {
+    nbvh_server *srv;
+    Slot *sl;
+    uint32_t model;
+    SlotPathQuery(nbvh_server *s, Slot *l, uint32_t m) : srv(s), sl(l), model(m) {}
+    const nbvh_neural_hit *operator()(const nbvh_ray *rays, uint32_t n, uint32_t depth) override
+    {
+        cuda_check(cudaMemcpyAsync(sl->rays.ptr, rays, (size_t)n * sizeof(nbvh_ray), cudaMemcpyDeviceToDevice,
+                                   sl->stream),
+                   "bounce rays");
+        slot_query(srv, *sl, model, n, depth);
+        return sl->hits.ptr;
+    }
+};
 
 void complete(nbvh_server *srv, const Work &w, nbvh_status st, uint64_t traced)
 {
@@ -286,9 +314,10 @@ void run_batch(nbvh_server *srv, Slot &sl, std::vector<Work> &batch)
             // samples [offset, offset + count) of the frame: the same paths the whole frame would trace
             pr.spp = w.count;
             const uint32_t px = pr.camera.width * pr.camera.height;
+            SlotPathQuery pq(srv, &sl, q0.model);
             const uint64_t traced =
                 render_path_core(srv->models[q0.model].h, sl.q, sl.counters.ptr, sl.path, &pr, sl.image.ptr, sl.stream,
-                                 q0.render.camera.sample_idx * q0.render.spp + w.offset);
+                                 q0.render.camera.sample_idx * q0.render.spp + w.offset, &pq);
             if (w.r->chunks == 1u) { // the whole frame: its image as it is
                 cuda_check(cudaMemcpy(q0.h_image, sl.image.ptr, (size_t)px * 4u * sizeof(float), cudaMemcpyDeviceToHost),
                            "image out");
@@ -493,11 +522,32 @@ nbvh_status nbvh_server_add_model(nbvh_server *srv, nbvh_handle *h, uint32_t *mo
         m.h = h;
         srv->models.push_back(m);
         const uint32_t id = (uint32_t)srv->models.size() - 1u;
-        // size every slot's query context for this model now, so serving never allocates
-        for (auto &sl : srv->slots)
+        // size every slot's query context for this model now, so serving never allocates; a context
+        // whose buffers moved drops its captured graphs (they hold the old addresses)
+        for (auto &sl : srv->slots) {
+            const uint64_t gen = sl->q.generation;
             grow_query_context(h, sl->q, sl->capacity);
-        if (srv->cfg.autotune)
+            if (sl->q.generation != gen) {
+                for (auto &g : sl->graphs)
+                    if (g.second)
+                        cudaGraphExecDestroy(g.second);
+                sl->graphs.clear();
+            }
+        }
+        if (srv->cfg.autotune) {
             autotune(srv, id);
+        } else { // one direct query sets the kernels' attributes before any capture
+            Slot &s0 = *srv->slots[0];
+            cuda_check(cudaMemcpy(s0.rays.ptr, srv->dead, kMinBucket * sizeof(nbvh_ray), cudaMemcpyDeviceToDevice),
+                       "warm rays");
+            run_neural_query(h, s0.q, s0.counters.ptr, s0.rays.ptr, kMinBucket, 1u, false, s0.hits.ptr, s0.stream);
+        }
+        // capture every slot's graphs for this model now, so the first requests do not pay for it
+        if (graphable(srv, h))
+            for (auto &sl : srv->slots)
+                for (uint32_t b = kMinBucket; b <= sl->capacity; b <<= 1)
+                    for (uint32_t depth = 1; depth <= 2; depth++)
+                        ensure_graph(srv, *sl, id, b, depth);
         *model_id = id;
     });
 }
