@@ -30,9 +30,10 @@
  *     (src/cuda/neural/neural_bvh_renderer.cu:141-288)
  *   NeuralBVHRenderer::render, m_run_inference branch           nbvh_run_inference
  *     (src/cuda/neural/neural_bvh_renderer.cu:299-379)
- *   trainer->serialize / deserialize, save/load of .nbvh        nbvh_save, nbvh_load
- *     (src/cuda/neural/neural_bvh_renderer_init.cu:385-404,
- *      src/cuda/neural/neural_bvh_renderer_accel.cpp:170-254)
+ *   trainer->serialize / deserialize (own checkpoint format)    nbvh_save, nbvh_load
+ *     (src/cuda/neural/neural_bvh_renderer_init.cu:385-404)
+ *   save_neural_bvh / load_neural_bvh (.nbvh neural cut)        nbvh_export_neural_cut,
+ *     (src/cuda/neural/neural_bvh_renderer_accel.cpp:170-254)   nbvh_import_neural_cut
  *   tcnn FullyFusedMLP::inference (the network half)            nbvh_mlp_inference
  *     (src/cuda/neural/neural_bvh_module.cu:232-238)
  *   path module scatter + next traversal, Lambertian case       nbvh_render_path
@@ -276,6 +277,18 @@ nbvh_status nbvh_get_classic_bvh(const nbvh_handle *h, uint32_t *h_nodes, uint32
 nbvh_status nbvh_build_neural_cut(nbvh_handle *h, uint32_t max_depth);
 nbvh_status nbvh_get_neural_bvh(const nbvh_handle *h, uint32_t *h_nodes, uint32_t *n_nodes,
                                 float *h_scene_bbox /* 6 floats: min, max */);
+
+/* The reference's .nbvh neural-cut file (NeuralBVHRenderer::save_neural_bvh / load_neural_bvh,
+ * src/cuda/neural/neural_bvh_renderer_accel.cpp:170-254; written through the madmann91/bvh v2
+ * serializer): u64 node count, u64 1, per node 40 bytes {f32 min.x, max.x, min.y, max.y, min.z,
+ * max.z, u64 first_id, u64 prim_count}, u64 0. Import replaces the handle's neural cut (the
+ * classic BVH must be built: it gives the scene box); files that fail the size, header or tree
+ * checks return NBVH_EIO. The host forms read / write 8 words per node in the nbvh_get_neural_bvh
+ * layout (h_nodes NULL: count only; *n_nodes is the capacity on input). */
+nbvh_status nbvh_import_neural_cut(nbvh_handle *h, const char *path);
+nbvh_status nbvh_export_neural_cut(nbvh_handle *h, const char *path);
+nbvh_status nbvh_read_nbvh_host(const char *path, uint32_t *h_nodes, uint32_t *n_nodes);
+nbvh_status nbvh_write_nbvh_host(const char *path, const uint32_t *h_nodes, uint32_t n_nodes);
 
 /* Marks neural leaves whose queries are answered by the classic BLAS (flag != 0). */
 nbvh_status nbvh_set_non_neural_leaves(nbvh_handle *h, const uint32_t *h_node_ids, uint32_t n,

@@ -192,6 +192,22 @@ def build_neural_cut_host(nodes, max_depth):
     return out[: n.value].copy()
 
 
+def read_nbvh(path):
+    """Neural-cut nodes (uint32 [n, 8]) of a reference .nbvh file (no device needed)."""
+    lib = load_library()
+    n = C.c_uint32(0)
+    _check(lib.nbvh_read_nbvh_host(str(path).encode(), None, C.byref(n)), None)
+    nodes = np.empty((n.value, 8), np.uint32)
+    _check(lib.nbvh_read_nbvh_host(str(path).encode(), _ptr(nodes), C.byref(n)), None)
+    return nodes
+
+
+def write_nbvh(path, nodes):
+    """Writes neural-cut nodes (uint32 [n, 8]) as a reference .nbvh file."""
+    nodes = np.ascontiguousarray(nodes, np.uint32)
+    _check(load_library().nbvh_write_nbvh_host(str(path).encode(), _ptr(nodes), len(nodes)), None)
+
+
 def nodes_to_float(nodes):
     """Bounding boxes of uint32 [n, 8] node records: (min [n,3], max [n,3]) float32."""
     f = nodes.view(np.float32)
@@ -405,6 +421,12 @@ class NBVH:
         img = torch.empty((req.width * req.height, 12), dtype=torch.int32, device=torch.device("cuda", self.device))
         self._check(self.lib.nbvh_run_inference(self.h, C.byref(req), _ptr(img), _stream(stream)))
         return img
+
+    def import_neural_cut(self, path):
+        self._check(self.lib.nbvh_import_neural_cut(self.h, str(path).encode()))
+
+    def export_neural_cut(self, path):
+        self._check(self.lib.nbvh_export_neural_cut(self.h, str(path).encode()))
 
     def render_path(self, req, stream=None):
         """Path-traced RGBA image (float32 [height * width, 4] on the device) and the rays traced."""

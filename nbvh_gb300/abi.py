@@ -163,6 +163,10 @@ PROTOTYPES = {
     "nbvh_run_inference": (ST, [P, C.POINTER(RenderRequest), P, P]),
     "nbvh_camera_rays": (ST, [P, C.POINTER(RenderRequest), P, P]),
     "nbvh_render_path": (ST, [P, C.POINTER(PathRequest), P, C.POINTER(C.c_uint64), P]),
+    "nbvh_import_neural_cut": (ST, [P, C.c_char_p]),
+    "nbvh_export_neural_cut": (ST, [P, C.c_char_p]),
+    "nbvh_read_nbvh_host": (ST, [C.c_char_p, P, C.POINTER(C.c_uint32)]),
+    "nbvh_write_nbvh_host": (ST, [C.c_char_p, P, C.c_uint32]),
     "nbvh_server_config_default": (ST, [C.POINTER(ServerConfig)]),
     "nbvh_server_create": (ST, [C.POINTER(ServerConfig), C.c_int, C.POINTER(C.c_void_p)]),
     "nbvh_server_add_model": (ST, [P, P, C.POINTER(C.c_uint32)]),

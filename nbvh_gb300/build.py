@@ -22,6 +22,7 @@ SOURCES = [
     "k_query.cu",
     "nbvh_api.cpp",
     "nbvh_server.cpp",
+    "nbvh_format.cpp",
     "bvh_builder.cpp",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -605,6 +605,33 @@ nbvh_status nbvh_get_classic_bvh(const nbvh_handle *hc, uint32_t *h_nodes, uint3
     });
 }
 
+nbvh_status nbvh_import_neural_cut(nbvh_handle *h, const char *path)
+{
+    return guarded(h, [&]() {
+        require(path != nullptr, NBVH_EINVAL, "null path");
+        require(h->classic_built, NBVH_ESTATE, "classic BVH not built (it gives the neural scene box)");
+        std::vector<BVHNode> nodes;
+        std::string err;
+        if (!read_nbvh(path, nodes, err))
+            fail(NBVH_EIO, err);
+        h->neural_nodes = std::move(nodes);
+        upload_neural(h);
+        h->neural_built = true;
+        cuda_check(cudaDeviceSynchronize(), "sync");
+    });
+}
+
+nbvh_status nbvh_export_neural_cut(nbvh_handle *h, const char *path)
+{
+    return guarded(h, [&]() {
+        require(path != nullptr, NBVH_EINVAL, "null path");
+        require(h->neural_built, NBVH_ESTATE, "neural cut not built");
+        std::string err;
+        if (!write_nbvh(path, h->neural_nodes, err))
+            fail(NBVH_EIO, err);
+    });
+}
+
 nbvh_status nbvh_build_neural_cut(nbvh_handle *h, uint32_t max_depth)
 {
     return guarded(h, [&]() {

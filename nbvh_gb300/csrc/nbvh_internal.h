@@ -497,3 +497,12 @@ uint64_t render_path_core(const nbvh_handle *h, QueryContext &q, QueryCounters *
 void camera_params(const nbvh_render_request *r, float du[3], float dv[3], float tl[3]);
 
 } // namespace nbvh
+
+namespace nbvh {
+
+// The reference's .nbvh neural-cut file (nbvh_format.cpp): read (with structural validation) and write.
+bool validate_cut(const std::vector<BVHNode> &nodes, std::string &err);
+bool read_nbvh(const std::string &path, std::vector<BVHNode> &nodes, std::string &err);
+bool write_nbvh(const std::string &path, const std::vector<BVHNode> &nodes, std::string &err);
+
+} // namespace nbvh
