@@ -34,6 +34,10 @@
  *     (src/cuda/neural/neural_bvh_renderer_init.cu:385-404)
  *   save_neural_bvh / load_neural_bvh (.nbvh neural cut)        nbvh_export_neural_cut,
  *     (src/cuda/neural/neural_bvh_renderer_accel.cpp:170-254)   nbvh_import_neural_cut
+ *   tree-cut learning, BvhSplitScheduler, split / LoD steps      nbvh_begin_tree_cut,
+ *     (src/cuda/neural/neural_bvh_renderer.cu:196-282,           nbvh_get_tree_cut_info,
+ *      include/cuda/neural/utils/bvh_split_scheduler.h:13-145,   nbvh_split_schedule_host
+ *      src/cuda/neural/neural_bvh_renderer_accel.cpp:256-441)
  *   tcnn FullyFusedMLP::inference (the network half)            nbvh_mlp_inference
  *     (src/cuda/neural/neural_bvh_module.cu:232-238)
  *   path module scatter + next traversal, Lambertian case       nbvh_render_path
@@ -413,6 +417,75 @@ typedef struct nbvh_train_stats {
  * (sample generation -> fused forward/loss/backward -> Adam). Synchronous; stats may be NULL. */
 nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_stats *stats);
 uint32_t nbvh_training_step(const nbvh_handle *h);
+
+/* ---------------------------------------------------------------------------------------------
+ * Learned tree cut (tree_cut_learning of NeuralBVHRenderer::render, neural_bvh_renderer.cu:196-282;
+ * BvhSplitScheduler, include/cuda/neural/utils/bvh_split_scheduler.h:13-145; node survival,
+ * neural_bvh_module_kernels.cu:184-199; split_neural_bvh_at / assign_lod_to_current_neural_leaf_nodes,
+ * neural_bvh_renderer_accel.cpp:256-441)
+ * ------------------------------------------------------------------------------------------- */
+
+typedef struct nbvh_tree_cut_options {
+    int32_t tree_cut_learning;        /* split leaves on the schedule below (m_tree_cut_learning) */
+    int32_t splitting_interval;       /* bvh_split_scheduler: 50 */
+    int32_t last_split_iteration;     /* 2000 */
+    int32_t start_split_num;          /* 1 */
+    float split_scaling;              /* 2 */
+    float split_interval_scaling;     /* 2 */
+    int32_t num_lods_learned;         /* bvh_constants.num_lods_learned: 1, at most 7 */
+    int32_t lod_decision_type;        /* 0 EqualIterations, 1 EqualSplits */
+    int32_t training_node_survival;   /* bvh_constants: 1 */
+    float survival_probability_scale; /* 1 */
+    float min_rr_survival_prob;       /* 0.005 */
+    uint32_t reserved[5];
+} nbvh_tree_cut_options;
+
+typedef struct nbvh_tree_cut_info {
+    uint32_t active;              /* a tree-cut session exists on the handle */
+    uint32_t learning;            /* splits still scheduled */
+    uint32_t n_nodes;
+    uint32_t capacity;            /* classic node count: a cut never holds more */
+    uint32_t iteration;           /* training steps since nbvh_begin_tree_cut */
+    uint32_t current_learned_lod;
+    uint32_t total_splits;
+    uint32_t max_depth;
+    uint32_t expected_nodes;      /* the scheduler's node count after last_split_iteration */
+    float max_node_loss;          /* heuristic maximum the next step's node survival uses */
+    uint32_t n_lod_nodes[7];      /* n_bvh_lod_nodes: node count when each LoD was assigned */
+    uint32_t reserved[3];
+} nbvh_tree_cut_info;
+
+/* The reference defaults (tree_cut_learning and training_node_survival on). */
+nbvh_status nbvh_tree_cut_options_default(nbvh_tree_cut_options *o);
+
+/* The split schedule alone (BvhSplitScheduler::update_stats_and_reset): splits requested at each
+ * of n_iterations steps, capped by the leaves of the growing cut (h_splits may be NULL), and the
+ * node count reached from start_nodes. No device needed. */
+nbvh_status nbvh_split_schedule_host(const nbvh_tree_cut_options *o, uint32_t start_nodes, uint32_t n_iterations,
+                                     uint32_t *h_splits, uint32_t *expected_nodes);
+
+/* Starts a tree-cut session: the cut is rebuilt at start_depth (m_neural_bvh_min_depth, 0 = the
+ * root alone) with its leaves at the coarsest LoD, per-node statistics are reset, and every later
+ * nbvh_run_optimisation step also accounts each sample's loss to its node, applies node survival
+ * to the sampler and, while learning, splits the leaves with the largest loss heuristic on the
+ * schedule (and assigns LoDs when num_lods_learned > 1). The session ends when the cut is replaced
+ * (nbvh_build_neural_cut, nbvh_import_neural_cut, nbvh_load, a new mesh). */
+nbvh_status nbvh_begin_tree_cut(nbvh_handle *h, const nbvh_tree_cut_options *o, uint32_t start_depth);
+nbvh_status nbvh_get_tree_cut_info(nbvh_handle *h, nbvh_tree_cut_info *info);
+
+/* The session's device state: nodes (8 words each), statistics (4 words each: f32 loss,
+ * iter_alive, depth, samples) and the classic node of each neural node; any pointer may be NULL;
+ * *n_nodes is the capacity on input and the node count on output. */
+nbvh_status nbvh_get_tree_cut(nbvh_handle *h, uint32_t *h_nodes, uint32_t *h_stats, uint32_t *h_node_map,
+                              uint32_t *n_nodes);
+/* Replaces the per-node statistics (n_nodes must be the session's node count), e.g. to resume. */
+nbvh_status nbvh_set_tree_cut_stats(nbvh_handle *h, const uint32_t *h_stats, uint32_t n_nodes);
+
+/* The batch of the last nbvh_run_optimisation step (host copies; any pointer may be NULL):
+ * positions n x points x 3, targets n x 8, sampled node per sample, and per sample the sum of its
+ * output channels' loss values (tcnn's L matrix summed over channels, already divided by n_total). */
+nbvh_status nbvh_get_training_batch(nbvh_handle *h, float *h_positions, float *h_targets, uint32_t *h_nodes,
+                                    float *h_sample_loss, uint32_t n);
 
 /* run-inference: renders one frame of primary rays from a pinhole camera (camera_raygen,
  * include/cuda/neural/neural_bvh_renderer_kernels.cuh:74-79; CudaBackend::update_camera,

@@ -192,6 +192,26 @@ def build_neural_cut_host(nodes, max_depth):
     return out[: n.value].copy()
 
 
+def tree_cut_options(**kw):
+    """nbvh_tree_cut_options with the reference defaults, fields overridden by keyword."""
+    o = abi.TreeCutOptions()
+    _check(load_library().nbvh_tree_cut_options_default(C.byref(o)), None)
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise AttributeError(k)
+        setattr(o, k, v)
+    return o
+
+
+def split_schedule(options, start_nodes, n_iterations):
+    """Splits per iteration (capped by the leaves) and the node count reached (no device needed)."""
+    splits = np.zeros(max(n_iterations, 1), np.uint32)
+    nodes = C.c_uint32(0)
+    _check(load_library().nbvh_split_schedule_host(C.byref(options), start_nodes, n_iterations, _ptr(splits),
+                                                   C.byref(nodes)), None)
+    return splits[:n_iterations], nodes.value
+
+
 def read_nbvh(path):
     """Neural-cut nodes (uint32 [n, 8]) of a reference .nbvh file (no device needed)."""
     lib = load_library()
@@ -421,6 +441,40 @@ class NBVH:
         img = torch.empty((req.width * req.height, 12), dtype=torch.int32, device=torch.device("cuda", self.device))
         self._check(self.lib.nbvh_run_inference(self.h, C.byref(req), _ptr(img), _stream(stream)))
         return img
+
+    def begin_tree_cut(self, options=None, start_depth=0):
+        options = options if options is not None else tree_cut_options()
+        self._check(self.lib.nbvh_begin_tree_cut(self.h, C.byref(options), start_depth))
+
+    def tree_cut_info(self):
+        info = abi.TreeCutInfo()
+        self._check(self.lib.nbvh_get_tree_cut_info(self.h, C.byref(info)))
+        return info
+
+    def tree_cut(self):
+        """(nodes uint32 [n, 8], stats uint32 [n, 4], node_map uint32 [n]) of the session."""
+        n = C.c_uint32(0)
+        self._check(self.lib.nbvh_get_tree_cut(self.h, None, None, None, C.byref(n)))
+        nodes = np.empty((n.value, 8), np.uint32)
+        stats = np.empty((n.value, 4), np.uint32)
+        nmap = np.empty(n.value, np.uint32)
+        self._check(self.lib.nbvh_get_tree_cut(self.h, _ptr(nodes), _ptr(stats), _ptr(nmap), C.byref(n)))
+        return nodes, stats, nmap
+
+    def set_tree_cut_stats(self, stats):
+        st = np.ascontiguousarray(stats, np.uint32).reshape(-1, 4)
+        self._check(self.lib.nbvh_set_tree_cut_stats(self.h, _ptr(st), len(st)))
+
+    def training_batch(self, n=None):
+        """(positions, targets, nodes, sample_loss) of the last run_optimisation step."""
+        n = self.cfg.batch_size if n is None else n
+        P = self.cfg.module.input_segment_points
+        pos = np.empty((n, P, 3), np.float32)
+        tgt = np.empty((n, 8), np.float32)
+        nodes = np.empty(n, np.uint32)
+        loss = np.empty(n, np.float32)
+        self._check(self.lib.nbvh_get_training_batch(self.h, _ptr(pos), _ptr(tgt), _ptr(nodes), _ptr(loss), n))
+        return pos, tgt, nodes, loss
 
     def import_neural_cut(self, path):
         self._check(self.lib.nbvh_import_neural_cut(self.h, str(path).encode()))

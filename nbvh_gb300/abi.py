@@ -79,6 +79,22 @@ class TrainStats(C.Structure):
                 ("mean_loss", C.c_float), ("learning_rate", C.c_float), ("ms_per_step", C.c_float)]
 
 
+class TreeCutOptions(C.Structure):
+    _fields_ = [("tree_cut_learning", C.c_int32), ("splitting_interval", C.c_int32),
+                ("last_split_iteration", C.c_int32), ("start_split_num", C.c_int32), ("split_scaling", C.c_float),
+                ("split_interval_scaling", C.c_float), ("num_lods_learned", C.c_int32),
+                ("lod_decision_type", C.c_int32), ("training_node_survival", C.c_int32),
+                ("survival_probability_scale", C.c_float), ("min_rr_survival_prob", C.c_float),
+                ("reserved", C.c_uint32 * 5)]
+
+
+class TreeCutInfo(C.Structure):
+    _fields_ = [("active", C.c_uint32), ("learning", C.c_uint32), ("n_nodes", C.c_uint32), ("capacity", C.c_uint32),
+                ("iteration", C.c_uint32), ("current_learned_lod", C.c_uint32), ("total_splits", C.c_uint32),
+                ("max_depth", C.c_uint32), ("expected_nodes", C.c_uint32), ("max_node_loss", C.c_float),
+                ("n_lod_nodes", C.c_uint32 * 7), ("reserved", C.c_uint32 * 3)]
+
+
 class RenderRequest(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("sample_idx", C.c_uint32),
                 ("sample_offset", C.c_uint32), ("origin", C.c_float * 3), ("target", C.c_float * 3),
@@ -159,6 +175,13 @@ PROTOTYPES = {
     "nbvh_adam_step": (ST, [P, P, P]),
     "nbvh_generate_training_batch": (ST, [P, U32, U32, P, P, P, P]),
     "nbvh_run_optimisation": (ST, [P, U32, C.POINTER(TrainStats)]),
+    "nbvh_tree_cut_options_default": (ST, [C.POINTER(TreeCutOptions)]),
+    "nbvh_split_schedule_host": (ST, [C.POINTER(TreeCutOptions), U32, U32, P, C.POINTER(C.c_uint32)]),
+    "nbvh_begin_tree_cut": (ST, [P, C.POINTER(TreeCutOptions), U32]),
+    "nbvh_get_tree_cut_info": (ST, [P, C.POINTER(TreeCutInfo)]),
+    "nbvh_get_tree_cut": (ST, [P, P, P, P, C.POINTER(C.c_uint32)]),
+    "nbvh_set_tree_cut_stats": (ST, [P, P, U32]),
+    "nbvh_get_training_batch": (ST, [P, P, P, P, P, U32]),
     "nbvh_training_step": (U32, [P]),
     "nbvh_run_inference": (ST, [P, C.POINTER(RenderRequest), P, P]),
     "nbvh_camera_rays": (ST, [P, C.POINTER(RenderRequest), P, P]),

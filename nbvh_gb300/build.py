@@ -23,6 +23,8 @@ SOURCES = [
     "nbvh_api.cpp",
     "nbvh_server.cpp",
     "nbvh_format.cpp",
+    "nbvh_tree_cut.cpp",
+    "k_tree_cut.cu",
     "bvh_builder.cpp",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

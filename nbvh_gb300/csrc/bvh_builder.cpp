@@ -233,10 +233,15 @@ bool build_bvh2(const std::vector<float> &vertices, const std::vector<uint32_t> 
 // traverse_and_build_neural_bvh, src/cuda/neural/neural_bvh_renderer_accel.cpp:25-88: copy the
 // classic BVH down to max_depth; leaves become LEAF_FINAL (1) when they are classic leaves and
 // LEAF_LOD(6) (= 8, the coarsest LoD, assigned first when building the cut) otherwise.
-void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std::vector<BVHNode> &neural)
+void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std::vector<BVHNode> &neural,
+                      std::vector<uint32_t> *node_map, std::vector<uint32_t> *depth)
 {
-    constexpr uint32_t kLeafFinal = 1u, kLeafLod6 = 8u;
+    constexpr uint32_t kLeafLod6 = kLeafLodBase + kNumBvhLods - 1u;
     neural.assign(1, BVHNode{});
+    if (node_map)
+        node_map->assign(1, 0u);
+    if (depth)
+        depth->assign(1, 0u);
     struct Task {
         uint32_t bvh_idx, neural_idx, depth;
     };
@@ -249,6 +254,10 @@ void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std
         stack.pop_back();
         const BVHNode &src = nodes[t.bvh_idx];
         BVHNode &dst = neural[t.neural_idx];
+        if (node_map)
+            (*node_map)[t.neural_idx] = t.bvh_idx;
+        if (depth)
+            (*depth)[t.neural_idx] = t.depth;
         std::memcpy(dst.min, src.min, sizeof(dst.min));
         std::memcpy(dst.max, src.max, sizeof(dst.max));
         if (src.prim_count > 0u || t.depth == max_depth) {
@@ -259,6 +268,10 @@ void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std
         const uint32_t left = (uint32_t)neural.size();
         neural.push_back(BVHNode{});
         neural.push_back(BVHNode{});
+        if (node_map)
+            node_map->resize(neural.size(), 0u);
+        if (depth)
+            depth->resize(neural.size(), 0u);
         BVHNode &d2 = neural[t.neural_idx];
         d2.prim_count = 0u;
         d2.left_or_prim_offset = left;
@@ -317,7 +330,9 @@ void build_inference_nodes(const std::vector<BVHNode> &neural, float dil, std::v
     for (size_t ii = n; ii-- > 0;) {
         float *b = &bounds[8u * ii];
         const BVHNode &d = dilated[ii];
-        const bool leaf = neural[ii].prim_count > 0u || neural[ii].left_or_prim_offset == kNoNeuralChild;
+        // a leaf at the rendered LoD (0): a final or LoD-0 leaf, or a node without a neural child
+        const uint32_t pc = neural[ii].prim_count;
+        const bool leaf = (pc > 0u && pc <= kLeafLodBase) || neural[ii].left_or_prim_offset == kNoNeuralChild;
         if (leaf) {
             for (int k = 0; k < 3; k++) {
                 b[k] = d.min[k];

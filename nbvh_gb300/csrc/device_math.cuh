@@ -613,4 +613,14 @@ __device__ __forceinline__ float decode_local_t(float out_depth, float mint, flo
     return depth;
 }
 
+// NeuralTreeCutData::compute_loss_heuristic (include/cuda/neural/neural_bvh_renderer.h:36-47):
+// loss / (iter_alive * sqrt(samples / iter_alive)), -FLT_MAX for a node without samples.
+__device__ __forceinline__ float tree_cut_heuristic(float loss, uint32_t iter_alive, uint32_t samples)
+{
+    if (samples == 0u)
+        return -FLT_MAX;
+    const float alive = __uint2float_rn(iter_alive);
+    return __fdiv_rn(loss, __fmul_rn(alive, __fsqrt_rn(__fdiv_rn(__uint2float_rn(samples), alive))));
+}
+
 } // namespace nbvh

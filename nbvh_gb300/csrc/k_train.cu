@@ -36,6 +36,8 @@ struct SampleArgs {
     uint32_t training_step;
     uint32_t batch_size;
     uint32_t n;
+    uint32_t learned_lod;
+    NodeSurvival survival;
 };
 
 __device__ __forceinline__ V3 cube_pos_on_face(int face, float u, float v) // sampling.cuh:85-94
@@ -62,7 +64,10 @@ __global__ void __launch_bounds__(128) k_training_samples(const __grid_constant_
     const float sx = lcg_randomf(rng);
     const float sy = lcg_randomf(rng);
     const V3 dir = uniform_sphere(sx, sy);
-    (void)lcg_randomf(rng); // sampled LoD (one learned LoD for a fixed cut)
+    // sampled LoD among the ones learned so far (common.cuh:719-721)
+    const uint32_t n_lods = kNumBvhLods - a.learned_lod;
+    const uint32_t lod_pick = __float2uint_rz(__fmul_rn(lcg_randomf(rng), __uint2float_rn(n_lods)));
+    const uint32_t sampled_lod = a.learned_lod + min(lod_pick, n_lods - 1u);
     const float dil = __fadd_rn(c.fixed_node_dilation, __fmul_rn(lcg_randomf(rng), c.node_extent_dilation));
     uint32_t stack[kNeuralStackSize];
     int sp = 0;
@@ -83,7 +88,7 @@ __global__ void __launch_bounds__(128) k_training_samples(const __grid_constant_
             o = add3(mul3(ps, sub3(smax, smin)), smin);
             d = dir;
         }
-        int res = neural_intersect(a.neural_nodes, c.bvh_lod, o, d, stack, sp, false, c.inference_mint_epsilon,
+        int res = neural_intersect(a.neural_nodes, sampled_lod, o, d, stack, sp, false, c.inference_mint_epsilon,
                                    c.inference_maxt_epsilon, c.learning_mint_epsilon, c.learning_maxt_epsilon, FLT_MAX,
                                    dil, mint, maxt, node);
         valid = (res == 1);
@@ -117,6 +122,18 @@ __global__ void __launch_bounds__(128) k_training_samples(const __grid_constant_
     }
     if (a.sample_nodes)
         a.sample_nodes[i] = node;
+    if (a.survival.enabled) {
+        // node survival (neural_bvh_module_kernels.cu:184-199): a rejected sample leaves its slot's
+        // previous input and target in place; its node index is already written
+        const uint4 st = reinterpret_cast<const uint4 *>(a.survival.stats)[node];
+        const float estimate = tree_cut_heuristic(__uint_as_float(st.x), st.y, st.w);
+        const float cur_max = a.survival.max_word ? __uint_as_float(*a.survival.max_word) : 0.0f;
+        float kept = fmaxf(a.survival.min_prob, __fdiv_rn(estimate, cur_max));
+        if (!(estimate <= cur_max))
+            kept = 1.0f;
+        if (__fmul_rn(a.survival.scale, kept) < lcg_randomf(rng))
+            return;
+    }
 
     // encoded segment points (neural_bvh_module_kernels.cu:10-97)
     const float dilation = __fadd_rn(__fadd_rn(1.0f, c.node_extent_dilation), c.fixed_node_dilation);
@@ -282,6 +299,7 @@ struct TrainArgs {
     __half *dz;        // n x dz_stride
     float2 *grid_grad; // n_grid_entries
     float *loss_sum;
+    float *sample_loss; // per row: sum of its output channels' loss values (may be NULL)
     uint32_t n_hidden_layers;
     uint32_t n;
 };
@@ -401,7 +419,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
             }
         }
         // ---------------- loss ----------------
-        float dzo[4];
+        float dzo[4], row_vals[4];
 #pragma unroll
         for (int e = 0; e < 4; e++) {
             const uint32_t row = (e < 2) ? r0 : r1;
@@ -416,7 +434,21 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
                 gr = Pr::round(gr); // 16-bit output gradient
             }
             loss_acc += value;
+            row_vals[e] = value;
             dzo[e] = gr * y * (1.0f - y); // sigmoid backward
+        }
+        if (a.sample_loss) { // the four lanes of a quad hold the eight channels of rows r0 and r1
+            float l0 = row_vals[0] + row_vals[1], l1 = row_vals[2] + row_vals[3];
+            l0 += __shfl_xor_sync(kFull, l0, 1);
+            l1 += __shfl_xor_sync(kFull, l1, 1);
+            l0 += __shfl_xor_sync(kFull, l0, 2);
+            l1 += __shfl_xor_sync(kFull, l1, 2);
+            if (tig == 0) {
+                if (act0)
+                    a.sample_loss[r0] = l0;
+                if (act1)
+                    a.sample_loss[r1] = l1;
+            }
         }
         // dz_out (cols 0..7; 8..15 stay zero)
         {
@@ -730,7 +762,8 @@ __global__ void k_scale(float *__restrict__ p, size_t n, float s)
 cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *nodes, const float4 *tris,
                                     const float *albedo, const NeuralConsts &nc, const GridParams &grid,
                                     uint32_t training_step, uint32_t batch_size, uint32_t n, float *positions,
-                                    float *targets, uint32_t *sample_nodes, cudaStream_t s)
+                                    float *targets, uint32_t *sample_nodes, uint32_t learned_lod,
+                                    const NodeSurvival *survival, cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
@@ -747,6 +780,11 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
     a.training_step = training_step;
     a.batch_size = batch_size;
     a.n = n;
+    a.learned_lod = learned_lod < kNumBvhLods ? learned_lod : kNumBvhLods - 1u;
+    if (survival && survival->enabled && survival->stats)
+        a.survival = *survival;
+    else
+        a.survival = NodeSurvival{nullptr, nullptr, 1.0f, 0.0f, 0u};
     k_training_samples<<<(n + 127u) / 128u, 128, 0, s>>>(a);
     return cudaGetLastError();
 }
@@ -754,7 +792,7 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
 cudaError_t launch_train_forward_backward(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                                           const LossConsts &lc, const float *positions, const float *targets,
                                           uint32_t n, __half *acts, __half *dz, float *grad, float *loss_sum,
-                                          bool bf16, int num_sms, cudaStream_t s)
+                                          float *sample_loss, bool bf16, int num_sms, cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
@@ -771,6 +809,7 @@ cudaError_t launch_train_forward_backward(const __half *params_h, const GridPara
     a.dz = dz;
     a.grid_grad = reinterpret_cast<float2 *>(grad + n_network_params);
     a.loss_sum = loss_sum;
+    a.sample_loss = sample_loss;
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
     const size_t smem = sizeof(GridParams) + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half);

@@ -232,6 +232,7 @@ float adam_step_size(const nbvh_config &c, uint32_t step)
 
 void upload_bvh(nbvh_handle *h)
 {
+    h->model_version++;
     // nodes: two float4 per node in the reference layout
     h->classic_fast_div = nodes_in_fast_div_domain(h->nodes);
     cuda_check(h->d_nodes.resize(2u * h->nodes.size()), "alloc nodes");
@@ -273,10 +274,19 @@ void upload_bvh(nbvh_handle *h)
 
 void upload_neural(nbvh_handle *h)
 {
+    end_tree_cut(h);
     cuda_check(h->d_neural_nodes.resize(2u * h->neural_nodes.size()), "alloc neural nodes");
     cuda_check(cudaMemcpy(h->d_neural_nodes.ptr, h->neural_nodes.data(), h->neural_nodes.size() * sizeof(BVHNode),
                           cudaMemcpyHostToDevice),
                "upload neural nodes");
+    upload_inference_nodes(h);
+}
+
+} // namespace
+
+void nbvh::upload_inference_nodes(nbvh_handle *h)
+{
+    h->model_version++;
     std::vector<BVHNode> dilated;
     std::vector<float> bounds;
     build_inference_nodes(h->neural_nodes, h->cfg.bvh.fixed_node_dilation, dilated, bounds);
@@ -292,6 +302,8 @@ void upload_neural(nbvh_handle *h)
     h->any_non_neural = false;
     h->d_non_neural.release();
 }
+
+namespace {
 
 // The MLP runs in BF16 (else FP16); its matrices are the first n_network_params parameters.
 bool mlp_bf16(const nbvh_handle *h) { return h->cfg.network.precision == NBVH_PRECISION_BF16; }
@@ -317,12 +329,24 @@ void upload_params(nbvh_handle *h, const float *params, bool reset_adam)
 void ensure_train_workspace(nbvh_handle *h, uint32_t n)
 {
     const uint32_t P = h->grid.n_points, ni = h->layout.n_inputs, H = (uint32_t)h->cfg.network.n_hidden_layers;
-    if (h->d_train_pos.count < (size_t)n * P * 3u)
+    // zero-filled on allocation: a sample that node survival rejects keeps its slot's previous
+    // content, which for the first step is this zero fill
+    if (h->d_train_pos.count < (size_t)n * P * 3u) {
         cuda_check(h->d_train_pos.resize((size_t)n * P * 3u), "alloc train positions");
-    if (h->d_train_tgt.count < (size_t)n * 8u)
+        cuda_check(cudaMemset(h->d_train_pos.ptr, 0, h->d_train_pos.count * sizeof(float)), "zero positions");
+    }
+    if (h->d_train_tgt.count < (size_t)n * 8u) {
         cuda_check(h->d_train_tgt.resize((size_t)n * 8u), "alloc train targets");
-    if (h->d_train_nodes.count < n)
+        cuda_check(cudaMemset(h->d_train_tgt.ptr, 0, h->d_train_tgt.count * sizeof(float)), "zero targets");
+    }
+    if (h->d_train_nodes.count < n) {
         cuda_check(h->d_train_nodes.resize(n), "alloc train nodes");
+        cuda_check(cudaMemset(h->d_train_nodes.ptr, 0, h->d_train_nodes.count * sizeof(uint32_t)), "zero nodes");
+    }
+    if (h->d_train_loss.count < n) {
+        cuda_check(h->d_train_loss.resize(n), "alloc sample losses");
+        cuda_check(cudaMemset(h->d_train_loss.ptr, 0, h->d_train_loss.count * sizeof(float)), "zero losses");
+    }
     if (h->d_train_acts.count < (size_t)n * (ni + H * kNeurons))
         cuda_check(h->d_train_acts.resize((size_t)n * (ni + H * kNeurons)), "alloc activations");
     if (h->d_train_dz.count < (size_t)n * (H * kNeurons + kOutputsPadded))
@@ -567,6 +591,7 @@ nbvh_status nbvh_set_mesh(nbvh_handle *h, const float *v, uint32_t nv, const uin
             h->albedo.clear();
         h->classic_built = false;
         h->neural_built = false;
+        end_tree_cut(h);
     });
 }
 
@@ -577,6 +602,7 @@ nbvh_status nbvh_build_classic(nbvh_handle *h)
         std::string err;
         if (!build_bvh2(h->vertices, h->indices, h->nodes, h->prim_indices, err))
             fail(NBVH_EINVAL, err);
+        end_tree_cut(h);
         upload_bvh(h);
         for (int k = 0; k < 3; k++) {
             h->scene_min[k] = h->nodes[0].min[k];
@@ -629,6 +655,102 @@ nbvh_status nbvh_export_neural_cut(nbvh_handle *h, const char *path)
         std::string err;
         if (!write_nbvh(path, h->neural_nodes, err))
             fail(NBVH_EIO, err);
+    });
+}
+
+nbvh_status nbvh_begin_tree_cut(nbvh_handle *h, const nbvh_tree_cut_options *o, uint32_t start_depth)
+{
+    return guarded(h, [&]() {
+        require(o != nullptr, NBVH_EINVAL, "null options");
+        begin_tree_cut(h, *o, start_depth);
+    });
+}
+
+nbvh_status nbvh_get_tree_cut_info(nbvh_handle *h, nbvh_tree_cut_info *info)
+{
+    return guarded(h, [&]() {
+        require(info != nullptr, NBVH_EINVAL, "null info");
+        std::memset(info, 0, sizeof(*info));
+        const TreeCutSession &c = h->cut;
+        if (!c.active)
+            return;
+        uint32_t words[kCutWords + kNumBvhLods];
+        tree_cut_words(h, words, h->pipe_stream[0]);
+        const uint32_t it = h->training_step - c.start_step;
+        info->active = 1u;
+        info->learning = c.learning ? 1u : 0u;
+        info->n_nodes = words[kCutCount];
+        info->capacity = c.capacity;
+        info->iteration = it;
+        info->current_learned_lod = c.current_lod;
+        info->total_splits = words[kCutSplits];
+        info->max_depth = words[kCutMaxDepth];
+        info->expected_nodes = c.expected_nodes;
+        const uint32_t max_bits = (it == 0 || c.zero_next_max) ? 0u : words[kCutMax0 + ((it - 1u) & 1u)];
+        std::memcpy(&info->max_node_loss, &max_bits, 4);
+        for (uint32_t l = 0; l < kNumBvhLods; l++)
+            info->n_lod_nodes[l] = words[kCutWords + l];
+    });
+}
+
+nbvh_status nbvh_get_tree_cut(nbvh_handle *h, uint32_t *h_nodes, uint32_t *h_stats, uint32_t *h_node_map,
+                              uint32_t *n_nodes)
+{
+    return guarded(h, [&]() {
+        require(n_nodes != nullptr, NBVH_EINVAL, "null count");
+        require(h->cut.active, NBVH_ESTATE, "no tree-cut session");
+        uint32_t words[kCutWords + kNumBvhLods];
+        tree_cut_words(h, words, h->pipe_stream[0]);
+        const uint32_t n = words[kCutCount];
+        if (h_nodes || h_stats || h_node_map)
+            require(*n_nodes >= n, NBVH_EINVAL, "buffers smaller than the cut");
+        if (h_nodes)
+            cuda_check(cudaMemcpy(h_nodes, h->d_neural_nodes.ptr, (size_t)n * sizeof(BVHNode), cudaMemcpyDeviceToHost),
+                       "download nodes");
+        if (h_stats)
+            cuda_check(cudaMemcpy(h_stats, h->cut.d_stats.ptr, (size_t)n * 16u, cudaMemcpyDeviceToHost),
+                       "download stats");
+        if (h_node_map)
+            cuda_check(cudaMemcpy(h_node_map, h->cut.d_map.ptr, (size_t)n * 4u, cudaMemcpyDeviceToHost),
+                       "download node map");
+        *n_nodes = n;
+    });
+}
+
+nbvh_status nbvh_set_tree_cut_stats(nbvh_handle *h, const uint32_t *h_stats, uint32_t n_nodes)
+{
+    return guarded(h, [&]() {
+        require(h_stats != nullptr, NBVH_EINVAL, "null stats");
+        require(h->cut.active, NBVH_ESTATE, "no tree-cut session");
+        uint32_t words[kCutWords + kNumBvhLods];
+        tree_cut_words(h, words, h->pipe_stream[0]);
+        require(n_nodes == words[kCutCount], NBVH_EINVAL, "stats count differs from the cut's node count");
+        cuda_check(cudaMemcpy(h->cut.d_stats.ptr, h_stats, (size_t)n_nodes * 16u, cudaMemcpyHostToDevice),
+                   "upload stats");
+    });
+}
+
+nbvh_status nbvh_get_training_batch(nbvh_handle *h, float *h_positions, float *h_targets, uint32_t *h_nodes,
+                                    float *h_sample_loss, uint32_t n)
+{
+    return guarded(h, [&]() {
+        require(n <= h->d_train_nodes.count && n <= h->d_train_loss.count, NBVH_ESTATE,
+                "no training batch of that size");
+        const size_t P = h->grid.n_points;
+        cuda_check(cudaDeviceSynchronize(), "sync");
+        if (h_positions)
+            cuda_check(cudaMemcpy(h_positions, h->d_train_pos.ptr, (size_t)n * P * 3u * sizeof(float),
+                                  cudaMemcpyDeviceToHost),
+                       "download positions");
+        if (h_targets)
+            cuda_check(cudaMemcpy(h_targets, h->d_train_tgt.ptr, (size_t)n * 8u * sizeof(float), cudaMemcpyDeviceToHost),
+                       "download targets");
+        if (h_nodes)
+            cuda_check(cudaMemcpy(h_nodes, h->d_train_nodes.ptr, (size_t)n * 4u, cudaMemcpyDeviceToHost),
+                       "download nodes");
+        if (h_sample_loss)
+            cuda_check(cudaMemcpy(h_sample_loss, h->d_train_loss.ptr, (size_t)n * 4u, cudaMemcpyDeviceToHost),
+                       "download losses");
     });
 }
 
@@ -922,7 +1044,7 @@ void gradients_into_workspace(nbvh_handle *h, const float *d_pos, const float *d
     cuda_check(cudaMemsetAsync(h->d_grad.ptr, 0, (size_t)h->layout.n_params * sizeof(float), s), "zero grad");
     cuda_check(launch_train_forward_backward(h->d_params_h.ptr, h->grid, H, make_loss_consts(h->cfg, n), d_pos, d_tgt, n,
                                              h->d_train_acts.ptr, h->d_train_dz.ptr, h->d_grad.ptr, loss_slot,
-                                             mlp_bf16(h), h->num_sms, s),
+                                             h->d_train_loss.ptr, mlp_bf16(h), h->num_sms, s),
                "forward/backward");
     cuda_check(launch_weight_gradients(h->grid, H, h->d_train_acts.ptr, h->d_train_dz.ptr, n, h->d_grad.ptr,
                                        mlp_bf16(h), h->num_sms, s),
@@ -978,8 +1100,8 @@ nbvh_status nbvh_generate_training_batch(nbvh_handle *h, uint32_t training_step,
         const NeuralConsts nc = make_neural_consts(h, 1u, false);
         cuda_check(launch_training_samples(h->d_neural_nodes.ptr, h->d_nodes.ptr, h->d_tris.ptr,
                                            h->albedo.empty() ? nullptr : h->d_albedo.ptr, nc, h->grid, training_step,
-                                           h->cfg.batch_size, n, d_positions, d_targets, d_nodes,
-                                           reinterpret_cast<cudaStream_t>(stream)),
+                                           h->cfg.batch_size, n, d_positions, d_targets, d_nodes, kNumBvhLods - 1u,
+                                           nullptr, reinterpret_cast<cudaStream_t>(stream)),
                    "training samples");
         h->last_launches = 1;
     });
@@ -1001,10 +1123,14 @@ nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_sta
         float lr_t = 0.f;
         cuda_check(cudaEventRecord(h->ev0, s), "event");
         for (uint32_t i = 0; i < steps; i++) {
+            NodeSurvival survival{nullptr, nullptr, 1.0f, 0.0f, 0u};
+            uint32_t learned_lod = kNumBvhLods - 1u; // build_and_upload_neural_bvh starts at the coarsest LoD
+            if (h->cut.active)
+                tree_cut_before_step(h, survival, learned_lod);
             cuda_check(launch_training_samples(h->d_neural_nodes.ptr, h->d_nodes.ptr, h->d_tris.ptr,
                                                h->albedo.empty() ? nullptr : h->d_albedo.ptr, nc, h->grid,
                                                h->training_step, n, n, h->d_train_pos.ptr, h->d_train_tgt.ptr,
-                                               h->d_train_nodes.ptr, s),
+                                               h->d_train_nodes.ptr, learned_lod, &survival, s),
                        "training samples");
             gradients_into_workspace(h, h->d_train_pos.ptr, h->d_train_tgt.ptr, n, s, h->d_loss_sum.ptr + i);
             lr_t = adam_step_size(c, h->training_step);
@@ -1012,9 +1138,13 @@ nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_sta
                                    h->layout.n_params, lr_t, c.optimizer.beta1, c.optimizer.beta2, c.optimizer.epsilon,
                                    c.optimizer.l2_reg, 1.0f / c.optimizer.loss_scale, n_bf16_params(h), s),
                        "adam");
+            if (h->cut.active)
+                tree_cut_after_step(h, h->d_train_loss.ptr, n, s);
             h->training_step++;
         }
         cuda_check(cudaEventRecord(h->ev1, s), "event");
+        if (h->cut.active)
+            tree_cut_sync(h, s);
         std::vector<float> losses(steps > 0 ? steps : 1u);
         if (steps > 0)
             cuda_check(cudaMemcpyAsync(losses.data(), h->d_loss_sum.ptr, steps * sizeof(float), cudaMemcpyDeviceToHost, s),

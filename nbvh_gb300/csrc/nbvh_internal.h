@@ -41,6 +41,11 @@ inline void cuda_check(cudaError_t e, const char *what)
 constexpr uint32_t kNeuralStackSize = 24;  // NEURAL_STACK_SIZE, include/cuda/neural/accel/neural_bvh.cuh:22
 constexpr uint32_t kClassicStackSize = 32; // CudaBVH2::intersect stack, include/cuda/accel/bvh2.cuh:22
 constexpr uint32_t kNoNeuralChild = 0xFFFFFFFFu;
+// NeuralBVH2Node leaf kinds (include/cuda/neural/accel/neural_bvh2.cuh:14-30): prim_count 1 is a
+// final leaf (a classic leaf), 2 + l a leaf of LoD l (l in [0, 7), 0 the finest).
+constexpr uint32_t kLeafFinal = 1u;
+constexpr uint32_t kLeafLodBase = 2u;
+constexpr uint32_t kNumBvhLods = 7u;
 constexpr uint32_t kMaxLevels = 32;
 constexpr uint32_t kMaxPoints = 16;
 constexpr uint32_t kOutputs = 8;      // visibility, depth, normal(3), albedo(3)
@@ -217,6 +222,44 @@ cudaError_t launch_path_resolve(const PathArgs &a, float *image, cudaStream_t s)
 
 } // namespace nbvh
 
+namespace nbvh {
+
+// BvhSplitScheduler (include/cuda/neural/utils/bvh_split_scheduler.h:13-145)
+struct SplitScheduler {
+    int splitting_interval = 50, last_split_iteration = 2000, start_split_num = 1;
+    float split_scaling = 2.0f, split_interval_scaling = 2.0f;
+    int lod_decision_type = 0;
+    int total_splits = 0; // expected over the whole schedule (m_stats.total_splits)
+    int current_num_splits = 1, current_splitting_interval = 50, current_total_splits = 0;
+    void configure(const nbvh_tree_cut_options &o);
+    void reset();
+    int get_bvh_splits(int iteration);
+    // update_stats_and_reset: node count after n_iterations; graph (may be NULL) gets the splits
+    // of each iteration capped by the leaves
+    uint32_t expected(uint32_t start_nodes, uint32_t n_iterations, uint32_t *graph);
+    bool should_assign_new_lod(int iteration, int current_lod, int num_lods_learned, int max_lods) const;
+};
+
+// A handle's learned-tree-cut session: the device holds nodes (in the handle's neural node array,
+// sized for the whole classic BVH), per-node statistics, the neural -> classic node map and the
+// TreeCutWord words; the host keeps the schedule.
+struct TreeCutSession {
+    bool active = false;
+    bool learning = false;
+    bool dirty = false;         // the device cut changed since the host copy was refreshed
+    bool all_assigned = false;
+    bool zero_next_max = false;
+    nbvh_tree_cut_options opt{};
+    SplitScheduler sched;
+    uint32_t start_step = 0;
+    uint32_t capacity = 0;
+    uint32_t current_lod = 6;
+    uint32_t expected_nodes = 0;
+    DeviceBuffer<uint32_t> d_stats, d_map, d_keys, d_words;
+};
+
+} // namespace nbvh
+
 struct nbvh_handle {
     std::mutex mu;
     std::string last_error;
@@ -263,7 +306,10 @@ struct nbvh_handle {
     nbvh::DeviceBuffer<uint32_t> d_train_nodes;
     nbvh::DeviceBuffer<__half> d_train_acts; // per row activations of every layer input
     nbvh::DeviceBuffer<__half> d_train_dz;   // per row pre-activation gradients of every layer
+    nbvh::DeviceBuffer<float> d_train_loss;  // per row loss (sum over output channels)
     nbvh::DeviceBuffer<float> d_loss_sum;
+    nbvh::TreeCutSession cut;
+    uint64_t model_version = 0; // bumped whenever a device array that queries read is reallocated
 
     // path-tracing workspace
     nbvh::PathBuffers path;
@@ -420,20 +466,60 @@ cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpack
 cudaError_t launch_encode(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                           const float *positions, uint32_t n, float *features, cudaStream_t s);
 
+// words of the device state: node count, the heuristic maximum of the two most recent steps (bits of
+// a non-negative float), the deepest node, splits done, an error flag (capacity exceeded)
+enum TreeCutWord : uint32_t {
+    kCutCount = 0,
+    kCutMax0 = 1,
+    kCutMax1 = 2,
+    kCutMaxDepth = 3,
+    kCutSplits = 4,
+    kCutError = 5,
+    kCutWords = 8
+};
+
+struct TreeCutArgs {
+    float4 *nodes;          // neural nodes, 2 float4 each, `capacity` of them
+    const float4 *classic;  // classic nodes
+    uint32_t *stats;        // 4 words per node: f32 loss, iter_alive, depth, samples
+    uint32_t *node_map;     // neural node -> classic node
+    uint32_t *keys;         // scratch, one word per node
+    uint32_t *words;        // TreeCutWord
+    uint32_t capacity;
+};
+
+// Node survival of the training sampler: stats / max_word NULL (or disabled) keeps every sample.
+struct NodeSurvival {
+    const uint32_t *stats;
+    const uint32_t *max_word; // heuristic maximum of the previous step; NULL reads as 0
+    float scale;
+    float min_prob;
+    uint32_t enabled;
+};
+
 cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *nodes, const float4 *tris,
                                     const float *albedo, const NeuralConsts &nc, const GridParams &grid,
                                     uint32_t training_step, uint32_t batch_size, uint32_t n, float *positions,
-                                    float *targets, uint32_t *sample_nodes, cudaStream_t s);
+                                    float *targets, uint32_t *sample_nodes, uint32_t learned_lod,
+                                    const NodeSurvival *survival, cudaStream_t s);
 
 // forward + loss + backward: writes per-row activations / gradients for the weight-gradient pass,
 // scatters the grid gradient into grad + n_network_params, accumulates the loss sum.
 cudaError_t launch_train_forward_backward(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                                           const LossConsts &lc, const float *positions, const float *targets,
                                           uint32_t n, __half *acts, __half *dz, float *grad,
-                                          float *loss_sum, bool bf16, int num_sms, cudaStream_t s);
+                                          float *loss_sum, float *sample_loss, bool bf16, int num_sms,
+                                          cudaStream_t s);
 
 cudaError_t launch_weight_gradients(const GridParams &grid, uint32_t n_hidden_layers, const __half *acts,
                                     const __half *dz, uint32_t n, float *grad, bool bf16, int num_sms, cudaStream_t s);
+
+// ---- learned tree cut (k_tree_cut.cu) ----
+cudaError_t launch_cut_accumulate(const float *sample_loss, const uint32_t *sample_nodes, uint32_t n, uint32_t dims,
+                                  uint32_t *stats, cudaStream_t s);
+cudaError_t launch_cut_alive_max(const TreeCutArgs &a, uint32_t slot, int num_sms, cudaStream_t s);
+cudaError_t launch_cut_split(const TreeCutArgs &a, uint32_t k, uint32_t lod, cudaStream_t s);
+cudaError_t launch_cut_assign_lod(const TreeCutArgs &a, uint32_t lod, int num_sms, cudaStream_t s);
 
 cudaError_t launch_scale(float *data, size_t n, float scale, cudaStream_t s);
 
@@ -454,7 +540,8 @@ cudaError_t launch_camera_rays(uint32_t width, uint32_t height, uint32_t sample_
 // when the tree depth exceeds the traversal stack.
 bool build_bvh2(const std::vector<float> &vertices, const std::vector<uint32_t> &indices,
                 std::vector<BVHNode> &nodes, std::vector<uint32_t> &prim_indices, std::string &err);
-void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std::vector<BVHNode> &neural);
+void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std::vector<BVHNode> &neural,
+                      std::vector<uint32_t> *node_map = nullptr, std::vector<uint32_t> *depth = nullptr);
 void build_inference_nodes(const std::vector<BVHNode> &neural, float dil, std::vector<BVHNode> &dilated,
                            std::vector<float> &bounds);
 // true when every coordinate is +0 or has magnitude in [2^-60, 2^11] (no -0, no subnormal range),
@@ -499,6 +586,18 @@ void camera_params(const nbvh_render_request *r, float du[3], float dv[3], float
 } // namespace nbvh
 
 namespace nbvh {
+
+// ---- learned tree cut (nbvh_tree_cut.cpp) ----
+void validate_tree_cut_options(const nbvh_tree_cut_options &o);
+void begin_tree_cut(nbvh_handle *h, const nbvh_tree_cut_options &o, uint32_t start_depth);
+void end_tree_cut(nbvh_handle *h);
+TreeCutArgs tree_cut_args(nbvh_handle *h);
+void tree_cut_before_step(nbvh_handle *h, NodeSurvival &survival, uint32_t &learned_lod);
+void tree_cut_after_step(nbvh_handle *h, const float *sample_loss, uint32_t n, cudaStream_t s);
+void tree_cut_words(nbvh_handle *h, uint32_t *words, cudaStream_t s); // kCutWords + kNumBvhLods words
+void tree_cut_sync(nbvh_handle *h, cudaStream_t s);
+// inference copies of the neural cut (dilated boxes, subtree bounds) from h->neural_nodes
+void upload_inference_nodes(nbvh_handle *h);
 
 // The reference's .nbvh neural-cut file (nbvh_format.cpp): read (with structural validation) and write.
 bool validate_cut(const std::vector<BVHNode> &nodes, std::string &err);

@@ -62,6 +62,71 @@ class LossConsts(C.Structure):
                 ("visibility_masking_loss", C.c_int32), ("learn_normal", C.c_int32), ("learn_albedo", C.c_int32)]
 
 
+class NodeSurvival(C.Structure):
+    _fields_ = [("stats", C.c_void_p), ("current_max_loss", C.c_float), ("survival_probability_scale", C.c_float),
+                ("min_survival_prob", C.c_float), ("current_learned_lod", C.c_uint32), ("enabled", C.c_int32)]
+
+
+class SplitScheduler:
+    """BvhSplitScheduler (include/cuda/neural/utils/bvh_split_scheduler.h:13-145), restated."""
+
+    def __init__(self, splitting_interval=50, last_split_iteration=2000, start_split_num=1, split_scaling=2.0,
+                 split_interval_scaling=2.0, lod_decision_type=0):
+        self.splitting_interval = splitting_interval
+        self.last_split_iteration = last_split_iteration
+        self.start_split_num = start_split_num
+        self.split_scaling = np.float32(split_scaling)
+        self.split_interval_scaling = np.float32(split_interval_scaling)
+        self.lod_decision_type = lod_decision_type
+        self.total_splits_expected = 0
+        self._reset()
+
+    def _reset(self):
+        self.current_num_splits = self.start_split_num
+        self.current_splitting_interval = self.splitting_interval
+        self.current_total_splits = 0
+
+    def get_bvh_splits(self, it):
+        if it == 0:
+            self._reset()
+        if it > self.last_split_iteration:
+            return 0
+        n = 0
+        if it % self.splitting_interval == 0:
+            n = self.current_num_splits
+            self.current_total_splits += n
+        if it % self.current_splitting_interval == 0:
+            # int *= float: the product in float, truncated back to int
+            self.current_num_splits = int(np.float32(self.current_num_splits) * self.split_scaling)
+            self.current_splitting_interval = int(np.float32(self.current_splitting_interval) *
+                                                  self.split_interval_scaling)
+        return n
+
+    def expected(self, start_nodes, n_iterations):
+        """update_stats_and_reset: splits per iteration (capped by the leaves) and the node count."""
+        nodes, total, graph = start_nodes, 0, []
+        for it in range(n_iterations):
+            leaves = (nodes + 1) // 2
+            k = self.get_bvh_splits(it)
+            if k > 0:
+                k = min(k, leaves)
+                total += k
+                nodes += 2 * k
+            graph.append(total)
+        self.total_splits_expected = total
+        self._reset()
+        return graph, nodes
+
+    def should_assign_new_lod(self, it, current_lod, num_lods_learned, max_lods=7):
+        if self.lod_decision_type == 0:
+            nxt = (max_lods - current_lod) * self.last_split_iteration // num_lods_learned
+            assign = nxt <= it
+        else:
+            nxt = (max_lods - current_lod) * self.total_splits_expected // num_lods_learned
+            assign = nxt <= self.current_total_splits
+        return assign or it >= self.last_split_iteration
+
+
 def bf16_bits(x):
     """bfloat16 bits of float32 values, round to nearest even (finite values)."""
     u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
@@ -249,6 +314,63 @@ class Oracle:
                                              C.c_uint32(training_step), C.c_uint32(batch_size), C.c_uint32(n),
                                              _p(pos), _p(tgt), _p(nodes))
         return pos, tgt, nodes
+
+    def training_batch_rr(self, nscene, cscene, albedo, consts, training_step, batch_size, n, stats, max_loss,
+                          prev_positions, prev_targets, scale=1.0, min_prob=0.005, learned_lod=6, enabled=True):
+        """Training batch with node survival: rejected slots keep prev_positions / prev_targets."""
+        pos = np.array(prev_positions, np.float32).reshape(n, consts.input_segment_points, 3)
+        tgt = np.array(prev_targets, np.float32).reshape(n, 8)
+        nodes = np.empty(n, np.uint32)
+        st = np.ascontiguousarray(stats, np.uint32).reshape(-1, 4)
+        rr = NodeSurvival(_p(st), float(max_loss), float(scale), float(min_prob), int(learned_lod), int(enabled))
+        alb = None if albedo is None else np.ascontiguousarray(albedo, np.float32)
+        self.lib.orc_generate_training_batch_rr(C.byref(nscene), C.byref(cscene), _p(alb), C.byref(consts),
+                                                C.c_uint32(training_step), C.c_uint32(batch_size), C.c_uint32(n),
+                                                _p(pos), _p(tgt), _p(nodes), C.byref(rr))
+        return pos, tgt, nodes
+
+    def loss_heuristic(self, stats):
+        st = np.ascontiguousarray(stats, np.uint32).reshape(-1, 4)
+        f = self.lib.orc_loss_heuristic
+        f.restype = C.c_float
+        return np.array([f(_p(st[i:i + 1])) for i in range(len(st))], np.float32)
+
+    def tree_cut_accumulate(self, stats, values, sample_nodes, dims):
+        st = np.array(stats, np.uint32).reshape(-1, 4)
+        v = np.ascontiguousarray(values, np.float32)
+        nd = np.ascontiguousarray(sample_nodes, np.uint32)
+        self.lib.orc_tree_cut_accumulate(_p(st), _p(v), _p(nd), C.c_uint32(len(nd)), C.c_uint32(dims))
+        return st
+
+    def tree_cut_decisions(self, nodes, stats, k):
+        nodes = np.ascontiguousarray(nodes, np.uint32)
+        st = np.array(stats, np.uint32).reshape(-1, 4)
+        mx = np.zeros(max(k, 1), np.float32)
+        idx = np.zeros(max(k, 1), np.uint32)
+        self.lib.orc_tree_cut_decisions(_p(nodes), C.c_uint32(len(nodes)), _p(st), C.c_uint32(k), _p(mx), _p(idx))
+        return mx[:k], idx[:k], st
+
+    def tree_cut_split(self, nodes, stats, node_map, classic_nodes, split_indices, k, lod, capacity):
+        n = len(nodes)
+        out = np.zeros((capacity, 8), np.uint32)
+        out[:n] = nodes
+        st = np.zeros((capacity, 4), np.uint32)
+        st[:n] = np.asarray(stats, np.uint32).reshape(-1, 4)
+        nm = np.zeros(capacity, np.uint32)
+        nm[:n] = node_map
+        cn = np.ascontiguousarray(classic_nodes, np.uint32)
+        si = np.ascontiguousarray(split_indices, np.uint32)
+        count = C.c_uint32(n)
+        self.lib.orc_tree_cut_split.restype = C.c_uint32
+        m = self.lib.orc_tree_cut_split(_p(out), C.byref(count), C.c_uint32(capacity), _p(st), _p(nm), _p(cn),
+                                        _p(si), C.c_uint32(k), C.c_uint32(lod))
+        c = count.value
+        return out[:c], st[:c], nm[:c], m
+
+    def tree_cut_assign_lod(self, nodes, lod):
+        out = np.array(nodes, np.uint32)
+        self.lib.orc_tree_cut_assign_lod(_p(out), C.c_uint32(len(out)), C.c_uint32(lod))
+        return out
 
     def composite_loss(self, lc, predictions, targets, loss_scale=1.0):
         pred = np.ascontiguousarray(predictions, np.float32).reshape(-1, 16)

@@ -1032,20 +1032,44 @@ static v3 cube_pos_on_face(int face, float u, float v) /* sampling.cuh:85-94 */
     }
 }
 
+/* NeuralTreeCutData::compute_loss_heuristic, include/cuda/neural/neural_bvh_renderer.h:36-47 */
+float orc_loss_heuristic(const uint32_t *stats)
+{
+    float loss;
+    memcpy(&loss, stats, 4);
+    const uint32_t alive = stats[1], samples = stats[3];
+    if (samples == 0u)
+        return -FLT_MAX;
+    return loss / ((float)alive * sqrtf((float)samples / (float)alive));
+}
+
 void orc_generate_training_batch(const orc_neural_scene *sc, const orc_classic_scene *classic,
                                  const float *albedo, const orc_neural_consts *c, uint32_t training_step,
                                  uint32_t batch_size, uint32_t n, float *positions, float *targets,
                                  uint32_t *nodes_out)
 {
+    orc_generate_training_batch_rr(sc, classic, albedo, c, training_step, batch_size, n, positions, targets,
+                                   nodes_out, NULL);
+}
+
+void orc_generate_training_batch_rr(const orc_neural_scene *sc, const orc_classic_scene *classic,
+                                    const float *albedo, const orc_neural_consts *c, uint32_t training_step,
+                                    uint32_t batch_size, uint32_t n, float *positions, float *targets,
+                                    uint32_t *nodes_out, const orc_node_survival *rr)
+{
     v3 smin = load3(sc->scene_min), smax = load3(sc->scene_max);
     const uint32_t *nodes = sc->neural_nodes;
+    const uint32_t learned_lod = rr ? rr->current_learned_lod : ORC_NUM_BVH_LODS - 1u;
     for (uint32_t i = 0; i < n; i++) {
         uint32_t rng = orc_lcg_seed(training_step * batch_size, 0u, i);
         /* stack_based_sample_uniform_bvh_density */
         float sx = orc_lcg_randomf(&rng);
         float sy = orc_lcg_randomf(&rng);
         v3 dir = uniform_sphere(sx, sy);
-        (void)orc_lcg_randomf(&rng); /* sampled LoD draw (single learned LoD for a fixed cut) */
+        /* sampled LoD among the ones learned so far (common.cuh:719-721) */
+        const uint32_t n_lods = ORC_NUM_BVH_LODS - learned_lod;
+        uint32_t lod_pick = (uint32_t)(orc_lcg_randomf(&rng) * (float)n_lods);
+        const uint32_t sampled_lod = learned_lod + (lod_pick < n_lods - 1u ? lod_pick : n_lods - 1u);
         float dil = c->fixed_node_dilation + orc_lcg_randomf(&rng) * c->node_extent_dilation;
         uint32_t stack[ORC_NEURAL_STACK];
         int sp = 0;
@@ -1067,7 +1091,7 @@ void orc_generate_training_batch(const orc_neural_scene *sc, const orc_classic_s
                 o = vadd(vmul(ps, vsub(smax, smin)), smin); /* Bbox::local_to_bbox, bbox.h:93-97 */
                 d = dir;
             }
-            int res = neural_intersect(nodes, c->bvh_lod, o, d, stack, &sp, 0, c, FLT_MAX, dil, &mint, &maxt, &node);
+            int res = neural_intersect(nodes, sampled_lod, o, d, stack, &sp, 0, c, FLT_MAX, dil, &mint, &maxt, &node);
             valid = (res == 1);
             if (res == -1)
                 sp = 0;
@@ -1101,6 +1125,16 @@ void orc_generate_training_batch(const orc_neural_scene *sc, const orc_classic_s
         }
         if (nodes_out)
             nodes_out[i] = node;
+        if (rr && rr->enabled) {
+            /* node survival (neural_bvh_module_kernels.cu:184-199): a rejected sample leaves its
+             * slot's previous input and target in place; its node index is already written */
+            const float estimate = orc_loss_heuristic(rr->stats + 4u * node);
+            float kept = fmaxf(rr->min_survival_prob, estimate / rr->current_max_loss);
+            if (!(estimate <= rr->current_max_loss))
+                kept = 1.0f;
+            if (rr->survival_probability_scale * kept < orc_lcg_randomf(&rng))
+                continue;
+        }
         float pts[48];
         encode_segment(sc, c, ray_at(o, d, mint), ray_at(o, d, maxt), &rng, pts);
         memcpy(positions + (size_t)i * 3u * (uint32_t)c->input_segment_points, pts,
@@ -1395,5 +1429,132 @@ void orc_camera_rays(uint32_t width, uint32_t height, uint32_t sample_idx, uint3
         r[5] = d.y;
         r[6] = d.z;
         r[7] = FLT_MAX;
+    }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Learned tree cut: include/cuda/neural/utils/bvh_split_scheduler.h:13-145,                  */
+/* src/cuda/neural/neural_bvh_renderer_kernels.cu:202-287,                                     */
+/* src/cuda/neural/neural_bvh_renderer_accel.cpp:256-441                                       */
+/* ------------------------------------------------------------------------------------------ */
+
+void orc_tree_cut_accumulate(uint32_t *stats, const float *values, const uint32_t *sample_nodes, uint32_t n,
+                             uint32_t dims)
+{
+    /* update_neural_tree_cut_loss: every output channel's loss value goes to its sample's node */
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t *st = stats + 4u * sample_nodes[i];
+        float loss;
+        memcpy(&loss, st, 4);
+        for (uint32_t ch = 0; ch < dims; ch++)
+            loss += values[(size_t)i * dims + ch];
+        memcpy(st, &loss, 4);
+        st[3] += dims;
+    }
+}
+
+static int node_has_child(const uint32_t *nd) { return nd[7] != ORC_NO_NEURAL_CHILD; }
+
+void orc_tree_cut_decisions(const uint32_t *nodes, uint32_t n_nodes, uint32_t *stats, uint32_t k,
+                            float *max_losses, uint32_t *split_indices)
+{
+    /* the k + 1 launches of update_neural_tree_cut_decisions, run in node order */
+    for (uint32_t j = 0; j < k; j++) {
+        max_losses[j] = 0.0f;
+        split_indices[j] = 0u;
+    }
+    for (uint32_t j = 0; j <= k; j++) {
+        for (uint32_t i = 0; i < n_nodes; i++) {
+            const uint32_t *nd = nodes + 8u * i;
+            if (node_has_child(nd))
+                continue;
+            uint32_t *st = stats + 4u * i;
+            if (j == 0)
+                st[1] += 1u;
+            if (nd[3] == ORC_LEAF_FINAL)
+                continue;
+            const float candidate = orc_loss_heuristic(st);
+            if (j > 0) {
+                const float prev = max_losses[j - 1u];
+                if (candidate >= prev) {
+                    if (candidate == prev)
+                        split_indices[j - 1u] = i;
+                    continue;
+                }
+            }
+            if (j == k)
+                continue;
+            max_losses[j] = fmaxf(candidate, max_losses[j]);
+        }
+    }
+}
+
+uint32_t orc_tree_cut_split(uint32_t *nodes, uint32_t *n_nodes, uint32_t capacity, uint32_t *stats,
+                            uint32_t *node_map, const uint32_t *classic_nodes, const uint32_t *split_indices,
+                            uint32_t k, uint32_t current_lod)
+{
+    /* split_neural_bvh_at: the first min(#leaves, k) indices, unique, ascending (std::set) */
+    uint32_t n = *n_nodes;
+    const uint32_t n_leaves = (n + 1u) / 2u;
+    const uint32_t m = k < n_leaves ? k : n_leaves;
+    uint8_t *chosen = (uint8_t *)calloc(n, 1);
+    for (uint32_t j = 0; j < m; j++)
+        if (split_indices[j] < n)
+            chosen[split_indices[j]] = 1u;
+    uint32_t splits = 0;
+    for (uint32_t i = 0; i < *n_nodes; i++) {
+        if (!chosen[i])
+            continue;
+        const uint32_t *parent = classic_nodes + 8u * node_map[i];
+        if (parent[3] > 0u) /* classic leaf: no split */
+            continue;
+        uint32_t *nd = nodes + 8u * i;
+        if (node_has_child(nd))
+            continue;
+        if (n + 2u > capacity)
+            break;
+        const uint32_t cl = parent[7];
+        const uint32_t left = n++, right = n++;
+        node_map[left] = cl;
+        node_map[right] = cl + 1u;
+        if (nd[3] == ORC_LEAF_LOD(current_lod))
+            nd[3] = 0u;
+        nd[7] = left;
+        for (int w = 0; w < 3; w++) {
+            nd[w] = parent[w];
+            nd[4 + w] = parent[4 + w];
+        }
+        for (uint32_t c = 0; c < 2; c++) {
+            const uint32_t *src = classic_nodes + 8u * (cl + c);
+            uint32_t *dst = nodes + 8u * (left + c);
+            for (int w = 0; w < 3; w++) {
+                dst[w] = src[w];
+                dst[4 + w] = src[4 + w];
+            }
+            dst[3] = src[3] > 0u ? ORC_LEAF_FINAL : ORC_LEAF_LOD(current_lod);
+            dst[7] = ORC_NO_NEURAL_CHILD;
+            uint32_t *cs = stats + 4u * (left + c);
+            const float zero = 0.0f;
+            memcpy(cs, &zero, 4);
+            cs[1] = 1u;
+            cs[2] = stats[4u * i + 2u] + 1u;
+            cs[3] = 0u;
+        }
+        splits++;
+    }
+    free(chosen);
+    *n_nodes = n;
+    return splits;
+}
+
+void orc_tree_cut_assign_lod(uint32_t *nodes, uint32_t n_nodes, uint32_t lod)
+{
+    /* assign_lod_to_current_neural_leaf_nodes */
+    if (lod == ORC_NUM_BVH_LODS - 1u)
+        return;
+    for (uint32_t i = 0; i < n_nodes; i++) {
+        uint32_t *nd = nodes + 8u * i;
+        if (!node_has_child(nd))
+            nd[3] = nd[3] == ORC_LEAF_FINAL ? ORC_LEAF_FINAL : ORC_LEAF_LOD(lod);
     }
 }

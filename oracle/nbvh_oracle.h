@@ -132,6 +132,51 @@ void orc_generate_training_batch(const orc_neural_scene *scene, const orc_classi
                                  uint32_t training_step, uint32_t batch_size, uint32_t n,
                                  float *positions, float *targets, uint32_t *nodes);
 
+/* --- learned tree cut (NeuralBVH2Node LoD encoding, include/cuda/neural/accel/neural_bvh2.cuh:14-30) --- */
+#define ORC_NUM_BVH_LODS 7u
+#define ORC_LEAF_FINAL 1u
+#define ORC_LEAF_LOD(l) (2u + (l))
+#define ORC_NO_NEURAL_CHILD 0xFFFFFFFFu
+
+/* Per-node tree-cut statistics are 4 words: f32 loss, u32 iter_alive, u32 depth, u32 samples
+ * (NeuralTreeCutData, include/cuda/neural/neural_bvh_renderer.h:36-47). */
+float orc_loss_heuristic(const uint32_t *stats);
+
+/* Node survival of the training sampler (neural_bvh_module_kernels.cu:184-199) and the sampled
+ * LoD (common.cuh:719-721). A rejected sample leaves positions / targets of its slot unchanged. */
+typedef struct orc_node_survival {
+    const uint32_t *stats;
+    float current_max_loss;
+    float survival_probability_scale;
+    float min_survival_prob;
+    uint32_t current_learned_lod;
+    int32_t enabled;
+} orc_node_survival;
+
+void orc_generate_training_batch_rr(const orc_neural_scene *scene, const orc_classic_scene *classic,
+                                    const float *albedo, const orc_neural_consts *c,
+                                    uint32_t training_step, uint32_t batch_size, uint32_t n,
+                                    float *positions, float *targets, uint32_t *nodes,
+                                    const orc_node_survival *rr);
+
+/* update_neural_tree_cut_loss (renderer_kernels.cu:202-230): values are n x dims loss values. */
+void orc_tree_cut_accumulate(uint32_t *stats, const float *values, const uint32_t *sample_nodes,
+                             uint32_t n, uint32_t dims);
+
+/* The k + 1 launches of update_neural_tree_cut_decisions (renderer_kernels.cu:232-287), in node
+ * order: iter_alive of every leaf + 1, then the k largest distinct heuristics of the non-final
+ * leaves (max_losses, floored at 0) and for each the last node in index order holding it. */
+void orc_tree_cut_decisions(const uint32_t *nodes, uint32_t n_nodes, uint32_t *stats, uint32_t k,
+                            float *max_losses, uint32_t *split_indices);
+
+/* split_neural_bvh_at (accel.cpp:256-392); returns the number of nodes split. */
+uint32_t orc_tree_cut_split(uint32_t *nodes, uint32_t *n_nodes, uint32_t capacity, uint32_t *stats,
+                            uint32_t *node_map, const uint32_t *classic_nodes,
+                            const uint32_t *split_indices, uint32_t k, uint32_t current_lod);
+
+/* assign_lod_to_current_neural_leaf_nodes (accel.cpp:394-441) */
+void orc_tree_cut_assign_lod(uint32_t *nodes, uint32_t n_nodes, uint32_t lod);
+
 typedef struct orc_loss_consts {
     int32_t visibility_loss, depth_loss, normal_loss, albedo_loss;
     float visibility_loss_scale, depth_loss_scale, normal_loss_scale, albedo_loss_scale;

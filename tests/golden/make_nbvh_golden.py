@@ -8,6 +8,8 @@ writer independently:
 * nbvh_chess_summary.json -- size, sha256, node count, prim_count histogram, root box and the first
   and last records of the reference file, plus the sha256 of its nodes in the library's 8-word
   layout (f32 min.xyz, u32 prim_count, f32 max.xyz, u32 first_id).
+* nbvh_chess_topology.npz -- the reference cut's topology without boxes (prim_count and first_id
+  per node): the learned tree cut's split order is checked against it.
 * nbvh_chess_top5.nbvh -- the reference cut's top five levels, renumbered breadth-first (children
   adjacent) with depth-5 interior nodes turned into LoD leaves (first_id 0xFFFFFFFF, prim_count
   8), written in the same byte layout. A small, valid cut that travels with the tests.
@@ -91,6 +93,8 @@ def main():
     }
     with open(os.path.join(HERE, "nbvh_chess_summary.json"), "w") as f:
         json.dump(summary, f, indent=1)
+    np.savez_compressed(os.path.join(HERE, "nbvh_chess_topology.npz"),
+                        prim_count=rec["count"].astype(np.uint8), first=rec["first"].astype(np.uint32))
     top = top_levels(rec, 5)
     with open(os.path.join(HERE, "nbvh_chess_top5.nbvh"), "wb") as f:
         f.write(encode(top))
