@@ -254,7 +254,7 @@ def test_lod_assignment_matches_oracle(built, oracle):
     h.run_optimisation(20)
     info = h.tree_cut_info()
     assert info.learning == 0 and info.current_learned_lod == 0
-    lod_nodes = np.array(info.n_lod_nodes)
+    lod_nodes = np.array(info.n_lod_nodes, np.int64)
     assert np.all(np.diff(lod_nodes) <= 0) and lod_nodes[0] == info.n_nodes
     nodes, _, nmap = h.tree_cut()
     # at every LoD the leaves form a complete cut: the cut of the moment that LoD was assigned
