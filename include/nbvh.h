@@ -590,7 +590,9 @@ typedef struct nbvh_server_stats {
 nbvh_status nbvh_server_config_default(nbvh_server_config *cfg);
 nbvh_status nbvh_server_create(const nbvh_server_config *cfg, int device, nbvh_server **out);
 /* Registers a built handle (scene, cuts and parameters stay on the device); sizes every slot
- * for it and autotunes its buckets. */
+ * for it and autotunes its buckets. The handle must not be changed while requests for it are in
+ * flight; between requests it may be (more training, a new or learned cut): a slot whose captured
+ * graphs hold arrays that moved since then drops and recaptures them. */
 nbvh_status nbvh_server_add_model(nbvh_server *s, nbvh_handle *model, uint32_t *model_id);
 /* Queues a request (the host buffers must stay valid until it is done); returns at once. */
 nbvh_status nbvh_server_submit(nbvh_server *s, const nbvh_request *req, uint64_t *ticket);

@@ -82,6 +82,7 @@ struct Slot {
     PathBuffers path;
     uint32_t capacity = 0;
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::map<uint32_t, uint64_t> model_versions; // model_version of each model when its graphs were made
     std::thread thread;
     ~Slot()
     {
@@ -220,7 +221,26 @@ void slot_query(nbvh_server *srv, Slot &sl, uint32_t model_id, uint32_t n, uint3
                                    cudaMemcpyDeviceToDevice, sl.stream),
                    "pad batch");
     const StepResources tune = tuning_of(m, bucket);
-    const nbvh_handle *h = m.h;
+    nbvh_handle *h = m.h;
+    // a model whose device arrays were reallocated since its graphs were captured (a new cut, a
+    // grown learned cut, a new mesh) drops them; the context is resized for the new cut first
+    auto ver = sl.model_versions.find(model_id);
+    if (ver == sl.model_versions.end()) {
+        sl.model_versions[model_id] = h->model_version;
+    } else if (ver->second != h->model_version) {
+        const uint64_t gen = sl.q.generation;
+        grow_query_context(h, sl.q, sl.capacity);
+        for (auto g = sl.graphs.begin(); g != sl.graphs.end();) {
+            if (sl.q.generation != gen || g->first.model == model_id) {
+                if (g->second)
+                    cudaGraphExecDestroy(g->second);
+                g = sl.graphs.erase(g);
+            } else {
+                ++g;
+            }
+        }
+        ver->second = h->model_version;
+    }
     cudaGraphExec_t exec = graphable(srv, h) ? ensure_graph(srv, sl, model_id, bucket, depth) : nullptr;
     if (!exec) {
         run_neural_query(h, sl.q, sl.counters.ptr, sl.rays.ptr, bucket, depth, false, sl.hits.ptr, sl.stream, &tune);
@@ -548,6 +568,8 @@ nbvh_status nbvh_server_add_model(nbvh_server *srv, nbvh_handle *h, uint32_t *mo
                 for (uint32_t b = kMinBucket; b <= sl->capacity; b <<= 1)
                     for (uint32_t depth = 1; depth <= 2; depth++)
                         ensure_graph(srv, *sl, id, b, depth);
+        for (auto &sl : srv->slots)
+            sl->model_versions[id] = h->model_version;
         *model_id = id;
     });
 }

@@ -110,3 +110,27 @@ def test_render_same_alone_and_split(models):
 def test_budget_too_small_is_refused(built):
     with pytest.raises(nb.NBVHError):
         nb.Server(n_slots=4, hbm_budget_gb=1e-4)
+
+
+def test_model_changed_between_requests(built):
+    h, s = handle(kind="sphere4k", seed=3, depth=5)
+    h.run_optimisation(50)
+    rays = scenes.uniform_rays(5000, s["bbox"][:3], s["bbox"][3:], seed=7)
+    srv = nb.Server(n_slots=2, hbm_budget_gb=0.1, max_batch_rays=1 << 14)
+    try:
+        mid = srv.add_model(h)
+        first = srv.wait(srv.submit_query(mid, rays))[0]
+        assert np.array_equal(first.view(np.uint32), h.query_closest_neural_host(rays).view(np.uint32))
+        # a deeper cut (new node arrays) and a learned cut grown by training: the slots drop the
+        # graphs that hold the old arrays and answer like the handle itself
+        h.build_neural_cut(9)
+        after = srv.wait(srv.submit_query(mid, rays))[0]
+        assert np.array_equal(after.view(np.uint32), h.query_closest_neural_host(rays).view(np.uint32))
+        h.begin_tree_cut(nb.tree_cut_options(splitting_interval=5, last_split_iteration=40), 2)
+        h.run_optimisation(45)
+        learned = srv.wait(srv.submit_query(mid, rays))[0]
+        assert np.array_equal(learned.view(np.uint32), h.query_closest_neural_host(rays).view(np.uint32))
+        assert not np.array_equal(learned.view(np.uint32), after.view(np.uint32))
+    finally:
+        srv.close()
+        h.close()
