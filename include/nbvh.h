@@ -321,8 +321,10 @@ nbvh_status nbvh_query_visibility_neural(nbvh_handle *h, const nbvh_ray *d_rays,
                                          uint32_t depth, nbvh_neural_hit *d_hits,
                                          nbvh_stream stream);
 
-/* Same queries from host buffers: the library stages the rays through pinned memory in chunks on
- * two internal streams so that copies overlap the kernels, and returns when h_hits is filled. */
+/* Same queries from host buffers, returning when h_hits is filled. Page-locked buffers (both
+ * h_rays and h_hits from cudaHostAlloc / cudaHostRegister) are read and written by the kernels
+ * directly over the host link, so the transfers overlap the query; other host memory is staged
+ * through device buffers in chunks on two internal streams. */
 nbvh_status nbvh_query_closest_neural_host(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n,
                                            uint32_t depth, nbvh_neural_hit *h_hits);
 nbvh_status nbvh_query_closest_classic_host(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n,

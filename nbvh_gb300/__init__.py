@@ -192,6 +192,47 @@ def build_neural_cut_host(nodes, max_depth):
     return out[: n.value].copy()
 
 
+class PinnedArray(np.ndarray):
+    """numpy array in page-locked host memory (nbvh_host_alloc); the *_host queries read and write
+    such buffers from the kernels directly."""
+
+    def __array_finalize__(self, obj):
+        if obj is not None and getattr(self, "_owner", None) is None:
+            self._owner = getattr(obj, "_owner", None)
+
+
+class _PinnedBlock:
+    def __init__(self, nbytes):
+        self.lib = load_library()
+        self.ptr = C.c_void_p()
+        _check(self.lib.nbvh_host_alloc(nbytes, C.byref(self.ptr)), None)
+
+    def __del__(self):
+        if self.ptr:
+            self.lib.nbvh_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+
+def pinned_empty(shape, dtype):
+    """An uninitialised PinnedArray of the given shape and dtype."""
+    dtype = np.dtype(dtype)
+    shape = (shape,) if np.isscalar(shape) else tuple(shape)
+    nbytes = int(np.prod(shape)) * dtype.itemsize
+    block = _PinnedBlock(max(nbytes, 1))
+    raw = (C.c_uint8 * max(nbytes, 1)).from_address(block.ptr.value)
+    arr = np.frombuffer(raw, np.uint8, count=nbytes).view(dtype).reshape(shape).view(PinnedArray)
+    arr._owner = block
+    return arr
+
+
+def pinned_copy(a):
+    """A PinnedArray holding a copy of a."""
+    a = np.ascontiguousarray(a)
+    out = pinned_empty(a.shape, a.dtype)
+    out[...] = a
+    return out
+
+
 def tree_cut_options(**kw):
     """nbvh_tree_cut_options with the reference defaults, fields overridden by keyword."""
     o = abi.TreeCutOptions()
@@ -346,18 +387,21 @@ class NBVH:
     # ---- queries on host arrays (pinned or pageable) ----
     @staticmethod
     def _host_rays(rays_np):
-        rays_np = np.ascontiguousarray(rays_np)
+        if not (isinstance(rays_np, PinnedArray) and rays_np.flags.c_contiguous):
+            rays_np = np.ascontiguousarray(rays_np)
         return rays_np, rays_np.nbytes // 32
 
     def query_closest_neural_host(self, rays_np, depth=1, out=None):
         rays_np, n = self._host_rays(rays_np)
-        out = np.empty(n, NEURAL_HIT_DTYPE) if out is None else out
+        if out is None:
+            out = pinned_empty(n, NEURAL_HIT_DTYPE) if isinstance(rays_np, PinnedArray) else np.empty(n, NEURAL_HIT_DTYPE)
         self._check(self.lib.nbvh_query_closest_neural_host(self.h, _ptr(rays_np), n, depth, _ptr(out)))
         return out
 
     def query_closest_classic_host(self, rays_np, out=None):
         rays_np, n = self._host_rays(rays_np)
-        out = np.empty(n, HIT_DTYPE) if out is None else out
+        if out is None:
+            out = pinned_empty(n, HIT_DTYPE) if isinstance(rays_np, PinnedArray) else np.empty(n, HIT_DTYPE)
         self._check(self.lib.nbvh_query_closest_classic_host(self.h, _ptr(rays_np), n, _ptr(out)))
         return out
 

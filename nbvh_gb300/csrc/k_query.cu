@@ -65,6 +65,11 @@ struct WaveArgs {
     uint32_t n_cut_nodes;
     uint32_t bf16;   // MLP inputs in BF16 (else FP16)
     uint32_t visits; // node visits per traversal round between lane refills
+    // rays finishing in step late_from or later are listed (the early copy of the records to the
+    // host was taken before them); late_from = ~0 lists nothing
+    uint32_t *late_list;
+    uint32_t *late_count;
+    uint32_t late_from;
 };
 
 __device__ __forceinline__ void write_hit(nbvh_neural_hit *hits, uint32_t id, float t, V3 nrm, V3 alb, float vis,
@@ -74,6 +79,19 @@ __device__ __forceinline__ void write_hit(nbvh_neural_hit *hits, uint32_t id, fl
     out[0] = make_float4(t, nrm.x, nrm.y, nrm.z);
     out[1] = make_float4(alb.x, alb.y, alb.z, vis);
     out[2] = make_float4(__uint_as_float(flags), __uint_as_float(segments), __uint_as_float(kInvalid), 0.f);
+}
+
+// The record of a ray that finishes in decode step `it`, plus its id on the late list when the
+// early host copy of the records was already taken.
+__device__ __forceinline__ void finish_hit(const WaveArgs &a, uint32_t it, uint32_t id, float t, V3 nrm, V3 alb,
+                                           float vis, uint32_t flags, uint32_t segments)
+{
+    write_hit(a.hits, id, t, nrm, alb, vis, flags, segments);
+    if (it >= a.late_from) {
+        const uint32_t k = atomicAdd(a.late_count, 1u);
+        if (k < a.n)
+            a.late_list[k] = id;
+    }
 }
 
 // packed meta.w: segments (bits 0-15), stack size (16-23), flags (24-31)
@@ -464,7 +482,7 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
                     s.flags |= NBVH_HIT_STEP_CAP;
                     st_capped++;
                     const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
-                    write_hit(a.hits, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f,
+                    finish_hit(a, it, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f,
                               s.flags, s.segments);
                 } else {
                     if (a.grid.segment_distribution == NBVH_SEGMENT_UNIFORM)
@@ -476,7 +494,7 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
                     s.segments++;
                     st_segments++;
                     if (nc.fallback_margin > 0.0f && fabsf(__fsub_rn(o8[0], thr)) < nc.fallback_margin) {
-                        write_hit(a.hits, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, s.flags & ~NBVH_HIT_VALID,
+                        finish_hit(a, it, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, s.flags & ~NBVH_HIT_VALID,
                                   s.segments);
                         const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
                         a.fallback_list[slot] = s.ray_id;
@@ -513,7 +531,7 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
                         traverse = !stop && s.sp > 0;
                         if (!traverse) {
                             const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
-                            write_hit(a.hits, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f,
+                            finish_hit(a, it, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f,
                                       s.flags, s.segments);
                         }
                     }
@@ -542,7 +560,7 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
                 bool done = false;
                 if (res == 1) {
                     if (a.non_neural && a.non_neural[s.seg_node]) {
-                        write_hit(a.hits, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, s.flags & ~NBVH_HIT_VALID,
+                        finish_hit(a, it, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, s.flags & ~NBVH_HIT_VALID,
                                   s.segments);
                         const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
                         a.fallback_list[slot] = s.ray_id;
@@ -557,7 +575,7 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
                 }
                 if (!keep && !done) {
                     const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
-                    write_hit(a.hits, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f, s.flags,
+                    finish_hit(a, it, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f, s.flags,
                               s.segments);
                 }
             }
@@ -621,6 +639,21 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
         if (e != cudaSuccess)
             return e;
         launches += 3u;
+        if (r.drain_host && it == r.drain_step) {
+            // early copy of every record to the host on the copy stream, overlapping the later
+            // steps; the rays finishing after this point are listed and rewritten at the end
+            e = cudaEventRecord(r.drain_snap, s);
+            if (e == cudaSuccess)
+                e = cudaStreamWaitEvent(r.drain_stream, r.drain_snap, 0);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(r.drain_host, a.hits, (size_t)a.n * sizeof(nbvh_neural_hit), cudaMemcpyDefault,
+                                    r.drain_stream);
+            if (e == cudaSuccess)
+                e = cudaEventRecord(r.drain_done, r.drain_stream);
+            if (e != cudaSuccess)
+                return e;
+            *r.drain_taken = true;
+        }
     }
     return cudaSuccess;
 }
@@ -734,6 +767,9 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     a.n = n;
     a.n_cut_nodes = n_cut_nodes;
     a.visits = res.visits_per_round ? res.visits_per_round : kDefaultVisitsPerRound;
+    a.late_list = res.late_list;
+    a.late_count = res.late_count;
+    a.late_from = res.drain_host ? res.drain_step + 1u : 0xFFFFFFFFu;
     const size_t smem_cut = (size_t)n_cut_nodes * 56u;
     if (res.resume_from > 0u) // continue a query whose first steps ran from a captured graph
         return smem_cut <= kSmemLimit
@@ -742,6 +778,8 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     // words 0-2: rotating list lengths; 3: the MLP's error word; 4-6: rotating work counters of
     // the decode kernel; 7: work counter of the first pass
     cudaError_t e = cudaMemsetAsync(wave_counts, 0, 8u * sizeof(uint32_t), s);
+    if (e == cudaSuccess && res.drain_host)
+        e = cudaMemsetAsync(res.late_count, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess)
         return e;
     if (sort) {
@@ -766,6 +804,42 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     if (smem_cut <= kSmemLimit)
         return run_steps<true>(a, res, smem_cut, num_sms, nc.max_traversal_steps, 0u, s, *launches);
     return run_steps<false>(a, res, 0, num_sms, nc.max_traversal_steps, 0u, s, *launches);
+}
+
+namespace {
+
+// The records of the rays listed as finishing after the early host copy, copied to the host. All
+// records are final in src by now, so the whole 64-byte lines a listed record touches are copied:
+// four threads write one line with 16-byte stores, and the host link receives full lines instead
+// of the 48-byte partial writes of single records (several times slower on the link).
+__global__ void __launch_bounds__(256) k_copy_late(const uint32_t *__restrict__ late, const uint32_t *late_count,
+                                                   uint32_t n, const nbvh_neural_hit *__restrict__ src,
+                                                   nbvh_neural_hit *dst)
+{
+    const uint32_t count = min(*late_count, n);
+    const size_t total = (size_t)n * sizeof(nbvh_neural_hit);
+    const unsigned char *in = reinterpret_cast<const unsigned char *>(src);
+    unsigned char *out = reinterpret_cast<unsigned char *>(dst);
+    for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < (size_t)count * 8u;
+         w += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t id = late[w >> 3], sub = (uint32_t)(w & 7u);
+        const size_t first = (size_t)id * sizeof(nbvh_neural_hit);
+        const size_t line = (first >> 6) + (sub >> 2);
+        if (line > ((first + sizeof(nbvh_neural_hit) - 1u) >> 6))
+            continue;
+        const size_t off = line * 64u + (sub & 3u) * 16u;
+        if (off + 16u <= total)
+            *reinterpret_cast<float4 *>(out + off) = *reinterpret_cast<const float4 *>(in + off);
+    }
+}
+
+} // namespace
+
+cudaError_t launch_copy_late(const uint32_t *late, const uint32_t *late_count, uint32_t n, const nbvh_neural_hit *src,
+                             nbvh_neural_hit *dst, int num_sms, cudaStream_t s)
+{
+    k_copy_late<<<(uint32_t)num_sms * 4u, 256, 0, s>>>(late, late_count, n, src, dst);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -572,6 +572,9 @@ nbvh_status nbvh_destroy(nbvh_handle *h)
         cudaEventDestroy(h->ev0);
     if (h->ev1)
         cudaEventDestroy(h->ev1);
+    for (int k = 0; k < 2; k++)
+        if (h->ev_drain[k])
+            cudaEventDestroy(h->ev_drain[k]);
     delete h;
     return NBVH_OK;
 }
@@ -900,6 +903,106 @@ void pipelined(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, Rec *h_out, Q
     h->last_rays = n;
 }
 
+// Device address of a page-locked host buffer (cudaHostAlloc / cudaHostRegister), NULL for any
+// other memory and for buffers that are not 16-byte aligned (the kernels move rays and records
+// with 16-byte loads and stores).
+const void *mapped_host(const void *p)
+{
+    if (reinterpret_cast<uintptr_t>(p) % 16u != 0u)
+        return nullptr;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (attr.type != cudaMemoryTypeHost || reinterpret_cast<uintptr_t>(attr.devicePointer) % 16u != 0u)
+        return nullptr;
+    return attr.devicePointer;
+}
+
+// Host-buffer queries on page-locked buffers: the kernels read the rays and write the records
+// over the host link themselves (NVLink-C2C on Grace), so the transfers overlap the traversal and
+// the network instead of preceding and following them. One query per 2^23 rays bounds the
+// device workspace.
+template <typename Rec, typename Q>
+bool zero_copy(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, Rec *h_out, Q &&query)
+{
+    const auto *drays = static_cast<const nbvh_ray *>(mapped_host(h_rays));
+    auto *dout = static_cast<Rec *>(const_cast<void *>(mapped_host(h_out)));
+    if (!drays || !dout)
+        return false;
+    const uint32_t chunk = 1u << 23;
+    uint32_t launches = 0;
+    cudaStream_t s = h->pipe_stream[0];
+    for (uint32_t c0 = 0; c0 < n; c0 += chunk) {
+        const uint32_t cnt = (n - c0) < chunk ? (n - c0) : chunk;
+        query(drays + c0, cnt, dout + c0, s, 1);
+        launches += h->last_launches;
+    }
+    cuda_check(cudaStreamSynchronize(s), "sync");
+    h->last_launches = launches;
+    h->last_rays = n;
+    return true;
+}
+
+// Neural host query on page-locked buffers: the first pass reads the rays over the host link; the
+// records are written to device memory and copied to the host in one transfer right after the
+// first network step (most rays are finished by then), overlapping the remaining steps; the rays
+// that finish later are listed by the decode kernel and their records copied at the end.
+bool zero_copy_neural(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, uint32_t depth, nbvh_neural_hit *h_hits)
+{
+    const auto *drays = static_cast<const nbvh_ray *>(mapped_host(h_rays));
+    auto *dhost = static_cast<nbvh_neural_hit *>(const_cast<void *>(mapped_host(h_hits)));
+    if (!drays || !dhost)
+        return false;
+    if (h->cfg.bvh.ignore_neural_blas || h->any_non_neural || h->cfg.fallback_margin > 0.f)
+        return zero_copy(h, h_rays, n, h_hits, [&](const nbvh_ray *din, uint32_t cnt, nbvh_neural_hit *dout,
+                                                    cudaStream_t s, int ctx) {
+            neural_query(h, din, cnt, depth, false, dout, s, ctx, false);
+        });
+    require(h->classic_built && h->neural_built, NBVH_ESTATE, "scene not built");
+    for (int k = 0; k < 2; k++)
+        if (!h->ev_drain[k])
+            cuda_check(cudaEventCreateWithFlags(&h->ev_drain[k], cudaEventDisableTiming), "event");
+    const uint32_t chunk = 1u << 23;
+    cudaStream_t s = h->pipe_stream[0];
+    uint32_t launches = 0;
+    for (uint32_t c0 = 0; c0 < n; c0 += chunk) {
+        const uint32_t cnt = (n - c0) < chunk ? (n - c0) : chunk;
+        ensure_query_workspace(h, cnt, 1);
+        if (h->d_drain_hits.count < cnt)
+            cuda_check(h->d_drain_hits.resize(cnt), "alloc records");
+        if (h->d_late.count < (size_t)cnt + 1u)
+            cuda_check(h->d_late.resize((size_t)cnt + 1u), "alloc late list");
+        bool taken = false;
+        StepResources t;
+        t.drain_host = dhost + c0;
+        t.drain_stream = h->pipe_stream[1];
+        t.drain_snap = h->ev_drain[0];
+        t.drain_done = h->ev_drain[1];
+        t.drain_step = 0;
+        t.late_count = h->d_late.ptr;
+        t.late_list = h->d_late.ptr + 1;
+        t.drain_taken = &taken;
+        launches += run_neural_query(h, h->qctx[1], h->d_counters.ptr + 1, drays + c0, cnt, depth, false,
+                                     h->d_drain_hits.ptr, s, &t);
+        if (taken) {
+            cuda_check(cudaStreamWaitEvent(s, h->ev_drain[1], 0), "wait early copy");
+            cuda_check(launch_copy_late(t.late_list, t.late_count, cnt, h->d_drain_hits.ptr, dhost + c0, h->num_sms, s),
+                       "late records");
+            launches++;
+        } else {
+            cuda_check(cudaMemcpyAsync(h_hits + c0, h->d_drain_hits.ptr, (size_t)cnt * sizeof(nbvh_neural_hit),
+                                       cudaMemcpyDeviceToHost, s),
+                       "D2H");
+        }
+        cuda_check(cudaStreamSynchronize(s), "sync");
+    }
+    h->last_launches = launches;
+    h->last_rays = n;
+    return true;
+}
+
 } // namespace
 
 extern "C" {
@@ -909,9 +1012,11 @@ nbvh_status nbvh_query_closest_neural_host(nbvh_handle *h, const nbvh_ray *h_ray
 {
     return guarded(h, [&]() {
         require((h_rays && h_hits) || n == 0, NBVH_EINVAL, "null buffers");
-        pipelined(h, h_rays, n, h_hits, [&](const nbvh_ray *din, uint32_t cnt, nbvh_neural_hit *dout, cudaStream_t s, int ctx) {
-            neural_query(h, din, cnt, depth, false, dout, s, ctx, false);
-        });
+        if (n == 0 || !zero_copy_neural(h, h_rays, n, depth, h_hits))
+            pipelined(h, h_rays, n, h_hits, [&](const nbvh_ray *din, uint32_t cnt, nbvh_neural_hit *dout,
+                                                cudaStream_t s, int ctx) {
+                neural_query(h, din, cnt, depth, false, dout, s, ctx, false);
+            });
     });
 }
 
@@ -920,12 +1025,14 @@ nbvh_status nbvh_query_closest_classic_host(nbvh_handle *h, const nbvh_ray *h_ra
     return guarded(h, [&]() {
         require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
         require((h_rays && h_hits) || n == 0, NBVH_EINVAL, "null buffers");
-        pipelined(h, h_rays, n, h_hits, [&](const nbvh_ray *din, uint32_t cnt, nbvh_hit *dout, cudaStream_t s, int) {
+        auto q = [&](const nbvh_ray *din, uint32_t cnt, nbvh_hit *dout, cudaStream_t s, int) {
             cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, din, cnt, dout, false, nullptr,
                                       h->classic_fast_div, s),
                        "classic");
             h->last_launches = 1;
-        });
+        };
+        if (n == 0 || !zero_copy(h, h_rays, n, h_hits, q))
+            pipelined(h, h_rays, n, h_hits, q);
     });
 }
 
@@ -1625,6 +1732,14 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
         res.unchecked_steps = tune->unchecked_steps;
         res.capture_only = tune->capture_only;
         res.resume_from = tune->resume_from;
+        res.drain_host = tune->drain_host;
+        res.drain_stream = tune->drain_stream;
+        res.drain_snap = tune->drain_snap;
+        res.drain_done = tune->drain_done;
+        res.drain_step = tune->drain_step;
+        res.late_list = tune->late_list;
+        res.late_count = tune->late_count;
+        res.drain_taken = tune->drain_taken;
     }
     cuda_check(make_feature_map(q.features.ptr, h->layout.n_inputs, q.capacity, &res.feature_map), "feature map");
     cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),

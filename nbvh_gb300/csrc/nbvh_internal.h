@@ -322,6 +322,9 @@ struct nbvh_handle {
     float last_kernel_ms = 0.f;
     uint32_t last_launches = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_drain[2] = {nullptr, nullptr}; // early host copy of the records: taken, done
+    nbvh::DeviceBuffer<uint32_t> d_late;           // late-finishing ray ids: [0] count, then the list
+    nbvh::DeviceBuffer<nbvh_neural_hit> d_drain_hits;
 
     // host-buffer query pipeline
     cudaStream_t pipe_stream[2] = {nullptr, nullptr};
@@ -398,6 +401,15 @@ struct StepResources {
     uint32_t unchecked_steps = 0;      // steps launched before the first host check
     bool capture_only = false;         // enqueue the unchecked steps and a counter copy, then return
     uint32_t resume_from = 0;          // > 0: skip the first pass and continue the checked loop here
+    // early host copy of the records (page-locked destination, device address): taken on
+    // drain_stream after the decode of step drain_step; rays finishing later go to late_list
+    nbvh_neural_hit *drain_host = nullptr;
+    cudaStream_t drain_stream = nullptr;
+    cudaEvent_t drain_snap = nullptr, drain_done = nullptr;
+    uint32_t drain_step = 0;
+    uint32_t *late_list = nullptr;  // [n]
+    uint32_t *late_count = nullptr;
+    bool *drain_taken = nullptr;    // set when the early copy was enqueued
 };
 
 // Scratch of the allocation-free neural query: one static device buffer per device holding, for
@@ -515,6 +527,10 @@ cudaError_t launch_weight_gradients(const GridParams &grid, uint32_t n_hidden_la
                                     const __half *dz, uint32_t n, float *grad, bool bf16, int num_sms, cudaStream_t s);
 
 // ---- learned tree cut (k_tree_cut.cu) ----
+// Copies the records of the late-listed rays from src (device) to dst (page-locked host).
+cudaError_t launch_copy_late(const uint32_t *late, const uint32_t *late_count, uint32_t n, const nbvh_neural_hit *src,
+                             nbvh_neural_hit *dst, int num_sms, cudaStream_t s);
+
 cudaError_t launch_cut_accumulate(const float *sample_loss, const uint32_t *sample_nodes, uint32_t n, uint32_t dims,
                                   uint32_t *stats, cudaStream_t s);
 cudaError_t launch_cut_alive_max(const TreeCutArgs &a, uint32_t slot, int num_sms, cudaStream_t s);

@@ -190,6 +190,18 @@ def test_host_pipeline_matches_device(scene):
     dev = as_u32(h.query_closest_neural(_cuda(rays)))
     host = h.query_closest_neural_host(rays)
     assert np.array_equal(host.view(np.uint32).reshape(-1, 12), dev)
+    # page-locked buffers: the kernels read rays and write records over the host link
+    pinned = nb.pinned_copy(rays)
+    zc = nb.pinned_empty(len(rays), nb.NEURAL_HIT_DTYPE)
+    np.asarray(zc).view(np.uint8)[:] = 0xAB  # no stale records can pass for results
+    zc = h.query_closest_neural_host(pinned, out=zc)
+    assert isinstance(zc, nb.PinnedArray)
+    assert np.array_equal(np.asarray(zc).view(np.uint32).reshape(-1, 12), dev)
+    cdev = h.query_closest_classic(_cuda(rays)).cpu().numpy().view(np.uint32)
+    czc = h.query_closest_classic_host(pinned)
+    assert np.array_equal(np.asarray(czc).view(np.uint32).reshape(-1, 4), cdev.reshape(-1, 4))
+    assert np.array_equal(np.asarray(h.query_closest_classic_host(rays)).view(np.uint32).reshape(-1, 4),
+                          cdev.reshape(-1, 4))
 
 
 def test_run_inference_camera(scene, oracle):
