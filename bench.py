@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=3.0,
                     help="seconds of Poisson arrivals in the serving load; 0 skips it")
     ap.add_argument("--serve-train-steps", type=int, default=1500)
+    ap.add_argument("--learned-cut-steps", type=int, default=4000,
+                    help="training steps of the fixed-cut vs learned-cut comparison (-1 skips it)")
     ap.add_argument("--log2-rays", type=int, default=22,
                     help="rays per step; smaller values are for profiling captures, not bench lines")
     return ap.parse_args()
@@ -425,6 +427,8 @@ def run_ours(args):
         line["mesh_4m"] = run_mesh_4m(args, nb, scenes, cfg, max_over_ranks, rank)
     if args.precision_sweep_steps > 0:
         line["precision_sweep"] = run_precision_sweep(args, nb, scenes, args.precision_sweep_steps)
+    if rank == 0 and args.learned_cut_steps >= 0:
+        line["learned_cut"] = run_learned_cut(args, nb, scenes, args.learned_cut_steps)
     if args.serve_seconds > 0:
         line["serving"] = run_serving(args, nb, scenes)
     if rank == 0:
@@ -595,6 +599,42 @@ def run_precision_sweep(args, nb, scenes, steps):
                      "last_loss": st.last_loss, "heldout_rays": n, "visibility_agreement": vis,
                      "depth_error": depth, "query_ms": float(times.mean()),
                      "query_mrays": n / (float(times.mean()) * 1e-3) / 1e6}
+        h.close()
+    return out
+
+
+def run_learned_cut(args, nb, scenes, steps):
+    """The learned tree cut against the fixed depth-10 cut: the same network trained for `steps`
+    steps either on the fixed cut or with tree-cut learning from the root on the schedule of the
+    reference's shipped chess cut (split interval 40, scaling 2.5, last split at 3000: 25,249
+    nodes), node survival on; then held-out accuracy and query time on 2^20 rays."""
+    import torch
+    out = {}
+    sched = dict(splitting_interval=40, split_scaling=2.5, last_split_iteration=3000)
+    for name in ("fixed_depth10", "learned"):
+        cfg = nb.default_config()
+        h, v, f, _ = build_scene(nb, scenes, cfg)
+        if name == "learned":
+            h.begin_tree_cut(nb.tree_cut_options(**sched), 0)
+        t0 = time.perf_counter()
+        st = h.run_optimisation(steps)
+        train_s = time.perf_counter() - t0
+        nn, bbox = h.neural_bvh()
+        n = 1 << 20
+        rays = torch.from_numpy(scenes.uniform_rays(n, bbox[:3], bbox[3:], seed=778)).cuda()
+        hits = torch.empty((n, 12), dtype=torch.int32, device="cuda")
+        chits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+        times, _, _, _ = time_queries(h, rays, hits, chits, 5, 3, "learned_cut")
+        vis, depth, segs = accuracy(hits, chits)
+        row = {"train_steps": steps, "train_ms_per_step": st.ms_per_step, "train_seconds": train_s,
+               "last_loss": st.last_loss, "cut_nodes": int(len(nn)), "heldout_rays": n,
+               "visibility_agreement": vis, "depth_error": depth, "segments_per_ray": segs,
+               "query_ms": float(times.mean()), "query_mrays": n / (float(times.mean()) * 1e-3) / 1e6}
+        if name == "learned":
+            info = h.tree_cut_info()
+            row.update({"schedule": sched, "expected_nodes": int(info.expected_nodes),
+                        "total_splits": int(info.total_splits), "max_depth": int(info.max_depth)})
+        out[name] = row
         h.close()
     return out
 
