@@ -280,6 +280,30 @@ void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std
     }
 }
 
+uint32_t build_sort_keys(const std::vector<BVHNode> &neural, uint32_t max_bins, std::vector<uint32_t> &keys)
+{
+    const size_t n = neural.size();
+    keys.assign(n, 0u);
+    std::vector<uint32_t> order;
+    std::vector<uint32_t> stack{0u};
+    while (!stack.empty()) {
+        const uint32_t i = stack.back();
+        stack.pop_back();
+        const uint32_t pc = neural[i].prim_count;
+        if ((pc > 0u && pc <= kLeafLodBase) || neural[i].left_or_prim_offset == kNoNeuralChild) {
+            order.push_back(i);
+            continue;
+        }
+        stack.push_back(neural[i].left_or_prim_offset + 1u);
+        stack.push_back(neural[i].left_or_prim_offset);
+    }
+    const uint64_t leaves = order.size();
+    const uint32_t bins = (uint32_t)std::min<uint64_t>(max_bins, leaves);
+    for (uint64_t r = 0; r < leaves; r++)
+        keys[order[r]] = (uint32_t)(r * bins / leaves);
+    return bins;
+}
+
 bool coords_in_fast_div_domain(const float *c, size_t n)
 {
     for (size_t i = 0; i < n; i++) {

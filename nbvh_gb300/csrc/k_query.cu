@@ -36,6 +36,14 @@ constexpr uint32_t kSortThreads = 1024;
 constexpr uint32_t kSortMinRows = 1u << 16;
 constexpr uint32_t kDefaultVisitsPerRound = 8;  // node visits of a traversal between lane refills
 constexpr uint32_t kDefaultEncodeBlocksPerSm = 8; // 2,048 resident threads
+// From this step on, the rays still listed are finished by one persistent kernel (k_wave_tail)
+// instead of one short wavefront step after another: the lists are short by then and each step
+// would cost about the same fixed 60-80 us whatever its length. The switch depends only on the
+// step, i.e. on how many segments a ray has evaluated, so a ray's record does not depend on the
+// other rays of its batch.
+constexpr uint32_t kTailFromStep = 3;
+constexpr uint32_t kTailWarps = 8;
+constexpr uint32_t kTailThreads = kTailWarps * 32;
 // decode: the shared-memory cut variant runs one 768-thread block per SM, the global-memory
 // variant two 384-thread blocks; both leave 85 registers per thread (the traversal stack stays in
 // registers and local memory without spilling)
@@ -48,6 +56,7 @@ struct WaveArgs {
     const float4 *bounds; // union of dilated leaf boxes per node
     const uint8_t *non_neural;
     const uint32_t *table;
+    const __half *weights; // 16-bit network matrices (network-first parameter layout)
     const nbvh_ray *rays;
     nbvh_neural_hit *hits;
     QueryCounters *counters;
@@ -59,7 +68,8 @@ struct WaveArgs {
     uint32_t *perm;        // list rows in leaf-node order (nullptr: rows in list order)
     uint32_t *node_bins;   // [2][n_sort_nodes] rows per leaf node of the current / next list
     uint32_t *node_cursor; // [2][n_sort_nodes] placement cursors of the sort
-    uint32_t n_sort_nodes;
+    const uint32_t *sort_key; // sort bin of each leaf (cuts above kMaxSortNodes nodes); NULL: the node
+    uint32_t n_sort_nodes;    // sort bins
     uint32_t n_hidden_layers;
     uint32_t n;
     uint32_t n_cut_nodes;
@@ -155,7 +165,14 @@ __device__ __forceinline__ uint32_t warp_append(bool want, uint32_t *counter)
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
-// Counts the rows a warp appends per leaf node (one atomic per distinct node in the warp); all 32
+// Sort bin of a leaf: the leaf itself, or for large cuts its bin among runs of leaves in
+// depth-first order (neighbouring leaves in space).
+__device__ __forceinline__ uint32_t sort_bin(const WaveArgs &a, uint32_t node)
+{
+    return a.sort_key ? a.sort_key[node] : node;
+}
+
+// Counts the rows a warp appends per sort bin (one atomic per distinct bin in the warp); all 32
 // lanes take part.
 __device__ __forceinline__ void count_nodes(uint32_t *bins, bool want, uint32_t node)
 {
@@ -246,7 +263,7 @@ __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_co
         if (listed)
             store_state(a.lists[0], pos, s, stack);
         if (a.perm)
-            count_nodes(a.node_bins, listed, s.seg_node);
+            count_nodes(a.node_bins, listed, listed ? sort_bin(a, s.seg_node) : 0u);
     }
 }
 
@@ -282,11 +299,19 @@ __global__ void __launch_bounds__(kEncodeThreads) k_wave_encode(const __grid_con
     uint32_t *feat = reinterpret_cast<uint32_t *>(a.features);
     const bool sorted = a.perm != nullptr && count_in >= kSortMinRows;
     const uint32_t total = count_in * P; // at most 2^22 rays x 16 points
+    // Short lists (the tail of the query) split each point's levels over G threads, 4 levels each,
+    // so that a point's gathers are in flight together instead of one level after another; long
+    // lists keep one thread per point (all levels), which the other points' threads already hide.
+    const uint32_t lanes = gridDim.x * blockDim.x;
+    const uint32_t G = (vec_store && (size_t)total * (L >> 2) <= 2u * (size_t)lanes) ? (L >> 2) : 1u;
+    const uint32_t LG = L / G;
+    const uint32_t work = total * G;
     // each block takes one contiguous range of the (node-sorted) rows, so an SM's L1 serves the
     // grid cells of a few leaf regions at a time
-    const uint32_t per_block = (total + gridDim.x - 1u) / gridDim.x;
-    const uint32_t g_end = min(total, blockIdx.x * per_block + per_block);
-    for (uint32_t g = blockIdx.x * per_block + threadIdx.x; g < g_end; g += blockDim.x) {
+    const uint32_t per_block = (work + gridDim.x - 1u) / gridDim.x;
+    const uint32_t w_end = min(work, blockIdx.x * per_block + per_block);
+    for (uint32_t w = blockIdx.x * per_block + threadIdx.x; w < w_end; w += blockDim.x) {
+        const uint32_t g = w / G, lg = w - g * G;
         const uint32_t i = g / P, p = g - i * P;
         const uint32_t row = sorted ? a.perm[i] : i;
         const float4 od0 = in.od0[row], od1 = in.od1[row];
@@ -311,7 +336,7 @@ __global__ void __launch_bounds__(kEncodeThreads) k_wave_encode(const __grid_con
         const V3 pos = segment_point(epo, epi, t);
         uint32_t *dst = feat + (size_t)g * L; // row * (P * L) + p * L
         if (vec_store) {
-            for (uint32_t l = 0; l < L; l += 4u) {
+            for (uint32_t l = lg * LG; l < lg * LG + LG; l += 4u) {
                 uint4 q;
                 float2 f = encode_level(a.table, gp, l, pos);
                 q.x = pack16(f.x, f.y);
@@ -388,7 +413,7 @@ __global__ void __launch_bounds__(kSortThreads) k_wave_sort(const __grid_constan
     }
     const WaveList &in = a.lists[it & 1u];
     for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
-        atomicAdd(&cnt[in.meta[r].y], 1u);
+        atomicAdd(&cnt[sort_bin(a, in.meta[r].y)], 1u);
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < NB; k += blockDim.x) {
         const uint32_t c = cnt[k];
@@ -397,7 +422,7 @@ __global__ void __launch_bounds__(kSortThreads) k_wave_sort(const __grid_constan
     }
     __syncthreads();
     for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        const uint32_t node = in.meta[r].y;
+        const uint32_t node = sort_bin(a, in.meta[r].y);
         const uint32_t slot = scan[node] + base[node] + atomicAdd(&cnt[node], 1u);
         if (slot < count_in) // the counts match the list; the check only keeps a stray row in bounds
             a.perm[slot] = r;
@@ -584,7 +609,273 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
         if (keep)
             store_state(out, pos, s, stack);
         if (a.perm)
-            count_nodes(a.node_bins + ((it + 1u) & 1u) * a.n_sort_nodes, keep, s.seg_node);
+            count_nodes(a.node_bins + ((it + 1u) & 1u) * a.n_sort_nodes, keep, keep ? sort_bin(a, s.seg_node) : 0u);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        st_segments += __shfl_xor_sync(kFull, st_segments, off);
+        st_capped += __shfl_xor_sync(kFull, st_capped, off);
+        st_overflow += __shfl_xor_sync(kFull, st_overflow, off);
+        st_fallback += __shfl_xor_sync(kFull, st_fallback, off);
+    }
+    if (lane == 0) {
+        if (st_segments)
+            atomicAdd(&a.counters->segments, st_segments);
+        if (st_capped)
+            atomicAdd(&a.counters->step_capped, st_capped);
+        if (st_overflow)
+            atomicAdd(&a.counters->stack_overflow, st_overflow);
+        if (st_fallback)
+            atomicAdd(&a.counters->fallback, st_fallback);
+    }
+}
+
+// Shared-memory layout of the tail kernel: [cut nodes + bounds when staged] [grid parameters]
+// [network matrices] then per warp a 16-row feature tile, the 32 segments' end points and the 32
+// rays' network outputs.
+struct TailLayout {
+    uint32_t cut_bytes, gp_off, w_off, warp_off, warp_bytes, fld, total;
+};
+
+__host__ __device__ inline TailLayout tail_layout(uint32_t n_cut_nodes, bool smem_cut, uint32_t n_inputs,
+                                                  uint32_t n_hidden_layers)
+{
+    TailLayout t;
+    t.cut_bytes = smem_cut ? ((n_cut_nodes * 56u + 15u) & ~15u) : 0u;
+    t.gp_off = t.cut_bytes;
+    t.w_off = t.gp_off + (((uint32_t)sizeof(GridParams) + 15u) & ~15u);
+    const SmemNetLayout SL = smem_net_layout(n_inputs, n_hidden_layers);
+    t.warp_off = t.w_off + ((SL.total * 2u + 15u) & ~15u);
+    t.fld = n_inputs + 8u;
+    t.warp_bytes = ((16u * t.fld * 2u + 15u) & ~15u) + 32u * 32u + 32u * 32u; // features, 2 x float4 ends, 8 outputs
+    t.total = t.warp_off + kTailWarps * t.warp_bytes;
+    return t;
+}
+
+// The rest of the query from step `it` on. Persistent warps own up to 32 rays each (one per lane,
+// refilled from the step's list as rays finish); per round every lane with a pending segment
+// gets its features encoded into the warp's tile (two 16-row tiles), the MLP runs on the tile
+// with mma.sync, and each lane decodes its outputs and searches its next leaf, exactly as
+// k_wave_decode does, until its ray is answered.
+template <bool SMEM_CUT, bool BF16>
+__global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(const __grid_constant__ WaveArgs a,
+                                                                             uint32_t it)
+{
+    const uint32_t count_in = *reinterpret_cast<volatile const uint32_t *>(&a.wave_counts[it % 3u]);
+    if (blockIdx.x * kTailThreads >= count_in)
+        return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const uint32_t n_in = a.grid.n_inputs, H = a.n_hidden_layers, P = a.grid.n_points;
+    const TailLayout TL = tail_layout(a.n_cut_nodes, SMEM_CUT, n_in, H);
+    float4 *s_nodes = reinterpret_cast<float4 *>(smem_raw);
+    float2 *s_bounds = reinterpret_cast<float2 *>(smem_raw + a.n_cut_nodes * 32u);
+    if (SMEM_CUT) {
+        for (uint32_t i = threadIdx.x; i < 2u * a.n_cut_nodes; i += blockDim.x)
+            s_nodes[i] = __ldg(a.nodes + i);
+        for (uint32_t i = threadIdx.x; i < a.n_cut_nodes; i += blockDim.x) {
+            const float4 u = __ldg(a.bounds + 2u * i), v = __ldg(a.bounds + 2u * i + 1u);
+            s_bounds[3u * i] = make_float2(u.x, u.y);
+            s_bounds[3u * i + 1u] = make_float2(u.z, v.x);
+            s_bounds[3u * i + 2u] = make_float2(v.y, v.z);
+        }
+    }
+    GridParams &gp = *reinterpret_cast<GridParams *>(smem_raw + TL.gp_off);
+    {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(&a.grid);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&gp);
+        for (uint32_t i = threadIdx.x; i < sizeof(GridParams) / 4u; i += blockDim.x)
+            dst[i] = src[i];
+    }
+    __half *sw = reinterpret_cast<__half *>(smem_raw + TL.w_off);
+    load_weights_to_smem(a.weights, sw, n_in, H);
+    __syncthreads();
+    using Cut = typename std::conditional<SMEM_CUT, SharedCut, GlobalCut>::type;
+    Cut cut;
+    if constexpr (SMEM_CUT) {
+        cut.nodes = s_nodes;
+        cut.bounds = s_bounds;
+    } else {
+        cut.nodes = a.nodes;
+        cut.bounds = a.bounds;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, tig = lane & 3;
+    unsigned char *wbase = smem_raw + TL.warp_off + (size_t)warp * TL.warp_bytes;
+    __half *feat = reinterpret_cast<__half *>(wbase);
+    float4 *ends = reinterpret_cast<float4 *>(wbase + ((16u * TL.fld * 2u + 15u) & ~15u)); // [32][2]
+    float *outs = reinterpret_cast<float *>(ends + 64);                                   // [32][8]
+
+    const NeuralConsts &nc = a.nc;
+    const float thr = nc.visibility_threshold;
+    const V3 smin = mk3(nc.scene_min[0], nc.scene_min[1], nc.scene_min[2]);
+    const V3 smax = mk3(nc.scene_max[0], nc.scene_max[1], nc.scene_max[2]);
+    const float dilation = __fadd_rn(__fadd_rn(1.0f, nc.node_extent_dilation), nc.fixed_node_dilation);
+    const V3 ext = scale3(sub3(smax, smin), dilation);
+    const V3 center = scale3(add3(smax, smin), 0.5f);
+    const WaveList &in = a.lists[it & 1u];
+    uint32_t *head = &a.wave_counts[4u + it % 3u];
+    const bool sorted = a.perm != nullptr && count_in >= kSortMinRows;
+    uint32_t st_segments = 0, st_capped = 0, st_overflow = 0, st_fallback = 0;
+
+    RayState s;
+    uint32_t stack[kNeuralStackSize];
+    RayDiv rdiv;
+    bool cull_ok = false, active = false, exhausted = false;
+    for (;;) {
+        // refill: lanes without a ray take the next rows of the list (node order when sorted)
+        const unsigned idle = __ballot_sync(kFull, !active);
+        if (idle != 0u && !exhausted) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader)
+                base = atomicAdd(head, (uint32_t)__popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            exhausted = base + (uint32_t)__popc(idle) >= count_in;
+            const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
+            if (!active && i < count_in) {
+                load_state(in, sorted ? a.perm[i] : i, s, stack);
+                active = true;
+                cull_ok = s.d.x != 0.0f && s.d.y != 0.0f && s.d.z != 0.0f;
+                rdiv = make_raydiv(s.o, s.d, nc.fast_div_ok != 0u);
+            }
+        }
+        // step cap (path_module.cu:68, last_inference): the pending segment is not evaluated
+        if (active && s.segments > nc.max_traversal_steps) {
+            s.flags |= NBVH_HIT_STEP_CAP;
+            st_capped++;
+            const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
+            finish_hit(a, it, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f, s.flags,
+                       s.segments);
+            active = false;
+        }
+        const unsigned live = __ballot_sync(kFull, active);
+        if (live == 0u) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        // the pending segment's end points (encode_bvh_network_input_data: swapped when mint < 0)
+        if (active) {
+            float ta = s.seg_mint, tb = s.seg_maxt;
+            if (ta < 0.0f) {
+                const float t = ta;
+                ta = tb;
+                tb = t;
+            }
+            const V3 epo = encode_world(ray_at(s.o, s.d, ta), center, ext);
+            const V3 epi = encode_world(ray_at(s.o, s.d, tb), center, ext);
+            ends[2 * lane] = make_float4(epo.x, epo.y, epo.z, __uint_as_float(s.rng));
+            ends[2 * lane + 1] = make_float4(epi.x, epi.y, epi.z, 0.f);
+        }
+        __syncwarp();
+        for (uint32_t tile = 0; tile < 2u; tile++) {
+            const uint32_t mask = (live >> (16u * tile)) & 0xFFFFu;
+            if (mask == 0u)
+                continue;
+            auto pos = [&](uint32_t r, uint32_t p) -> V3 {
+                const float4 e0 = ends[2u * (16u * tile + r)], e1 = ends[2u * (16u * tile + r) + 1u];
+                float t;
+                if (gp.segment_distribution == NBVH_SEGMENT_UNIFORM) {
+                    uint32_t rng = __float_as_uint(e0.w);
+                    for (uint32_t k = 0; k <= p; k++)
+                        t = lcg_randomf(rng);
+                } else {
+                    uint32_t unused = 0;
+                    t = segment_t(p, P, gp.segment_distribution, unused);
+                }
+                return segment_point(mk3(e0.x, e0.y, e0.z), mk3(e1.x, e1.y, e1.z), t);
+            };
+            encode_tile_to_smem<BF16>(a.table, gp, pos, mask, feat, TL.fld);
+            float o4[4];
+            mlp_tile_from_smem<BF16>(sw, feat, TL.fld, n_in, H, o4);
+            float *ob = outs + 16u * tile * 8u;
+            ob[g * 8u + tig * 2u] = o4[0];
+            ob[g * 8u + tig * 2u + 1u] = o4[1];
+            ob[(g + 8u) * 8u + tig * 2u] = o4[2];
+            ob[(g + 8u) * 8u + tig * 2u + 1u] = o4[3];
+            __syncwarp();
+        }
+        if (active) {
+            if (a.grid.segment_distribution == NBVH_SEGMENT_UNIFORM)
+                for (uint32_t k = 0; k < P; k++) // the draws the encoder made for this segment
+                    (void)lcg_randomf(s.rng);
+            float o8[8];
+#pragma unroll
+            for (int c = 0; c < 8; c++)
+                o8[c] = outs[lane * 8 + c];
+            s.segments++;
+            st_segments++;
+            bool traverse = false;
+            if (nc.fallback_margin > 0.0f && fabsf(__fsub_rn(o8[0], thr)) < nc.fallback_margin) {
+                finish_hit(a, it, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, s.flags & ~NBVH_HIT_VALID,
+                           s.segments);
+                const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
+                a.fallback_list[slot] = s.ray_id;
+                st_fallback++;
+                active = false;
+            } else {
+                // process_neural_bvh_traversal_step, path_inference_kernels.cu:61-131
+                bool stop = false;
+                if (o8[0] > thr) {
+                    const bool inside = s.seg_mint < 0.0f;
+                    if (nc.visibility_only && !inside) {
+                        s.flags |= NBVH_HIT_VALID;
+                        s.vis = o8[0];
+                        stop = true;
+                    } else {
+                        const float de = decode_local_t(o8[1], s.seg_mint, s.seg_maxt, inside, nc.depth_epsilon,
+                                                        nc.fixed_depth_epsilon);
+                        if (de != FLT_MAX) {
+                            if (nc.visibility_only) {
+                                s.flags |= NBVH_HIT_VALID;
+                                s.vis = o8[0];
+                                stop = true;
+                            } else if (de < s.best_t) {
+                                s.flags |= NBVH_HIT_VALID;
+                                s.best_t = de;
+                                s.vis = o8[0];
+                                s.nrm = normalize3(mk3(__fsub_rn(__fmul_rn(o8[2], 2.0f), 1.0f),
+                                                       __fsub_rn(__fmul_rn(o8[3], 2.0f), 1.0f),
+                                                       __fsub_rn(__fmul_rn(o8[4], 2.0f), 1.0f)));
+                                s.alb = mk3(o8[5], o8[6], o8[7]);
+                            }
+                        }
+                    }
+                }
+                traverse = !stop && s.sp > 0;
+            }
+            if (active) {
+                bool done = !traverse;
+                if (traverse) {
+                    // the next entered leaf, bounded by the closest hit so far
+                    const int res = neural_intersect_inference(cut, nc.bvh_lod, s.o, rdiv, cull_ok, stack, s.sp,
+                                                               nc.inference_mint_epsilon, nc.inference_maxt_epsilon,
+                                                               s.best_t, s.seg_mint, s.seg_maxt, s.seg_node);
+                    if (res == 1) {
+                        if (a.non_neural && a.non_neural[s.seg_node]) {
+                            finish_hit(a, it, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f,
+                                       s.flags & ~NBVH_HIT_VALID, s.segments);
+                            const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
+                            a.fallback_list[slot] = s.ray_id;
+                            st_fallback++;
+                            active = false;
+                        }
+                    } else {
+                        if (res < 0) {
+                            s.flags |= 0x8u;
+                            st_overflow++;
+                        }
+                        done = true;
+                    }
+                }
+                if (done) {
+                    const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
+                    finish_hit(a, it, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f,
+                               s.flags, s.segments);
+                    active = false;
+                }
+            }
+        }
+        __syncwarp();
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -608,6 +899,32 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
 constexpr size_t kSmemLimit = (size_t)kMaxDynamicSmem;
 constexpr uint32_t kStepsPerCheck = 4;
 
+template <bool SMEM_CUT, bool BF16>
+cudaError_t launch_tail_variant(const WaveArgs &a, uint32_t it, int num_sms, bool configure, size_t smem,
+                                cudaStream_t s)
+{
+    if (configure) {
+        cudaError_t e = allow_max_dynamic_smem(k_wave_tail<SMEM_CUT, BF16>);
+        if (e != cudaSuccess)
+            return e;
+    }
+    k_wave_tail<SMEM_CUT, BF16><<<(uint32_t)num_sms * (SMEM_CUT ? 1u : 2u), kTailThreads, smem, s>>>(a, it);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tail(const WaveArgs &a, uint32_t it, int num_sms, bool configure, cudaStream_t s)
+{
+    const TailLayout staged = tail_layout(a.n_cut_nodes, true, a.grid.n_inputs, a.n_hidden_layers);
+    const TailLayout global = tail_layout(a.n_cut_nodes, false, a.grid.n_inputs, a.n_hidden_layers);
+    const bool smem_cut = staged.total <= kMaxDynamicSmem;
+    const size_t smem = smem_cut ? staged.total : global.total;
+    if (a.bf16)
+        return smem_cut ? launch_tail_variant<true, true>(a, it, num_sms, configure, smem, s)
+                        : launch_tail_variant<false, true>(a, it, num_sms, configure, smem, s);
+    return smem_cut ? launch_tail_variant<true, false>(a, it, num_sms, configure, smem, s)
+                    : launch_tail_variant<false, false>(a, it, num_sms, configure, smem, s);
+}
+
 // The kernels of steps [it0, it1): sort, K3, K4, K2 per step, no host synchronisation.
 template <bool SMEM_CUT>
 cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_smem, int num_sms, uint32_t it0,
@@ -618,6 +935,24 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
     const uint32_t enc_blocks = (uint32_t)num_sms * enc_per_sm;
     const uint32_t dec_blocks = (uint32_t)num_sms * (SMEM_CUT ? 1u : 2u);
     for (uint32_t it = it0; it < it1; it++) {
+        if (it == kTailFromStep) {
+            // the rest of the query in one launch; the list counters are cleared after it, so every
+            // later check (or the counters a captured graph copies out) reads an empty list
+            if (a.perm) {
+                k_wave_sort<<<(uint32_t)num_sms, kSortThreads, 3u * a.n_sort_nodes * 4u, s>>>(a, it);
+                e = cudaGetLastError();
+                if (e != cudaSuccess)
+                    return e;
+                launches++;
+            }
+            e = launch_tail(a, it, num_sms, !r.capture_only, s);
+            if (e == cudaSuccess)
+                e = cudaMemsetAsync(a.wave_counts, 0, 3u * sizeof(uint32_t), s);
+            if (e != cudaSuccess)
+                return e;
+            launches++;
+            return cudaSuccess;
+        }
         if (a.perm) {
             k_wave_sort<<<(uint32_t)num_sms, kSortThreads, 3u * a.n_sort_nodes * 4u, s>>>(a, it);
             e = cudaGetLastError();
@@ -748,6 +1083,7 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     const uint32_t n_network_params =
         kNeurons * grid.n_inputs + (n_hidden_layers - 1u) * kNeurons * kNeurons + kOutputsPadded * kNeurons;
     a.table = reinterpret_cast<const uint32_t *>(params_h + n_network_params);
+    a.weights = params_h;
     a.rays = rays;
     a.hits = hits;
     a.counters = counters;
@@ -757,9 +1093,12 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     a.wave_counts = wave_counts;
     a.features = res.features;
     a.outputs = res.outputs;
-    a.n_sort_nodes = n_cut_nodes;
+    const bool keyed = res.sort_key != nullptr && res.n_sort_bins > 0u;
+    const uint32_t n_bins = keyed ? res.n_sort_bins : n_cut_nodes;
+    a.sort_key = keyed ? res.sort_key : nullptr;
+    a.n_sort_nodes = n_bins;
     a.bf16 = bf16 ? 1u : 0u;
-    const bool sort = res.perm != nullptr && n_cut_nodes <= kMaxSortNodes;
+    const bool sort = res.perm != nullptr && n_bins <= kMaxSortNodes;
     a.perm = sort ? res.perm : nullptr;
     a.node_bins = res.node_bins;
     a.node_cursor = res.node_cursor;
@@ -783,9 +1122,9 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     if (e != cudaSuccess)
         return e;
     if (sort) {
-        e = cudaMemsetAsync(res.node_bins, 0, 2u * n_cut_nodes * sizeof(uint32_t), s);
+        e = cudaMemsetAsync(res.node_bins, 0, 2u * n_bins * sizeof(uint32_t), s);
         if (e == cudaSuccess)
-            e = cudaMemsetAsync(res.node_cursor, 0, 2u * n_cut_nodes * sizeof(uint32_t), s);
+            e = cudaMemsetAsync(res.node_cursor, 0, 2u * n_bins * sizeof(uint32_t), s);
         if (e != cudaSuccess)
             return e;
     }

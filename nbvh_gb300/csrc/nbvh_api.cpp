@@ -301,6 +301,17 @@ void nbvh::upload_inference_nodes(nbvh_handle *h)
     h->non_neural.assign(h->neural_nodes.size(), 0u);
     h->any_non_neural = false;
     h->d_non_neural.release();
+    // cuts above kMaxSortNodes nodes sort the query rays by runs of depth-first leaves
+    if (h->neural_nodes.size() > kMaxSortNodes) {
+        std::vector<uint32_t> keys;
+        h->n_sort_bins = build_sort_keys(h->neural_nodes, kMaxSortNodes, keys);
+        cuda_check(h->d_sort_key.resize(keys.size()), "alloc sort keys");
+        cuda_check(cudaMemcpy(h->d_sort_key.ptr, keys.data(), keys.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+                   "upload sort keys");
+    } else {
+        h->n_sort_bins = 0;
+        h->d_sort_key.release();
+    }
 }
 
 namespace {
@@ -410,6 +421,8 @@ void neural_query_noalloc(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, ui
         res.node_cursor = sc.node_cursor;
         res.h_words = host_words;
         res.ev = nullptr;
+        res.sort_key = h->n_sort_bins ? h->d_sort_key.ptr : nullptr;
+        res.n_sort_bins = h->n_sort_bins;
         cuda_check(make_feature_map(sc.features, h->layout.n_inputs, (uint32_t)kNoallocRays, &res.feature_map),
                    "feature map");
         cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr,
@@ -1741,6 +1754,8 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
         res.late_count = tune->late_count;
         res.drain_taken = tune->drain_taken;
     }
+    res.sort_key = h->n_sort_bins ? h->d_sort_key.ptr : nullptr;
+    res.n_sort_bins = h->n_sort_bins;
     cuda_check(make_feature_map(q.features.ptr, h->layout.n_inputs, q.capacity, &res.feature_map), "feature map");
     cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),
                                  h->any_non_neural ? h->d_non_neural.ptr : nullptr, h->d_params_h.ptr, h->grid, nc,

@@ -284,6 +284,8 @@ struct nbvh_handle {
     nbvh::DeviceBuffer<float4> d_neural_nodes; // 2 float4 per node
     nbvh::DeviceBuffer<float4> d_neural_dilated; // inference copy: boxes dilated by fixed_node_dilation
     nbvh::DeviceBuffer<float4> d_neural_bounds;  // union of the dilated leaf boxes below each node
+    nbvh::DeviceBuffer<uint32_t> d_sort_key;     // leaf -> sort bin for cuts above kMaxSortNodes nodes
+    uint32_t n_sort_bins = 0;
     nbvh::DeviceBuffer<uint8_t> d_non_neural;
     bool any_non_neural = false;
     bool neural_fast_div = false;  // box coordinates of the cut inside the fast-division domain
@@ -410,6 +412,9 @@ struct StepResources {
     uint32_t *late_list = nullptr;  // [n]
     uint32_t *late_count = nullptr;
     bool *drain_taken = nullptr;    // set when the early copy was enqueued
+    // sort bins of the leaves of a cut above kMaxSortNodes nodes (NULL: one bin per node)
+    const uint32_t *sort_key = nullptr;
+    uint32_t n_sort_bins = 0;
 };
 
 // Scratch of the allocation-free neural query: one static device buffer per device holding, for
@@ -556,6 +561,9 @@ cudaError_t launch_camera_rays(uint32_t width, uint32_t height, uint32_t sample_
 // when the tree depth exceeds the traversal stack.
 bool build_bvh2(const std::vector<float> &vertices, const std::vector<uint32_t> &indices,
                 std::vector<BVHNode> &nodes, std::vector<uint32_t> &prim_indices, std::string &err);
+// Sort bins of the leaves of a cut (rendered LoD): leaves in depth-first order split into at most
+// max_bins runs of equal length; interior nodes get bin 0. Returns the number of bins.
+uint32_t build_sort_keys(const std::vector<BVHNode> &neural, uint32_t max_bins, std::vector<uint32_t> &keys);
 void build_neural_cut(const std::vector<BVHNode> &nodes, uint32_t max_depth, std::vector<BVHNode> &neural,
                       std::vector<uint32_t> *node_map = nullptr, std::vector<uint32_t> *depth = nullptr);
 void build_inference_nodes(const std::vector<BVHNode> &neural, float dil, std::vector<BVHNode> &dilated,

@@ -215,3 +215,29 @@ def test_run_inference_camera(scene, oracle):
     q = as_u32(h.query_closest_neural(_cuda(ref_rays)))
     assert np.array_equal(img, q)
     assert (img[:, 8] & 1).sum() > 100
+
+
+def test_large_cut_sorted_by_leaf_runs(built, oracle):
+    """A cut above 8,192 nodes sorts each step's rays by runs of depth-first leaves: every ray's
+    record is the one it gets alone (the ray order of the batch does not matter) and matches the
+    oracle on a sample."""
+    h, s = handle(kind="sphere65k", seed=1, depth=14)
+    assert len(s["neural"]) > 8192
+    params = _spread_params(h, seed=5)
+    n = 1 << 20
+    rays = scenes.uniform_rays(n, s["bbox"][:3], s["bbox"][3:], seed=41)
+    got = as_u32(h.query_closest_neural(_cuda(rays)))
+    assert h.query_stats().segments > 1 << 17  # the steps are long enough to be sorted
+    perm = np.random.default_rng(2).permutation(n)
+    shuffled = as_u32(h.query_closest_neural(_cuda(rays[perm])))
+    assert np.array_equal(shuffled, got[perm])
+    idx = np.random.default_rng(3).choice(n, 1 << 13, replace=False)
+    net = oracle.network(h.cfg, h.layout, params)
+    consts = oracle.neural_consts(h.cfg)
+    nscene = oracle.neural_scene(s["neural"], s["bbox"])
+    ref = oracle.neural_query(nscene, net, consts, rays[idx], threads=8)
+    s2 = dict(s, params=params)
+    border = _borderline(h, oracle, s2, rays[idx])
+    both = _compare_queries(got[idx], ref, border)
+    assert both.sum() > 100
+    h.close()
