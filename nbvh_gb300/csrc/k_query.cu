@@ -36,12 +36,17 @@ constexpr uint32_t kSortThreads = 1024;
 constexpr uint32_t kSortMinRows = 1u << 16;
 constexpr uint32_t kDefaultVisitsPerRound = 8;  // node visits of a traversal between lane refills
 constexpr uint32_t kDefaultEncodeBlocksPerSm = 8; // 2,048 resident threads
-// From this step on, the rays still listed are finished by one persistent kernel (k_wave_tail)
-// instead of one short wavefront step after another: the lists are short by then and each step
-// would cost about the same fixed 60-80 us whatever its length. The switch depends only on the
-// step, i.e. on how many segments a ray has evaluated, so a ray's record does not depend on the
-// other rays of its batch.
-constexpr uint32_t kTailFromStep = 3;
+// From step tail_step() on, the rays still listed are finished by one persistent kernel
+// (k_wave_tail) instead of one short wavefront step after another: the lists are short by then and
+// each step would cost about the same fixed 60-80 us whatever its length. The switch depends only
+// on the step (how many segments a ray has evaluated) and on the cut, so a ray's record does not
+// depend on the other rays of its batch. Measured on GB300: cuts up to kMaxSortNodes nodes (their
+// later steps still fill the GPU) gain most from step 5 on, larger learned cuts (long runs of
+// small leaves, lists that stay short for 20-30 steps) from step 3 on.
+__host__ __device__ constexpr uint32_t tail_step(uint32_t n_cut_nodes)
+{
+    return n_cut_nodes <= kMaxSortNodes ? 5u : 3u;
+}
 constexpr uint32_t kTailWarps = 8;
 constexpr uint32_t kTailThreads = kTailWarps * 32;
 // decode: the shared-memory cut variant runs one 768-thread block per SM, the global-memory
@@ -631,10 +636,12 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
 }
 
 // Shared-memory layout of the tail kernel: [cut nodes + bounds when staged] [grid parameters]
-// [network matrices] then per warp a 16-row feature tile, the 32 segments' end points and the 32
-// rays' network outputs.
+// [network matrices] then per warp a 16-row feature tile, the 32 rows' segment end points, the 32
+// rows' network outputs and each lane's enumerated segments.
+constexpr uint32_t kTailMaxAhead = 8; // segments a lane may enumerate ahead of its decode
+
 struct TailLayout {
-    uint32_t cut_bytes, gp_off, w_off, warp_off, warp_bytes, fld, total;
+    uint32_t cut_bytes, gp_off, w_off, warp_off, warp_bytes, fld, ends_off, outs_off, segs_off, total;
 };
 
 __host__ __device__ inline TailLayout tail_layout(uint32_t n_cut_nodes, bool smem_cut, uint32_t n_inputs,
@@ -647,16 +654,29 @@ __host__ __device__ inline TailLayout tail_layout(uint32_t n_cut_nodes, bool sme
     const SmemNetLayout SL = smem_net_layout(n_inputs, n_hidden_layers);
     t.warp_off = t.w_off + ((SL.total * 2u + 15u) & ~15u);
     t.fld = n_inputs + 8u;
-    t.warp_bytes = ((16u * t.fld * 2u + 15u) & ~15u) + 32u * 32u + 32u * 32u; // features, 2 x float4 ends, 8 outputs
+    t.ends_off = (16u * t.fld * 2u + 15u) & ~15u;     // float4 [32][2]
+    t.outs_off = t.ends_off + 32u * 32u;              // float [32][8]
+    t.segs_off = t.outs_off + 32u * 32u;              // float2 [32 lanes][kTailMaxAhead]
+    t.warp_bytes = t.segs_off + 32u * kTailMaxAhead * 8u;
     t.total = t.warp_off + kTailWarps * t.warp_bytes;
     return t;
 }
 
 // The rest of the query from step `it` on. Persistent warps own up to 32 rays each (one per lane,
-// refilled from the step's list as rays finish); per round every lane with a pending segment
-// gets its features encoded into the warp's tile (two 16-row tiles), the MLP runs on the tile
-// with mma.sync, and each lane decodes its outputs and searches its next leaf, exactly as
-// k_wave_decode does, until its ray is answered.
+// refilled from the step's list as rays finish). Per round, every lane lists the segments its ray
+// evaluates next, the features of all listed segments are encoded into the warp's feature tile
+// (up to two 16-row tiles), the MLP runs on them with mma.sync, and each lane decodes its outputs
+// in order, exactly as k_wave_decode does one step at a time.
+//
+// While the list still has rays every lane lists one segment. Once it is exhausted and the warp
+// thins out, a lane lists up to min(8, 32 / live lanes) segments ahead: the next leaves its
+// traversal enters with the current closest hit as bound, keeping a copy of its stack after each.
+// Decoding them in order is exact while no hit is accepted, since the bound and hence the
+// traversal do not change; when one is accepted, the segments listed after it are dropped (not
+// evaluated, not counted) and the stack goes back to its copy, so the traversal continues with
+// the new bound exactly as the step-by-step query would. Rays with uniformly sampled segment
+// points (whose random draws follow the evaluated segments) or with non-neural leaves list one
+// segment at a time.
 template <bool SMEM_CUT, bool BF16>
 __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(const __grid_constant__ WaveArgs a,
                                                                              uint32_t it)
@@ -701,8 +721,9 @@ __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(co
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, tig = lane & 3;
     unsigned char *wbase = smem_raw + TL.warp_off + (size_t)warp * TL.warp_bytes;
     __half *feat = reinterpret_cast<__half *>(wbase);
-    float4 *ends = reinterpret_cast<float4 *>(wbase + ((16u * TL.fld * 2u + 15u) & ~15u)); // [32][2]
-    float *outs = reinterpret_cast<float *>(ends + 64);                                   // [32][8]
+    float4 *ends = reinterpret_cast<float4 *>(wbase + TL.ends_off); // [row][2]
+    float *outs = reinterpret_cast<float *>(wbase + TL.outs_off);   // [row][8]
+    float2 *segs = reinterpret_cast<float2 *>(wbase + TL.segs_off) + lane * kTailMaxAhead; // this lane's
 
     const NeuralConsts &nc = a.nc;
     const float thr = nc.visibility_threshold;
@@ -714,12 +735,16 @@ __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(co
     const WaveList &in = a.lists[it & 1u];
     uint32_t *head = &a.wave_counts[4u + it % 3u];
     const bool sorted = a.perm != nullptr && count_in >= kSortMinRows;
+    const bool ahead_ok = a.grid.segment_distribution != NBVH_SEGMENT_UNIFORM && a.non_neural == nullptr;
     uint32_t st_segments = 0, st_capped = 0, st_overflow = 0, st_fallback = 0;
 
     RayState s;
     uint32_t stack[kNeuralStackSize];
+    uint32_t snap[kTailMaxAhead - 1u][kNeuralStackSize]; // stack after listing segment j (j < ahead - 1)
+    int snap_sp[kTailMaxAhead - 1u];
     RayDiv rdiv;
     bool cull_ok = false, active = false, exhausted = false;
+    uint32_t npend = 0;  // segments listed for this round (the loaded row brings one)
     for (;;) {
         // refill: lanes without a ray take the next rows of the list (node order when sorted)
         const unsigned idle = __ballot_sync(kFull, !active);
@@ -736,41 +761,88 @@ __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(co
                 active = true;
                 cull_ok = s.d.x != 0.0f && s.d.y != 0.0f && s.d.z != 0.0f;
                 rdiv = make_raydiv(s.o, s.d, nc.fast_div_ok != 0u);
+                segs[0] = make_float2(s.seg_mint, s.seg_maxt);
+                npend = 1;
             }
         }
-        // step cap (path_module.cu:68, last_inference): the pending segment is not evaluated
-        if (active && s.segments > nc.max_traversal_steps) {
-            s.flags |= NBVH_HIT_STEP_CAP;
-            st_capped++;
+        const unsigned live0 = __ballot_sync(kFull, active);
+        if (live0 == 0u) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        // list this round's segments: one, or more ahead once the warp thins out
+        uint32_t want = 1u;
+        if (ahead_ok && exhausted)
+            want = min(kTailMaxAhead, 32u / (uint32_t)__popc(live0));
+        bool trav_end = false; // the traversal found no further leaf (res = 0) or overflowed (res < 0)
+        int trav_res = 1;
+        while (active && npend < want && !trav_end && s.sp > 0) {
+            if (npend > 0u) { // the stack as it was right after listing segment npend - 1
+                for (int k = 0; k < s.sp; k++)
+                    snap[npend - 1u][k] = stack[k];
+                snap_sp[npend - 1u] = s.sp;
+            }
+            float mint, maxt;
+            uint32_t node;
+            const int res = neural_intersect_inference(cut, nc.bvh_lod, s.o, rdiv, cull_ok, stack, s.sp,
+                                                       nc.inference_mint_epsilon, nc.inference_maxt_epsilon, s.best_t,
+                                                       mint, maxt, node);
+            if (res == 1) {
+                if (a.non_neural && a.non_neural[node]) { // only with npend == 0 (no listing ahead)
+                    finish_hit(a, it, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, s.flags & ~NBVH_HIT_VALID,
+                               s.segments);
+                    const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
+                    a.fallback_list[slot] = s.ray_id;
+                    st_fallback++;
+                    active = false;
+                    break;
+                }
+                segs[npend++] = make_float2(mint, maxt);
+            } else {
+                trav_end = true;
+                trav_res = res;
+            }
+        }
+        if (active && npend == 0u) { // nothing left to evaluate: the ray is answered
+            if (trav_res < 0) {
+                s.flags |= 0x8u;
+                st_overflow++;
+            }
             const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
             finish_hit(a, it, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f, s.flags,
                        s.segments);
             active = false;
         }
-        const unsigned live = __ballot_sync(kFull, active);
-        if (live == 0u) {
-            if (exhausted)
-                break;
-            continue;
+        // rows of this round: each live lane's segments, consecutive
+        const uint32_t mine = active ? npend : 0u;
+        uint32_t row0 = mine;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t v = __shfl_up_sync(kFull, row0, off);
+            if (lane >= off)
+                row0 += v;
         }
-        // the pending segment's end points (encode_bvh_network_input_data: swapped when mint < 0)
-        if (active) {
-            float ta = s.seg_mint, tb = s.seg_maxt;
-            if (ta < 0.0f) {
+        const uint32_t rows = __shfl_sync(kFull, row0, 31);
+        row0 -= mine;
+        if (rows == 0u)
+            continue;
+        for (uint32_t j = 0; j < mine; j++) {
+            float ta = segs[j].x, tb = segs[j].y;
+            if (ta < 0.0f) { // encode_bvh_network_input_data swaps for a negative mint
                 const float t = ta;
                 ta = tb;
                 tb = t;
             }
             const V3 epo = encode_world(ray_at(s.o, s.d, ta), center, ext);
             const V3 epi = encode_world(ray_at(s.o, s.d, tb), center, ext);
-            ends[2 * lane] = make_float4(epo.x, epo.y, epo.z, __uint_as_float(s.rng));
-            ends[2 * lane + 1] = make_float4(epi.x, epi.y, epi.z, 0.f);
+            ends[2u * (row0 + j)] = make_float4(epo.x, epo.y, epo.z, __uint_as_float(s.rng));
+            ends[2u * (row0 + j) + 1u] = make_float4(epi.x, epi.y, epi.z, 0.f);
         }
         __syncwarp();
-        for (uint32_t tile = 0; tile < 2u; tile++) {
-            const uint32_t mask = (live >> (16u * tile)) & 0xFFFFu;
-            if (mask == 0u)
-                continue;
+        for (uint32_t tile = 0; tile * 16u < rows; tile++) {
+            const uint32_t n_t = min(16u, rows - tile * 16u);
+            const uint32_t mask = n_t >= 16u ? 0xFFFFu : ((1u << n_t) - 1u);
             auto pos = [&](uint32_t r, uint32_t p) -> V3 {
                 const float4 e0 = ends[2u * (16u * tile + r)], e1 = ends[2u * (16u * tile + r) + 1u];
                 float t;
@@ -794,87 +866,112 @@ __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(co
             ob[(g + 8u) * 8u + tig * 2u + 1u] = o4[3];
             __syncwarp();
         }
-        if (active) {
+        // decode the listed segments in order
+        bool finished = false, rewound = false;
+        for (uint32_t j = 0; j < mine && !finished; j++) {
+            const float mint = segs[j].x, maxt = segs[j].y;
+            if (j > 0u && !(mint < s.best_t))
+                continue; // beyond the closest hit accepted since it was listed: never entered
+            if (s.segments > nc.max_traversal_steps) { // step cap (path_module.cu:68, last_inference)
+                s.flags |= NBVH_HIT_STEP_CAP;
+                st_capped++;
+                const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
+                finish_hit(a, it, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f, s.flags,
+                           s.segments);
+                finished = true;
+                break;
+            }
             if (a.grid.segment_distribution == NBVH_SEGMENT_UNIFORM)
                 for (uint32_t k = 0; k < P; k++) // the draws the encoder made for this segment
                     (void)lcg_randomf(s.rng);
             float o8[8];
 #pragma unroll
             for (int c = 0; c < 8; c++)
-                o8[c] = outs[lane * 8 + c];
+                o8[c] = outs[(row0 + j) * 8u + (uint32_t)c];
             s.segments++;
             st_segments++;
-            bool traverse = false;
             if (nc.fallback_margin > 0.0f && fabsf(__fsub_rn(o8[0], thr)) < nc.fallback_margin) {
                 finish_hit(a, it, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f, s.flags & ~NBVH_HIT_VALID,
                            s.segments);
                 const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
                 a.fallback_list[slot] = s.ray_id;
                 st_fallback++;
-                active = false;
-            } else {
-                // process_neural_bvh_traversal_step, path_inference_kernels.cu:61-131
-                bool stop = false;
-                if (o8[0] > thr) {
-                    const bool inside = s.seg_mint < 0.0f;
-                    if (nc.visibility_only && !inside) {
-                        s.flags |= NBVH_HIT_VALID;
-                        s.vis = o8[0];
-                        stop = true;
-                    } else {
-                        const float de = decode_local_t(o8[1], s.seg_mint, s.seg_maxt, inside, nc.depth_epsilon,
-                                                        nc.fixed_depth_epsilon);
-                        if (de != FLT_MAX) {
-                            if (nc.visibility_only) {
-                                s.flags |= NBVH_HIT_VALID;
-                                s.vis = o8[0];
-                                stop = true;
-                            } else if (de < s.best_t) {
-                                s.flags |= NBVH_HIT_VALID;
-                                s.best_t = de;
-                                s.vis = o8[0];
-                                s.nrm = normalize3(mk3(__fsub_rn(__fmul_rn(o8[2], 2.0f), 1.0f),
-                                                       __fsub_rn(__fmul_rn(o8[3], 2.0f), 1.0f),
-                                                       __fsub_rn(__fmul_rn(o8[4], 2.0f), 1.0f)));
-                                s.alb = mk3(o8[5], o8[6], o8[7]);
+                finished = true;
+                break;
+            }
+            // process_neural_bvh_traversal_step, path_inference_kernels.cu:61-131
+            bool stop = false;
+            if (o8[0] > thr) {
+                const bool inside = mint < 0.0f;
+                if (nc.visibility_only && !inside) {
+                    s.flags |= NBVH_HIT_VALID;
+                    s.vis = o8[0];
+                    stop = true;
+                } else {
+                    const float de =
+                        decode_local_t(o8[1], mint, maxt, inside, nc.depth_epsilon, nc.fixed_depth_epsilon);
+                    if (de != FLT_MAX) {
+                        if (nc.visibility_only) {
+                            s.flags |= NBVH_HIT_VALID;
+                            s.vis = o8[0];
+                            stop = true;
+                        } else if (de < s.best_t) {
+                            s.flags |= NBVH_HIT_VALID;
+                            s.best_t = de;
+                            s.vis = o8[0];
+                            s.nrm = normalize3(mk3(__fsub_rn(__fmul_rn(o8[2], 2.0f), 1.0f),
+                                                   __fsub_rn(__fmul_rn(o8[3], 2.0f), 1.0f),
+                                                   __fsub_rn(__fmul_rn(o8[4], 2.0f), 1.0f)));
+                            s.alb = mk3(o8[5], o8[6], o8[7]);
+                            if (j + 1u < mine || (j + 1u == mine && trav_end && j < kTailMaxAhead - 1u &&
+                                                  want > 1u)) {
+                                // a traversal ran past this segment with the old bound: drop what it
+                                // listed and resume from the stack as it was after this segment
+                                for (int k = 0; k < snap_sp[j]; k++)
+                                    stack[k] = snap[j][k];
+                                s.sp = snap_sp[j];
+                                trav_end = false;
+                                trav_res = 1;
+                                if (s.sp == 0) {
+                                    const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
+                                    finish_hit(a, it, s.ray_id, s.best_t, s.nrm, s.alb, valid ? s.vis : 0.f,
+                                               s.flags, s.segments);
+                                    finished = true;
+                                }
+                                rewound = true;
+                                break;
                             }
                         }
                     }
                 }
-                traverse = !stop && s.sp > 0;
             }
-            if (active) {
-                bool done = !traverse;
-                if (traverse) {
-                    // the next entered leaf, bounded by the closest hit so far
-                    const int res = neural_intersect_inference(cut, nc.bvh_lod, s.o, rdiv, cull_ok, stack, s.sp,
-                                                               nc.inference_mint_epsilon, nc.inference_maxt_epsilon,
-                                                               s.best_t, s.seg_mint, s.seg_maxt, s.seg_node);
-                    if (res == 1) {
-                        if (a.non_neural && a.non_neural[s.seg_node]) {
-                            finish_hit(a, it, s.ray_id, FLT_MAX, mk3(0, 0, 0), mk3(0, 0, 0), 0.f,
-                                       s.flags & ~NBVH_HIT_VALID, s.segments);
-                            const uint32_t slot = atomicAdd(&a.counters->fallback_count, 1u);
-                            a.fallback_list[slot] = s.ray_id;
-                            st_fallback++;
-                            active = false;
-                        }
-                    } else {
-                        if (res < 0) {
-                            s.flags |= 0x8u;
-                            st_overflow++;
-                        }
-                        done = true;
-                    }
+            if (stop || (j + 1u == mine && (trav_end || s.sp == 0))) {
+                // answered: a visibility stop, or the last listed segment with no leaf after it
+                if (!stop && trav_res < 0) {
+                    s.flags |= 0x8u;
+                    st_overflow++;
                 }
-                if (done) {
-                    const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
-                    finish_hit(a, it, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f,
-                               s.flags, s.segments);
-                    active = false;
-                }
+                const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
+                finish_hit(a, it, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f, s.flags,
+                           s.segments);
+                finished = true;
             }
         }
+        if (active && !finished && !rewound && mine > 0u && (trav_end || s.sp == 0)) {
+            // every listed segment after the last one decoded lay beyond the closest hit, and the
+            // traversal had already ended: the ray is answered
+            if (trav_res < 0) {
+                s.flags |= 0x8u;
+                st_overflow++;
+            }
+            const bool valid = (s.flags & NBVH_HIT_VALID) != 0u;
+            finish_hit(a, it, s.ray_id, valid ? s.best_t : FLT_MAX, s.nrm, s.alb, valid ? s.vis : 0.f, s.flags,
+                       s.segments);
+            finished = true;
+        }
+        if (finished)
+            active = false;
+        npend = 0;
         __syncwarp();
     }
 #pragma unroll
@@ -935,7 +1032,7 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
     const uint32_t enc_blocks = (uint32_t)num_sms * enc_per_sm;
     const uint32_t dec_blocks = (uint32_t)num_sms * (SMEM_CUT ? 1u : 2u);
     for (uint32_t it = it0; it < it1; it++) {
-        if (it == kTailFromStep) {
+        if (it == tail_step(a.n_cut_nodes)) {
             // the rest of the query in one launch; the list counters are cleared after it, so every
             // later check (or the counters a captured graph copies out) reads an empty list
             if (a.perm) {
