@@ -738,6 +738,11 @@ __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(co
     const bool ahead_ok = a.grid.segment_distribution != NBVH_SEGMENT_UNIFORM && a.non_neural == nullptr;
     uint32_t st_segments = 0, st_capped = 0, st_overflow = 0, st_fallback = 0;
 
+    // Rays that need many more segments cluster in space, and so in the node-sorted list: handing
+    // out consecutive rows would leave a few warps with 32 long rays each. Rows are dealt in
+    // transposed order instead (claim i -> row (i mod 32) * R + i / 32), so each warp gets rays
+    // from 32 places of the list.
+    const uint32_t deal_rows = (count_in + 31u) / 32u, deal_total = 32u * deal_rows;
     RayState s;
     uint32_t stack[kNeuralStackSize];
     uint32_t snap[kTailMaxAhead - 1u][kNeuralStackSize]; // stack after listing segment j (j < ahead - 1)
@@ -754,9 +759,10 @@ __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(co
             if (lane == leader)
                 base = atomicAdd(head, (uint32_t)__popc(idle));
             base = __shfl_sync(kFull, base, leader);
-            exhausted = base + (uint32_t)__popc(idle) >= count_in;
-            const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
-            if (!active && i < count_in) {
+            exhausted = base + (uint32_t)__popc(idle) >= deal_total;
+            const uint32_t c = base + __popc(idle & ((1u << lane) - 1u));
+            const uint32_t i = (c & 31u) * deal_rows + (c >> 5);
+            if (!active && c < deal_total && i < count_in) {
                 load_state(in, sorted ? a.perm[i] : i, s, stack);
                 active = true;
                 cull_ok = s.d.x != 0.0f && s.d.y != 0.0f && s.d.z != 0.0f;
