@@ -247,8 +247,10 @@ __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p)
 
 // Encode phase of a 16-row tile: FP16 features of every (row, point, level) written to the warp's
 // feature tile feat[16][ld] (ld = n_inputs + 8 halves); rows not in active_mask16 are zero. Lane j
-// handles the (point, level) pairs j, j + 32, ... for all rows, four rows at a time so that 32
-// independent gathers are in flight per lane; no MLP accumulator is live here.
+// handles the (point, level) pairs j, j + 32, ... for all rows, four rows at a time: the four
+// rows' points are formed first (an inactive row takes the cube centre, whose gathers are cheap L1
+// hits) and then encoded without branches in between, so that the 32 gathers are in flight
+// together; groups of four inactive rows are skipped. No MLP accumulator is live here.
 template <bool BF16, typename PosFn>
 __device__ __forceinline__ void encode_tile_to_smem(const uint32_t *__restrict__ table, const GridParams &gp,
                                                     PosFn &&pos, uint32_t active_mask16, __half *feat, uint32_t ld)
@@ -257,14 +259,26 @@ __device__ __forceinline__ void encode_tile_to_smem(const uint32_t *__restrict__
     const uint32_t L = gp.n_levels, PL = gp.n_points * gp.n_levels;
     for (uint32_t j = (uint32_t)lane; j < PL; j += 32u) {
         const uint32_t p = j / L, l = j - p * L;
-#pragma unroll 4
-        for (uint32_t r = 0; r < 16u; r++) {
-            uint32_t v = 0u;
-            if ((active_mask16 >> r) & 1u) {
-                const float2 f = encode_level(table, gp, l, pos(r, p));
-                v = MlpPrec<BF16>::pack(f.x, f.y);
+        for (uint32_t r0 = 0; r0 < 16u; r0 += 4u) {
+            const uint32_t m4 = (active_mask16 >> r0) & 0xFu;
+            if (m4 == 0u) {
+#pragma unroll
+                for (uint32_t k = 0; k < 4u; k++)
+                    *reinterpret_cast<uint32_t *>(feat + (r0 + k) * ld + 2u * j) = 0u;
+                continue;
             }
-            *reinterpret_cast<uint32_t *>(feat + r * ld + 2u * j) = v;
+            V3 q[4];
+#pragma unroll
+            for (uint32_t k = 0; k < 4u; k++)
+                q[k] = ((m4 >> k) & 1u) ? pos(r0 + k, p) : mk3(0.5f, 0.5f, 0.5f);
+            float2 f[4];
+#pragma unroll
+            for (uint32_t k = 0; k < 4u; k++)
+                f[k] = encode_level(table, gp, l, q[k]);
+#pragma unroll
+            for (uint32_t k = 0; k < 4u; k++)
+                *reinterpret_cast<uint32_t *>(feat + (r0 + k) * ld + 2u * j) =
+                    ((m4 >> k) & 1u) ? MlpPrec<BF16>::pack(f[k].x, f[k].y) : 0u;
         }
     }
     __syncwarp();
