@@ -41,6 +41,7 @@
  *   tcnn FullyFusedMLP::inference (the network half)            nbvh_mlp_inference
  *     (src/cuda/neural/neural_bvh_module.cu:232-238)
  *   path module scatter + next traversal, Lambertian case       nbvh_render_path
+ *   CudaTLAS instancing (include/cuda/accel/tlas.cuh:123-324)   nbvh_scene_* (instanced scenes)
  *     (src/cuda/neural/path/path_inference_kernels.cu:224-429)
  *   (no counterpart: one model per process)                     nbvh_server_* serving loop,
  *                                                               nbvh_query_closest_neural_noalloc
@@ -531,6 +532,32 @@ typedef struct nbvh_path_request {
  * Synchronous: returns when the image is written. */
 nbvh_status nbvh_render_path(nbvh_handle *h, const nbvh_path_request *req, float *d_image, uint64_t *rays_traced,
                              nbvh_stream stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Instanced scenes: several models (handles) placed by affine transforms and queried or path
+ * traced together. The reference renders one neural BLAS with pre-transformed vertices
+ * (src/cuda/neural/neural_bvh_renderer_init.cu:23-25, src/base/scene.cpp:38-44); its TLAS walk is
+ * include/cuda/accel/tlas.cuh:123-324. Each query tests the rays against every instance's world
+ * box and answers those that enter it with the instance's model in object space; the record kept
+ * is the closest hit in world space, with the instance in `reserved` (~0 when nothing is hit) and
+ * the segment counts of all instances summed. Models must not change while a scene call runs.
+ * ------------------------------------------------------------------------------------------- */
+
+typedef struct nbvh_scene nbvh_scene;
+
+nbvh_status nbvh_scene_create(int device, nbvh_scene **out);
+nbvh_status nbvh_scene_destroy(nbvh_scene *scene);
+const char *nbvh_scene_last_error(const nbvh_scene *scene);
+/* object_to_world: row-major 3x4 [A | b], A invertible; world = A * object + b. */
+nbvh_status nbvh_scene_add_instance(nbvh_scene *scene, nbvh_handle *model, const float *object_to_world,
+                                    uint32_t *instance_id);
+nbvh_status nbvh_scene_query_closest(nbvh_scene *scene, const nbvh_ray *d_rays, uint32_t n, uint32_t depth,
+                                     nbvh_neural_hit *d_hits, nbvh_stream stream);
+/* The Lambertian path tracer of nbvh_render_path over the instanced scene (plus the classic ground
+ * plane and the sky of the request). */
+nbvh_status nbvh_scene_render_path(nbvh_scene *scene, const nbvh_path_request *req, float *d_image,
+                                   uint64_t *rays_traced, nbvh_stream stream);
+
 
 /* ---------------------------------------------------------------------------------------------
  * Serving loop (no counterpart in the reference, which renders one model in one process).

@@ -593,6 +593,57 @@ __all__ = [
 ]
 
 
+class Scene:
+    """Instanced scene (nbvh_scene_*): models placed by 3x4 object-to-world transforms."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        self.device = device
+        self.s = C.c_void_p()
+        _check(self.lib.nbvh_scene_create(device, C.byref(self.s)), None, self.lib)
+        self.models = []  # keep the handles alive while the scene uses them
+
+    def _check(self, st):
+        if st != abi.NBVH_OK:
+            raise NBVHError(st, self.lib.nbvh_scene_last_error(self.s).decode())
+
+    def add_instance(self, model, object_to_world=None):
+        m = np.eye(3, 4, dtype=np.float32) if object_to_world is None else np.ascontiguousarray(object_to_world,
+                                                                                                np.float32)
+        assert m.shape == (3, 4)
+        iid = C.c_uint32(0)
+        self._check(self.lib.nbvh_scene_add_instance(self.s, model.h, _ptr(m), C.byref(iid)))
+        self.models.append(model)
+        return iid.value
+
+    def query_closest(self, rays, depth=1, out=None, stream=None):
+        import torch
+        n = rays.shape[0]
+        out = torch.empty((n, 12), dtype=torch.int32, device=rays.device) if out is None else out
+        self._check(self.lib.nbvh_scene_query_closest(self.s, _ptr(rays), n, depth, _ptr(out), _stream(stream)))
+        return out
+
+    def render_path(self, req, stream=None):
+        import torch
+        cam = req.camera
+        img = torch.empty((cam.width * cam.height, 4), dtype=torch.float32, device=torch.device("cuda", self.device))
+        traced = C.c_uint64(0)
+        self._check(self.lib.nbvh_scene_render_path(self.s, C.byref(req), _ptr(img), C.byref(traced),
+                                                    _stream(stream)))
+        return img, traced.value
+
+    def close(self):
+        if self.s:
+            self.lib.nbvh_scene_destroy(self.s)
+            self.s = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Server:
     """The serving loop (nbvh_server_*): continuous batching of query and render requests from
     many client threads against several resident models. Host buffers passed to submit must stay

@@ -175,6 +175,12 @@ PROTOTYPES = {
     "nbvh_adam_step": (ST, [P, P, P]),
     "nbvh_generate_training_batch": (ST, [P, U32, U32, P, P, P, P]),
     "nbvh_run_optimisation": (ST, [P, U32, C.POINTER(TrainStats)]),
+    "nbvh_scene_create": (ST, [C.c_int, C.POINTER(P)]),
+    "nbvh_scene_destroy": (ST, [P]),
+    "nbvh_scene_last_error": (C.c_char_p, [P]),
+    "nbvh_scene_add_instance": (ST, [P, P, P, C.POINTER(C.c_uint32)]),
+    "nbvh_scene_query_closest": (ST, [P, P, U32, U32, P, P]),
+    "nbvh_scene_render_path": (ST, [P, C.POINTER(PathRequest), P, C.POINTER(C.c_uint64), P]),
     "nbvh_tree_cut_options_default": (ST, [C.POINTER(TreeCutOptions)]),
     "nbvh_split_schedule_host": (ST, [C.POINTER(TreeCutOptions), U32, U32, P, C.POINTER(C.c_uint32)]),
     "nbvh_begin_tree_cut": (ST, [P, C.POINTER(TreeCutOptions), U32]),

@@ -24,6 +24,7 @@ SOURCES = [
     "nbvh_server.cpp",
     "nbvh_format.cpp",
     "nbvh_tree_cut.cpp",
+    "nbvh_scene.cpp",
     "k_tree_cut.cu",
     "bvh_builder.cpp",
 ]

@@ -1800,7 +1800,8 @@ uint64_t render_path_core(const nbvh_handle *h, QueryContext &q, QueryCounters *
     if (!pb.h_count)
         cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&pb.h_count), sizeof(uint32_t), cudaHostAllocDefault),
                    "pinned path count");
-    grow_query_context(h, q, n);
+    if (!query)
+        grow_query_context(h, q, n);
     PathArgs a{};
     camera_params(&cam, a.du, a.dv, a.tl);
     for (int k = 0; k < 3; k++) {

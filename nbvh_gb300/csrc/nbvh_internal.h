@@ -202,6 +202,17 @@ struct PathArgs {
     uint32_t *count_out;
 };
 
+// One instance of an instanced scene: object-to-world affine map [A | b] (row-major 3x4), A^-1,
+// the world box of the model's scene box, and whether the map is the identity (rays pass as they
+// are).
+struct InstanceArgs {
+    float xform[12];
+    float inv[9];
+    float box_min[3], box_max[3];
+    uint32_t identity;
+    uint32_t instance;
+};
+
 struct PathBuffers {
     DeviceBuffer<float4> thr, rad;
     DeviceBuffer<nbvh_ray> rays[2];
@@ -219,6 +230,13 @@ struct PathBuffers {
 cudaError_t launch_path_raygen(const PathArgs &a, cudaStream_t s);
 cudaError_t launch_path_shade(const PathArgs &a, uint32_t count_in, uint32_t bounce, cudaStream_t s);
 cudaError_t launch_path_resolve(const PathArgs &a, float *image, cudaStream_t s);
+cudaError_t launch_inst_init(nbvh_neural_hit *hits, uint32_t n, cudaStream_t s);
+cudaError_t launch_inst_prepare(const InstanceArgs &a, const nbvh_ray *rays, uint32_t n, const nbvh_neural_hit *hits,
+                                nbvh_ray *obj_rays, uint32_t *obj_ids, float *obj_scale, uint32_t *count,
+                                cudaStream_t s);
+cudaError_t launch_inst_merge(const InstanceArgs &a, const nbvh_neural_hit *obj_hits, const uint32_t *obj_ids,
+                              const float *obj_scale, const uint32_t *count, uint32_t max_count, nbvh_neural_hit *hits,
+                              cudaStream_t s);
 
 } // namespace nbvh
 
