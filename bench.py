@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=3.0,
                     help="seconds of Poisson arrivals in the serving load; 0 skips it")
     ap.add_argument("--serve-train-steps", type=int, default=1500)
+    ap.add_argument("--scene-train-steps", type=int, default=2000,
+                    help="training steps per model of the instanced config-4 scene (-1 skips it)")
     ap.add_argument("--learned-cut-steps", type=int, default=4000,
                     help="training steps of the fixed-cut vs learned-cut comparison (-1 skips it)")
     ap.add_argument("--log2-rays", type=int, default=22,
@@ -429,6 +431,8 @@ def run_ours(args):
         line["precision_sweep"] = run_precision_sweep(args, nb, scenes, args.precision_sweep_steps)
     if rank == 0 and args.learned_cut_steps >= 0:
         line["learned_cut"] = run_learned_cut(args, nb, scenes, args.learned_cut_steps)
+    if rank == 0 and args.scene_train_steps >= 0:
+        line["scene_config4"] = run_scene_config4(args, nb, scenes)
     if args.serve_seconds > 0:
         line["serving"] = run_serving(args, nb, scenes)
     if rank == 0:
@@ -479,9 +483,65 @@ def run_classic_config1(h, v, f, bbox, scenes, steps, warmup, cpu_sample):
             "sample": len(idx), "cpu_mrays": len(idx) / cpu_s / 1e6, "cpu_threads": threads}
 
 
+def run_scene_config4(args, nb, scenes, reps=3):
+    """Config 4: hybrid path tracing at 1920 x 1080, 1 sample per pixel, 6 bounces over 16 instances
+    of 3 neural BLAS (262,144-triangle fBm sphere, 1,048,576-triangle terrain, 4,194,304-triangle
+    soup with 1e-3..1e-2 edges; each trained `args.scene_train_steps` steps) placed on a 4 x 4 grid
+    with seeded rotations about y and scales 0.8-1.2, a classic ground plane and an analytic sky."""
+    rng = np.random.default_rng(44)
+    models, build_s, train_s = [], 0.0, 0.0
+    for kind in ("sphere", "terrain", "soup"):
+        t0 = time.perf_counter()
+        if kind == "sphere":
+            v, f = scenes.fbm_sphere(8, seed=21)
+        elif kind == "terrain":
+            v, f = scenes.terrain(1024, 512, seed=22)
+        else:
+            v, f = scenes.soup(4194304, seed=23)
+        h = nb.NBVH(nb.default_config())
+        h.set_mesh(v, f, scenes.palette_albedo(len(f), 24 + len(models)))
+        h.build_classic()
+        h.build_neural_cut(10)
+        build_s += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        h.run_optimisation(args.scene_train_steps)
+        train_s += time.perf_counter() - t0
+        models.append((h, len(f)))
+    sc = nb.Scene()
+    for k in range(16):
+        h, _ = models[k % 3]
+        ang = rng.uniform(0, 2 * np.pi)
+        scl = rng.uniform(0.8, 1.2)
+        c, s_ = np.cos(ang), np.sin(ang)
+        A = scl * np.array([[c, 0, s_], [0, 1, 0], [-s_, 0, c]])
+        centre = np.array([0.5, 0.0, 0.5])  # meshes live in the unit cube: rotate about its vertical axis
+        gx, gz = k % 4, k // 4
+        b = np.array([1.5 * gx, 0.0, 1.5 * gz]) - A @ centre
+        sc.add_instance(h, np.hstack([A, b[:, None]]).astype(np.float32))
+    lo, hi = np.array([-0.3, 0.0, -0.3]), np.array([5.3, 1.2, 5.3])
+    cam = nb.render_request(1920, 1080, [2.5, 3.2, -2.8], [2.5, 0.2, 2.5], [0, 1, 0], 50.0)
+    req = nb.path_request(cam, spp=1, max_bounces=6, seed=1, ground_height=-0.01, ground_albedo=(0.6, 0.6, 0.6))
+    sc.render_path(req)  # warm
+    ts, traced = [], 0
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        _, traced = sc.render_path(req)
+        ts.append(time.perf_counter() - t0)
+    t = float(np.median(ts))
+    out = {"width": 1920, "height": 1080, "spp": 1, "bounces": 6, "instances": 16,
+           "models_triangles": [m[1] for m in models], "train_steps_per_model": args.scene_train_steps,
+           "build_seconds": build_s, "train_seconds": train_s, "rays_per_frame": int(traced),
+           "ms_per_frame": t * 1e3, "mrays": traced / t / 1e6, "ground_plane": True}
+    sc.close()
+    for h, _ in models:
+        h.close()
+    del lo, hi
+    return out
+
+
 def run_path_config4(h, nb, scenes, bbox, reps=3):
-    """Hybrid path tracing at 1920 x 1080, 1 sample per pixel, 6 bounces: the neural BLAS plus a
-    classic ground plane under an analytic sky (one model; instancing is not built)."""
+    """Hybrid path tracing at 1920 x 1080, 1 sample per pixel, 6 bounces: one neural BLAS plus a
+    classic ground plane under an analytic sky (the instanced form is run_scene_config4)."""
     org, tgt, up = scenes.orbit_camera(bbox[:3], bbox[3:], seed=12)
     cam = nb.render_request(1920, 1080, org, tgt, up, 45.0, sample_idx=0, sample_offset=0)
     req = nb.path_request(cam, spp=1, max_bounces=6, seed=1, ground_height=float(bbox[1]) - 0.01,
