@@ -637,12 +637,13 @@ def run_serving(args, nb, scenes):
 
 
 def run_precision_sweep(args, nb, scenes, steps):
-    """Config 3: the same network trained from the same seed in each MLP precision (FP16, BF16) for
+    """Config 3: the same network trained from the same seed in each MLP precision (FP16, BF16,
+    FP8-E4M3 hidden layers) for
     `steps` steps of 2^18 device-labelled rays, then evaluated against the classic kernel on 2^20
     held-out rays (visibility agreement, depth error) and timed as a query."""
     import torch
     out = {}
-    for name, prec in (("fp16", 0), ("bf16", 1)):
+    for name, prec in (("fp16", 0), ("bf16", 1), ("fp8", 2)):
         cfg = nb.default_config(**{"network.precision": prec})
         h, v, f, _ = build_scene(nb, scenes, cfg)
         nn, bbox = h.neural_bvh()

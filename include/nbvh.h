@@ -149,7 +149,11 @@ typedef enum nbvh_segment_distribution { /* neural_bvh_module.h:23-25 */
 typedef enum nbvh_precision {
     NBVH_PRECISION_FP16 = 0, /* MLP operands FP16, FP32 accumulation */
     NBVH_PRECISION_BF16 = 1, /* MLP operands BF16, FP32 accumulation */
-    NBVH_PRECISION_FP8  = 2  /* hidden layers FP8-E4M3 (per-tensor scale), first/last layer FP16 */
+    NBVH_PRECISION_FP8  = 2  /* hidden 64x64 layers FP8-E4M3: weights e4m3(w * 2^6) / 2^6, their
+                                input activations e4m3(a * 2^7) / 2^7 (ties to even, saturating);
+                                first and last layers FP16. E4M3 values are exact in FP16, so the
+                                FP16 tensor-core paths compute them; FP32 accumulation and master
+                                weights, straight-through gradients */
 } nbvh_precision;
 
 /* HashGridOptions, include/cuda/neural/utils/tcnn_config.h:69-78. n_features_per_level must be 2;

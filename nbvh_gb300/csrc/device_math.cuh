@@ -8,6 +8,7 @@
 // max(a, b) = a < b ? b : a, normalize(v) = v * (1 / sqrt(dot(v, v))).
 #pragma once
 
+#include <cstring>
 #include <cfloat>
 #include <cstdint>
 
@@ -621,6 +622,52 @@ __device__ __forceinline__ float tree_cut_heuristic(float loss, uint32_t iter_al
         return -FLT_MAX;
     const float alive = __uint2float_rn(iter_alive);
     return __fdiv_rn(loss, __fmul_rn(alive, __fsqrt_rn(__fdiv_rn(__uint2float_rn(samples), alive))));
+}
+
+// Round to the nearest FP8 E4M3 value (ties to even), saturating at +-448 (the "satfinite"
+// convention: E4M3 has no infinity). 4 exponent bits (bias 7), 3 mantissa bits, subnormals on the
+// 2^-9 grid below 2^-6. The same integer/float steps run on the host in the CPU restatement.
+__host__ __device__ inline float e4m3_round(float x)
+{
+    uint32_t b;
+    memcpy(&b, &x, 4);
+    const uint32_t sign = b & 0x80000000u;
+    uint32_t a = b & 0x7FFFFFFFu;
+    if (a > 0x7F800000u)
+        return x; // NaN
+    float r;
+    if (a >= 0x43E00000u) { // |x| >= 448
+        a = 0x43E00000u;
+        memcpy(&r, &a, 4);
+    } else if (a < 0x3C800000u) { // |x| < 2^-6: the subnormal grid
+        float m;
+        memcpy(&m, &a, 4);
+        r = rintf(m * 512.0f) * (1.0f / 512.0f);
+    } else {
+        const uint32_t lsb = (a >> 20) & 1u;
+        a = (a + 0x7FFFFu + lsb) & 0xFFF00000u;
+        if (a > 0x43E00000u)
+            a = 0x43E00000u;
+        memcpy(&r, &a, 4);
+    }
+    uint32_t rb;
+    memcpy(&rb, &r, 4);
+    rb |= sign;
+    memcpy(&r, &rb, 4);
+    return r;
+}
+
+// Scale of the hidden weight matrices in FP8 mode: w8 = e4m3(w * 2^6) / 2^6 (|w| up to 7 kept,
+// normal values from 2^-12); every such value is exact in FP16.
+constexpr float kFp8WeightScale = 64.0f;
+// Scale of the activations entering the hidden matrices in FP8 mode: a8 = e4m3(a * 2^7) / 2^7
+// (values up to 3.5, normal from 2^-13; without it the small activations of an untrained network
+// round to zero and their ReLU gradients vanish).
+constexpr float kFp8ActScale = 128.0f;
+
+__host__ __device__ inline float fp8_act(float a)
+{
+    return e4m3_round(a * kFp8ActScale) * (1.0f / kFp8ActScale);
 }
 
 } // namespace nbvh

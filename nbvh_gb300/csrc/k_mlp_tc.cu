@@ -68,6 +68,7 @@ struct MlpTcArgs {
     const uint32_t *d_count; // optional row count produced on the device (min with n)
     float *outputs;
     uint32_t *status;
+    uint32_t fp8; // inputs of the hidden matrices rounded to FP8-E4M3
 };
 
 // D = A * W^T for the 128-row tile: A (128 x K) at a_addr, W (N x K) at w_addr, both in the
@@ -86,9 +87,11 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, uint
 // Hidden-layer epilogue for this thread's row: 64 accumulator columns -> ReLU -> 16-bit (FP16 or
 // BF16) -> the next layer's A operand (128 x 64) at act.
 template <bool BF16>
-__device__ __forceinline__ void epilogue_hidden(uint32_t tmem_row, unsigned char *act, uint32_t row)
+__device__ __forceinline__ void epilogue_hidden(uint32_t tmem_row, unsigned char *act, uint32_t row, bool fp8)
 {
     using Pr = MlpPrec<BF16>;
+    // FP8 mode: the input of a hidden matrix is an FP8-E4M3 value (exact in FP16)
+    auto relu = [fp8](uint32_t u) { return fp8 ? fp8_act(fmaxf(__uint_as_float(u), 0.f)) : fmaxf(__uint_as_float(u), 0.f); };
     uint32_t v[4][16];
 #pragma unroll
     for (int q = 0; q < 4; q++)
@@ -98,10 +101,10 @@ __device__ __forceinline__ void epilogue_hidden(uint32_t tmem_row, unsigned char
     for (int c = 0; c < 8; c++) {
         const uint32_t *s = &v[c >> 1][(c & 1) * 8];
         uint4 q;
-        q.x = Pr::pack(fmaxf(__uint_as_float(s[0]), 0.f), fmaxf(__uint_as_float(s[1]), 0.f));
-        q.y = Pr::pack(fmaxf(__uint_as_float(s[2]), 0.f), fmaxf(__uint_as_float(s[3]), 0.f));
-        q.z = Pr::pack(fmaxf(__uint_as_float(s[4]), 0.f), fmaxf(__uint_as_float(s[5]), 0.f));
-        q.w = Pr::pack(fmaxf(__uint_as_float(s[6]), 0.f), fmaxf(__uint_as_float(s[7]), 0.f));
+        q.x = Pr::pack(relu(s[0]), relu(s[1]));
+        q.y = Pr::pack(relu(s[2]), relu(s[3]));
+        q.z = Pr::pack(relu(s[4]), relu(s[5]));
+        q.w = Pr::pack(relu(s[6]), relu(s[7]));
         *reinterpret_cast<uint4 *>(act + tc::operand_offset(row, 8u * c, kTileRows)) = q;
     }
 }
@@ -204,7 +207,7 @@ __global__ void __launch_bounds__(kMlpThreads, 3) k_mlp_tc(const __grid_constant
             mma_pending = false;
             tc::fence_after_sync();
             if (layer < H) {
-                epilogue_hidden<BF16>(tmem_row, tile, row);
+                epilogue_hidden<BF16>(tmem_row, tile, row, a.fp8 != 0u && layer + 1u < H);
                 tc::fence_async_shared();
             } else {
                 // the tile buffer is free: start the next tile's copy under this epilogue
@@ -295,10 +298,11 @@ cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t
 
 cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
                           uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
-                          uint32_t *status, bool bf16, int num_sms, cudaStream_t s, bool configure)
+                          uint32_t *status, uint32_t prec, int num_sms, cudaStream_t s, bool configure)
 {
     if (rows == 0)
         return cudaSuccess;
+    const bool bf16 = prec == NBVH_PRECISION_BF16;
     CUtensorMap fmap;
     memcpy(&fmap, feature_map.bytes, sizeof(fmap));
     MlpTcArgs a;
@@ -310,6 +314,7 @@ cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpack
     a.d_count = d_count;
     a.outputs = outputs;
     a.status = status;
+    a.fp8 = prec == NBVH_PRECISION_FP8 ? 1u : 0u;
     const size_t smem = ((a.wbytes + 1023u) & ~1023u) + kTileRows * n_inputs * 2u + 32u;
     if (configure) {
         const cudaError_t e = bf16 ? allow_max_dynamic_smem(k_mlp_tc<true>)

@@ -69,6 +69,7 @@ struct InferArgs {
     float *outputs;
     uint32_t n_hidden_layers;
     uint32_t n;
+    uint32_t fp8;
 };
 
 // Network inference on explicit encoded positions: one warp per 16-row tile, grid-stride.
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_network_inference(const __grid_
         };
         encode_tile_to_smem<BF16>(args.table, gp, pos, mask, feat, fld);
         float o4[4];
-        mlp_tile_from_smem<BF16>(sw, feat, fld, n_inputs, args.n_hidden_layers, o4);
+        mlp_tile_from_smem<BF16>(sw, feat, fld, n_inputs, args.n_hidden_layers, o4, args.fp8 != 0u);
         __syncwarp();
         if (act0) {
             args.outputs[(size_t)r0 * 8u + tig * 2] = o4[0];
@@ -150,12 +151,14 @@ cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, c
 }
 
 cudaError_t launch_network_inference(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
-                                     const float *positions, uint32_t n, float *outputs, bool bf16, int num_sms,
+                                     const float *positions, uint32_t n, float *outputs, uint32_t prec, int num_sms,
                                      cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
+    const bool bf16 = prec == NBVH_PRECISION_BF16;
     InferArgs a;
+    a.fp8 = prec == NBVH_PRECISION_FP8 ? 1u : 0u;
     a.grid = grid;
     uint32_t n_network_params = kNeurons * grid.n_inputs + (n_hidden_layers - 1u) * kNeurons * kNeurons +
                                 kOutputsPadded * kNeurons;

@@ -79,6 +79,7 @@ struct WaveArgs {
     uint32_t n;
     uint32_t n_cut_nodes;
     uint32_t bf16;   // MLP inputs in BF16 (else FP16)
+    uint32_t prec;   // nbvh_precision of the MLP (FP8: hidden-matrix inputs rounded to E4M3)
     uint32_t visits; // node visits per traversal round between lane refills
     // rays finishing in step late_from or later are listed (the early copy of the records to the
     // host was taken before them); late_from = ~0 lists nothing
@@ -864,7 +865,7 @@ __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(co
             };
             encode_tile_to_smem<BF16>(a.table, gp, pos, mask, feat, TL.fld);
             float o4[4];
-            mlp_tile_from_smem<BF16>(sw, feat, TL.fld, n_in, H, o4);
+            mlp_tile_from_smem<BF16>(sw, feat, TL.fld, n_in, H, o4, a.prec == NBVH_PRECISION_FP8);
             float *ob = outs + 16u * tile * 8u;
             ob[g * 8u + tig * 2u] = o4[0];
             ob[g * 8u + tig * 2u + 1u] = o4[1];
@@ -1068,7 +1069,7 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
         if (e != cudaSuccess)
             return e;
         e = launch_mlp_tc(r.feature_map, r.wpacked, a.grid.n_inputs, a.n_hidden_layers, a.lists[0].capacity,
-                          &a.wave_counts[it % 3u], a.outputs, &a.wave_counts[3], a.bf16 != 0u, num_sms, s,
+                          &a.wave_counts[it % 3u], a.outputs, &a.wave_counts[3], a.prec, num_sms, s,
                           !r.capture_only);
         if (e != cudaSuccess)
             return e;
@@ -1171,7 +1172,7 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
                               const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
                               const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
                               nbvh_neural_hit *hits, QueryCounters *counters, uint32_t *fallback_list,
-                              const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, bool bf16,
+                              const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, uint32_t prec,
                               int num_sms, cudaStream_t s, uint32_t *launches)
 {
     *launches = 0;
@@ -1200,7 +1201,8 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     const uint32_t n_bins = keyed ? res.n_sort_bins : n_cut_nodes;
     a.sort_key = keyed ? res.sort_key : nullptr;
     a.n_sort_nodes = n_bins;
-    a.bf16 = bf16 ? 1u : 0u;
+    a.bf16 = prec == NBVH_PRECISION_BF16 ? 1u : 0u;
+    a.prec = prec;
     const bool sort = res.perm != nullptr && n_bins <= kMaxSortNodes;
     a.perm = sort ? res.perm : nullptr;
     a.node_bins = res.node_bins;

@@ -300,6 +300,7 @@ struct TrainArgs {
     float2 *grid_grad; // n_grid_entries
     float *loss_sum;
     float *sample_loss; // per row: sum of its output channels' loss values (may be NULL)
+    uint32_t fp8;       // hidden-matrix inputs rounded to FP8-E4M3 (straight-through in the backward)
     uint32_t n_hidden_layers;
     uint32_t n;
 };
@@ -375,7 +376,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
         }
         uint32_t ah[4][4];
         for (uint32_t layer = 1; layer <= H; layer++) {
-            relu_pack<BF16>(acc, ah);
+            relu_pack<BF16>(acc, ah, a.fp8 && layer < H); // FP8 mode: inputs of the hidden matrices
             // store x_layer (input of matrix `layer`)
             __half *dst0 = a.acts + (size_t)r0 * acts_stride + n_in + (layer - 1u) * kNeurons;
             __half *dst1 = a.acts + (size_t)r1 * acts_stride + n_in + (layer - 1u) * kNeurons;
@@ -716,20 +717,24 @@ __global__ void __launch_bounds__(kWgThreads, 1) k_weight_grads(const __grid_con
 // ---------------------------------------------------------------------------------------------
 
 // 16-bit copy of parameter i: the first n_bf16 parameters (the network matrices in BF16 mode) as
-// BF16, the rest (or all, in FP16 mode) as FP16.
-__device__ __forceinline__ __half to_param16(float x, uint32_t i, uint32_t n_bf16)
+// BF16, those in [fp8_lo, fp8_hi) (the hidden 64x64 matrices in FP8 mode) as their FP8-E4M3 value
+// at scale 2^6 (exact in FP16), the rest as FP16.
+__device__ __forceinline__ __half to_param16(float x, uint32_t i, const ParamPrecision &pp)
 {
-    if (i < n_bf16) {
+    if (i < pp.n_bf16) {
         const __nv_bfloat16 b = __float2bfloat16_rn(x);
         return *reinterpret_cast<const __half *>(&b);
     }
+    if (i >= pp.fp8_lo && i < pp.fp8_hi)
+        return __float2half_rn(__fmul_rn(e4m3_round(__fmul_rn(x, kFp8WeightScale)), 1.0f / kFp8WeightScale));
     return __float2half_rn(x);
 }
 
 __global__ void __launch_bounds__(256) k_adam(float *__restrict__ params, __half *__restrict__ params_h,
                                               float *__restrict__ m, float *__restrict__ v,
                                               const float *__restrict__ grad, uint32_t n, float lr_t, float beta1,
-                                              float beta2, float eps, float l2_reg, float grad_scale, uint32_t n_bf16)
+                                              float beta2, float eps, float l2_reg, float grad_scale,
+                                              const ParamPrecision pp)
 {
     const float omb1 = __fsub_rn(1.0f, beta1), omb2 = __fsub_rn(1.0f, beta2);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -741,14 +746,14 @@ __global__ void __launch_bounds__(256) k_adam(float *__restrict__ params, __half
         v[i] = vi;
         const float nw = __fsub_rn(w, __fmul_rn(lr_t, __fdiv_rn(mi, __fadd_rn(__fsqrt_rn(vi), eps))));
         params[i] = nw;
-        params_h[i] = to_param16(nw, i, n_bf16);
+        params_h[i] = to_param16(nw, i, pp);
     }
 }
 
-__global__ void k_to_half(const float *__restrict__ p, __half *__restrict__ h, uint32_t n, uint32_t n_bf16)
+__global__ void k_to_half(const float *__restrict__ p, __half *__restrict__ h, uint32_t n, const ParamPrecision pp)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        h[i] = to_param16(p[i], i, n_bf16);
+        h[i] = to_param16(p[i], i, pp);
 }
 
 __global__ void k_scale(float *__restrict__ p, size_t n, float s)
@@ -792,7 +797,7 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
 cudaError_t launch_train_forward_backward(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                                           const LossConsts &lc, const float *positions, const float *targets,
                                           uint32_t n, __half *acts, __half *dz, float *grad, float *loss_sum,
-                                          float *sample_loss, bool bf16, int num_sms, cudaStream_t s)
+                                          float *sample_loss, bool bf16, bool fp8, int num_sms, cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
@@ -810,6 +815,7 @@ cudaError_t launch_train_forward_backward(const __half *params_h, const GridPara
     a.grid_grad = reinterpret_cast<float2 *>(grad + n_network_params);
     a.loss_sum = loss_sum;
     a.sample_loss = sample_loss;
+    a.fp8 = fp8 ? 1u : 0u;
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
     const size_t smem = sizeof(GridParams) + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half);
@@ -880,7 +886,7 @@ cudaError_t launch_scale(float *data, size_t n, float scale, cudaStream_t s)
 }
 
 cudaError_t launch_adam(float *params, __half *params_h, float *m, float *v, const float *grad, uint32_t n, float lr_t,
-                        float beta1, float beta2, float eps, float l2_reg, float grad_scale, uint32_t n_bf16,
+                        float beta1, float beta2, float eps, float l2_reg, float grad_scale, const ParamPrecision &pp,
                         cudaStream_t s)
 {
     if (n == 0)
@@ -888,18 +894,19 @@ cudaError_t launch_adam(float *params, __half *params_h, float *m, float *v, con
     uint32_t blocks = (n + 255u) / 256u;
     if (blocks > 8192u)
         blocks = 8192u;
-    k_adam<<<blocks, 256, 0, s>>>(params, params_h, m, v, grad, n, lr_t, beta1, beta2, eps, l2_reg, grad_scale, n_bf16);
+    k_adam<<<blocks, 256, 0, s>>>(params, params_h, m, v, grad, n, lr_t, beta1, beta2, eps, l2_reg, grad_scale, pp);
     return cudaGetLastError();
 }
 
-cudaError_t launch_params_to_half(const float *params, __half *params_h, uint32_t n, uint32_t n_bf16, cudaStream_t s)
+cudaError_t launch_params_to_half(const float *params, __half *params_h, uint32_t n, const ParamPrecision &pp,
+                                  cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
     uint32_t blocks = (n + 255u) / 256u;
     if (blocks > 8192u)
         blocks = 8192u;
-    k_to_half<<<blocks, 256, 0, s>>>(params, params_h, n, n_bf16);
+    k_to_half<<<blocks, 256, 0, s>>>(params, params_h, n, pp);
     return cudaGetLastError();
 }
 

@@ -87,8 +87,9 @@ void validate_config(const nbvh_config &c)
         fail(NBVH_EINVAL, "n_neurons must be 64");
     if (c.network.n_hidden_layers < 1 || c.network.n_hidden_layers > (int)kMaxHiddenLayers)
         fail(NBVH_EINVAL, "n_hidden_layers must be in [1, 8]");
-    if (c.network.precision != NBVH_PRECISION_FP16 && c.network.precision != NBVH_PRECISION_BF16)
-        fail(NBVH_EINVAL, "network precision must be NBVH_PRECISION_FP16 or NBVH_PRECISION_BF16");
+    if (c.network.precision != NBVH_PRECISION_FP16 && c.network.precision != NBVH_PRECISION_BF16 &&
+        c.network.precision != NBVH_PRECISION_FP8)
+        fail(NBVH_EINVAL, "network precision must be NBVH_PRECISION_FP16, _BF16 or _FP8");
     if (c.batch_size == 0 || (c.batch_size & (c.batch_size - 1u)) != 0)
         fail(NBVH_EINVAL, "batch_size must be a power of two");
     if (c.bvh.log2_bvh_max_traversals != 0)
@@ -319,6 +320,19 @@ namespace {
 // The MLP runs in BF16 (else FP16); its matrices are the first n_network_params parameters.
 bool mlp_bf16(const nbvh_handle *h) { return h->cfg.network.precision == NBVH_PRECISION_BF16; }
 uint32_t n_bf16_params(const nbvh_handle *h) { return mlp_bf16(h) ? h->layout.n_network_params : 0u; }
+// nbvh_precision of the MLP
+uint32_t mlp_prec(const nbvh_handle *h) { return (uint32_t)h->cfg.network.precision; }
+// FP32 master -> 16-bit copy: BF16 network in BF16 mode; in FP8 mode the hidden 64x64 matrices as
+// FP8-E4M3 values (they follow the first matrix, 64 x n_inputs)
+ParamPrecision param_precision(const nbvh_handle *h)
+{
+    ParamPrecision pp{n_bf16_params(h), 0u, 0u};
+    if (h->cfg.network.precision == NBVH_PRECISION_FP8) {
+        pp.fp8_lo = kNeurons * h->layout.n_inputs;
+        pp.fp8_hi = pp.fp8_lo + ((uint32_t)h->cfg.network.n_hidden_layers - 1u) * kNeurons * kNeurons;
+    }
+    return pp;
+}
 
 void upload_params(nbvh_handle *h, const float *params, bool reset_adam)
 {
@@ -326,7 +340,7 @@ void upload_params(nbvh_handle *h, const float *params, bool reset_adam)
     cuda_check(h->d_params.resize(n), "alloc params");
     cuda_check(h->d_params_h.resize(n), "alloc fp16 params");
     cuda_check(cudaMemcpy(h->d_params.ptr, params, (size_t)n * sizeof(float), cudaMemcpyHostToDevice), "upload params");
-    cuda_check(launch_params_to_half(h->d_params.ptr, h->d_params_h.ptr, n, n_bf16_params(h), nullptr), "to half");
+    cuda_check(launch_params_to_half(h->d_params.ptr, h->d_params_h.ptr, n, param_precision(h), nullptr), "to half");
     if (reset_adam) {
         cuda_check(h->d_adam_m.resize(n), "alloc adam m");
         cuda_check(h->d_adam_v.resize(n), "alloc adam v");
@@ -429,7 +443,7 @@ void neural_query_noalloc(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, ui
                                      (uint32_t)h->neural_nodes.size(), h->any_non_neural ? h->d_non_neural.ptr : nullptr,
                                      h->d_params_h.ptr, h->grid, nc, (uint32_t)h->cfg.network.n_hidden_layers, d_rays,
                                      n, d_hits, sc.counters, sc.fallback_list, sc.lists, sc.wave_counts, res,
-                                     mlp_bf16(h), h->num_sms, s, &launches),
+                                     mlp_prec(h), h->num_sms, s, &launches),
                    "neural query");
         if (h->any_non_neural || h->cfg.fallback_margin > 0.f)
             cuda_check(launch_classic_fallback(h->d_nodes.ptr, h->d_tris.ptr, d_rays, sc.fallback_list, sc.counters,
@@ -1100,7 +1114,7 @@ nbvh_status nbvh_network_inference(nbvh_handle *h, const float *d_positions, uin
         cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
         cuda_check(cudaEventRecord(h->ev0, s), "event");
         cuda_check(launch_network_inference(h->d_params_h.ptr, h->grid, (uint32_t)h->cfg.network.n_hidden_layers,
-                                            d_positions, n, d_outputs, mlp_bf16(h), h->num_sms, s),
+                                            d_positions, n, d_outputs, mlp_prec(h), h->num_sms, s),
                    "network inference");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
         h->last_launches = 1;
@@ -1128,7 +1142,7 @@ nbvh_status nbvh_mlp_inference(nbvh_handle *h, const uint16_t *d_features, uint3
         TensorMapBytes map;
         cuda_check(make_feature_map(reinterpret_cast<const __half *>(d_features), ni, n, &map), "feature map");
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-        cuda_check(launch_mlp_tc(map, h->d_wpacked.ptr, ni, H, n, nullptr, d_outputs, h->d_status.ptr, mlp_bf16(h),
+        cuda_check(launch_mlp_tc(map, h->d_wpacked.ptr, ni, H, n, nullptr, d_outputs, h->d_status.ptr, mlp_prec(h),
                                  h->num_sms, s),
                    "tensor-core MLP");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
@@ -1164,7 +1178,8 @@ void gradients_into_workspace(nbvh_handle *h, const float *d_pos, const float *d
     cuda_check(cudaMemsetAsync(h->d_grad.ptr, 0, (size_t)h->layout.n_params * sizeof(float), s), "zero grad");
     cuda_check(launch_train_forward_backward(h->d_params_h.ptr, h->grid, H, make_loss_consts(h->cfg, n), d_pos, d_tgt, n,
                                              h->d_train_acts.ptr, h->d_train_dz.ptr, h->d_grad.ptr, loss_slot,
-                                             h->d_train_loss.ptr, mlp_bf16(h), h->num_sms, s),
+                                             h->d_train_loss.ptr, mlp_bf16(h),
+                                             h->cfg.network.precision == NBVH_PRECISION_FP8, h->num_sms, s),
                "forward/backward");
     cuda_check(launch_weight_gradients(h->grid, H, h->d_train_acts.ptr, h->d_train_dz.ptr, n, h->d_grad.ptr,
                                        mlp_bf16(h), h->num_sms, s),
@@ -1203,7 +1218,7 @@ nbvh_status nbvh_adam_step(nbvh_handle *h, const float *d_gradients, nbvh_stream
         const nbvh_config &c = h->cfg;
         cuda_check(launch_adam(h->d_params.ptr, h->d_params_h.ptr, h->d_adam_m.ptr, h->d_adam_v.ptr, d_gradients,
                                h->layout.n_params, adam_step_size(c, h->training_step), c.optimizer.beta1,
-                               c.optimizer.beta2, c.optimizer.epsilon, c.optimizer.l2_reg, 1.0f, n_bf16_params(h),
+                               c.optimizer.beta2, c.optimizer.epsilon, c.optimizer.l2_reg, 1.0f, param_precision(h),
                                reinterpret_cast<cudaStream_t>(stream)),
                    "adam");
         h->training_step++;
@@ -1256,7 +1271,7 @@ nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_sta
             lr_t = adam_step_size(c, h->training_step);
             cuda_check(launch_adam(h->d_params.ptr, h->d_params_h.ptr, h->d_adam_m.ptr, h->d_adam_v.ptr, h->d_grad.ptr,
                                    h->layout.n_params, lr_t, c.optimizer.beta1, c.optimizer.beta2, c.optimizer.epsilon,
-                                   c.optimizer.l2_reg, 1.0f / c.optimizer.loss_scale, n_bf16_params(h), s),
+                                   c.optimizer.l2_reg, 1.0f / c.optimizer.loss_scale, param_precision(h), s),
                        "adam");
             if (h->cut.active)
                 tree_cut_after_step(h, h->d_train_loss.ptr, n, s);
@@ -1760,7 +1775,7 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
     cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),
                                  h->any_non_neural ? h->d_non_neural.ptr : nullptr, h->d_params_h.ptr, h->grid, nc,
                                  (uint32_t)h->cfg.network.n_hidden_layers, d_rays, n, d_hits, counters, list, lists,
-                                 q.wave_counts.ptr, res, mlp_bf16(h), h->num_sms, s, &launches),
+                                 q.wave_counts.ptr, res, mlp_prec(h), h->num_sms, s, &launches),
                "neural query");
     if (tune && tune->capture_only)
         return launches; // the rest runs after the captured part is replayed

@@ -405,6 +405,12 @@ struct alignas(64) TensorMapBytes {
 // and the host words the end-of-batch check copies the 4 wave counters into (pinned, with ev
 // recorded after the copy; when ev is null, h_words may be pageable and the host waits on the
 // stream instead).
+// How the FP32 master parameters become the 16-bit copy the kernels read.
+struct ParamPrecision {
+    uint32_t n_bf16; // the first n_bf16 parameters as BF16
+    uint32_t fp8_lo, fp8_hi; // these as FP8-E4M3 values (scale 2^6) in FP16
+};
+
 struct StepResources {
     __half *features;
     float *outputs;
@@ -473,7 +479,7 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
                               const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
                               const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
                               nbvh_neural_hit *hits, QueryCounters *counters, uint32_t *fallback_list,
-                              const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, bool bf16,
+                              const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, uint32_t prec,
                               int num_sms, cudaStream_t s, uint32_t *launches);
 
 cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, const NeuralConsts &nc,
@@ -481,7 +487,7 @@ cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, c
                             uint32_t *counts, cudaStream_t s);
 
 cudaError_t launch_network_inference(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
-                                     const float *positions, uint32_t n, float *outputs, bool bf16, int num_sms,
+                                     const float *positions, uint32_t n, float *outputs, uint32_t prec, int num_sms,
                                      cudaStream_t s);
 
 // tcgen05 fully fused MLP (k_mlp_tc.cu): weights packed into the tensor-core operand layout, then
@@ -496,7 +502,7 @@ cudaError_t launch_pack_weights(const __half *params_h, uint32_t n_inputs, uint3
 cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t rows, TensorMapBytes *out);
 cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
                           uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
-                          uint32_t *status, bool bf16, int num_sms, cudaStream_t s, bool configure = true);
+                          uint32_t *status, uint32_t prec, int num_sms, cudaStream_t s, bool configure = true);
 
 cudaError_t launch_encode(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                           const float *positions, uint32_t n, float *features, cudaStream_t s);
@@ -543,7 +549,7 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
 cudaError_t launch_train_forward_backward(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                                           const LossConsts &lc, const float *positions, const float *targets,
                                           uint32_t n, __half *acts, __half *dz, float *grad,
-                                          float *loss_sum, float *sample_loss, bool bf16, int num_sms,
+                                          float *loss_sum, float *sample_loss, bool bf16, bool fp8, int num_sms,
                                           cudaStream_t s);
 
 cudaError_t launch_weight_gradients(const GridParams &grid, uint32_t n_hidden_layers, const __half *acts,
@@ -564,11 +570,13 @@ cudaError_t launch_scale(float *data, size_t n, float scale, cudaStream_t s);
 
 cudaError_t launch_adam(float *params, __half *params_h, float *m, float *v, const float *grad, uint32_t n,
                         float lr_t, float beta1, float beta2, float eps, float l2_reg, float grad_scale,
-                        uint32_t n_bf16, cudaStream_t s);
+                        const ParamPrecision &pp, cudaStream_t s);
 
-// 16-bit copy of the FP32 parameters: the first n_bf16 (the network matrices when the MLP runs in
-// BF16) as BF16, the rest as FP16.
-cudaError_t launch_params_to_half(const float *params, __half *params_h, uint32_t n, uint32_t n_bf16, cudaStream_t s);
+// 16-bit copy of the FP32 parameters: the first pp.n_bf16 (the network matrices when the MLP runs
+// in BF16) as BF16, [pp.fp8_lo, pp.fp8_hi) (the hidden matrices in FP8 mode) as FP8-E4M3 values at
+// scale 2^6 held in FP16, the rest as FP16.
+cudaError_t launch_params_to_half(const float *params, __half *params_h, uint32_t n, const ParamPrecision &pp,
+                                  cudaStream_t s);
 
 cudaError_t launch_camera_rays(uint32_t width, uint32_t height, uint32_t sample_idx, uint32_t sample_offset,
                                const float *origin, const float *du, const float *dv, const float *top_left,

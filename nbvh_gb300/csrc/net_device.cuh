@@ -164,16 +164,19 @@ __device__ __forceinline__ float2 encode_level(const uint32_t *__restrict__ tabl
 }
 
 // Rebuilds the 16-bit A fragments of the next layer from the FP32 accumulators (after ReLU).
+// (fp8: the activations go through FP8-E4M3 first, the input format of the hidden matrices in FP8
+// mode; E4M3 values are exact in FP16.)
 template <bool BF16>
-__device__ __forceinline__ void relu_pack(const float (&acc)[8][4], uint32_t (&a)[4][4])
+__device__ __forceinline__ void relu_pack(const float (&acc)[8][4], uint32_t (&a)[4][4], bool fp8 = false)
 {
     using Pr = MlpPrec<BF16>;
+    auto act = [fp8](float x) { return fp8 ? fp8_act(fmaxf(x, 0.f)) : fmaxf(x, 0.f); };
 #pragma unroll
     for (int kb = 0; kb < 4; kb++) {
-        a[kb][0] = Pr::pack(fmaxf(acc[2 * kb][0], 0.f), fmaxf(acc[2 * kb][1], 0.f));
-        a[kb][1] = Pr::pack(fmaxf(acc[2 * kb][2], 0.f), fmaxf(acc[2 * kb][3], 0.f));
-        a[kb][2] = Pr::pack(fmaxf(acc[2 * kb + 1][0], 0.f), fmaxf(acc[2 * kb + 1][1], 0.f));
-        a[kb][3] = Pr::pack(fmaxf(acc[2 * kb + 1][2], 0.f), fmaxf(acc[2 * kb + 1][3], 0.f));
+        a[kb][0] = Pr::pack(act(acc[2 * kb][0]), act(acc[2 * kb][1]));
+        a[kb][1] = Pr::pack(act(acc[2 * kb][2]), act(acc[2 * kb][3]));
+        a[kb][2] = Pr::pack(act(acc[2 * kb + 1][0]), act(acc[2 * kb + 1][1]));
+        a[kb][3] = Pr::pack(act(acc[2 * kb + 1][2]), act(acc[2 * kb + 1][3]));
     }
 }
 
@@ -182,7 +185,7 @@ __device__ __forceinline__ void relu_pack(const float (&acc)[8][4], uint32_t (&a
 // those of row g + 8 (g = lane / 4, tig = lane % 4), for output columns 0..7.
 template <bool BF16, typename AMaker>
 __device__ __forceinline__ void mlp_forward_tile(const __half *sw, uint32_t n_inputs, uint32_t n_hidden_layers,
-                                                 AMaker &&make_a, float (&o)[4])
+                                                 AMaker &&make_a, float (&o)[4], bool fp8 = false)
 {
     using Pr = MlpPrec<BF16>;
     const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
@@ -206,7 +209,7 @@ __device__ __forceinline__ void mlp_forward_tile(const __half *sw, uint32_t n_in
     const __half *wl = sw + L.hidden_off;
     for (uint32_t layer = 1; layer < n_hidden_layers; layer++) {
         uint32_t a[4][4];
-        relu_pack<BF16>(acc, a);
+        relu_pack<BF16>(acc, a, fp8);
 #pragma unroll
         for (int nt = 0; nt < 8; nt++)
             acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
@@ -287,12 +290,13 @@ __device__ __forceinline__ void encode_tile_to_smem(const uint32_t *__restrict__
 // MLP phase of a 16-row tile whose 16-bit features are in feat[16][ld]; outputs as mlp_forward_tile.
 template <bool BF16>
 __device__ __forceinline__ void mlp_tile_from_smem(const __half *sw, const __half *feat, uint32_t ld,
-                                                   uint32_t n_inputs, uint32_t n_hidden_layers, float (&o)[4])
+                                                   uint32_t n_inputs, uint32_t n_hidden_layers, float (&o)[4],
+                                                   bool fp8 = false)
 {
     const int lane = threadIdx.x & 31;
     const __half *arow = feat + ((lane & 7) + ((lane >> 3) & 1) * 8) * ld + (lane >> 4) * 8;
     auto make_a = [&](uint32_t kb, uint32_t(&a)[4]) { ldsm_x4(a, arow + kb * 16u); };
-    mlp_forward_tile<BF16>(sw, n_inputs, n_hidden_layers, make_a, o);
+    mlp_forward_tile<BF16>(sw, n_inputs, n_hidden_layers, make_a, o, fp8);
 }
 
 // Encoded segment points along [po, pi] (neural_bvh_module_kernels.cu:57-96).

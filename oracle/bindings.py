@@ -46,7 +46,7 @@ class Network(C.Structure):
                 ("n_neurons", C.c_uint32), ("n_hidden_layers", C.c_uint32), ("level_offset", C.c_void_p),
                 ("level_size", C.c_void_p), ("level_resolution", C.c_void_p), ("level_scale", C.c_void_p),
                 ("grid_f16", C.c_void_p), ("weights_f16", C.c_void_p), ("exact", C.c_int32),
-                ("grid_f32", C.c_void_p), ("weights_f32", C.c_void_p), ("bf16", C.c_int32)]
+                ("grid_f32", C.c_void_p), ("weights_f32", C.c_void_p), ("bf16", C.c_int32), ("fp8", C.c_int32)]
 
 
 class NeuralScene(C.Structure):
@@ -223,7 +223,8 @@ class Oracle:
 
     def network(self, cfg, layout, params, exact=False):
         """Network struct over FP32 parameters: the network matrices rounded to the configured MLP
-        precision (FP16, or BF16 when cfg.network.precision is 1) and the grid to FP16, unless exact."""
+        precision (FP16; BF16 when cfg.network.precision is 1; FP8-E4M3 hidden matrices and their
+        inputs when it is 2) and the grid to FP16, unless exact."""
         params = np.ascontiguousarray(params, np.float32)
         nl = layout.n_levels
         off = np.array(layout.level_offset[:nl], np.uint32)
@@ -249,6 +250,7 @@ class Oracle:
         net.exact = 1 if exact else 0
         net.grid_f32, net.weights_f32 = _p(g32).value, _p(w32).value
         net.bf16 = 1 if bf16 else 0
+        net.fp8 = 1 if int(cfg.network.precision) == 2 else 0
         return net
 
     # ---- queries ----
@@ -328,6 +330,12 @@ class Oracle:
                                                 C.c_uint32(training_step), C.c_uint32(batch_size), C.c_uint32(n),
                                                 _p(pos), _p(tgt), _p(nodes), C.byref(rr))
         return pos, tgt, nodes
+
+    def e4m3_round(self, x):
+        f = self.lib.orc_e4m3_round
+        f.restype = C.c_float
+        f.argtypes = [C.c_float]
+        return np.array([f(float(v)) for v in np.asarray(x, np.float32).ravel()], np.float32)
 
     def loss_heuristic(self, stats):
         st = np.ascontiguousarray(stats, np.uint32).reshape(-1, 4)

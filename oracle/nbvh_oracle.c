@@ -593,11 +593,44 @@ static inline float round_bf16(float x) { return orc_bf16_to_f32(orc_f32_to_bf16
 
 /* rounding of an MLP operand in the network's precision */
 static inline float round_mlp(const orc_network *net, float x) { return net->bf16 ? round_bf16(x) : round_f16(x); }
+
+/* FP8 E4M3: 4 exponent bits (bias 7), 3 mantissa bits, max 448, no infinity */
+float orc_e4m3_round(float x)
+{
+    uint32_t b = f2u(x);
+    const uint32_t sign = b & 0x80000000u;
+    uint32_t a = b & 0x7FFFFFFFu;
+    if (a > 0x7F800000u)
+        return x;
+    float r;
+    if (a >= 0x43E00000u) {
+        r = u2f(0x43E00000u);
+    } else if (a < 0x3C800000u) {
+        r = rintf(u2f(a) * 512.0f) * (1.0f / 512.0f);
+    } else {
+        const uint32_t lsb = (a >> 20) & 1u;
+        a = (a + 0x7FFFFu + lsb) & 0xFFF00000u;
+        if (a > 0x43E00000u)
+            a = 0x43E00000u;
+        r = u2f(a);
+    }
+    return u2f(f2u(r) | sign);
+}
+
+/* index range of the hidden 64x64 matrices in the network parameters */
+static inline int fp8_weight(const orc_network *net, size_t i)
+{
+    const size_t lo = (size_t)net->n_neurons * net->n_inputs;
+    const size_t hi = lo + (size_t)(net->n_hidden_layers - 1u) * net->n_neurons * net->n_neurons;
+    return net->fp8 && i >= lo && i < hi;
+}
 static inline float net_round(const orc_network *net, float x) { return net->exact ? x : round_mlp(net, x); }
 static inline float net_w(const orc_network *net, size_t i)
 {
     if (net->exact)
         return net->weights_f32[i];
+    if (fp8_weight(net, i))
+        return orc_e4m3_round(net->weights_f32[i] * 64.0f) * (1.0f / 64.0f);
     return net->bf16 ? orc_bf16_to_f32(net->weights_f16[i]) : orc_f16_to_f32(net->weights_f16[i]);
 }
 static inline float net_g(const orc_network *net, size_t i)
@@ -728,6 +761,9 @@ static void mlp_row(const orc_network *net, const float *x_in, float *out, float
                 if (pre_out)
                     pre_out[r] = acc;
                 out[r] = (float)(1.0 / (1.0 + exp(-acc)));
+            } else if (net->fp8 && !net->exact && m + 2u < nm) {
+                /* input of a hidden matrix (m + 1 <= nm - 2) in FP8 mode */
+                b[r] = orc_e4m3_round((acc > 0.0 ? (float)acc : 0.0f) * 128.0f) * (1.0f / 128.0f);
             } else {
                 b[r] = net_round(net, acc > 0.0 ? (float)acc : 0.0f);
             }

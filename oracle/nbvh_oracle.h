@@ -90,7 +90,14 @@ typedef struct orc_network {
      * (weights_f16 holds BF16 bits; encoded features, hidden activations and backward gradients are
      * rounded to BF16). The grid table is FP16 either way. */
     int32_t bf16;
+    /* FP8 mode (MLP operands FP16 otherwise): the hidden 64x64 matrices hold FP8-E4M3 values at
+     * scale 2^6 (e4m3(w * 64) / 64 of the FP32 weights) and the activations entering them are
+     * FP8-E4M3 values at scale 2^7 (e4m3(a * 128) / 128). */
+    int32_t fp8;
 } orc_network;
+
+/* Nearest FP8-E4M3 value (ties to even, saturating at +-448, subnormals on the 2^-9 grid). */
+float orc_e4m3_round(float x);
 
 void orc_grid_layout(uint32_t n_levels, uint32_t log2_hashmap_size, uint32_t base_resolution,
                      float per_level_scale, uint32_t *offset, uint32_t *size, uint32_t *resolution,

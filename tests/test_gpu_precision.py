@@ -1,4 +1,4 @@
-"""BF16 network precision on the GPU against the oracle in the same precision.
+"""BF16 and FP8 network precision on the GPU against the oracle in the same precision.
 
 With network.precision = BF16 the network matrices, the encoded inputs, the hidden activations
 and the backward pass's activation gradients are bfloat16 (FP32 accumulation, FP32 master
@@ -116,6 +116,84 @@ def test_bf16_gradients_match_oracle(scene, oracle):
 
 def test_bf16_training_lowers_loss(built):
     cfg = nb.default_config(batch_size=1 << 14, **BF16)
+    h, s = handle(cfg, kind="sphere4k", seed=2, depth=6)
+    try:
+        first = h.run_optimisation(20).mean_loss
+        h.run_optimisation(300)
+        last = h.run_optimisation(20).mean_loss
+        assert last < 0.7 * first
+    finally:
+        h.close()
+
+
+# ---------------------------------------------------------------------------------------------
+# FP8: hidden 64x64 matrices as FP8-E4M3 values (scale 2^6) and their inputs rounded to E4M3, on
+# the FP16 tensor-core paths (E4M3 values are exact in FP16; activations at scale 2^7). E4M3 keeps 3 mantissa bits: an
+# activation that sits at a rounding boundary can round one step (6-12%) apart under FP32 vs FP64
+# accumulation, so the bars are: outputs within 0.25 absolute and 99% within 1e-2.
+# ---------------------------------------------------------------------------------------------
+
+FP8 = {"network.precision": 2}
+
+
+@pytest.fixture(scope="module")
+def scene8(built):
+    h, s = handle(nb.default_config(**FP8), kind="sphere65k", seed=1, albedo=True)
+    rng = np.random.default_rng(0)
+    p = h.params()
+    nn = h.layout.n_network_params
+    p[:nn] *= 2.5
+    p[nn:] = rng.uniform(-1.0, 1.0, p.size - nn).astype(np.float32)
+    h.set_params(p)
+    s["params"] = p
+    yield h, s
+    h.close()
+
+
+def test_fp8_network_inference(scene8, oracle):
+    h, s = scene8
+    pos = np.random.default_rng(4).uniform(0.0, 1.0, (8192, h.cfg.module.input_segment_points, 3)).astype(np.float32)
+    got = h.network_inference(_cuda(pos)).cpu().numpy()
+    ref = oracle.network_inference(oracle.network(h.cfg, h.layout, s["params"]), pos, threads=8)[:, :8]
+    assert ref.std() > 0.05
+    _close(got, ref, worst=0.25, tight=1e-2, frac=0.99)
+    # FP8 is not FP16: the same parameters in FP16 answer differently
+    ref16 = oracle.network_inference(oracle.network(nb.default_config(), h.layout, s["params"]), pos, threads=8)[:, :8]
+    assert np.abs(ref16 - ref).max() > 1e-2
+
+
+def test_fp8_tensor_core_mlp(scene8, oracle):
+    h, s = scene8
+    pos = np.random.default_rng(5).uniform(0.0, 1.0, (5003, h.cfg.module.input_segment_points, 3)).astype(np.float32)
+    feats = h.encode(_cuda(pos)).to(torch.float16).contiguous()
+    got = h.mlp_inference(feats).cpu().numpy()
+    ref = oracle.network_inference(oracle.network(h.cfg, h.layout, s["params"]), pos, threads=8)[:, :8]
+    _close(got, ref, worst=0.25, tight=1e-2, frac=0.99)
+    # the tcgen05 path and the mma.sync path round the same values
+    _close(got, h.network_inference(_cuda(pos)).cpu().numpy(), worst=0.25, tight=1e-2, frac=0.99)
+
+
+def test_fp8_query_matches_oracle(scene8, oracle):
+    h, s = scene8
+    rays = scenes.uniform_rays(1 << 14, s["bbox"][:3], s["bbox"][3:], seed=43)
+    got = as_u32(h.query_closest_neural(_cuda(rays)))
+    net = oracle.network(h.cfg, h.layout, s["params"])
+    consts = oracle.neural_consts(h.cfg)
+    nscene = oracle.neural_scene(s["neural"], s["bbox"])
+    ref = oracle.neural_query(nscene, net, consts, rays, threads=8)
+    cs = oracle.classic_scene(s["nodes"], s["prims"], s["v"], s["f"])
+    border = (oracle.neural_query(nscene, net, consts, rays, classic=cs, fallback_margin=5e-2, threads=8)[:, 8] & 2) != 0
+    differ = (got[:, 8] & 1) != (ref[:, 8] & 1)
+    assert (differ & ~border).mean() < 5e-3
+    both = ((got[:, 8] & 1) == 1) & ((ref[:, 8] & 1) == 1) & ~border
+    assert both.sum() > 100
+    tg, tr = got[both, 0].view(np.float32), ref[both, 0].view(np.float32)
+    rel = np.abs(tg - tr) / np.maximum(np.abs(tr), 1e-6)
+    assert np.mean(rel <= 2e-2) > 0.98
+
+
+def test_fp8_training_lowers_loss(built):
+    cfg = nb.default_config(batch_size=1 << 14, **FP8)
     h, s = handle(cfg, kind="sphere4k", seed=2, depth=6)
     try:
         first = h.run_optimisation(20).mean_loss

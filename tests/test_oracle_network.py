@@ -133,3 +133,76 @@ def test_composite_loss_rules(oracle, built):
     # loss scale multiplies the gradient only
     v2, g2 = oracle.composite_loss(lc, pred, tgt, loss_scale=128.0)
     assert np.array_equal(v2, vals) and np.allclose(g2, grads * 128.0)
+
+
+def _e4m3_table():
+    """All finite FP8-E4M3 values, from their bit patterns (independent of the rounding code)."""
+    vals = []
+    for code in range(256):
+        s, e, m = code >> 7, (code >> 3) & 0xF, code & 7
+        if e == 15 and m == 7:
+            continue  # NaN
+        v = (m / 8.0) * 2.0 ** -6 if e == 0 else (1 + m / 8.0) * 2.0 ** (e - 7)
+        vals.append((-v if s else v, m & 1))
+    return vals
+
+
+def _e4m3_reference(x):
+    """Nearest E4M3 value, ties to the even mantissa, saturating at +-448."""
+    table = _e4m3_table()
+    out = np.empty_like(x)
+    for i, v in enumerate(x.astype(np.float64)):
+        if abs(v) >= 448.0:
+            out[i] = np.copysign(448.0, v)
+            continue
+        d = [(abs(v - t), odd, t) for t, odd in table]
+        best = min(d)[0]
+        cands = [(odd, t) for dist, odd, t in d if dist == best]
+        cands.sort()
+        out[i] = cands[0][1] if cands[0][1] != 0 or len(cands) == 1 else np.copysign(0.0, v)
+    return out
+
+
+def test_e4m3_rounding_matches_the_format(oracle, built):
+    rng = np.random.default_rng(8)
+    x = np.concatenate([
+        np.array([0.0, 1.0, 1.0625, 1.1875, 448.0, 464.0, 500.0, 1e9, 2.0 ** -6, 2.0 ** -10, 3 * 2.0 ** -10,
+                  2.0 ** -9, 0.0147, -3.3, -2.0 ** -8, 240.0, 255.9], np.float32),
+        (rng.standard_normal(400) * np.exp(rng.uniform(-9, 6, 400))).astype(np.float32)])
+    got = oracle.e4m3_round(x)
+    ref = _e4m3_reference(x).astype(np.float32)
+    assert np.array_equal(np.abs(got), np.abs(ref)), x[np.abs(got) != np.abs(ref)][:5]
+    assert np.all(np.sign(got[got != 0]) == np.sign(x[got != 0]))
+
+
+def test_fp8_forward_matches_rounded_numpy(oracle, built):
+    """FP8 mode: the hidden 64x64 matrices are FP8-E4M3 values at scale 2^6 and the activations
+    entering them are E4M3 values at scale 2^7; the first and last matrices stay FP16."""
+    cfg = small_cfg(**{"network.precision": 2})
+    L, p = random_params(cfg, seed=5)
+    net = oracle.network(cfg, L, p)
+    pos = np.random.default_rng(6).uniform(0, 1, (64, 2, 3)).astype(np.float32)
+    feats = oracle.encode(net, pos)
+    H = cfg.network.n_hidden_layers
+    x = feats.astype(np.float16).astype(np.float64)
+    off = 0
+    for m in range(H + 1):
+        rows = 16 if m == H else 64
+        cols = L.n_inputs if m == 0 else 64
+        w = p[off:off + rows * cols]
+        if 1 <= m <= H - 1:
+            w = oracle.e4m3_round(w * 64.0) / np.float32(64.0)
+        else:
+            w = w.astype(np.float16).astype(np.float32)
+        W = w.reshape(rows, cols).astype(np.float64)
+        off += rows * cols
+        x = x @ W.T
+        if m < H:
+            a = np.maximum(x, 0).astype(np.float32)
+            q = (oracle.e4m3_round(a * np.float32(128.0)) / np.float32(128.0)).reshape(a.shape)
+            x = (q if m + 1 <= H - 1 else a.astype(np.float16)).astype(np.float64)
+    ref = 1.0 / (1.0 + np.exp(-x))
+    out = oracle.network_inference(net, pos)
+    assert np.max(np.abs(out - ref)) < 1e-5
+    out16 = oracle.network_inference(oracle.network(small_cfg(), L, p), pos)
+    assert np.max(np.abs(out16 - out)) > 1e-3
