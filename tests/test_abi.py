@@ -74,9 +74,12 @@ def test_config_validation(built):
     lib = nb.load_library()
     L = abi.ParamLayout()
     for key, val in (("hashgrid.n_features_per_level", 4), ("network.n_neurons", 128), ("batch_size", 1000),
-                     ("module.input_segment_points", 5), ("network.precision", 2)):
+                     ("module.input_segment_points", 5), ("network.precision", 3)):
         cfg = nb.default_config(**{key: val})
         assert lib.nbvh_param_layout_host(C.byref(cfg), C.byref(L)) == abi.NBVH_EINVAL, key
+    for prec in (0, 1, 2):  # FP16, BF16, FP8
+        cfg = nb.default_config(**{"network.precision": prec})
+        assert lib.nbvh_param_layout_host(C.byref(cfg), C.byref(L)) == abi.NBVH_OK, prec
 
 
 def test_status_strings_and_null_handles(built):
