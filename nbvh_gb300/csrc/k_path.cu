@@ -153,158 +153,184 @@ __global__ void __launch_bounds__(256) k_pt_resolve(const __grid_constant__ Path
 
 // ---------------------------------------------------------------------------------------------
 // Instanced scenes: the rays of a bounce are tested against each instance's world box, the ones
-// that enter it are moved into the instance's object space and answered by its model's neural
-// query, and the closest hit over the instances is kept in world space.
+// that enter it are moved into the instance's object space (o' = A^-1 (o - b), d' = A^-1 d
+// normalised, t' = t * |A^-1 d|) and answered by its model's neural query, and the closest hit
+// over the instances is kept in world space.
 // ---------------------------------------------------------------------------------------------
 
-// World hit records of a bounce start as misses (no instance: reserved = ~0).
-__global__ void __launch_bounds__(256) k_inst_init(nbvh_neural_hit *hits, uint32_t n)
+// Batched by model: all (ray, instance) pairs of one model's instances in one list, answered by
+// one query of that model; the closest entry per world ray is chosen with a 64-bit atomic min of
+// (distance bits, entry index) and written by k_inst_finalize.
+__global__ void __launch_bounds__(256) k_inst_prepare_group(const InstanceArgs *__restrict__ group, uint32_t n_group,
+                                                            const nbvh_ray *rays, uint32_t n, nbvh_ray *obj_rays,
+                                                            uint32_t *obj_ids, float *obj_scale, uint32_t *obj_inst,
+                                                            uint32_t *count, uint32_t capacity)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
+    if (i < n) {
+        const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
+        ra = rp[0];
+        rb = rp[1];
+    }
+    const float o[3] = {ra.x, ra.y, ra.z}, d[3] = {rb.x, rb.y, rb.z};
+    for (uint32_t gi = 0; gi < n_group; gi++) {
+        const InstanceArgs &a = group[gi];
+        bool want = false;
+        nbvh_ray r{};
+        float sc = 1.0f;
+        if (i < n) {
+            float t0 = ra.w, t1 = rb.w;
+            bool hit = t0 < t1;
+            for (int k = 0; k < 3 && hit; k++) {
+                if (d[k] == 0.0f) {
+                    hit = o[k] >= a.box_min[k] && o[k] <= a.box_max[k];
+                } else {
+                    const float inv = 1.0f / d[k];
+                    float ta = (a.box_min[k] - o[k]) * inv, tb = (a.box_max[k] - o[k]) * inv;
+                    if (ta > tb) {
+                        const float t = ta;
+                        ta = tb;
+                        tb = t;
+                    }
+                    t0 = fmaxf(t0, ta);
+                    t1 = fminf(t1, tb);
+                    hit = t0 <= t1;
+                }
+            }
+            if (hit) {
+                want = true;
+                if (a.identity) {
+                    for (int k = 0; k < 3; k++) {
+                        r.o[k] = o[k];
+                        r.d[k] = d[k];
+                    }
+                } else {
+                    const float q[3] = {o[0] - a.xform[3], o[1] - a.xform[7], o[2] - a.xform[11]};
+                    float dd[3];
+                    for (int row = 0; row < 3; row++) {
+                        r.o[row] = a.inv[3 * row] * q[0] + a.inv[3 * row + 1] * q[1] + a.inv[3 * row + 2] * q[2];
+                        dd[row] = a.inv[3 * row] * d[0] + a.inv[3 * row + 1] * d[1] + a.inv[3 * row + 2] * d[2];
+                    }
+                    sc = sqrtf(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+                    for (int k = 0; k < 3; k++)
+                        r.d[k] = dd[k] / sc;
+                }
+                r.tmin = ra.w * sc;
+                r.tmax = FLT_MAX;
+            }
+        }
+        const uint32_t pos = warp_append(want, count);
+        if (want && pos < capacity) {
+            obj_rays[pos] = r;
+            obj_ids[pos] = i;
+            obj_scale[pos] = sc;
+            obj_inst[pos] = a.instance;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_inst_reset(unsigned long long *keys, nbvh_neural_hit *hits, uint32_t n)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
+    keys[i] = ~0ull;
     float4 *o = reinterpret_cast<float4 *>(hits + i);
     o[0] = make_float4(FLT_MAX, 0.f, 0.f, 0.f);
     o[1] = make_float4(0.f, 0.f, 0.f, 0.f);
     o[2] = make_float4(0.f, 0.f, __uint_as_float(0xFFFFFFFFu), __uint_as_float(0xFFFFFFFFu));
 }
 
-// Rays whose segment [tmin, closest hit so far) enters the instance's world box, moved into object
-// space (o' = A^-1 (o - b), d' = A^-1 d normalised; t' = t * |A^-1 d|) and listed with their world
-// index and scale.
-__global__ void __launch_bounds__(256) k_inst_prepare(const __grid_constant__ InstanceArgs a, const nbvh_ray *rays,
-                                                      uint32_t n, const nbvh_neural_hit *hits, nbvh_ray *obj_rays,
-                                                      uint32_t *obj_ids, float *obj_scale, uint32_t *count)
-{
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool want = false;
-    nbvh_ray r{};
-    float sc = 1.0f;
-    if (i < n) {
-        const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
-        const float4 ra = rp[0], rb = rp[1];
-        const float best = hits[i].t;
-        // slab test of the world box on [tmin, best)
-        float t0 = ra.w, t1 = fminf(best, rb.w);
-        const float o[3] = {ra.x, ra.y, ra.z}, d[3] = {rb.x, rb.y, rb.z};
-        bool hit = t0 < t1;
-        for (int k = 0; k < 3 && hit; k++) {
-            if (d[k] == 0.0f) {
-                hit = o[k] >= a.box_min[k] && o[k] <= a.box_max[k];
-            } else {
-                const float inv = 1.0f / d[k];
-                float ta = (a.box_min[k] - o[k]) * inv, tb = (a.box_max[k] - o[k]) * inv;
-                if (ta > tb) {
-                    const float t = ta;
-                    ta = tb;
-                    tb = t;
-                }
-                t0 = fmaxf(t0, ta);
-                t1 = fminf(t1, tb);
-                hit = t0 <= t1;
-            }
-        }
-        if (hit) {
-            want = true;
-            if (a.identity) {
-                r.o[0] = o[0];
-                r.o[1] = o[1];
-                r.o[2] = o[2];
-                r.d[0] = d[0];
-                r.d[1] = d[1];
-                r.d[2] = d[2];
-            } else {
-                const float q[3] = {o[0] - a.xform[3], o[1] - a.xform[7], o[2] - a.xform[11]};
-                float dd[3];
-                for (int row = 0; row < 3; row++) {
-                    r.o[row] = a.inv[3 * row] * q[0] + a.inv[3 * row + 1] * q[1] + a.inv[3 * row + 2] * q[2];
-                    dd[row] = a.inv[3 * row] * d[0] + a.inv[3 * row + 1] * d[1] + a.inv[3 * row + 2] * d[2];
-                }
-                sc = sqrtf(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
-                for (int k = 0; k < 3; k++)
-                    r.d[k] = dd[k] / sc;
-            }
-            r.tmin = ra.w * sc;
-            r.tmax = FLT_MAX;
-        }
-    }
-    const uint32_t pos = warp_append(want, count);
-    if (want) {
-        obj_rays[pos] = r;
-        obj_ids[pos] = i;
-        obj_scale[pos] = sc;
-    }
-}
-
-// The instance's answers merged into the world records: a valid hit closer than the record so far
-// replaces it (t back to world units, normal by the inverse transpose); segment counts add up.
-__global__ void __launch_bounds__(256) k_inst_merge(const __grid_constant__ InstanceArgs a,
-                                                    const nbvh_neural_hit *obj_hits, const uint32_t *obj_ids,
-                                                    const float *obj_scale, const uint32_t *count,
-                                                    nbvh_neural_hit *hits)
+__global__ void __launch_bounds__(256) k_inst_vote(const nbvh_neural_hit *obj_hits, const uint32_t *obj_ids,
+                                                   const float *obj_scale, uint32_t total, unsigned long long *keys,
+                                                   nbvh_neural_hit *hits)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= *count)
+    if (k >= total)
         return;
     const nbvh_neural_hit oh = obj_hits[k];
-    nbvh_neural_hit &w = hits[obj_ids[k]];
-    const uint32_t traversal_flags = NBVH_HIT_STEP_CAP | 0x8u; // step cap, stack overflow: kept from any instance
-    w.segments += oh.segments;
-    w.flags |= oh.flags & traversal_flags;
+    const uint32_t i = obj_ids[k];
+    atomicAdd(&hits[i].segments, oh.segments);
+    const uint32_t trav = oh.flags & (NBVH_HIT_STEP_CAP | 0x8u); // step cap, stack overflow: from any entry
+    if (trav)
+        atomicOr(&hits[i].flags, trav);
     if (!(oh.flags & NBVH_HIT_VALID))
         return;
     const float t = oh.t / obj_scale[k];
-    if (!(t < w.t))
+    const uint32_t b = __float_as_uint(t);
+    const uint32_t ord = (b & 0x80000000u) ? ~b : (b | 0x80000000u); // orders as the float
+    atomicMin(keys + i, ((unsigned long long)ord << 32) | k);
+}
+
+__global__ void __launch_bounds__(256) k_inst_finalize(const InstanceArgs *__restrict__ all, const nbvh_neural_hit *obj_hits,
+                                                       const float *obj_scale, const uint32_t *obj_inst,
+                                                       const unsigned long long *keys, uint32_t n, nbvh_neural_hit *hits)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
         return;
-    w.flags = (w.flags & traversal_flags) | oh.flags;
-    float n[3] = {oh.normal[0], oh.normal[1], oh.normal[2]};
+    const unsigned long long key = keys[i];
+    if (key == ~0ull)
+        return;
+    const uint32_t k = (uint32_t)(key & 0xFFFFFFFFull);
+    const nbvh_neural_hit oh = obj_hits[k];
+    const InstanceArgs &a = all[obj_inst[k]];
+    float nrm[3] = {oh.normal[0], oh.normal[1], oh.normal[2]};
     if (!a.identity) {
         float m[3];
         for (int row = 0; row < 3; row++) // inverse transpose: column `row` of A^-1
-            m[row] = a.inv[row] * n[0] + a.inv[3 + row] * n[1] + a.inv[6 + row] * n[2];
+            m[row] = a.inv[row] * nrm[0] + a.inv[3 + row] * nrm[1] + a.inv[6 + row] * nrm[2];
         const float len = sqrtf(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
         for (int c = 0; c < 3; c++)
-            n[c] = len > 0.f ? m[c] / len : m[c];
+            nrm[c] = len > 0.f ? m[c] / len : m[c];
     }
-    w.t = t;
-    w.normal[0] = n[0];
-    w.normal[1] = n[1];
-    w.normal[2] = n[2];
+    nbvh_neural_hit &w = hits[i];
+    const uint32_t ord = (uint32_t)(key >> 32);
+    w.t = __uint_as_float((ord & 0x80000000u) ? (ord & 0x7FFFFFFFu) : ~ord);
+    w.normal[0] = nrm[0];
+    w.normal[1] = nrm[1];
+    w.normal[2] = nrm[2];
     w.albedo[0] = oh.albedo[0];
     w.albedo[1] = oh.albedo[1];
     w.albedo[2] = oh.albedo[2];
     w.visibility = oh.visibility;
+    w.flags = (w.flags & (NBVH_HIT_STEP_CAP | 0x8u)) | oh.flags;
     w.prim = oh.prim;
     w.reserved = a.instance;
 }
 
 } // namespace
 
-cudaError_t launch_inst_init(nbvh_neural_hit *hits, uint32_t n, cudaStream_t s)
+cudaError_t launch_inst_group(const InstanceArgs *group, uint32_t n_group, const nbvh_ray *rays, uint32_t n,
+                              nbvh_ray *obj_rays, uint32_t *obj_ids, float *obj_scale, uint32_t *obj_inst,
+                              uint32_t *count, uint32_t capacity, cudaStream_t s)
 {
-    if (n == 0)
+    if (n == 0 || n_group == 0)
         return cudaSuccess;
-    k_inst_init<<<(n + 255u) / 256u, 256, 0, s>>>(hits, n);
+    k_inst_prepare_group<<<(n + 255u) / 256u, 256, 0, s>>>(group, n_group, rays, n, obj_rays, obj_ids, obj_scale,
+                                                           obj_inst, count, capacity);
     return cudaGetLastError();
 }
 
-cudaError_t launch_inst_prepare(const InstanceArgs &a, const nbvh_ray *rays, uint32_t n, const nbvh_neural_hit *hits,
-                                nbvh_ray *obj_rays, uint32_t *obj_ids, float *obj_scale, uint32_t *count,
-                                cudaStream_t s)
+cudaError_t launch_inst_reset(unsigned long long *keys, nbvh_neural_hit *hits, uint32_t n, cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
-    k_inst_prepare<<<(n + 255u) / 256u, 256, 0, s>>>(a, rays, n, hits, obj_rays, obj_ids, obj_scale, count);
+    k_inst_reset<<<(n + 255u) / 256u, 256, 0, s>>>(keys, hits, n);
     return cudaGetLastError();
 }
 
-cudaError_t launch_inst_merge(const InstanceArgs &a, const nbvh_neural_hit *obj_hits, const uint32_t *obj_ids,
-                              const float *obj_scale, const uint32_t *count, uint32_t max_count, nbvh_neural_hit *hits,
-                              cudaStream_t s)
+cudaError_t launch_inst_vote_finalize(const InstanceArgs *all, const nbvh_neural_hit *obj_hits, const uint32_t *obj_ids,
+                                      const float *obj_scale, const uint32_t *obj_inst, uint32_t total,
+                                      unsigned long long *keys, nbvh_neural_hit *hits, uint32_t n, cudaStream_t s)
 {
-    if (max_count == 0)
-        return cudaSuccess;
-    k_inst_merge<<<(max_count + 255u) / 256u, 256, 0, s>>>(a, obj_hits, obj_ids, obj_scale, count, hits);
+    if (total > 0)
+        k_inst_vote<<<(total + 255u) / 256u, 256, 0, s>>>(obj_hits, obj_ids, obj_scale, total, keys, hits);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || n == 0)
+        return e;
+    k_inst_finalize<<<(n + 255u) / 256u, 256, 0, s>>>(all, obj_hits, obj_scale, obj_inst, keys, n, hits);
     return cudaGetLastError();
 }
 

@@ -230,13 +230,15 @@ struct PathBuffers {
 cudaError_t launch_path_raygen(const PathArgs &a, cudaStream_t s);
 cudaError_t launch_path_shade(const PathArgs &a, uint32_t count_in, uint32_t bounce, cudaStream_t s);
 cudaError_t launch_path_resolve(const PathArgs &a, float *image, cudaStream_t s);
-cudaError_t launch_inst_init(nbvh_neural_hit *hits, uint32_t n, cudaStream_t s);
-cudaError_t launch_inst_prepare(const InstanceArgs &a, const nbvh_ray *rays, uint32_t n, const nbvh_neural_hit *hits,
-                                nbvh_ray *obj_rays, uint32_t *obj_ids, float *obj_scale, uint32_t *count,
-                                cudaStream_t s);
-cudaError_t launch_inst_merge(const InstanceArgs &a, const nbvh_neural_hit *obj_hits, const uint32_t *obj_ids,
-                              const float *obj_scale, const uint32_t *count, uint32_t max_count, nbvh_neural_hit *hits,
-                              cudaStream_t s);
+// (ray, instance) pairs of one model's instances (group, device array) appended to the object list
+cudaError_t launch_inst_group(const InstanceArgs *group, uint32_t n_group, const nbvh_ray *rays, uint32_t n,
+                              nbvh_ray *obj_rays, uint32_t *obj_ids, float *obj_scale, uint32_t *obj_inst,
+                              uint32_t *count, uint32_t capacity, cudaStream_t s);
+cudaError_t launch_inst_reset(unsigned long long *keys, nbvh_neural_hit *hits, uint32_t n, cudaStream_t s);
+// closest entry per world ray (64-bit atomic min of distance and entry) and its world record
+cudaError_t launch_inst_vote_finalize(const InstanceArgs *all, const nbvh_neural_hit *obj_hits, const uint32_t *obj_ids,
+                                      const float *obj_scale, const uint32_t *obj_inst, uint32_t total,
+                                      unsigned long long *keys, nbvh_neural_hit *hits, uint32_t n, cudaStream_t s);
 
 } // namespace nbvh
 

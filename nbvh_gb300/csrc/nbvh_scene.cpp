@@ -4,9 +4,10 @@
 // The reference renders one neural BLAS per scene and pre-transforms vertices instead of
 // instancing (src/cuda/neural/neural_bvh_renderer_init.cu:23-25, src/base/scene.cpp:38-44,225-226);
 // its TLAS (include/cuda/accel/tlas.cuh:123-324) walks BLAS roots. Here each bounce (or query)
-// tests its rays against every instance's world box, answers the rays that enter it with that
-// instance's model in object space, and keeps the closest hit in world space (k_path.cu: k_inst_*).
-// Scenes hold a few tens of instances, so the box tests are a flat loop rather than a tree.
+// tests its rays against every instance's world box, lists for each model the (ray, instance)
+// pairs whose ray enters one of its instances, answers each model's list with one neural query in
+// object space, and keeps the closest hit per ray in world space (k_path.cu: k_inst_*). Scenes
+// hold a few tens of instances, so the box tests are a flat loop rather than a tree.
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -42,6 +43,18 @@ struct nbvh_scene {
     DeviceBuffer<nbvh_neural_hit> obj_hits;
     DeviceBuffer<uint32_t> count;
     DeviceBuffer<nbvh_neural_hit> bounce_hits;
+    DeviceBuffer<uint32_t> obj_inst;
+    DeviceBuffer<unsigned long long> keys;
+    // instances grouped by model (one query per model and bounce), and all instances by id
+    struct Group {
+        nbvh_handle *model;
+        DeviceBuffer<InstanceArgs> args;
+        uint32_t n = 0;
+    };
+    std::vector<std::unique_ptr<Group>> groups;
+    DeviceBuffer<InstanceArgs> all_args;
+    bool groups_dirty = true;
+    size_t obj_capacity = 0;
     uint32_t *h_count = nullptr;
     QueryContext unused_q; // render_path_core takes a context; the scene's query brings its own
     PathBuffers path;
@@ -77,14 +90,23 @@ nbvh_status scene_guarded(nbvh_scene *sc, F &&f)
     }
 }
 
+void ensure_object_capacity(nbvh_scene *sc, size_t m)
+{
+    if (sc->obj_capacity >= m)
+        return;
+    cuda_check(sc->obj_rays.resize(m), "alloc object rays");
+    cuda_check(sc->obj_ids.resize(m), "alloc object ids");
+    cuda_check(sc->obj_scale.resize(m), "alloc object scales");
+    cuda_check(sc->obj_hits.resize(m), "alloc object hits");
+    cuda_check(sc->obj_inst.resize(m), "alloc object instances");
+    sc->obj_capacity = m;
+}
+
 void ensure_scene_buffers(nbvh_scene *sc, uint32_t n)
 {
-    if (sc->obj_rays.count < n) {
-        cuda_check(sc->obj_rays.resize(n), "alloc object rays");
-        cuda_check(sc->obj_ids.resize(n), "alloc object ids");
-        cuda_check(sc->obj_scale.resize(n), "alloc object scales");
-        cuda_check(sc->obj_hits.resize(n), "alloc object hits");
-    }
+    ensure_object_capacity(sc, n);
+    if (sc->keys.count < n)
+        cuda_check(sc->keys.resize(n), "alloc keys");
     if (sc->count.count < 1u)
         cuda_check(sc->count.resize(1u), "alloc count");
     if (!sc->h_count)
@@ -103,30 +125,77 @@ ModelContext &context_of(nbvh_scene *sc, nbvh_handle *model, uint32_t n)
     return *slot;
 }
 
+void upload_groups(nbvh_scene *sc)
+{
+    if (!sc->groups_dirty)
+        return;
+    sc->groups.clear();
+    std::vector<InstanceArgs> all;
+    std::map<nbvh_handle *, std::vector<InstanceArgs>> by_model;
+    std::vector<nbvh_handle *> order;
+    for (const auto &inst : sc->instances) {
+        all.push_back(inst.args);
+        if (!by_model.count(inst.model))
+            order.push_back(inst.model);
+        by_model[inst.model].push_back(inst.args);
+    }
+    cuda_check(sc->all_args.resize(all.size()), "alloc instances");
+    cuda_check(cudaMemcpy(sc->all_args.ptr, all.data(), all.size() * sizeof(InstanceArgs), cudaMemcpyHostToDevice),
+               "upload instances");
+    for (nbvh_handle *m : order) {
+        std::unique_ptr<nbvh_scene::Group> g(new nbvh_scene::Group());
+        g->model = m;
+        const auto &v = by_model[m];
+        g->n = (uint32_t)v.size();
+        cuda_check(g->args.resize(v.size()), "alloc instance group");
+        cuda_check(cudaMemcpy(g->args.ptr, v.data(), v.size() * sizeof(InstanceArgs), cudaMemcpyHostToDevice),
+                   "upload instance group");
+        sc->groups.push_back(std::move(g));
+    }
+    sc->groups_dirty = false;
+}
+
 // Closest hit over all instances for n world rays (device buffers); the record's `reserved` word
-// is the instance that gave it (~0: none).
+// is the instance that gave it (~0: none). Per model, every (ray, instance) pair whose ray enters
+// the instance's world box is listed and the whole list answered by one query of the model; the
+// closest entry per ray wins.
 void scene_query(nbvh_scene *sc, const nbvh_ray *d_rays, uint32_t n, uint32_t depth, nbvh_neural_hit *d_hits,
                  cudaStream_t s)
 {
     ensure_scene_buffers(sc, n);
-    cuda_check(launch_inst_init(d_hits, n, s), "init records");
-    for (const auto &inst : sc->instances) {
+    upload_groups(sc);
+    cuda_check(launch_inst_reset(sc->keys.ptr, d_hits, n, s), "reset records");
+    std::vector<uint32_t> start(sc->groups.size() + 1u, 0u);
+    for (int attempt = 0; attempt < 2; attempt++) {
         cuda_check(cudaMemsetAsync(sc->count.ptr, 0, sizeof(uint32_t), s), "reset count");
-        cuda_check(launch_inst_prepare(inst.args, d_rays, n, d_hits, sc->obj_rays.ptr, sc->obj_ids.ptr,
-                                       sc->obj_scale.ptr, sc->count.ptr, s),
-                   "instance rays");
-        cuda_check(cudaMemcpyAsync(sc->h_count, sc->count.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "count");
-        cuda_check(cudaStreamSynchronize(s), "sync");
-        const uint32_t m = *sc->h_count;
+        for (size_t gi = 0; gi < sc->groups.size(); gi++) {
+            const auto &g = *sc->groups[gi];
+            cuda_check(launch_inst_group(g.args.ptr, g.n, d_rays, n, sc->obj_rays.ptr, sc->obj_ids.ptr,
+                                         sc->obj_scale.ptr, sc->obj_inst.ptr, sc->count.ptr,
+                                         (uint32_t)sc->obj_capacity, s),
+                       "instance rays");
+            cuda_check(cudaMemcpyAsync(sc->h_count, sc->count.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s),
+                       "count");
+            cuda_check(cudaStreamSynchronize(s), "sync");
+            start[gi + 1u] = *sc->h_count;
+        }
+        if (start.back() <= sc->obj_capacity)
+            break;
+        // more (ray, instance) pairs than room (the kernel wrote only what fits): grow, list again
+        ensure_object_capacity(sc, (size_t)start.back() + start.back() / 4u);
+    }
+    for (size_t gi = 0; gi < sc->groups.size(); gi++) {
+        const uint32_t m = start[gi + 1u] - start[gi];
         if (m == 0)
             continue;
-        nbvh_handle *model = inst.model;
+        nbvh_handle *model = sc->groups[gi]->model;
         ModelContext &mc = context_of(sc, model, m);
-        run_neural_query(model, mc.q, mc.counters.ptr, sc->obj_rays.ptr, m, depth, false, sc->obj_hits.ptr, s);
-        cuda_check(launch_inst_merge(inst.args, sc->obj_hits.ptr, sc->obj_ids.ptr, sc->obj_scale.ptr, sc->count.ptr, m,
-                                     d_hits, s),
-                   "merge instance hits");
+        run_neural_query(model, mc.q, mc.counters.ptr, sc->obj_rays.ptr + start[gi], m, depth, false,
+                         sc->obj_hits.ptr + start[gi], s);
     }
+    cuda_check(launch_inst_vote_finalize(sc->all_args.ptr, sc->obj_hits.ptr, sc->obj_ids.ptr, sc->obj_scale.ptr,
+                                         sc->obj_inst.ptr, start.back(), sc->keys.ptr, d_hits, n, s),
+               "closest instance hits");
 }
 
 struct SceneBounceQuery : PathQuery {
@@ -235,6 +304,7 @@ nbvh_status nbvh_scene_add_instance(nbvh_scene *sc, nbvh_handle *model, const fl
         }
         a.instance = (uint32_t)sc->instances.size();
         sc->instances.push_back({model, a});
+        sc->groups_dirty = true;
         *instance_id = a.instance;
     });
 }
