@@ -86,12 +86,14 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, uint
 
 // Hidden-layer epilogue for this thread's row: 64 accumulator columns -> ReLU -> 16-bit (FP16 or
 // BF16) -> the next layer's A operand (128 x 64) at act.
-template <bool BF16>
-__device__ __forceinline__ void epilogue_hidden(uint32_t tmem_row, unsigned char *act, uint32_t row, bool fp8)
+template <bool BF16, bool FP8>
+__device__ __forceinline__ void epilogue_hidden(uint32_t tmem_row, unsigned char *act, uint32_t row, bool quant)
 {
     using Pr = MlpPrec<BF16>;
     // FP8 mode: the input of a hidden matrix is an FP8-E4M3 value (exact in FP16)
-    auto relu = [fp8](uint32_t u) { return fp8 ? fp8_act(fmaxf(__uint_as_float(u), 0.f)) : fmaxf(__uint_as_float(u), 0.f); };
+    auto relu = [quant](uint32_t u) {
+        return (FP8 && quant) ? fp8_act(fmaxf(__uint_as_float(u), 0.f)) : fmaxf(__uint_as_float(u), 0.f);
+    };
     uint32_t v[4][16];
 #pragma unroll
     for (int q = 0; q < 4; q++)
@@ -120,7 +122,7 @@ __device__ __forceinline__ void epilogue_out(uint32_t tmem_row, float (&o)[8])
         o[i] = 1.0f / (1.0f + expf(-__uint_as_float(v[i])));
 }
 
-template <bool BF16>
+template <bool BF16, bool FP8>
 __global__ void __launch_bounds__(kMlpThreads, 3) k_mlp_tc(const __grid_constant__ CUtensorMap fmap, const MlpTcArgs a)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(kMlpThreads, 3) k_mlp_tc(const __grid_constant
             mma_pending = false;
             tc::fence_after_sync();
             if (layer < H) {
-                epilogue_hidden<BF16>(tmem_row, tile, row, a.fp8 != 0u && layer + 1u < H);
+                epilogue_hidden<BF16, FP8>(tmem_row, tile, row, layer + 1u < H);
                 tc::fence_async_shared();
             } else {
                 // the tile buffer is free: start the next tile's copy under this epilogue
@@ -317,8 +319,9 @@ cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpack
     a.fp8 = prec == NBVH_PRECISION_FP8 ? 1u : 0u;
     const size_t smem = ((a.wbytes + 1023u) & ~1023u) + kTileRows * n_inputs * 2u + 32u;
     if (configure) {
-        const cudaError_t e = bf16 ? allow_max_dynamic_smem(k_mlp_tc<true>)
-                                   : allow_max_dynamic_smem(k_mlp_tc<false>);
+        const cudaError_t e = bf16      ? allow_max_dynamic_smem(k_mlp_tc<true, false>)
+                              : a.fp8 ? allow_max_dynamic_smem(k_mlp_tc<false, true>)
+                                      : allow_max_dynamic_smem(k_mlp_tc<false, false>);
         if (e != cudaSuccess)
             return e;
     }
@@ -327,9 +330,11 @@ cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpack
     if (blocks > tiles)
         blocks = tiles;
     if (bf16)
-        k_mlp_tc<true><<<blocks, kMlpThreads, smem, s>>>(fmap, a);
+        k_mlp_tc<true, false><<<blocks, kMlpThreads, smem, s>>>(fmap, a);
+    else if (a.fp8)
+        k_mlp_tc<false, true><<<blocks, kMlpThreads, smem, s>>>(fmap, a);
     else
-        k_mlp_tc<false><<<blocks, kMlpThreads, smem, s>>>(fmap, a);
+        k_mlp_tc<false, false><<<blocks, kMlpThreads, smem, s>>>(fmap, a);
     return cudaGetLastError();
 }
 

@@ -73,7 +73,7 @@ struct InferArgs {
 };
 
 // Network inference on explicit encoded positions: one warp per 16-row tile, grid-stride.
-template <bool BF16>
+template <bool BF16, bool FP8>
 __global__ void __launch_bounds__(kThreads, 2) k_network_inference(const __grid_constant__ InferArgs args)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_network_inference(const __grid_
         };
         encode_tile_to_smem<BF16>(args.table, gp, pos, mask, feat, fld);
         float o4[4];
-        mlp_tile_from_smem<BF16>(sw, feat, fld, n_inputs, args.n_hidden_layers, o4, args.fp8 != 0u);
+        mlp_tile_from_smem<BF16, FP8>(sw, feat, fld, n_inputs, args.n_hidden_layers, o4);
         __syncwarp();
         if (act0) {
             args.outputs[(size_t)r0 * 8u + tig * 2] = o4[0];
@@ -170,7 +170,10 @@ cudaError_t launch_network_inference(const __half *params_h, const GridParams &g
     a.n = n;
     size_t smem = sizeof(GridParams) + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half) +
                   (size_t)kWarps * 16u * (grid.n_inputs + 8u) * sizeof(__half);
-    cudaError_t e = bf16 ? prepare_smem(k_network_inference<true>, smem) : prepare_smem(k_network_inference<false>, smem);
+    const bool fp8 = a.fp8 != 0u;
+    cudaError_t e = bf16  ? prepare_smem(k_network_inference<true, false>, smem)
+                    : fp8 ? prepare_smem(k_network_inference<false, true>, smem)
+                          : prepare_smem(k_network_inference<false, false>, smem);
     if (e != cudaSuccess)
         return e;
     uint32_t tiles = (n + 15u) / 16u;
@@ -179,9 +182,11 @@ cudaError_t launch_network_inference(const __half *params_h, const GridParams &g
     if (blocks > cap)
         blocks = cap;
     if (bf16)
-        k_network_inference<true><<<blocks, kThreads, smem, s>>>(a);
+        k_network_inference<true, false><<<blocks, kThreads, smem, s>>>(a);
+    else if (fp8)
+        k_network_inference<false, true><<<blocks, kThreads, smem, s>>>(a);
     else
-        k_network_inference<false><<<blocks, kThreads, smem, s>>>(a);
+        k_network_inference<false, false><<<blocks, kThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 

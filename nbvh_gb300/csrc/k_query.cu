@@ -678,7 +678,7 @@ __host__ __device__ inline TailLayout tail_layout(uint32_t n_cut_nodes, bool sme
 // the new bound exactly as the step-by-step query would. Rays with uniformly sampled segment
 // points (whose random draws follow the evaluated segments) or with non-neural leaves list one
 // segment at a time.
-template <bool SMEM_CUT, bool BF16>
+template <bool SMEM_CUT, bool BF16, bool FP8>
 __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(const __grid_constant__ WaveArgs a,
                                                                              uint32_t it)
 {
@@ -865,7 +865,7 @@ __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(co
             };
             encode_tile_to_smem<BF16>(a.table, gp, pos, mask, feat, TL.fld);
             float o4[4];
-            mlp_tile_from_smem<BF16>(sw, feat, TL.fld, n_in, H, o4, a.prec == NBVH_PRECISION_FP8);
+            mlp_tile_from_smem<BF16, FP8>(sw, feat, TL.fld, n_in, H, o4);
             float *ob = outs + 16u * tile * 8u;
             ob[g * 8u + tig * 2u] = o4[0];
             ob[g * 8u + tig * 2u + 1u] = o4[1];
@@ -1003,16 +1003,16 @@ __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(co
 constexpr size_t kSmemLimit = (size_t)kMaxDynamicSmem;
 constexpr uint32_t kStepsPerCheck = 4;
 
-template <bool SMEM_CUT, bool BF16>
+template <bool SMEM_CUT, bool BF16, bool FP8>
 cudaError_t launch_tail_variant(const WaveArgs &a, uint32_t it, int num_sms, bool configure, size_t smem,
                                 cudaStream_t s)
 {
     if (configure) {
-        cudaError_t e = allow_max_dynamic_smem(k_wave_tail<SMEM_CUT, BF16>);
+        cudaError_t e = allow_max_dynamic_smem(k_wave_tail<SMEM_CUT, BF16, FP8>);
         if (e != cudaSuccess)
             return e;
     }
-    k_wave_tail<SMEM_CUT, BF16><<<(uint32_t)num_sms * (SMEM_CUT ? 1u : 2u), kTailThreads, smem, s>>>(a, it);
+    k_wave_tail<SMEM_CUT, BF16, FP8><<<(uint32_t)num_sms * (SMEM_CUT ? 1u : 2u), kTailThreads, smem, s>>>(a, it);
     return cudaGetLastError();
 }
 
@@ -1023,10 +1023,13 @@ cudaError_t launch_tail(const WaveArgs &a, uint32_t it, int num_sms, bool config
     const bool smem_cut = staged.total <= kMaxDynamicSmem;
     const size_t smem = smem_cut ? staged.total : global.total;
     if (a.bf16)
-        return smem_cut ? launch_tail_variant<true, true>(a, it, num_sms, configure, smem, s)
-                        : launch_tail_variant<false, true>(a, it, num_sms, configure, smem, s);
-    return smem_cut ? launch_tail_variant<true, false>(a, it, num_sms, configure, smem, s)
-                    : launch_tail_variant<false, false>(a, it, num_sms, configure, smem, s);
+        return smem_cut ? launch_tail_variant<true, true, false>(a, it, num_sms, configure, smem, s)
+                        : launch_tail_variant<false, true, false>(a, it, num_sms, configure, smem, s);
+    if (a.prec == NBVH_PRECISION_FP8)
+        return smem_cut ? launch_tail_variant<true, false, true>(a, it, num_sms, configure, smem, s)
+                        : launch_tail_variant<false, false, true>(a, it, num_sms, configure, smem, s);
+    return smem_cut ? launch_tail_variant<true, false, false>(a, it, num_sms, configure, smem, s)
+                    : launch_tail_variant<false, false, false>(a, it, num_sms, configure, smem, s);
 }
 
 // The kernels of steps [it0, it1): sort, K3, K4, K2 per step, no host synchronisation.

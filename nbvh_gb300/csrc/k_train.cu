@@ -308,7 +308,7 @@ struct TrainArgs {
 constexpr int kTrainWarps = 8;
 constexpr int kTrainThreads = kTrainWarps * 32;
 
-template <bool BF16>
+template <bool BF16, bool FP8>
 __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid_constant__ TrainArgs a)
 {
     using Pr = MlpPrec<BF16>;
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
         }
         uint32_t ah[4][4];
         for (uint32_t layer = 1; layer <= H; layer++) {
-            relu_pack<BF16>(acc, ah, a.fp8 && layer < H); // FP8 mode: inputs of the hidden matrices
+            relu_pack<BF16, FP8>(acc, ah, layer < H); // FP8 mode: inputs of the hidden matrices
             // store x_layer (input of matrix `layer`)
             __half *dst0 = a.acts + (size_t)r0 * acts_stride + n_in + (layer - 1u) * kNeurons;
             __half *dst1 = a.acts + (size_t)r1 * acts_stride + n_in + (layer - 1u) * kNeurons;
@@ -819,8 +819,9 @@ cudaError_t launch_train_forward_backward(const __half *params_h, const GridPara
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
     const size_t smem = sizeof(GridParams) + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half);
-    cudaError_t e = bf16 ? allow_max_dynamic_smem(k_train_fwd_bwd<true>)
-                         : allow_max_dynamic_smem(k_train_fwd_bwd<false>);
+    cudaError_t e = bf16  ? allow_max_dynamic_smem(k_train_fwd_bwd<true, false>)
+                    : fp8 ? allow_max_dynamic_smem(k_train_fwd_bwd<false, true>)
+                          : allow_max_dynamic_smem(k_train_fwd_bwd<false, false>);
     if (e != cudaSuccess)
         return e;
     const uint32_t tiles = (n + 15u) / 16u;
@@ -829,9 +830,11 @@ cudaError_t launch_train_forward_backward(const __half *params_h, const GridPara
     if (blocks > cap)
         blocks = cap;
     if (bf16)
-        k_train_fwd_bwd<true><<<blocks, kTrainThreads, smem, s>>>(a);
+        k_train_fwd_bwd<true, false><<<blocks, kTrainThreads, smem, s>>>(a);
+    else if (fp8)
+        k_train_fwd_bwd<false, true><<<blocks, kTrainThreads, smem, s>>>(a);
     else
-        k_train_fwd_bwd<false><<<blocks, kTrainThreads, smem, s>>>(a);
+        k_train_fwd_bwd<false, false><<<blocks, kTrainThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -164,13 +164,14 @@ __device__ __forceinline__ float2 encode_level(const uint32_t *__restrict__ tabl
 }
 
 // Rebuilds the 16-bit A fragments of the next layer from the FP32 accumulators (after ReLU).
-// (fp8: the activations go through FP8-E4M3 first, the input format of the hidden matrices in FP8
-// mode; E4M3 values are exact in FP16.)
-template <bool BF16>
-__device__ __forceinline__ void relu_pack(const float (&acc)[8][4], uint32_t (&a)[4][4], bool fp8 = false)
+// (FP8 and quant: the activations go through FP8-E4M3 first, the input format of the hidden
+// matrices in FP8 mode; E4M3 values are exact in FP16. FP8 is a template argument so that the
+// FP16 / BF16 kernels carry none of that code.)
+template <bool BF16, bool FP8 = false>
+__device__ __forceinline__ void relu_pack(const float (&acc)[8][4], uint32_t (&a)[4][4], bool quant = false)
 {
     using Pr = MlpPrec<BF16>;
-    auto act = [fp8](float x) { return fp8 ? fp8_act(fmaxf(x, 0.f)) : fmaxf(x, 0.f); };
+    auto act = [quant](float x) { return (FP8 && quant) ? fp8_act(fmaxf(x, 0.f)) : fmaxf(x, 0.f); };
 #pragma unroll
     for (int kb = 0; kb < 4; kb++) {
         a[kb][0] = Pr::pack(act(acc[2 * kb][0]), act(acc[2 * kb][1]));
@@ -183,9 +184,9 @@ __device__ __forceinline__ void relu_pack(const float (&acc)[8][4], uint32_t (&a
 // Forward of one 16-row tile. make_a(kb, a) fills the layer-0 A fragment of k-block kb (16
 // inputs). On return o[0..1] are the sigmoid outputs (row g, cols 2*tig, 2*tig+1) and o[2..3]
 // those of row g + 8 (g = lane / 4, tig = lane % 4), for output columns 0..7.
-template <bool BF16, typename AMaker>
+template <bool BF16, bool FP8 = false, typename AMaker>
 __device__ __forceinline__ void mlp_forward_tile(const __half *sw, uint32_t n_inputs, uint32_t n_hidden_layers,
-                                                 AMaker &&make_a, float (&o)[4], bool fp8 = false)
+                                                 AMaker &&make_a, float (&o)[4])
 {
     using Pr = MlpPrec<BF16>;
     const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
@@ -209,7 +210,7 @@ __device__ __forceinline__ void mlp_forward_tile(const __half *sw, uint32_t n_in
     const __half *wl = sw + L.hidden_off;
     for (uint32_t layer = 1; layer < n_hidden_layers; layer++) {
         uint32_t a[4][4];
-        relu_pack<BF16>(acc, a, fp8);
+        relu_pack<BF16, FP8>(acc, a, true);
 #pragma unroll
         for (int nt = 0; nt < 8; nt++)
             acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
@@ -288,15 +289,14 @@ __device__ __forceinline__ void encode_tile_to_smem(const uint32_t *__restrict__
 }
 
 // MLP phase of a 16-row tile whose 16-bit features are in feat[16][ld]; outputs as mlp_forward_tile.
-template <bool BF16>
+template <bool BF16, bool FP8 = false>
 __device__ __forceinline__ void mlp_tile_from_smem(const __half *sw, const __half *feat, uint32_t ld,
-                                                   uint32_t n_inputs, uint32_t n_hidden_layers, float (&o)[4],
-                                                   bool fp8 = false)
+                                                   uint32_t n_inputs, uint32_t n_hidden_layers, float (&o)[4])
 {
     const int lane = threadIdx.x & 31;
     const __half *arow = feat + ((lane & 7) + ((lane >> 3) & 1) * 8) * ld + (lane >> 4) * 8;
     auto make_a = [&](uint32_t kb, uint32_t(&a)[4]) { ldsm_x4(a, arow + kb * 16u); };
-    mlp_forward_tile<BF16>(sw, n_inputs, n_hidden_layers, make_a, o, fp8);
+    mlp_forward_tile<BF16, FP8>(sw, n_inputs, n_hidden_layers, make_a, o);
 }
 
 // Encoded segment points along [po, pi] (neural_bvh_module_kernels.cu:57-96).
