@@ -43,6 +43,9 @@ N_RAYS = 1 << 22
 SUBDIV = 7  # 4 * 4^7 = 65,536 triangles
 CUT_DEPTH = 10
 FLOP_PER_SEGMENT = 43008  # 2 * (128*64 + 3*64*64 + 64*16)
+# wavefront encoder, per segment: 4 points x 16 levels x 8 corners x 4 B gathered, the 256 B FP16
+# feature row written, 52 B of list state read (origin/t, direction/mint, meta, sort order)
+ENCODE_BYTES_PER_SEGMENT = 2048 + 256 + 52
 WORKLOAD = "nbvh_inference_sphere65k_cut1024_rays4M"
 
 
@@ -137,12 +140,12 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the neural query kernel from the committed ncu summary, if any."""
+def profiled_traffic(key="neural_query_dram_bytes_per_launch_full_workload"):
+    """A DRAM-bytes figure (`key: value` line) from the committed ncu summaries, if any."""
     for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.txt")) + glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
         with open(path) as f:
             for line in f:
-                m = re.match(r"\s*neural_query_dram_bytes_per_launch_full_workload:\s*([0-9.eE+]+)", line)
+                m = re.match(r"\s*%s:\s*([0-9.eE+]+)" % re.escape(key), line)
                 if m:
                     return float(m.group(1))
     return None
@@ -158,9 +161,11 @@ def build_scene(nb, scenes, cfg, subdiv=SUBDIV):
     return h, v, f, alb
 
 
-def time_queries(h, rays, hits, chits, steps, warmup, nvtx_name):
+def time_queries(h, rays, hits, chits, steps, warmup, nvtx_name, profile=None):
     """Device times (ms) of `steps` neural and classic queries over resident rays, L2 flushed
-    between steps, CUDA events on the launching stream."""
+    between steps, CUDA events on the launching stream. With a `profile` list, the library also
+    times each wavefront-encoder launch of every timed neural query (CUDA events on the query's
+    stream) and one nbvh_kernel_profile per query is appended to it."""
     import torch
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     stream = torch.cuda.current_stream()
@@ -172,12 +177,16 @@ def time_queries(h, rays, hits, chits, steps, warmup, nvtx_name):
         h.query_closest_classic(rays, chits)
         classic_launches = h.last_kernel_time()[1]
     torch.cuda.synchronize()
+    if profile is not None:
+        h.set_kernel_profile(True)
     torch.cuda.nvtx.range_push(nvtx_name)  # ncu --nvtx --nvtx-include "timed/" selects these launches
     for i in range(steps):
         flush.zero_()
         ev[i][0].record(stream)
         h.query_closest_neural(rays, 1, hits)
         ev[i][1].record(stream)
+        if profile is not None:
+            profile.append(h.kernel_profile())  # waits for this query's encoder events
     for i in range(steps):
         flush.zero_()
         cev[i][0].record(stream)
@@ -185,6 +194,8 @@ def time_queries(h, rays, hits, chits, steps, warmup, nvtx_name):
         cev[i][1].record(stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
+    if profile is not None:
+        h.set_kernel_profile(False)
     times = np.array([a.elapsed_time(b) for a, b in ev])
     ctimes = np.array([a.elapsed_time(b) for a, b in cev])
     return times, ctimes, neural_launches, classic_launches
@@ -346,8 +357,9 @@ def run_ours(args):
     barrier()
     torch.cuda.synchronize()
     wall0 = time.perf_counter()
+    enc_prof = []
     times, ctimes, neural_launches, classic_launches = time_queries(h, rays, hits, chits, args.steps, args.warmup,
-                                                                     "timed")
+                                                                     "timed", profile=enc_prof)
     barrier()
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
@@ -374,6 +386,13 @@ def run_ours(args):
     peak = float(peaks.get("bf16_tflops", 1900.0))
     flops = FLOP_PER_SEGMENT * stats.segments
     achieved = flops / (ms * 1e-3) / 1e12
+    # dominant kernel: the wavefront encoder, timed per launch inside the timed region
+    enc_launches = sum(p.encode_launches for p in enc_prof)
+    enc_ms = sum(p.encode_ms for p in enc_prof)
+    enc_bytes = ENCODE_BYTES_PER_SEGMENT * sum(p.encoded_segments for p in enc_prof)
+    enc_gbs = enc_bytes / (enc_ms * 1e-3) / 1e9 if enc_ms > 0 else None
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    enc_traffic = profiled_traffic("encode_dram_bytes_per_launch_full_workload")
     value = world * N_RAYS / (ms * 1e-3) / 1e6
     line = {
         "metric": "neural vs classic Mrays/s at <=1% depth err on 1 GB300; p50/p99 batch latency",
@@ -393,12 +412,19 @@ def run_ours(args):
         "visibility_agreement": vis_agree, "segments_per_ray": segs_per_ray,
         "train": {"steps": args.train_steps, "seconds": train_s,
                   "last_loss": (st.last_loss if st else None), "ms_per_step": (st.ms_per_step if st else None)},
-        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind + " bf16 dense burst (FP16 MMA shares the rate)",
-                     "traffic": profiled_traffic(),
-                     "algorithmic": "43,008 FLOP per inferred leaf segment x %d segments per query" % stats.segments,
-                     "scope": "whole neural query (first pass + all steps); the per-kernel figures are in "
-                              "roofline_kernels"},
+        "roofline": {"bound": "hbm", "achieved": enc_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": (enc_gbs / hbm_peak) if enc_gbs else None,
+                     "peak_kind": peak_kind + " copy bandwidth (burst)",
+                     "traffic": enc_traffic,
+                     "kernel": "k_wave_encode (wavefront hash-grid encoder, %.0f%% of the query's device time)"
+                               % (100.0 * enc_ms / max(1e-9, sum(times))),
+                     "launches": enc_launches, "avg_launch_ms": enc_ms / max(1, enc_launches),
+                     "algorithmic": "%d B per encoded segment (4 points x 16 levels x 8 corners x 4 B of table "
+                                    "gathers + 256 B feature row + 52 B list state) x %d segments per launch"
+                                    % (ENCODE_BYTES_PER_SEGMENT,
+                                       sum(p.encoded_segments for p in enc_prof) // max(1, enc_launches)),
+                     "note": "the 24 MB table is L2-resident: the gathers are served by L2 (DRAM traffic is "
+                             "below the algorithmic bytes); the kernel is bound by the L1 miss path"},
         "e2e": {"value": world * N_RAYS / (e2e_ms * 1e-3) / 1e6, "unit": "Mrays/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": N_RAYS * 32, "d2h_bytes_per_step": N_RAYS * 48},
         "gpu_launches": args.steps * (neural_launches + classic_launches),
@@ -407,9 +433,10 @@ def run_ours(args):
     }
     line["roofline_kernels"] = {
         "mlp_tc": mlp_roofline(h, peak),
-        "encode_gather": {"kernel": "k_wave_encode", "bound": "L1->L2 miss requests (table L2-resident)",
-                          "algorithmic_bytes_per_segment": 2048,
-                          "note": "4 points x 16 levels x 8 corners x 4 B gathered per segment"},
+        "whole_query_tensor": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                               "frac": achieved / peak, "traffic": profiled_traffic(),
+                               "algorithmic": "43,008 FLOP per inferred leaf segment x %d segments per query"
+                                              % stats.segments},
     }
     if rank == 0:
         params = h.params()

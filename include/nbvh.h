@@ -655,6 +655,21 @@ nbvh_status nbvh_last_query_stats(nbvh_handle *h, nbvh_query_stats *out);
  * or training call, and the number of kernels that call launched. */
 nbvh_status nbvh_last_kernel_time(nbvh_handle *h, float *ms, uint32_t *launches);
 
+/* Per-kernel timing of the dominant kernel of the neural query, the wavefront hash-grid encoder
+ * (no counterpart in the reference, whose kernels are timed by external profilers). While enabled,
+ * every neural query on the handle's own first context records a CUDA event pair around each
+ * encoder launch on the query's stream (up to 32 launches); nbvh_last_kernel_profile waits for the
+ * last query's events and reports the summed device time, the launches and the segments they
+ * encoded. Disabled by default (the events cost a few microseconds per query). */
+typedef struct nbvh_kernel_profile {
+    float encode_ms;           /* summed device time of the encoder launches */
+    uint32_t encode_launches;  /* encoder launches of the last query */
+    uint32_t encoded_segments; /* leaf segments those launches encoded */
+    uint32_t segments;         /* all leaf segments of the last query (the tail kernel encodes the rest) */
+} nbvh_kernel_profile;
+nbvh_status nbvh_set_kernel_profile(nbvh_handle *h, int enable);
+nbvh_status nbvh_last_kernel_profile(nbvh_handle *h, nbvh_kernel_profile *out);
+
 /* ---------------------------------------------------------------------------------------------
  * Allocation-free neural query. This entry point has no counterpart in the reference.
  *

@@ -14,7 +14,7 @@ import os
 import numpy as np
 
 from . import abi
-from .abi import (Config, ParamLayout, PathRequest, QueryStats, RenderRequest, Request, RequestResult,
+from .abi import (Config, KernelProfile, ParamLayout, PathRequest, QueryStats, RenderRequest, Request, RequestResult,
                   ServerConfig, ServerStats, TrainStats)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -549,6 +549,16 @@ class NBVH:
         s = QueryStats()
         self._check(self.lib.nbvh_last_query_stats(self.h, C.byref(s)))
         return s
+
+    def set_kernel_profile(self, enable=True):
+        """Time every wavefront-encoder launch of the following queries with CUDA events."""
+        self._check(self.lib.nbvh_set_kernel_profile(self.h, 1 if enable else 0))
+
+    def kernel_profile(self):
+        """Encoder device time, launches and encoded segments of the last profiled query."""
+        p = KernelProfile()
+        self._check(self.lib.nbvh_last_kernel_profile(self.h, C.byref(p)))
+        return p
 
     def last_kernel_time(self):
         ms = C.c_float(0)

@@ -134,6 +134,11 @@ class QueryStats(C.Structure):
                 ("stack_overflow", C.c_uint32), ("fallback", C.c_uint32)]
 
 
+class KernelProfile(C.Structure):
+    _fields_ = [("encode_ms", C.c_float), ("encode_launches", C.c_uint32), ("encoded_segments", C.c_uint32),
+                ("segments", C.c_uint32)]
+
+
 P = C.c_void_p
 U32 = C.c_uint32
 I32 = C.c_int
@@ -209,6 +214,8 @@ PROTOTYPES = {
     "nbvh_load": (ST, [P, C.c_char_p]),
     "nbvh_last_query_stats": (ST, [P, C.POINTER(QueryStats)]),
     "nbvh_last_kernel_time": (ST, [P, PF, PU32]),
+    "nbvh_set_kernel_profile": (ST, [P, I32]),
+    "nbvh_last_kernel_profile": (ST, [P, C.POINTER(KernelProfile)]),
     "nbvh_build_bvh2_host": (ST, [P, U32, P, U32, P, PU32, P]),
     "nbvh_build_neural_cut_host": (ST, [P, U32, U32, P, PU32]),
     "nbvh_param_layout_host": (ST, [PCFG, C.POINTER(ParamLayout)]),

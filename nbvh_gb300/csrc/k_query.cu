@@ -291,6 +291,8 @@ __global__ void __launch_bounds__(kEncodeThreads) k_wave_encode(const __grid_con
     }
     __syncthreads();
     const uint32_t count_in = *reinterpret_cast<volatile const uint32_t *>(&a.wave_counts[it % 3u]);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && count_in)
+        atomicAdd(&a.counters->encoded, count_in);
     const uint32_t L = gp.n_levels, P = gp.n_points;
     const WaveList &in = a.lists[it & 1u];
     const NeuralConsts &nc = a.nc;
@@ -1067,10 +1069,18 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
                 return e;
             launches++;
         }
+        const bool prof = r.prof && !r.capture_only && r.prof->used + 2u <= 2u * kMaxProfiledLaunches;
+        if (prof && (e = cudaEventRecord(r.prof->ev[r.prof->used], s)) != cudaSuccess)
+            return e;
         k_wave_encode<<<enc_blocks, kEncodeThreads, 0, s>>>(a, it);
         e = cudaGetLastError();
         if (e != cudaSuccess)
             return e;
+        if (prof) {
+            if ((e = cudaEventRecord(r.prof->ev[r.prof->used + 1u], s)) != cudaSuccess)
+                return e;
+            r.prof->used += 2u;
+        }
         e = launch_mlp_tc(r.feature_map, r.wpacked, a.grid.n_inputs, a.n_hidden_layers, a.lists[0].capacity,
                           &a.wave_counts[it % 3u], a.outputs, &a.wave_counts[3], a.prec, num_sms, s,
                           !r.capture_only);

@@ -322,6 +322,17 @@ bool mlp_bf16(const nbvh_handle *h) { return h->cfg.network.precision == NBVH_PR
 uint32_t n_bf16_params(const nbvh_handle *h) { return mlp_bf16(h) ? h->layout.n_network_params : 0u; }
 // nbvh_precision of the MLP
 uint32_t mlp_prec(const nbvh_handle *h) { return (uint32_t)h->cfg.network.precision; }
+
+void free_kernel_profile(nbvh_handle *h)
+{
+    if (!h->kprof)
+        return;
+    for (cudaEvent_t e : h->kprof->ev)
+        if (e)
+            cudaEventDestroy(e);
+    delete h->kprof;
+    h->kprof = nullptr;
+}
 // FP32 master -> 16-bit copy: BF16 network in BF16 mode; in FP8 mode the hidden 64x64 matrices as
 // FP8-E4M3 values (they follow the first matrix, 64 x n_inputs)
 ParamPrecision param_precision(const nbvh_handle *h)
@@ -398,9 +409,30 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
     if (timed)
         cuda_check(cudaEventRecord(h->ev0, s), "event");
     h->last_launches = run_neural_query(h, h->qctx[ctx], h->d_counters.ptr + ctx, d_rays, n, depth, vis_only, d_hits, s);
-    if (timed)
+    if (timed) { // a device-buffer call: its statistics are this context's counters
         cuda_check(cudaEventRecord(h->ev1, s), "event");
+        h->n_stat_chunks = 0;
+        h->stat_ctx_mask = 1u << ctx;
+    }
     h->last_rays = n;
+}
+
+// Host-buffer calls run chunk after chunk on contexts 1-2; before a context's counters are reset
+// by its next chunk, they are copied (on the chunk's stream) into slot `chunk` of d_stat_chunks.
+void reserve_stat_chunks(nbvh_handle *h, uint32_t n, uint32_t chunk)
+{
+    const uint32_t chunks = n == 0 ? 0u : (uint32_t)(((uint64_t)n + chunk - 1u) / chunk);
+    if (h->d_stat_chunks.count < chunks)
+        cuda_check(h->d_stat_chunks.resize(chunks), "alloc statistics");
+    h->n_stat_chunks = 0;
+}
+
+void snapshot_stats(nbvh_handle *h, uint32_t chunk, int ctx, cudaStream_t s)
+{
+    cuda_check(cudaMemcpyAsync(h->d_stat_chunks.ptr + chunk, h->d_counters.ptr + ctx, sizeof(QueryCounters),
+                               cudaMemcpyDeviceToDevice, s),
+               "statistics");
+    h->n_stat_chunks = chunk + 1u;
 }
 
 // The closest-hit neural query on the fixed per-device scratch (noalloc_scratch): the same
@@ -595,6 +627,7 @@ nbvh_status nbvh_destroy(nbvh_handle *h)
         if (h->pipe_stream[k])
             cudaStreamDestroy(h->pipe_stream[k]);
     }
+    free_kernel_profile(h);
     if (h->ev0)
         cudaEventDestroy(h->ev0);
     if (h->ev1)
@@ -913,6 +946,7 @@ void pipelined(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, Rec *h_out, Q
             cuda_check(h->d_pipe_out[k].resize(out_bytes), "alloc pipeline out");
     }
     uint32_t launches = 0;
+    reserve_stat_chunks(h, n, chunk);
     for (uint32_t c0 = 0, ci = 0; c0 < n; c0 += chunk, ci++) {
         const int k = (int)(ci & 1u);
         const uint32_t cnt = (n - c0) < chunk ? (n - c0) : chunk;
@@ -921,6 +955,7 @@ void pipelined(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, Rec *h_out, Q
         auto *dout = reinterpret_cast<Rec *>(h->d_pipe_out[k].ptr);
         cuda_check(cudaMemcpyAsync(din, h_rays + c0, (size_t)cnt * sizeof(nbvh_ray), cudaMemcpyHostToDevice, s), "H2D");
         query(din, cnt, dout, s, 1 + k);
+        snapshot_stats(h, ci, 1 + k, s);
         launches += h->last_launches;
         cuda_check(cudaMemcpyAsync(h_out + c0, dout, (size_t)cnt * sizeof(Rec), cudaMemcpyDeviceToHost, s), "D2H");
     }
@@ -961,9 +996,11 @@ bool zero_copy(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, Rec *h_out, Q
     const uint32_t chunk = 1u << 23;
     uint32_t launches = 0;
     cudaStream_t s = h->pipe_stream[0];
-    for (uint32_t c0 = 0; c0 < n; c0 += chunk) {
+    reserve_stat_chunks(h, n, chunk);
+    for (uint32_t c0 = 0, ci = 0; c0 < n; c0 += chunk, ci++) {
         const uint32_t cnt = (n - c0) < chunk ? (n - c0) : chunk;
         query(drays + c0, cnt, dout + c0, s, 1);
+        snapshot_stats(h, ci, 1, s);
         launches += h->last_launches;
     }
     cuda_check(cudaStreamSynchronize(s), "sync");
@@ -994,7 +1031,8 @@ bool zero_copy_neural(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, uint32
     const uint32_t chunk = 1u << 23;
     cudaStream_t s = h->pipe_stream[0];
     uint32_t launches = 0;
-    for (uint32_t c0 = 0; c0 < n; c0 += chunk) {
+    reserve_stat_chunks(h, n, chunk);
+    for (uint32_t c0 = 0, ci = 0; c0 < n; c0 += chunk, ci++) {
         const uint32_t cnt = (n - c0) < chunk ? (n - c0) : chunk;
         ensure_query_workspace(h, cnt, 1);
         if (h->d_drain_hits.count < cnt)
@@ -1013,6 +1051,7 @@ bool zero_copy_neural(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, uint32
         t.drain_taken = &taken;
         launches += run_neural_query(h, h->qctx[1], h->d_counters.ptr + 1, drays + c0, cnt, depth, false,
                                      h->d_drain_hits.ptr, s, &t);
+        snapshot_stats(h, ci, 1, s);
         if (taken) {
             cuda_check(cudaStreamWaitEvent(s, h->ev_drain[1], 0), "wait early copy");
             cuda_check(launch_copy_late(t.late_list, t.late_count, cnt, h->d_drain_hits.ptr, dhost + c0, h->num_sms, s),
@@ -1395,6 +1434,8 @@ nbvh_status nbvh_render_path(nbvh_handle *h, const nbvh_path_request *req, float
         const uint64_t traced = render_path_core(h, h->qctx[0], h->d_counters.ptr, h->path, req, d_image,
                                                  reinterpret_cast<cudaStream_t>(stream),
                                                  req->camera.sample_idx * req->spp);
+        h->n_stat_chunks = 0;
+        h->stat_ctx_mask = 1u;
         if (rays_traced)
             *rays_traced = traced;
     });
@@ -1405,16 +1446,71 @@ nbvh_status nbvh_last_query_stats(nbvh_handle *h, nbvh_query_stats *out)
     return guarded(h, [&]() {
         require(out != nullptr, NBVH_EINVAL, "null output");
         cuda_check(cudaDeviceSynchronize(), "sync");
-        QueryCounters c[3];
-        cuda_check(cudaMemcpy(c, h->d_counters.ptr, sizeof(c), cudaMemcpyDeviceToHost), "counters");
+        std::vector<QueryCounters> c;
+        if (h->n_stat_chunks) {
+            c.resize(h->n_stat_chunks);
+            cuda_check(cudaMemcpy(c.data(), h->d_stat_chunks.ptr, c.size() * sizeof(QueryCounters),
+                                  cudaMemcpyDeviceToHost),
+                       "statistics");
+        } else {
+            QueryCounters all[3];
+            cuda_check(cudaMemcpy(all, h->d_counters.ptr, sizeof(all), cudaMemcpyDeviceToHost), "counters");
+            for (int k = 0; k < 3; k++)
+                if (h->stat_ctx_mask >> k & 1u)
+                    c.push_back(all[k]);
+        }
         std::memset(out, 0, sizeof(*out));
         out->rays = h->last_rays;
-        for (int k = 0; k < 3; k++) {
+        for (size_t k = 0; k < c.size(); k++) {
             out->segments += c[k].segments;
             out->step_capped += c[k].step_capped;
             out->stack_overflow += c[k].stack_overflow;
             out->fallback += c[k].fallback;
         }
+    });
+}
+
+nbvh_status nbvh_set_kernel_profile(nbvh_handle *h, int enable)
+{
+    return guarded(h, [&]() {
+        if (enable && !h->kprof) {
+            auto *p = new KernelProfile();
+            for (uint32_t k = 0; k < 2u * kMaxProfiledLaunches; k++) {
+                const cudaError_t e = cudaEventCreate(&p->ev[k]);
+                if (e != cudaSuccess) {
+                    for (uint32_t j = 0; j < k; j++)
+                        cudaEventDestroy(p->ev[j]);
+                    delete p;
+                    cuda_check(e, "event");
+                }
+            }
+            h->kprof = p;
+        } else if (!enable && h->kprof) {
+            cuda_check(cudaDeviceSynchronize(), "sync");
+            free_kernel_profile(h);
+        }
+    });
+}
+
+nbvh_status nbvh_last_kernel_profile(nbvh_handle *h, nbvh_kernel_profile *out)
+{
+    return guarded(h, [&]() {
+        require(out != nullptr, NBVH_EINVAL, "null output");
+        require(h->kprof != nullptr, NBVH_ESTATE, "kernel profiling is off (nbvh_set_kernel_profile)");
+        std::memset(out, 0, sizeof(*out));
+        const KernelProfile &p = *h->kprof;
+        if (p.used)
+            cuda_check(cudaEventSynchronize(p.ev[p.used - 1u]), "event sync");
+        for (uint32_t k = 0; k + 1u < p.used; k += 2u) {
+            float t = 0.f;
+            cuda_check(cudaEventElapsedTime(&t, p.ev[k], p.ev[k + 1u]), "elapsed");
+            out->encode_ms += t;
+            out->encode_launches++;
+        }
+        QueryCounters c;
+        cuda_check(cudaMemcpy(&c, h->d_counters.ptr, sizeof(c), cudaMemcpyDeviceToHost), "counters");
+        out->encoded_segments = c.encoded;
+        out->segments = c.segments;
     });
 }
 
@@ -1771,6 +1867,10 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
     }
     res.sort_key = h->n_sort_bins ? h->d_sort_key.ptr : nullptr;
     res.n_sort_bins = h->n_sort_bins;
+    if (h->kprof && !tune && &q == &h->qctx[0]) {
+        h->kprof->used = 0;
+        res.prof = h->kprof;
+    }
     cuda_check(make_feature_map(q.features.ptr, h->layout.n_inputs, q.capacity, &res.feature_map), "feature map");
     cuda_check(launch_wave_query(h->d_neural_dilated.ptr, h->d_neural_bounds.ptr, (uint32_t)h->neural_nodes.size(),
                                  h->any_non_neural ? h->d_non_neural.ptr : nullptr, h->d_params_h.ptr, h->grid, nc,

@@ -111,7 +111,15 @@ struct QueryCounters {
     uint32_t fallback;
     uint32_t fallback_count; // entries written to the fallback list
     uint32_t work_count;     // rays that enter at least one leaf (compacted by the first pass)
-    uint32_t pad;
+    uint32_t encoded;        // segments whose features the wavefront encoder (k_wave_encode) computed
+};
+
+// Opt-in device timing of the wavefront encoder: one event pair around each k_wave_encode launch
+// of a query (steps before the tail kernel; kMaxProfiledLaunches at most).
+constexpr uint32_t kMaxProfiledLaunches = 32;
+struct KernelProfile {
+    cudaEvent_t ev[2 * kMaxProfiledLaunches] = {};
+    uint32_t used = 0; // events recorded by the last profiled query
 };
 
 // One state list of the wavefront neural query (structure of arrays, `capacity` rays):
@@ -338,10 +346,17 @@ struct nbvh_handle {
 
     // query workspace
     nbvh::DeviceBuffer<nbvh::QueryCounters> d_counters;
+    // what nbvh_last_query_stats sums: the counters of the contexts in stat_ctx_mask (device-buffer
+    // calls), or the n_stat_chunks per-chunk copies in d_stat_chunks (host-buffer calls, whose
+    // chunks reuse a context's counters)
+    nbvh::DeviceBuffer<nbvh::QueryCounters> d_stat_chunks;
+    uint32_t n_stat_chunks = 0;
+    uint32_t stat_ctx_mask = 1u;
     nbvh::DeviceBuffer<uint32_t> d_fallback_list;
     nbvh::QueryCounters last_counters{};
     uint32_t last_rays = 0;
     float last_kernel_ms = 0.f;
+    nbvh::KernelProfile *kprof = nullptr; // set by nbvh_set_kernel_profile
     uint32_t last_launches = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t ev_drain[2] = {nullptr, nullptr}; // early host copy of the records: taken, done
@@ -441,6 +456,7 @@ struct StepResources {
     // sort bins of the leaves of a cut above kMaxSortNodes nodes (NULL: one bin per node)
     const uint32_t *sort_key = nullptr;
     uint32_t n_sort_bins = 0;
+    KernelProfile *prof = nullptr; // record encoder launch events (not under stream capture)
 };
 
 // Scratch of the allocation-free neural query: one static device buffer per device holding, for

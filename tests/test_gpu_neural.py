@@ -188,13 +188,16 @@ def test_host_pipeline_matches_device(scene):
     h, s = scene
     rays = scenes.uniform_rays((1 << 20) + 12345, s["bbox"][:3], s["bbox"][3:], seed=36)
     dev = as_u32(h.query_closest_neural(_cuda(rays)))
+    segs = h.query_stats().segments
     host = h.query_closest_neural_host(rays)
     assert np.array_equal(host.view(np.uint32).reshape(-1, 12), dev)
+    assert h.query_stats().segments == segs  # statistics summed over the pipeline's chunks
     # page-locked buffers: the kernels read rays and write records over the host link
     pinned = nb.pinned_copy(rays)
     zc = nb.pinned_empty(len(rays), nb.NEURAL_HIT_DTYPE)
     np.asarray(zc).view(np.uint8)[:] = 0xAB  # no stale records can pass for results
     zc = h.query_closest_neural_host(pinned, out=zc)
+    assert h.query_stats().segments == segs
     assert isinstance(zc, nb.PinnedArray)
     assert np.array_equal(np.asarray(zc).view(np.uint32).reshape(-1, 12), dev)
     cdev = h.query_closest_classic(_cuda(rays)).cpu().numpy().view(np.uint32)
@@ -241,3 +244,24 @@ def test_large_cut_sorted_by_leaf_runs(built, oracle):
     both = _compare_queries(got[idx], ref, border)
     assert both.sum() > 100
     h.close()
+
+
+def test_kernel_profile_times_every_encoder_launch(scene):
+    """nbvh_set_kernel_profile / nbvh_last_kernel_profile: one event pair per wavefront-encoder
+    launch, the segments they encoded counted on the device, results unchanged."""
+    h, s = scene
+    rays = _cuda(scenes.uniform_rays(1 << 18, s["bbox"][:3], s["bbox"][3:], seed=41))
+    ref = as_u32(h.query_closest_neural(rays))
+    with pytest.raises(nb.NBVHError):
+        h.kernel_profile()  # off by default
+    h.set_kernel_profile(True)
+    got = as_u32(h.query_closest_neural(rays))
+    p = h.kernel_profile()
+    h.set_kernel_profile(False)
+    assert np.array_equal(got, ref)
+    st = h.query_stats()
+    assert p.segments == st.segments
+    # the wavefront steps run up to the tail kernel (step 5 for this 1,024-leaf cut)
+    assert 1 <= p.encode_launches <= 5
+    assert 0 < p.encoded_segments <= p.segments
+    assert p.encode_ms > 0
