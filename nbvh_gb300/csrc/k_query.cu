@@ -13,7 +13,7 @@
 //   k_wave_decode  K2: LocalT decode and closest-hit update, then the next entered leaf for the
 //                  rays that continue, appended to the other list.
 //
-// Splitting the step lets each phase run at the occupancy it needs: the gathers of K3 with 64
+// Splitting the step lets each phase run at the occupancy it needs: the gathers of K3 with 48
 // warps per SM, the MLP with its accumulators in tensor memory, the divergent traversal with the
 // cut staged in shared memory. Every kernel reads the list length from device memory, so the host
 // checks it only once per batch of steps (one 16-byte copy).
@@ -35,7 +35,9 @@ constexpr uint32_t kSortThreads = 1024;
 // Lists shorter than this are walked in list order: the sort would cost more than the locality it buys.
 constexpr uint32_t kSortMinRows = 1u << 16;
 constexpr uint32_t kDefaultVisitsPerRound = 8;  // node visits of a traversal between lane refills
-constexpr uint32_t kDefaultEncodeBlocksPerSm = 8; // 2,048 resident threads
+// Encoder blocks per SM: all resident at once (40 registers a thread, 48 warps per SM), so each
+// block's contiguous range of rows runs in a single wave.
+constexpr uint32_t kDefaultEncodeBlocksPerSm = 6;
 // From step tail_step() on, the rays still listed are finished by one persistent kernel
 // (k_wave_tail) instead of one short wavefront step after another: the lists are short by then and
 // each step would cost about the same fixed 60-80 us whatever its length. The switch depends only
@@ -280,7 +282,7 @@ __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_co
 // negative mint, then encoded into the dilated scene box. The point is computed once for all its
 // levels, so the kernel's instructions go to the gathers and their interpolation; it holds no
 // MLP state and runs at high occupancy to hide the gather latency.
-__global__ void __launch_bounds__(kEncodeThreads) k_wave_encode(const __grid_constant__ WaveArgs a, uint32_t it)
+__global__ void __launch_bounds__(kEncodeThreads, kDefaultEncodeBlocksPerSm) k_wave_encode(const __grid_constant__ WaveArgs a, uint32_t it)
 {
     __shared__ GridParams gp;
     {
@@ -1040,7 +1042,9 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
                           uint32_t it1, cudaStream_t s, uint32_t &launches)
 {
     cudaError_t e = cudaSuccess;
-    const uint32_t enc_per_sm = r.encode_blocks_per_sm ? r.encode_blocks_per_sm : kDefaultEncodeBlocksPerSm;
+    const uint32_t enc_per_sm =
+        (r.encode_blocks_per_sm && r.encode_blocks_per_sm <= kDefaultEncodeBlocksPerSm) ? r.encode_blocks_per_sm
+                                                                                      : kDefaultEncodeBlocksPerSm;
     const uint32_t enc_blocks = (uint32_t)num_sms * enc_per_sm;
     const uint32_t dec_blocks = (uint32_t)num_sms * (SMEM_CUT ? 1u : 2u);
     for (uint32_t it = it0; it < it1; it++) {
