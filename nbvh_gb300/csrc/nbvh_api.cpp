@@ -1189,6 +1189,7 @@ nbvh_status nbvh_mlp_inference(nbvh_handle *h, const uint16_t *d_features, uint3
         uint32_t status = 0;
         cuda_check(cudaMemcpyAsync(&status, h->d_status.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "status");
         cuda_check(cudaStreamSynchronize(s), "sync");
+        require((status & 2u) == 0u, NBVH_EDEVICE, "tensor-core MLP: shared memory not 1,024-byte aligned");
         require(status == 0u, NBVH_ETIMEOUT, "tensor-core MLP: a bounded wait gave up");
     });
 }
