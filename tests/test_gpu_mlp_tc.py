@@ -86,3 +86,36 @@ def test_mlp_tc_zero_rows(net):
     h, _ = net
     feats = torch.empty((0, h.layout.n_inputs), dtype=torch.float16, device="cuda")
     assert h.mlp_inference(feats).shape == (0, 8)
+
+
+@pytest.mark.parametrize("points,layers,bf16", [(1, 2, False), (2, 4, True), (3, 8, False), (4, 1, False)])
+def test_mlp_tc_input_widths_and_depths(built, points, layers, bf16):
+    """Other network shapes: 32 / 96 inputs (16-byte TMA boxes), 64 / 128 inputs (128-byte swizzled
+    boxes), 1 to 8 hidden layers, FP16 and BF16 operands."""
+    import nbvh_gb300 as nb
+    cfg = nb.default_config()
+    cfg.module.input_segment_points = points
+    cfg.network.n_hidden_layers = layers
+    cfg.network.precision = 1 if bf16 else 0
+    h, s = handle(cfg, kind="sphere4k", seed=5)
+    assert h.layout.n_inputs == 32 * points
+    rng = np.random.default_rng(points)
+    p = h.params()
+    nn = h.layout.n_network_params
+    p[:nn] *= 2.5
+    p[nn:] = rng.uniform(-1.0, 1.0, p.size - nn).astype(np.float32)
+    h.set_params(p)
+    n = 3 * 128 * 152 + 17  # more tiles than one pass of the CTAs' tile pipelines
+    g = torch.Generator(device="cuda").manual_seed(points)
+    pos = torch.rand((n, points, 3), device="cuda", generator=g)
+    feats = h.encode(pos)
+    feats = (feats.bfloat16() if bf16 else feats.half()).contiguous()
+    out = h.mlp_inference(feats)
+    fused = h.network_inference(pos)
+    if bf16:  # one BF16 ulp of a hidden activation is 2^-8 relative: the precision tests' bar
+        d = (out - fused).abs()
+        assert float(d.max()) <= 5e-2 and float((d <= 5e-3).float().mean()) >= 0.999
+    else:
+        check_close(out, fused)
+    assert float(out[:, 0].std()) > 0.02
+    h.close()
