@@ -36,8 +36,9 @@ constexpr uint32_t kGroupThreads = 128; // one tile pipeline: 4 warps, one TMEM 
 constexpr uint32_t kMaxGroups = 5;      // 5 x 96 TMEM columns fit the SM's 512
 constexpr uint32_t kGroupCols = 96;     // a group's accumulator in columns [0, 64), activations in [64, 96)
 constexpr uint32_t kActCol = 64;
-// More than half of an SM's shared memory, so that one CTA (and one TMEM allocation) runs per SM.
-constexpr uint32_t kMinSmem = 116u * 1024u;
+// Shared memory of an SM and the part the runtime reserves per CTA (sm_100 family).
+constexpr size_t kSmPerSm = 228u * 1024u;
+constexpr size_t kSmemReservedPerCta = 1024u;
 
 // TMEM columns a CTA of `groups` allocates (a power of two, at least 32)
 __host__ __device__ constexpr uint32_t tmem_alloc_cols(uint32_t groups)
@@ -434,9 +435,17 @@ cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpack
         return cudaErrorInvalidValue;
     uint32_t groups = (uint32_t)((room - fixed) / tile_bytes);
     groups = groups < kMaxGroups ? groups : kMaxGroups;
+    // no more pipelines than the batch's tiles per SM: small batches (a serving slot's) leave
+    // shared memory to the kernels of the other streams
+    const uint32_t tiles_per_sm = (uint32_t)(((rows + kTileRows - 1u) / kTileRows + (uint32_t)num_sms - 1u) / (uint32_t)num_sms);
+    groups = tiles_per_sm < groups ? (tiles_per_sm > 0u ? tiles_per_sm : 1u) : groups;
     a.groups = groups;
     size_t smem = tile_offset(a.wbytes) + groups * tile_bytes + 8u * (2u * groups + 1u) + 16u;
-    smem = smem < kMinSmem ? kMinSmem : smem;
+    // at most 512 / tmem_alloc_cols(groups) CTAs on an SM, so that their TMEM allocations always
+    // fit: one CTA more must not fit the SM's 228 KB (each CTA also reserves 1 KB)
+    const size_t max_ctas = 512u / tmem_alloc_cols(groups);
+    const size_t smem_min = kSmPerSm / (max_ctas + 1u) - kSmemReservedPerCta + 128u;
+    smem = smem < smem_min ? smem_min : smem;
     if (configure) {
         const cudaError_t e = bf16      ? allow_max_dynamic_smem(k_mlp_tc<true, false>)
                               : a.fp8 ? allow_max_dynamic_smem(k_mlp_tc<false, true>)
