@@ -70,6 +70,9 @@ def parse():
                     help="training steps of the fixed-cut vs learned-cut comparison (-1 skips it)")
     ap.add_argument("--log2-rays", type=int, default=22,
                     help="rays per step; smaller values are for profiling captures, not bench lines")
+    ap.add_argument("--mlp-only", type=int, default=0, metavar="LOG2_ROWS",
+                    help="time only the tcgen05 MLP on 2^LOG2_ROWS resident rows (inside the NVTX range "
+                         "`mlp_roofline`), print its line and exit; for profiling captures")
     return ap.parse_args()
 
 
@@ -342,6 +345,15 @@ def run_ours(args):
     cfg = nb.default_config()
     h, v, f, alb = build_scene(nb, scenes, cfg)
     nn, bbox = h.neural_bvh()
+    if args.mlp_only:
+        peaks, peak_kind = measured_peaks()
+        torch.cuda.nvtx.range_push("mlp_roofline")
+        r = mlp_roofline(h, float(peaks.get("bf16_tflops", 1900.0)), rows=1 << args.mlp_only, reps=3)
+        torch.cuda.nvtx.range_pop()
+        if rank == 0:
+            print(json.dumps({"mlp_tc": r, "peak_kind": peak_kind}))
+        h.close()
+        return
     # train the network on device (outside the timed region)
     t0 = time.perf_counter()
     st = h.run_optimisation(args.train_steps) if args.train_steps > 0 else None
