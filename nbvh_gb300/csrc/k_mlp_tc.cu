@@ -148,11 +148,7 @@ __device__ __forceinline__ uint32_t pack_relu(float lo, float hi)
 template <bool BF16, bool FP8>
 __device__ __forceinline__ void epilogue_hidden(uint32_t tmem_row, bool quant)
 {
-    using Pr = MlpPrec<BF16>;
-    // FP8 mode: the input of a hidden matrix is an FP8-E4M3 value (exact in FP16)
-    auto relu = [quant](uint32_t u) {
-        return (FP8 && quant) ? fp8_act(fmaxf(__uint_as_float(u), 0.f)) : fmaxf(__uint_as_float(u), 0.f);
-    };
+    static_assert(!(FP8 && BF16), "FP8 hidden layers run on the FP16 tensor-core path");
     uint32_t v[4][16];
 #pragma unroll
     for (int q = 0; q < 4; q++)
@@ -162,8 +158,8 @@ __device__ __forceinline__ void epilogue_hidden(uint32_t tmem_row, bool quant)
 #pragma unroll
     for (int j = 0; j < 32; j++) {
         const uint32_t lo = v[j >> 3][(2 * j) & 15], hi = v[j >> 3][(2 * j + 1) & 15];
-        if constexpr (FP8)
-            packed[j] = Pr::pack(relu(lo), relu(hi));
+        if (FP8 && quant) // FP8 mode: the input of a hidden matrix is an E4M3 value (exact in FP16)
+            packed[j] = fp8_act_relu_half2(__uint_as_float(lo), __uint_as_float(hi));
         else // ReLU and rounding in one conversion: max(x, 0) rounded to nearest even
             packed[j] = pack_relu<BF16>(__uint_as_float(lo), __uint_as_float(hi));
     }

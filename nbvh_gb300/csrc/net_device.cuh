@@ -163,6 +163,21 @@ __device__ __forceinline__ float2 encode_level(const uint32_t *__restrict__ tabl
     return make_float2(a0, a1);
 }
 
+// FP8 activations of a pair packed as FP16 (lo in the low half): e4m3(max(x, 0) * 2^7) / 2^7 per
+// value, through the hardware conversions to and from E4M3 (nearest even, saturating at 448,
+// subnormals on the 2^-9 grid: the rounding e4m3_round states); the 2^-7 scale is exact in FP16.
+__device__ __forceinline__ uint32_t fp8_act_relu_half2(float lo, float hi)
+{
+    const float a = __fmul_rn(fmaxf(lo, 0.f), kFp8ActScale), b = __fmul_rn(fmaxf(hi, 0.f), kFp8ActScale);
+    uint16_t e;
+    asm("cvt.rn.satfinite.e4m3x2.f32 %0, %1, %2;\n" : "=h"(e) : "f"(b), "f"(a));
+    uint32_t h;
+    asm("cvt.rn.f16x2.e4m3x2 %0, %1;\n" : "=r"(h) : "h"(e));
+    __half2 v = *reinterpret_cast<const __half2 *>(&h);
+    v = __hmul2(v, __float2half2_rn(1.0f / kFp8ActScale));
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
 // Rebuilds the 16-bit A fragments of the next layer from the FP32 accumulators (after ReLU).
 // (FP8 and quant: the activations go through FP8-E4M3 first, the input format of the hidden
 // matrices in FP8 mode; E4M3 values are exact in FP16. FP8 is a template argument so that the
@@ -171,7 +186,18 @@ template <bool BF16, bool FP8 = false>
 __device__ __forceinline__ void relu_pack(const float (&acc)[8][4], uint32_t (&a)[4][4], bool quant = false)
 {
     using Pr = MlpPrec<BF16>;
-    auto act = [quant](float x) { return (FP8 && quant) ? fp8_act(fmaxf(x, 0.f)) : fmaxf(x, 0.f); };
+    static_assert(!(FP8 && BF16), "FP8 hidden layers run on the FP16 tensor-core path");
+    if (FP8 && quant) {
+#pragma unroll
+        for (int kb = 0; kb < 4; kb++) {
+            a[kb][0] = fp8_act_relu_half2(acc[2 * kb][0], acc[2 * kb][1]);
+            a[kb][1] = fp8_act_relu_half2(acc[2 * kb][2], acc[2 * kb][3]);
+            a[kb][2] = fp8_act_relu_half2(acc[2 * kb + 1][0], acc[2 * kb + 1][1]);
+            a[kb][3] = fp8_act_relu_half2(acc[2 * kb + 1][2], acc[2 * kb + 1][3]);
+        }
+        return;
+    }
+    auto act = [](float x) { return fmaxf(x, 0.f); };
 #pragma unroll
     for (int kb = 0; kb < 4; kb++) {
         a[kb][0] = Pr::pack(act(acc[2 * kb][0]), act(acc[2 * kb][1]));
