@@ -665,9 +665,4 @@ constexpr float kFp8WeightScale = 64.0f;
 // round to zero and their ReLU gradients vanish).
 constexpr float kFp8ActScale = 128.0f;
 
-__host__ __device__ inline float fp8_act(float a)
-{
-    return e4m3_round(a * kFp8ActScale) * (1.0f / kFp8ActScale);
-}
-
 } // namespace nbvh
