@@ -9,18 +9,22 @@ timing (weights of the reference are not available). A step is one neural closes
 the 2^22 resident rays; the classic BVH kernel answers the same rays for the "vs classic" figure and
 judges depth / visibility.
 
-The same comparison is repeated on the 4,194,304-triangle sphere (key "mesh_4m"), where the
-classic traversal is deeper while the neural query still works on a 1,024-leaf cut. The tcgen05
-MLP kernel is also timed alone on 2^22 rows ("roofline_kernels.mlp_tc"), the network is trained in
-FP16 and in BF16 from the same seed and compared on held-out rays ("precision_sweep"), a
-1920x1080 6-bounce hybrid path trace is timed ("path_config4"), the serving loop runs a Poisson
-load of render requests against 4 resident models, beside the same load on their classic BLAS
-("serving"), and the CPU restatements of the neural and classic queries run on the host cores
+The roofline object is the dominant kernel, the wavefront encoder, timed per launch with CUDA
+events inside the timed region. The same comparison is repeated on the 4,194,304-triangle sphere
+(key "mesh_4m"), where the classic traversal is deeper while the neural query still works on a
+1,024-leaf cut. The tcgen05 MLP kernel is also timed alone on 2^22 rows
+("roofline_kernels.mlp_tc"), the network is trained in FP16, BF16 and FP8 from the same seed and
+compared on held-out rays ("precision_sweep"), a fixed depth-10 cut is compared with a learned tree
+cut ("learned_cut"), a 1920x1080 6-bounce hybrid path trace is timed on one model
+("path_config4") and on 16 instances of three models ("scene_config4"), the serving loop runs a
+Poisson load of render requests against 4 resident models, beside the same load on their classic
+BLAS ("serving"), and the CPU restatements of the neural and classic queries run on the host cores
 ("cpu_baseline").
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--train-steps T]
                     [--mesh4m-train-steps T4 | -1] [--precision-sweep-steps T3 | 0] [--serve-seconds S | 0]
-                    [--log2-rays R]
+                    [--learned-cut-steps T5 | -1] [--scene-train-steps T6 | -1] [--log2-rays R]
+                    [--mlp-only LOG2_ROWS]
 """
 
 import argparse
@@ -60,7 +64,7 @@ def parse():
     ap.add_argument("--mesh4m-train-steps", type=int, default=10000,
                     help="training steps for the 4M-triangle comparison; -1 skips it")
     ap.add_argument("--precision-sweep-steps", type=int, default=5000,
-                    help="training steps per precision in the FP16/BF16 sweep; 0 skips it")
+                    help="training steps per precision in the FP16/BF16/FP8 sweep; 0 skips it")
     ap.add_argument("--serve-seconds", type=float, default=3.0,
                     help="seconds of Poisson arrivals in the serving load; 0 skips it")
     ap.add_argument("--serve-train-steps", type=int, default=1500)
