@@ -51,6 +51,7 @@ FLOP_PER_SEGMENT = 43008  # 2 * (128*64 + 3*64*64 + 64*16)
 # feature row written, 52 B of list state read (origin/t, direction/mint, meta, sort order)
 ENCODE_BYTES_PER_SEGMENT = 2048 + 256 + 52
 WORKLOAD = "nbvh_inference_sphere65k_cut1024_rays4M"
+METRIC = "neural vs classic Mrays/s at <=1% depth err on 1 GB300; p50/p99 batch latency"
 
 
 def parse():
@@ -317,7 +318,7 @@ def run_reference(args):
     value = float(np.mean(vals))
     sample = "%d rays of the 2^22-ray batch per step, seeded initial weights" % args.cpu_sample
     print(json.dumps({
-        "impl": "reference", "metric": "neural ray queries per second (N-BVH closest hit)", "value": value,
+        "impl": "reference", "metric": METRIC, "value": value,
         "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": args.cpu_sample / (value * 1e6) * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -411,7 +412,7 @@ def run_ours(args):
     enc_traffic = profiled_traffic("encode_dram_bytes_per_launch_full_workload")
     value = world * N_RAYS / (ms * 1e-3) / 1e6
     line = {
-        "metric": "neural vs classic Mrays/s at <=1% depth err on 1 GB300; p50/p99 batch latency",
+        "metric": METRIC,
         "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16",
         "data": "synthetic (seeded mesh and rays; weights trained on device by this library)",
