@@ -1500,8 +1500,8 @@ nbvh_status nbvh_last_kernel_profile(nbvh_handle *h, nbvh_kernel_profile *out)
         require(h->kprof != nullptr, NBVH_ESTATE, "kernel profiling is off (nbvh_set_kernel_profile)");
         std::memset(out, 0, sizeof(*out));
         const KernelProfile &p = *h->kprof;
-        if (p.used)
-            cuda_check(cudaEventSynchronize(p.ev[p.used - 1u]), "event sync");
+        // the query's last kernels (decode, tail, fallback) follow its last encoder launch
+        cuda_check(cudaDeviceSynchronize(), "sync");
         for (uint32_t k = 0; k + 1u < p.used; k += 2u) {
             float t = 0.f;
             cuda_check(cudaEventElapsedTime(&t, p.ev[k], p.ev[k + 1u]), "elapsed");
