@@ -96,3 +96,18 @@ def test_mesh_generators_deterministic():
     assert len(scenes.terrain(64, 32)[1]) == 64 * 32 * 2
     v, f = scenes.soup(1000, seed=1)
     assert len(f) == 1000 and v.min() >= 0 and v.max() <= 1
+
+
+def test_parallel_build_is_identical_to_single_thread(monkeypatch):
+    """Meshes of 65,536 triangles or more build on several threads (NBVH_BUILD_THREADS or the
+    host's hardware threads): the top of the tree depth-first with large ranges binned in chunks,
+    the subtrees concurrently, every node placed where the single-threaded build puts it. The
+    nodes and the primitive order are identical for any thread count."""
+    v, f = scenes.fbm_sphere(8, seed=3)  # 262,144 triangles
+    monkeypatch.setenv("NBVH_BUILD_THREADS", "1")
+    ref_nodes, ref_prims = nb.build_bvh2_host(v, f)
+    for threads in ("2", "5", "16"):
+        monkeypatch.setenv("NBVH_BUILD_THREADS", threads)
+        nodes, prims = nb.build_bvh2_host(v, f)
+        assert np.array_equal(nodes, ref_nodes) and np.array_equal(prims, ref_prims), threads
+    _check_bvh(ref_nodes, ref_prims, v, f)
