@@ -70,11 +70,33 @@ def default_config(**overrides):
     return cfg
 
 
+def reference_default_config():
+    """The configuration the reference renderer starts from before it reads a JSON file: this
+    library's defaults (the benchmark's inference configuration) with the reference's own defaults
+    where they differ: hash grid of 8 levels x 4 features x 2^18 entries, base resolution 8, level
+    scale 2.0 (include/cuda/neural/utils/tcnn_config.h:70-74), 3 segment points
+    (include/cuda/neural/neural_bvh_module.h:81) and a neural cut from the root
+    (m_neural_bvh_min_depth = 0, include/cuda/neural/neural_bvh_renderer.h:206). Note that 4
+    features per level is not supported by this library's kernels (n_features_per_level must be 2):
+    a handle created from such a config fails with NBVH_EINVAL."""
+    cfg = default_config()
+    cfg.hashgrid.n_levels = 8
+    cfg.hashgrid.n_features_per_level = 4
+    cfg.hashgrid.log2_hashmap_size = 18
+    cfg.hashgrid.base_resolution = 8
+    cfg.hashgrid.per_level_scale = 2.0
+    cfg.module.input_segment_points = 3
+    cfg.neural_bvh_max_depth = 0
+    return cfg
+
+
 def config_from_reference_json(js, base=None):
     """Builds a config from a reference-style JSON dict (neural_bvh_renderer section keys:
     bvh_constants, neural_module.{pt_output_constants, bvh_module_constants, network, optimizer,
-    segment_encoding.hashgrid_options}, batch_size, neural_bvh_min_depth)."""
-    cfg = base if base is not None else default_config()
+    segment_encoding.hashgrid_options}, batch_size, neural_bvh_min_depth). Keys the dict leaves out
+    take the reference's defaults (reference_default_config), as the reference's loaders do, unless
+    `base` is given."""
+    cfg = base if base is not None else reference_default_config()
     r = js.get("neural_bvh_renderer", js)
     nm = r.get("neural_module", {})
     bc = r.get("bvh_constants", {})
@@ -241,6 +263,35 @@ def tree_cut_options(**kw):
         if not hasattr(o, k):
             raise AttributeError(k)
         setattr(o, k, v)
+    return o
+
+
+def tree_cut_options_from_reference_json(js, base=None):
+    """Tree-cut options from a reference-style JSON dict, read as the reference renderer reads them
+    (src/cuda/neural/neural_bvh_renderer_init.cu:705-712): `tree_cut_learning` and
+    `bvh_split_scheduler.{splitting_interval, last_split_iteration, start_split_num, split_scaling,
+    split_interval_scaling}` (include/cuda/neural/utils/bvh_split_scheduler.h:131-140) of the
+    neural_bvh_renderer section, and `bvh_constants.{num_lods_learned, training_node_survival,
+    survival_probability_scale, min_rr_survival_prob}` (include/cuda/neural/
+    neural_bvh_renderer_constants.cuh:78-108). Missing keys keep the defaults."""
+    o = base if base is not None else tree_cut_options()
+    r = js.get("neural_bvh_renderer", js)
+    if "tree_cut_learning" in r:
+        o.tree_cut_learning = int(bool(r["tree_cut_learning"]))
+    sch = r.get("bvh_split_scheduler", {})
+    for k in ("splitting_interval", "last_split_iteration", "start_split_num"):
+        if k in sch:
+            setattr(o, k, int(sch[k]))
+    for k in ("split_scaling", "split_interval_scaling"):
+        if k in sch:
+            setattr(o, k, float(sch[k]))
+    bc = r.get("bvh_constants", {})
+    for k in ("num_lods_learned", "training_node_survival"):
+        if k in bc:
+            setattr(o, k, int(bc[k]))
+    for k in ("survival_probability_scale", "min_rr_survival_prob"):
+        if k in bc:
+            setattr(o, k, float(bc[k]))
     return o
 
 
@@ -597,7 +648,9 @@ def render_request(width, height, origin, target, up=(0.0, 1.0, 0.0), yfov_degre
 
 __all__ = [
     "NBVH", "NBVHError", "Config", "ParamLayout", "RenderRequest", "TrainStats", "QueryStats", "abi",
-    "load_library", "default_config", "config_from_reference_json", "param_layout", "init_params",
+    "load_library", "default_config", "reference_default_config", "config_from_reference_json",
+    "tree_cut_options_from_reference_json",
+    "param_layout", "init_params",
     "build_bvh2_host", "build_neural_cut_host", "nodes_to_float", "render_request", "RAY_DTYPE", "HIT_DTYPE",
     "NEURAL_HIT_DTYPE", "SEGMENT_DTYPE", "FLT_MAX",
 ]

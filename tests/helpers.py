@@ -1,5 +1,7 @@
 """Shared scene setup and comparison helpers for the tests."""
 
+import os
+
 import numpy as np
 
 import nbvh_gb300 as nb
@@ -46,3 +48,9 @@ def as_u32(t):
 
 def float_view(a):
     return np.ascontiguousarray(a).view(np.float32)
+
+
+def reference_root():
+    """Root of the reference source tree when it is present on this machine (NBVH_REFERENCE
+    overrides the default); tests that read its shipped data files skip without it."""
+    return os.environ.get("NBVH_REFERENCE", "/root/reference")

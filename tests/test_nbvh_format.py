@@ -16,12 +16,12 @@ import numpy as np
 import pytest
 
 import nbvh_gb300 as nb
+from helpers import reference_root
 from nbvh_gb300 import abi
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 TOP5 = os.path.join(GOLDEN, "nbvh_chess_top5.nbvh")
-REFERENCE_FILE = os.path.join(os.environ.get("NBVH_REFERENCE", "/root/reference"),
-                              "scene_data/scenes_path_tracing/chess/nbvhs/"
+REFERENCE_FILE = os.path.join(reference_root(), "scene_data/scenes_path_tracing/chess/nbvhs/"
                               "nodes_32940_hash_18_lvl_8_tsteps_10000.nbvh")
 
 
