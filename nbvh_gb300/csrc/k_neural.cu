@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_network_inference(const __grid_
     extern __shared__ __align__(16) unsigned char smem_raw[];
     GridParams &gp = *reinterpret_cast<GridParams *>(smem_raw);
     const uint32_t n_inputs = args.grid.n_inputs, P = args.grid.n_points, L = args.grid.n_levels;
-    __half *sw = reinterpret_cast<__half *>(smem_raw + sizeof(GridParams));
+    __half *sw = reinterpret_cast<__half *>(smem_raw + kGridParamsSmem);
     const SmemNetLayout SL = smem_net_layout(n_inputs, args.n_hidden_layers);
     const uint32_t fld = n_inputs + 8u;
     __half *feat = sw + SL.total + (size_t)(threadIdx.x >> 5) * 16u * fld; // per-warp feature tile
@@ -168,7 +168,7 @@ cudaError_t launch_network_inference(const __half *params_h, const GridParams &g
     a.outputs = outputs;
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
-    size_t smem = sizeof(GridParams) + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half) +
+    size_t smem = kGridParamsSmem + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half) +
                   (size_t)kWarps * 16u * (grid.n_inputs + 8u) * sizeof(__half);
     const bool fp8 = a.fp8 != 0u;
     cudaError_t e = bf16  ? prepare_smem(k_network_inference<true, false>, smem)

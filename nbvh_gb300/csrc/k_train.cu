@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
     GridParams &gp = *reinterpret_cast<GridParams *>(smem_raw);
     const uint32_t n_in = a.grid.n_inputs, P = a.grid.n_points, L = a.grid.n_levels, H = a.n_hidden_layers;
     const SmemNetLayout SL = smem_net_layout(n_in, H);
-    __half *sw = reinterpret_cast<__half *>(smem_raw + sizeof(GridParams));
+    __half *sw = reinterpret_cast<__half *>(smem_raw + kGridParamsSmem);
     {
         const uint32_t *s = reinterpret_cast<const uint32_t *>(&a.grid);
         uint32_t *dd = reinterpret_cast<uint32_t *>(&gp);
@@ -818,7 +818,7 @@ cudaError_t launch_train_forward_backward(const __half *params_h, const GridPara
     a.fp8 = fp8 ? 1u : 0u;
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
-    const size_t smem = sizeof(GridParams) + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half);
+    const size_t smem = kGridParamsSmem + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half);
     cudaError_t e = bf16  ? allow_max_dynamic_smem(k_train_fwd_bwd<true, false>)
                     : fp8 ? allow_max_dynamic_smem(k_train_fwd_bwd<false, true>)
                           : allow_max_dynamic_smem(k_train_fwd_bwd<false, false>);

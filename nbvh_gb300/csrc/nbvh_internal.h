@@ -75,6 +75,9 @@ struct GridParams {
     uint32_t hashed[kMaxLevels];
     float scale[kMaxLevels];
 };
+static_assert(sizeof(GridParams) % 16 == 0, "GridParams must keep 16-byte alignment after it");
+// bytes a shared-memory copy of GridParams takes before the 16-byte aligned data that follows it
+constexpr size_t kGridParamsSmem = (sizeof(GridParams) + 15u) & ~size_t(15);
 
 // Constants of the neural traversal and decode (NeuralBVHRendererConstants /
 // PathTracingOutputConstants subsets).
