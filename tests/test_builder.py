@@ -98,12 +98,18 @@ def test_mesh_generators_deterministic():
     assert len(f) == 1000 and v.min() >= 0 and v.max() <= 1
 
 
-def test_parallel_build_is_identical_to_single_thread(monkeypatch):
+@pytest.mark.parametrize("kind", ["sphere262k", "soup200k", "terrain131k"])
+def test_parallel_build_is_identical_to_single_thread(monkeypatch, kind):
     """Meshes of 65,536 triangles or more build on several threads (NBVH_BUILD_THREADS or the
     host's hardware threads): the top of the tree depth-first with large ranges binned in chunks,
     the subtrees concurrently, every node placed where the single-threaded build puts it. The
     nodes and the primitive order are identical for any thread count."""
-    v, f = scenes.fbm_sphere(8, seed=3)  # 262,144 triangles
+    if kind == "sphere262k":
+        v, f = scenes.fbm_sphere(8, seed=3)
+    elif kind == "soup200k":  # overlapping random triangles: many equal-centroid and median splits
+        v, f = scenes.soup(200000, seed=4)
+    else:  # a height field: flat boxes, regular centroids
+        v, f = scenes.terrain(256, 256, seed=5)
     monkeypatch.setenv("NBVH_BUILD_THREADS", "1")
     ref_nodes, ref_prims = nb.build_bvh2_host(v, f)
     for threads in ("2", "5", "16"):
