@@ -156,8 +156,9 @@ typedef enum nbvh_precision {
                                 weights, straight-through gradients */
 } nbvh_precision;
 
-/* HashGridOptions, include/cuda/neural/utils/tcnn_config.h:69-78. n_features_per_level must be 2;
- * input_segment_points * n_levels * 2 must be a multiple of 16 and at most 128. */
+/* HashGridOptions, include/cuda/neural/utils/tcnn_config.h:69-78. n_features_per_level is 2, 4 or
+ * 8 (the reference default is 4); input_segment_points * n_levels * n_features_per_level must be a
+ * multiple of 16 and at most 128. */
 typedef struct nbvh_hashgrid_options {
     int32_t n_levels;
     int32_t n_features_per_level;
@@ -353,21 +354,22 @@ nbvh_status nbvh_query_segments(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t
  * ------------------------------------------------------------------------------------------- */
 
 /* Parameter layout (one flat FP32 vector, network first as tcnn orders it):
- *   W_0   [n_neurons][n_inputs]     n_inputs = input_segment_points * n_levels * 2
+ *   W_0   [n_neurons][n_inputs]     n_inputs = input_segment_points * n_levels * F
  *   W_1.. [n_neurons][n_neurons]    (n_hidden_layers - 1 matrices)
  *   W_out [16][n_neurons]           rows 8..15 are padding and stay zero
- *   grid  [n_grid_entries][2]       levels concatenated; level offsets from nbvh_grid_layout
+ *   grid  [n_grid_entries][F]       levels concatenated; F = n_features_per_level
  */
 typedef struct nbvh_param_layout {
     uint32_t n_inputs;
     uint32_t n_network_params;
     uint32_t n_grid_entries;
-    uint32_t n_params; /* n_network_params + 2 * n_grid_entries */
+    uint32_t n_params; /* n_network_params + F * n_grid_entries */
     uint32_t n_levels;
     uint32_t level_offset[32];     /* in entries */
     uint32_t level_size[32];       /* entries in the level (hashed levels: 2^log2_hashmap_size) */
     uint32_t level_resolution[32]; /* grid points per axis */
     float level_scale[32];         /* position scale: pos = scale * x + 0.5 */
+    uint32_t n_features_per_level; /* F: values per grid entry (2, 4 or 8) */
 } nbvh_param_layout;
 nbvh_status nbvh_get_param_layout(const nbvh_handle *h, nbvh_param_layout *out);
 

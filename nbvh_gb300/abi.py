@@ -71,7 +71,7 @@ class ParamLayout(C.Structure):
     _fields_ = [("n_inputs", C.c_uint32), ("n_network_params", C.c_uint32), ("n_grid_entries", C.c_uint32),
                 ("n_params", C.c_uint32), ("n_levels", C.c_uint32), ("level_offset", C.c_uint32 * 32),
                 ("level_size", C.c_uint32 * 32), ("level_resolution", C.c_uint32 * 32),
-                ("level_scale", C.c_float * 32)]
+                ("level_scale", C.c_float * 32), ("n_features_per_level", C.c_uint32)]
 
 
 class TrainStats(C.Structure):

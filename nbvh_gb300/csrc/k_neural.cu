@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_network_inference(const __grid_
             const float *src = args.positions + ((size_t)(tile * 16u + r) * P + p) * 3u;
             return mk3(__ldg(src), __ldg(src + 1), __ldg(src + 2));
         };
-        encode_tile_to_smem<BF16>(args.table, gp, pos, mask, feat, fld);
+        encode_tile_any<BF16>(args.table, gp, pos, mask, feat, fld);
         float o4[4];
         mlp_tile_from_smem<BF16, FP8>(sw, feat, fld, n_inputs, args.n_hidden_layers, o4);
         __syncwarp();
@@ -114,7 +114,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_network_inference(const __grid_
     }
 }
 
-// Hash-grid features (FP32 before the FP16 rounding), one thread per (row, point, level).
+// Hash-grid features (FP32 before the FP16 rounding), one thread per (row, point, level); level l
+// of a point's block holds its F features at l * F.
 __global__ void __launch_bounds__(128) k_encode(const __grid_constant__ GridParams grid, const uint32_t *__restrict__ table,
                                                 const float *__restrict__ positions, uint32_t n,
                                                 float *__restrict__ features)
@@ -123,12 +124,27 @@ __global__ void __launch_bounds__(128) k_encode(const __grid_constant__ GridPara
     uint64_t total = (uint64_t)n * grid.n_points * grid.n_levels;
     if (i >= total)
         return;
+    const uint32_t F = grid.n_features;
     uint32_t l = (uint32_t)(i % grid.n_levels);
     uint64_t rp = i / grid.n_levels; // row * points + point
     const float *src = positions + rp * 3u;
-    float2 f = encode_level(table, grid, l, mk3(src[0], src[1], src[2]));
-    features[rp * grid.n_levels * 2u + 2u * l] = f.x;
-    features[rp * grid.n_levels * 2u + 2u * l + 1u] = f.y;
+    const V3 p = mk3(src[0], src[1], src[2]);
+    float *dst = features + (rp * grid.n_levels + l) * F;
+    if (F == 4u) {
+        float f[4];
+        encode_level_wide<4>(table, grid, l, p, f);
+        for (uint32_t k = 0; k < 4u; k++)
+            dst[k] = f[k];
+    } else if (F == 8u) {
+        float f[8];
+        encode_level_wide<8>(table, grid, l, p, f);
+        for (uint32_t k = 0; k < 8u; k++)
+            dst[k] = f[k];
+    } else {
+        const float2 f = encode_level(table, grid, l, p);
+        dst[0] = f.x;
+        dst[1] = f.y;
+    }
 }
 
 template <typename K>

@@ -277,12 +277,22 @@ __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_co
 
 // K3 of one step: the FP16 hash-grid features of every listed ray's current leaf segment, one
 // thread per (ray, point) looping over the levels, written row-major to features[row][n_inputs]
-// (point-major, then level, 2 features per level). Points follow encode_bvh_network_input_data
+// (point-major, then level, F features per level). Points follow encode_bvh_network_input_data
 // (src/cuda/neural/neural_bvh_module_kernels.cu:266-303): the segment ends are swapped for a
 // negative mint, then encoded into the dilated scene box. The point is computed once for all its
 // levels, so the kernel's instructions go to the gathers and their interpolation; it holds no
-// MLP state and runs at high occupancy to hide the gather latency.
-__global__ void __launch_bounds__(kEncodeThreads, kDefaultEncodeBlocksPerSm) k_wave_encode(const __grid_constant__ WaveArgs a, uint32_t it)
+// MLP state and runs at high occupancy to hide the gather latency. F = 2 (one 32-bit entry per
+// corner) runs 6 blocks of 256 threads per SM at 40 registers; the wider entries of F = 4 and 8
+// hold more gathered words and run 4.
+template <uint32_t F>
+constexpr uint32_t encode_blocks_per_sm()
+{
+    return F == 2u ? kDefaultEncodeBlocksPerSm : 4u;
+}
+
+template <uint32_t F>
+__global__ void __launch_bounds__(kEncodeThreads, encode_blocks_per_sm<F>())
+    k_wave_encode(const __grid_constant__ WaveArgs a, uint32_t it)
 {
     __shared__ GridParams gp;
     {
@@ -303,17 +313,20 @@ __global__ void __launch_bounds__(kEncodeThreads, kDefaultEncodeBlocksPerSm) k_w
     const float dilation = __fadd_rn(__fadd_rn(1.0f, nc.node_extent_dilation), nc.fixed_node_dilation);
     const V3 ext = scale3(sub3(smax, smin), dilation);
     const V3 center = scale3(add3(smax, smin), 0.5f);
-    const bool vec_store = (L & 3u) == 0u; // each point's block of L words starts 16-byte aligned
+    // levels whose features fill one 16-byte store: 4 (F = 2), 2 (F = 4), 1 (F = 8)
+    constexpr uint32_t LPS = 8u / F;
+    const bool vec_store = (L % LPS) == 0u; // each point's block of L * F halves starts 16-byte aligned
     const bool bf16 = a.bf16 != 0u;
     auto pack16 = [bf16](float lo, float hi) { return bf16 ? pack_bf162(lo, hi) : pack_half2(lo, hi); };
     uint32_t *feat = reinterpret_cast<uint32_t *>(a.features);
     const bool sorted = a.perm != nullptr && count_in >= kSortMinRows;
     const uint32_t total = count_in * P; // at most 2^22 rays x 16 points
-    // Short lists (the tail of the query) split each point's levels over G threads, 4 levels each,
-    // so that a point's gathers are in flight together instead of one level after another; long
-    // lists keep one thread per point (all levels), which the other points' threads already hide.
+    // Short lists (the tail of the query) split each point's levels over G threads, LPS levels
+    // (one 16-byte store) each, so that a point's gathers are in flight together instead of one
+    // level after another; long lists keep one thread per point (all levels), which the other
+    // points' threads already hide.
     const uint32_t lanes = gridDim.x * blockDim.x;
-    const uint32_t G = (vec_store && (size_t)total * (L >> 2) <= 2u * (size_t)lanes) ? (L >> 2) : 1u;
+    const uint32_t G = (vec_store && (size_t)total * (L / LPS) <= 2u * (size_t)lanes) ? (L / LPS) : 1u;
     const uint32_t LG = L / G;
     const uint32_t work = total * G;
     // each block takes one contiguous range of the (node-sorted) rows, so an SM's L1 serves the
@@ -344,24 +357,37 @@ __global__ void __launch_bounds__(kEncodeThreads, kDefaultEncodeBlocksPerSm) k_w
             t = segment_t(p, P, gp.segment_distribution, unused);
         }
         const V3 pos = segment_point(epo, epi, t);
-        uint32_t *dst = feat + (size_t)g * L; // row * (P * L) + p * L
-        if (vec_store) {
-            for (uint32_t l = lg * LG; l < lg * LG + LG; l += 4u) {
-                uint4 q;
-                float2 f = encode_level(a.table, gp, l, pos);
-                q.x = pack16(f.x, f.y);
-                f = encode_level(a.table, gp, l + 1u, pos);
-                q.y = pack16(f.x, f.y);
-                f = encode_level(a.table, gp, l + 2u, pos);
-                q.z = pack16(f.x, f.y);
-                f = encode_level(a.table, gp, l + 3u, pos);
-                q.w = pack16(f.x, f.y);
-                *reinterpret_cast<uint4 *>(dst + l) = q;
+        uint32_t *dst = feat + (size_t)g * L * (F / 2u); // row * (P * L * F / 2) + p * L * F / 2 words
+        if constexpr (F == 2u) {
+            if (vec_store) {
+                for (uint32_t l = lg * LG; l < lg * LG + LG; l += 4u) {
+                    uint4 q;
+                    float2 f = encode_level(a.table, gp, l, pos);
+                    q.x = pack16(f.x, f.y);
+                    f = encode_level(a.table, gp, l + 1u, pos);
+                    q.y = pack16(f.x, f.y);
+                    f = encode_level(a.table, gp, l + 2u, pos);
+                    q.z = pack16(f.x, f.y);
+                    f = encode_level(a.table, gp, l + 3u, pos);
+                    q.w = pack16(f.x, f.y);
+                    *reinterpret_cast<uint4 *>(dst + l) = q;
+                }
+            } else {
+                for (uint32_t l = 0; l < L; l++) {
+                    const float2 f = encode_level(a.table, gp, l, pos);
+                    dst[l] = pack16(f.x, f.y);
+                }
             }
         } else {
-            for (uint32_t l = 0; l < L; l++) {
-                const float2 f = encode_level(a.table, gp, l, pos);
-                dst[l] = pack16(f.x, f.y);
+            // F = 4: 8 bytes per level; F = 8: 16 bytes per level (always aligned to its size)
+            for (uint32_t l = lg * LG; l < lg * LG + LG; l++) {
+                float f[F];
+                encode_level_wide<F>(a.table, gp, l, pos, f);
+                if constexpr (F == 4u)
+                    *reinterpret_cast<uint2 *>(dst + 2u * l) = make_uint2(pack16(f[0], f[1]), pack16(f[2], f[3]));
+                else
+                    *reinterpret_cast<uint4 *>(dst + 4u * l) = make_uint4(pack16(f[0], f[1]), pack16(f[2], f[3]),
+                                                                          pack16(f[4], f[5]), pack16(f[6], f[7]));
             }
         }
     }
@@ -867,7 +893,7 @@ __global__ void __launch_bounds__(kTailThreads, SMEM_CUT ? 1 : 2) k_wave_tail(co
                 }
                 return segment_point(mk3(e0.x, e0.y, e0.z), mk3(e1.x, e1.y, e1.z), t);
             };
-            encode_tile_to_smem<BF16>(a.table, gp, pos, mask, feat, TL.fld);
+            encode_tile_any<BF16>(a.table, gp, pos, mask, feat, TL.fld);
             float o4[4];
             mlp_tile_from_smem<BF16, FP8>(sw, feat, TL.fld, n_in, H, o4);
             float *ob = outs + 16u * tile * 8u;
@@ -1042,9 +1068,10 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
                           uint32_t it1, cudaStream_t s, uint32_t &launches)
 {
     cudaError_t e = cudaSuccess;
+    const uint32_t F = a.grid.n_features;
+    const uint32_t enc_max = F == 2u ? encode_blocks_per_sm<2>() : encode_blocks_per_sm<4>();
     const uint32_t enc_per_sm =
-        (r.encode_blocks_per_sm && r.encode_blocks_per_sm <= kDefaultEncodeBlocksPerSm) ? r.encode_blocks_per_sm
-                                                                                      : kDefaultEncodeBlocksPerSm;
+        (r.encode_blocks_per_sm && r.encode_blocks_per_sm <= enc_max) ? r.encode_blocks_per_sm : enc_max;
     const uint32_t enc_blocks = (uint32_t)num_sms * enc_per_sm;
     const uint32_t dec_blocks = (uint32_t)num_sms * (SMEM_CUT ? 1u : 2u);
     for (uint32_t it = it0; it < it1; it++) {
@@ -1076,7 +1103,12 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
         const bool prof = r.prof && !r.capture_only && r.prof->used + 2u <= 2u * kMaxProfiledLaunches;
         if (prof && (e = cudaEventRecord(r.prof->ev[r.prof->used], s)) != cudaSuccess)
             return e;
-        k_wave_encode<<<enc_blocks, kEncodeThreads, 0, s>>>(a, it);
+        if (F == 4u)
+            k_wave_encode<4><<<enc_blocks, kEncodeThreads, 0, s>>>(a, it);
+        else if (F == 8u)
+            k_wave_encode<8><<<enc_blocks, kEncodeThreads, 0, s>>>(a, it);
+        else
+            k_wave_encode<2><<<enc_blocks, kEncodeThreads, 0, s>>>(a, it);
         e = cudaGetLastError();
         if (e != cudaSuccess)
             return e;

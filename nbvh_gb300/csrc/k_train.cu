@@ -288,6 +288,40 @@ __device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const void *p)
                  : "r"(a));
 }
 
+// The hash-grid features of the training rows, in the MLP precision, into the first n_inputs
+// activations of each row (acts row stride acts_stride halves): one thread per (row, point), the
+// levels in order, F features per level stored together.
+__global__ void __launch_bounds__(256) k_train_encode(const __grid_constant__ GridParams grid,
+                                                      const uint32_t *__restrict__ table,
+                                                      const float *__restrict__ positions, uint32_t n,
+                                                      __half *__restrict__ acts, uint32_t acts_stride, uint32_t bf16)
+{
+    const uint32_t P = grid.n_points, L = grid.n_levels, F = grid.n_features;
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint64_t)n * P)
+        return;
+    const uint32_t row = (uint32_t)(i / P), p = (uint32_t)(i - (uint64_t)row * P);
+    const float *src = positions + i * 3u;
+    const V3 pos = mk3(__ldg(src), __ldg(src + 1), __ldg(src + 2));
+    auto pack16 = [bf16](float lo, float hi) { return bf16 ? pack_bf162(lo, hi) : pack_half2(lo, hi); };
+    __half *dst = acts + (size_t)row * acts_stride + (size_t)p * L * F;
+    for (uint32_t l = 0; l < L; l++) {
+        if (F == 4u) {
+            float f[4];
+            encode_level_wide<4>(table, grid, l, pos, f);
+            *reinterpret_cast<uint2 *>(dst + 4u * l) = make_uint2(pack16(f[0], f[1]), pack16(f[2], f[3]));
+        } else if (F == 8u) {
+            float f[8];
+            encode_level_wide<8>(table, grid, l, pos, f);
+            *reinterpret_cast<uint4 *>(dst + 8u * l) =
+                make_uint4(pack16(f[0], f[1]), pack16(f[2], f[3]), pack16(f[4], f[5]), pack16(f[6], f[7]));
+        } else {
+            const float2 f = encode_level(table, grid, l, pos);
+            *reinterpret_cast<uint32_t *>(dst + 2u * l) = pack16(f.x, f.y);
+        }
+    }
+}
+
 struct TrainArgs {
     GridParams grid;
     LossConsts lc;
@@ -297,7 +331,7 @@ struct TrainArgs {
     const float *targets;
     __half *acts;      // n x acts_stride
     __half *dz;        // n x dz_stride
-    float2 *grid_grad; // n_grid_entries
+    float2 *grid_grad; // n_grid_entries x (n_features / 2) feature pairs
     float *loss_sum;
     float *sample_loss; // per row: sum of its output channels' loss values (may be NULL)
     uint32_t fp8;       // hidden-matrix inputs rounded to FP8-E4M3 (straight-through in the backward)
@@ -345,27 +379,15 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
         for (int nt = 0; nt < 8; nt++)
             acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
         for (uint32_t kb = 0; kb < n_in / 16u; kb++) {
+            // the encoded features (k_train_encode wrote them to the rows' first n_in activations)
             uint32_t af[4];
-            const uint32_t j0 = kb * 8u + (uint32_t)tig, j1 = j0 + 4u;
-            auto feat = [&](bool act, uint32_t row, uint32_t j) -> uint32_t {
-                if (!act)
-                    return 0u;
-                uint32_t p = j / L, l = j - p * L;
-                float2 f = encode_level(a.table, gp, l, pos_of(row, p));
-                return Pr::pack(f.x, f.y);
+            auto feat = [&](bool act, uint32_t row, uint32_t col) -> uint32_t {
+                return act ? *reinterpret_cast<const uint32_t *>(a.acts + (size_t)row * acts_stride + col) : 0u;
             };
-            af[0] = feat(act0, r0, j0);
-            af[1] = feat(act1, r1, j0);
-            af[2] = feat(act0, r0, j1);
-            af[3] = feat(act1, r1, j1);
-            if (act0) {
-                *reinterpret_cast<uint32_t *>(a.acts + (size_t)r0 * acts_stride + kb * 16u + tig * 2u) = af[0];
-                *reinterpret_cast<uint32_t *>(a.acts + (size_t)r0 * acts_stride + kb * 16u + tig * 2u + 8u) = af[2];
-            }
-            if (act1) {
-                *reinterpret_cast<uint32_t *>(a.acts + (size_t)r1 * acts_stride + kb * 16u + tig * 2u) = af[1];
-                *reinterpret_cast<uint32_t *>(a.acts + (size_t)r1 * acts_stride + kb * 16u + tig * 2u + 8u) = af[3];
-            }
+            af[0] = feat(act0, r0, kb * 16u + tig * 2u);
+            af[1] = feat(act1, r1, kb * 16u + tig * 2u);
+            af[2] = feat(act0, r0, kb * 16u + tig * 2u + 8u);
+            af[3] = feat(act1, r1, kb * 16u + tig * 2u + 8u);
             const __half *wrow = sw + g * SL.ld0 + kb * 16u + tig * 2;
 #pragma unroll
             for (int nt = 0; nt < 8; nt++) {
@@ -536,9 +558,12 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
                 ldsm_x4_trans(b, addr);
                 Pr::mma(dx, adz[kb], b[0], b[1]);
             }
-            // feature pair j = nt * 4 + tig (both features) for rows r0, r1
+            // feature pair j = nt * 4 + tig (features 2 sub, 2 sub + 1 of level l of point p) for
+            // rows r0, r1
             const uint32_t j = nt * 4u + (uint32_t)tig;
-            const uint32_t p = j / L, l = j - p * L;
+            const uint32_t pairs = gp.n_features / 2u;
+            const uint32_t pl = j / pairs, sub = j - pl * pairs;
+            const uint32_t p = pl / L, l = pl - p * L;
 #pragma unroll
             for (int rr = 0; rr < 2; rr++) {
                 const bool act = rr ? act1 : act0;
@@ -571,7 +596,7 @@ __global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid
                     }
                     float w = __fmul_rn(__fmul_rn((c & 1u) ? rx : __fsub_rn(1.0f, rx), (c & 2u) ? ry : __fsub_rn(1.0f, ry)),
                                         (c & 4u) ? rz : __fsub_rn(1.0f, rz));
-                    atomicAdd(a.grid_grad + off + idx, make_float2(w * g0, w * g1));
+                    atomicAdd(a.grid_grad + (size_t)(off + idx) * pairs + sub, make_float2(w * g0, w * g1));
                 }
             }
         }
@@ -819,6 +844,14 @@ cudaError_t launch_train_forward_backward(const __half *params_h, const GridPara
     a.n_hidden_layers = n_hidden_layers;
     a.n = n;
     const size_t smem = kGridParamsSmem + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half);
+    {
+        const uint64_t threads = (uint64_t)n * grid.n_points;
+        k_train_encode<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(
+            grid, a.table, positions, n, acts, grid.n_inputs + n_hidden_layers * kNeurons, bf16 ? 1u : 0u);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return e;
+    }
     cudaError_t e = bf16  ? allow_max_dynamic_smem(k_train_fwd_bwd<true, false>)
                     : fp8 ? allow_max_dynamic_smem(k_train_fwd_bwd<false, true>)
                           : allow_max_dynamic_smem(k_train_fwd_bwd<false, false>);

@@ -61,15 +61,17 @@ nbvh_status guarded_free(F &&f)
 
 uint32_t n_inputs_of(const nbvh_config &c)
 {
-    return (uint32_t)c.module.input_segment_points * (uint32_t)c.hashgrid.n_levels * 2u;
+    return (uint32_t)c.module.input_segment_points * (uint32_t)c.hashgrid.n_levels *
+           (uint32_t)c.hashgrid.n_features_per_level;
 }
 
 void validate_config(const nbvh_config &c)
 {
     if (c.abi_version != NBVH_ABI_VERSION)
         fail(NBVH_EINVAL, "config abi_version mismatch");
-    if (c.hashgrid.n_features_per_level != 2)
-        fail(NBVH_EINVAL, "n_features_per_level must be 2");
+    const int F = c.hashgrid.n_features_per_level;
+    if (F != 2 && F != 4 && F != 8)
+        fail(NBVH_EINVAL, "n_features_per_level must be 2, 4 or 8");
     if (c.hashgrid.n_levels < 1 || c.hashgrid.n_levels > (int)kMaxLevels)
         fail(NBVH_EINVAL, "n_levels must be in [1, 32]");
     if (c.hashgrid.log2_hashmap_size < 4 || c.hashgrid.log2_hashmap_size > 24)
@@ -82,7 +84,7 @@ void validate_config(const nbvh_config &c)
         fail(NBVH_EINVAL, "bad segment_distribution");
     const uint32_t ni = n_inputs_of(c);
     if (ni % 16u != 0u || ni > kMaxInputs)
-        fail(NBVH_EINVAL, "points * levels * 2 must be a multiple of 16 and at most 128");
+        fail(NBVH_EINVAL, "points * levels * features_per_level must be a multiple of 16 and at most 128");
     if (c.network.n_neurons != (int)kNeurons)
         fail(NBVH_EINVAL, "n_neurons must be 64");
     if (c.network.n_hidden_layers < 1 || c.network.n_hidden_layers > (int)kMaxHiddenLayers)
@@ -131,7 +133,12 @@ void compute_layout(const nbvh_config &c, nbvh_param_layout &L, GridParams &g)
     const uint32_t H = (uint32_t)c.network.n_hidden_layers;
     L.n_network_params = kNeurons * L.n_inputs + (H - 1u) * kNeurons * kNeurons + kOutputsPadded * kNeurons;
     L.n_grid_entries = (uint32_t)off;
-    L.n_params = L.n_network_params + 2u * L.n_grid_entries;
+    const uint32_t F = (uint32_t)c.hashgrid.n_features_per_level;
+    if ((uint64_t)L.n_network_params + (uint64_t)F * off >= (1ull << 31))
+        fail(NBVH_EINVAL, "the parameter vector must stay below 2^31 values");
+    L.n_params = L.n_network_params + F * L.n_grid_entries;
+    L.n_features_per_level = F;
+    g.n_features = F;
     g.n_levels = nl;
     g.n_points = (uint32_t)c.module.input_segment_points;
     g.n_inputs = L.n_inputs;
@@ -163,7 +170,7 @@ void init_params(const nbvh_config &c, const nbvh_param_layout &L, float *out)
                 out[o + r * cols + k] = (m == H && r >= kOutputs) ? 0.0f : (float)((2.0 * next() - 1.0) * s);
         o += rows * cols;
     }
-    for (uint32_t i = 0; i < 2u * L.n_grid_entries; i++)
+    for (uint32_t i = 0; i < L.n_features_per_level * L.n_grid_entries; i++)
         out[L.n_network_params + i] = (float)((2.0 * next() - 1.0) * 1e-4);
 }
 

@@ -64,6 +64,9 @@ struct BVHNode {
 static_assert(sizeof(BVHNode) == 32, "node layout");
 
 // Hash-grid geometry shared by every kernel (copied into shared memory at kernel start).
+// Kernels keep a copy in shared memory with 16-byte aligned data (matrices, ldmatrix tiles) placed
+// right after it, so its size stays a multiple of 16 bytes: n_features comes with three words of
+// padding.
 struct GridParams {
     uint32_t n_levels;
     uint32_t n_points;
@@ -74,6 +77,8 @@ struct GridParams {
     uint32_t res[kMaxLevels];
     uint32_t hashed[kMaxLevels];
     float scale[kMaxLevels];
+    uint32_t n_features; // per level: 2, 4 or 8 FP16 values per table entry
+    uint32_t pad[3];
 };
 static_assert(sizeof(GridParams) % 16 == 0, "GridParams must keep 16-byte alignment after it");
 // bytes a shared-memory copy of GridParams takes before the 16-byte aligned data that follows it

@@ -163,6 +163,78 @@ __device__ __forceinline__ float2 encode_level(const uint32_t *__restrict__ tabl
     return make_float2(a0, a1);
 }
 
+// Table entry of F FP16 features: F = 4 one 8-byte word, F = 8 one 16-byte word (F = 2 is the
+// 32-bit word encode_level reads).
+template <uint32_t F>
+struct GridEntry;
+template <>
+struct GridEntry<4> {
+    using T = uint2;
+    __device__ static __forceinline__ void halves(const T &v, uint32_t (&w)[2]) { w[0] = v.x, w[1] = v.y; }
+};
+template <>
+struct GridEntry<8> {
+    using T = uint4;
+    __device__ static __forceinline__ void halves(const T &v, uint32_t (&w)[4])
+    {
+        w[0] = v.x, w[1] = v.y, w[2] = v.z, w[3] = v.w;
+    }
+};
+
+// Features of one point at one level for F = 4 or 8 features per entry: the corners and weights of
+// encode_level, feature k of corner c accumulated as acc_k = fma(w_c, entry_c[k], acc_k) in corner
+// order (the CPU restatement's order). `table` is the grid's first entry (16-byte aligned).
+template <uint32_t F>
+__device__ __forceinline__ void encode_level_wide(const void *__restrict__ table, const GridParams &gp, uint32_t l,
+                                                  V3 p, float (&acc)[F])
+{
+    using E = GridEntry<F>;
+    const typename E::T *tab = reinterpret_cast<const typename E::T *>(table);
+    const float s = gp.scale[l];
+    const float px = __fmaf_rn(p.x, s, 0.5f), py = __fmaf_rn(p.y, s, 0.5f), pz = __fmaf_rn(p.z, s, 0.5f);
+    const float flx = floorf(px), fly = floorf(py), flz = floorf(pz);
+    const uint32_t gx = (uint32_t)(int32_t)flx, gy = (uint32_t)(int32_t)fly, gz = (uint32_t)(int32_t)flz;
+    const float rx = __fsub_rn(px, flx), ry = __fsub_rn(py, fly), rz = __fsub_rn(pz, flz);
+    const uint32_t res = gp.res[l], size = gp.size[l], off = gp.offset[l];
+    const bool hashed = gp.hashed[l] != 0u;
+    const float wx0 = __fsub_rn(1.0f, rx), wy0 = __fsub_rn(1.0f, ry), wz0 = __fsub_rn(1.0f, rz);
+#pragma unroll
+    for (uint32_t k = 0; k < F; k++)
+        acc[k] = 0.0f;
+    // corners in two groups of four, so that at most four wide gathers are live at once
+#pragma unroll
+    for (uint32_t c0 = 0; c0 < 8; c0 += 4) {
+        typename E::T v[4];
+#pragma unroll
+        for (uint32_t cc = 0; cc < 4; cc++) {
+            const uint32_t c = c0 + cc;
+            const uint32_t x = gx + (c & 1u), y = gy + ((c >> 1) & 1u), z = gz + ((c >> 2) & 1u);
+            uint32_t idx;
+            if (hashed) {
+                idx = (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (size - 1u);
+            } else {
+                idx = x + y * res + z * res * res;
+                if (idx >= size)
+                    idx %= size;
+            }
+            v[cc] = __ldg(tab + off + idx);
+        }
+#pragma unroll
+        for (uint32_t cc = 0; cc < 4; cc++) {
+            const uint32_t c = c0 + cc;
+            const float w = __fmul_rn(__fmul_rn((c & 1u) ? rx : wx0, (c & 2u) ? ry : wy0), (c & 4u) ? rz : wz0);
+            uint32_t h[F / 2];
+            E::halves(v[cc], h);
+#pragma unroll
+            for (uint32_t k = 0; k < F / 2; k++) {
+                const float2 f = unpack_half2(h[k]);
+                acc[2 * k] = __fmaf_rn(w, f.x, acc[2 * k]);
+                acc[2 * k + 1] = __fmaf_rn(w, f.y, acc[2 * k + 1]);
+            }
+        }
+    }
+}
+
 // FP8 activations of a pair packed as FP16 (lo in the low half): e4m3(max(x, 0) * 2^7) / 2^7 per
 // value, through the hardware conversions to and from E4M3 (nearest even, saturating at 448,
 // subnormals on the 2^-9 grid: the rounding e4m3_round states); the 2^-7 scale is exact in FP16.
@@ -312,6 +384,68 @@ __device__ __forceinline__ void encode_tile_to_smem(const uint32_t *__restrict__
         }
     }
     __syncwarp();
+}
+
+// encode_tile_to_smem for 4 or 8 features per level: lane j handles the (point, level) pairs
+// j, j + 32, ... and writes their F features (one 8- or 16-byte store per row), 8 / F rows at a
+// time so that the same number of gathered words is in flight as in the 2-feature form.
+template <bool BF16, uint32_t F, typename PosFn>
+__device__ __forceinline__ void encode_tile_to_smem_wide(const void *__restrict__ table, const GridParams &gp,
+                                                         PosFn &&pos, uint32_t active_mask16, __half *feat,
+                                                         uint32_t ld)
+{
+    constexpr uint32_t RB = 8u / F; // rows per batch
+    const int lane = threadIdx.x & 31;
+    const uint32_t L = gp.n_levels, PL = gp.n_points * gp.n_levels;
+    for (uint32_t j = (uint32_t)lane; j < PL; j += 32u) {
+        const uint32_t p = j / L, l = j - p * L;
+        for (uint32_t r0 = 0; r0 < 16u; r0 += RB) {
+            const uint32_t mb = (active_mask16 >> r0) & ((1u << RB) - 1u);
+            uint32_t w[RB][F / 2];
+            if (mb == 0u) {
+#pragma unroll
+                for (uint32_t k = 0; k < RB; k++)
+#pragma unroll
+                    for (uint32_t q = 0; q < F / 2; q++)
+                        w[k][q] = 0u;
+            } else {
+                V3 qp[RB];
+#pragma unroll
+                for (uint32_t k = 0; k < RB; k++)
+                    qp[k] = ((mb >> k) & 1u) ? pos(r0 + k, p) : mk3(0.5f, 0.5f, 0.5f);
+#pragma unroll
+                for (uint32_t k = 0; k < RB; k++) {
+                    float f[F];
+                    encode_level_wide<F>(table, gp, l, qp[k], f);
+#pragma unroll
+                    for (uint32_t q = 0; q < F / 2; q++)
+                        w[k][q] = ((mb >> k) & 1u) ? MlpPrec<BF16>::pack(f[2 * q], f[2 * q + 1]) : 0u;
+                }
+            }
+#pragma unroll
+            for (uint32_t k = 0; k < RB; k++) {
+                __half *dst = feat + (r0 + k) * ld + F * j;
+                if constexpr (F == 4)
+                    *reinterpret_cast<uint2 *>(dst) = make_uint2(w[k][0], w[k][1]);
+                else
+                    *reinterpret_cast<uint4 *>(dst) = make_uint4(w[k][0], w[k][1], w[k][2], w[k][3]);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// The encode phase of a 16-row tile for the grid's features per level (2, 4 or 8).
+template <bool BF16, typename PosFn>
+__device__ __forceinline__ void encode_tile_any(const uint32_t *__restrict__ table, const GridParams &gp, PosFn &&pos,
+                                                uint32_t active_mask16, __half *feat, uint32_t ld)
+{
+    if (gp.n_features == 4u)
+        encode_tile_to_smem_wide<BF16, 4>(table, gp, pos, active_mask16, feat, ld);
+    else if (gp.n_features == 8u)
+        encode_tile_to_smem_wide<BF16, 8>(table, gp, pos, active_mask16, feat, ld);
+    else
+        encode_tile_to_smem<BF16>(table, gp, pos, active_mask16, feat, ld);
 }
 
 // MLP phase of a 16-row tile whose 16-bit features are in feat[16][ld]; outputs as mlp_forward_tile.

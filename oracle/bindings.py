@@ -46,7 +46,8 @@ class Network(C.Structure):
                 ("n_neurons", C.c_uint32), ("n_hidden_layers", C.c_uint32), ("level_offset", C.c_void_p),
                 ("level_size", C.c_void_p), ("level_resolution", C.c_void_p), ("level_scale", C.c_void_p),
                 ("grid_f16", C.c_void_p), ("weights_f16", C.c_void_p), ("exact", C.c_int32),
-                ("grid_f32", C.c_void_p), ("weights_f32", C.c_void_p), ("bf16", C.c_int32), ("fp8", C.c_int32)]
+                ("grid_f32", C.c_void_p), ("weights_f32", C.c_void_p), ("bf16", C.c_int32), ("fp8", C.c_int32),
+                ("n_features", C.c_uint32)]
 
 
 class NeuralScene(C.Structure):
@@ -251,6 +252,7 @@ class Oracle:
         net.grid_f32, net.weights_f32 = _p(g32).value, _p(w32).value
         net.bf16 = 1 if bf16 else 0
         net.fp8 = 1 if int(cfg.network.precision) == 2 else 0
+        net.n_features = cfg.hashgrid.n_features_per_level
         return net
 
     # ---- queries ----

@@ -680,11 +680,15 @@ static inline uint32_t grid_index(uint32_t level_size, uint32_t res, uint32_t x,
     return idx % level_size;
 }
 
-/* features of one point for one level (2 values), fused multiply-add accumulation over the 8
- * corners in order c = 0..7 (bit d of c selects the upper corner along axis d) */
-static void encode_level(const orc_network *net, uint32_t l, v3 p, float *f0, float *f1, uint32_t *cidx,
-                         float *cw)
+/* number of features per level (entries hold that many FP16 values); 2 when unset */
+static inline uint32_t net_features(const orc_network *net) { return net->n_features ? net->n_features : 2u; }
+
+/* features of one point for one level (F values), fused multiply-add accumulation over the 8
+ * corners in order c = 0..7 (bit d of c selects the upper corner along axis d), feature f of
+ * corner c accumulated as f_acc = fma(w_c, entry_c[f], f_acc) */
+static void encode_level(const orc_network *net, uint32_t l, v3 p, float *f, uint32_t *cidx, float *cw)
 {
+    const uint32_t F = net_features(net);
     float s = net->level_scale[l];
     float pos[3] = {fmaf(p.x, s, 0.5f), fmaf(p.y, s, 0.5f), fmaf(p.z, s, 0.5f)};
     uint32_t g[3];
@@ -694,7 +698,7 @@ static void encode_level(const orc_network *net, uint32_t l, v3 p, float *f0, fl
         g[d] = (uint32_t)(int32_t)fl;
         fr[d] = pos[d] - fl;
     }
-    float a0 = 0.f, a1 = 0.f;
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (uint32_t c = 0; c < 8; c++) {
         float wx = (c & 1u) ? fr[0] : 1.0f - fr[0];
         float wy = (c & 2u) ? fr[1] : 1.0f - fr[1];
@@ -703,26 +707,32 @@ static void encode_level(const orc_network *net, uint32_t l, v3 p, float *f0, fl
         uint32_t idx = grid_index(net->level_size[l], net->level_resolution[l], g[0] + (c & 1u),
                                   g[1] + ((c >> 1) & 1u), g[2] + ((c >> 2) & 1u));
         uint32_t e = net->level_offset[l] + idx;
-        a0 = fmaf(w, net_g(net, 2u * e), a0);
-        a1 = fmaf(w, net_g(net, 2u * e + 1u), a1);
+        for (uint32_t k = 0; k < F; k++)
+            acc[k] = fmaf(w, net_g(net, (size_t)F * e + k), acc[k]);
         if (cidx) {
             cidx[c] = e;
             cw[c] = w;
         }
     }
-    *f0 = a0;
-    *f1 = a1;
+    for (uint32_t k = 0; k < F; k++)
+        f[k] = acc[k];
+}
+
+/* features of one point: level l's F values at l * F (tcnn GridEncoding output order) */
+static void encode_point(const orc_network *net, v3 p, float *f, uint32_t (*cidx)[8], float (*cw)[8])
+{
+    const uint32_t F = net_features(net);
+    for (uint32_t l = 0; l < net->n_levels; l++)
+        encode_level(net, l, p, f + (size_t)F * l, cidx ? cidx[l] : NULL, cw ? cw[l] : NULL);
 }
 
 void orc_encode(const orc_network *net, const float *positions, uint32_t n, float *features)
 {
+    const uint32_t F = net_features(net);
     for (uint32_t i = 0; i < n; i++)
         for (uint32_t k = 0; k < net->n_points; k++) {
             v3 p = load3(positions + 3u * ((size_t)i * net->n_points + k));
-            for (uint32_t l = 0; l < net->n_levels; l++) {
-                float *f = features + (size_t)i * net->n_inputs + (size_t)k * net->n_levels * 2u + 2u * l;
-                encode_level(net, l, p, &f[0], &f[1], NULL, NULL);
-            }
+            encode_point(net, p, features + (size_t)i * net->n_inputs + (size_t)k * net->n_levels * F, NULL, NULL);
         }
 }
 
@@ -934,12 +944,9 @@ static void neural_query_one(const nq_job *j, uint32_t i)
         }
         float pts[3 * 16], feat[128], out[16];
         encode_segment(j->scene, c, ray_at(r.o, r.d, a), ray_at(r.o, r.d, b), &rng, pts);
-        for (int k = 0; k < c->input_segment_points; k++) {
-            v3 p = load3(pts + 3 * k);
-            for (uint32_t l = 0; l < j->net->n_levels; l++)
-                encode_level(j->net, l, p, &feat[(size_t)k * j->net->n_levels * 2u + 2u * l],
-                             &feat[(size_t)k * j->net->n_levels * 2u + 2u * l + 1u], NULL, NULL);
-        }
+        for (int k = 0; k < c->input_segment_points; k++)
+            encode_point(j->net, load3(pts + 3 * k), &feat[(size_t)k * j->net->n_levels * net_features(j->net)],
+                         NULL, NULL);
         mlp_row(j->net, feat, out, NULL, NULL);
         segments++;
         if (j->margin > 0.0f && fabsf(out[0] - thr) < j->margin) {
@@ -1327,7 +1334,8 @@ void orc_compute_gradients(const orc_network *net, const orc_loss_consts *lc, co
     matrix_offsets(net, off, rows, cols, &nm);
     uint32_t n_net = off[nm - 1u] + rows[nm - 1u] * cols[nm - 1u];
     uint32_t n_grid = net->level_offset[net->n_levels - 1u] + net->level_size[net->n_levels - 1u];
-    memset(gradients, 0, sizeof(double) * ((size_t)n_net + 2u * (size_t)n_grid));
+    const uint32_t F = net_features(net);
+    memset(gradients, 0, sizeof(double) * ((size_t)n_net + (size_t)F * n_grid));
     double total_loss = 0.0;
     float *acts = (float *)malloc(sizeof(float) * 128u * 16u);
     double dz[128], da[128];
@@ -1338,12 +1346,8 @@ void orc_compute_gradients(const orc_network *net, const orc_loss_consts *lc, co
         /* forward, keeping the corner indices and weights for the grid backward */
         uint32_t cidx[16][32][8];
         float cw[16][32][8];
-        for (uint32_t k = 0; k < net->n_points; k++) {
-            v3 p = load3(pos + 3u * k);
-            for (uint32_t l = 0; l < net->n_levels; l++)
-                encode_level(net, l, p, &feat[k * net->n_levels * 2u + 2u * l],
-                             &feat[k * net->n_levels * 2u + 2u * l + 1u], cidx[k][l], cw[k][l]);
-        }
+        for (uint32_t k = 0; k < net->n_points; k++)
+            encode_point(net, load3(pos + 3u * k), &feat[k * net->n_levels * F], cidx[k], cw[k]);
         mlp_row(net, feat, out, acts, pre);
         orc_composite_loss(lc, out, targets + 8u * (size_t)i, 1, loss_scale, vals, grads);
         /* the per-row loss values are normalised by n_total of a batch of one; rescale to n */
@@ -1385,21 +1389,17 @@ void orc_compute_gradients(const orc_network *net, const orc_loss_consts *lc, co
         /* grid backward: d feature = da (input gradient of the first layer) */
         double *gg = gradients + n_net;
         for (uint32_t k = 0; k < net->n_points; k++)
-            for (uint32_t l = 0; l < net->n_levels; l++) {
-                double g0 = da[k * net->n_levels * 2u + 2u * l];
-                double g1 = da[k * net->n_levels * 2u + 2u * l + 1u];
-                if (fp16_backward) {
-                    g0 = (double)round_mlp(net, (float)g0);
-                    g1 = (double)round_mlp(net, (float)g1);
+            for (uint32_t l = 0; l < net->n_levels; l++)
+                for (uint32_t q = 0; q < F; q++) {
+                    double gq = da[(k * net->n_levels + l) * F + q];
+                    if (fp16_backward)
+                        gq = (double)round_mlp(net, (float)gq);
+                    for (uint32_t cc = 0; cc < 8; cc++)
+                        gg[(size_t)F * cidx[k][l][cc] + q] += (double)cw[k][l][cc] * gq;
                 }
-                for (uint32_t cc = 0; cc < 8; cc++) {
-                    gg[2u * cidx[k][l][cc]] += (double)cw[k][l][cc] * g0;
-                    gg[2u * cidx[k][l][cc] + 1u] += (double)cw[k][l][cc] * g1;
-                }
-            }
     }
     free(acts);
-    for (size_t p = 0; p < (size_t)n_net + 2u * (size_t)n_grid; p++)
+    for (size_t p = 0; p < (size_t)n_net + (size_t)F * n_grid; p++)
         gradients[p] /= (double)loss_scale;
     *mean_loss = total_loss;
 }

@@ -73,14 +73,14 @@ void orc_neural_segments(const uint32_t *neural_nodes, const orc_neural_consts *
 typedef struct orc_network {
     uint32_t n_levels;
     uint32_t n_points;
-    uint32_t n_inputs;   /* n_points * n_levels * 2 */
+    uint32_t n_inputs;   /* n_points * n_levels * n_features */
     uint32_t n_neurons;  /* 64 */
     uint32_t n_hidden_layers;
     const uint32_t *level_offset;
     const uint32_t *level_size;
     const uint32_t *level_resolution;
     const float *level_scale;
-    const uint16_t *grid_f16;   /* n_grid_entries x 2 half bits */
+    const uint16_t *grid_f16;   /* n_grid_entries x n_features half bits */
     const uint16_t *weights_f16; /* network matrices as laid out by nbvh_param_layout */
     /* exact mode (finite-difference checks): FP32 parameters, no FP16 rounding anywhere */
     int32_t exact;
@@ -94,6 +94,8 @@ typedef struct orc_network {
      * scale 2^6 (e4m3(w * 64) / 64 of the FP32 weights) and the activations entering them are
      * FP8-E4M3 values at scale 2^7 (e4m3(a * 128) / 128). */
     int32_t fp8;
+    /* features per hash-grid level (HashGridOptions::n_features_per_level): 2, 4 or 8; 0 reads as 2 */
+    uint32_t n_features;
 } orc_network;
 
 /* Nearest FP8-E4M3 value (ties to even, saturating at +-448, subnormals on the 2^-9 grid). */

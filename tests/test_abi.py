@@ -67,13 +67,13 @@ def test_config_defaults(built):
     L = nb.param_layout(cfg)
     assert L.n_inputs == 128 and L.n_network_params == 128 * 64 + 3 * 64 * 64 + 16 * 64
     assert list(L.level_resolution[:16])[0] == 16 and list(L.level_resolution[:16])[-1] == 2048
-    assert L.n_params == L.n_network_params + 2 * L.n_grid_entries
+    assert L.n_params == L.n_network_params + 2 * L.n_grid_entries and L.n_features_per_level == 2
 
 
 def test_config_validation(built):
     lib = nb.load_library()
     L = abi.ParamLayout()
-    for key, val in (("hashgrid.n_features_per_level", 4), ("network.n_neurons", 128), ("batch_size", 1000),
+    for key, val in (("hashgrid.n_features_per_level", 3), ("network.n_neurons", 128), ("batch_size", 1000),
                      ("module.input_segment_points", 5), ("network.precision", 3)):
         cfg = nb.default_config(**{key: val})
         assert lib.nbvh_param_layout_host(C.byref(cfg), C.byref(L)) == abi.NBVH_EINVAL, key

@@ -20,16 +20,29 @@ from helpers import reference_root
 from nbvh_gb300 import abi
 
 
-def test_reference_defaults_and_unsupported_features(built):
+def test_reference_defaults_and_features_per_level(built):
     cfg = nb.reference_default_config()
     hg = cfg.hashgrid
     assert (hg.n_levels, hg.n_features_per_level, hg.log2_hashmap_size, hg.base_resolution) == (8, 4, 18, 8)
     assert hg.per_level_scale == 2.0 and cfg.module.input_segment_points == 3 and cfg.neural_bvh_max_depth == 0
-    # 4 features per level is the reference default but not supported here: validation says so
-    with pytest.raises(nb.NBVHError):
-        nb.param_layout(cfg)
-    cfg.hashgrid.n_features_per_level = 2
-    assert nb.param_layout(cfg).n_inputs == 3 * 8 * 2
+    # the reference default (3 points x 8 levels x 4 features = 96 network inputs) lays out
+    L = nb.param_layout(cfg)
+    assert L.n_inputs == 3 * 8 * 4 and L.n_features_per_level == 4
+    assert L.n_params == L.n_network_params + 4 * L.n_grid_entries
+    for f in (2, 8):
+        cfg.hashgrid.n_features_per_level = f
+        if 3 * 8 * f <= 128:
+            L = nb.param_layout(cfg)
+            assert L.n_inputs == 3 * 8 * f and L.n_params == L.n_network_params + f * L.n_grid_entries
+        else:  # 3 x 8 x 8 = 192 inputs: more than the fused MLP takes
+            with pytest.raises(nb.NBVHError):
+                nb.param_layout(cfg)
+    cfg.module.input_segment_points = 2
+    assert nb.param_layout(cfg).n_inputs == 2 * 8 * 8
+    for f in (1, 3, 16):  # feature counts the table layout does not support
+        cfg.hashgrid.n_features_per_level = f
+        with pytest.raises(nb.NBVHError):
+            nb.param_layout(cfg)
 
 
 def test_every_key_maps_to_its_field(built):
@@ -116,7 +129,8 @@ def test_shipped_configurations_load_as_the_reference_reads_them(built):
         for k in ("splitting_interval", "last_split_iteration", "start_split_num"):
             if k in sch:
                 assert getattr(t, k) == sch[k], (p, k)
-        # the shipped grids use the reference's 4 features per level, which this library's kernels
-        # do not support: the configuration validates once that is set to 2
-        cfg.hashgrid.n_features_per_level = 2
-        assert nb.param_layout(cfg).n_inputs == cfg.module.input_segment_points * cfg.hashgrid.n_levels * 2
+        # the shipped grids use the reference's 4 features per level: they lay out as they are
+        L = nb.param_layout(cfg)
+        assert L.n_inputs == (cfg.module.input_segment_points * cfg.hashgrid.n_levels *
+                              cfg.hashgrid.n_features_per_level)
+        assert L.n_params == L.n_network_params + cfg.hashgrid.n_features_per_level * L.n_grid_entries

@@ -1,0 +1,146 @@
+"""Hash grids with 4 and 8 features per level on the GPU against the CPU oracle.
+
+The reference's own default grid (include/cuda/neural/utils/tcnn_config.h:69-78: 8 levels x 4
+features x 2^18 entries, base resolution 8, scale 2) and its shipped chess configurations encode
+3 points per segment into 96 network inputs. Here:
+
+* the shipped chess configuration (tests/golden/chess_config_hash18.json, made by
+  tests/golden/make_config_golden.py) creates a handle, trains and answers queries;
+* with F = 4 (the reference default, 96 inputs) and F = 8 (2 points x 8 levels, 128 inputs):
+  encoding bit-identical, network outputs within 5e-3, full neural queries as in
+  test_gpu_neural.py, gradients within 2e-2 relative L2 per parameter block, and training lowers
+  the loss.
+"""
+
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import nbvh_gb300 as nb
+from helpers import as_u32, handle
+from nbvh_gb300 import scenes
+from test_gpu_neural import _borderline, _compare_queries, _cuda, _spread_params
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "chess_config_hash18.json")
+
+
+def _config(features):
+    cfg = nb.reference_default_config()
+    cfg.neural_bvh_max_depth = 10
+    cfg.batch_size = 1 << 14
+    if features == 8:
+        cfg.hashgrid.n_features_per_level = 8
+        cfg.hashgrid.log2_hashmap_size = 16
+        cfg.module.input_segment_points = 2
+    return cfg
+
+
+@pytest.fixture(scope="module", params=[4, 8])
+def scene(request, built):
+    h, s = handle(_config(request.param), kind="sphere65k", seed=1, albedo=True)
+    s["params"] = _spread_params(h, seed=7)
+    s["features"] = request.param
+    yield h, s
+    h.close()
+
+
+def test_layout(scene):
+    h, s = scene
+    F = s["features"]
+    assert h.layout.n_features_per_level == F
+    assert h.layout.n_inputs == h.cfg.module.input_segment_points * 8 * F
+    assert h.layout.n_params == h.layout.n_network_params + F * h.layout.n_grid_entries
+
+
+def test_encoding_bit_exact(scene, oracle):
+    h, s = scene
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(-0.01, 1.01, (4096, h.cfg.module.input_segment_points, 3)).astype(np.float32)
+    got = h.encode(_cuda(pos)).cpu().numpy()
+    ref = oracle.encode(oracle.network(h.cfg, h.layout, s["params"]), pos)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_network_inference(scene, oracle):
+    h, s = scene
+    rng = np.random.default_rng(4)
+    pos = rng.uniform(0.0, 1.0, (8192, h.cfg.module.input_segment_points, 3)).astype(np.float32)
+    got = h.network_inference(_cuda(pos)).cpu().numpy()
+    ref = oracle.network_inference(oracle.network(h.cfg, h.layout, s["params"]), pos, threads=8)[:, :8]
+    assert ref.std() > 0.05
+    assert np.max(np.abs(got - ref)) < 5e-3
+
+
+def test_neural_query_matches_oracle(scene, oracle):
+    h, s = scene
+    rays = scenes.uniform_rays(1 << 15, s["bbox"][:3], s["bbox"][3:], seed=32)
+    got = as_u32(h.query_closest_neural(_cuda(rays)))
+    net = oracle.network(h.cfg, h.layout, s["params"])
+    ref = oracle.neural_query(oracle.neural_scene(s["neural"], s["bbox"]), net, oracle.neural_consts(h.cfg), rays,
+                              threads=8)
+    border = _borderline(h, oracle, s, rays)
+    both = _compare_queries(got, ref, border)
+    assert both.sum() > 100
+    assert np.mean(got[~border, 9] == ref[~border, 9]) > 0.998  # segments evaluated
+    st = h.query_stats()
+    assert st.step_capped == 0 and st.stack_overflow == 0
+
+
+def test_gradients_match_oracle(scene, oracle):
+    h, s = scene
+    h.set_params(s["params"])
+    pos, tgt, _ = h.generate_training_batch(3, 2048)
+    g, loss = h.compute_gradients(pos, tgt)
+    g = g.cpu().numpy().astype(np.float64)
+    net = oracle.network(h.cfg, h.layout, s["params"])
+    rg, rloss = oracle.compute_gradients(net, oracle.loss_consts(h.cfg), pos.cpu().numpy(), tgt.cpu().numpy(),
+                                         h.layout.n_params, loss_scale=h.cfg.optimizer.loss_scale)
+    assert abs(loss - rloss) <= 1e-3 * abs(rloss) + 1e-6
+    nn = h.layout.n_network_params
+    H = h.cfg.network.n_hidden_layers
+    off, blocks = 0, []
+    for m in range(H + 1):
+        rows, cols = (16 if m == H else 64), (h.layout.n_inputs if m == 0 else 64)
+        blocks.append((off, off + rows * cols))
+        off += rows * cols
+    blocks.append((nn, h.layout.n_params))
+    for a, b in blocks:
+        err = np.linalg.norm(g[a:b] - rg[a:b]) / max(np.linalg.norm(rg[a:b]), 1e-30)
+        assert err < 2e-2, (a, b, err)
+
+
+def test_training_lowers_loss(scene):
+    h, s = scene
+    h.set_params(nb.init_params(h.cfg))
+    first = h.run_optimisation(20)
+    last = h.run_optimisation(200)
+    assert np.isfinite(last.last_loss) and last.mean_loss < first.mean_loss
+    h.set_params(s["params"])
+
+
+def test_shipped_chess_configuration_runs(built, oracle):
+    with open(GOLDEN) as f:
+        js = json.load(f)
+    cfg = nb.config_from_reference_json(js)
+    hg = cfg.hashgrid
+    assert (hg.n_levels, hg.n_features_per_level, hg.log2_hashmap_size) == (8, 4, 18)
+    cfg.batch_size = 1 << 14  # the shipped 2^18 rays per step, scaled down for the test
+    h, s = handle(cfg, kind="sphere65k", seed=1, depth=10, albedo=True)
+    try:
+        assert h.layout.n_inputs == 96
+        st = h.run_optimisation(30)
+        assert np.isfinite(st.last_loss)
+        rays = scenes.uniform_rays(1 << 14, s["bbox"][:3], s["bbox"][3:], seed=5)
+        got = as_u32(h.query_closest_neural(_cuda(rays)))
+        s["params"] = h.params()
+        net = oracle.network(h.cfg, h.layout, s["params"])
+        ref = oracle.neural_query(oracle.neural_scene(s["neural"], s["bbox"]), net, oracle.neural_consts(h.cfg),
+                                  rays, threads=8)
+        _compare_queries(got, ref, _borderline(h, oracle, s, rays))
+    finally:
+        h.close()

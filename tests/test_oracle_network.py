@@ -39,8 +39,9 @@ def numpy_forward(cfg, L, p, feats):
     return 1.0 / (1.0 + np.exp(-x))
 
 
-def test_forward_matches_numpy(oracle, built):
-    cfg = small_cfg()
+@pytest.mark.parametrize("features", [2, 4, 8])
+def test_forward_matches_numpy(oracle, built, features):
+    cfg = small_cfg(**{"hashgrid.n_features_per_level": features})
     L, p = random_params(cfg)
     net = oracle.network(cfg, L, p, exact=True)
     pos = np.random.default_rng(1).uniform(0, 1, (64, 2, 3)).astype(np.float32)
@@ -51,6 +52,26 @@ def test_forward_matches_numpy(oracle, built):
     # FP16 mode rounds features / activations / parameters: close but not equal
     out16 = oracle.network_inference(oracle.network(cfg, L, p), pos)
     assert 0 < np.max(np.abs(out16 - ref)) < 2e-2
+
+
+@pytest.mark.parametrize("features", [4, 8])
+def test_wide_entries_equal_two_feature_grids(oracle, built, features):
+    """A level of F features per entry computes exactly what F / 2 grids of 2-feature entries
+    compute when grid k holds features 2k and 2k + 1 of every entry: the corners, weights and
+    per-feature accumulation order do not depend on F."""
+    cfg = small_cfg(**{"hashgrid.n_features_per_level": features})
+    L, p = random_params(cfg, seed=11)
+    pos = np.random.default_rng(12).uniform(-0.2, 1.2, (257, 2, 3)).astype(np.float32)
+    wide = oracle.encode(oracle.network(cfg, L, p), pos).reshape(257, 2, 4, features)
+    cfg2 = small_cfg()
+    L2 = nb.param_layout(cfg2)
+    assert L2.n_grid_entries == L.n_grid_entries
+    grid = p[L.n_network_params:].reshape(L.n_grid_entries, features)
+    for k in range(features // 2):
+        p2 = np.zeros(L2.n_params, np.float32)
+        p2[L2.n_network_params:] = grid[:, 2 * k:2 * k + 2].reshape(-1)
+        narrow = oracle.encode(oracle.network(cfg2, L2, p2), pos).reshape(257, 2, 4, 2)
+        assert np.array_equal(narrow.view(np.uint32), wide[..., 2 * k:2 * k + 2].copy().view(np.uint32))
 
 
 def _bf16_round(x):
@@ -85,8 +106,10 @@ def test_bf16_forward_matches_rounded_numpy(oracle, built):
     assert np.max(np.abs(out16 - out)) > 1e-4
 
 
-def test_backward_matches_finite_differences(oracle, built):
-    cfg = small_cfg(**{"output.visibility_loss": nb.abi.LOSS["L2"], "output.depth_loss": nb.abi.LOSS["L2"],
+@pytest.mark.parametrize("features", [2, 4, 8])
+def test_backward_matches_finite_differences(oracle, built, features):
+    cfg = small_cfg(**{"hashgrid.n_features_per_level": features,
+                       "output.visibility_loss": nb.abi.LOSS["L2"], "output.depth_loss": nb.abi.LOSS["L2"],
                        "output.normal_loss": nb.abi.LOSS["L2"], "output.albedo_loss": nb.abi.LOSS["L2"],
                        "output.visibility_masking_loss": 0, "output.output_normal_linear_activation": 0})
     L, p = random_params(cfg, seed=3)
