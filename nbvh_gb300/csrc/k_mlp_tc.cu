@@ -131,18 +131,6 @@ __device__ __forceinline__ void issue_layer_ta(uint32_t tmem, uint32_t a_col, ui
     }
 }
 
-// Two FP32 values -> ReLU -> 16-bit pair (lo in the low half), one cvt.rn.relu instruction.
-template <bool BF16>
-__device__ __forceinline__ uint32_t pack_relu(float lo, float hi)
-{
-    uint32_t r;
-    if constexpr (BF16)
-        asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;\n" : "=r"(r) : "f"(hi), "f"(lo));
-    else
-        asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;\n" : "=r"(r) : "f"(hi), "f"(lo));
-    return r;
-}
-
 // Hidden-layer epilogue for this thread's row: 64 accumulator columns -> ReLU -> 16-bit (FP16 or
 // BF16) -> the next layer's A operand, 32 columns of this row's lane from column kActCol on.
 template <bool BF16, bool FP8>
@@ -379,7 +367,8 @@ cudaError_t launch_pack_weights(const __half *params_h, uint32_t n_inputs, uint3
     return cudaGetLastError();
 }
 
-cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t rows, TensorMapBytes *out)
+cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t rows, TensorMapBytes *out,
+                             bool allow_swizzle)
 {
     static_assert(sizeof(CUtensorMap) == sizeof(TensorMapBytes), "tensor map size");
     if ((reinterpret_cast<uintptr_t>(features) & 15u) != 0u || n_inputs % 16u != 0u || n_inputs > 128u || rows == 0u)
@@ -392,7 +381,7 @@ cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t
     const cuuint64_t strides[1] = {(cuuint64_t)n_inputs * 2u};
     // 64 values x 128 rows, 128-byte swizzle (one atom column of the K-major swizzled layout), or
     // 8 values x 128 rows unswizzled (one K column of core matrices)
-    const bool sw = feature_map_swizzled(n_inputs);
+    const bool sw = allow_swizzle && feature_map_swizzled(n_inputs);
     const cuuint32_t box[2] = {sw ? 64u : 8u, kTileRows};
     const cuuint32_t estr[2] = {1u, 1u};
     // 16-bit rows; the element type of the map only sizes the copy (FP16 and BF16 move the same bits)

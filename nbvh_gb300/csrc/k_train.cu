@@ -1,15 +1,22 @@
 // k_train.cu -- run-optimisation kernels: training-ray generation and labelling on the device,
-// fused forward + composite loss + backward (K3/K4 backward, hash-grid gradient scatter), the
-// weight-gradient pass on the tensor cores, and the fused Adam step (K5).
+// the hash-grid encoding of the training rows, forward + composite loss + backward with the weight
+// gradients on the tcgen05 tensor cores (K4 backward), the hash-grid gradient scatter (K3
+// backward) and the fused Adam step (K5).
 //
 // Reference path: NeuralBVHRenderer::render, m_run_optimisation branch
 // (src/cuda/neural/neural_bvh_renderer.cu:141-288): granular_sample_bvh_network_input_data
 // (src/cuda/neural/neural_bvh_module_kernels.cu:119-264), then tcnn's trainer->training_step
 // (encoding + FullyFusedMLP forward, PathTracingCompositeLoss, backward, Adam wrapped in
 // ExponentialDecay; configured at src/cuda/neural/neural_bvh_module.cu:118-263).
+#include <cuda.h>
+
+#include <cstring>
+#include <vector>
+
 #include "device_math.cuh"
 #include "net_device.cuh"
 #include "nbvh_internal.h"
+#include "tc_device.cuh"
 
 namespace nbvh {
 
@@ -274,27 +281,14 @@ __device__ __forceinline__ void composite_loss(const LossConsts &lc, uint32_t ch
 }
 
 // ---------------------------------------------------------------------------------------------
-// Fused forward + loss + backward (data gradients). One warp per 16-row tile. Per row it writes
-// the FP16 input activation of every layer (acts) and the pre-activation gradient of every layer
-// (dz) for the weight-gradient pass, and scatters the input-feature gradient into the hash-grid
-// gradient with 64-bit vector atomics.
+// The hash-grid features of the training rows, in the MLP precision, into rows of row_stride
+// halves (n_inputs: the tensor-core kernel's feature rows): one thread per (row, point), the
+// levels in order, F features per level stored together (K3 forward).
 // ---------------------------------------------------------------------------------------------
-
-__device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const void *p)
-{
-    uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(a));
-}
-
-// The hash-grid features of the training rows, in the MLP precision, into the first n_inputs
-// activations of each row (acts row stride acts_stride halves): one thread per (row, point), the
-// levels in order, F features per level stored together.
 __global__ void __launch_bounds__(256) k_train_encode(const __grid_constant__ GridParams grid,
                                                       const uint32_t *__restrict__ table,
                                                       const float *__restrict__ positions, uint32_t n,
-                                                      __half *__restrict__ acts, uint32_t acts_stride, uint32_t bf16)
+                                                      __half *__restrict__ feat, uint32_t row_stride, uint32_t bf16)
 {
     const uint32_t P = grid.n_points, L = grid.n_levels, F = grid.n_features;
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -304,7 +298,7 @@ __global__ void __launch_bounds__(256) k_train_encode(const __grid_constant__ Gr
     const float *src = positions + i * 3u;
     const V3 pos = mk3(__ldg(src), __ldg(src + 1), __ldg(src + 2));
     auto pack16 = [bf16](float lo, float hi) { return bf16 ? pack_bf162(lo, hi) : pack_half2(lo, hi); };
-    __half *dst = acts + (size_t)row * acts_stride + (size_t)p * L * F;
+    __half *dst = feat + (size_t)row * row_stride + (size_t)p * L * F;
     for (uint32_t l = 0; l < L; l++) {
         if (F == 4u) {
             float f[4];
@@ -322,416 +316,417 @@ __global__ void __launch_bounds__(256) k_train_encode(const __grid_constant__ Gr
     }
 }
 
-struct TrainArgs {
-    GridParams grid;
-    LossConsts lc;
-    const uint32_t *table;
-    const __half *weights;
-    const float *positions;
-    const float *targets;
-    __half *acts;      // n x acts_stride
-    __half *dz;        // n x dz_stride
-    float2 *grid_grad; // n_grid_entries x (n_features / 2) feature pairs
-    float *loss_sum;
-    float *sample_loss; // per row: sum of its output channels' loss values (may be NULL)
-    uint32_t fp8;       // hidden-matrix inputs rounded to FP8-E4M3 (straight-through in the backward)
-    uint32_t n_hidden_layers;
-    uint32_t n;
-};
-
-constexpr int kTrainWarps = 8;
-constexpr int kTrainThreads = kTrainWarps * 32;
-
-template <bool BF16, bool FP8>
-__global__ void __launch_bounds__(kTrainThreads, 1) k_train_fwd_bwd(const __grid_constant__ TrainArgs a)
-{
-    using Pr = MlpPrec<BF16>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    GridParams &gp = *reinterpret_cast<GridParams *>(smem_raw);
-    const uint32_t n_in = a.grid.n_inputs, P = a.grid.n_points, L = a.grid.n_levels, H = a.n_hidden_layers;
-    const SmemNetLayout SL = smem_net_layout(n_in, H);
-    __half *sw = reinterpret_cast<__half *>(smem_raw + kGridParamsSmem);
-    {
-        const uint32_t *s = reinterpret_cast<const uint32_t *>(&a.grid);
-        uint32_t *dd = reinterpret_cast<uint32_t *>(&gp);
-        for (uint32_t i = threadIdx.x; i < sizeof(GridParams) / 4u; i += blockDim.x)
-            dd[i] = s[i];
-    }
-    load_weights_to_smem(a.weights, sw, n_in, H);
-    __syncthreads();
-
-    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
-    const uint32_t acts_stride = n_in + H * kNeurons, dz_stride = H * kNeurons + kOutputsPadded;
-    const uint32_t n_tiles = (a.n + 15u) / 16u;
-    const uint32_t warps_total = gridDim.x * kTrainWarps;
-    float loss_acc = 0.f;
-
-    for (uint32_t tile = blockIdx.x * kTrainWarps + (threadIdx.x >> 5); tile < n_tiles; tile += warps_total) {
-        const uint32_t r0 = tile * 16u + g, r1 = r0 + 8u;
-        const bool act0 = r0 < a.n, act1 = r1 < a.n;
-        auto pos_of = [&](uint32_t row, uint32_t p) -> V3 {
-            const float *src = a.positions + ((size_t)row * P + p) * 3u;
-            return mk3(__ldg(src), __ldg(src + 1), __ldg(src + 2));
-        };
-        // ---------------- forward ----------------
-        float acc[8][4];
-#pragma unroll
-        for (int nt = 0; nt < 8; nt++)
-            acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-        for (uint32_t kb = 0; kb < n_in / 16u; kb++) {
-            // the encoded features (k_train_encode wrote them to the rows' first n_in activations)
-            uint32_t af[4];
-            auto feat = [&](bool act, uint32_t row, uint32_t col) -> uint32_t {
-                return act ? *reinterpret_cast<const uint32_t *>(a.acts + (size_t)row * acts_stride + col) : 0u;
-            };
-            af[0] = feat(act0, r0, kb * 16u + tig * 2u);
-            af[1] = feat(act1, r1, kb * 16u + tig * 2u);
-            af[2] = feat(act0, r0, kb * 16u + tig * 2u + 8u);
-            af[3] = feat(act1, r1, kb * 16u + tig * 2u + 8u);
-            const __half *wrow = sw + g * SL.ld0 + kb * 16u + tig * 2;
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                uint32_t b0 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * SL.ld0);
-                uint32_t b1 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * SL.ld0 + 8);
-                Pr::mma(acc[nt], af, b0, b1);
-            }
-        }
-        uint32_t ah[4][4];
-        for (uint32_t layer = 1; layer <= H; layer++) {
-            relu_pack<BF16, FP8>(acc, ah, layer < H); // FP8 mode: inputs of the hidden matrices
-            // store x_layer (input of matrix `layer`)
-            __half *dst0 = a.acts + (size_t)r0 * acts_stride + n_in + (layer - 1u) * kNeurons;
-            __half *dst1 = a.acts + (size_t)r1 * acts_stride + n_in + (layer - 1u) * kNeurons;
-#pragma unroll
-            for (int kb = 0; kb < 4; kb++) {
-                if (act0) {
-                    *reinterpret_cast<uint32_t *>(dst0 + kb * 16 + tig * 2) = ah[kb][0];
-                    *reinterpret_cast<uint32_t *>(dst0 + kb * 16 + tig * 2 + 8) = ah[kb][2];
-                }
-                if (act1) {
-                    *reinterpret_cast<uint32_t *>(dst1 + kb * 16 + tig * 2) = ah[kb][1];
-                    *reinterpret_cast<uint32_t *>(dst1 + kb * 16 + tig * 2 + 8) = ah[kb][3];
-                }
-            }
-            if (layer == H)
-                break;
-            const __half *wl = sw + SL.hidden_off + (layer - 1u) * kNeurons * kHiddenLd;
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++)
-                acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-#pragma unroll
-            for (int kb = 0; kb < 4; kb++) {
-                const __half *wrow = wl + g * kHiddenLd + kb * 16 + tig * 2;
-#pragma unroll
-                for (int nt = 0; nt < 8; nt++) {
-                    uint32_t b0 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * kHiddenLd);
-                    uint32_t b1 = *reinterpret_cast<const uint32_t *>(wrow + nt * 8 * kHiddenLd + 8);
-                    Pr::mma(acc[nt], ah[kb], b0, b1);
-                }
-            }
-        }
-        // output layer: only columns 0..7 carry outputs
-        float oc[4] = {0.f, 0.f, 0.f, 0.f};
-        {
-            const __half *wo = sw + SL.out_off + g * kHiddenLd + tig * 2;
-#pragma unroll
-            for (int kb = 0; kb < 4; kb++) {
-                uint32_t b0 = *reinterpret_cast<const uint32_t *>(wo + kb * 16);
-                uint32_t b1 = *reinterpret_cast<const uint32_t *>(wo + kb * 16 + 8);
-                Pr::mma(oc, ah[kb], b0, b1);
-            }
-        }
-        // ---------------- loss ----------------
-        float dzo[4], row_vals[4];
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-            const uint32_t row = (e < 2) ? r0 : r1;
-            const bool act = (e < 2) ? act0 : act1;
-            const uint32_t ch = (uint32_t)tig * 2u + (uint32_t)(e & 1);
-            float y = 1.0f / (1.0f + expf(-oc[e]));
-            float value = 0.f, gr = 0.f;
-            if (act) {
-                const float tgt = __ldg(a.targets + (size_t)row * 8u + ch);
-                const float tvis = __ldg(a.targets + (size_t)row * 8u);
-                composite_loss(a.lc, ch, y, tgt, tvis, value, gr);
-                gr = Pr::round(gr); // 16-bit output gradient
-            }
-            loss_acc += value;
-            row_vals[e] = value;
-            dzo[e] = gr * y * (1.0f - y); // sigmoid backward
-        }
-        if (a.sample_loss) { // the four lanes of a quad hold the eight channels of rows r0 and r1
-            float l0 = row_vals[0] + row_vals[1], l1 = row_vals[2] + row_vals[3];
-            l0 += __shfl_xor_sync(kFull, l0, 1);
-            l1 += __shfl_xor_sync(kFull, l1, 1);
-            l0 += __shfl_xor_sync(kFull, l0, 2);
-            l1 += __shfl_xor_sync(kFull, l1, 2);
-            if (tig == 0) {
-                if (act0)
-                    a.sample_loss[r0] = l0;
-                if (act1)
-                    a.sample_loss[r1] = l1;
-            }
-        }
-        // dz_out (cols 0..7; 8..15 stay zero)
-        {
-            uint32_t lo = Pr::pack(dzo[0], dzo[1]), hi = Pr::pack(dzo[2], dzo[3]);
-            if (act0) {
-                __half *dst = a.dz + (size_t)r0 * dz_stride + H * kNeurons;
-                *reinterpret_cast<uint32_t *>(dst + tig * 2) = lo;
-                *reinterpret_cast<uint32_t *>(dst + 8 + tig * 2) = 0u;
-            }
-            if (act1) {
-                __half *dst = a.dz + (size_t)r1 * dz_stride + H * kNeurons;
-                *reinterpret_cast<uint32_t *>(dst + tig * 2) = hi;
-                *reinterpret_cast<uint32_t *>(dst + 8 + tig * 2) = 0u;
-            }
-        }
-        // ---------------- backward ----------------
-        // dx_H = dz_out . W_out (K = 16 outputs, only 0..7 non-zero)
-        uint32_t adz[4][4]; // A fragments of the current dz (k = out channel)
-        adz[0][0] = Pr::pack(dzo[0], dzo[1]);
-        adz[0][1] = Pr::pack(dzo[2], dzo[3]);
-        adz[0][2] = 0u;
-        adz[0][3] = 0u;
-        uint32_t n_kb = 1;
-        const __half *wmat = sw + SL.out_off; // matrix whose transpose maps dz to dx
-        uint32_t wld = kHiddenLd;
-        for (int layer = (int)H; layer >= 1; layer--) {
-            // dx_layer (16 x 64) = dz . W  (B from W rows = k, contiguous in = n: ldmatrix.trans)
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++)
-                acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-            for (uint32_t kb = 0; kb < n_kb; kb++) {
-#pragma unroll
-                for (int np = 0; np < 4; np++) {
-                    uint32_t b[4];
-                    const __half *addr = wmat + (kb * 16u + (lane & 15)) * wld + np * 16 + (lane >> 4) * 8;
-                    ldsm_x4_trans(b, addr);
-                    Pr::mma(acc[2 * np], adz[kb], b[0], b[1]);
-                    Pr::mma(acc[2 * np + 1], adz[kb], b[2], b[3]);
-                }
-            }
-            // dz_layer = dx_layer * (x_layer > 0), x_layer = input activation of matrix `layer`
-            const __half *x0 = a.acts + (size_t)r0 * acts_stride + n_in + (uint32_t)(layer - 1) * kNeurons;
-            const __half *x1 = a.acts + (size_t)r1 * acts_stride + n_in + (uint32_t)(layer - 1) * kNeurons;
-            __half *dzw0 = a.dz + (size_t)r0 * dz_stride + (uint32_t)(layer - 1) * kNeurons;
-            __half *dzw1 = a.dz + (size_t)r1 * dz_stride + (uint32_t)(layer - 1) * kNeurons;
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                float2 m0 = act0 ? Pr::unpack(*reinterpret_cast<const uint32_t *>(x0 + nt * 8 + tig * 2))
-                                 : make_float2(0.f, 0.f);
-                float2 m1 = act1 ? Pr::unpack(*reinterpret_cast<const uint32_t *>(x1 + nt * 8 + tig * 2))
-                                 : make_float2(0.f, 0.f);
-                acc[nt][0] = m0.x > 0.f ? acc[nt][0] : 0.f;
-                acc[nt][1] = m0.y > 0.f ? acc[nt][1] : 0.f;
-                acc[nt][2] = m1.x > 0.f ? acc[nt][2] : 0.f;
-                acc[nt][3] = m1.y > 0.f ? acc[nt][3] : 0.f;
-            }
-#pragma unroll
-            for (int kb = 0; kb < 4; kb++) {
-                adz[kb][0] = Pr::pack(acc[2 * kb][0], acc[2 * kb][1]);
-                adz[kb][1] = Pr::pack(acc[2 * kb][2], acc[2 * kb][3]);
-                adz[kb][2] = Pr::pack(acc[2 * kb + 1][0], acc[2 * kb + 1][1]);
-                adz[kb][3] = Pr::pack(acc[2 * kb + 1][2], acc[2 * kb + 1][3]);
-                if (act0) {
-                    *reinterpret_cast<uint32_t *>(dzw0 + kb * 16 + tig * 2) = adz[kb][0];
-                    *reinterpret_cast<uint32_t *>(dzw0 + kb * 16 + tig * 2 + 8) = adz[kb][2];
-                }
-                if (act1) {
-                    *reinterpret_cast<uint32_t *>(dzw1 + kb * 16 + tig * 2) = adz[kb][1];
-                    *reinterpret_cast<uint32_t *>(dzw1 + kb * 16 + tig * 2 + 8) = adz[kb][3];
-                }
-            }
-            n_kb = 4;
-            wmat = (layer >= 2) ? sw + SL.hidden_off + (uint32_t)(layer - 2) * kNeurons * kHiddenLd : sw;
-            wld = (layer >= 2) ? kHiddenLd : SL.ld0;
-        }
-        // dx_0 (16 x n_in) = dz_1 . W_0, n-tile by n-tile, scattered into the grid gradient
-        for (uint32_t nt = 0; nt < n_in / 8u; nt++) {
-            float dx[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int kb = 0; kb < 4; kb++) {
-                uint32_t b[4];
-                // x2 is enough here; reuse the x4 form with the upper half pointing at the same tile
-                const __half *addr = sw + (kb * 16u + (lane & 15)) * SL.ld0 + nt * 8u;
-                ldsm_x4_trans(b, addr);
-                Pr::mma(dx, adz[kb], b[0], b[1]);
-            }
-            // feature pair j = nt * 4 + tig (features 2 sub, 2 sub + 1 of level l of point p) for
-            // rows r0, r1
-            const uint32_t j = nt * 4u + (uint32_t)tig;
-            const uint32_t pairs = gp.n_features / 2u;
-            const uint32_t pl = j / pairs, sub = j - pl * pairs;
-            const uint32_t p = pl / L, l = pl - p * L;
-#pragma unroll
-            for (int rr = 0; rr < 2; rr++) {
-                const bool act = rr ? act1 : act0;
-                if (!act)
-                    continue;
-                const uint32_t row = rr ? r1 : r0;
-                const float g0 = Pr::round(dx[2 * rr]);
-                const float g1 = Pr::round(dx[2 * rr + 1]);
-                if (g0 == 0.f && g1 == 0.f)
-                    continue;
-                // corner indices / weights of this (row, point, level), as encode_level
-                V3 pp = pos_of(row, p);
-                const float s = gp.scale[l];
-                const float px = __fmaf_rn(pp.x, s, 0.5f), py = __fmaf_rn(pp.y, s, 0.5f), pz = __fmaf_rn(pp.z, s, 0.5f);
-                const float flx = floorf(px), fly = floorf(py), flz = floorf(pz);
-                const uint32_t gx = (uint32_t)(int32_t)flx, gy = (uint32_t)(int32_t)fly, gz = (uint32_t)(int32_t)flz;
-                const float rx = __fsub_rn(px, flx), ry = __fsub_rn(py, fly), rz = __fsub_rn(pz, flz);
-                const uint32_t res = gp.res[l], size = gp.size[l], off = gp.offset[l];
-                const bool hashed = gp.hashed[l] != 0u;
-#pragma unroll
-                for (uint32_t c = 0; c < 8; c++) {
-                    uint32_t x = gx + (c & 1u), y = gy + ((c >> 1) & 1u), z = gz + ((c >> 2) & 1u);
-                    uint32_t idx;
-                    if (hashed) {
-                        idx = (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (size - 1u);
-                    } else {
-                        idx = x + y * res + z * res * res;
-                        if (idx >= size)
-                            idx %= size;
-                    }
-                    float w = __fmul_rn(__fmul_rn((c & 1u) ? rx : __fsub_rn(1.0f, rx), (c & 2u) ? ry : __fsub_rn(1.0f, ry)),
-                                        (c & 4u) ? rz : __fsub_rn(1.0f, rz));
-                    atomicAdd(a.grid_grad + (size_t)(off + idx) * pairs + sub, make_float2(w * g0, w * g1));
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-        loss_acc += __shfl_xor_sync(kFull, loss_acc, off);
-    if (lane == 0 && loss_acc != 0.f)
-        atomicAdd(a.loss_sum, loss_acc);
-}
-
 // ---------------------------------------------------------------------------------------------
-// Weight gradients dW_m = sum_rows dz_m^T x_m, split over row chunks: every block stages 64 rows of
-// activations and gradients in shared memory and accumulates all (m16, n8) output tiles of every
-// matrix in registers (tiles dealt round-robin to the warps), then adds them to the global FP32
-// gradient once.
+// Training forward + composite loss + backward on the tensor cores (K3/K4 backward).
+//
+// k_train_encode writes each row's FP16 features; then one CTA per SM (128 threads, one tile row
+// per thread and TMEM lane) runs 128-row tiles through
+//   forward   Z_{j+1} = X_j W_j^T for every matrix j (tcgen05, M = 128 rows), the ReLU'd 16-bit
+//             activations X_{j+1} written back to shared memory (and their ReLU masks kept in
+//             registers), then the sigmoid, the composite loss and dZ_out = dL/dZ_out;
+//   backward  for j = H .. 0: dX_j = dZ_{j+1} W_j (W_j read transposed, as an MN-major operand)
+//             and dW_j^T += X_j^T dZ_{j+1} over the tile's 128 rows (both operands read
+//             transposed from the same shared-memory tiles), then dZ_j = dX_j * (X_j > 0);
+//             dX_0, rounded to the MLP precision, goes to global memory for the grid scatter.
+// The weight gradients stay in tensor memory, accumulated over all the CTA's tiles, and are
+// added to the FP32 gradient once per CTA at the end. Every [128 rows][C columns] tile lives in
+// shared memory in the K-major core-matrix layout (8-column block c at c * 2,048 bytes, row r at
+// r * 16 within it): with M = rows it is a K-major operand (LBO 2,048, SBO 128), with K = rows an
+// MN-major one (LBO 128, SBO 2,048). The input tile arrives in that layout from TMA (8-value boxes).
 // ---------------------------------------------------------------------------------------------
 
-constexpr int kWgWarps = 8;
-constexpr int kWgThreads = kWgWarps * 32;
-constexpr uint32_t kWgRows = 64;
-constexpr int kMaxTilesPerWarp = 32;
+constexpr uint32_t kTcRows = 128;
+constexpr uint32_t kTcThreads = 128;
+constexpr uint32_t kColBlock = kTcRows * 16u; // bytes between 8-column blocks of a row tile
+constexpr uint32_t kTcAccCols = 128;          // TMEM columns of the current layer's accumulator
+constexpr uint32_t kTcTmemCols = 512;
+constexpr uint32_t kTcWgColsMax = kTcTmemCols - kTcAccCols;
+constexpr uint32_t kTcMaxMatrices = kMaxHiddenLayers + 1u;
 
-struct WgArgs {
-    const __half *acts;
-    const __half *dz;
-    float *grad;
+struct TrainTcArgs {
+    const __half *wpacked; // 16-bit matrices in the K-major operand layout, back to back
+    uint32_t wbytes;
     uint32_t n_inputs;
     uint32_t n_hidden_layers;
     uint32_t n;
-    uint32_t rows_per_block;
+    const float *targets; // n x 8
+    LossConsts lc;
+    __half *dfeat;        // n x n_inputs gradients of the encoded features (emit launches)
+    float *grad;          // FP32 gradient vector (network matrices first)
+    float *loss_sum;
+    float *sample_loss;   // per row: sum of its output channels' loss values (may be NULL)
+    uint32_t *status;     // nonzero when a bounded wait gave up
+    uint32_t wg_mask;     // bit j: this launch accumulates the gradient of matrix j
+    uint32_t emit;        // this launch writes dfeat, the loss and the per-row losses
+    uint32_t min_matrix;  // the backward runs from matrix H down to this one
+    // shared-memory offsets (bytes from the 1,024-byte aligned base)
+    uint32_t x0_off;                      // two input tile buffers of n_inputs * 256 bytes
+    uint32_t x_off[kTcMaxMatrices];       // X_j (j = 1..H): 64-column tile (shared when not in wg_mask)
+    uint32_t dz_off, dzo_off, bar_off;
+    uint32_t wg_col[kTcMaxMatrices];      // TMEM column of the dW_j^T accumulator
 };
 
-__device__ __forceinline__ void tile_info(uint32_t t, uint32_t n_in, uint32_t H, uint32_t &mat, uint32_t &mt,
-                                          uint32_t &nt)
+__host__ __device__ constexpr uint32_t tc_w0_bytes(uint32_t n_in) { return kNeurons * n_in * 2u; }
+__host__ __device__ constexpr uint32_t tc_hidden_w_bytes() { return kNeurons * kNeurons * 2u; }
+// byte offset of matrix j in the packed weights; its output and input widths
+__host__ __device__ inline uint32_t tc_w_off(uint32_t j, uint32_t n_in)
 {
-    const uint32_t t0 = 4u * (n_in / 8u); // tiles of matrix 0
-    if (t < t0) {
-        mat = 0;
-        mt = t / (n_in / 8u);
-        nt = t % (n_in / 8u);
-        return;
-    }
-    t -= t0;
-    const uint32_t th = 32u * (H - 1u);
-    if (t < th) {
-        mat = 1u + t / 32u;
-        mt = (t % 32u) / 8u;
-        nt = t % 8u;
-        return;
-    }
-    t -= th;
-    mat = H; // output matrix: one m-tile (16 rows), 8 n-tiles
-    mt = 0;
-    nt = t;
+    return j == 0u ? 0u : tc_w0_bytes(n_in) + (j - 1u) * tc_hidden_w_bytes();
+}
+__host__ __device__ inline uint32_t tc_n_out(uint32_t j, uint32_t H) { return j < H ? kNeurons : kOutputsPadded; }
+__host__ __device__ inline uint32_t tc_n_in(uint32_t j, uint32_t n_in) { return j == 0u ? n_in : kNeurons; }
+// FP32 parameter offset of matrix j (row-major [out][in])
+__host__ __device__ inline uint32_t tc_param_off(uint32_t j, uint32_t n_in)
+{
+    return j == 0u ? 0u : kNeurons * n_in + (j - 1u) * kNeurons * kNeurons;
 }
 
-template <int TPW, bool BF16>
-__global__ void __launch_bounds__(kWgThreads, 1) k_weight_grads(const __grid_constant__ WgArgs a)
+// this thread's row of a [128][cols] tile: 16-byte chunk c (columns 8c .. 8c + 7)
+__device__ __forceinline__ void store_row_chunks(unsigned char *tile, uint32_t row, const uint32_t *words,
+                                                 uint32_t chunks)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const uint32_t n_in = a.n_inputs, H = a.n_hidden_layers;
-    const uint32_t acts_stride = n_in + H * kNeurons, dz_stride = H * kNeurons + kOutputsPadded;
-    const uint32_t sa_ld = acts_stride + 8u, sz_ld = dz_stride + 8u;
-    __half *sa = reinterpret_cast<__half *>(smem_raw);
-    __half *sz = sa + kWgRows * sa_ld;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
-    const uint32_t n_tiles = 4u * (n_in / 8u) + 32u * (H - 1u) + 8u;
+    for (uint32_t c = 0; c < chunks; c++)
+        *reinterpret_cast<uint4 *>(tile + c * kColBlock + row * 16u) =
+            make_uint4(words[4u * c], words[4u * c + 1u], words[4u * c + 2u], words[4u * c + 3u]);
+}
 
-    float acc[TPW][4];
-#pragma unroll
-    for (int i = 0; i < TPW; i++)
-        acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
+template <bool BF16, bool FP8>
+__global__ void __launch_bounds__(kTcThreads, 1) k_train_tc(const __grid_constant__ CUtensorMap fmap,
+                                                            const __grid_constant__ TrainTcArgs a)
+{
+    using Pr = MlpPrec<BF16>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const uint32_t K0 = a.n_inputs, H = a.n_hidden_layers;
+    const uint32_t n_tiles = (a.n + kTcRows - 1u) / kTcRows;
+    if (blockIdx.x >= n_tiles)
+        return;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const bool issuer = tid == 0u;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.bar_off); // weights, load 0, load 1, mma
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 4);
+    const uint32_t base = tc::smem_addr(smem);
+    const uint32_t bar_w = tc::smem_addr(&bars[0]), bar_mma = tc::smem_addr(&bars[3]);
+    const uint32_t x0_bytes = K0 * kTcRows * 2u;
 
-    const uint32_t row_begin = blockIdx.x * a.rows_per_block;
-    uint32_t row_end = row_begin + a.rows_per_block;
-    if (row_end > a.n)
-        row_end = a.n;
-    for (uint32_t c0 = row_begin; c0 < row_end; c0 += kWgRows) {
-        __syncthreads();
-        // stage 64 rows (zero-filled past the end)
-        const uint32_t wa = acts_stride / 2u, wz = dz_stride / 2u;
-        for (uint32_t i = threadIdx.x; i < kWgRows * wa; i += blockDim.x) {
-            uint32_t r = i / wa, c = i % wa;
-            uint32_t v = (c0 + r < row_end) ? __ldg(reinterpret_cast<const uint32_t *>(a.acts + (size_t)(c0 + r) * acts_stride) + c) : 0u;
-            *reinterpret_cast<uint32_t *>(sa + r * sa_ld + 2u * c) = v;
+    if (warp == 0u) {
+        tc::tmem_alloc(tc::smem_addr(slot), kTcTmemCols);
+        tc::tmem_relinquish();
+    }
+    if (issuer) {
+        for (uint32_t b = 0; b < 4u; b++)
+            tc::mbar_init(tc::smem_addr(&bars[b]), 1u);
+        tc::mbar_init_fence();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint32_t lane_off = (32u * warp) << 16; // this warp's TMEM lanes
+
+    auto load_tile = [&](uint32_t t, uint32_t buf) {
+        const uint32_t bar = tc::smem_addr(&bars[1u + buf]);
+        const uint32_t dst = base + a.x0_off + buf * x0_bytes;
+        tc::mbar_expect_tx(bar, x0_bytes);
+        for (uint32_t c = 0; c < K0 / 8u; c++)
+            tc::tma_load_2d(dst + c * kColBlock, &fmap, (int32_t)(8u * c), (int32_t)(t * kTcRows), bar);
+    };
+    uint32_t t = blockIdx.x;
+    bool load_pending[2] = {false, false};
+    if (issuer) {
+        tc::mbar_expect_tx(bar_w, a.wbytes);
+        for (uint32_t o = 0; o < a.wbytes; o += 16384u)
+            tc::bulk_load(base + o, reinterpret_cast<const unsigned char *>(a.wpacked) + o,
+                          a.wbytes - o < 16384u ? a.wbytes - o : 16384u, bar_w);
+        load_tile(t, 0u);
+    }
+    load_pending[0] = true;
+    bool ok = issuer ? tc::mbar_wait(bar_w, 0u) : true;
+    ok = __syncthreads_and(ok);
+
+    uint32_t ph_load[2] = {0u, 0u}, ph_mma = 0u, buf = 0u;
+    bool mma_pending = false, first_tile = true;
+    float loss_acc = 0.f;
+    // waits for the MMAs committed so far; false (everyone) if the wait gave up
+    auto mma_done = [&]() -> bool {
+        bool r = issuer ? tc::mbar_wait(bar_mma, ph_mma) : true;
+        r = __syncthreads_and(r);
+        if (r) {
+            ph_mma ^= 1u;
+            mma_pending = false;
+            tc::fence_after_sync();
         }
-        for (uint32_t i = threadIdx.x; i < kWgRows * wz; i += blockDim.x) {
-            uint32_t r = i / wz, c = i % wz;
-            uint32_t v = (c0 + r < row_end) ? __ldg(reinterpret_cast<const uint32_t *>(a.dz + (size_t)(c0 + r) * dz_stride) + c) : 0u;
-            *reinterpret_cast<uint32_t *>(sz + r * sz_ld + 2u * c) = v;
+        return r;
+    };
+    for (; ok && t < n_tiles; t += gridDim.x, buf ^= 1u) {
+        ok = issuer ? tc::mbar_wait(tc::smem_addr(&bars[1u + buf]), ph_load[buf]) : true;
+        ok = __syncthreads_and(ok);
+        if (!ok)
+            break;
+        ph_load[buf] ^= 1u;
+        load_pending[buf] = false;
+        // the other buffer's last reader (the previous tile's MMAs) has completed
+        if (t + gridDim.x < n_tiles) {
+            if (issuer)
+                load_tile(t + gridDim.x, buf ^ 1u);
+            load_pending[buf ^ 1u] = true;
         }
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < TPW; i++) {
-            const uint32_t t = (uint32_t)warp + (uint32_t)i * kWgWarps;
-            if (t >= n_tiles)
+        const uint32_t x0_addr = base + a.x0_off + buf * x0_bytes;
+        auto x_addr = [&](uint32_t j) { return j == 0u ? x0_addr : base + a.x_off[j]; };
+        const uint32_t row = t * kTcRows + tid;
+        const bool valid = row < a.n;
+        uint32_t relu_mask[2u * kTcMaxMatrices]; // bit c of X_j's row: words 2j, 2j + 1
+        // ---------------- forward ----------------
+        for (uint32_t j = 0; j <= H && ok; j++) {
+            const uint32_t nout = tc_n_out(j, H), nin = tc_n_in(j, K0);
+            if (issuer) {
+                tc::fence_after_sync();
+                const uint32_t idesc = tc::idesc_f16(kTcRows, nout, BF16);
+                const uint32_t w_addr = base + tc_w_off(j, K0), a_addr = x_addr(j);
+                for (uint32_t k = 0; k < nin / 16u; k++) {
+                    const uint64_t ad = tc::smem_desc(a_addr + 2u * k * kColBlock, kColBlock, 128u);
+                    const uint64_t bd = tc::smem_desc(w_addr + 2u * k * (nout * 16u), nout * 16u, 128u);
+                    tc::mma_f16(tmem, ad, bd, idesc, k > 0u ? 1u : 0u);
+                }
+                tc::mma_commit(bar_mma);
+            }
+            mma_pending = true;
+            if (!(ok = mma_done()))
                 break;
-            uint32_t mat, mt, nt;
-            tile_info(t, n_in, H, mat, mt, nt);
-            const uint32_t zoff = mat * kNeurons + mt * 16u; // dz column of this tile's first out row
-            const uint32_t xoff = (mat == 0) ? nt * 8u : n_in + (mat - 1u) * kNeurons + nt * 8u;
+            if (j < H) { // X_{j+1} = relu(Z_{j+1}) in the MLP precision (FP8 mode: E4M3 into hidden matrices)
+                uint32_t v[4][16];
 #pragma unroll
-            for (uint32_t kb = 0; kb < kWgRows / 16u; kb++) {
-                uint32_t af[4], bf[4];
-                // A = dz^T (m = out channel, k = row): ldmatrix.trans of the [row][out] tile
-                const __half *pa = sz + (kb * 16u + (lane & 7) + ((lane >> 4) << 3)) * sz_ld + zoff + ((lane >> 3) & 1) * 8;
-                ldsm_x4_trans(af, pa);
-                // B = x (k = row, n = in channel): ldmatrix.trans of the [row][in] tile
-                const __half *pb = sa + (kb * 16u + (lane & 15)) * sa_ld + xoff;
-                ldsm_x4_trans(bf, pb);
-                MlpPrec<BF16>::mma(acc[i], af, bf[0], bf[1]);
+                for (int q = 0; q < 4; q++)
+                    tc::tmem_ld16(tmem + lane_off + 16u * q, v[q]);
+                tc::tmem_wait_ld();
+                uint32_t packed[32];
+                const bool quant = FP8 && j + 1u < H;
+                uint32_t m0 = 0u, m1 = 0u;
+#pragma unroll
+                for (int c = 0; c < 32; c++) {
+                    const float lo = __uint_as_float(v[c >> 3][(2 * c) & 15]);
+                    const float hi = __uint_as_float(v[c >> 3][(2 * c + 1) & 15]);
+                    const uint32_t p = quant ? fp8_act_relu_half2(lo, hi) : pack_relu<BF16>(lo, hi);
+                    packed[c] = p;
+                    const uint32_t bits = ((p & 0xFFFFu) != 0u ? 1u : 0u) | ((p >> 16) != 0u ? 2u : 0u);
+                    if (c < 16)
+                        m0 |= bits << (2 * c);
+                    else
+                        m1 |= bits << (2 * (c - 16));
+                }
+                relu_mask[2u * (j + 1u)] = m0;
+                relu_mask[2u * (j + 1u) + 1u] = m1;
+                store_row_chunks(smem + a.x_off[j + 1u], tid, packed, 8u);
+            } else { // sigmoid, composite loss, dZ_out
+                uint32_t v[8];
+                tc::tmem_ld8(tmem + lane_off, v);
+                tc::tmem_wait_ld();
+                float tgt[8];
+                if (valid) {
+                    const float4 t0 = __ldg(reinterpret_cast<const float4 *>(a.targets + (size_t)row * 8u));
+                    const float4 t1 = __ldg(reinterpret_cast<const float4 *>(a.targets + (size_t)row * 8u) + 1);
+                    tgt[0] = t0.x, tgt[1] = t0.y, tgt[2] = t0.z, tgt[3] = t0.w;
+                    tgt[4] = t1.x, tgt[5] = t1.y, tgt[6] = t1.z, tgt[7] = t1.w;
+                }
+                float dz[8], val[8];
+#pragma unroll
+                for (int ch = 0; ch < 8; ch++) {
+                    const float y = 1.0f / (1.0f + expf(-__uint_as_float(v[ch])));
+                    float value = 0.f, gr = 0.f;
+                    if (valid) {
+                        composite_loss(a.lc, (uint32_t)ch, y, tgt[ch], tgt[0], value, gr);
+                        gr = Pr::round(gr); // 16-bit output gradient
+                    }
+                    val[ch] = value;
+                    dz[ch] = gr * y * (1.0f - y); // sigmoid backward
+                }
+                const float rl = ((val[0] + val[1]) + (val[2] + val[3])) + ((val[4] + val[5]) + (val[6] + val[7]));
+                loss_acc += rl;
+                if (valid && a.emit && a.sample_loss)
+                    a.sample_loss[row] = rl;
+                uint32_t packed[8] = {Pr::pack(dz[0], dz[1]), Pr::pack(dz[2], dz[3]), Pr::pack(dz[4], dz[5]),
+                                      Pr::pack(dz[6], dz[7]), 0u, 0u, 0u, 0u};
+                store_row_chunks(smem + a.dzo_off, tid, packed, 2u);
+            }
+            tc::fence_async_shared(); // the tile rows written above are read by the next MMAs
+            tc::fence_before_sync();
+            __syncthreads();
+        }
+        // ---------------- backward ----------------
+        for (int jj = (int)H; jj >= (int)a.min_matrix && ok; jj--) {
+            const uint32_t j = (uint32_t)jj;
+            const uint32_t nout = tc_n_out(j, H), nin = tc_n_in(j, K0);
+            const uint32_t dz_addr = base + (j == H ? a.dzo_off : a.dz_off);
+            const bool dgrad = j > a.min_matrix || (j == 0u && a.emit);
+            const bool wgrad = (a.wg_mask >> j) & 1u;
+            if (issuer) {
+                tc::fence_after_sync();
+                if (dgrad) { // dX_j (128 x nin) = dZ_{j+1} (128 x nout) . W_j (nout x nin), W_j MN-major
+                    const uint32_t idesc = tc::idesc_f16_major(kTcRows, nin, BF16, false, true);
+                    const uint32_t w_addr = base + tc_w_off(j, K0);
+                    for (uint32_t k = 0; k < nout / 16u; k++) {
+                        const uint64_t ad = tc::smem_desc(dz_addr + 2u * k * kColBlock, kColBlock, 128u);
+                        const uint64_t bd = tc::smem_desc(w_addr + 256u * k, 128u, nout * 16u);
+                        tc::mma_f16(tmem, ad, bd, idesc, k > 0u ? 1u : 0u);
+                    }
+                }
+                if (wgrad) { // dW_j^T (128 x nout; rows >= nin unused) += X_j^T . dZ_{j+1}, K = the 128 rows
+                    const uint32_t idesc = tc::idesc_f16_major(kTcRows, nout, BF16, true, true);
+                    const uint32_t xa = x_addr(j);
+                    for (uint32_t k = 0; k < kTcRows / 16u; k++) {
+                        const uint64_t ad = tc::smem_desc(xa + 256u * k, 128u, kColBlock);
+                        const uint64_t bd = tc::smem_desc(dz_addr + 256u * k, 128u, kColBlock);
+                        tc::mma_f16(tmem + a.wg_col[j], ad, bd, idesc, (first_tile && k == 0u) ? 0u : 1u);
+                    }
+                }
+                tc::mma_commit(bar_mma);
+            }
+            mma_pending = true;
+            if (!(ok = mma_done()))
+                break;
+            if (j >= 1u && j > a.min_matrix) { // dZ_j = dX_j * (X_j > 0), 16-bit
+                uint32_t v[4][16];
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    tc::tmem_ld16(tmem + lane_off + 16u * q, v[q]);
+                tc::tmem_wait_ld();
+                const uint32_t m0 = relu_mask[2u * j], m1 = relu_mask[2u * j + 1u];
+                uint32_t packed[32];
+#pragma unroll
+                for (int c = 0; c < 32; c++) {
+                    const uint32_t bits = (c < 16 ? m0 >> (2 * c) : m1 >> (2 * (c - 16))) & 3u;
+                    const float lo = (bits & 1u) ? __uint_as_float(v[c >> 3][(2 * c) & 15]) : 0.f;
+                    const float hi = (bits & 2u) ? __uint_as_float(v[c >> 3][(2 * c + 1) & 15]) : 0.f;
+                    packed[c] = Pr::pack(lo, hi);
+                }
+                store_row_chunks(smem + a.dz_off, tid, packed, 8u);
+            } else if (j == 0u && a.emit) { // dX_0, rounded to the MLP precision, for the grid scatter
+                uint4 *dst = reinterpret_cast<uint4 *>(a.dfeat + (size_t)row * K0);
+                for (uint32_t q = 0; q < K0 / 16u; q++) {
+                    uint32_t v[16];
+                    tc::tmem_ld16(tmem + lane_off + 16u * q, v); // warp-wide: rows past the batch too
+                    tc::tmem_wait_ld();
+                    if (valid) {
+                        uint32_t w[8];
+#pragma unroll
+                        for (int c = 0; c < 8; c++)
+                            w[c] = Pr::pack(__uint_as_float(v[2 * c]), __uint_as_float(v[2 * c + 1]));
+                        dst[2u * q] = make_uint4(w[0], w[1], w[2], w[3]);
+                        dst[2u * q + 1u] = make_uint4(w[4], w[5], w[6], w[7]);
+                    }
+                }
+            }
+            tc::fence_async_shared();
+            tc::fence_before_sync();
+            __syncthreads();
+        }
+        first_tile = false;
+    }
+    if (!ok) {
+        // a wait ran out: record it, give copies and MMAs still in flight one more bounded wait
+        if (issuer) {
+            atomicOr(a.status, 1u);
+            for (uint32_t b = 0; b < 2u; b++)
+                if (load_pending[b])
+                    tc::mbar_wait(tc::smem_addr(&bars[1u + b]), ph_load[b]);
+            if (mma_pending)
+                tc::mbar_wait(bar_mma, ph_mma);
+        }
+    } else if (!first_tile) {
+        // the CTA's weight gradients: lane m of the dW_j^T accumulator holds column m of dW_j
+        for (uint32_t j = 0; j <= H; j++) {
+            if (!((a.wg_mask >> j) & 1u))
+                continue;
+            const uint32_t nout = tc_n_out(j, H), nin = tc_n_in(j, K0);
+            float *g = a.grad + tc_param_off(j, K0);
+            for (uint32_t q = 0; q < nout / 16u; q++) {
+                uint32_t v[16];
+                tc::tmem_ld16(tmem + lane_off + a.wg_col[j] + 16u * q, v);
+                tc::tmem_wait_ld();
+                if (tid < nin) {
+#pragma unroll
+                    for (int c = 0; c < 16; c++) {
+                        const float x = __uint_as_float(v[c]);
+                        if (x != 0.f)
+                            atomicAdd(g + (size_t)(16u * q + (uint32_t)c) * nin + tid, x);
+                    }
+                }
             }
         }
-    }
-    // one global accumulation per block
+        if (a.emit) {
 #pragma unroll
-    for (int i = 0; i < TPW; i++) {
-        const uint32_t t = (uint32_t)warp + (uint32_t)i * kWgWarps;
-        if (t >= n_tiles)
-            break;
-        uint32_t mat, mt, nt;
-        tile_info(t, n_in, H, mat, mt, nt);
-        const uint32_t cols = (mat == 0) ? n_in : kNeurons;
-        const uint32_t moff = (mat == 0) ? 0u : kNeurons * n_in + (mat - 1u) * kNeurons * kNeurons;
-        const uint32_t row_a = mt * 16u + g, row_b = row_a + 8u, col = nt * 8u + tig * 2u;
-        float *gw = a.grad + moff;
-        if (mat == H && row_a >= kOutputs) {
-        } else {
-            atomicAdd(gw + row_a * cols + col, acc[i][0]);
-            atomicAdd(gw + row_a * cols + col + 1, acc[i][1]);
+            for (int off = 16; off > 0; off >>= 1)
+                loss_acc += __shfl_xor_sync(kFull, loss_acc, off);
+            if ((tid & 31u) == 0u && loss_acc != 0.f)
+                atomicAdd(a.loss_sum, loss_acc);
         }
-        if (!(mat == H && row_b >= kOutputs)) {
-            atomicAdd(gw + row_b * cols + col, acc[i][2]);
-            atomicAdd(gw + row_b * cols + col + 1, acc[i][3]);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0u) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, kTcTmemCols);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Hash-grid gradient scatter: one thread per (row, point), the levels in order; the corners and
+// weights of the forward encoding, each corner's F feature gradients added with vector atomics
+// (the 16-bit input-feature gradients come from k_train_tc).
+// ---------------------------------------------------------------------------------------------
+
+template <bool BF16>
+__global__ void __launch_bounds__(256) k_grid_scatter(const __grid_constant__ GridParams grid,
+                                                      const float *__restrict__ positions,
+                                                      const __half *__restrict__ dfeat, uint32_t n,
+                                                      float *__restrict__ grid_grad)
+{
+    const uint32_t P = grid.n_points, L = grid.n_levels, F = grid.n_features, n_in = grid.n_inputs;
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint64_t)n * P)
+        return;
+    const uint32_t row = (uint32_t)(i / P), p = (uint32_t)(i - (uint64_t)row * P);
+    const float *src = positions + i * 3u;
+    const V3 pp = mk3(__ldg(src), __ldg(src + 1), __ldg(src + 2));
+    const uint32_t *gw = reinterpret_cast<const uint32_t *>(dfeat + (size_t)row * n_in + (size_t)p * L * F);
+    for (uint32_t l = 0; l < L; l++) {
+        float g[8];
+        bool any = false;
+        for (uint32_t q = 0; q < F / 2u; q++) {
+            const float2 v = MlpPrec<BF16>::unpack(__ldg(gw + l * (F / 2u) + q));
+            g[2 * q] = v.x;
+            g[2 * q + 1] = v.y;
+            any |= v.x != 0.f || v.y != 0.f;
+        }
+        if (!any)
+            continue;
+        const float s = grid.scale[l];
+        const float px = __fmaf_rn(pp.x, s, 0.5f), py = __fmaf_rn(pp.y, s, 0.5f), pz = __fmaf_rn(pp.z, s, 0.5f);
+        const float flx = floorf(px), fly = floorf(py), flz = floorf(pz);
+        const uint32_t gx = (uint32_t)(int32_t)flx, gy = (uint32_t)(int32_t)fly, gz = (uint32_t)(int32_t)flz;
+        const float rx = __fsub_rn(px, flx), ry = __fsub_rn(py, fly), rz = __fsub_rn(pz, flz);
+        const uint32_t res = grid.res[l], size = grid.size[l], off = grid.offset[l];
+        const bool hashed = grid.hashed[l] != 0u;
+#pragma unroll
+        for (uint32_t c = 0; c < 8; c++) {
+            const uint32_t x = gx + (c & 1u), y = gy + ((c >> 1) & 1u), z = gz + ((c >> 2) & 1u);
+            uint32_t idx;
+            if (hashed) {
+                idx = (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (size - 1u);
+            } else {
+                idx = x + y * res + z * res * res;
+                if (idx >= size)
+                    idx %= size;
+            }
+            const float w = __fmul_rn(__fmul_rn((c & 1u) ? rx : __fsub_rn(1.0f, rx), (c & 2u) ? ry : __fsub_rn(1.0f, ry)),
+                                      (c & 4u) ? rz : __fsub_rn(1.0f, rz));
+            float *e = grid_grad + (size_t)(off + idx) * F;
+            if (F == 2u) {
+                atomicAdd(reinterpret_cast<float2 *>(e), make_float2(w * g[0], w * g[1]));
+            } else {
+                for (uint32_t q = 0; q < F / 4u; q++)
+                    atomicAdd(reinterpret_cast<float4 *>(e) + q,
+                              make_float4(w * g[4 * q], w * g[4 * q + 1], w * g[4 * q + 2], w * g[4 * q + 3]));
+            }
         }
     }
 }
@@ -787,6 +782,106 @@ __global__ void k_scale(float *__restrict__ p, size_t n, float s)
         p[i] *= s;
 }
 
+// One launch of k_train_tc: the matrices whose weight gradients it accumulates (wg_mask), whether
+// it also writes the loss and the feature gradients (the launch that reaches matrix 0), and its
+// shared-memory layout and TMEM columns.
+struct TrainTcPass {
+    TrainTcArgs a;
+    size_t smem;
+};
+
+constexpr size_t kTcSmemLimit = 227u * 1024u;
+constexpr size_t kTcSmPerSm = 228u * 1024u;
+
+// Lays out one pass over the matrices in `mask`; false if it does not fit shared memory or TMEM.
+bool plan_train_pass(uint32_t n_in, uint32_t H, uint32_t mask, bool emit, TrainTcPass &p)
+{
+    TrainTcArgs &a = p.a;
+    std::memset(&a, 0, sizeof(a));
+    const uint32_t wbytes = packed_weight_bytes(n_in, H);
+    uint32_t off = (wbytes + 1023u) & ~1023u;
+    a.wbytes = wbytes;
+    a.x0_off = off;
+    off += 2u * n_in * kTcRows * 2u;
+    bool transient = false;
+    for (uint32_t j = 1; j <= H; j++) {
+        if ((mask >> j) & 1u) {
+            a.x_off[j] = off;
+            off += kNeurons * kTcRows * 2u;
+        } else {
+            transient = true;
+        }
+    }
+    if (transient) {
+        for (uint32_t j = 1; j <= H; j++)
+            if (!((mask >> j) & 1u))
+                a.x_off[j] = off;
+        off += kNeurons * kTcRows * 2u;
+    }
+    // the weight-gradient MMAs read 128 columns of every X tile (rows past the matrix's input width
+    // are ignored): a 64-column tile is always followed by at least 16 KB (the next tile or dZ)
+    a.dz_off = off;
+    off += kNeurons * kTcRows * 2u;
+    a.dzo_off = off;
+    off += kOutputsPadded * kTcRows * 2u;
+    a.bar_off = off;
+    off += 64u;
+    uint32_t col = kTcAccCols;
+    for (uint32_t j = 0; j <= H; j++) {
+        if (!((mask >> j) & 1u))
+            continue;
+        a.wg_col[j] = col;
+        col += tc_n_out(j, H);
+    }
+    if (col > kTcTmemCols || off > kTcSmemLimit)
+        return false;
+    uint32_t lo = H;
+    for (uint32_t j = 0; j <= H; j++)
+        if ((mask >> j) & 1u) {
+            lo = j;
+            break;
+        }
+    a.wg_mask = mask;
+    a.emit = emit ? 1u : 0u;
+    a.min_matrix = emit ? 0u : lo;
+    // at least half an SM of shared memory, so that one CTA (and its 512 TMEM columns) per SM
+    const size_t one_per_sm = kTcSmPerSm / 2u - 1024u + 128u;
+    p.smem = off < one_per_sm ? one_per_sm : off;
+    return true;
+}
+
+// The passes: all matrices in one launch when they fit (up to 5 hidden layers), else groups of
+// matrices from the output matrix down, the last group (with matrix 0) writing the loss.
+std::vector<TrainTcPass> plan_train_passes(uint32_t n_in, uint32_t H)
+{
+    std::vector<TrainTcPass> passes;
+    TrainTcPass p;
+    const uint32_t all = (1u << (H + 1u)) - 1u;
+    if (plan_train_pass(n_in, H, all, true, p)) {
+        passes.push_back(p);
+        return passes;
+    }
+    uint32_t mask = 0u;
+    for (int j = (int)H; j >= 0; j--) {
+        const uint32_t trial = mask | (1u << j);
+        if (plan_train_pass(n_in, H, trial, j == 0, p)) {
+            mask = trial;
+            if (j == 0)
+                passes.push_back(p);
+            continue;
+        }
+        TrainTcPass done;
+        plan_train_pass(n_in, H, mask, false, done);
+        passes.push_back(done);
+        mask = 1u << j;
+        if (j == 0) {
+            plan_train_pass(n_in, H, mask, true, p);
+            passes.push_back(p);
+        }
+    }
+    return passes;
+}
+
 } // namespace
 
 cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *nodes, const float4 *tris,
@@ -819,98 +914,62 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
     return cudaGetLastError();
 }
 
-cudaError_t launch_train_forward_backward(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
-                                          const LossConsts &lc, const float *positions, const float *targets,
-                                          uint32_t n, __half *acts, __half *dz, float *grad, float *loss_sum,
-                                          float *sample_loss, bool bf16, bool fp8, int num_sms, cudaStream_t s)
+cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
+                              const LossConsts &lc, const float *positions, const float *targets, uint32_t n,
+                              __half *features, __half *dfeat, __half *wpacked, float *grad, float *loss_sum,
+                              float *sample_loss, uint32_t *status, bool bf16, bool fp8, int num_sms, cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
-    TrainArgs a;
-    a.grid = grid;
-    a.lc = lc;
+    const uint32_t H = n_hidden_layers, n_in = grid.n_inputs;
     const uint32_t n_network_params =
-        kNeurons * grid.n_inputs + (n_hidden_layers - 1u) * kNeurons * kNeurons + kOutputsPadded * kNeurons;
-    a.table = reinterpret_cast<const uint32_t *>(params_h + n_network_params);
-    a.weights = params_h;
-    a.positions = positions;
-    a.targets = targets;
-    a.acts = acts;
-    a.dz = dz;
-    a.grid_grad = reinterpret_cast<float2 *>(grad + n_network_params);
-    a.loss_sum = loss_sum;
-    a.sample_loss = sample_loss;
-    a.fp8 = fp8 ? 1u : 0u;
-    a.n_hidden_layers = n_hidden_layers;
-    a.n = n;
-    const size_t smem = kGridParamsSmem + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half);
+        kNeurons * n_in + (H - 1u) * kNeurons * kNeurons + kOutputsPadded * kNeurons;
+    const uint32_t *table = reinterpret_cast<const uint32_t *>(params_h + n_network_params);
     {
         const uint64_t threads = (uint64_t)n * grid.n_points;
-        k_train_encode<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(
-            grid, a.table, positions, n, acts, grid.n_inputs + n_hidden_layers * kNeurons, bf16 ? 1u : 0u);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess)
+        k_train_encode<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(grid, table, positions, n, features, n_in,
+                                                                          bf16 ? 1u : 0u);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = launch_pack_weights(params_h, n_in, H, wpacked, s);
+    if (e != cudaSuccess)
+        return e;
+    TensorMapBytes mb;
+    if ((e = make_feature_map(features, n_in, n, &mb, false)) != cudaSuccess)
+        return e;
+    CUtensorMap fmap;
+    std::memcpy(&fmap, mb.bytes, sizeof(fmap));
+    auto kernel = bf16 ? k_train_tc<true, false> : (fp8 ? k_train_tc<false, true> : k_train_tc<false, false>);
+    if ((e = allow_max_dynamic_smem(kernel)) != cudaSuccess)
+        return e;
+    const uint32_t tiles = (n + kTcRows - 1u) / kTcRows;
+    const uint32_t blocks = tiles < (uint32_t)num_sms ? tiles : (uint32_t)num_sms;
+    for (TrainTcPass &p : plan_train_passes(n_in, H)) {
+        TrainTcArgs &a = p.a;
+        a.wpacked = wpacked;
+        a.n_inputs = n_in;
+        a.n_hidden_layers = H;
+        a.n = n;
+        a.targets = targets;
+        a.lc = lc;
+        a.dfeat = dfeat;
+        a.grad = grad;
+        a.loss_sum = loss_sum;
+        a.sample_loss = sample_loss;
+        a.status = status;
+        kernel<<<blocks, kTcThreads, p.smem, s>>>(fmap, a);
+        if ((e = cudaGetLastError()) != cudaSuccess)
             return e;
     }
-    cudaError_t e = bf16  ? allow_max_dynamic_smem(k_train_fwd_bwd<true, false>)
-                    : fp8 ? allow_max_dynamic_smem(k_train_fwd_bwd<false, true>)
-                          : allow_max_dynamic_smem(k_train_fwd_bwd<false, false>);
-    if (e != cudaSuccess)
-        return e;
-    const uint32_t tiles = (n + 15u) / 16u;
-    uint32_t blocks = (tiles + kTrainWarps - 1u) / kTrainWarps;
-    const uint32_t cap = (uint32_t)num_sms * 2u;
-    if (blocks > cap)
-        blocks = cap;
+    const uint64_t threads = (uint64_t)n * grid.n_points;
     if (bf16)
-        k_train_fwd_bwd<true, false><<<blocks, kTrainThreads, smem, s>>>(a);
-    else if (fp8)
-        k_train_fwd_bwd<false, true><<<blocks, kTrainThreads, smem, s>>>(a);
+        k_grid_scatter<true><<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(grid, positions, dfeat, n,
+                                                                                 grad + n_network_params);
     else
-        k_train_fwd_bwd<false, false><<<blocks, kTrainThreads, smem, s>>>(a);
+        k_grid_scatter<false><<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(grid, positions, dfeat, n,
+                                                                                  grad + n_network_params);
     return cudaGetLastError();
-}
-
-template <int TPW, bool BF16>
-cudaError_t run_weight_grads(const WgArgs &a, uint32_t blocks, size_t smem, cudaStream_t s)
-{
-    cudaError_t e = allow_max_dynamic_smem(k_weight_grads<TPW, BF16>);
-    if (e != cudaSuccess)
-        return e;
-    k_weight_grads<TPW, BF16><<<blocks, kWgThreads, smem, s>>>(a);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_weight_gradients(const GridParams &grid, uint32_t n_hidden_layers, const __half *acts,
-                                    const __half *dz, uint32_t n, float *grad, bool bf16, int num_sms, cudaStream_t s)
-{
-    if (n == 0)
-        return cudaSuccess;
-    WgArgs a;
-    a.acts = acts;
-    a.dz = dz;
-    a.grad = grad;
-    a.n_inputs = grid.n_inputs;
-    a.n_hidden_layers = n_hidden_layers;
-    a.n = n;
-    uint32_t blocks = (uint32_t)num_sms;
-    uint32_t rows = (n + blocks - 1u) / blocks;
-    rows = (rows + kWgRows - 1u) / kWgRows * kWgRows;
-    blocks = (n + rows - 1u) / rows;
-    a.rows_per_block = rows;
-    const uint32_t acts_stride = grid.n_inputs + n_hidden_layers * kNeurons;
-    const uint32_t dz_stride = n_hidden_layers * kNeurons + kOutputsPadded;
-    const size_t smem = (size_t)kWgRows * ((acts_stride + 8u) + (dz_stride + 8u)) * sizeof(__half);
-    const uint32_t n_tiles = 4u * (grid.n_inputs / 8u) + 32u * (n_hidden_layers - 1u) + 8u;
-    const uint32_t tpw = (n_tiles + kWgWarps - 1u) / kWgWarps;
-    if (tpw <= 16)
-        return bf16 ? run_weight_grads<16, true>(a, blocks, smem, s) : run_weight_grads<16, false>(a, blocks, smem, s);
-    if (tpw <= 24)
-        return bf16 ? run_weight_grads<24, true>(a, blocks, smem, s) : run_weight_grads<24, false>(a, blocks, smem, s);
-    if (tpw <= kMaxTilesPerWarp)
-        return bf16 ? run_weight_grads<kMaxTilesPerWarp, true>(a, blocks, smem, s)
-                    : run_weight_grads<kMaxTilesPerWarp, false>(a, blocks, smem, s);
-    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_scale(float *data, size_t n, float scale, cudaStream_t s)

@@ -390,10 +390,16 @@ void ensure_train_workspace(nbvh_handle *h, uint32_t n)
         cuda_check(h->d_train_loss.resize(n), "alloc sample losses");
         cuda_check(cudaMemset(h->d_train_loss.ptr, 0, h->d_train_loss.count * sizeof(float)), "zero losses");
     }
-    if (h->d_train_acts.count < (size_t)n * (ni + H * kNeurons))
-        cuda_check(h->d_train_acts.resize((size_t)n * (ni + H * kNeurons)), "alloc activations");
-    if (h->d_train_dz.count < (size_t)n * (H * kNeurons + kOutputsPadded))
-        cuda_check(h->d_train_dz.resize((size_t)n * (H * kNeurons + kOutputsPadded)), "alloc gradients");
+    if (h->d_train_feat.count < (size_t)n * ni)
+        cuda_check(h->d_train_feat.resize((size_t)n * ni), "alloc features");
+    if (h->d_train_dfeat.count < (size_t)n * ni)
+        cuda_check(h->d_train_dfeat.resize((size_t)n * ni), "alloc feature gradients");
+    if (h->d_train_wpacked.count < packed_weight_bytes(ni, H) / 2u)
+        cuda_check(h->d_train_wpacked.resize(packed_weight_bytes(ni, H) / 2u), "alloc packed weights");
+    if (h->d_status.count < 1u) {
+        cuda_check(h->d_status.resize(1u), "alloc status");
+        cuda_check(cudaMemset(h->d_status.ptr, 0, sizeof(uint32_t)), "reset status");
+    }
     if (h->d_grad.count < h->layout.n_params)
         cuda_check(h->d_grad.resize(h->layout.n_params), "alloc grad");
 }
@@ -1223,14 +1229,11 @@ void gradients_into_workspace(nbvh_handle *h, const float *d_pos, const float *d
     ensure_train_workspace(h, n);
     const uint32_t H = (uint32_t)h->cfg.network.n_hidden_layers;
     cuda_check(cudaMemsetAsync(h->d_grad.ptr, 0, (size_t)h->layout.n_params * sizeof(float), s), "zero grad");
-    cuda_check(launch_train_forward_backward(h->d_params_h.ptr, h->grid, H, make_loss_consts(h->cfg, n), d_pos, d_tgt, n,
-                                             h->d_train_acts.ptr, h->d_train_dz.ptr, h->d_grad.ptr, loss_slot,
-                                             h->d_train_loss.ptr, mlp_bf16(h),
-                                             h->cfg.network.precision == NBVH_PRECISION_FP8, h->num_sms, s),
+    cuda_check(launch_train_step(h->d_params_h.ptr, h->grid, H, make_loss_consts(h->cfg, n), d_pos, d_tgt, n,
+                                 h->d_train_feat.ptr, h->d_train_dfeat.ptr, h->d_train_wpacked.ptr, h->d_grad.ptr,
+                                 loss_slot, h->d_train_loss.ptr, h->d_status.ptr, mlp_bf16(h),
+                                 h->cfg.network.precision == NBVH_PRECISION_FP8, h->num_sms, s),
                "forward/backward");
-    cuda_check(launch_weight_gradients(h->grid, H, h->d_train_acts.ptr, h->d_train_dz.ptr, n, h->d_grad.ptr,
-                                       mlp_bf16(h), h->num_sms, s),
-               "weight gradients");
 }
 
 } // namespace
@@ -1243,15 +1246,20 @@ nbvh_status nbvh_compute_gradients(nbvh_handle *h, const float *d_positions, con
     return guarded(h, [&]() {
         require(d_positions && d_targets && d_gradients && n > 0, NBVH_EINVAL, "null buffers");
         cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        ensure_train_workspace(h, n);
         cuda_check(cudaMemsetAsync(h->d_loss_sum.ptr, 0, sizeof(float), s), "zero loss");
+        cuda_check(cudaMemsetAsync(h->d_status.ptr, 0, sizeof(uint32_t), s), "reset status");
         gradients_into_workspace(h, d_positions, d_targets, n, s, h->d_loss_sum.ptr);
         cuda_check(cudaMemcpyAsync(d_gradients, h->d_grad.ptr, (size_t)h->layout.n_params * sizeof(float),
                                    cudaMemcpyDeviceToDevice, s),
                    "copy grad");
         cuda_check(launch_scale(d_gradients, h->layout.n_params, 1.0f / h->cfg.optimizer.loss_scale, s), "unscale");
         float loss = 0.f;
+        uint32_t status = 0;
         cuda_check(cudaMemcpyAsync(&loss, h->d_loss_sum.ptr, sizeof(float), cudaMemcpyDeviceToHost, s), "loss");
+        cuda_check(cudaMemcpyAsync(&status, h->d_status.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "status");
         cuda_check(cudaStreamSynchronize(s), "sync");
+        require(status == 0u, NBVH_ETIMEOUT, "tensor-core training kernel: a bounded wait gave up");
         if (h_loss)
             *h_loss = loss;
         h->last_launches = 4;
@@ -1300,6 +1308,7 @@ nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_sta
             cuda_check(h->d_loss_sum.resize((size_t)steps + 1u), "alloc loss");
         cudaStream_t s = h->pipe_stream[0];
         cuda_check(cudaMemsetAsync(h->d_loss_sum.ptr, 0, ((size_t)steps + 1u) * sizeof(float), s), "zero loss");
+        cuda_check(cudaMemsetAsync(h->d_status.ptr, 0, sizeof(uint32_t), s), "reset status");
         const NeuralConsts nc = make_neural_consts(h, 1u, false);
         const uint32_t first = h->training_step;
         float lr_t = 0.f;
@@ -1331,7 +1340,10 @@ nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_sta
         if (steps > 0)
             cuda_check(cudaMemcpyAsync(losses.data(), h->d_loss_sum.ptr, steps * sizeof(float), cudaMemcpyDeviceToHost, s),
                        "losses");
+        uint32_t status = 0;
+        cuda_check(cudaMemcpyAsync(&status, h->d_status.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "status");
         cuda_check(cudaStreamSynchronize(s), "sync");
+        require(status == 0u, NBVH_ETIMEOUT, "tensor-core training kernel: a bounded wait gave up");
         float ms = 0.f;
         cuda_check(cudaEventElapsedTime(&ms, h->ev0, h->ev1), "elapsed");
         h->last_kernel_ms = ms;

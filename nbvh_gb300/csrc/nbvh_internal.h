@@ -342,8 +342,9 @@ struct nbvh_handle {
     // training workspace
     nbvh::DeviceBuffer<float> d_train_pos, d_train_tgt;
     nbvh::DeviceBuffer<uint32_t> d_train_nodes;
-    nbvh::DeviceBuffer<__half> d_train_acts; // per row activations of every layer input
-    nbvh::DeviceBuffer<__half> d_train_dz;   // per row pre-activation gradients of every layer
+    nbvh::DeviceBuffer<__half> d_train_feat;    // n x n_inputs encoded features (16-bit)
+    nbvh::DeviceBuffer<__half> d_train_dfeat;   // n x n_inputs gradients of the features (16-bit)
+    nbvh::DeviceBuffer<__half> d_train_wpacked; // network matrices in the tensor-core operand layout
     nbvh::DeviceBuffer<float> d_train_loss;  // per row loss (sum over output channels)
     nbvh::DeviceBuffer<float> d_loss_sum;
     nbvh::TreeCutSession cut;
@@ -525,7 +526,10 @@ cudaError_t launch_network_inference(const __half *params_h, const GridParams &g
 uint32_t packed_weight_bytes(uint32_t n_inputs, uint32_t n_hidden_layers);
 cudaError_t launch_pack_weights(const __half *params_h, uint32_t n_inputs, uint32_t n_hidden_layers, __half *packed,
                                 cudaStream_t s);
-cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t rows, TensorMapBytes *out);
+// allow_swizzle = false: always 8-value boxes, so that a 128-row tile lands in shared memory in
+// the unswizzled K-major core-matrix layout (column block c of 8 values at c * 2,048 bytes).
+cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t rows, TensorMapBytes *out,
+                             bool allow_swizzle = true);
 cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
                           uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
                           uint32_t *status, uint32_t prec, int num_sms, cudaStream_t s, bool configure = true);
@@ -570,16 +574,17 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
                                     float *targets, uint32_t *sample_nodes, uint32_t learned_lod,
                                     const NodeSurvival *survival, cudaStream_t s);
 
-// forward + loss + backward: writes per-row activations / gradients for the weight-gradient pass,
-// scatters the grid gradient into grad + n_network_params, accumulates the loss sum.
-cudaError_t launch_train_forward_backward(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
-                                          const LossConsts &lc, const float *positions, const float *targets,
-                                          uint32_t n, __half *acts, __half *dz, float *grad,
-                                          float *loss_sum, float *sample_loss, bool bf16, bool fp8, int num_sms,
-                                          cudaStream_t s);
-
-cudaError_t launch_weight_gradients(const GridParams &grid, uint32_t n_hidden_layers, const __half *acts,
-                                    const __half *dz, uint32_t n, float *grad, bool bf16, int num_sms, cudaStream_t s);
+// One training pass over n rows (positions n x points x 3, targets n x 8): the hash-grid features
+// into `features` (n x n_inputs, 16-bit), the network matrices packed into `wpacked`
+// (packed_weight_bytes), forward + composite loss + backward on the tcgen05 tensor cores (the
+// weight gradients added to grad, the loss sum into *loss_sum, per-row losses into sample_loss
+// when not NULL, the 16-bit feature gradients into dfeat, n x n_inputs), then the hash-grid
+// gradient scattered into grad + n_network_params. grad holds the gradient times the loss scale.
+// status receives a nonzero word if a bounded wait inside the tensor-core kernel gave up.
+cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
+                              const LossConsts &lc, const float *positions, const float *targets, uint32_t n,
+                              __half *features, __half *dfeat, __half *wpacked, float *grad, float *loss_sum,
+                              float *sample_loss, uint32_t *status, bool bf16, bool fp8, int num_sms, cudaStream_t s);
 
 // ---- learned tree cut (k_tree_cut.cu) ----
 // Copies the records of the late-listed rays from src (device) to dst (page-locked host).

@@ -250,6 +250,18 @@ __device__ __forceinline__ uint32_t fp8_act_relu_half2(float lo, float hi)
     return *reinterpret_cast<const uint32_t *>(&v);
 }
 
+// Two FP32 values -> ReLU -> 16-bit pair (lo in the low half), one cvt.rn.relu instruction.
+template <bool BF16>
+__device__ __forceinline__ uint32_t pack_relu(float lo, float hi)
+{
+    uint32_t r;
+    if constexpr (BF16)
+        asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;\n" : "=r"(r) : "f"(hi), "f"(lo));
+    else
+        asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;\n" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
 // Rebuilds the 16-bit A fragments of the next layer from the FP32 accumulators (after ReLU).
 // (FP8 and quant: the activations go through FP8-E4M3 first, the input format of the hidden
 // matrices in FP8 mode; E4M3 values are exact in FP16. FP8 is a template argument so that the

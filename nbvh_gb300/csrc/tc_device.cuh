@@ -198,5 +198,17 @@ __host__ __device__ constexpr uint32_t idesc_f16(uint32_t m, uint32_t n, bool bf
     return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
 
+// The same with A and / or B MN-major (bits 15 and 16: the operand's M, resp. N, index is the one
+// contiguous in memory). An MN-major operand without swizzle uses core matrices of 8 K-rows x 16
+// bytes (8 values along M or N): the descriptor's LBO is then the byte distance between core
+// matrices adjacent along K and SBO the distance between core matrices adjacent along M / N, the
+// same roles as for a K-major operand. So a [rows][cols] buffer in the K-major layout above (core
+// matrix = 8 rows x 8 columns, LBO = 16 * rows between column blocks, SBO = 128 between row
+// blocks) is also the MN-major operand whose K index is the row: LBO = 128, SBO = 16 * rows.
+__host__ __device__ constexpr uint32_t idesc_f16_major(uint32_t m, uint32_t n, bool bf16, bool a_mn, bool b_mn)
+{
+    return idesc_f16(m, n, bf16) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16);
+}
+
 } // namespace tc
 } // namespace nbvh
