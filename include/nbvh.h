@@ -672,6 +672,25 @@ typedef struct nbvh_kernel_profile {
 nbvh_status nbvh_set_kernel_profile(nbvh_handle *h, int enable);
 nbvh_status nbvh_last_kernel_profile(nbvh_handle *h, nbvh_kernel_profile *out);
 
+/* Failure-path testing (no counterpart in the reference, which stops the process on a CUDA error,
+ * include/ntwr.h:30-54).
+ * nbvh_debug_set_wait_limit: time limit of the phase waits inside this handle's tensor-core
+ * kernels (the fused MLP of the queries and of nbvh_mlp_inference, the training kernel), in
+ * nanoseconds; 0 restores the default of one second. A wait that runs out makes the kernel record
+ * the failure, let the copies and MMAs it has in flight finish, release its tensor memory and
+ * return; the call then fails with NBVH_ETIMEOUT and the handle stays usable.
+ * nbvh_debug_inject_stall: while enabled, every tensor-core kernel this handle launches first waits
+ * on an mbarrier that nothing arrives at, so that its wait runs out after the wait limit (a wait
+ * that would otherwise never end, made on purpose and bounded).
+ * nbvh_debug_fail_allocations: every device allocation the library makes after the next `after`
+ * ones fails as if the device were out of memory (the call reports NBVH_ENOMEM); a negative value
+ * switches this off. Process-wide.
+ * nbvh_debug_alloc_count: device allocations the library has made so far (process-wide). */
+nbvh_status nbvh_debug_set_wait_limit(nbvh_handle *h, uint64_t ns);
+nbvh_status nbvh_debug_inject_stall(nbvh_handle *h, int enable);
+nbvh_status nbvh_debug_fail_allocations(int64_t after);
+nbvh_status nbvh_debug_alloc_count(uint64_t *out);
+
 /* ---------------------------------------------------------------------------------------------
  * Allocation-free neural query. This entry point has no counterpart in the reference.
  *
@@ -685,8 +704,10 @@ nbvh_status nbvh_last_kernel_profile(nbvh_handle *h, nbvh_kernel_profile *out);
  * library's device code is loaded.
  *  - n must be at most NBVH_NOALLOC_MAX_RAYS; a larger n returns NBVH_EINVAL and launches nothing.
  *    Split larger batches into several calls.
- *  - The first call on each device looks up the buffer's address (setup). Make one call, n = 0 is
- *    enough, before capturing a stream.
+ *  - The first call on each device, with that device current, looks up the buffer's device
+ *    address once (setup) and keeps it for the life of the process. Make that first call (n = 0
+ *    is enough) before any stream capture. Do not use the library across a reset of the device
+ *    (cudaDeviceReset), which may move the buffer.
  *  - Each call zeroes the counters it uses before its first kernel; nothing relies on the buffer's
  *    contents from an earlier call.
  *  - There is one buffer per device, shared by every handle on it. Calls that overlap in time on

@@ -216,6 +216,10 @@ PROTOTYPES = {
     "nbvh_last_kernel_time": (ST, [P, PF, PU32]),
     "nbvh_set_kernel_profile": (ST, [P, I32]),
     "nbvh_last_kernel_profile": (ST, [P, C.POINTER(KernelProfile)]),
+    "nbvh_debug_set_wait_limit": (ST, [P, C.c_uint64]),
+    "nbvh_debug_inject_stall": (ST, [P, I32]),
+    "nbvh_debug_fail_allocations": (ST, [C.c_int64]),
+    "nbvh_debug_alloc_count": (ST, [C.POINTER(C.c_uint64)]),
     "nbvh_build_bvh2_host": (ST, [P, U32, P, U32, P, PU32, P]),
     "nbvh_build_neural_cut_host": (ST, [P, U32, U32, P, PU32]),
     "nbvh_param_layout_host": (ST, [PCFG, C.POINTER(ParamLayout)]),

@@ -91,6 +91,8 @@ struct MlpTcArgs {
     uint32_t *status;
     uint32_t fp8;    // inputs of the hidden matrices rounded to FP8-E4M3
     uint32_t groups; // tile pipelines per CTA (blockDim.x / 128)
+    uint64_t wait_ns; // time limit of the phase waits
+    uint32_t stall;   // failure-path test: wait on an mbarrier nothing arrives at (it runs out)
 };
 
 // D = A * W^T for the 128-row tile: A (128 x K) at a_addr, W (N x K) at w_addr, both in the
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(kMaxGroups * kGroupThreads, 1) k_mlp_tc(const 
     const bool issuer = gtid == 32u * (gid & 3u);
     unsigned char *tile = smem + tile_offset(a.wbytes) + gid * tile_bytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + tile_offset(a.wbytes) + G * tile_bytes);
-    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2u * G + 1u);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2u * G + 2u);
     const uint32_t bar_w = tc::smem_addr(&bars[2u * G]);
     const uint32_t bar_load = tc::smem_addr(&bars[2u * gid]), bar_mma = tc::smem_addr(&bars[2u * gid + 1u]);
     const uint32_t w_addr = tc::smem_addr(smem), t_addr = tc::smem_addr(tile);
@@ -226,7 +228,7 @@ __global__ void __launch_bounds__(kMaxGroups * kGroupThreads, 1) k_mlp_tc(const 
         tc::tmem_relinquish();
     }
     if (tid == 0) {
-        for (uint32_t b = 0; b < 2u * G + 1u; b++)
+        for (uint32_t b = 0; b < 2u * G + 2u; b++) // the last one is the failure-path test's
             tc::mbar_init(tc::smem_addr(&bars[b]), 1u);
         tc::mbar_init_fence();
     }
@@ -263,12 +265,14 @@ __global__ void __launch_bounds__(kMaxGroups * kGroupThreads, 1) k_mlp_tc(const 
             tc::bulk_load(w_addr + o, reinterpret_cast<const unsigned char *>(a.wpacked) + o,
                           a.wbytes - o < 16384u ? a.wbytes - o : 16384u, bar_w);
     }
-    bool ok = tc::mbar_wait(bar_w, 0u);
+    bool ok = tc::mbar_wait(bar_w, 0u, a.wait_ns);
+    if (a.stall && tid == 0) // nothing ever arrives at this barrier: the wait runs out
+        ok = ok && tc::mbar_wait(tc::smem_addr(&bars[2u * G + 1u]), 0u, a.wait_ns);
     ok = __syncthreads_and(ok);
     const uint32_t id_hidden = tc::idesc_f16(kTileRows, kNeurons, BF16);
     const uint32_t id_out = tc::idesc_f16(kTileRows, kOutputsPadded, BF16);
     for (; ok && t < n_tiles; t += stride) {
-        ok = issuer ? tc::mbar_wait(bar_load, ph_load) : true;
+        ok = issuer ? tc::mbar_wait(bar_load, ph_load, a.wait_ns) : true;
         ok = group_sync_and(gbar, ok);
         if (!ok)
             break;
@@ -290,7 +294,7 @@ __global__ void __launch_bounds__(kMaxGroups * kGroupThreads, 1) k_mlp_tc(const 
                 tc::mma_commit(bar_mma);
             }
             mma_pending = true;
-            ok = issuer ? tc::mbar_wait(bar_mma, ph_mma) : true;
+            ok = issuer ? tc::mbar_wait(bar_mma, ph_mma, a.wait_ns) : true;
             ok = group_sync_and(gbar, ok);
             if (!ok)
                 break;
@@ -395,7 +399,8 @@ cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t
 
 cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
                           uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
-                          uint32_t *status, uint32_t prec, int num_sms, cudaStream_t s, bool configure)
+                          uint32_t *status, uint32_t prec, int num_sms, cudaStream_t s, bool configure,
+                          uint64_t wait_ns, bool stall)
 {
     if (rows == 0)
         return cudaSuccess;
@@ -412,9 +417,11 @@ cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpack
     a.outputs = outputs;
     a.status = status;
     a.fp8 = prec == NBVH_PRECISION_FP8 ? 1u : 0u;
+    a.wait_ns = wait_ns ? wait_ns : tc::kWaitLimitNs;
+    a.stall = stall ? 1u : 0u;
     // as many tile groups as shared memory holds (227 KB per CTA), at most kMaxGroups
     const size_t tile_bytes = (size_t)kTileRows * n_inputs * 2u;
-    const size_t fixed = tile_offset(a.wbytes) + 8u * (2u * kMaxGroups + 1u) + 16u;
+    const size_t fixed = tile_offset(a.wbytes) + 8u * (2u * kMaxGroups + 2u) + 16u;
     const size_t room = 227u * 1024u;
     if (fixed + tile_bytes > room)
         return cudaErrorInvalidValue;
@@ -425,7 +432,7 @@ cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpack
     const uint32_t tiles_per_sm = (uint32_t)(((rows + kTileRows - 1u) / kTileRows + (uint32_t)num_sms - 1u) / (uint32_t)num_sms);
     groups = tiles_per_sm < groups ? (tiles_per_sm > 0u ? tiles_per_sm : 1u) : groups;
     a.groups = groups;
-    size_t smem = tile_offset(a.wbytes) + groups * tile_bytes + 8u * (2u * groups + 1u) + 16u;
+    size_t smem = tile_offset(a.wbytes) + groups * tile_bytes + 8u * (2u * groups + 2u) + 16u;
     // at most 512 / tmem_alloc_cols(groups) CTAs on an SM, so that their TMEM allocations always
     // fit: one CTA more must not fit the SM's 228 KB (each CTA also reserves 1 KB)
     const size_t max_ctas = 512u / tmem_alloc_cols(groups);

@@ -1119,7 +1119,7 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
         }
         e = launch_mlp_tc(r.feature_map, r.wpacked, a.grid.n_inputs, a.n_hidden_layers, a.lists[0].capacity,
                           &a.wave_counts[it % 3u], a.outputs, &a.wave_counts[3], a.prec, num_sms, s,
-                          !r.capture_only);
+                          !r.capture_only, r.wait_ns, r.stall);
         if (e != cudaSuccess)
             return e;
         k_wave_decode<SMEM_CUT><<<dec_blocks, decode_threads(SMEM_CUT), dec_smem, s>>>(a, it);

@@ -364,6 +364,8 @@ struct TrainTcArgs {
     uint32_t x_off[kTcMaxMatrices];       // X_j (j = 1..H): 64-column tile (shared when not in wg_mask)
     uint32_t dz_off, dzo_off, bar_off;
     uint32_t wg_col[kTcMaxMatrices];      // TMEM column of the dW_j^T accumulator
+    uint64_t wait_ns;                     // time limit of the phase waits
+    uint32_t stall;                       // failure-path test: wait on an mbarrier nothing arrives at
 };
 
 __host__ __device__ constexpr uint32_t tc_w0_bytes(uint32_t n_in) { return kNeurons * n_in * 2u; }
@@ -402,8 +404,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_train_tc(const __grid_constan
         return;
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
     const bool issuer = tid == 0u;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.bar_off); // weights, load 0, load 1, mma
-    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 4);
+    // weights, load 0, load 1, mma, and one nothing arrives at (failure-path test)
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.bar_off);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 5);
     const uint32_t base = tc::smem_addr(smem);
     const uint32_t bar_w = tc::smem_addr(&bars[0]), bar_mma = tc::smem_addr(&bars[3]);
     const uint32_t x0_bytes = K0 * kTcRows * 2u;
@@ -413,7 +416,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_train_tc(const __grid_constan
         tc::tmem_relinquish();
     }
     if (issuer) {
-        for (uint32_t b = 0; b < 4u; b++)
+        for (uint32_t b = 0; b < 5u; b++)
             tc::mbar_init(tc::smem_addr(&bars[b]), 1u);
         tc::mbar_init_fence();
     }
@@ -440,7 +443,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_train_tc(const __grid_constan
         load_tile(t, 0u);
     }
     load_pending[0] = true;
-    bool ok = issuer ? tc::mbar_wait(bar_w, 0u) : true;
+    bool ok = issuer ? tc::mbar_wait(bar_w, 0u, a.wait_ns) : true;
+    if (a.stall && issuer) // nothing ever arrives at this barrier: the wait runs out
+        ok = ok && tc::mbar_wait(tc::smem_addr(&bars[4]), 0u, a.wait_ns);
     ok = __syncthreads_and(ok);
 
     uint32_t ph_load[2] = {0u, 0u}, ph_mma = 0u, buf = 0u;
@@ -448,7 +453,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_train_tc(const __grid_constan
     float loss_acc = 0.f;
     // waits for the MMAs committed so far; false (everyone) if the wait gave up
     auto mma_done = [&]() -> bool {
-        bool r = issuer ? tc::mbar_wait(bar_mma, ph_mma) : true;
+        bool r = issuer ? tc::mbar_wait(bar_mma, ph_mma, a.wait_ns) : true;
         r = __syncthreads_and(r);
         if (r) {
             ph_mma ^= 1u;
@@ -458,7 +463,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_train_tc(const __grid_constan
         return r;
     };
     for (; ok && t < n_tiles; t += gridDim.x, buf ^= 1u) {
-        ok = issuer ? tc::mbar_wait(tc::smem_addr(&bars[1u + buf]), ph_load[buf]) : true;
+        ok = issuer ? tc::mbar_wait(tc::smem_addr(&bars[1u + buf]), ph_load[buf], a.wait_ns) : true;
         ok = __syncthreads_and(ok);
         if (!ok)
             break;
@@ -917,7 +922,8 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
 cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                               const LossConsts &lc, const float *positions, const float *targets, uint32_t n,
                               __half *features, __half *dfeat, __half *wpacked, float *grad, float *loss_sum,
-                              float *sample_loss, uint32_t *status, bool bf16, bool fp8, int num_sms, cudaStream_t s)
+                              float *sample_loss, uint32_t *status, bool bf16, bool fp8, int num_sms, cudaStream_t s,
+                              uint64_t wait_ns, bool stall)
 {
     if (n == 0)
         return cudaSuccess;
@@ -958,6 +964,8 @@ cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, ui
         a.loss_sum = loss_sum;
         a.sample_loss = sample_loss;
         a.status = status;
+        a.wait_ns = wait_ns ? wait_ns : tc::kWaitLimitNs;
+        a.stall = stall ? 1u : 0u;
         kernel<<<blocks, kTcThreads, p.smem, s>>>(fmap, a);
         if ((e = cudaGetLastError()) != cudaSuccess)
             return e;

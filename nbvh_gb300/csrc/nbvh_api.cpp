@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <exception>
 #include <fstream>
 #include <new>
@@ -18,6 +19,40 @@ using namespace nbvh;
 
 namespace {
 
+std::atomic<uint64_t> g_alloc_count{0};
+std::atomic<int64_t> g_alloc_fail_after{-1}; // < 0: never fail
+
+} // namespace
+
+cudaError_t nbvh::device_alloc(void **ptr, size_t bytes)
+{
+    int64_t left = g_alloc_fail_after.load();
+    while (left >= 0) { // injected failure: the next `left` allocations succeed, then every one fails
+        if (left == 0)
+            return cudaErrorMemoryAllocation;
+        if (g_alloc_fail_after.compare_exchange_weak(left, left - 1))
+            break;
+    }
+    const cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e == cudaSuccess)
+        g_alloc_count.fetch_add(1);
+    return e;
+}
+
+namespace {
+
+// Restores the caller's current device when a call returns (the library makes the handle's device
+// current for its work).
+struct DeviceScope {
+    int saved = -1;
+    DeviceScope() { (void)cudaGetDevice(&saved); }
+    ~DeviceScope()
+    {
+        if (saved >= 0)
+            (void)cudaSetDevice(saved);
+    }
+};
+
 
 template <typename F>
 nbvh_status guarded(nbvh_handle *h, F &&f)
@@ -25,6 +60,7 @@ nbvh_status guarded(nbvh_handle *h, F &&f)
     if (!h)
         return NBVH_EINVAL;
     std::lock_guard<std::mutex> lock(h->mu);
+    DeviceScope scope;
     try {
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         f();
@@ -480,6 +516,8 @@ void neural_query_noalloc(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, ui
         res.node_cursor = sc.node_cursor;
         res.h_words = host_words;
         res.ev = nullptr;
+        res.wait_ns = h->wait_limit_ns;
+        res.stall = h->debug_stall;
         res.sort_key = h->n_sort_bins ? h->d_sort_key.ptr : nullptr;
         res.n_sort_bins = h->n_sort_bins;
         cuda_check(make_feature_map(sc.features, h->layout.n_inputs, (uint32_t)kNoallocRays, &res.feature_map),
@@ -1195,7 +1233,7 @@ nbvh_status nbvh_mlp_inference(nbvh_handle *h, const uint16_t *d_features, uint3
         cuda_check(make_feature_map(reinterpret_cast<const __half *>(d_features), ni, n, &map), "feature map");
         cuda_check(cudaEventRecord(h->ev0, s), "event");
         cuda_check(launch_mlp_tc(map, h->d_wpacked.ptr, ni, H, n, nullptr, d_outputs, h->d_status.ptr, mlp_prec(h),
-                                 h->num_sms, s),
+                                 h->num_sms, s, true, h->wait_limit_ns, h->debug_stall),
                    "tensor-core MLP");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
         h->last_launches = 2;
@@ -1232,7 +1270,8 @@ void gradients_into_workspace(nbvh_handle *h, const float *d_pos, const float *d
     cuda_check(launch_train_step(h->d_params_h.ptr, h->grid, H, make_loss_consts(h->cfg, n), d_pos, d_tgt, n,
                                  h->d_train_feat.ptr, h->d_train_dfeat.ptr, h->d_train_wpacked.ptr, h->d_grad.ptr,
                                  loss_slot, h->d_train_loss.ptr, h->d_status.ptr, mlp_bf16(h),
-                                 h->cfg.network.precision == NBVH_PRECISION_FP8, h->num_sms, s),
+                                 h->cfg.network.precision == NBVH_PRECISION_FP8, h->num_sms, s, h->wait_limit_ns,
+                                 h->debug_stall),
                "forward/backward");
 }
 
@@ -1532,6 +1571,30 @@ nbvh_status nbvh_last_kernel_profile(nbvh_handle *h, nbvh_kernel_profile *out)
         out->encoded_segments = c.encoded;
         out->segments = c.segments;
     });
+}
+
+nbvh_status nbvh_debug_set_wait_limit(nbvh_handle *h, uint64_t ns)
+{
+    return guarded(h, [&]() { h->wait_limit_ns = ns; });
+}
+
+nbvh_status nbvh_debug_inject_stall(nbvh_handle *h, int enable)
+{
+    return guarded(h, [&]() { h->debug_stall = enable != 0; });
+}
+
+nbvh_status nbvh_debug_fail_allocations(int64_t after)
+{
+    g_alloc_fail_after.store(after < 0 ? -1 : after);
+    return NBVH_OK;
+}
+
+nbvh_status nbvh_debug_alloc_count(uint64_t *out)
+{
+    if (!out)
+        return NBVH_EINVAL;
+    *out = g_alloc_count.load();
+    return NBVH_OK;
 }
 
 nbvh_status nbvh_last_kernel_time(nbvh_handle *h, float *ms, uint32_t *launches)
@@ -1870,6 +1933,8 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
     res.node_cursor = q.node_cursor.ptr;
     res.h_words = q.h_words;
     res.ev = q.ev;
+    res.wait_ns = h->wait_limit_ns;
+    res.stall = h->debug_stall;
     if (tune) {
         res.visits_per_round = tune->visits_per_round;
         res.encode_blocks_per_sm = tune->encode_blocks_per_sm;

@@ -141,6 +141,10 @@ struct WaveList {
     uint32_t capacity;
 };
 
+// Device allocations of the library's buffers: a count (nbvh_debug_alloc_count) and an injected
+// failure (nbvh_debug_fail_allocations) for tests of the NBVH_ENOMEM paths.
+cudaError_t device_alloc(void **ptr, size_t bytes);
+
 template <typename T>
 struct DeviceBuffer {
     T *ptr = nullptr;
@@ -163,7 +167,7 @@ struct DeviceBuffer {
         release();
         if (n == 0)
             return cudaSuccess;
-        cudaError_t e = cudaMalloc(&ptr, n * sizeof(T));
+        cudaError_t e = device_alloc(reinterpret_cast<void **>(&ptr), n * sizeof(T));
         if (e == cudaSuccess)
             count = n;
         else
@@ -381,6 +385,8 @@ struct nbvh_handle {
     nbvh::QueryContext qctx[3]; // 0: device-buffer calls, 1-2: the host-buffer pipeline streams
 
     int num_sms = 0;
+    uint64_t wait_limit_ns = 0; // nbvh_debug_set_wait_limit (0: the kernels' default of one second)
+    bool debug_stall = false;   // nbvh_debug_inject_stall
 };
 
 namespace nbvh {
@@ -466,6 +472,8 @@ struct StepResources {
     const uint32_t *sort_key = nullptr;
     uint32_t n_sort_bins = 0;
     KernelProfile *prof = nullptr; // record encoder launch events (not under stream capture)
+    uint64_t wait_ns = 0;          // time limit of the tensor-core kernels' phase waits (0: default)
+    bool stall = false;            // failure-path tests: the MLP kernels wait on a barrier nothing arrives at
 };
 
 // Scratch of the allocation-free neural query: one static device buffer per device holding, for
@@ -530,9 +538,12 @@ cudaError_t launch_pack_weights(const __half *params_h, uint32_t n_inputs, uint3
 // the unswizzled K-major core-matrix layout (column block c of 8 values at c * 2,048 bytes).
 cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t rows, TensorMapBytes *out,
                              bool allow_swizzle = true);
+// wait_ns: time limit of the kernel's phase waits (0: the default of one second). stall (failure-path
+// tests): one wait on an mbarrier that nothing arrives at, which runs out after wait_ns.
 cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
                           uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
-                          uint32_t *status, uint32_t prec, int num_sms, cudaStream_t s, bool configure = true);
+                          uint32_t *status, uint32_t prec, int num_sms, cudaStream_t s, bool configure = true,
+                          uint64_t wait_ns = 0, bool stall = false);
 
 cudaError_t launch_encode(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                           const float *positions, uint32_t n, float *features, cudaStream_t s);
@@ -584,7 +595,8 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
 cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                               const LossConsts &lc, const float *positions, const float *targets, uint32_t n,
                               __half *features, __half *dfeat, __half *wpacked, float *grad, float *loss_sum,
-                              float *sample_loss, uint32_t *status, bool bf16, bool fp8, int num_sms, cudaStream_t s);
+                              float *sample_loss, uint32_t *status, bool bf16, bool fp8, int num_sms, cudaStream_t s,
+                              uint64_t wait_ns = 0, bool stall = false);
 
 // ---- learned tree cut (k_tree_cut.cu) ----
 // Copies the records of the late-listed rays from src (device) to dst (page-locked host).

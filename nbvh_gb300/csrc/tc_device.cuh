@@ -62,14 +62,16 @@ __device__ __forceinline__ uint64_t global_ns()
 // work behind one phase takes microseconds), so the kernel records an error and winds down.
 constexpr uint64_t kWaitLimitNs = 1000000000ull;
 
-// Waits until the phase with the given parity has completed; false after kWaitLimitNs.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+// Waits until the phase with the given parity has completed; false after limit_ns (a handle may
+// set a shorter limit for its kernels' phase waits; the waits that drain copies and MMAs still in
+// flight before a kernel exits always use kWaitLimitNs).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs)
 {
     if (mbar_try_wait(bar, parity))
         return true;
     const uint64_t t0 = global_ns();
     while (!mbar_try_wait(bar, parity)) {
-        if (global_ns() - t0 > kWaitLimitNs)
+        if (global_ns() - t0 > limit_ns)
             return false;
     }
     return true;

@@ -56,19 +56,35 @@ def test_noalloc_matches_ordinary_query_twice(scene, n):
         np.testing.assert_array_equal(out.cpu().numpy(), ref)
 
 
-def test_noalloc_uses_no_device_memory(scene):
-    h, s = scene
-    rays = torch.from_numpy(scenes.uniform_rays(MAX_RAYS, s["bbox"][:3], s["bbox"][3:], seed=9)).cuda()
-    outs = [torch.empty((MAX_RAYS, 12), dtype=torch.int32, device="cuda") for _ in range(2)]
-    assert _noalloc(h, rays, outs[0], n=0) == NBVH_OK  # setup call
-    torch.cuda.synchronize()
-    free0, _ = torch.cuda.mem_get_info()
-    for o in outs:
-        assert _noalloc(h, rays, o) == NBVH_OK, _err(h)
-    torch.cuda.synchronize()
-    free1, _ = torch.cuda.mem_get_info()
-    assert free0 - free1 < (1 << 20)
-    np.testing.assert_array_equal(outs[0].cpu().numpy(), outs[1].cpu().numpy())
+def _alloc_count(h):
+    c = C.c_uint64(0)
+    assert h.lib.nbvh_debug_alloc_count(C.byref(c)) == NBVH_OK
+    return c.value
+
+
+def test_noalloc_uses_no_device_memory(built):
+    """A fresh handle that has only ever answered allocation-free queries: the library's count of
+    its own device allocations does not move across the calls, and no device memory goes."""
+    h, s = handle(kind="sphere4k", seed=2)
+    try:
+        rays = torch.from_numpy(scenes.uniform_rays(MAX_RAYS, s["bbox"][:3], s["bbox"][3:], seed=9)).cuda()
+        outs = [torch.empty((MAX_RAYS, 12), dtype=torch.int32, device="cuda") for _ in range(2)]
+        assert _noalloc(h, rays, outs[0], n=0) == NBVH_OK  # setup call
+        torch.cuda.synchronize()
+        count0 = _alloc_count(h)
+        free0, _ = torch.cuda.mem_get_info()
+        for o in outs:
+            assert _noalloc(h, rays, o) == NBVH_OK, _err(h)
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert _alloc_count(h) == count0
+        assert free0 - free1 < (1 << 20)
+        np.testing.assert_array_equal(outs[0].cpu().numpy(), outs[1].cpu().numpy())
+        # the ordinary query on the same handle does allocate (its buffers grow to the batch)
+        h.query_closest_neural(rays, 1)
+        assert _alloc_count(h) > count0
+    finally:
+        h.close()
 
 
 def test_noalloc_rejects_batches_above_the_limit(scene):
