@@ -394,6 +394,9 @@ class NBVH:
         ids = np.ascontiguousarray(node_ids, np.uint32)
         self._check(self.lib.nbvh_set_non_neural_leaves(self.h, _ptr(ids), len(ids), int(bool(flag))))
 
+    def set_ray_ordering(self, enable):
+        self._check(self.lib.nbvh_set_ray_ordering(self.h, 1 if enable else 0))
+
     def set_ignore_neural_blas(self, ignore):
         self._check(self.lib.nbvh_set_ignore_neural_blas(self.h, int(bool(ignore))))
 

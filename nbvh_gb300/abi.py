@@ -162,6 +162,7 @@ PROTOTYPES = {
     "nbvh_get_neural_bvh": (ST, [P, P, PU32, P]),
     "nbvh_set_non_neural_leaves": (ST, [P, P, U32, I32]),
     "nbvh_set_ignore_neural_blas": (ST, [P, I32]),
+    "nbvh_set_ray_ordering": (ST, [P, I32]),
     "nbvh_query_closest_classic": (ST, [P, P, U32, P, P]),
     "nbvh_query_any_classic": (ST, [P, P, U32, P, P]),
     "nbvh_query_closest_neural": (ST, [P, P, U32, U32, P, P]),

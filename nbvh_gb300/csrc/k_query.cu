@@ -73,6 +73,7 @@ struct WaveArgs {
     __half *features;      // [capacity][n_inputs] FP16 rows of the current step
     float *outputs;        // [capacity][8] network outputs of the current step
     uint32_t *perm;        // list rows in leaf-node order (nullptr: rows in list order)
+    const uint32_t *ray_order; // the first pass's order of the rays (nullptr: batch order)
     uint32_t *node_bins;   // [2][n_sort_nodes] rows per leaf node of the current / next list
     uint32_t *node_cursor; // [2][n_sort_nodes] placement cursors of the sort
     const uint32_t *sort_key; // sort bin of each leaf (cuts above kMaxSortNodes nodes); NULL: the node
@@ -192,6 +193,118 @@ __device__ __forceinline__ void count_nodes(uint32_t *bins, bool want, uint32_t 
         atomicAdd(&bins[node], (uint32_t)__popc(same));
 }
 
+// Coherence bin of a ray: direction octant (3 bits) above the Morton code of its origin's cell in
+// an 8 x 8 x 8 grid over the scene box grown by half its size on every side (origins outside are
+// clamped to the border cells).
+__device__ __forceinline__ uint32_t ray_bin(const nbvh_ray *rays, uint32_t i, V3 lo, V3 scale)
+{
+    const float4 *r = reinterpret_cast<const float4 *>(rays + i);
+    const float4 ra = __ldg(r), rb = __ldg(r + 1);
+    const uint32_t oct = (rb.x > 0.0f ? 1u : 0u) | (rb.y > 0.0f ? 2u : 0u) | (rb.z > 0.0f ? 4u : 0u);
+    auto cell = [](float x, float l, float s) {
+        const float c = (x - l) * s;
+        return c >= 7.0f ? 7u : (c > 0.0f ? (uint32_t)c : 0u); // NaN -> 0
+    };
+    const uint32_t cx = cell(ra.x, lo.x, scale.x), cy = cell(ra.y, lo.y, scale.y), cz = cell(ra.z, lo.z, scale.z);
+    uint32_t m = 0;
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+        m |= (((cx >> b) & 1u) << (3 * b)) | (((cy >> b) & 1u) << (3 * b + 1)) | (((cz >> b) & 1u) << (3 * b + 2));
+    return (oct << 9) | m;
+}
+
+struct RayBinArgs {
+    const nbvh_ray *rays;
+    uint32_t n;
+    V3 lo, scale;
+    uint16_t *keys;
+    uint32_t *bins;  // kRayBins counts (zeroed before), then the cursors
+    uint32_t *order; // n ray ids, bin by bin
+};
+
+// Counts the rays per bin and keeps every ray's bin. Each block takes one contiguous chunk of the
+// batch and adds its shared-memory counts to the global ones (one atomic per non-empty bin).
+constexpr uint32_t kRayBinThreads = 1024;
+
+__device__ __forceinline__ void ray_chunk(uint32_t n, uint32_t &r0, uint32_t &r1)
+{
+    const uint32_t per = (n + gridDim.x - 1u) / gridDim.x;
+    r0 = min(n, blockIdx.x * per);
+    r1 = min(n, r0 + per);
+}
+
+__global__ void __launch_bounds__(kRayBinThreads) k_ray_bins(const __grid_constant__ RayBinArgs a)
+{
+    __shared__ uint32_t cnt[kRayBins];
+    for (uint32_t b = threadIdx.x; b < kRayBins; b += blockDim.x)
+        cnt[b] = 0u;
+    __syncthreads();
+    uint32_t r0, r1;
+    ray_chunk(a.n, r0, r1);
+    for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const uint32_t b = ray_bin(a.rays, i, a.lo, a.scale);
+        a.keys[i] = (uint16_t)b;
+        atomicAdd(&cnt[b], 1u);
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < kRayBins; b += blockDim.x)
+        if (cnt[b])
+            atomicAdd(&a.bins[b], cnt[b]);
+}
+
+// Exclusive scan of the bin counts into placement cursors (one block of 1,024 threads, 4 bins each).
+__global__ void __launch_bounds__(1024) k_ray_bin_scan(uint32_t *bins)
+{
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    uint32_t v[4], run = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        v[k] = bins[4u * t + k];
+        run += v[k];
+    }
+    uint32_t incl = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t x = __shfl_up_sync(kFull, incl, off);
+        if (lane >= (uint32_t)off)
+            incl += x;
+    }
+    if (lane == 31u)
+        warp_sums[warp] = incl;
+    __syncthreads();
+    uint32_t base = incl - run;
+    for (uint32_t w = 0; w < warp; w++)
+        base += warp_sums[w];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        bins[4u * t + k] = base;
+        base += v[k];
+    }
+}
+
+// Places the ray ids bin by bin: each block takes the same chunk as k_ray_bins, counts it per bin
+// again in shared memory, reserves one range per non-empty bin from the global cursors, then
+// places its rays with shared-memory atomics (the order inside a bin does not matter).
+__global__ void __launch_bounds__(kRayBinThreads) k_ray_bin_place(const __grid_constant__ RayBinArgs a)
+{
+    __shared__ uint32_t cnt[kRayBins];
+    for (uint32_t b = threadIdx.x; b < kRayBins; b += blockDim.x)
+        cnt[b] = 0u;
+    __syncthreads();
+    uint32_t r0, r1;
+    ray_chunk(a.n, r0, r1);
+    for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+        atomicAdd(&cnt[a.keys[i]], 1u);
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < kRayBins; b += blockDim.x)
+        if (cnt[b])
+            cnt[b] = atomicAdd(&a.bins[b], cnt[b]); // now this block's next position in bin b
+    __syncthreads();
+    for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+        a.order[atomicAdd(&cnt[a.keys[i]], 1u)] = i;
+}
+
 // K2 first pass: the first entered leaf of every ray (the first leaf is searched with an unbounded
 // current_maxt, include/cuda/neural/neural_bvh_module_common.cuh:332-343). Rays that enter none
 // are answered at once; the others are appended to state list 0. Persistent warps take rays from
@@ -218,7 +331,8 @@ __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_co
             exhausted = base + (uint32_t)__popc(idle) >= a.n;
             const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
             if (!active && i < a.n) {
-                const float4 *r = reinterpret_cast<const float4 *>(a.rays + i);
+                const uint32_t ray = a.ray_order ? a.ray_order[i] : i;
+                const float4 *r = reinterpret_cast<const float4 *>(a.rays + ray);
                 const float4 ra = __ldg(r), rb = __ldg(r + 1);
                 s.o = mk3(ra.x, ra.y, ra.z);
                 s.d = mk3(rb.x, rb.y, rb.z);
@@ -227,7 +341,7 @@ __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_co
                 rdiv = make_raydiv(s.o, s.d, a.nc.fast_div_ok != 0u);
                 s.sp = 1;
                 stack[0] = 0;
-                s.ray_id = i;
+                s.ray_id = ray;
                 active = true;
             }
         }
@@ -1217,6 +1331,35 @@ cudaError_t run_steps(const WaveArgs &a, const StepResources &r, size_t dec_smem
 
 } // namespace
 
+cudaError_t launch_ray_order(const nbvh_ray *rays, uint32_t n, const float scene_min[3], const float scene_max[3],
+                             uint16_t *keys, uint32_t *bins, uint32_t *order, int num_sms, cudaStream_t s)
+{
+    if (n == 0)
+        return cudaSuccess;
+    RayBinArgs rb;
+    rb.rays = rays;
+    rb.n = n;
+    float lo[3], sc[3];
+    for (int k = 0; k < 3; k++) {
+        const float ext = scene_max[k] - scene_min[k];
+        lo[k] = scene_min[k] - 0.5f * ext;
+        sc[k] = ext > 0.f ? 4.0f / ext : 0.f; // 8 cells over twice the extent
+    }
+    rb.lo.x = lo[0], rb.lo.y = lo[1], rb.lo.z = lo[2];
+    rb.scale.x = sc[0], rb.scale.y = sc[1], rb.scale.z = sc[2];
+    rb.keys = keys;
+    rb.bins = bins;
+    rb.order = order;
+    const uint32_t blocks = (uint32_t)num_sms;
+    cudaError_t e = cudaMemsetAsync(bins, 0, kRayBins * sizeof(uint32_t), s);
+    if (e != cudaSuccess)
+        return e;
+    k_ray_bins<<<blocks, kRayBinThreads, 0, s>>>(rb);
+    k_ray_bin_scan<<<1, 1024, 0, s>>>(bins);
+    k_ray_bin_place<<<blocks, kRayBinThreads, 0, s>>>(rb);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds, uint32_t n_cut_nodes,
                               const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
                               const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
@@ -1254,6 +1397,7 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     a.prec = prec;
     const bool sort = res.perm != nullptr && n_bins <= kMaxSortNodes;
     a.perm = sort ? res.perm : nullptr;
+    a.ray_order = nullptr;
     a.node_bins = res.node_bins;
     a.node_cursor = res.node_cursor;
     a.n_hidden_layers = n_hidden_layers;
@@ -1285,6 +1429,16 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     e = launch_pack_weights(params_h, grid.n_inputs, n_hidden_layers, res.wpacked, s);
     if (e != cudaSuccess)
         return e;
+    *launches = 2;
+    if (res.ray_keys && res.ray_bins && res.perm && n >= kRaySortMin) {
+        // the first pass takes the rays bin by bin (its list rows are re-sorted by node afterwards,
+        // so the buffer of the node order holds the ray order until then)
+        e = launch_ray_order(rays, n, nc.scene_min, nc.scene_max, res.ray_keys, res.ray_bins, res.perm, num_sms, s);
+        if (e != cudaSuccess)
+            return e;
+        a.ray_order = res.perm;
+        *launches += 3u;
+    }
     uint32_t first_blocks = (n + kFirstThreads - 1u) / kFirstThreads;
     const uint32_t first_cap = (uint32_t)num_sms * 4u; // resident blocks (64 registers a thread)
     if (first_blocks > first_cap)
@@ -1293,7 +1447,6 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
-    *launches = 2;
     if (smem_cut <= kSmemLimit)
         return run_steps<true>(a, res, smem_cut, num_sms, nc.max_traversal_steps, 0u, s, *launches);
     return run_steps<false>(a, res, 0, num_sms, nc.max_traversal_steps, 0u, s, *launches);

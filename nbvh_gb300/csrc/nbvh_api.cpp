@@ -920,6 +920,34 @@ nbvh_status nbvh_set_ignore_neural_blas(nbvh_handle *h, int ignore)
     return guarded(h, [&]() { h->cfg.bvh.ignore_neural_blas = ignore ? 1 : 0; });
 }
 
+} // extern "C"
+
+namespace {
+
+// The classic queries of kRaySortMin rays or more take the rays bin by bin (when ray ordering is
+// on): the order buffers, grown to n, or nullptr for batch order.
+const uint32_t *classic_order(nbvh_handle *h, uint32_t n)
+{
+    if (!h->ray_ordering || n < kRaySortMin)
+        return nullptr;
+    if (h->d_classic_order.count < n) {
+        cuda_check(h->d_classic_order.resize(n), "alloc ray order");
+        cuda_check(h->d_classic_keys.resize(n), "alloc ray bins");
+    }
+    if (h->d_classic_bins.count < kRayBins)
+        cuda_check(h->d_classic_bins.resize(kRayBins), "alloc ray bin counts");
+    return h->d_classic_order.ptr;
+}
+
+} // namespace
+
+extern "C" {
+
+nbvh_status nbvh_set_ray_ordering(nbvh_handle *h, int enable)
+{
+    return guarded(h, [&]() { h->ray_ordering = enable != 0; });
+}
+
 nbvh_status nbvh_query_closest_classic(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, nbvh_hit *d_hits,
                                        nbvh_stream stream)
 {
@@ -927,11 +955,16 @@ nbvh_status nbvh_query_closest_classic(nbvh_handle *h, const nbvh_ray *d_rays, u
         require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
         require((d_rays && d_hits) || n == 0, NBVH_EINVAL, "null buffers");
         cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        const uint32_t *order = classic_order(h, n);
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-        cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, false, nullptr, h->classic_fast_div, s),
+        if (order)
+            cuda_check(launch_ray_order(d_rays, n, h->scene_min, h->scene_max, h->d_classic_keys.ptr,
+                                        h->d_classic_bins.ptr, h->d_classic_order.ptr, h->num_sms, s),
+                       "ray order");
+        cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, false, order, h->classic_fast_div, s),
                    "classic");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
-        h->last_launches = 1;
+        h->last_launches = order ? 4u : 1u;
         h->last_rays = n;
     });
 }
@@ -943,8 +976,13 @@ nbvh_status nbvh_query_any_classic(nbvh_handle *h, const nbvh_ray *d_rays, uint3
         require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
         require((d_rays && d_hits) || n == 0, NBVH_EINVAL, "null buffers");
         cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        const uint32_t *order = classic_order(h, n);
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-        cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, true, nullptr, h->classic_fast_div, s),
+        if (order)
+            cuda_check(launch_ray_order(d_rays, n, h->scene_min, h->scene_max, h->d_classic_keys.ptr,
+                                        h->d_classic_bins.ptr, h->d_classic_order.ptr, h->num_sms, s),
+                       "ray order");
+        cuda_check(launch_classic(h->d_nodes.ptr, h->d_tris.ptr, d_rays, n, d_hits, true, order, h->classic_fast_div, s),
                    "classic");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
         h->last_launches = 1;
@@ -1857,9 +1895,10 @@ namespace nbvh {
 void grow_query_context(const nbvh_handle *h, QueryContext &q, uint32_t n)
 {
     // record every device buffer's address: a capture of this context holds them
-    const void *before[12] = {q.fallback_list.ptr, q.wave_counts.ptr, q.node_bins.ptr, q.node_cursor.ptr,
+    const void *before[14] = {q.fallback_list.ptr, q.wave_counts.ptr, q.node_bins.ptr, q.node_cursor.ptr,
                               q.wpacked.ptr,       q.od0[0].ptr,       q.stack[0].ptr,  q.stack[1].ptr,
-                              q.features.ptr,      q.outputs.ptr,      q.perm.ptr,      q.meta[1].ptr};
+                              q.features.ptr,      q.outputs.ptr,      q.perm.ptr,      q.meta[1].ptr,
+                              q.ray_keys.ptr,      q.ray_bins.ptr};
     if (q.fallback_list.count < n)
         cuda_check(q.fallback_list.resize(n), "alloc fallback list");
     if (q.wave_counts.count < 8u)
@@ -1878,6 +1917,8 @@ void grow_query_context(const nbvh_handle *h, QueryContext &q, uint32_t n)
     const uint32_t wb = packed_weight_bytes(h->layout.n_inputs, (uint32_t)h->cfg.network.n_hidden_layers);
     if (q.wpacked.count < wb / 2u)
         cuda_check(q.wpacked.resize(wb / 2u), "alloc packed weights");
+    if (q.ray_bins.count < kRayBins)
+        cuda_check(q.ray_bins.resize(kRayBins), "alloc ray bin counts");
     if (!q.ev)
         cuda_check(cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming), "event");
     if (q.capacity < n || q.features.count < (size_t)n * h->layout.n_inputs) {
@@ -1892,11 +1933,13 @@ void grow_query_context(const nbvh_handle *h, QueryContext &q, uint32_t n)
         cuda_check(q.features.resize((size_t)n * h->layout.n_inputs), "alloc feature rows");
         cuda_check(q.outputs.resize((size_t)n * kOutputs), "alloc network outputs");
         cuda_check(q.perm.resize(n), "alloc node order");
+        cuda_check(q.ray_keys.resize(n), "alloc ray bins");
         q.capacity = n;
     }
-    const void *after[12] = {q.fallback_list.ptr, q.wave_counts.ptr, q.node_bins.ptr, q.node_cursor.ptr,
+    const void *after[14] = {q.fallback_list.ptr, q.wave_counts.ptr, q.node_bins.ptr, q.node_cursor.ptr,
                              q.wpacked.ptr,       q.od0[0].ptr,       q.stack[0].ptr,  q.stack[1].ptr,
-                             q.features.ptr,      q.outputs.ptr,      q.perm.ptr,      q.meta[1].ptr};
+                             q.features.ptr,      q.outputs.ptr,      q.perm.ptr,      q.meta[1].ptr,
+                             q.ray_keys.ptr,      q.ray_bins.ptr};
     if (std::memcmp(before, after, sizeof(before)) != 0)
         q.generation++;
 }
@@ -1929,6 +1972,8 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
     res.outputs = q.outputs.ptr;
     res.wpacked = q.wpacked.ptr;
     res.perm = q.perm.ptr;
+    res.ray_keys = h->ray_ordering ? q.ray_keys.ptr : nullptr;
+    res.ray_bins = q.ray_bins.ptr;
     res.node_bins = q.node_bins.ptr;
     res.node_cursor = q.node_cursor.ptr;
     res.h_words = q.h_words;

@@ -189,6 +189,8 @@ struct QueryContext {
     DeviceBuffer<float> outputs;   // [capacity][8]
     DeviceBuffer<__half> wpacked;
     DeviceBuffer<uint32_t> perm;                   // [capacity]
+    DeviceBuffer<uint16_t> ray_keys;               // [capacity] coherence bin of each ray
+    DeviceBuffer<uint32_t> ray_bins;               // [kRayBins]
     DeviceBuffer<uint32_t> node_bins, node_cursor; // [2][cut nodes]
     uint32_t capacity = 0;
     uint64_t generation = 0;     // incremented whenever a buffer is reallocated
@@ -386,6 +388,9 @@ struct nbvh_handle {
 
     int num_sms = 0;
     uint64_t wait_limit_ns = 0; // nbvh_debug_set_wait_limit (0: the kernels' default of one second)
+    bool ray_ordering = true;   // nbvh_set_ray_ordering: batches of kRaySortMin rays or more taken bin by bin
+    nbvh::DeviceBuffer<uint16_t> d_classic_keys;  // ray order of the classic queries
+    nbvh::DeviceBuffer<uint32_t> d_classic_bins, d_classic_order;
     bool debug_stall = false;   // nbvh_debug_inject_stall
 };
 
@@ -423,6 +428,13 @@ inline cudaError_t allow_max_dynamic_smem(K kernel)
                                 kMaxDynamicSmem - (int)fa.sharedSizeBytes);
 }
 
+// Coherence bins of the rays of a query (direction octant x 8^3 origin cells of the scene box
+// grown by half its size on every side): the first pass and the classic kernel take the rays bin
+// by bin, so that the rays of a warp start near one another in the same direction. Batches below
+// kRaySortMin rays are taken in batch order.
+constexpr uint32_t kRayBins = 4096;
+constexpr uint32_t kRaySortMin = 1u << 16;
+
 // Cuts with more nodes than this are not sorted by node between steps (the sort scans the node
 // counts in shared memory).
 constexpr uint32_t kMaxSortNodes = 8192;
@@ -447,7 +459,10 @@ struct StepResources {
     __half *features;
     float *outputs;
     __half *wpacked;
-    uint32_t *perm;        // [capacity] rows in leaf-node order (nullptr: no sorting)
+    uint32_t *perm;        // [capacity] rows in leaf-node order (nullptr: no sorting); before the first
+                           // step, the order in which the first pass takes the rays
+    uint16_t *ray_keys = nullptr; // [capacity] coherence bins of the rays (nullptr: rays in batch order)
+    uint32_t *ray_bins = nullptr; // [kRayBins] counts, then placement cursors, of those bins
     uint32_t *node_bins;   // [2][n_cut_nodes]
     uint32_t *node_cursor; // [2][n_cut_nodes]
     TensorMapBytes feature_map;
@@ -516,6 +531,11 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
                               nbvh_neural_hit *hits, QueryCounters *counters, uint32_t *fallback_list,
                               const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, uint32_t prec,
                               int num_sms, cudaStream_t s, uint32_t *launches);
+
+// order[0..n) = the ray ids bin by bin (coherence bins over the scene box, kRayBins of them);
+// keys: n, bins: kRayBins device words of scratch. Three kernels and a memset on the stream.
+cudaError_t launch_ray_order(const nbvh_ray *rays, uint32_t n, const float scene_min[3], const float scene_max[3],
+                             uint16_t *keys, uint32_t *bins, uint32_t *order, int num_sms, cudaStream_t s);
 
 cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, const NeuralConsts &nc,
                             const nbvh_ray *rays, uint32_t n, uint32_t max_segments, nbvh_segment *segs,

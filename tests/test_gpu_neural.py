@@ -265,3 +265,19 @@ def test_kernel_profile_times_every_encoder_launch(scene):
     assert 1 <= p.encode_launches <= 5
     assert 0 < p.encoded_segments <= p.segments
     assert p.encode_ms > 0
+
+
+def test_ray_ordering_changes_no_result(scene):
+    """Batches of 2^16 rays or more are taken bin by bin (origin cell, direction octant); the records
+    are the same as in batch order, word for word, for the neural and the classic queries."""
+    h, s = scene
+    rays = _cuda(scenes.uniform_rays((1 << 17) + 77, s["bbox"][:3], s["bbox"][3:], seed=43))
+    a = as_u32(h.query_closest_neural(rays))
+    c = as_u32(h.query_closest_classic(rays))
+    h.set_ray_ordering(False)
+    try:
+        b = as_u32(h.query_closest_neural(rays))
+        d = as_u32(h.query_closest_classic(rays))
+    finally:
+        h.set_ray_ordering(True)
+    assert np.array_equal(a, b) and np.array_equal(c, d)
