@@ -536,6 +536,8 @@ def run_ours(args):
 
     if args.mesh4m_train_steps >= 0:
         line["mesh_4m"] = run_mesh_4m(args, nb, scenes, cfg, max_over_ranks, rank)
+    if rank == 0:
+        line["train_roofline"] = run_train_roofline(nb, scenes, peaks)
     if args.precision_sweep_steps > 0:
         line["precision_sweep"] = run_precision_sweep(args, nb, scenes, args.precision_sweep_steps)
     if rank == 0 and args.learned_cut_steps >= 0:
@@ -566,7 +568,10 @@ def summary_of(line):
             "depth_rel_mean_floor1pct": r(de.get("mean_rel_floor1pct"), 4),
             "depth_within_1pct": r(de.get("within_1pct"), 4),
             "cpu_classic_mrays_all": r(cb.get("value"), 2), "cpu_classic_mrays_1thr": r(cb.get("single_thread"), 3),
-            "cpu_cores": cb.get("cores"), "serving_p99_ms_per_1m": r(sv.get("ms_per_1m_rays_p99"))}
+            "cpu_cores": cb.get("cores"), "serving_p99_ms_per_1m": r(sv.get("ms_per_1m_rays_p99")),
+            "train_ms_per_step": r(line.get("train_roofline", {}).get("ms_per_step"), 3),
+            "train_mlp_tc_frac": r(line.get("train_roofline", {}).get("mlp_tc", {}).get("frac"), 3),
+            "mlp_tc_frac": r(line.get("roofline_kernels", {}).get("mlp_tc", {}).get("frac"), 3)}
 
 
 def run_classic_config1(h, v, f, bbox, scenes, steps, warmup, cpu_sample):
@@ -826,6 +831,42 @@ def run_learned_cut(args, nb, scenes, steps):
         out[name] = row
         h.close()
     return out
+
+
+def run_train_roofline(nb, scenes, peaks, steps=50, warmup=5):
+    """Config 3's training step (2^18 rays per step on the 65,536-triangle sphere, FP16): device time
+    of each phase of a step (kernel profile of the last step of each call), the tensor-core
+    training kernel against the sustained dense peak, Adam against the copy bandwidth."""
+    cfg = nb.default_config()
+    h, v, f, alb = build_scene(nb, scenes, cfg)
+    try:
+        h.run_optimisation(warmup)
+        h.set_kernel_profile(True)
+        st = h.run_optimisation(steps)
+        p = h.kernel_profile()
+        h.set_kernel_profile(False)
+        rows = int(p.train_rows)
+        L = h.layout
+        flop = 3.0 * FLOP_PER_SEGMENT * rows  # forward, data gradients, weight gradients
+        tc_tflops = flop / (p.train_mlp_ms * 1e-3) / 1e12
+        sustained = float(peaks.get("bf16_tflops_sustained", 1700.0))
+        # Adam per parameter: FP32 master, m, v and gradient read; master, m, v and the 16-bit copy written
+        adam_bytes = 30.0 * L.n_params
+        adam_gbs = adam_bytes / (p.train_adam_ms * 1e-3) / 1e9
+        hbm = float(peaks.get("hbm_gbs", 6800.0))
+        gathers = rows * cfg.module.input_segment_points * cfg.hashgrid.n_levels * 8
+        return {"rows_per_step": rows, "ms_per_step": st.ms_per_step, "steps": steps,
+                "phases_ms": {"sample": p.train_sample_ms, "encode": p.train_encode_ms, "mlp_tc": p.train_mlp_ms,
+                              "grid_scatter": p.train_scatter_ms, "adam": p.train_adam_ms},
+                "mlp_tc": {"kernel": "k_train_tc", "bound": "tensor", "achieved": tc_tflops, "peak": sustained,
+                           "unit": "TFLOP/s", "frac": tc_tflops / sustained,
+                           "algorithmic": "3 x 43,008 FLOP per row (forward, data and weight gradients)"},
+                "adam": {"kernel": "k_adam", "bound": "hbm", "achieved": adam_gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": adam_gbs / hbm, "algorithmic": "30 B per parameter x %d parameters" % L.n_params},
+                "grid_scatter": {"atomics_per_s": gathers / (p.train_scatter_ms * 1e-3),
+                                 "algorithmic": "one 8-byte vector atomic per (row, point, level, corner)"}}
+    finally:
+        h.close()
 
 
 def run_mesh_4m(args, nb, scenes, cfg, max_over_ranks, rank):

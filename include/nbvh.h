@@ -666,14 +666,23 @@ nbvh_status nbvh_last_kernel_time(nbvh_handle *h, float *ms, uint32_t *launches)
 /* Per-kernel timing of the dominant kernel of the neural query, the wavefront hash-grid encoder
  * (no counterpart in the reference, whose kernels are timed by external profilers). While enabled,
  * every neural query on the handle's own first context records a CUDA event pair around each
- * encoder launch on the query's stream (up to 32 launches); nbvh_last_kernel_profile waits for the
- * last query's events and reports the summed device time, the launches and the segments they
- * encoded. Disabled by default (the events cost a few microseconds per query). */
+ * encoder launch on the query's stream (up to 32 launches), and the last step of each
+ * nbvh_run_optimisation call records its phases; nbvh_last_kernel_profile waits for the events
+ * and reports the summed device time, the launches and the segments they encoded, and the
+ * training step's phases. Disabled by default (the events cost a few microseconds per query). */
 typedef struct nbvh_kernel_profile {
     float encode_ms;           /* summed device time of the encoder launches */
     uint32_t encode_launches;  /* encoder launches of the last query */
     uint32_t encoded_segments; /* leaf segments those launches encoded */
     uint32_t segments;         /* all leaf segments of the last query (the tail kernel encodes the rest) */
+    /* the last step of the last nbvh_run_optimisation call made while profiling was on (device
+     * time of each phase; train_rows = 0 if there was none) */
+    float train_sample_ms;     /* training-ray generation and labels */
+    float train_encode_ms;     /* hash-grid encoding of the rows (and the packing of the matrices) */
+    float train_mlp_ms;        /* tensor-core forward, loss, backward and weight gradients */
+    float train_scatter_ms;    /* hash-grid gradient scatter */
+    float train_adam_ms;       /* Adam */
+    uint32_t train_rows;
 } nbvh_kernel_profile;
 nbvh_status nbvh_set_kernel_profile(nbvh_handle *h, int enable);
 nbvh_status nbvh_last_kernel_profile(nbvh_handle *h, nbvh_kernel_profile *out);

@@ -136,7 +136,9 @@ class QueryStats(C.Structure):
 
 class KernelProfile(C.Structure):
     _fields_ = [("encode_ms", C.c_float), ("encode_launches", C.c_uint32), ("encoded_segments", C.c_uint32),
-                ("segments", C.c_uint32)]
+                ("segments", C.c_uint32), ("train_sample_ms", C.c_float), ("train_encode_ms", C.c_float),
+                ("train_mlp_ms", C.c_float), ("train_scatter_ms", C.c_float), ("train_adam_ms", C.c_float),
+                ("train_rows", C.c_uint32)]
 
 
 P = C.c_void_p

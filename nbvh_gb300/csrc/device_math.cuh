@@ -336,16 +336,24 @@ __device__ __forceinline__ void classic_traverse(const float4 *__restrict__ node
 
 // NeuralBVH2::intersect, include/cuda/neural/accel/neural_bvh2.cuh:170-292. Pops the next node
 // from `stack` and returns 1 with the next entered leaf segment, 0 when the stack runs empty,
-// -1 on a stack overflow (the reference prints and returns false).
+// -1 on a stack overflow (the reference prints and returns false), 2 when `budget` node visits
+// ran out first (call again to continue).
 template <typename Stack>
 __device__ __forceinline__ int neural_intersect(const float4 *__restrict__ nodes, uint32_t lod, V3 o, V3 d, Stack &stack,
                                                 int &sp, bool inference, float mint_eps_inf, float maxt_eps_inf,
                                                 float mint_eps_learn, float maxt_eps_learn, float current_maxt,
-                                                float dil, float &seg_mint, float &seg_maxt, uint32_t &seg_node)
+                                                float dil, float &seg_mint, float &seg_maxt, uint32_t &seg_node,
+                                                int budget = 0x7FFFFFFF)
 {
     const float rmint = -FLT_MAX, rmaxt = current_maxt;
     uint32_t node_idx = stack[--sp];
-    for (;;) {
+    for (;; budget--) {
+        if (budget <= 0) {
+            // out of node visits: the current node goes back on the stack and the call reports "not
+            // finished" (2); the next call resumes exactly here (sp <= 23: a push to 24 returned -1)
+            stack[sp++] = node_idx;
+            return 2;
+        }
         NodeBox node = load_node(nodes, node_idx);
         if ((node.count > 0u && node.count <= 2u + lod) || node.offset == 0xFFFFFFFFu) {
             V3 bmin, bmax;

@@ -44,6 +44,7 @@ struct SampleArgs {
     uint32_t batch_size;
     uint32_t n;
     uint32_t learned_lod;
+    uint32_t classic_fast_div; // classic BVH coordinates in the fast-division domain
     NodeSurvival survival;
 };
 
@@ -59,7 +60,107 @@ __device__ __forceinline__ V3 cube_pos_on_face(int face, float u, float v) // sa
     }
 }
 
-__global__ void __launch_bounds__(128) k_training_samples(const __grid_constant__ SampleArgs a)
+// A sample's state after its leaf segment was found: origin | mint, direction | maxt, node | rng |
+// dilation.
+struct SampleFound {
+    float4 o_mint, d_maxt;
+    uint4 node_rng;
+};
+
+constexpr uint32_t kFindThreads = 256;
+constexpr int kFindVisits = 8; // node visits of a traversal between lane refills
+
+// First part of the sampler: every sample's direction, LoD and dilation, then its search for an
+// entered leaf segment from random origins in the scaled scene box (a fresh origin after every
+// traversal that finds none). Persistent warps take samples from a counter and run the traversals
+// in rounds of kFindVisits node visits, refilling the lanes whose sample is done, so that one
+// sample's many retries do not hold its warp's other lanes idle. Every sample draws the same
+// random numbers in the same order as a thread running it alone.
+__global__ void __launch_bounds__(kFindThreads, 4) k_training_find(const __grid_constant__ SampleArgs a,
+                                                                  SampleFound *__restrict__ found,
+                                                                  uint32_t *__restrict__ counter)
+{
+    const NeuralConsts &c = a.nc;
+    const V3 smin = mk3(c.scene_min[0], c.scene_min[1], c.scene_min[2]);
+    const V3 smax = mk3(c.scene_max[0], c.scene_max[1], c.scene_max[2]);
+    const float h = __fmul_rn(__fsub_rn(c.sampling_bbox_scaling, 1.0f), 0.5f);
+    const int lane = threadIdx.x & 31;
+    uint32_t i = 0, rng = 0, sampled_lod = 0, node = 0, guard = 0;
+    float dil = 0.f, mint = 0.f, maxt = 0.f;
+    V3 o = mk3(0, 0, 0), dir = mk3(0, 0, 0);
+    uint32_t stack[kNeuralStackSize];
+    int sp = 0;
+    bool active = false, need_origin = false, exhausted = false;
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active);
+        if (idle != 0u && !exhausted) {
+            const int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader)
+                base = atomicAdd(counter, (uint32_t)__popc(idle));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            exhausted = base + (uint32_t)__popc(idle) >= a.n;
+            const uint32_t k = base + __popc(idle & ((1u << lane) - 1u));
+            if (!active && k < a.n) {
+                i = k;
+                rng = lcg_seed(a.training_step * a.batch_size, 0u, i);
+                const float sx = lcg_randomf(rng);
+                const float sy = lcg_randomf(rng);
+                dir = uniform_sphere(sx, sy);
+                // sampled LoD among the ones learned so far (common.cuh:719-721)
+                const uint32_t n_lods = kNumBvhLods - a.learned_lod;
+                const uint32_t lod_pick = __float2uint_rz(__fmul_rn(lcg_randomf(rng), __uint2float_rn(n_lods)));
+                sampled_lod = a.learned_lod + min(lod_pick, n_lods - 1u);
+                dil = __fadd_rn(c.fixed_node_dilation, __fmul_rn(lcg_randomf(rng), c.node_extent_dilation));
+                mint = maxt = 0.f;
+                node = 0;
+                guard = 0;
+                need_origin = true;
+                active = true;
+            }
+        }
+        if (!__any_sync(0xFFFFFFFFu, active)) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        if (active) {
+            if (need_origin) {
+                stack[0] = 0;
+                sp = 1;
+                const float px = lcg_randomf(rng);
+                const float py = lcg_randomf(rng);
+                const float pz = lcg_randomf(rng);
+                V3 ps = sub3(scale3(mk3(px, py, pz), c.sampling_bbox_scaling), mk3(h, h, h));
+                o = add3(mul3(ps, sub3(smax, smin)), smin);
+                need_origin = false;
+            }
+            const int res = neural_intersect(a.neural_nodes, sampled_lod, o, dir, stack, sp, false,
+                                             c.inference_mint_epsilon, c.inference_maxt_epsilon,
+                                             c.learning_mint_epsilon, c.learning_maxt_epsilon, FLT_MAX, dil, mint,
+                                             maxt, node, kFindVisits);
+            if (res != 2) {
+                if (res < 0)
+                    sp = 0;
+                if (res != 1 && ++guard < 100000u) {
+                    need_origin = true; // no leaf from this origin: the next attempt draws another
+                } else {
+                    SampleFound f;
+                    f.o_mint = make_float4(o.x, o.y, o.z, mint);
+                    f.d_maxt = make_float4(dir.x, dir.y, dir.z, maxt);
+                    f.node_rng = make_uint4(node, rng, __float_as_uint(dil), 0u);
+                    found[i] = f;
+                    active = false;
+                }
+            }
+        }
+    }
+}
+
+// Second part of the sampler, one thread per sample: leaf-boundary origins, node survival, the
+// encoded segment points and the classic-BVH labels.
+__global__ void __launch_bounds__(128) k_training_samples(const __grid_constant__ SampleArgs a,
+                                                          const SampleFound *__restrict__ found)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n)
@@ -67,42 +168,12 @@ __global__ void __launch_bounds__(128) k_training_samples(const __grid_constant_
     const NeuralConsts &c = a.nc;
     const V3 smin = mk3(c.scene_min[0], c.scene_min[1], c.scene_min[2]);
     const V3 smax = mk3(c.scene_max[0], c.scene_max[1], c.scene_max[2]);
-    uint32_t rng = lcg_seed(a.training_step * a.batch_size, 0u, i);
-    const float sx = lcg_randomf(rng);
-    const float sy = lcg_randomf(rng);
-    const V3 dir = uniform_sphere(sx, sy);
-    // sampled LoD among the ones learned so far (common.cuh:719-721)
-    const uint32_t n_lods = kNumBvhLods - a.learned_lod;
-    const uint32_t lod_pick = __float2uint_rz(__fmul_rn(lcg_randomf(rng), __uint2float_rn(n_lods)));
-    const uint32_t sampled_lod = a.learned_lod + min(lod_pick, n_lods - 1u);
-    const float dil = __fadd_rn(c.fixed_node_dilation, __fmul_rn(lcg_randomf(rng), c.node_extent_dilation));
-    uint32_t stack[kNeuralStackSize];
-    int sp = 0;
-    bool valid = false;
-    V3 o = mk3(0, 0, 0), d = dir;
-    float mint = 0.f, maxt = 0.f;
-    uint32_t node = 0;
-    uint32_t guard = 0;
-    const float h = __fmul_rn(__fsub_rn(c.sampling_bbox_scaling, 1.0f), 0.5f);
-    do {
-        if (!valid) {
-            stack[0] = 0;
-            sp = 1;
-            const float px = lcg_randomf(rng);
-            const float py = lcg_randomf(rng);
-            const float pz = lcg_randomf(rng);
-            V3 ps = sub3(scale3(mk3(px, py, pz), c.sampling_bbox_scaling), mk3(h, h, h));
-            o = add3(mul3(ps, sub3(smax, smin)), smin);
-            d = dir;
-        }
-        int res = neural_intersect(a.neural_nodes, sampled_lod, o, d, stack, sp, false, c.inference_mint_epsilon,
-                                   c.inference_maxt_epsilon, c.learning_mint_epsilon, c.learning_maxt_epsilon, FLT_MAX,
-                                   dil, mint, maxt, node);
-        valid = (res == 1);
-        if (res < 0)
-            sp = 0;
-    } while (!valid && ++guard < 100000u);
-
+    const SampleFound f = found[i];
+    V3 o = mk3(f.o_mint.x, f.o_mint.y, f.o_mint.z), d = mk3(f.d_maxt.x, f.d_maxt.y, f.d_maxt.z);
+    float mint = f.o_mint.w, maxt = f.d_maxt.w;
+    const uint32_t node = f.node_rng.x;
+    uint32_t rng = f.node_rng.y;
+    const float dil = __uint_as_float(f.node_rng.z);
     if (c.leaf_boundary_sampling_ratio != 0.0f && lcg_randomf(rng) <= c.leaf_boundary_sampling_ratio) {
         int f1 = __float2int_rz(__fmul_rn(lcg_randomf(rng), 6.0f));
         f1 = f1 < 5 ? f1 : 5;
@@ -160,7 +231,7 @@ __global__ void __launch_bounds__(128) k_training_samples(const __grid_constant_
     // labels from the classic BLAS on [mint, maxt]
     float t, u, v;
     uint32_t prim, rec = 0;
-    classic_traverse<false>(a.nodes, a.tris, o, d, mint, maxt, t, u, v, prim, &rec);
+    classic_traverse<false>(a.nodes, a.tris, o, d, mint, maxt, t, u, v, prim, &rec, a.classic_fast_div != 0u);
     float4 *tg = reinterpret_cast<float4 *>(a.targets + 8u * (size_t)i);
     if (t != FLT_MAX) {
         const float depth =
@@ -711,10 +782,8 @@ __global__ void __launch_bounds__(256) k_grid_scatter(const __grid_constant__ Gr
         const float rx = __fsub_rn(px, flx), ry = __fsub_rn(py, fly), rz = __fsub_rn(pz, flz);
         const uint32_t res = grid.res[l], size = grid.size[l], off = grid.offset[l];
         const bool hashed = grid.hashed[l] != 0u;
-#pragma unroll
-        for (uint32_t c = 0; c < 8; c++) {
+        auto corner = [&](uint32_t c, uint32_t &idx, float &w) {
             const uint32_t x = gx + (c & 1u), y = gy + ((c >> 1) & 1u), z = gz + ((c >> 2) & 1u);
-            uint32_t idx;
             if (hashed) {
                 idx = (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (size - 1u);
             } else {
@@ -722,15 +791,37 @@ __global__ void __launch_bounds__(256) k_grid_scatter(const __grid_constant__ Gr
                 if (idx >= size)
                     idx %= size;
             }
-            const float w = __fmul_rn(__fmul_rn((c & 1u) ? rx : __fsub_rn(1.0f, rx), (c & 2u) ? ry : __fsub_rn(1.0f, ry)),
-                                      (c & 4u) ? rz : __fsub_rn(1.0f, rz));
-            float *e = grid_grad + (size_t)(off + idx) * F;
+            w = __fmul_rn(__fmul_rn((c & 1u) ? rx : __fsub_rn(1.0f, rx), (c & 2u) ? ry : __fsub_rn(1.0f, ry)),
+                          (c & 4u) ? rz : __fsub_rn(1.0f, rz));
+        };
+        // corners in pairs (x, x + 1): with 2 features, a pair whose entries are the two halves of
+        // one aligned 16-byte word (every even x on hashed levels, every even entry on dense
+        // ones) takes one 16-byte atomic instead of two 8-byte ones
+#pragma unroll
+        for (uint32_t c = 0; c < 8; c += 2) {
+            uint32_t i0, i1;
+            float w0, w1;
+            corner(c, i0, w0);
+            corner(c + 1u, i1, w1);
             if (F == 2u) {
-                atomicAdd(reinterpret_cast<float2 *>(e), make_float2(w * g[0], w * g[1]));
+                const uint32_t e0 = off + i0, e1 = off + i1;
+                if ((e0 ^ e1) == 1u) {
+                    const uint32_t lo = e0 < e1 ? e0 : e1;
+                    const float wl = e0 < e1 ? w0 : w1, wh = e0 < e1 ? w1 : w0;
+                    atomicAdd(reinterpret_cast<float4 *>(grid_grad + (size_t)lo * 2u),
+                              make_float4(wl * g[0], wl * g[1], wh * g[0], wh * g[1]));
+                } else {
+                    atomicAdd(reinterpret_cast<float2 *>(grid_grad + (size_t)e0 * 2u), make_float2(w0 * g[0], w0 * g[1]));
+                    atomicAdd(reinterpret_cast<float2 *>(grid_grad + (size_t)e1 * 2u), make_float2(w1 * g[0], w1 * g[1]));
+                }
             } else {
-                for (uint32_t q = 0; q < F / 4u; q++)
-                    atomicAdd(reinterpret_cast<float4 *>(e) + q,
-                              make_float4(w * g[4 * q], w * g[4 * q + 1], w * g[4 * q + 2], w * g[4 * q + 3]));
+                float *ea = grid_grad + (size_t)(off + i0) * F, *eb = grid_grad + (size_t)(off + i1) * F;
+                for (uint32_t q = 0; q < F / 4u; q++) {
+                    atomicAdd(reinterpret_cast<float4 *>(ea) + q,
+                              make_float4(w0 * g[4 * q], w0 * g[4 * q + 1], w0 * g[4 * q + 2], w0 * g[4 * q + 3]));
+                    atomicAdd(reinterpret_cast<float4 *>(eb) + q,
+                              make_float4(w1 * g[4 * q], w1 * g[4 * q + 1], w1 * g[4 * q + 2], w1 * g[4 * q + 3]));
+                }
             }
         }
     }
@@ -893,7 +984,8 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
                                     const float *albedo, const NeuralConsts &nc, const GridParams &grid,
                                     uint32_t training_step, uint32_t batch_size, uint32_t n, float *positions,
                                     float *targets, uint32_t *sample_nodes, uint32_t learned_lod,
-                                    const NodeSurvival *survival, cudaStream_t s)
+                                    const NodeSurvival *survival, float4 *state, bool classic_fast_div, int num_sms,
+                                    cudaStream_t s)
 {
     if (n == 0)
         return cudaSuccess;
@@ -911,11 +1003,21 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
     a.batch_size = batch_size;
     a.n = n;
     a.learned_lod = learned_lod < kNumBvhLods ? learned_lod : kNumBvhLods - 1u;
+    a.classic_fast_div = classic_fast_div ? 1u : 0u;
     if (survival && survival->enabled && survival->stats)
         a.survival = *survival;
     else
         a.survival = NodeSurvival{nullptr, nullptr, 1.0f, 0.0f, 0u};
-    k_training_samples<<<(n + 127u) / 128u, 128, 0, s>>>(a);
+    SampleFound *found = reinterpret_cast<SampleFound *>(state);
+    uint32_t *counter = reinterpret_cast<uint32_t *>(found + n);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess)
+        return e;
+    uint32_t blocks = (n + kFindThreads - 1u) / kFindThreads;
+    if (blocks > (uint32_t)num_sms * 4u)
+        blocks = (uint32_t)num_sms * 4u;
+    k_training_find<<<blocks, kFindThreads, 0, s>>>(a, found, counter);
+    k_training_samples<<<(n + 127u) / 128u, 128, 0, s>>>(a, found);
     return cudaGetLastError();
 }
 
@@ -923,10 +1025,13 @@ cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, ui
                               const LossConsts &lc, const float *positions, const float *targets, uint32_t n,
                               __half *features, __half *dfeat, __half *wpacked, float *grad, float *loss_sum,
                               float *sample_loss, uint32_t *status, bool bf16, bool fp8, int num_sms, cudaStream_t s,
-                              uint64_t wait_ns, bool stall)
+                              uint64_t wait_ns, bool stall, const cudaEvent_t *marks)
 {
     if (n == 0)
         return cudaSuccess;
+    cudaError_t e = marks ? cudaEventRecord(marks[0], s) : cudaSuccess;
+    if (e != cudaSuccess)
+        return e;
     const uint32_t H = n_hidden_layers, n_in = grid.n_inputs;
     const uint32_t n_network_params =
         kNeurons * n_in + (H - 1u) * kNeurons * kNeurons + kOutputsPadded * kNeurons;
@@ -936,9 +1041,11 @@ cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, ui
         k_train_encode<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(grid, table, positions, n, features, n_in,
                                                                           bf16 ? 1u : 0u);
     }
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e == cudaSuccess)
         e = launch_pack_weights(params_h, n_in, H, wpacked, s);
+    if (e == cudaSuccess && marks)
+        e = cudaEventRecord(marks[1], s);
     if (e != cudaSuccess)
         return e;
     TensorMapBytes mb;
@@ -970,6 +1077,8 @@ cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, ui
         if ((e = cudaGetLastError()) != cudaSuccess)
             return e;
     }
+    if (marks && (e = cudaEventRecord(marks[2], s)) != cudaSuccess)
+        return e;
     const uint64_t threads = (uint64_t)n * grid.n_points;
     if (bf16)
         k_grid_scatter<true><<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(grid, positions, dfeat, n,
@@ -977,7 +1086,10 @@ cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, ui
     else
         k_grid_scatter<false><<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(grid, positions, dfeat, n,
                                                                                   grad + n_network_params);
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if (e == cudaSuccess && marks)
+        e = cudaEventRecord(marks[3], s);
+    return e;
 }
 
 cudaError_t launch_scale(float *data, size_t n, float scale, cudaStream_t s)

@@ -373,6 +373,9 @@ void free_kernel_profile(nbvh_handle *h)
     for (cudaEvent_t e : h->kprof->ev)
         if (e)
             cudaEventDestroy(e);
+    for (cudaEvent_t e : h->kprof->train_ev)
+        if (e)
+            cudaEventDestroy(e);
     delete h->kprof;
     h->kprof = nullptr;
 }
@@ -405,8 +408,15 @@ void upload_params(nbvh_handle *h, const float *params, bool reset_adam)
     cuda_check(cudaDeviceSynchronize(), "sync");
 }
 
+void ensure_sample_state(nbvh_handle *h, uint32_t n)
+{
+    if (h->d_sample_state.count < sample_state_float4s(n))
+        cuda_check(h->d_sample_state.resize(sample_state_float4s(n)), "alloc sampler state");
+}
+
 void ensure_train_workspace(nbvh_handle *h, uint32_t n)
 {
+    ensure_sample_state(h, n);
     const uint32_t P = h->grid.n_points, ni = h->layout.n_inputs, H = (uint32_t)h->cfg.network.n_hidden_layers;
     // zero-filled on allocation: a sample that node survival rejects keeps its slot's previous
     // content, which for the first step is this zero fill
@@ -1300,7 +1310,7 @@ namespace {
 
 // forward + loss + backward of one batch into h->d_grad (scaled by the loss scale) and loss_sum
 void gradients_into_workspace(nbvh_handle *h, const float *d_pos, const float *d_tgt, uint32_t n, cudaStream_t s,
-                              float *loss_slot)
+                              float *loss_slot, const cudaEvent_t *marks = nullptr)
 {
     ensure_train_workspace(h, n);
     const uint32_t H = (uint32_t)h->cfg.network.n_hidden_layers;
@@ -1309,7 +1319,7 @@ void gradients_into_workspace(nbvh_handle *h, const float *d_pos, const float *d
                                  h->d_train_feat.ptr, h->d_train_dfeat.ptr, h->d_train_wpacked.ptr, h->d_grad.ptr,
                                  loss_slot, h->d_train_loss.ptr, h->d_status.ptr, mlp_bf16(h),
                                  h->cfg.network.precision == NBVH_PRECISION_FP8, h->num_sms, s, h->wait_limit_ns,
-                                 h->debug_stall),
+                                 h->debug_stall, marks),
                "forward/backward");
 }
 
@@ -1365,12 +1375,14 @@ nbvh_status nbvh_generate_training_batch(nbvh_handle *h, uint32_t training_step,
         require(h->neural_built, NBVH_ESTATE, "neural cut not built");
         require((d_positions && d_targets) || n == 0, NBVH_EINVAL, "null buffers");
         const NeuralConsts nc = make_neural_consts(h, 1u, false);
+        ensure_sample_state(h, n);
         cuda_check(launch_training_samples(h->d_neural_nodes.ptr, h->d_nodes.ptr, h->d_tris.ptr,
                                            h->albedo.empty() ? nullptr : h->d_albedo.ptr, nc, h->grid, training_step,
                                            h->cfg.batch_size, n, d_positions, d_targets, d_nodes, kNumBvhLods - 1u,
-                                           nullptr, reinterpret_cast<cudaStream_t>(stream)),
+                                           nullptr, h->d_sample_state.ptr, h->classic_fast_div, h->num_sms,
+                                           reinterpret_cast<cudaStream_t>(stream)),
                    "training samples");
-        h->last_launches = 1;
+        h->last_launches = 2;
     });
 }
 
@@ -1395,17 +1407,27 @@ nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_sta
             uint32_t learned_lod = kNumBvhLods - 1u; // build_and_upload_neural_bvh starts at the coarsest LoD
             if (h->cut.active)
                 tree_cut_before_step(h, survival, learned_lod);
+            // with kernel profiling on, the last step records its phases
+            const bool prof = h->kprof && i + 1u == steps;
+            if (prof)
+                cuda_check(cudaEventRecord(h->kprof->train_ev[0], s), "event");
             cuda_check(launch_training_samples(h->d_neural_nodes.ptr, h->d_nodes.ptr, h->d_tris.ptr,
                                                h->albedo.empty() ? nullptr : h->d_albedo.ptr, nc, h->grid,
                                                h->training_step, n, n, h->d_train_pos.ptr, h->d_train_tgt.ptr,
-                                               h->d_train_nodes.ptr, learned_lod, &survival, s),
+                                               h->d_train_nodes.ptr, learned_lod, &survival, h->d_sample_state.ptr,
+                                               h->classic_fast_div, h->num_sms, s),
                        "training samples");
-            gradients_into_workspace(h, h->d_train_pos.ptr, h->d_train_tgt.ptr, n, s, h->d_loss_sum.ptr + i);
+            gradients_into_workspace(h, h->d_train_pos.ptr, h->d_train_tgt.ptr, n, s, h->d_loss_sum.ptr + i,
+                                     prof ? h->kprof->train_ev + 1 : nullptr);
             lr_t = adam_step_size(c, h->training_step);
             cuda_check(launch_adam(h->d_params.ptr, h->d_params_h.ptr, h->d_adam_m.ptr, h->d_adam_v.ptr, h->d_grad.ptr,
                                    h->layout.n_params, lr_t, c.optimizer.beta1, c.optimizer.beta2, c.optimizer.epsilon,
                                    c.optimizer.l2_reg, 1.0f / c.optimizer.loss_scale, param_precision(h), s),
                        "adam");
+            if (prof) {
+                cuda_check(cudaEventRecord(h->kprof->train_ev[5], s), "event");
+                h->kprof->train_rows = n;
+            }
             if (h->cut.active)
                 tree_cut_after_step(h, h->d_train_loss.ptr, n, s);
             h->training_step++;
@@ -1424,7 +1446,7 @@ nbvh_status nbvh_run_optimisation(nbvh_handle *h, uint32_t steps, nbvh_train_sta
         float ms = 0.f;
         cuda_check(cudaEventElapsedTime(&ms, h->ev0, h->ev1), "elapsed");
         h->last_kernel_ms = ms;
-        h->last_launches = 4u * steps;
+        h->last_launches = 7u * steps;
         if (stats) {
             double sum = 0.0;
             for (uint32_t i = 0; i < steps; i++)
@@ -1572,16 +1594,11 @@ nbvh_status nbvh_set_kernel_profile(nbvh_handle *h, int enable)
     return guarded(h, [&]() {
         if (enable && !h->kprof) {
             auto *p = new KernelProfile();
-            for (uint32_t k = 0; k < 2u * kMaxProfiledLaunches; k++) {
-                const cudaError_t e = cudaEventCreate(&p->ev[k]);
-                if (e != cudaSuccess) {
-                    for (uint32_t j = 0; j < k; j++)
-                        cudaEventDestroy(p->ev[j]);
-                    delete p;
-                    cuda_check(e, "event");
-                }
-            }
-            h->kprof = p;
+            h->kprof = p; // freed with its events by free_kernel_profile, also on failure here
+            for (uint32_t k = 0; k < 2u * kMaxProfiledLaunches; k++)
+                cuda_check(cudaEventCreate(&p->ev[k]), "event");
+            for (uint32_t k = 0; k < 6u; k++)
+                cuda_check(cudaEventCreate(&p->train_ev[k]), "event");
         } else if (!enable && h->kprof) {
             cuda_check(cudaDeviceSynchronize(), "sync");
             free_kernel_profile(h);
@@ -1604,10 +1621,23 @@ nbvh_status nbvh_last_kernel_profile(nbvh_handle *h, nbvh_kernel_profile *out)
             out->encode_ms += t;
             out->encode_launches++;
         }
-        QueryCounters c;
-        cuda_check(cudaMemcpy(&c, h->d_counters.ptr, sizeof(c), cudaMemcpyDeviceToHost), "counters");
-        out->encoded_segments = c.encoded;
-        out->segments = c.segments;
+        if (h->d_counters.ptr) {
+            QueryCounters c;
+            cuda_check(cudaMemcpy(&c, h->d_counters.ptr, sizeof(c), cudaMemcpyDeviceToHost), "counters");
+            out->encoded_segments = c.encoded;
+            out->segments = c.segments;
+        }
+        if (p.train_rows) {
+            float t[5];
+            for (int k = 0; k < 5; k++)
+                cuda_check(cudaEventElapsedTime(&t[k], p.train_ev[k], p.train_ev[k + 1]), "elapsed");
+            out->train_sample_ms = t[0];
+            out->train_encode_ms = t[1];
+            out->train_mlp_ms = t[2];
+            out->train_scatter_ms = t[3];
+            out->train_adam_ms = t[4];
+            out->train_rows = p.train_rows;
+        }
     });
 }
 

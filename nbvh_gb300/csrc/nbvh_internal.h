@@ -128,6 +128,10 @@ constexpr uint32_t kMaxProfiledLaunches = 32;
 struct KernelProfile {
     cudaEvent_t ev[2 * kMaxProfiledLaunches] = {};
     uint32_t used = 0; // events recorded by the last profiled query
+    // the last step of the last profiled run-optimisation call: before sampling, before the
+    // encoding, before the tensor-core passes, after them, after the grid scatter, after Adam
+    cudaEvent_t train_ev[6] = {};
+    uint32_t train_rows = 0; // 0: no training step profiled yet
 };
 
 // One state list of the wavefront neural query (structure of arrays, `capacity` rays):
@@ -347,6 +351,7 @@ struct nbvh_handle {
 
     // training workspace
     nbvh::DeviceBuffer<float> d_train_pos, d_train_tgt;
+    nbvh::DeviceBuffer<float4> d_sample_state; // scratch of the training-ray search
     nbvh::DeviceBuffer<uint32_t> d_train_nodes;
     nbvh::DeviceBuffer<__half> d_train_feat;    // n x n_inputs encoded features (16-bit)
     nbvh::DeviceBuffer<__half> d_train_dfeat;   // n x n_inputs gradients of the features (16-bit)
@@ -599,11 +604,15 @@ struct NodeSurvival {
     uint32_t enabled;
 };
 
+// Training rays of one step: the leaf-segment search, then the labels (two kernels). state:
+// sample_state_float4s(n) float4 of device scratch.
+inline size_t sample_state_float4s(uint32_t n) { return (size_t)n * 3u + 1u; }
 cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *nodes, const float4 *tris,
                                     const float *albedo, const NeuralConsts &nc, const GridParams &grid,
                                     uint32_t training_step, uint32_t batch_size, uint32_t n, float *positions,
                                     float *targets, uint32_t *sample_nodes, uint32_t learned_lod,
-                                    const NodeSurvival *survival, cudaStream_t s);
+                                    const NodeSurvival *survival, float4 *state, bool classic_fast_div, int num_sms,
+                                    cudaStream_t s);
 
 // One training pass over n rows (positions n x points x 3, targets n x 8): the hash-grid features
 // into `features` (n x n_inputs, 16-bit), the network matrices packed into `wpacked`
@@ -616,7 +625,9 @@ cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, ui
                               const LossConsts &lc, const float *positions, const float *targets, uint32_t n,
                               __half *features, __half *dfeat, __half *wpacked, float *grad, float *loss_sum,
                               float *sample_loss, uint32_t *status, bool bf16, bool fp8, int num_sms, cudaStream_t s,
-                              uint64_t wait_ns = 0, bool stall = false);
+                              uint64_t wait_ns = 0, bool stall = false, const cudaEvent_t *marks = nullptr);
+// (marks, when given: 4 events recorded before the encoding, before and after the tensor-core
+// passes, and after the grid scatter)
 
 // ---- learned tree cut (k_tree_cut.cu) ----
 // Copies the records of the late-listed rays from src (device) to dst (page-locked host).

@@ -142,3 +142,17 @@ def test_checkpoint_round_trip(scene, tmp_path):
         with pytest.raises(nb.NBVHError) as e:
             h3.load(path)
         assert e.value.status == nb.abi.NBVH_EIO
+
+
+def test_training_step_profile(scene):
+    """With kernel profiling on, the last step of a run-optimisation call reports its phases."""
+    h, s = scene
+    h.set_kernel_profile(True)
+    try:
+        h.run_optimisation(2)
+        p = h.kernel_profile()
+    finally:
+        h.set_kernel_profile(False)
+    assert p.train_rows == h.cfg.batch_size
+    for f in ("train_sample_ms", "train_encode_ms", "train_mlp_ms", "train_scatter_ms", "train_adam_ms"):
+        assert getattr(p, f) > 0, f
