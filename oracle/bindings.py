@@ -50,6 +50,14 @@ class Network(C.Structure):
                 ("n_features", C.c_uint32)]
 
 
+class PathParams(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("du", C.c_float * 3), ("dv", C.c_float * 3), ("tl", C.c_float * 3),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32), ("sample_base", C.c_uint32),
+                ("sample_offset", C.c_uint32), ("seed", C.c_uint32), ("max_bounces", C.c_uint32),
+                ("has_ground", C.c_uint32), ("ground_y", C.c_float), ("ground_albedo", C.c_float * 3),
+                ("sky_zenith", C.c_float * 3), ("sky_horizon", C.c_float * 3)]
+
+
 class NeuralScene(C.Structure):
     _fields_ = [("neural_nodes", C.c_void_p), ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3),
                 ("non_neural", C.c_void_p)]
@@ -158,6 +166,7 @@ class Oracle:
         L.orc_f32_to_f16.argtypes = [C.c_float]
         L.orc_f16_to_f32.restype = C.c_float
         L.orc_f16_to_f32.argtypes = [C.c_uint16]
+        L.orc_path_trace.restype = C.c_uint64
         self._keep = []
 
     # ---- RNG ----
@@ -407,6 +416,31 @@ class Oracle:
                                C.c_uint32(len(params)), C.c_uint32(step), C.c_float(o.learning_rate),
                                C.c_float(o.beta1), C.c_float(o.beta2), C.c_float(o.epsilon), C.c_float(o.l2_reg),
                                C.c_int32(o.decay_start), C.c_int32(o.decay_interval), C.c_float(o.decay_base))
+
+    def path_trace(self, nscene, net, consts, req, sample_base=None, threads=1):
+        """One path-traced frame of an nbvh_path_request (the library's k_path.cu restated): RGBA
+        image [height * width, 4] and the rays traced. sample_base defaults to camera.sample_idx *
+        spp, as nbvh_render_path uses."""
+        cam = req.camera
+        p = PathParams()
+        du, dv, tl = (C.c_float * 3)(), (C.c_float * 3)(), (C.c_float * 3)()
+        o = np.array(cam.origin[:], np.float32)
+        t = np.array(cam.target[:], np.float32)
+        u = np.array(cam.up[:], np.float32)
+        self.lib.orc_camera_basis(C.c_uint32(cam.width), C.c_uint32(cam.height), _p(o), _p(t), _p(u),
+                                  C.c_float(cam.yfov_degrees), du, dv, tl)
+        for k in range(3):
+            p.origin[k], p.du[k], p.dv[k], p.tl[k] = cam.origin[k], du[k], dv[k], tl[k]
+            p.ground_albedo[k], p.sky_zenith[k], p.sky_horizon[k] = (req.ground_albedo[k], req.sky_zenith[k],
+                                                                     req.sky_horizon[k])
+        p.width, p.height, p.spp = cam.width, cam.height, req.spp
+        p.sample_base = cam.sample_idx * req.spp if sample_base is None else sample_base
+        p.sample_offset, p.seed, p.max_bounces = cam.sample_offset, req.seed, req.max_bounces
+        p.has_ground, p.ground_y = 1 if req.has_ground else 0, req.ground_height
+        img = np.empty((cam.width * cam.height, 4), np.float32)
+        traced = self.lib.orc_path_trace(C.byref(nscene), C.byref(net), C.byref(consts), C.byref(p), _p(img),
+                                         C.c_int(threads))
+        return img, int(traced)
 
     def camera_rays(self, req):
         n = req.width * req.height

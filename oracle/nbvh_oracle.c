@@ -1436,6 +1436,23 @@ void orc_adam_step(float *params, float *m, float *v, const float *grad, uint32_
 /* neural_bvh_module_common.cuh:222-228                                                         */
 /* ------------------------------------------------------------------------------------------ */
 
+void orc_camera_basis(uint32_t width, uint32_t height, const float *origin, const float *target, const float *up,
+                      float yfov_degrees, float *du_out, float *dv_out, float *tl_out)
+{
+    float ipy = 2.0f * tanf((0.5f * yfov_degrees) * 0.0174532925199432958f);
+    float aspect = (float)width / (float)height;
+    float ipx = ipy * aspect;
+    v3 org = load3(origin);
+    v3 dir = vnormalize(vsub(load3(target), org));
+    v3 upv = vnormalize(load3(up));
+    v3 du = vscale(vnormalize(vcross(dir, upv)), ipx);
+    v3 dv = vscale(vnormalize(vcross(du, dir)), -ipy);
+    v3 tl = vsub(vsub(dir, vscale(du, 0.5f)), vscale(dv, 0.5f));
+    du_out[0] = du.x, du_out[1] = du.y, du_out[2] = du.z;
+    dv_out[0] = dv.x, dv_out[1] = dv.y, dv_out[2] = dv.z;
+    tl_out[0] = tl.x, tl_out[1] = tl.y, tl_out[2] = tl.z;
+}
+
 void orc_camera_rays(uint32_t width, uint32_t height, uint32_t sample_idx, uint32_t sample_offset,
                      const float *origin, const float *target, const float *up, float yfov_degrees, float *rays)
 {
@@ -1593,4 +1610,138 @@ void orc_tree_cut_assign_lod(uint32_t *nodes, uint32_t n_nodes, uint32_t lod)
         if (!node_has_child(nd))
             nd[3] = nd[3] == ORC_LEAF_FINAL ? ORC_LEAF_FINAL : ORC_LEAF_LOD(lod);
     }
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Hybrid path tracer: camera paths, Lambertian bounces on the neural hits (the network's normal */
+/* and albedo), an analytic ground plane and an analytic sky as the only light (the library's   */
+/* k_path.cu; the reference's scatter is path_inference_kernels.cu:224-429 with a Disney BSDF,  */
+/* of which this is the Lambertian case, cosine sampling as material.cuh:101-200). Every FP32   */
+/* operation in the same order as the kernels, which are compiled without FMA contraction.      */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Duff et al., "Building an Orthonormal Basis, Revisited", JCGT 6(1), 2017 */
+static void path_onb(v3 n, v3 *t, v3 *b)
+{
+    const float sign = n.z >= 0.0f ? 1.0f : -1.0f;
+    const float a = -1.0f / (sign + n.z);
+    const float c = n.x * n.y * a;
+    *t = mk(1.0f + sign * n.x * n.x * a, sign * c, -sign * n.x);
+    *b = mk(c, sign + n.y * n.y * a, -n.y);
+}
+
+/* cosine-weighted direction about n: a uniform disk point lifted to the hemisphere */
+static v3 path_cosine_sample(v3 n, uint32_t *rng)
+{
+    const float u1 = orc_lcg_randomf(rng), u2 = orc_lcg_randomf(rng);
+    float sp, cp;
+    orc_sincos_turns(u2, &sp, &cp);
+    const float r = sqrtf(u1), z = sqrtf(fmaxf(0.0f, 1.0f - u1));
+    v3 t, b;
+    path_onb(n, &t, &b);
+    return mk(r * cp * t.x + r * sp * b.x + z * n.x, r * cp * t.y + r * sp * b.y + z * n.y,
+              r * cp * t.z + r * sp * b.z + z * n.z);
+}
+
+uint64_t orc_path_trace(const orc_neural_scene *scene, const orc_network *net, const orc_neural_consts *c,
+                        const orc_path_params *p, float *image, int n_threads)
+{
+    const uint32_t n = p->width * p->height * p->spp;
+    float *thr = (float *)malloc(sizeof(float) * 4u * n), *rad = (float *)calloc(4u * (size_t)n, sizeof(float));
+    float *rays = (float *)malloc(sizeof(float) * 8u * n), *next = (float *)malloc(sizeof(float) * 8u * n);
+    uint32_t *ids = (uint32_t *)malloc(sizeof(uint32_t) * n), *next_ids = (uint32_t *)malloc(sizeof(uint32_t) * n);
+    uint32_t *hits = (uint32_t *)malloc(sizeof(uint32_t) * 12u * n);
+    const v3 du = load3(p->du), dv = load3(p->dv), tl = load3(p->tl);
+    for (uint32_t i = 0; i < n; i++) { /* raygen: the camera jitter of sample sample_base + s */
+        const uint32_t px_ = i / p->spp, smp = i - px_ * p->spp;
+        const uint32_t x = px_ % p->width, y = px_ / p->width;
+        uint32_t rng = orc_lcg_seed(p->sample_base + smp, p->sample_offset, px_);
+        const float jx = orc_lcg_randomf(&rng), jy = orc_lcg_randomf(&rng);
+        const float xf = ((float)x + jx) / (float)p->width;
+        const float yf = ((float)y + jy) / (float)p->height;
+        const v3 d = vnormalize(vadd(vadd(vscale(du, xf), vscale(dv, yf)), tl));
+        float *r = rays + 8u * (size_t)i;
+        r[0] = p->origin[0], r[1] = p->origin[1], r[2] = p->origin[2], r[3] = 1e-4f;
+        r[4] = d.x, r[5] = d.y, r[6] = d.z, r[7] = FLT_MAX;
+        ids[i] = i;
+        thr[4u * i] = thr[4u * i + 1u] = thr[4u * i + 2u] = 1.0f;
+        const uint32_t bits = rng ^ (p->seed * 0x9E3779B9u);
+        memcpy(&thr[4u * i + 3u], &bits, 4);
+    }
+    uint32_t count = n;
+    uint64_t traced = 0;
+    for (uint32_t bounce = 0; count > 0 && bounce <= p->max_bounces; bounce++) {
+        orc_neural_query(scene, net, c, NULL, 0.0f, rays, count, bounce == 0 ? 1u : 2u, 0, hits, n_threads);
+        traced += count;
+        uint32_t out = 0;
+        for (uint32_t j = 0; j < count; j++) {
+            const uint32_t id = ids[j];
+            const float *r = rays + 8u * (size_t)j;
+            const v3 ro = mk(r[0], r[1], r[2]), d = mk(r[4], r[5], r[6]);
+            const uint32_t *h = hits + 12u * (size_t)j;
+            float hf[8];
+            memcpy(hf, h, sizeof(hf));
+            const int nhit = (h[8] & 1u) != 0u;
+            float t = nhit ? hf[0] : FLT_MAX;
+            v3 nrm = mk(hf[1], hf[2], hf[3]), alb = mk(hf[4], hf[5], hf[6]);
+            if (p->has_ground && d.y != 0.0f) {
+                const float tp = (p->ground_y - ro.y) / d.y;
+                if (tp > 1e-4f && tp < t) {
+                    t = tp;
+                    nrm = mk(0.0f, 1.0f, 0.0f);
+                    alb = load3(p->ground_albedo);
+                }
+            }
+            float *th = thr + 4u * (size_t)id;
+            if (t == FLT_MAX) {
+                const float w = fmaxf(d.y, 0.0f);
+                float *ra = rad + 4u * (size_t)id;
+                for (int k = 0; k < 3; k++)
+                    ra[k] += th[k] * (p->sky_horizon[k] + (p->sky_zenith[k] - p->sky_horizon[k]) * w);
+            } else if (bounce < p->max_bounces) {
+                const float len = sqrtf(nrm.x * nrm.x + nrm.y * nrm.y + nrm.z * nrm.z);
+                nrm = len > 0.0f ? mk(nrm.x / len, nrm.y / len, nrm.z / len) : mk(-d.x, -d.y, -d.z);
+                if (nrm.x * d.x + nrm.y * d.y + nrm.z * d.z > 0.0f)
+                    nrm = mk(-nrm.x, -nrm.y, -nrm.z);
+                uint32_t rng;
+                memcpy(&rng, &th[3], 4);
+                const v3 nd = path_cosine_sample(nrm, &rng);
+                th[0] = th[0] * alb.x;
+                th[1] = th[1] * alb.y;
+                th[2] = th[2] * alb.z;
+                memcpy(&th[3], &rng, 4);
+                const v3 o = mk(ro.x + t * d.x + 1e-3f * nrm.x, ro.y + t * d.y + 1e-3f * nrm.y,
+                                ro.z + t * d.z + 1e-3f * nrm.z);
+                if (th[0] + th[1] + th[2] > 0.0f) {
+                    float *q = next + 8u * (size_t)out;
+                    q[0] = o.x, q[1] = o.y, q[2] = o.z, q[3] = 1e-4f;
+                    q[4] = nd.x, q[5] = nd.y, q[6] = nd.z, q[7] = FLT_MAX;
+                    next_ids[out++] = id;
+                }
+            }
+        }
+        float *tr = rays;
+        rays = next;
+        next = tr;
+        uint32_t *ti = ids;
+        ids = next_ids;
+        next_ids = ti;
+        count = out;
+    }
+    const float inv = 1.0f / (float)p->spp;
+    for (uint32_t px_ = 0; px_ < p->width * p->height; px_++) {
+        float r = 0.f, g = 0.f, b = 0.f;
+        for (uint32_t s = 0; s < p->spp; s++) {
+            const float *v = rad + 4u * ((size_t)px_ * p->spp + s);
+            r += v[0];
+            g += v[1];
+            b += v[2];
+        }
+        image[4u * px_] = r * inv;
+        image[4u * px_ + 1u] = g * inv;
+        image[4u * px_ + 2u] = b * inv;
+        image[4u * px_ + 3u] = 1.0f;
+    }
+    free(thr), free(rad), free(rays), free(next), free(ids), free(next_ids), free(hits);
+    return traced;
 }

@@ -220,4 +220,21 @@ void orc_camera_rays(uint32_t width, uint32_t height, uint32_t sample_idx, uint3
 }
 #endif
 
+/* --- hybrid path tracer (the library's wavefront path tracer, k_path.cu, after the reference's
+ *     Lambertian case of path_inference_kernels.cu:224-429 and material.cuh:101-200) --- */
+typedef struct orc_path_params {
+    float origin[3], du[3], dv[3], tl[3]; /* pinhole camera: d = normalize(du * x + dv * y + tl) */
+    uint32_t width, height, spp, sample_base, sample_offset, seed, max_bounces, has_ground;
+    float ground_y;
+    float ground_albedo[3], sky_zenith[3], sky_horizon[3];
+} orc_path_params;
+
+/* Camera basis of CudaBackend::update_camera (cuda_backend.cpp:595-611), as orc_camera_rays. */
+void orc_camera_basis(uint32_t width, uint32_t height, const float *origin, const float *target, const float *up,
+                      float yfov_degrees, float *du, float *dv, float *tl);
+
+/* One frame: image receives width x height RGBA values; returns the rays traced. */
+uint64_t orc_path_trace(const orc_neural_scene *scene, const orc_network *net, const orc_neural_consts *c,
+                        const orc_path_params *p, float *image, int n_threads);
+
 #endif
