@@ -87,6 +87,12 @@ def parse():
     ap.add_argument("--mlp-only", type=int, default=0, metavar="LOG2_ROWS",
                     help="time only the tcgen05 MLP on 2^LOG2_ROWS resident rows (inside the NVTX range "
                          "`mlp_roofline`), print its line and exit; for profiling captures")
+    ap.add_argument("--query-only", action="store_true",
+                    help="time only the neural and classic queries of the headline workload (--log2-rays rays, "
+                         "committed weights), print their line and exit; for profiling captures")
+    ap.add_argument("--train-only", type=int, default=0, metavar="STEPS",
+                    help="run only the training roofline (STEPS profiled steps of 2^18 rays), print it and exit; "
+                         "for profiling captures")
     return ap.parse_args()
 
 
@@ -394,6 +400,13 @@ def run_ours(args):
     cfg = nb.default_config()
     h, v, f, alb = build_scene(nb, scenes, cfg)
     nn, bbox = h.neural_bvh()
+    if args.train_only:
+        peaks, _ = measured_peaks()
+        h.close()
+        if rank == 0:
+            print(json.dumps({"train_roofline": run_train_roofline(nb, scenes, peaks, steps=args.train_only,
+                                                                   warmup=3)}))
+        return
     if args.mlp_only:
         peaks, peak_kind = measured_peaks()
         torch.cuda.nvtx.range_push("mlp_roofline")
@@ -418,6 +431,17 @@ def run_ours(args):
     if not use_file:
         st = h.run_optimisation(args.train_steps) if args.train_steps > 0 else None
     train_s = time.perf_counter() - t0
+    if args.query_only:
+        rays_np = scenes.uniform_rays(N_RAYS, bbox[:3], bbox[3:], seed=2024 + rank)
+        rays = torch.from_numpy(rays_np).cuda()
+        hits = torch.empty((N_RAYS, 12), dtype=torch.int32, device="cuda")
+        chits = torch.empty((N_RAYS, 4), dtype=torch.int32, device="cuda")
+        times, ctimes, nl, cl = time_queries(h, rays, hits, chits, args.steps, args.warmup, "timed")
+        if rank == 0:
+            print(json.dumps({"rays": N_RAYS, "neural_ms": float(times.mean()), "classic_ms": float(ctimes.mean()),
+                              "neural_launches": nl, "classic_launches": cl, "weights": weights_from}))
+        h.close()
+        return
     if args.save_bench_data:
         if rank == 0:
             save_bench_data(args.save_bench_data, h, cfg, nn, bbox, st, args.train_steps)
@@ -473,7 +497,10 @@ def run_ours(args):
     enc_bytes = ENCODE_BYTES_PER_SEGMENT * sum(p.encoded_segments for p in enc_prof)
     enc_gbs = enc_bytes / (enc_ms * 1e-3) / 1e9 if enc_ms > 0 else None
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    enc_traffic = profiled_traffic("encode_dram_bytes_per_launch_full_workload")
+    # DRAM bytes per launch: the encoder's DRAM bytes per encoded segment from its ncu capture
+    # (profiles/k_wave_encode_sphere65k_rays1M.md) x the segments an average launch encodes here
+    per_seg = profiled_traffic("encode_dram_bytes_per_segment")
+    enc_traffic = (per_seg * sum(p.encoded_segments for p in enc_prof) / max(1, enc_launches)) if per_seg else None
     value = world * N_RAYS / (ms * 1e-3) / 1e6
     line = {
         "metric": METRIC,
@@ -515,7 +542,7 @@ def run_ours(args):
     line["roofline_kernels"] = {
         "mlp_tc": mlp_roofline(h, peak),
         "whole_query_tensor": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                               "frac": achieved / peak, "traffic": profiled_traffic(),
+                               "frac": achieved / peak, "traffic": None,
                                "algorithmic": "43,008 FLOP per inferred leaf segment x %d segments per query"
                                               % stats.segments},
     }
@@ -560,6 +587,7 @@ def summary_of(line):
     m4 = line.get("mesh_4m", {})
     de = line.get("depth_error", {})
     sv = line.get("serving", {}).get("neural", {}) if isinstance(line.get("serving"), dict) else {}
+    b1m = sv.get("batch_1m", {})
     return {"neural_mrays": r(line["value"]), "classic_mrays": r(line.get("classic_mrays")),
             "neural_over_classic": r(line.get("neural_over_classic"), 3),
             "mesh4m_neural_over_classic": r(m4.get("neural_over_classic"), 3),
@@ -569,6 +597,7 @@ def summary_of(line):
             "depth_within_1pct": r(de.get("within_1pct"), 4),
             "cpu_classic_mrays_all": r(cb.get("value"), 2), "cpu_classic_mrays_1thr": r(cb.get("single_thread"), 3),
             "cpu_cores": cb.get("cores"), "serving_p99_ms_per_1m": r(sv.get("ms_per_1m_rays_p99")),
+            "serving_1m_batch_p99_ms": r(b1m.get("p99_ms"), 2), "serving_1m_batch_p50_ms": r(b1m.get("p50_ms"), 2),
             "train_ms_per_step": r(line.get("train_roofline", {}).get("ms_per_step"), 3),
             "train_mlp_tc_frac": r(line.get("train_roofline", {}).get("mlp_tc", {}).get("frac"), 3),
             "mlp_tc_frac": r(line.get("roofline_kernels", {}).get("mlp_tc", {}).get("frac"), 3)}
@@ -703,8 +732,29 @@ def run_serving(args, nb, scenes):
         h.run_optimisation(args.serve_train_steps)
         models.append((h, h.neural_bvh()[1], len(f)))
 
+    # 1M-ray query batches (rays through the model's scene box) submitted 10 times a second on top of
+    # the render load: their latency is the p50 / p99 "per 1M-ray batch"
+    probe_rays = [scenes.uniform_rays(1 << 20, m[1][:3], m[1][3:], seed=900 + k) for k, m in enumerate(models)]
+
     def load(srv, ids, seconds, rate, clients, seed):
         done, lock = [], threading.Lock()
+        probes = []
+
+        def prober():
+            rng = np.random.default_rng(seed + 77)
+            tickets, t_end = [], time.perf_counter() + seconds
+            t_next = time.perf_counter() + 0.05
+            while t_next < t_end:
+                delay = t_next - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                m = int(rng.integers(len(ids)))
+                tickets.append(srv.submit_query(ids[m], probe_rays[m], 1))
+                t_next += 0.1
+            for t in tickets:
+                _, res = srv.wait(t, timeout_ms=600000)
+                with lock:
+                    probes.append(res.latency_ms)
 
         def client(c):
             rng = np.random.default_rng(seed * 1000 + c)
@@ -729,6 +779,7 @@ def run_serving(args, nb, scenes):
                     done.append((res.latency_ms, res.rays_traced))
 
         threads = [threading.Thread(target=client, args=(c,)) for c in range(clients)]
+        threads.append(threading.Thread(target=prober))
         t0 = time.perf_counter()
         for t in threads:
             t.start()
@@ -748,7 +799,10 @@ def run_serving(args, nb, scenes):
                 "ms_per_1m_rays_p99": float(np.percentile(per_m, 99)),
                 "requests_0p5_to_2m_rays": int(near_1m.size),
                 "p99_ms_requests_0p5_to_2m_rays": float(np.percentile(near_1m, 99)) if near_1m.size else None,
-                "mean_rays_per_request": float(rays.mean())}
+                "mean_rays_per_request": float(rays.mean()),
+                "batch_1m": {"count": len(probes), "p50_ms": float(np.percentile(probes, 50)) if probes else None,
+                             "p99_ms": float(np.percentile(probes, 99)) if probes else None,
+                             "what": "1,048,576-ray query batches, 10 per second, under the render load"}}
 
     out = {"models_triangles": [m[2] for m in models], "clients": 64, "rate_req_per_s": 200.0,
            "seconds_of_arrivals": args.serve_seconds, "hbm_budget_gb": 150}
