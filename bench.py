@@ -350,6 +350,15 @@ def run_reference(args):
     rays = scenes.uniform_rays(N_RAYS, bbox[:3], bbox[3:], seed=2024)
     sample = rays[:args.cpu_sample]
     orc = Oracle()
+    # the level scales as this machine's C library computes them (tcnn's exp2f / log2f formula), the
+    # same the GPU arm's library computes here; the committed offsets and sizes must agree
+    hg = cfg.hashgrid
+    off, size, res, scale, total = orc.grid_layout(hg.n_levels, hg.log2_hashmap_size, hg.base_resolution,
+                                                   hg.per_level_scale)
+    assert list(off) == list(layout.level_offset[:hg.n_levels]) and list(size) == list(layout.level_size[:hg.n_levels])
+    for l in range(hg.n_levels):
+        layout.level_scale[l] = float(scale[l])
+        layout.level_resolution[l] = int(res[l])
     net = orc.network(cfg, layout, params)
     consts = orc.neural_consts(cfg)
     nscene = orc.neural_scene(nn, bbox)

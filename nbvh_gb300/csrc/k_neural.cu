@@ -1,6 +1,7 @@
-// k_neural.cu -- stand-alone kernels of the neural path: the N-BVH segment enumeration (K2 alone),
-// hash-grid encoding (K3 forward alone) and network inference on explicit positions (K3 + K4
-// forward). The neural closest-hit query itself is the wavefront in k_query.cu.
+// k_neural.cu -- stand-alone kernels of the neural path: the N-BVH segment enumeration (K2 alone)
+// and the hash-grid encoding (K3 forward alone, FP32 features). Network inference on explicit
+// positions is the training encoder's FP16 rows followed by the tcgen05 MLP (k_train.cu,
+// k_mlp_tc.cu); the neural closest-hit query itself is the wavefront in k_query.cu.
 #include "device_math.cuh"
 #include "net_device.cuh"
 #include "nbvh_internal.h"
@@ -8,17 +9,6 @@
 namespace nbvh {
 
 namespace {
-
-constexpr int kWarps = 8;
-constexpr int kThreads = kWarps * 32;
-
-__device__ __forceinline__ void copy_grid_params(GridParams &dst, const GridParams &src)
-{
-    const uint32_t *s = reinterpret_cast<const uint32_t *>(&src);
-    uint32_t *d = reinterpret_cast<uint32_t *>(&dst);
-    for (uint32_t i = threadIdx.x; i < sizeof(GridParams) / 4u; i += blockDim.x)
-        d[i] = s[i];
-}
 
 // Every leaf segment a ray enters with current_maxt = FLT_MAX (NeuralBVH2::intersect alone, on the
 // same pre-dilated, culling traversal the query kernel uses).
@@ -61,59 +51,6 @@ __global__ void __launch_bounds__(128) k_segments(const float4 *__restrict__ nod
     counts[i] = cnt;
 }
 
-struct InferArgs {
-    GridParams grid;
-    const uint32_t *table;
-    const __half *weights;
-    const float *positions;
-    float *outputs;
-    uint32_t n_hidden_layers;
-    uint32_t n;
-    uint32_t fp8;
-};
-
-// Network inference on explicit encoded positions: one warp per 16-row tile, grid-stride.
-template <bool BF16, bool FP8>
-__global__ void __launch_bounds__(kThreads, 2) k_network_inference(const __grid_constant__ InferArgs args)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    GridParams &gp = *reinterpret_cast<GridParams *>(smem_raw);
-    const uint32_t n_inputs = args.grid.n_inputs, P = args.grid.n_points, L = args.grid.n_levels;
-    __half *sw = reinterpret_cast<__half *>(smem_raw + kGridParamsSmem);
-    const SmemNetLayout SL = smem_net_layout(n_inputs, args.n_hidden_layers);
-    const uint32_t fld = n_inputs + 8u;
-    __half *feat = sw + SL.total + (size_t)(threadIdx.x >> 5) * 16u * fld; // per-warp feature tile
-    copy_grid_params(gp, args.grid);
-    load_weights_to_smem(args.weights, sw, n_inputs, args.n_hidden_layers);
-    __syncthreads();
-    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
-    const uint32_t warps_total = gridDim.x * kWarps;
-    const uint32_t n_tiles = (args.n + 15u) / 16u;
-    (void)L;
-    for (uint32_t tile = blockIdx.x * kWarps + (threadIdx.x >> 5); tile < n_tiles; tile += warps_total) {
-        const uint32_t r0 = tile * 16u + g, r1 = r0 + 8u;
-        const bool act0 = r0 < args.n, act1 = r1 < args.n;
-        const uint32_t rows = args.n - tile * 16u;
-        const uint32_t mask = rows >= 16u ? 0xFFFFu : ((1u << rows) - 1u);
-        auto pos = [&](uint32_t r, uint32_t p) -> V3 {
-            const float *src = args.positions + ((size_t)(tile * 16u + r) * P + p) * 3u;
-            return mk3(__ldg(src), __ldg(src + 1), __ldg(src + 2));
-        };
-        encode_tile_any<BF16>(args.table, gp, pos, mask, feat, fld);
-        float o4[4];
-        mlp_tile_from_smem<BF16, FP8>(sw, feat, fld, n_inputs, args.n_hidden_layers, o4);
-        __syncwarp();
-        if (act0) {
-            args.outputs[(size_t)r0 * 8u + tig * 2] = o4[0];
-            args.outputs[(size_t)r0 * 8u + tig * 2 + 1] = o4[1];
-        }
-        if (act1) {
-            args.outputs[(size_t)r1 * 8u + tig * 2] = o4[2];
-            args.outputs[(size_t)r1 * 8u + tig * 2 + 1] = o4[3];
-        }
-    }
-}
-
 // Hash-grid features (FP32 before the FP16 rounding), one thread per (row, point, level); level l
 // of a point's block holds its F features at l * F.
 __global__ void __launch_bounds__(128) k_encode(const __grid_constant__ GridParams grid, const uint32_t *__restrict__ table,
@@ -147,12 +84,6 @@ __global__ void __launch_bounds__(128) k_encode(const __grid_constant__ GridPara
     }
 }
 
-template <typename K>
-cudaError_t prepare_smem(K kernel, size_t bytes)
-{
-    (void)bytes; // every launch stays below the common limit
-    return allow_max_dynamic_smem(kernel);
-}
 
 } // namespace
 
@@ -163,46 +94,6 @@ cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, c
     if (n == 0)
         return cudaSuccess;
     k_segments<<<(n + 127u) / 128u, 128, 0, s>>>(dilated_nodes, bounds, nc, rays, n, max_segments, segs, counts);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_network_inference(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
-                                     const float *positions, uint32_t n, float *outputs, uint32_t prec, int num_sms,
-                                     cudaStream_t s)
-{
-    if (n == 0)
-        return cudaSuccess;
-    const bool bf16 = prec == NBVH_PRECISION_BF16;
-    InferArgs a;
-    a.fp8 = prec == NBVH_PRECISION_FP8 ? 1u : 0u;
-    a.grid = grid;
-    uint32_t n_network_params = kNeurons * grid.n_inputs + (n_hidden_layers - 1u) * kNeurons * kNeurons +
-                                kOutputsPadded * kNeurons;
-    a.table = reinterpret_cast<const uint32_t *>(params_h + n_network_params);
-    a.weights = params_h;
-    a.positions = positions;
-    a.outputs = outputs;
-    a.n_hidden_layers = n_hidden_layers;
-    a.n = n;
-    size_t smem = kGridParamsSmem + smem_net_layout(grid.n_inputs, n_hidden_layers).total * sizeof(__half) +
-                  (size_t)kWarps * 16u * (grid.n_inputs + 8u) * sizeof(__half);
-    const bool fp8 = a.fp8 != 0u;
-    cudaError_t e = bf16  ? prepare_smem(k_network_inference<true, false>, smem)
-                    : fp8 ? prepare_smem(k_network_inference<false, true>, smem)
-                          : prepare_smem(k_network_inference<false, false>, smem);
-    if (e != cudaSuccess)
-        return e;
-    uint32_t tiles = (n + 15u) / 16u;
-    uint32_t blocks = (tiles + kWarps - 1u) / kWarps;
-    uint32_t cap = (uint32_t)num_sms * 2u;
-    if (blocks > cap)
-        blocks = cap;
-    if (bf16)
-        k_network_inference<true, false><<<blocks, kThreads, smem, s>>>(a);
-    else if (fp8)
-        k_network_inference<false, true><<<blocks, kThreads, smem, s>>>(a);
-    else
-        k_network_inference<false, false><<<blocks, kThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 

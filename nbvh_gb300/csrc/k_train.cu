@@ -1021,6 +1021,20 @@ cudaError_t launch_training_samples(const float4 *neural_nodes, const float4 *no
     return cudaGetLastError();
 }
 
+cudaError_t launch_encode_rows(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
+                               const float *positions, uint32_t n, __half *features, bool bf16, cudaStream_t s)
+{
+    if (n == 0)
+        return cudaSuccess;
+    const uint32_t n_network_params =
+        kNeurons * grid.n_inputs + (n_hidden_layers - 1u) * kNeurons * kNeurons + kOutputsPadded * kNeurons;
+    const uint32_t *table = reinterpret_cast<const uint32_t *>(params_h + n_network_params);
+    const uint64_t threads = (uint64_t)n * grid.n_points;
+    k_train_encode<<<(unsigned)((threads + 255u) / 256u), 256, 0, s>>>(grid, table, positions, n, features,
+                                                                      grid.n_inputs, bf16 ? 1u : 0u);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_train_step(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
                               const LossConsts &lc, const float *positions, const float *targets, uint32_t n,
                               __half *features, __half *dfeat, __half *wpacked, float *grad, float *loss_sum,

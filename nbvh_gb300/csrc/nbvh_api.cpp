@@ -136,8 +136,9 @@ void validate_config(const nbvh_config &c)
         fail(NBVH_EINVAL, "loss_scale must be positive");
 }
 
-// Grid geometry: scale_l = base * per_level_scale^l - 1 (power by repeated double
-// multiplication), res = ceil(scale) + 1, entries = min(roundup8(res^3), 2^log2T).
+// Grid geometry (tcnn's GridEncoding conventions): scale_l = exp2f(l * log2f(per_level_scale)) *
+// base - 1 in single precision, the C library's exp2f and log2f called as tcnn's grid_scale does;
+// res = ceil(scale) + 1; entries = min(roundup8(res^3), 2^log2T).
 void compute_layout(const nbvh_config &c, nbvh_param_layout &L, GridParams &g)
 {
     std::memset(&L, 0, sizeof(L));
@@ -145,9 +146,10 @@ void compute_layout(const nbvh_config &c, nbvh_param_layout &L, GridParams &g)
     const uint32_t nl = (uint32_t)c.hashgrid.n_levels;
     const uint64_t hashmap = 1ull << c.hashgrid.log2_hashmap_size;
     uint64_t off = 0;
-    double p = 1.0;
+    const float log2_scale = std::log2(c.hashgrid.per_level_scale);
     for (uint32_t l = 0; l < nl; l++) {
-        float s = (float)((double)c.hashgrid.base_resolution * p - 1.0);
+        const float grow = std::exp2((float)l * log2_scale);
+        const float s = grow * (float)c.hashgrid.base_resolution - 1.0f;
         uint32_t res = (uint32_t)std::ceil(s) + 1u;
         uint64_t dense = (uint64_t)res * res * res;
         uint64_t dense8 = (dense + 7u) & ~7ull;
@@ -162,7 +164,6 @@ void compute_layout(const nbvh_config &c, nbvh_param_layout &L, GridParams &g)
         g.scale[l] = s;
         g.hashed[l] = dense > sz ? 1u : 0u;
         off += sz;
-        p *= (double)c.hashgrid.per_level_scale;
     }
     L.n_levels = nl;
     L.n_inputs = n_inputs_of(c);
@@ -1250,12 +1251,35 @@ nbvh_status nbvh_network_inference(nbvh_handle *h, const float *d_positions, uin
     return guarded(h, [&]() {
         require((d_positions && d_outputs) || n == 0, NBVH_EINVAL, "null buffers");
         cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+        const uint32_t ni = h->layout.n_inputs, H = (uint32_t)h->cfg.network.n_hidden_layers;
+        h->last_launches = 0;
+        if (n == 0)
+            return;
+        // the encoder writes FP16 feature rows, the tcgen05 MLP reads them by TMA
+        if (h->d_infer_feat.count < (size_t)n * ni)
+            cuda_check(h->d_infer_feat.resize((size_t)n * ni), "alloc feature rows");
+        const uint32_t wb = packed_weight_bytes(ni, H);
+        if (h->d_wpacked.count < wb / 2u)
+            cuda_check(h->d_wpacked.resize(wb / 2u), "alloc packed weights");
+        if (h->d_status.count < 1u)
+            cuda_check(h->d_status.resize(1u), "alloc status");
+        TensorMapBytes map;
+        cuda_check(make_feature_map(h->d_infer_feat.ptr, ni, n, &map), "feature map");
+        cuda_check(cudaMemsetAsync(h->d_status.ptr, 0, sizeof(uint32_t), s), "reset status");
         cuda_check(cudaEventRecord(h->ev0, s), "event");
-        cuda_check(launch_network_inference(h->d_params_h.ptr, h->grid, (uint32_t)h->cfg.network.n_hidden_layers,
-                                            d_positions, n, d_outputs, mlp_prec(h), h->num_sms, s),
-                   "network inference");
+        cuda_check(launch_encode_rows(h->d_params_h.ptr, h->grid, H, d_positions, n, h->d_infer_feat.ptr, mlp_bf16(h), s),
+                   "encode");
+        cuda_check(launch_pack_weights(h->d_params_h.ptr, ni, H, h->d_wpacked.ptr, s), "pack weights");
+        cuda_check(launch_mlp_tc(map, h->d_wpacked.ptr, ni, H, n, nullptr, d_outputs, h->d_status.ptr, mlp_prec(h),
+                                 h->num_sms, s, true, h->wait_limit_ns, h->debug_stall),
+                   "tensor-core MLP");
         cuda_check(cudaEventRecord(h->ev1, s), "event");
-        h->last_launches = 1;
+        h->last_launches = 3;
+        uint32_t status = 0;
+        cuda_check(cudaMemcpyAsync(&status, h->d_status.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "status");
+        cuda_check(cudaStreamSynchronize(s), "sync");
+        require((status & 2u) == 0u, NBVH_EDEVICE, "tensor-core MLP: shared memory not 1,024-byte aligned");
+        require(status == 0u, NBVH_ETIMEOUT, "tensor-core MLP: a bounded wait gave up");
     });
 }
 

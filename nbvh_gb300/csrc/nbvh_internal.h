@@ -344,6 +344,7 @@ struct nbvh_handle {
     nbvh::DeviceBuffer<float> d_params;   // FP32 master
     nbvh::DeviceBuffer<__half> d_params_h; // 16-bit copy used by the kernels (MLP part FP16 or BF16, grid FP16)
     nbvh::DeviceBuffer<__half> d_wpacked;  // network matrices in the tensor-core operand layout
+    nbvh::DeviceBuffer<__half> d_infer_feat; // feature rows of nbvh_network_inference
     nbvh::DeviceBuffer<uint32_t> d_status; // error word of kernels with bounded waits
     nbvh::DeviceBuffer<float> d_adam_m, d_adam_v;
     nbvh::DeviceBuffer<float> d_grad;
@@ -546,9 +547,10 @@ cudaError_t launch_segments(const float4 *dilated_nodes, const float4 *bounds, c
                             const nbvh_ray *rays, uint32_t n, uint32_t max_segments, nbvh_segment *segs,
                             uint32_t *counts, cudaStream_t s);
 
-cudaError_t launch_network_inference(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
-                                     const float *positions, uint32_t n, float *outputs, uint32_t prec, int num_sms,
-                                     cudaStream_t s);
+// The FP16 (BF16 when bf16) hash-grid features of n rows of encoded positions into rows of
+// n_inputs values (the tcgen05 MLP's input layout).
+cudaError_t launch_encode_rows(const __half *params_h, const GridParams &grid, uint32_t n_hidden_layers,
+                               const float *positions, uint32_t n, __half *features, bool bf16, cudaStream_t s);
 
 // tcgen05 fully fused MLP (k_mlp_tc.cu): weights packed into the tensor-core operand layout, then
 // 128-row tiles of FP16 inputs (row-major [rows][n_inputs], 16-byte aligned) fed by TMA through

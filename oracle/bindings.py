@@ -417,6 +417,15 @@ class Oracle:
                                C.c_float(o.beta1), C.c_float(o.beta2), C.c_float(o.epsilon), C.c_float(o.l2_reg),
                                C.c_int32(o.decay_start), C.c_int32(o.decay_interval), C.c_float(o.decay_base))
 
+    def grid_layout(self, n_levels, log2_hashmap_size, base_resolution, per_level_scale):
+        """Level offsets, sizes, resolutions and position scales of the hash grid (tcnn's conventions)."""
+        off, size, res = (np.empty(n_levels, np.uint32) for _ in range(3))
+        scale = np.empty(n_levels, np.float32)
+        total = C.c_uint32(0)
+        self.lib.orc_grid_layout(C.c_uint32(n_levels), C.c_uint32(log2_hashmap_size), C.c_uint32(base_resolution),
+                                 C.c_float(per_level_scale), _p(off), _p(size), _p(res), _p(scale), C.byref(total))
+        return off, size, res, scale, total.value
+
     def path_trace(self, nscene, net, consts, req, sample_base=None, threads=1):
         """One path-traced frame of an nbvh_path_request (the library's k_path.cu restated): RGBA
         image [height * width, 4] and the rays traced. sample_base defaults to camera.sample_idx *

@@ -642,17 +642,18 @@ static inline float net_g(const orc_network *net, size_t i)
 /* Multiresolution hash grid (tcnn GridEncoding behaviour; Muller et al. 2022, Instant NGP)    */
 /* ------------------------------------------------------------------------------------------ */
 
-/* Level l: scale = base_resolution * per_level_scale^l - 1 (per_level_scale^l by repeated
- * double multiplication), resolution = ceil(scale) + 1, entries = min(roundup8(res^3), 2^log2T). */
+/* Level l (tcnn grid_scale): scale = exp2f(l * log2f(per_level_scale)) * base_resolution - 1 in
+ * single precision, resolution = ceil(scale) + 1, entries = min(roundup8(res^3), 2^log2T). */
 void orc_grid_layout(uint32_t n_levels, uint32_t log2_hashmap_size, uint32_t base_resolution,
                      float per_level_scale, uint32_t *offset, uint32_t *size, uint32_t *resolution,
                      float *scale, uint32_t *total_entries)
 {
     uint64_t off = 0;
-    double p = 1.0;
     uint64_t hashmap = 1ull << log2_hashmap_size;
+    const float log2_scale = log2f(per_level_scale);
     for (uint32_t l = 0; l < n_levels; l++) {
-        float s = (float)((double)base_resolution * p - 1.0);
+        const float grow = exp2f((float)l * log2_scale);
+        float s = grow * (float)base_resolution - 1.0f;
         uint32_t res = (uint32_t)ceilf(s) + 1u;
         uint64_t dense = (uint64_t)res * res * res;
         dense = (dense + 7u) & ~7ull;
@@ -662,7 +663,6 @@ void orc_grid_layout(uint32_t n_levels, uint32_t log2_hashmap_size, uint32_t bas
         resolution[l] = res;
         scale[l] = s;
         off += sz;
-        p *= (double)per_level_scale;
     }
     *total_entries = (uint32_t)off;
 }

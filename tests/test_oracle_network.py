@@ -229,3 +229,24 @@ def test_fp8_forward_matches_rounded_numpy(oracle, built):
     assert np.max(np.abs(out - ref)) < 1e-5
     out16 = oracle.network_inference(oracle.network(small_cfg(), L, p), pos)
     assert np.max(np.abs(out16 - out)) > 1e-3
+
+
+@pytest.mark.parametrize("levels,log2t,base,scale", [(16, 19, 16, (2048 / 16) ** (1 / 15)), (8, 18, 8, 2.0),
+                                                     (12, 17, 4, 1.5), (32, 22, 2, 1.26)])
+def test_grid_layout_follows_tcnn_and_matches_library(oracle, built, levels, log2t, base, scale):
+    """Level scale exp2f(l * log2f(s)) * base - 1 (tcnn's grid_scale), resolution ceil(scale) + 1,
+    entries min(roundup8(res^3), 2^log2T): the library's layout equals the oracle's bit for bit."""
+    cfg = nb.default_config(**{"hashgrid.n_levels": levels, "hashgrid.log2_hashmap_size": log2t,
+                               "hashgrid.base_resolution": base, "hashgrid.per_level_scale": scale,
+                               "module.input_segment_points": 1 if levels == 32 else 4})
+    if levels == 12:
+        cfg.module.input_segment_points = 2
+    L = nb.param_layout(cfg)
+    off, size, res, scl, total = oracle.grid_layout(levels, log2t, base, cfg.hashgrid.per_level_scale)
+    assert np.array_equal(np.array(L.level_scale[:levels], np.float32).view(np.uint32), scl.view(np.uint32))
+    assert list(L.level_resolution[:levels]) == list(res) and list(L.level_size[:levels]) == list(size)
+    assert list(L.level_offset[:levels]) == list(off) and L.n_grid_entries == total
+    lg = np.log2(np.float32(cfg.hashgrid.per_level_scale))
+    expect = (np.exp2(np.arange(levels, dtype=np.float64) * lg) * base - 1).astype(np.float32)
+    np.testing.assert_allclose(scl, expect, rtol=1e-6)
+    assert np.all(res == np.ceil(scl).astype(np.uint32) + 1)
