@@ -304,7 +304,7 @@ nbvh_status nbvh_write_nbvh_host(const char *path, const uint32_t *h_nodes, uint
 nbvh_status nbvh_set_non_neural_leaves(nbvh_handle *h, const uint32_t *h_node_ids, uint32_t n,
                                        int flag);
 nbvh_status nbvh_set_ignore_neural_blas(nbvh_handle *h, int ignore);
-/* Ray ordering (on by default; no counterpart in the reference): batches of 65,536 rays or more are
+/* Ray ordering (on by default; no counterpart in the reference): batches of 524,288 rays or more are
  * answered bin by bin, the bins being the direction octant x 8^3 cells of the ray origin over the
  * scene box grown by half its size on every side, so that the rays of a warp fetch the same nodes.
  * It changes no result, only the order in which the classic kernel and the neural query's first

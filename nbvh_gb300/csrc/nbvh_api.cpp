@@ -1149,6 +1149,7 @@ bool zero_copy_neural(nbvh_handle *h, const nbvh_ray *h_rays, uint32_t n, uint32
         t.late_count = h->d_late.ptr;
         t.late_list = h->d_late.ptr + 1;
         t.drain_taken = &taken;
+        t.ray_order_ok = false; // the first pass reads the rays over the host link: once, in order
         launches += run_neural_query(h, h->qctx[1], h->d_counters.ptr + 1, drays + c0, cnt, depth, false,
                                      h->d_drain_hits.ptr, s, &t);
         snapshot_stats(h, ci, 1, s);
@@ -2026,7 +2027,7 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
     res.outputs = q.outputs.ptr;
     res.wpacked = q.wpacked.ptr;
     res.perm = q.perm.ptr;
-    res.ray_keys = h->ray_ordering ? q.ray_keys.ptr : nullptr;
+    res.ray_keys = (h->ray_ordering && (!tune || tune->ray_order_ok)) ? q.ray_keys.ptr : nullptr;
     res.ray_bins = q.ray_bins.ptr;
     res.node_bins = q.node_bins.ptr;
     res.node_cursor = q.node_cursor.ptr;

@@ -437,9 +437,11 @@ inline cudaError_t allow_max_dynamic_smem(K kernel)
 // Coherence bins of the rays of a query (direction octant x 8^3 origin cells of the scene box
 // grown by half its size on every side): the first pass and the classic kernel take the rays bin
 // by bin, so that the rays of a warp start near one another in the same direction. Batches below
-// kRaySortMin rays are taken in batch order.
+// kRaySortMin rays are taken in batch order: the ordering's three launches (about 50 us) pay only
+// on larger batches (measured: 2^22 uniform rays, classic 1.49 -> 1.09 ms; a 389K-ray camera batch,
+// already coherent, 0.174 -> 0.213 ms).
 constexpr uint32_t kRayBins = 4096;
-constexpr uint32_t kRaySortMin = 1u << 16;
+constexpr uint32_t kRaySortMin = 1u << 19;
 
 // Cuts with more nodes than this are not sorted by node between steps (the sort scans the node
 // counts in shared memory).
@@ -494,6 +496,7 @@ struct StepResources {
     uint32_t n_sort_bins = 0;
     KernelProfile *prof = nullptr; // record encoder launch events (not under stream capture)
     uint64_t wait_ns = 0;          // time limit of the tensor-core kernels' phase waits (0: default)
+    bool ray_order_ok = true;      // false: rays in host memory read over the link, taken in batch order
     bool stall = false;            // failure-path tests: the MLP kernels wait on a barrier nothing arrives at
 };
 

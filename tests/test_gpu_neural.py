@@ -268,10 +268,10 @@ def test_kernel_profile_times_every_encoder_launch(scene):
 
 
 def test_ray_ordering_changes_no_result(scene):
-    """Batches of 2^16 rays or more are taken bin by bin (origin cell, direction octant); the records
+    """Batches of 2^19 rays or more are taken bin by bin (origin cell, direction octant); the records
     are the same as in batch order, word for word, for the neural and the classic queries."""
     h, s = scene
-    rays = _cuda(scenes.uniform_rays((1 << 17) + 77, s["bbox"][:3], s["bbox"][3:], seed=43))
+    rays = _cuda(scenes.uniform_rays((1 << 19) + 77, s["bbox"][:3], s["bbox"][3:], seed=43))
     a = as_u32(h.query_closest_neural(rays))
     c = as_u32(h.query_closest_classic(rays))
     h.set_ray_ordering(False)
