@@ -591,7 +591,10 @@ typedef struct nbvh_server_config {
     uint64_t hbm_budget_bytes; /* device memory all slots' buffers may take together (default 150 GiB) */
     uint32_t use_graphs;       /* replay captured CUDA graphs per batch-size bucket (default 1) */
     uint32_t autotune;         /* time the launch-parameter candidates per bucket (default 1) */
-    uint32_t reserved[8];
+    uint32_t query_slots;      /* of the n_slots, how many take query requests only, on streams of the
+                                  device's highest priority (default 0; must be < n_slots when renders
+                                  are submitted). Every slot takes pending query work before renders. */
+    uint32_t reserved[7];
 } nbvh_server_config;
 
 typedef enum nbvh_request_kind { NBVH_REQUEST_QUERY = 0, NBVH_REQUEST_RENDER = 1 } nbvh_request_kind;

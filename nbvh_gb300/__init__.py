@@ -716,11 +716,11 @@ class Server:
     alive until wait returns."""
 
     def __init__(self, n_slots=4, hbm_budget_gb=150.0, max_batch_rays=1 << 22, use_graphs=True, autotune=True,
-                 device=0):
+                 device=0, query_slots=0):
         self.lib = load_library()
         cfg = ServerConfig()
         _check(self.lib.nbvh_server_config_default(C.byref(cfg)), None)
-        cfg.n_slots, cfg.max_batch_rays = n_slots, max_batch_rays
+        cfg.n_slots, cfg.max_batch_rays, cfg.query_slots = n_slots, max_batch_rays, query_slots
         cfg.hbm_budget_bytes = int(hbm_budget_gb * (1 << 30))
         cfg.use_graphs, cfg.autotune = int(use_graphs), int(autotune)
         s = C.c_void_p()
@@ -739,9 +739,14 @@ class Server:
         self._check(self.lib.nbvh_server_add_model(self.s, handle.h, C.byref(mid)))
         return mid.value
 
-    def submit_query(self, model, rays_np, depth=1):
+    def submit_query(self, model, rays_np, depth=1, hits=None):
+        """`hits`: an optional caller-owned output array (len(rays) records of NEURAL_HIT_DTYPE, e.g. in
+        page-locked memory); a new array is made otherwise."""
         rays = np.ascontiguousarray(rays_np, np.float32).reshape(-1, 8)
-        hits = np.empty(len(rays), NEURAL_HIT_DTYPE)
+        if hits is None:
+            hits = np.empty(len(rays), NEURAL_HIT_DTYPE)
+        elif hits.dtype != NEURAL_HIT_DTYPE or hits.shape != (len(rays),) or not hits.flags.c_contiguous:
+            raise ValueError("hits must be a contiguous array of len(rays) NEURAL_HIT_DTYPE records")
         r = Request()
         r.kind, r.model, r.n_rays, r.depth = 0, model, len(rays), depth
         r.h_rays, r.h_hits = rays.ctypes.data, hits.ctypes.data

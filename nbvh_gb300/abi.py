@@ -109,7 +109,8 @@ class PathRequest(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("n_slots", C.c_uint32), ("max_batch_rays", C.c_uint32), ("hbm_budget_bytes", C.c_uint64),
-                ("use_graphs", C.c_uint32), ("autotune", C.c_uint32), ("reserved", C.c_uint32 * 8)]
+                ("use_graphs", C.c_uint32), ("autotune", C.c_uint32), ("query_slots", C.c_uint32),
+                ("reserved", C.c_uint32 * 7)]
 
 
 class Request(C.Structure):

@@ -5,10 +5,15 @@
 //  * Slots. n_slots worker threads, each with its own CUDA stream, query context, ray / hit /
 //    image buffers and path-tracing buffers, sized once from the HBM budget (admission: a request
 //    is admitted when a slot is free; a slot's share of the budget bounds what it holds).
-//  * Continuous batching. A free slot takes the oldest pending work; pending query requests for the
-//    same model and depth are merged into one batch up to the slot's capacity (larger requests are
-//    split into chunks, each a batch of its own). Requests that arrive while others run are taken
-//    by the next slot that frees up, so batches of different requests overlap on the device.
+//  * Continuous batching. A free slot takes the oldest pending query work, else the oldest pending
+//    render work; pending query requests for the same model and depth are merged into one batch up
+//    to the slot's capacity (larger requests are split into chunks, each a batch of its own).
+//    Requests that arrive while others run are taken by the next slot that frees up, so batches of
+//    different requests overlap on the device.
+//  * Query lane. query_slots of the slots take query requests only and launch on streams of the
+//    device's highest priority (the others on its lowest), so a latency-bound query batch neither
+//    waits for a slot behind long renders nor queues behind their kernels for SMs: the block
+//    scheduler starts its blocks first as resident ones finish.
 //  * Graphs. A query batch is padded to a power-of-two bucket; the first part of its query (the
 //    first-leaf pass and the first steps) is captured once per (slot, model, bucket) as a CUDA graph
 //    and replayed; the host then checks the list length and finishes any remaining steps directly.
@@ -57,6 +62,7 @@ struct Request {
     uint64_t rays_traced = 0;
     bool done = false;
     std::vector<float> accum; // render split over spp: summed chunk images
+    std::mutex accum_mu;      // guards accum (not the server's lock: summing an image takes a while)
 };
 
 struct Work {
@@ -74,6 +80,7 @@ struct GraphKey {
 
 struct Slot {
     cudaStream_t stream = nullptr;
+    bool query_only = false; // a slot of the query lane
     QueryContext q;
     DeviceBuffer<QueryCounters> counters;
     DeviceBuffer<nbvh_ray> rays;
@@ -130,6 +137,7 @@ struct nbvh_server {
     Clock::time_point first_submit, last_done;
     bool any_submit = false;
     nbvh_ray *dead = nullptr; // device buffer of padding rays (max bucket)
+    uint32_t idle_query_slots = 0; // query-lane slots waiting for work (guarded by mu)
 };
 
 namespace {
@@ -280,28 +288,35 @@ struct SlotPathQuery : PathQuery {
 
 void complete(nbvh_server *srv, const Work &w, nbvh_status st, uint64_t traced)
 {
-    std::lock_guard<std::mutex> lock(srv->mu);
     Request &r = *w.r;
-    if (st != NBVH_OK)
-        r.status = st;
-    r.rays_traced += traced;
-    srv->rays_traced += traced;
-    if (++r.chunks_done == r.chunks) {
-        if (r.req.kind == NBVH_REQUEST_RENDER && r.status == NBVH_OK && r.chunks > 1u) {
-            const uint32_t px = r.req.render.camera.width * r.req.render.camera.height;
-            const float inv = 1.0f / (float)r.req.render.spp;
-            for (size_t i = 0; i < (size_t)px * 4u; i++)
-                r.req.h_image[i] = (i % 4u == 3u) ? 1.0f : r.accum[i] * inv;
-            r.accum.clear();
-            r.accum.shrink_to_fit();
-        }
-        r.done = true;
-        r.done_at = Clock::now();
-        srv->last_done = r.done_at;
-        srv->requests_done++;
-        srv->latencies_ms.push_back(std::chrono::duration<double, std::milli>(r.done_at - r.submitted).count());
-        srv->cv_done.notify_all();
+    bool last;
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        if (st != NBVH_OK)
+            r.status = st;
+        r.rays_traced += traced;
+        srv->rays_traced += traced;
+        last = ++r.chunks_done == r.chunks;
     }
+    if (!last)
+        return;
+    // every chunk is done: nothing else touches the request's image until it is marked done, so the
+    // average is formed without the server's lock (which the slots need to take new work)
+    if (r.req.kind == NBVH_REQUEST_RENDER && r.status == NBVH_OK && r.chunks > 1u) {
+        const uint32_t px = r.req.render.camera.width * r.req.render.camera.height;
+        const float inv = 1.0f / (float)r.req.render.spp;
+        for (size_t i = 0; i < (size_t)px * 4u; i++)
+            r.req.h_image[i] = (i % 4u == 3u) ? 1.0f : r.accum[i] * inv;
+        r.accum.clear();
+        r.accum.shrink_to_fit();
+    }
+    std::lock_guard<std::mutex> lock(srv->mu);
+    r.done = true;
+    r.done_at = Clock::now();
+    srv->last_done = r.done_at;
+    srv->requests_done++;
+    srv->latencies_ms.push_back(std::chrono::duration<double, std::milli>(r.done_at - r.submitted).count());
+    srv->cv_done.notify_all();
 }
 
 void run_batch(nbvh_server *srv, Slot &sl, std::vector<Work> &batch)
@@ -345,8 +360,8 @@ void run_batch(nbvh_server *srv, Slot &sl, std::vector<Work> &batch)
                 std::vector<float> img((size_t)px * 4u);
                 cuda_check(cudaMemcpy(img.data(), sl.image.ptr, img.size() * sizeof(float), cudaMemcpyDeviceToHost),
                            "image out");
-                std::lock_guard<std::mutex> lock(srv->mu);
                 Request &r = *w.r;
+                std::lock_guard<std::mutex> lock(r.accum_mu);
                 for (size_t i = 0; i < img.size(); i++)
                     r.accum[i] += img[i] * (float)w.count; // chunk mean x chunk samples
             }
@@ -367,6 +382,24 @@ void run_batch(nbvh_server *srv, Slot &sl, std::vector<Work> &batch)
     }
 }
 
+// The pending work a slot takes next: the oldest query work, else (for a slot outside the query
+// lane) the oldest work of any kind; end() when there is none for it. While a slot of the query lane
+// is idle, the other slots leave query work to it (it runs at the higher stream priority).
+std::deque<Work>::iterator next_work(nbvh_server *srv, const Slot &sl)
+{
+    const bool take_queries = sl.query_only || srv->idle_query_slots == 0u;
+    std::deque<Work>::iterator first_render = srv->pending.end();
+    for (auto it = srv->pending.begin(); it != srv->pending.end(); ++it) {
+        if (it->r->req.kind == NBVH_REQUEST_QUERY) {
+            if (take_queries)
+                return it;
+        } else if (first_render == srv->pending.end()) {
+            first_render = it;
+        }
+    }
+    return sl.query_only ? srv->pending.end() : first_render;
+}
+
 void slot_loop(nbvh_server *srv, Slot *sl)
 {
     cudaSetDevice(srv->device);
@@ -374,11 +407,18 @@ void slot_loop(nbvh_server *srv, Slot *sl)
         std::vector<Work> batch;
         {
             std::unique_lock<std::mutex> lock(srv->mu);
-            srv->cv_work.wait(lock, [&] { return srv->stop || !srv->pending.empty(); });
-            if (srv->stop && srv->pending.empty())
-                return;
-            Work first = srv->pending.front();
-            srv->pending.pop_front();
+            if (sl->query_only)
+                srv->idle_query_slots++;
+            srv->cv_work.wait(lock, [&] { return srv->stop || next_work(srv, *sl) != srv->pending.end(); });
+            if (sl->query_only)
+                srv->idle_query_slots--;
+            const auto pick = next_work(srv, *sl);
+            if (pick == srv->pending.end())
+                return; // stopping, and nothing left that this slot takes
+            Work first = *pick;
+            srv->pending.erase(pick);
+            if (sl->query_only && !srv->pending.empty())
+                srv->cv_work.notify_all(); // the lane is busy now: the other slots may take queries
             if (first.r->chunks_done == 0 && first.offset == 0)
                 first.r->started = Clock::now();
             batch.push_back(first);
@@ -480,12 +520,14 @@ nbvh_status nbvh_server_config_default(nbvh_server_config *cfg)
     cfg->hbm_budget_bytes = 150ull << 30;
     cfg->use_graphs = 1;
     cfg->autotune = 1;
+    cfg->query_slots = 0;
     return NBVH_OK;
 }
 
 nbvh_status nbvh_server_create(const nbvh_server_config *cfg, int device, nbvh_server **out)
 {
-    if (!cfg || !out || cfg->n_slots == 0 || cfg->n_slots > 64 || cfg->max_batch_rays < kMinBucket)
+    if (!cfg || !out || cfg->n_slots == 0 || cfg->n_slots > 64 || cfg->max_batch_rays < kMinBucket ||
+        cfg->query_slots >= cfg->n_slots)
         return NBVH_EINVAL;
     auto *srv = new (std::nothrow) nbvh_server();
     if (!srv)
@@ -502,6 +544,8 @@ nbvh_status nbvh_server_create(const nbvh_server_config *cfg, int device, nbvh_s
             pow2 <<= 1;
         require(cap >= kMinBucket, NBVH_EINVAL, "HBM budget too small for one minimal batch per slot");
         cap = pow2;
+        int least_priority = 0, greatest_priority = 0; // numerically lower = higher priority
+        cuda_check(cudaDeviceGetStreamPriorityRange(&least_priority, &greatest_priority), "stream priorities");
         std::vector<nbvh_ray> dead(cap);
         fill_dead_rays(dead.data(), cap);
         cuda_check(cudaMalloc(&srv->dead, (size_t)cap * sizeof(nbvh_ray)), "alloc padding rays");
@@ -509,7 +553,9 @@ nbvh_status nbvh_server_create(const nbvh_server_config *cfg, int device, nbvh_s
         for (uint32_t i = 0; i < cfg->n_slots; i++) {
             auto sl = std::make_unique<Slot>();
             sl->capacity = cap;
-            cuda_check(cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking), "stream");
+            sl->query_only = i < cfg->query_slots;
+            const int priority = cfg->query_slots == 0 ? 0 : sl->query_only ? greatest_priority : least_priority;
+            cuda_check(cudaStreamCreateWithPriority(&sl->stream, cudaStreamNonBlocking, priority), "stream");
             cuda_check(sl->counters.resize(1u), "alloc counters");
             cuda_check(sl->rays.resize(cap), "alloc slot rays");
             cuda_check(sl->hits.resize(cap), "alloc slot hits");

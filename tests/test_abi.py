@@ -115,3 +115,13 @@ def test_create_without_device_reports_edevice(built):
     with pytest.raises(nb.NBVHError) as e:
         nb.NBVH(nb.default_config())
     assert e.value.status == abi.NBVH_EDEVICE
+
+
+def test_server_config_checked_before_the_device(built):
+    """A query lane must leave at least one slot for renders; the configuration is refused with
+    EINVAL before any device call (so this runs without a GPU)."""
+    for n_slots, q in ((2, 2), (1, 1), (3, 5)):
+        with pytest.raises(nb.NBVHError) as e:
+            nb.Server(n_slots=n_slots, query_slots=q)
+        assert e.value.status == abi.NBVH_EINVAL
+    assert C.sizeof(abi.ServerConfig) == 56

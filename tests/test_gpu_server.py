@@ -7,6 +7,8 @@
 * A render request equals nbvh_render_path alone; when its samples are split across batches the
   image equals the unsplit one up to float summation order (relative 1e-5).
 * The server reports request latency percentiles and merged batches.
+* A query-lane slot (queries only, highest stream priority) answers queries submitted beside
+  renders with the same hits.
 """
 
 import threading
@@ -103,6 +105,41 @@ def test_render_same_alone_and_split(models):
         img, res = srv.wait(srv.submit_render(mid, req))
         assert res.status == 0 and res.rays_traced == traced
         np.testing.assert_allclose(img, alone, rtol=1e-5, atol=1e-6)
+    finally:
+        srv.close()
+
+
+def test_query_lane_same_results_beside_renders(models):
+    """A server with one query-lane slot (highest stream priority, queries only) and two render
+    slots: query hits submitted while renders run equal the handle's own, page-locked caller-owned
+    hit buffers included, and every render equals nbvh_render_path alone."""
+    import torch
+    h, s = models[0]
+    reqs = _requests(models, seed=5)[:8]
+    alone = [models[m][0].query_closest_neural_host(r, depth=d) for m, r, d in reqs]
+    org, tgt, up = scenes.orbit_camera(s["bbox"][:3], s["bbox"][3:], seed=11)
+    cam = nb.render_request(96, 64, org, tgt, up, 45.0, sample_idx=3)
+    preq = nb.path_request(cam, spp=2, max_bounces=2, seed=8, ground_height=float(s["bbox"][1]) - 0.01)
+    ref_img, ref_traced = h.render_path(preq)
+    ref_img = ref_img.cpu().numpy()
+    srv = nb.Server(n_slots=3, query_slots=1, hbm_budget_gb=0.3, max_batch_rays=1 << 16)
+    try:
+        ids = [srv.add_model(hh) for hh, _ in models]
+        renders = [srv.submit_render(ids[0], preq) for _ in range(6)]
+        tickets = []
+        for i, (m, r, d) in enumerate(reqs):
+            out = None
+            if i % 2 == 0:  # caller-owned page-locked output
+                out = torch.empty(len(r) * 12, dtype=torch.int32).pin_memory().numpy().view(nb.NEURAL_HIT_DTYPE)
+            tickets.append(srv.submit_query(ids[m], r, d, hits=out))
+        for i, t in enumerate(tickets):
+            hits, res = srv.wait(t)
+            assert res.status == 0
+            assert np.array_equal(hits.view(np.uint32), alone[i].view(np.uint32)), i
+        for t in renders:
+            img, res = srv.wait(t)
+            assert res.status == 0 and res.rays_traced == ref_traced
+            np.testing.assert_array_equal(img, ref_img)
     finally:
         srv.close()
 
