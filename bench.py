@@ -75,6 +75,9 @@ def parse():
     ap.add_argument("--serve-train-steps", type=int, default=1500)
     ap.add_argument("--scene-train-steps", type=int, default=2000,
                     help="training steps per model of the instanced config-4 scene (-1 skips it)")
+    ap.add_argument("--reference-default-steps", type=int, default=5000,
+                    help="training steps of the reference's default grid (8 levels x 4 features x 2^18, 3 points) "
+                         "on the headline scene before its query is timed (-1 skips it)")
     ap.add_argument("--learned-cut-steps", type=int, default=4000,
                     help="training steps of the fixed-cut vs learned-cut comparison (-1 skips it)")
     ap.add_argument("--log2-rays", type=int, default=22,
@@ -576,6 +579,8 @@ def run_ours(args):
         line["train_roofline"] = run_train_roofline(nb, scenes, peaks)
     if args.precision_sweep_steps > 0:
         line["precision_sweep"] = run_precision_sweep(args, nb, scenes, args.precision_sweep_steps)
+    if rank == 0 and args.reference_default_steps >= 0:
+        line["config_reference_default"] = run_reference_default(args, nb, scenes, args.reference_default_steps)
     if rank == 0 and args.learned_cut_steps >= 0:
         line["learned_cut"] = run_learned_cut(args, nb, scenes, args.learned_cut_steps)
     if rank == 0 and args.scene_train_steps >= 0:
@@ -609,7 +614,10 @@ def summary_of(line):
             "serving_1m_batch_p99_ms": r(b1m.get("p99_ms"), 2), "serving_1m_batch_p50_ms": r(b1m.get("p50_ms"), 2),
             "train_ms_per_step": r(line.get("train_roofline", {}).get("ms_per_step"), 3),
             "train_mlp_tc_frac": r(line.get("train_roofline", {}).get("mlp_tc", {}).get("frac"), 3),
-            "mlp_tc_frac": r(line.get("roofline_kernels", {}).get("mlp_tc", {}).get("frac"), 3)}
+            "mlp_tc_frac": r(line.get("roofline_kernels", {}).get("mlp_tc", {}).get("frac"), 3),
+            "e2e_mrays": r(line.get("e2e", {}).get("value")),
+            "refdefault_f4_mrays": r(line.get("config_reference_default", {}).get("query_mrays")),
+            "refdefault_f4_vis_agree": r(line.get("config_reference_default", {}).get("visibility_agreement"), 4)}
 
 
 def run_classic_config1(h, v, f, bbox, scenes, steps, warmup, cpu_sample):
@@ -859,6 +867,40 @@ def run_serving(args, nb, scenes):
         srv.close()
         for m in models:
             m[0].close()
+    return out
+
+
+def run_reference_default(args, nb, scenes, steps):
+    """The reference's own default encoding (include/cuda/neural/utils/tcnn_config.h:70-74: hash grid
+    of 8 levels x 4 FP16 features x 2^18 entries, base resolution 8, level scale 2; 3 points per
+    segment, 96 network inputs) on the headline scene and cut (65,536 triangles, depth-10 cut):
+    `steps` training steps of 2^18 rays, then the neural and classic queries timed on the headline's
+    2^22 rays and compared (visibility agreement, depth error). The reference default also learns
+    its cut from the root; here the cut is the headline's fixed one, so that only the encoding
+    differs from the headline."""
+    import torch
+    cfg = nb.reference_default_config()
+    cfg.neural_bvh_max_depth = CUT_DEPTH
+    h, v, f, _ = build_scene(nb, scenes, cfg)
+    _, bbox = h.neural_bvh()
+    t0 = time.perf_counter()
+    st = h.run_optimisation(steps)
+    train_s = time.perf_counter() - t0
+    rays = torch.from_numpy(scenes.uniform_rays(N_RAYS, bbox[:3], bbox[3:], seed=2)).cuda()
+    hits = torch.empty((N_RAYS, 12), dtype=torch.int32, device="cuda")
+    chits = torch.empty((N_RAYS, 4), dtype=torch.int32, device="cuda")
+    times, ctimes, _, _ = time_queries(h, rays, hits, chits, 5, 3, "reference_default")
+    vis, depth, segs = accuracy(hits, chits)
+    L = nb.param_layout(cfg)
+    out = {"grid": "8 levels x 4 FP16 features x 2^18, res 8-1024 (scale 2)", "points_per_segment": 3,
+           "network_inputs": 96, "params": int(L.n_params), "cut": "fixed depth 10 (1,024 leaves)",
+           "train_steps": steps, "train_ms_per_step": st.ms_per_step, "train_seconds": train_s,
+           "last_loss": st.last_loss, "rays": N_RAYS, "query_ms": float(times.mean()),
+           "query_mrays": N_RAYS / (float(times.mean()) * 1e-3) / 1e6,
+           "classic_mrays": N_RAYS / (float(ctimes.mean()) * 1e-3) / 1e6,
+           "visibility_agreement": vis, "depth_error": depth, "segments_per_ray": segs}
+    out["neural_over_classic"] = out["query_mrays"] / out["classic_mrays"]
+    h.close()
     return out
 
 

@@ -76,9 +76,7 @@ def reference_default_config():
     where they differ: hash grid of 8 levels x 4 features x 2^18 entries, base resolution 8, level
     scale 2.0 (include/cuda/neural/utils/tcnn_config.h:70-74), 3 segment points
     (include/cuda/neural/neural_bvh_module.h:81) and a neural cut from the root
-    (m_neural_bvh_min_depth = 0, include/cuda/neural/neural_bvh_renderer.h:206). Note that 4
-    features per level is not supported by this library's kernels (n_features_per_level must be 2):
-    a handle created from such a config fails with NBVH_EINVAL."""
+    (m_neural_bvh_min_depth = 0, include/cuda/neural/neural_bvh_renderer.h:206)."""
     cfg = default_config()
     cfg.hashgrid.n_levels = 8
     cfg.hashgrid.n_features_per_level = 4
