@@ -722,10 +722,12 @@ nbvh_status nbvh_debug_alloc_count(uint64_t *out);
  * library's device code is loaded.
  *  - n must be at most NBVH_NOALLOC_MAX_RAYS; a larger n returns NBVH_EINVAL and launches nothing.
  *    Split larger batches into several calls.
+ *  - The call cannot be captured into a CUDA graph: it reads the list lengths back to the host
+ *    between steps and synchronises its stream before it returns.
  *  - The first call on each device, with that device current, looks up the buffer's device
- *    address once (setup) and keeps it for the life of the process. Make that first call (n = 0
- *    is enough) before any stream capture. Do not use the library across a reset of the device
- *    (cudaDeviceReset), which may move the buffer.
+ *    address once (setup) and keeps it for the life of the process; a first call with n = 0 does
+ *    only that, so a caller can take the setup's latency before its first frame. Do not use the
+ *    library across a reset of the device (cudaDeviceReset), which may move the buffer.
  *  - Each call zeroes the counters it uses before its first kernel; nothing relies on the buffer's
  *    contents from an earlier call.
  *  - There is one buffer per device, shared by every handle on it. Calls that overlap in time on
