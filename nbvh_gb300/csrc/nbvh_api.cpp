@@ -465,6 +465,20 @@ void neural_query(nbvh_handle *h, const nbvh_ray *d_rays, uint32_t n, uint32_t d
 {
     require(h->classic_built, NBVH_ESTATE, "classic BVH not built");
     require(h->neural_built, NBVH_ESTATE, "neural cut not built");
+    if (n == 0) { // nothing to launch; the statistics of this call are all zero
+        if (h->d_counters.count < 3u)
+            cuda_check(h->d_counters.resize(3u), "alloc counters");
+        cuda_check(cudaMemsetAsync(h->d_counters.ptr + ctx, 0, sizeof(QueryCounters), s), "reset counters");
+        if (timed) {
+            cuda_check(cudaEventRecord(h->ev0, s), "event");
+            cuda_check(cudaEventRecord(h->ev1, s), "event");
+            h->n_stat_chunks = 0;
+            h->stat_ctx_mask = 1u << ctx;
+        }
+        h->last_launches = 0;
+        h->last_rays = 0;
+        return;
+    }
     ensure_query_workspace(h, n, ctx);
     if (timed)
         cuda_check(cudaEventRecord(h->ev0, s), "event");
