@@ -358,6 +358,16 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 
 } // namespace
 
+cudaError_t configure_mlp_tc()
+{
+    cudaError_t e = allow_max_dynamic_smem(k_mlp_tc<false, false>);
+    if (e == cudaSuccess)
+        e = allow_max_dynamic_smem(k_mlp_tc<true, false>);
+    if (e == cudaSuccess)
+        e = allow_max_dynamic_smem(k_mlp_tc<false, true>);
+    return e;
+}
+
 uint32_t packed_weight_bytes(uint32_t n_inputs, uint32_t n_hidden_layers)
 {
     return w0_bytes(n_inputs) + (n_hidden_layers - 1u) * hidden_w_bytes() + out_w_bytes();

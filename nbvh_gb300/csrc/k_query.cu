@@ -1360,6 +1360,20 @@ cudaError_t launch_ray_order(const nbvh_ray *rays, uint32_t n, const float scene
     return cudaGetLastError();
 }
 
+cudaError_t configure_query_kernels()
+{
+    const cudaError_t es[] = {
+        allow_max_dynamic_smem(k_wave_decode<true>),          allow_max_dynamic_smem(k_wave_decode<false>),
+        allow_max_dynamic_smem(k_wave_tail<true, false, false>), allow_max_dynamic_smem(k_wave_tail<false, false, false>),
+        allow_max_dynamic_smem(k_wave_tail<true, true, false>),  allow_max_dynamic_smem(k_wave_tail<false, true, false>),
+        allow_max_dynamic_smem(k_wave_tail<true, false, true>),  allow_max_dynamic_smem(k_wave_tail<false, false, true>),
+        configure_mlp_tc()};
+    for (cudaError_t e : es)
+        if (e != cudaSuccess)
+            return e;
+    return cudaSuccess;
+}
+
 cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds, uint32_t n_cut_nodes,
                               const uint8_t *non_neural, const __half *params_h, const GridParams &grid,
                               const NeuralConsts &nc, uint32_t n_hidden_layers, const nbvh_ray *rays, uint32_t n,
@@ -1408,8 +1422,9 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     a.late_count = res.late_count;
     a.late_from = res.drain_host ? res.drain_step + 1u : 0xFFFFFFFFu;
     const size_t smem_cut = (size_t)n_cut_nodes * 56u;
+    const bool use_smem_cut = smem_cut <= kSmemLimit;
     if (res.resume_from > 0u) // continue a query whose first steps ran from a captured graph
-        return smem_cut <= kSmemLimit
+        return use_smem_cut
                    ? run_steps<true>(a, res, smem_cut, num_sms, nc.max_traversal_steps, res.resume_from, s, *launches)
                    : run_steps<false>(a, res, 0, num_sms, nc.max_traversal_steps, res.resume_from, s, *launches);
     // words 0-2: rotating list lengths; 3: the MLP's error word; 4-6: rotating work counters of
@@ -1447,7 +1462,7 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
-    if (smem_cut <= kSmemLimit)
+    if (use_smem_cut)
         return run_steps<true>(a, res, smem_cut, num_sms, nc.max_traversal_steps, 0u, s, *launches);
     return run_steps<false>(a, res, 0, num_sms, nc.max_traversal_steps, 0u, s, *launches);
 }

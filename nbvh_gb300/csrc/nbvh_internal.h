@@ -541,6 +541,11 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
                               const WaveList lists[2], uint32_t *wave_counts, const StepResources &res, uint32_t prec,
                               int num_sms, cudaStream_t s, uint32_t *launches);
 
+// Sets the shared-memory attributes of every variant of the query's kernels with dynamic shared
+// memory (decode, tail, tensor-core MLP) on the current device. A direct query sets those of the
+// variants it launches; a stream capture cannot, so the serving loop calls this before capturing.
+cudaError_t configure_query_kernels();
+
 // order[0..n) = the ray ids bin by bin (coherence bins over the scene box, kRayBins of them);
 // keys: n, bins: kRayBins device words of scratch. Three kernels and a memset on the stream.
 cudaError_t launch_ray_order(const nbvh_ray *rays, uint32_t n, const float scene_min[3], const float scene_max[3],
@@ -570,6 +575,8 @@ cudaError_t make_feature_map(const __half *features, uint32_t n_inputs, uint32_t
                              bool allow_swizzle = true);
 // wait_ns: time limit of the kernel's phase waits (0: the default of one second). stall (failure-path
 // tests): one wait on an mbarrier that nothing arrives at, which runs out after wait_ns.
+// MaxDynamicSharedMemorySize of the tensor-core MLP's variants (FP16, BF16, FP8) on the current device.
+cudaError_t configure_mlp_tc();
 cudaError_t launch_mlp_tc(const TensorMapBytes &feature_map, const __half *wpacked, uint32_t n_inputs,
                           uint32_t n_hidden_layers, uint32_t rows, const uint32_t *d_count, float *outputs,
                           uint32_t *status, uint32_t prec, int num_sms, cudaStream_t s, bool configure = true,

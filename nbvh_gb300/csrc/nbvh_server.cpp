@@ -13,7 +13,9 @@
 //  * Query lane. query_slots of the slots take query requests only and launch on streams of the
 //    device's highest priority (the others on its lowest), so a latency-bound query batch neither
 //    waits for a slot behind long renders nor queues behind their kernels for SMs: the block
-//    scheduler starts its blocks first as resident ones finish.
+//    scheduler starts its blocks first as resident ones finish. While the lane runs a batch, the
+//    render slots hold back their next bounce query (for at most kYieldMs), so the lane's kernels
+//    meet only the render work already on the device.
 //  * Graphs. A query batch is padded to a power-of-two bucket; the first part of its query (the
 //    first-leaf pass and the first steps) is captured once per (slot, model, bucket) as a CUDA graph
 //    and replayed; the host then checks the list length and finishes any remaining steps directly.
@@ -43,6 +45,7 @@ using Clock = std::chrono::steady_clock;
 constexpr uint32_t kMinBucket = 1u << 12;
 constexpr uint32_t kGraphSteps = 8;          // steps inside the captured graph
 constexpr uint64_t kBytesPerRay = 1024;      // query + path buffers per ray of slot capacity (upper bound)
+constexpr int kYieldMs = 20;                 // longest a render bounce waits for the query lane
 
 struct Tuning {
     uint32_t visits = 0, encode_blocks = 0;
@@ -138,6 +141,10 @@ struct nbvh_server {
     bool any_submit = false;
     nbvh_ray *dead = nullptr; // device buffer of padding rays (max bucket)
     uint32_t idle_query_slots = 0; // query-lane slots waiting for work (guarded by mu)
+    // query-lane batches on the device; render bounces wait for 0 (guarded by lane_mu)
+    std::mutex lane_mu;
+    std::condition_variable lane_cv;
+    uint32_t lane_busy = 0;
 };
 
 namespace {
@@ -182,8 +189,8 @@ StepResources tuning_of(const Model &m, uint32_t bucket)
 
 // Captures (once) the graph of a padded batch of `bucket` rays in the slot's buffers: the first-leaf
 // pass and the first kGraphSteps steps, ending with a copy of the wave counters to the host. Nothing
-// runs; the kernels' attributes must have been set by an earlier direct query. A shape whose
-// capture fails is recorded without a graph and keeps running directly.
+// runs; the kernels' attributes are set beforehand (a captured launch cannot set them). A shape
+// whose capture fails is recorded without a graph and keeps running directly.
 cudaGraphExec_t ensure_graph(nbvh_server *srv, Slot &sl, uint32_t model_id, uint32_t bucket, uint32_t depth)
 {
     const GraphKey key{model_id, bucket, depth};
@@ -195,6 +202,8 @@ cudaGraphExec_t ensure_graph(nbvh_server *srv, Slot &sl, uint32_t model_id, uint
     cap.unchecked_steps = kGraphSteps;
     cap.capture_only = true;
     cudaGraphExec_t exec = nullptr;
+    // the captured launches cannot set kernel attributes: set those of every variant first
+    cuda_check(configure_query_kernels(), "kernel attributes");
     if (cudaStreamBeginCapture(sl.stream, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
         bool ok = true;
         try {
@@ -278,6 +287,10 @@ struct SlotPathQuery : PathQuery {
     SlotPathQuery(nbvh_server *s, Slot *l, uint32_t m) : srv(s), sl(l), model(m) {}
     const nbvh_neural_hit *operator()(const nbvh_ray *rays, uint32_t n, uint32_t depth) override
     {
+        if (srv->cfg.query_slots > 0u && !sl->query_only) { // yield to a query-lane batch in flight
+            std::unique_lock<std::mutex> lock(srv->lane_mu);
+            srv->lane_cv.wait_for(lock, std::chrono::milliseconds(kYieldMs), [&] { return srv->lane_busy == 0u; });
+        }
         cuda_check(cudaMemcpyAsync(sl->rays.ptr, rays, (size_t)n * sizeof(nbvh_ray), cudaMemcpyDeviceToDevice,
                                    sl->stream),
                    "bounce rays");
@@ -319,9 +332,33 @@ void complete(nbvh_server *srv, const Work &w, nbvh_status st, uint64_t traced)
     srv->cv_done.notify_all();
 }
 
+// Marks a query-lane batch as on the device for its lifetime (render bounces wait meanwhile).
+struct LaneBusy {
+    nbvh_server *srv;
+    bool on;
+    LaneBusy(nbvh_server *s, bool lane) : srv(s), on(lane)
+    {
+        if (on) {
+            std::lock_guard<std::mutex> lock(srv->lane_mu);
+            srv->lane_busy++;
+        }
+    }
+    ~LaneBusy()
+    {
+        if (on) {
+            {
+                std::lock_guard<std::mutex> lock(srv->lane_mu);
+                srv->lane_busy--;
+            }
+            srv->lane_cv.notify_all();
+        }
+    }
+};
+
 void run_batch(nbvh_server *srv, Slot &sl, std::vector<Work> &batch)
 {
     const nbvh_request &q0 = batch[0].r->req;
+    const LaneBusy busy(srv, sl.query_only && q0.kind == NBVH_REQUEST_QUERY);
     try {
         cuda_check(cudaSetDevice(srv->device), "cudaSetDevice");
         if (q0.kind == NBVH_REQUEST_QUERY) {
