@@ -353,15 +353,17 @@ def run_reference(args):
     rays = scenes.uniform_rays(N_RAYS, bbox[:3], bbox[3:], seed=2024)
     sample = rays[:args.cpu_sample]
     orc = Oracle()
-    # the level scales as this machine's C library computes them (tcnn's exp2f / log2f formula), the
-    # same the GPU arm's library computes here; the committed offsets and sizes must agree
+    # the committed layout holds the level scales the GPU arm's handle encodes with (tcnn's
+    # exp2f(l * log2f(s)) * base - 1 evaluated on the device); the oracle's own host evaluation must
+    # give the same offsets, sizes and resolutions and scales within 2 ulp (CUDA's exp2f bound)
     hg = cfg.hashgrid
     off, size, res, scale, total = orc.grid_layout(hg.n_levels, hg.log2_hashmap_size, hg.base_resolution,
                                                    hg.per_level_scale)
-    assert list(off) == list(layout.level_offset[:hg.n_levels]) and list(size) == list(layout.level_size[:hg.n_levels])
-    for l in range(hg.n_levels):
-        layout.level_scale[l] = float(scale[l])
-        layout.level_resolution[l] = int(res[l])
+    nl = hg.n_levels
+    assert list(off) == list(layout.level_offset[:nl]) and list(size) == list(layout.level_size[:nl])
+    assert list(res) == list(layout.level_resolution[:nl])
+    committed = np.array(layout.level_scale[:nl], np.float32)
+    assert np.abs(committed.view(np.int32).astype(np.int64) - np.asarray(scale, np.float32).view(np.int32)).max() <= 2
     net = orc.network(cfg, layout, params)
     consts = orc.neural_consts(cfg)
     nscene = orc.neural_scene(nn, bbox)

@@ -703,11 +703,16 @@ nbvh_status nbvh_last_kernel_profile(nbvh_handle *h, nbvh_kernel_profile *out);
  * nbvh_debug_fail_allocations: every device allocation the library makes after the next `after`
  * ones fails as if the device were out of memory (the call reports NBVH_ENOMEM); a negative value
  * switches this off. Process-wide.
- * nbvh_debug_alloc_count: device allocations the library has made so far (process-wide). */
+ * nbvh_debug_alloc_count: device allocations the library has made so far (process-wide).
+ * nbvh_debug_device_level_scales: the configuration's hash-grid level scales (n_levels values)
+ * evaluated on `device` the way tcnn's encoding kernels do, exp2f(l * log2f(per_level_scale)) *
+ * base_resolution - 1 with CUDA's exp2f; the library itself takes them from the host's exp2f
+ * (nbvh_get_param_layout, level_scale), so that a layout needs no GPU. A test compares the two. */
 nbvh_status nbvh_debug_set_wait_limit(nbvh_handle *h, uint64_t ns);
 nbvh_status nbvh_debug_inject_stall(nbvh_handle *h, int enable);
 nbvh_status nbvh_debug_fail_allocations(int64_t after);
 nbvh_status nbvh_debug_alloc_count(uint64_t *out);
+nbvh_status nbvh_debug_device_level_scales(const nbvh_config *cfg, int device, float *out);
 
 /* ---------------------------------------------------------------------------------------------
  * Allocation-free neural query. This entry point has no counterpart in the reference.

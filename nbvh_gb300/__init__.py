@@ -184,6 +184,15 @@ def param_layout(cfg):
     return L
 
 
+def device_level_scales(cfg, device=0):
+    """The hash-grid level scales evaluated on the GPU the way tcnn's kernels do (CUDA's exp2f),
+    for comparison with param_layout(cfg).level_scale (the host's exp2f)."""
+    n = int(cfg.hashgrid.n_levels)
+    out = (C.c_float * 32)()
+    _check(load_library().nbvh_debug_device_level_scales(C.byref(cfg), device, out), None)
+    return np.array(out[:n], np.float32)
+
+
 def init_params(cfg):
     L = param_layout(cfg)
     p = np.empty(L.n_params, np.float32)

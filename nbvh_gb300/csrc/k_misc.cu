@@ -1,4 +1,5 @@
-// k_misc.cu -- pinhole camera ray generation for run-inference.
+// k_misc.cu -- pinhole camera ray generation for run-inference, and the hash-grid level scales
+// as the GPU evaluates them (a check of the host's values).
 //
 // camera_raygen (include/cuda/neural/neural_bvh_renderer_kernels.cuh:74-79) with the pixel jitter of
 // camera_raygen_and_intersect_neural_bvh (include/cuda/neural/neural_bvh_module_common.cuh:222-228):
@@ -36,7 +37,25 @@ __global__ void __launch_bounds__(256) k_camera_rays(const __grid_constant__ Cam
     out[1] = make_float4(d.x, d.y, d.z, FLT_MAX);
 }
 
+// tcnn's grid_scale evaluated on the device, as tcnn's encoding kernels do:
+// exp2f(level * log2_per_level_scale) * base_resolution - 1 (nvcc contracts the multiply and the
+// subtraction into one FMA by default; written out here as that FMA).
+__global__ void k_level_scales(float log2_scale, float base, uint32_t n, float *out)
+{
+    const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l < n)
+        out[l] = __fmaf_rn(exp2f(__fmul_rn((float)l, log2_scale)), base, -1.0f);
+}
+
 } // namespace
+
+cudaError_t launch_level_scales(float log2_scale, float base, uint32_t n, float *out, cudaStream_t s)
+{
+    if (n == 0)
+        return cudaSuccess;
+    k_level_scales<<<1, 32, 0, s>>>(log2_scale, base, n, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_camera_rays(uint32_t width, uint32_t height, uint32_t sample_idx, uint32_t sample_offset,
                                const float *origin, const float *du, const float *dv, const float *top_left,

@@ -137,8 +137,33 @@ void validate_config(const nbvh_config &c)
 }
 
 // Grid geometry (tcnn's GridEncoding conventions): scale_l = exp2f(l * log2f(per_level_scale)) *
-// base - 1 in single precision, the C library's exp2f and log2f called as tcnn's grid_scale does;
-// res = ceil(scale) + 1; entries = min(roundup8(res^3), 2^log2T).
+// base - 1 in single precision, here with the host C library's exp2f and log2f (a layout needs no
+// GPU; a handle then takes its device's values, apply_device_level_scales); res = ceil(scale) + 1;
+// entries = min(roundup8(res^3), 2^log2T).
+void compute_layout(const nbvh_config &c, nbvh_param_layout &L, GridParams &g);
+
+// tcnn evaluates grid_scale inside its encoding kernels, with CUDA's exp2f, which differs from the
+// host C library's by an ulp for some arguments (5 of the 16 levels of the benchmark's grid). A
+// handle encodes with its device's values, the ones tcnn would use; a level whose resolution the
+// device value would change (a scale within an ulp of an integer) keeps the host value, so that the
+// layout stays the one nbvh_param_layout_host reports.
+void apply_device_level_scales(const nbvh_config &c, nbvh_param_layout &L, GridParams &g)
+{
+    const uint32_t n = L.n_levels;
+    DeviceBuffer<float> d;
+    cuda_check(d.resize(32u), "alloc level scales");
+    const float log2_scale = std::log2(c.hashgrid.per_level_scale);
+    cuda_check(launch_level_scales(log2_scale, (float)c.hashgrid.base_resolution, n, d.ptr, nullptr), "level scales");
+    float s[32];
+    cuda_check(cudaMemcpy(s, d.ptr, n * sizeof(float), cudaMemcpyDeviceToHost), "level scales");
+    for (uint32_t l = 0; l < n; l++) {
+        if ((uint32_t)std::ceil(s[l]) + 1u == g.res[l]) {
+            g.scale[l] = s[l];
+            L.level_scale[l] = s[l];
+        }
+    }
+}
+
 void compute_layout(const nbvh_config &c, nbvh_param_layout &L, GridParams &g)
 {
     std::memset(&L, 0, sizeof(L));
@@ -681,6 +706,7 @@ nbvh_status nbvh_create(const nbvh_config *cfg, int device, nbvh_handle **out)
         cuda_check(cudaMemset(h->d_counters.ptr, 0, 3u * sizeof(QueryCounters)), "zero counters");
         cuda_check(h->d_loss_sum.resize(1u), "alloc loss");
         compute_layout(h->cfg, h->layout, h->grid);
+        apply_device_level_scales(h->cfg, h->layout, h->grid);
         std::vector<float> p(h->layout.n_params);
         init_params(h->cfg, h->layout, p.data());
         upload_params(h, p.data(), true);
@@ -1704,6 +1730,27 @@ nbvh_status nbvh_debug_alloc_count(uint64_t *out)
     return NBVH_OK;
 }
 
+nbvh_status nbvh_debug_device_level_scales(const nbvh_config *cfg, int device, float *out)
+{
+    if (!cfg || !out || cfg->hashgrid.n_levels <= 0 || cfg->hashgrid.n_levels > 32 ||
+        !(cfg->hashgrid.per_level_scale > 0.0f))
+        return NBVH_EINVAL;
+    DeviceScope scope;
+    if (cudaSetDevice(device) != cudaSuccess)
+        return NBVH_EDEVICE;
+    const uint32_t n = (uint32_t)cfg->hashgrid.n_levels;
+    float *d = nullptr;
+    if (cudaMalloc(&d, 32u * sizeof(float)) != cudaSuccess)
+        return NBVH_ENOMEM;
+    // log2 of the level scale on the host in single precision, as tcnn's GridEncoding does
+    const float log2_scale = std::log2(cfg->hashgrid.per_level_scale);
+    cudaError_t e = launch_level_scales(log2_scale, (float)cfg->hashgrid.base_resolution, n, d, nullptr);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, d, n * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? NBVH_OK : NBVH_EDEVICE;
+}
+
 nbvh_status nbvh_last_kernel_time(nbvh_handle *h, float *ms, uint32_t *launches)
 {
     return guarded(h, [&]() {
@@ -1837,6 +1884,7 @@ nbvh_status nbvh_load(nbvh_handle *h, const char *path)
             if (i >= verts.size() / 3u)
                 fail(NBVH_EIO, "checkpoint triangle index out of range");
         // commit
+        apply_device_level_scales(cfg, L, g);
         h->cfg = cfg;
         h->layout = L;
         h->grid = g;

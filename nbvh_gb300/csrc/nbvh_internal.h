@@ -664,6 +664,8 @@ cudaError_t launch_adam(float *params, __half *params_h, float *m, float *v, con
 cudaError_t launch_params_to_half(const float *params, __half *params_h, uint32_t n, const ParamPrecision &pp,
                                   cudaStream_t s);
 
+// scale_l of levels 0 .. n-1 (n <= 32) evaluated on the device: exp2f(l * log2_scale) * base - 1
+cudaError_t launch_level_scales(float log2_scale, float base, uint32_t n, float *out, cudaStream_t s);
 cudaError_t launch_camera_rays(uint32_t width, uint32_t height, uint32_t sample_idx, uint32_t sample_offset,
                                const float *origin, const float *du, const float *dv, const float *top_left,
                                nbvh_ray *rays, cudaStream_t s);

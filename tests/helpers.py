@@ -54,3 +54,38 @@ def reference_root():
     """Root of the reference source tree when it is present on this machine (NBVH_REFERENCE
     overrides the default); tests that read its shipped data files skip without it."""
     return os.environ.get("NBVH_REFERENCE", "/root/reference")
+
+
+def gradient_blocks(h):
+    """[start, end) of every network matrix in the parameter vector, then the hash grid."""
+    off, blocks = 0, []
+    H = h.cfg.network.n_hidden_layers
+    for m in range(H + 1):
+        rows = 16 if m == H else 64
+        cols = h.layout.n_inputs if m == 0 else 64
+        blocks.append((off, off + rows * cols))
+        off += rows * cols
+    blocks.append((h.layout.n_network_params, h.layout.n_params))
+    return blocks
+
+
+def check_gradients(oracle, h, params, pos, tgt, g, rg, base_tol):
+    """GPU gradient g against the oracle's rg, block by block. The gradient summed over a batch
+    cancels strongly, so its relative error is set by the 16-bit rounding of a few activations that
+    lands on the other side of a rounding or ReLU boundary (the GPU sums in another order): the
+    oracle's own gradient moves by a few percent when the positions move by one float ulp. Each
+    block's bound is the larger of base_tol and 2.5 x the largest such movement over two nudges
+    (positions one ulp up, one ulp down), measured here; a wrong backward pass is off by far more."""
+    import numpy as np
+    net = oracle.network(h.cfg, h.layout, params)
+    moved = []
+    for toward in (np.float32(2), np.float32(-1)):
+        pos_n = np.nextafter(pos, toward).astype(np.float32)
+        rg_n, _ = oracle.compute_gradients(net, oracle.loss_consts(h.cfg), pos_n, tgt, h.layout.n_params,
+                                           loss_scale=h.cfg.optimizer.loss_scale)
+        moved.append(rg_n.astype(np.float64))
+    for a, b in gradient_blocks(h):
+        den = max(np.linalg.norm(rg[a:b]), 1e-30)
+        noise = max(np.linalg.norm(m[a:b] - rg[a:b]) / den for m in moved)
+        err = np.linalg.norm(g[a:b] - rg[a:b]) / den
+        assert err < max(base_tol, 2.5 * noise), (a, b, err, noise)

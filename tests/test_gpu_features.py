@@ -8,7 +8,8 @@ features x 2^18 entries, base resolution 8, scale 2) and its shipped chess confi
   tests/golden/make_config_golden.py) creates a handle, trains and answers queries;
 * with F = 4 (the reference default, 96 inputs) and F = 8 (2 points x 8 levels, 128 inputs):
   encoding bit-identical, network outputs within 5e-3, full neural queries as in
-  test_gpu_neural.py, gradients within 2e-2 relative L2 per parameter block, and training lowers
+  test_gpu_neural.py, gradients within 2e-2 relative L2 per parameter block (or the oracle's own
+  one-ulp sensitivity, helpers.check_gradients), and training lowers
   the loss.
 """
 
@@ -20,7 +21,7 @@ import pytest
 import torch
 
 import nbvh_gb300 as nb
-from helpers import as_u32, handle
+from helpers import as_u32, check_gradients, handle
 from nbvh_gb300 import scenes
 from test_gpu_neural import _borderline, _compare_queries, _cuda, _spread_params
 
@@ -101,17 +102,7 @@ def test_gradients_match_oracle(scene, oracle):
     rg, rloss = oracle.compute_gradients(net, oracle.loss_consts(h.cfg), pos.cpu().numpy(), tgt.cpu().numpy(),
                                          h.layout.n_params, loss_scale=h.cfg.optimizer.loss_scale)
     assert abs(loss - rloss) <= 1e-3 * abs(rloss) + 1e-6
-    nn = h.layout.n_network_params
-    H = h.cfg.network.n_hidden_layers
-    off, blocks = 0, []
-    for m in range(H + 1):
-        rows, cols = (16 if m == H else 64), (h.layout.n_inputs if m == 0 else 64)
-        blocks.append((off, off + rows * cols))
-        off += rows * cols
-    blocks.append((nn, h.layout.n_params))
-    for a, b in blocks:
-        err = np.linalg.norm(g[a:b] - rg[a:b]) / max(np.linalg.norm(rg[a:b]), 1e-30)
-        assert err < 2e-2, (a, b, err)
+    check_gradients(oracle, h, s["params"], pos.cpu().numpy(), tgt.cpu().numpy(), g, rg.astype(np.float64), 2e-2)
 
 
 def test_training_lowers_loss(scene):
@@ -144,3 +135,34 @@ def test_shipped_chess_configuration_runs(built, oracle):
         _compare_queries(got, ref, _borderline(h, oracle, s, rays))
     finally:
         h.close()
+
+
+def test_handles_encode_with_tcnns_device_level_scales(built):
+    """tcnn evaluates the level scales exp2f(l * log2f(s)) * base - 1 inside its kernels, with CUDA's
+    exp2f; the host's exp2f differs from it by an ulp or two on some levels (5 of the benchmark
+    grid's 16).
+    A handle encodes with the device's values (its layout reports them, and the oracle reads them
+    from there), while sizes, offsets and resolutions stay those of the host-only layout. Checked on
+    the benchmark's grid (16 levels, base 16, 16..2048), the reference default (8 levels, base 8,
+    scale 2), the shipped chess configuration and two non-power-of-two bases and scales."""
+    with open(GOLDEN) as fh:
+        chess = nb.config_from_reference_json(json.load(fh))
+    odd = nb.default_config(**{"hashgrid.n_levels": 12, "hashgrid.base_resolution": 12,
+                               "hashgrid.per_level_scale": 1.5})
+    wide = nb.default_config(**{"hashgrid.base_resolution": 7, "hashgrid.per_level_scale": 1.17})
+    for cfg in (nb.default_config(), nb.reference_default_config(), chess, odd, wide):
+        n = int(cfg.hashgrid.n_levels)
+        host = nb.param_layout(cfg)
+        dev = nb.device_level_scales(cfg)
+        h = nb.NBVH(cfg)
+        try:
+            L = h.layout
+            assert np.array_equal(np.array(L.level_scale[:n], np.float32).view(np.uint32), dev.view(np.uint32))
+            for k in ("level_offset", "level_size", "level_resolution"):
+                assert list(getattr(L, k)[:n]) == list(getattr(host, k)[:n]), k
+            assert L.n_params == host.n_params
+            ulps = np.abs(np.array(host.level_scale[:n], np.float32).view(np.int32).astype(np.int64)
+                          - dev.view(np.int32).astype(np.int64))
+            assert ulps.max() <= 2, ulps  # CUDA's exp2f is within 2 ulp of the exact value
+        finally:
+            h.close()
