@@ -1,5 +1,7 @@
-// net_device.cuh -- multiresolution hash-grid encoding and the fused MLP, warp-level building
-// blocks shared by the inference and training kernels.
+// net_device.cuh -- multiresolution hash-grid encoding (used by every encoder: the wavefront and
+// tail kernels of the query, the training rows, the stand-alone encode) and the warp-level MLP of
+// the persistent tail kernel (the wavefront steps and training run the MLP on tcgen05 tensor
+// cores: k_mlp_tc.cu, k_train.cu).
 //
 // The encoding follows the tcnn HashGrid behaviour the reference configures
 // (src/cuda/neural/neural_bvh_module.cu:170-191): per level, position = x * scale + 0.5, trilinear
@@ -8,9 +10,11 @@
 // (RepeatedComposite), features concatenated point-major then level-major.
 //
 // The MLP is tcnn's FullyFusedMLP shape (64 neurons, ReLU, Sigmoid output, no biases, output
-// padded to 16). Warp tiles of 16 rows are computed with mma.sync m16n8k16 (FP16 in, FP32
-// accumulate); hidden activations never leave registers: the FP32 accumulator fragment of one
-// layer, after ReLU and rounding to FP16, is exactly the A-operand fragment of the next layer.
+// padded to 16). The tail kernel's warps each own 16-row tiles, too few rows for a tcgen05 MMA
+// (M = 64 or 128 per CTA, issued by one thread for the whole CTA), so these are computed with
+// mma.sync m16n8k16 (FP16 in, FP32 accumulate); hidden activations never leave registers: the FP32
+// accumulator fragment of one layer, after ReLU and rounding to FP16, is exactly the A-operand
+// fragment of the next layer.
 #pragma once
 
 #include <cuda_bf16.h>

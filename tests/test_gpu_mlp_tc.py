@@ -1,11 +1,11 @@
 """The tcgen05 fully fused MLP (K4 forward, TMA-fed, accumulators in tensor memory).
 
 Checked against a plain PyTorch FP32 restatement of the same network (FP16 weights, hidden
-activations rounded to FP16 between layers, sigmoid output) and against the mma.sync network path
-of nbvh_network_inference on the same encoded positions. The paths differ only in FP32
-accumulation order, which can move a hidden activation by one FP16 ulp; with the deliberately
-spread test weights such a flip moves an output by a few 1e-3. Tolerance: every sigmoid output
-within 1e-2 absolute (the visibility bar of the neural path), and 99.9% within 1e-3.
+activations rounded to FP16 between layers, sigmoid output) and against nbvh_network_inference on
+the same positions (its own row encoder feeding the same kernel). The PyTorch restatement differs
+only in FP32 accumulation order, which can move a hidden activation by one FP16 ulp; with the
+deliberately spread test weights such a flip moves an output by a few 1e-3. Tolerance: every
+sigmoid output within 1e-2 absolute (the visibility bar of the neural path), and 99.9% within 1e-3.
 """
 
 import numpy as np
@@ -55,7 +55,7 @@ def torch_mlp(h, p, feats):
 
 
 @pytest.mark.parametrize("n", [5003, 4096, 1, 129])
-def test_mlp_tc_matches_torch_and_mma_path(net, n):
+def test_mlp_tc_matches_torch_and_network_inference(net, n):
     h, p = net
     g = torch.Generator(device="cuda").manual_seed(n)
     pos = torch.rand((n, h.cfg.module.input_segment_points, 3), device="cuda", generator=g)

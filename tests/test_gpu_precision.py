@@ -159,7 +159,7 @@ def test_fp8_tensor_core_mlp(scene8, oracle):
     got = h.mlp_inference(feats).cpu().numpy()
     ref = oracle.network_inference(oracle.network(h.cfg, h.layout, s["params"]), pos, threads=8)[:, :8]
     _close(got, ref, worst=0.25, tight=1e-2, frac=0.99)
-    # the tcgen05 path and the mma.sync path round the same values
+    # the MLP on encoded features and the network on positions (row encoder + the same MLP) agree
     _close(got, h.network_inference(_cuda(pos)).cpu().numpy(), worst=0.25, tight=1e-2, frac=0.99)
 
 
