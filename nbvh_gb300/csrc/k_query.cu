@@ -15,7 +15,7 @@
 //
 // Splitting the step lets each phase run at the occupancy it needs: the gathers of K3 with 48
 // warps per SM, the MLP with its accumulators in tensor memory, the divergent traversal with the
-// cut staged in shared memory. Every kernel reads the list length from device memory, so the host
+// cut read through L1 (or staged in shared memory: StepResources::stage_cut). Every kernel reads the list length from device memory, so the host
 // checks it only once per batch of steps (one 16-byte copy).
 #include <type_traits>
 
@@ -1160,11 +1160,12 @@ cudaError_t launch_tail_variant(const WaveArgs &a, uint32_t it, int num_sms, boo
     return cudaGetLastError();
 }
 
-cudaError_t launch_tail(const WaveArgs &a, uint32_t it, int num_sms, bool configure, cudaStream_t s)
+cudaError_t launch_tail(const WaveArgs &a, uint32_t it, int num_sms, bool configure, bool stage_cut,
+                        cudaStream_t s)
 {
     const TailLayout staged = tail_layout(a.n_cut_nodes, true, a.grid.n_inputs, a.n_hidden_layers);
     const TailLayout global = tail_layout(a.n_cut_nodes, false, a.grid.n_inputs, a.n_hidden_layers);
-    const bool smem_cut = staged.total <= kMaxDynamicSmem;
+    const bool smem_cut = stage_cut && staged.total <= kMaxDynamicSmem;
     const size_t smem = smem_cut ? staged.total : global.total;
     if (a.bf16)
         return smem_cut ? launch_tail_variant<true, true, false>(a, it, num_sms, configure, smem, s)
@@ -1199,7 +1200,7 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
                     return e;
                 launches++;
             }
-            e = launch_tail(a, it, num_sms, !r.capture_only, s);
+            e = launch_tail(a, it, num_sms, !r.capture_only, r.stage_cut, s);
             if (e == cudaSuccess)
                 e = cudaMemsetAsync(a.wave_counts, 0, 3u * sizeof(uint32_t), s);
             if (e != cudaSuccess)
@@ -1422,7 +1423,7 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     a.late_count = res.late_count;
     a.late_from = res.drain_host ? res.drain_step + 1u : 0xFFFFFFFFu;
     const size_t smem_cut = (size_t)n_cut_nodes * 56u;
-    const bool use_smem_cut = smem_cut <= kSmemLimit;
+    const bool use_smem_cut = res.stage_cut && smem_cut <= kSmemLimit;
     if (res.resume_from > 0u) // continue a query whose first steps ran from a captured graph
         return use_smem_cut
                    ? run_steps<true>(a, res, smem_cut, num_sms, nc.max_traversal_steps, res.resume_from, s, *launches)

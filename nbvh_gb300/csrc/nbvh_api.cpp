@@ -2111,6 +2111,7 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
         res.late_list = tune->late_list;
         res.late_count = tune->late_count;
         res.drain_taken = tune->drain_taken;
+        res.stage_cut = tune->stage_cut;
     }
     res.sort_key = h->n_sort_bins ? h->d_sort_key.ptr : nullptr;
     res.n_sort_bins = h->n_sort_bins;

@@ -49,6 +49,7 @@ constexpr int kYieldMs = 20;                 // longest a render bounce waits fo
 
 struct Tuning {
     uint32_t visits = 0, encode_blocks = 0;
+    bool stage_cut = false;
 };
 
 struct Model {
@@ -183,6 +184,7 @@ StepResources tuning_of(const Model &m, uint32_t bucket)
     if (it != m.tune.end()) {
         t.visits_per_round = it->second.visits;
         t.encode_blocks_per_sm = it->second.encode_blocks;
+        t.stage_cut = it->second.stage_cut;
     }
     return t;
 }
@@ -481,8 +483,9 @@ void slot_loop(nbvh_server *srv, Slot *sl)
     }
 }
 
-// Chooses, per bucket, the node visits per traversal round and the encoder blocks per SM that
-// give the shortest query on rays through the model's scene box (CUDA events on slot 0's stream).
+// Chooses, per bucket, the node visits per traversal round, the encoder blocks per SM and the cut
+// variant of the decode and tail kernels (staged in shared memory or read through L1) that give
+// the shortest query on rays through the model's scene box (CUDA events on slot 0's stream).
 void autotune(nbvh_server *srv, uint32_t model_id)
 {
     Slot &sl = *srv->slots[0];
@@ -513,27 +516,30 @@ void autotune(nbvh_server *srv, uint32_t model_id)
         float best = 1e30f;
         Tuning pick;
         for (uint32_t v : visits)
-            for (uint32_t eb : enc) {
-                StepResources t;
-                t.visits_per_round = v;
-                t.encode_blocks_per_sm = eb;
-                run_neural_query(h, sl.q, sl.counters.ptr, sl.rays.ptr, b, 1u, false, sl.hits.ptr, sl.stream, &t);
-                float ms_total = 0.f;
-                for (int rep = 0; rep < 2; rep++) {
-                    cuda_check(cudaEventRecord(e0, sl.stream), "event");
+            for (uint32_t eb : enc)
+                for (bool stage : {false, true}) {
+                    StepResources t;
+                    t.visits_per_round = v;
+                    t.encode_blocks_per_sm = eb;
+                    t.stage_cut = stage;
                     run_neural_query(h, sl.q, sl.counters.ptr, sl.rays.ptr, b, 1u, false, sl.hits.ptr, sl.stream, &t);
-                    cuda_check(cudaEventRecord(e1, sl.stream), "event");
-                    cuda_check(cudaEventSynchronize(e1), "event sync");
-                    float ms = 0.f;
-                    cuda_check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
-                    ms_total += ms;
+                    float ms_total = 0.f;
+                    for (int rep = 0; rep < 2; rep++) {
+                        cuda_check(cudaEventRecord(e0, sl.stream), "event");
+                        run_neural_query(h, sl.q, sl.counters.ptr, sl.rays.ptr, b, 1u, false, sl.hits.ptr, sl.stream, &t);
+                        cuda_check(cudaEventRecord(e1, sl.stream), "event");
+                        cuda_check(cudaEventSynchronize(e1), "event sync");
+                        float ms = 0.f;
+                        cuda_check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+                        ms_total += ms;
+                    }
+                    if (ms_total < best) {
+                        best = ms_total;
+                        pick.visits = v;
+                        pick.encode_blocks = eb;
+                        pick.stage_cut = stage;
+                    }
                 }
-                if (ms_total < best) {
-                    best = ms_total;
-                    pick.visits = v;
-                    pick.encode_blocks = eb;
-                }
-            }
         // buckets between the tuned powers of four take the nearest tuned value below
         m.tune[b] = pick;
         if ((b << 1) <= sl.capacity)
