@@ -30,8 +30,9 @@
  *     (src/cuda/neural/neural_bvh_renderer.cu:141-288)
  *   NeuralBVHRenderer::render, m_run_inference branch           nbvh_run_inference
  *     (src/cuda/neural/neural_bvh_renderer.cu:299-379)
- *   trainer->serialize / deserialize (own checkpoint format)    nbvh_save, nbvh_load
- *     (src/cuda/neural/neural_bvh_renderer_init.cu:385-404)
+ *   save_network_model / load_network_model (tcnn trainer      nbvh_export_tcnn_weights,
+ *     JSON, src/cuda/neural/neural_bvh_renderer_init.cu:385-404) nbvh_import_tcnn_weights;
+ *                                                               nbvh_save, nbvh_load (whole state)
  *   save_neural_bvh / load_neural_bvh (.nbvh neural cut)        nbvh_export_neural_cut,
  *     (src/cuda/neural/neural_bvh_renderer_accel.cpp:170-254)   nbvh_import_neural_cut
  *   tree-cut learning, BvhSplitScheduler, split / LoD steps      nbvh_begin_tree_cut,
@@ -382,6 +383,21 @@ nbvh_status nbvh_get_param_layout(const nbvh_handle *h, nbvh_param_layout *out);
 /* FP32 master parameters; set also refreshes the FP16 (or BF16/FP8) copies and resets Adam. */
 nbvh_status nbvh_get_params(nbvh_handle *h, float *h_params);
 nbvh_status nbvh_set_params(nbvh_handle *h, const float *h_params);
+
+/* tcnn trainer weights as the reference saves and loads them (NeuralBVHRenderer::save_network_model /
+ * load_network_model, src/cuda/neural/neural_bvh_renderer_init.cu:385-404: the JSON text of
+ * trainer->serialize(false)): {"n_params": N, "params_type": "float" | "__half", "params_binary":
+ * {"bytes": [...], "subtype": null}}, the binary value in nlohmann's text form (a bare byte array is
+ * read too). The parameters are in tcnn's NetworkWithInputEncoding order, which is this library's:
+ * the network matrices [out][in] row-major (first, hidden, output padded to 16 rows), then the hash
+ * grid level by level, F values per entry. FP16 files are widened to FP32; export writes FP32.
+ * Import replaces the handle's parameters like nbvh_set_params (N must equal its layout's
+ * n_params, else NBVH_EINVAL; a malformed file gives NBVH_EIO). The host forms need no device:
+ * read gives *n_params and, when h_params is not NULL and capacity suffices, the values. */
+nbvh_status nbvh_import_tcnn_weights(nbvh_handle *h, const char *path);
+nbvh_status nbvh_export_tcnn_weights(nbvh_handle *h, const char *path);
+nbvh_status nbvh_read_tcnn_params_host(const char *path, float *h_params, uint64_t capacity, uint64_t *n_params);
+nbvh_status nbvh_write_tcnn_params_host(const char *path, const float *h_params, uint64_t n_params);
 
 /* Network inference on explicit inputs: d_positions holds n x points x 3 encoded positions in
  * [0,1]^3; d_outputs receives n x 8 sigmoid outputs. (Hash-grid encoding + fused MLP.) */

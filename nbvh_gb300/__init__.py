@@ -184,6 +184,24 @@ def param_layout(cfg):
     return L
 
 
+def read_tcnn_params(path):
+    """The parameters of a tcnn trainer JSON file as FP32 (no device needed)."""
+    lib = load_library()
+    n = C.c_uint64(0)
+    _check(lib.nbvh_read_tcnn_params_host(str(path).encode(), None, 0, C.byref(n)), None)
+    out = np.empty(n.value, np.float32)
+    _check(lib.nbvh_read_tcnn_params_host(str(path).encode(), out.ctypes.data_as(C.POINTER(C.c_float)), n.value,
+                                          C.byref(n)), None)
+    return out
+
+
+def write_tcnn_params(path, params):
+    """Writes FP32 parameters as a tcnn trainer JSON file (no device needed)."""
+    p = np.ascontiguousarray(params, np.float32)
+    _check(load_library().nbvh_write_tcnn_params_host(str(path).encode(), p.ctypes.data_as(C.POINTER(C.c_float)),
+                                                      p.size), None)
+
+
 def device_level_scales(cfg, device=0):
     """The hash-grid level scales evaluated on the GPU the way tcnn's kernels do (CUDA's exp2f),
     for comparison with param_layout(cfg).level_scale (the host's exp2f)."""
@@ -586,6 +604,13 @@ class NBVH:
 
     def export_neural_cut(self, path):
         self._check(self.lib.nbvh_export_neural_cut(self.h, str(path).encode()))
+
+    def import_tcnn_weights(self, path):
+        """Parameters from a tcnn trainer JSON file (the reference's save_network_model format)."""
+        self._check(self.lib.nbvh_import_tcnn_weights(self.h, str(path).encode()))
+
+    def export_tcnn_weights(self, path):
+        self._check(self.lib.nbvh_export_tcnn_weights(self.h, str(path).encode()))
 
     def render_path(self, req, stream=None):
         """Path-traced RGBA image (float32 [height * width, 4] on the device) and the rays traced."""

@@ -225,6 +225,10 @@ PROTOTYPES = {
     "nbvh_debug_fail_allocations": (ST, [C.c_int64]),
     "nbvh_debug_alloc_count": (ST, [C.POINTER(C.c_uint64)]),
     "nbvh_debug_device_level_scales": (ST, [C.POINTER(Config), C.c_int, C.POINTER(C.c_float)]),
+    "nbvh_import_tcnn_weights": (ST, [P, C.c_char_p]),
+    "nbvh_export_tcnn_weights": (ST, [P, C.c_char_p]),
+    "nbvh_read_tcnn_params_host": (ST, [C.c_char_p, PF, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "nbvh_write_tcnn_params_host": (ST, [C.c_char_p, PF, C.c_uint64]),
     "nbvh_build_bvh2_host": (ST, [P, U32, P, U32, P, PU32, P]),
     "nbvh_build_neural_cut_host": (ST, [P, U32, U32, P, PU32]),
     "nbvh_param_layout_host": (ST, [PCFG, C.POINTER(ParamLayout)]),

@@ -1286,6 +1286,35 @@ nbvh_status nbvh_set_params(nbvh_handle *h, const float *h_params)
     });
 }
 
+nbvh_status nbvh_import_tcnn_weights(nbvh_handle *h, const char *path)
+{
+    return guarded(h, [&]() {
+        require(path != nullptr, NBVH_EINVAL, "null path");
+        std::vector<float> p;
+        std::string err;
+        if (!read_tcnn_params(path, p, err))
+            fail(NBVH_EIO, "tcnn weights " + std::string(path) + ": " + err);
+        if (p.size() != h->layout.n_params)
+            fail(NBVH_EINVAL, "tcnn weights hold " + std::to_string(p.size()) + " parameters, the configuration " +
+                                  std::to_string(h->layout.n_params));
+        upload_params(h, p.data(), true);
+    });
+}
+
+nbvh_status nbvh_export_tcnn_weights(nbvh_handle *h, const char *path)
+{
+    return guarded(h, [&]() {
+        require(path != nullptr, NBVH_EINVAL, "null path");
+        std::vector<float> p(h->layout.n_params);
+        cuda_check(cudaDeviceSynchronize(), "sync");
+        cuda_check(cudaMemcpy(p.data(), h->d_params.ptr, p.size() * sizeof(float), cudaMemcpyDeviceToHost),
+                   "download params");
+        std::string err;
+        if (!write_tcnn_params(path, p.data(), p.size(), err))
+            fail(NBVH_EIO, "tcnn weights " + std::string(path) + ": " + err);
+    });
+}
+
 nbvh_status nbvh_network_inference(nbvh_handle *h, const float *d_positions, uint32_t n, float *d_outputs,
                                    nbvh_stream stream)
 {

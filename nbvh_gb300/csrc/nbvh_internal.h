@@ -745,5 +745,8 @@ void upload_inference_nodes(nbvh_handle *h);
 bool validate_cut(const std::vector<BVHNode> &nodes, std::string &err);
 bool read_nbvh(const std::string &path, std::vector<BVHNode> &nodes, std::string &err);
 bool write_nbvh(const std::string &path, const std::vector<BVHNode> &nodes, std::string &err);
+// tcnn trainer weights (JSON text of trainer->serialize): parameters as FP32 (16-bit widened)
+bool read_tcnn_params(const char *path, std::vector<float> &params, std::string &err);
+bool write_tcnn_params(const char *path, const float *params, uint64_t n, std::string &err);
 
 } // namespace nbvh

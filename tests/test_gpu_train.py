@@ -7,6 +7,8 @@
   below 2.5x the oracle's own change when the positions move by one float ulp where that is larger
   (the batch sum cancels, so a few activations rounded across a boundary move it by percents).
 * Adam + ExponentialDecay: bit-identical to the restatement.
+* Parameters through a tcnn trainer JSON file (the reference's save / load_network_model format):
+  export, import into a second handle, same parameters and query records.
 * The optimisation loop lowers the loss, and the trained network beats the untrained one against
   the classic judge.
 """
@@ -133,6 +135,29 @@ def test_checkpoint_round_trip(scene, tmp_path):
         with pytest.raises(nb.NBVHError) as e:
             h3.load(path)
         assert e.value.status == nb.abi.NBVH_EIO
+
+
+def test_tcnn_weights_round_trip(scene, tmp_path):
+    """The handle's parameters exported as a tcnn trainer JSON file and imported into a second
+    handle of the same configuration and scene: the same FP32 master parameters and the same query
+    records; a file with another parameter count is refused with NBVH_EINVAL."""
+    h, s = scene
+    path = str(tmp_path / "weights.json")
+    h.export_tcnn_weights(path)
+    rays = scenes.uniform_rays(4096, s["bbox"][:3], s["bbox"][3:], seed=43)
+    a = as_u32(h.query_closest_neural(_cuda(rays)))
+    h2, _ = handle(h.cfg, kind="sphere65k", seed=1, albedo=True)
+    try:
+        h2.import_tcnn_weights(path)
+        assert np.array_equal(h2.params().view(np.uint32), h.params().view(np.uint32))
+        assert np.array_equal(as_u32(h2.query_closest_neural(_cuda(rays))), a)
+        short = str(tmp_path / "short.json")
+        nb.write_tcnn_params(short, h.params()[:-8])
+        with pytest.raises(nb.NBVHError) as e:
+            h2.import_tcnn_weights(short)
+        assert e.value.status == nb.abi.NBVH_EINVAL
+    finally:
+        h2.close()
 
 
 def test_training_step_profile(scene):
