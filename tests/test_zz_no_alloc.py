@@ -108,3 +108,32 @@ def test_noalloc_follows_the_classic_switch(scene):
     finally:
         h.set_ignore_neural_blas(False)
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+def test_noalloc_deep_cut_fallback_and_non_neural_leaves(built):
+    """A cut deeper than the node-sorted range (16,383 nodes: the tail takes over after step 3), a
+    confidence fallback margin and non-neural leaves (both answered from the fallback list by the
+    classic BLAS, on the fixed scratch): every word equals the ordinary query's."""
+    import nbvh_gb300 as nb
+    h, s = handle(nb.default_config(fallback_margin=0.05), kind="sphere65k", seed=1, depth=13, albedo=True)
+    try:
+        assert h.neural_bvh()[0].shape[0] > 8192
+        rng = np.random.default_rng(6)
+        p = h.params()
+        nn = h.layout.n_network_params
+        p[:nn] *= 2.5
+        p[nn:] = rng.uniform(-1.0, 1.0, p.size - nn).astype(np.float32)
+        h.set_params(p)
+        nodes = h.neural_bvh()[0]
+        leaves = np.where(nodes.view(np.uint32)[:, 3] != 0)[0].astype(np.uint32)
+        h.set_non_neural_leaves(leaves[::7], True)
+        rays = torch.from_numpy(scenes.uniform_rays(MAX_RAYS, s["bbox"][:3], s["bbox"][3:], seed=91)).cuda()
+        ref = h.query_closest_neural(rays, 1).cpu().numpy()
+        assert ((ref[:, 8] & 2) != 0).sum() > 100  # answered by the classic BLAS
+        for _ in range(2):
+            out = torch.full((MAX_RAYS, 12), -1, dtype=torch.int32, device="cuda")
+            assert _noalloc(h, rays, out) == NBVH_OK, _err(h)
+            np.testing.assert_array_equal(out.cpu().numpy(), ref)
+    finally:
+        h.close()
+
