@@ -227,6 +227,21 @@ def time_queries(h, rays, hits, chits, steps, warmup, nvtx_name, profile=None):
     return times, ctimes, neural_launches, classic_launches
 
 
+def relative_depth_error(tn, tc):
+    """Relative depth error of neural hit distances tn against classic ones tc (rays that hit in both)."""
+    err = np.abs(tn - tc).astype(np.float64)
+    rel = err / np.maximum(tc, 1e-6)
+    # relative error is ill-conditioned for rays starting on the surface (t -> 0): the headline
+    # mean floors the denominator at 1% of the unit scene; the raw mean is reported beside it
+    any_ = bool(len(tn) > 0)
+    return {"mean_rel_floor1pct": float(np.mean(err / np.maximum(tc, 1e-2))) if any_ else None,
+            "mean_rel_raw": float(rel.mean()) if any_ else None,
+            "median_rel": float(np.median(rel)) if any_ else None,
+            "p90_rel": float(np.percentile(rel, 90)) if any_ else None,
+            "p99_rel": float(np.percentile(rel, 99)) if any_ else None,
+            "within_1pct": float(np.mean(rel <= 0.01)) if any_ else None}
+
+
 def accuracy(hits, chits):
     """Visibility agreement and depth error of the neural hits against the classic kernel."""
     g = hits.cpu().numpy().view(np.uint32)
@@ -235,19 +250,34 @@ def accuracy(hits, chits):
     cvalid = c[:, 3] != 0xFFFFFFFF
     vis_agree = float(np.mean(nvalid == cvalid))
     both = nvalid & cvalid
-    tn, tc = g[both, 0].view(np.float32), c[both, 0].view(np.float32)
-    err = np.abs(tn - tc).astype(np.float64)
-    rel = err / np.maximum(tc, 1e-6)
-    # relative error is ill-conditioned for rays starting on the surface (t -> 0): the headline
-    # mean floors the denominator at 1% of the unit scene; the raw mean is reported beside it
-    any_ = bool(both.any())
-    depth = {"mean_rel_floor1pct": float(np.mean(err / np.maximum(tc, 1e-2))) if any_ else None,
-             "mean_rel_raw": float(rel.mean()) if any_ else None,
-             "median_rel": float(np.median(rel)) if any_ else None,
-             "p90_rel": float(np.percentile(rel, 90)) if any_ else None,
-             "p99_rel": float(np.percentile(rel, 99)) if any_ else None,
-             "within_1pct": float(np.mean(rel <= 0.01)) if any_ else None}
+    depth = relative_depth_error(g[both, 0].view(np.float32), c[both, 0].view(np.float32))
     return vis_agree, depth, float(g[:, 9].astype(np.float64).mean())
+
+
+def depth_error_by_origin(hits, chits, rays, nn):
+    """The depth error split by where a ray starts: inside a leaf box of the neural cut (next to
+    the surface, where the classic hit distance tends to 0 and any miss of the network is a large
+    relative error) or outside every leaf box (as camera rays do)."""
+    import torch
+    g = hits.cpu().numpy().view(np.uint32)
+    c = chits.cpu().numpy().view(np.uint32)
+    both = ((g[:, 8] & 1) != 0) & (c[:, 3] != 0xFFFFFFFF)
+    nodes = torch.from_numpy(np.ascontiguousarray(nn).view(np.float32)).cuda()
+    leaf = torch.from_numpy(np.ascontiguousarray(nn)[:, 3] != 0).cuda()
+    lo, hi = nodes[leaf, 0:3], nodes[leaf, 4:7]
+    o = rays[:, 0:3]
+    inside = torch.zeros(o.shape[0], dtype=torch.bool, device=o.device)
+    for k in range(0, o.shape[0], 1 << 15):
+        oo = o[k:k + (1 << 15), None, :]
+        inside[k:k + (1 << 15)] = ((oo >= lo[None]) & (oo <= hi[None])).all(dim=2).any(dim=1)
+    inside = inside.cpu().numpy()
+    tn, tc = g[:, 0].view(np.float32), c[:, 0].view(np.float32)
+    out = {}
+    for name, m in (("origin_outside_leaves", both & ~inside), ("origin_inside_leaves", both & inside)):
+        d = relative_depth_error(tn[m], tc[m])
+        d["rays"] = int(m.sum())
+        out[name] = d
+    return out
 
 
 def mlp_roofline(h, peak, rows=1 << 22, reps=10):
@@ -485,6 +515,7 @@ def run_ours(args):
     ms, cms = max_over_ranks([float(times.mean()), float(ctimes.mean())])
     stats = h.query_stats()
     vis_agree, depth_stats, segs_per_ray = accuracy(hits, chits)
+    depth_by_origin = depth_error_by_origin(hits, chits, rays, nn)
 
     # e2e through the host-buffer C-ABI call: pinned host rays in, hits out, copies timed
     pin_in = torch.from_numpy(rays_np).pin_memory()
@@ -531,6 +562,7 @@ def run_ours(args):
         "neural_over_classic": cms / ms,
         "p50_ms": float(np.percentile(times, 50)), "p99_ms": float(np.percentile(times, 99)),
         "depth_rel_err_mean": depth_stats["mean_rel_floor1pct"], "depth_error": depth_stats,
+        "depth_error_by_origin": depth_by_origin,
         "visibility_agreement": vis_agree, "segments_per_ray": segs_per_ray,
         "train": {"steps": args.train_steps if st else 0, "seconds": train_s,
                   "last_loss": (st.last_loss if st else None), "ms_per_step": (st.ms_per_step if st else None)},
@@ -611,6 +643,8 @@ def summary_of(line):
             "vis_agree": r(line.get("visibility_agreement"), 4), "depth_rel_mean_raw": r(de.get("mean_rel_raw"), 4),
             "depth_rel_mean_floor1pct": r(de.get("mean_rel_floor1pct"), 4),
             "depth_within_1pct": r(de.get("within_1pct"), 4),
+            "depth_rel_mean_raw_origin_outside_leaves":
+                r(line.get("depth_error_by_origin", {}).get("origin_outside_leaves", {}).get("mean_rel_raw"), 4),
             "cpu_classic_mrays_all": r(cb.get("value"), 2), "cpu_classic_mrays_1thr": r(cb.get("single_thread"), 3),
             "cpu_cores": cb.get("cores"), "serving_p99_ms_per_1m": r(sv.get("ms_per_1m_rays_p99")),
             "serving_1m_batch_p99_ms": r(b1m.get("p99_ms"), 2), "serving_1m_batch_p50_ms": r(b1m.get("p50_ms"), 2),
