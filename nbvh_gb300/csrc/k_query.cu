@@ -78,6 +78,7 @@ struct WaveArgs {
     uint32_t *node_cursor; // [2][n_sort_nodes] placement cursors of the sort
     const uint32_t *sort_key; // sort bin of each leaf (cuts above kMaxSortNodes nodes); NULL: the node
     uint32_t n_sort_nodes;    // sort bins
+    uint32_t sub_bins;        // 1: each leaf's rows in 8 bins by the octant of their segment midpoint
     uint32_t n_hidden_layers;
     uint32_t n;
     uint32_t n_cut_nodes;
@@ -179,6 +180,33 @@ __device__ __forceinline__ uint32_t warp_append(bool want, uint32_t *counter)
 __device__ __forceinline__ uint32_t sort_bin(const WaveArgs &a, uint32_t node)
 {
     return a.sort_key ? a.sort_key[node] : node;
+}
+
+// Sort bin of a listed row: its leaf's bin, and with sub-bins the octant of the leaf box that holds
+// the midpoint of the row's segment, so that the encoder meets the rows of a leaf region by region.
+// The first pass and the decode (counting the rows they append) and the sort (placing them)
+// evaluate it on the same stored values.
+__device__ __forceinline__ uint32_t row_bin(const WaveArgs &a, uint32_t node, V3 o, V3 d, float mint, float maxt)
+{
+    const uint32_t b = sort_bin(a, node);
+    if (!a.sub_bins)
+        return b;
+    // explicit roundings: every call site must get the same bits, whatever the compiler contracts
+    const float tm = __fmul_rn(0.5f, __fadd_rn(mint, maxt));
+    const float4 lo = __ldg(a.nodes + 2u * node), hi = __ldg(a.nodes + 2u * node + 1u);
+    const uint32_t oct = (__fmaf_rn(d.x, tm, o.x) > __fmul_rn(0.5f, __fadd_rn(lo.x, hi.x)) ? 1u : 0u) |
+                         (__fmaf_rn(d.y, tm, o.y) > __fmul_rn(0.5f, __fadd_rn(lo.y, hi.y)) ? 2u : 0u) |
+                         (__fmaf_rn(d.z, tm, o.z) > __fmul_rn(0.5f, __fadd_rn(lo.z, hi.z)) ? 4u : 0u);
+    return kSubBins * b + oct;
+}
+
+__device__ __forceinline__ uint32_t listed_row_bin(const WaveArgs &a, const WaveList &in, uint32_t r)
+{
+    if (!a.sub_bins)
+        return sort_bin(a, in.meta[r].y);
+    const float4 od0 = in.od0[r], od1 = in.od1[r];
+    const uint4 m = in.meta[r];
+    return row_bin(a, m.y, mk3(od0.x, od0.y, od0.z), mk3(od1.x, od1.y, od1.z), od1.w, __uint_as_float(m.x));
 }
 
 // Counts the rows a warp appends per sort bin (one atomic per distinct bin in the warp); all 32
@@ -385,7 +413,7 @@ __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_co
         if (listed)
             store_state(a.lists[0], pos, s, stack);
         if (a.perm)
-            count_nodes(a.node_bins, listed, listed ? sort_bin(a, s.seg_node) : 0u);
+            count_nodes(a.node_bins, listed, listed ? row_bin(a, s.seg_node, s.o, s.d, s.seg_mint, s.seg_maxt) : 0u);
     }
 }
 
@@ -563,7 +591,7 @@ __global__ void __launch_bounds__(kSortThreads) k_wave_sort(const __grid_constan
     }
     const WaveList &in = a.lists[it & 1u];
     for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
-        atomicAdd(&cnt[sort_bin(a, in.meta[r].y)], 1u);
+        atomicAdd(&cnt[listed_row_bin(a, in, r)], 1u);
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < NB; k += blockDim.x) {
         const uint32_t c = cnt[k];
@@ -572,7 +600,7 @@ __global__ void __launch_bounds__(kSortThreads) k_wave_sort(const __grid_constan
     }
     __syncthreads();
     for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        const uint32_t node = sort_bin(a, in.meta[r].y);
+        const uint32_t node = listed_row_bin(a, in, r);
         const uint32_t slot = scan[node] + base[node] + atomicAdd(&cnt[node], 1u);
         if (slot < count_in) // the counts match the list; the check only keeps a stray row in bounds
             a.perm[slot] = r;
@@ -759,7 +787,8 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
         if (keep)
             store_state(out, pos, s, stack);
         if (a.perm)
-            count_nodes(a.node_bins + ((it + 1u) & 1u) * a.n_sort_nodes, keep, keep ? sort_bin(a, s.seg_node) : 0u);
+            count_nodes(a.node_bins + ((it + 1u) & 1u) * a.n_sort_nodes, keep,
+                        keep ? row_bin(a, s.seg_node, s.o, s.d, s.seg_mint, s.seg_maxt) : 0u);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -1368,7 +1397,7 @@ cudaError_t configure_query_kernels()
         allow_max_dynamic_smem(k_wave_tail<true, false, false>), allow_max_dynamic_smem(k_wave_tail<false, false, false>),
         allow_max_dynamic_smem(k_wave_tail<true, true, false>),  allow_max_dynamic_smem(k_wave_tail<false, true, false>),
         allow_max_dynamic_smem(k_wave_tail<true, false, true>),  allow_max_dynamic_smem(k_wave_tail<false, false, true>),
-        configure_mlp_tc()};
+        allow_max_dynamic_smem(k_wave_sort), configure_mlp_tc()};
     for (cudaError_t e : es)
         if (e != cudaSuccess)
             return e;
@@ -1407,7 +1436,10 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     const bool keyed = res.sort_key != nullptr && res.n_sort_bins > 0u;
     const uint32_t n_bins = keyed ? res.n_sort_bins : n_cut_nodes;
     a.sort_key = keyed ? res.sort_key : nullptr;
-    a.n_sort_nodes = n_bins;
+    // octant sub-bins where the caller sized the count buffers for them and the sort's three
+    // shared-memory arrays of 8 x n_bins words fit
+    a.sub_bins = (res.sub_bins && (size_t)3u * 4u * kSubBins * n_bins <= (size_t)kMaxDynamicSmem) ? 1u : 0u;
+    a.n_sort_nodes = a.sub_bins ? kSubBins * n_bins : n_bins;
     a.bf16 = prec == NBVH_PRECISION_BF16 ? 1u : 0u;
     a.prec = prec;
     const bool sort = res.perm != nullptr && n_bins <= kMaxSortNodes;
@@ -1436,9 +1468,9 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     if (e != cudaSuccess)
         return e;
     if (sort) {
-        e = cudaMemsetAsync(res.node_bins, 0, 2u * n_bins * sizeof(uint32_t), s);
+        e = cudaMemsetAsync(res.node_bins, 0, 2u * a.n_sort_nodes * sizeof(uint32_t), s);
         if (e == cudaSuccess)
-            e = cudaMemsetAsync(res.node_cursor, 0, 2u * n_bins * sizeof(uint32_t), s);
+            e = cudaMemsetAsync(res.node_cursor, 0, 2u * a.n_sort_nodes * sizeof(uint32_t), s);
         if (e != cudaSuccess)
             return e;
     }

@@ -2056,9 +2056,9 @@ void grow_query_context(const nbvh_handle *h, QueryContext &q, uint32_t n)
             q.h_words[k] = 0;
     }
     const size_t cut = h->neural_nodes.size();
-    if (q.node_bins.count < 2u * cut) {
-        cuda_check(q.node_bins.resize(2u * cut), "alloc node counts");
-        cuda_check(q.node_cursor.resize(2u * cut), "alloc node cursors");
+    if (q.node_bins.count < 2u * kSubBins * cut) { // room for the octant sub-bins of every node
+        cuda_check(q.node_bins.resize(2u * kSubBins * cut), "alloc node counts");
+        cuda_check(q.node_cursor.resize(2u * kSubBins * cut), "alloc node cursors");
     }
     const uint32_t wb = packed_weight_bytes(h->layout.n_inputs, (uint32_t)h->cfg.network.n_hidden_layers);
     if (q.wpacked.count < wb / 2u)
@@ -2122,6 +2122,7 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
     res.ray_bins = q.ray_bins.ptr;
     res.node_bins = q.node_bins.ptr;
     res.node_cursor = q.node_cursor.ptr;
+    res.sub_bins = q.node_bins.count >= 2u * kSubBins * h->neural_nodes.size();
     res.h_words = q.h_words;
     res.ev = q.ev;
     res.wait_ns = h->wait_limit_ns;

@@ -446,6 +446,7 @@ constexpr uint32_t kRaySortMin = 1u << 19;
 // Cuts with more nodes than this are not sorted by node between steps (the sort scans the node
 // counts in shared memory).
 constexpr uint32_t kMaxSortNodes = 8192;
+constexpr uint32_t kSubBins = 8; // octants of a leaf box
 
 // Opaque 128-byte CUDA tensor map (CUtensorMap) built on the host for TMA copies.
 struct alignas(64) TensorMapBytes {
@@ -501,6 +502,9 @@ struct StepResources {
     // through L1; off by default: through L1 the tail runs two blocks per SM instead of one, more
     // gathers in flight (2,047-node cut, 2^22 rays: 3.33 against 3.37 ms per query)
     bool stage_cut = false;
+    // the rows of each leaf in kSubBins sort bins by the octant of their segment midpoint (needs
+    // node_bins / node_cursor of 2 x kSubBins x the cut's nodes)
+    bool sub_bins = false;
     bool stall = false;            // failure-path tests: the MLP kernels wait on a barrier nothing arrives at
 };
 
