@@ -5,7 +5,8 @@ the edges of the input domain, through device buffers and pageable and page-lock
 * A batch of 0 rays returns NBVH_OK and an empty result, on every route.
 * A ray's record does not depend on the other rays of its batch: every ragged sub-batch (1, 2, 31,
   32, 33, 127, 1,000 and 4,097 rays at odd offsets) gives the same record words as the ray got in
-  the whole batch.
+  the whole batch, and a batch large enough for the leaf sort gives the words of the same rays
+  queried in batches below the sort's threshold.
 * Rays at the domain's edges (an empty interval tmin > tmax, a zero-length interval, rays far
   outside pointing away, axis-aligned rays from the scene centre, rays with a huge tmax, rays whose
   direction is not of unit length, rays starting on the scene box's corner) answer like the
@@ -115,3 +116,14 @@ def test_edge_rays_match_oracle(scene, oracle):
     assert np.all((got[e, 8][away] & 1) == 0)
     st = h.query_stats()
     assert st.step_capped == 0 and st.stack_overflow == 0
+
+
+def test_sorted_and_unsorted_batches_agree(scene):
+    """A batch large enough for the leaf sort (2^17 rays: rows grouped by leaf and by the octant of
+    their segment midpoint before the encoder) and the same rays in batches below the sort's
+    threshold (walked in list order) give the same record words."""
+    h, s = scene
+    rays = scenes.uniform_rays(1 << 17, s["bbox"][:3], s["bbox"][3:], seed=79)
+    whole = as_u32(h.query_closest_neural(_cuda(rays)))
+    parts = [as_u32(h.query_closest_neural(_cuda(rays[k:k + (1 << 15)]))) for k in range(0, 1 << 17, 1 << 15)]
+    assert np.array_equal(whole, np.concatenate(parts))
