@@ -223,14 +223,18 @@ __device__ __forceinline__ void count_nodes(uint32_t *bins, bool want, uint32_t 
         atomicAdd(&bins[node], (uint32_t)__popc(same));
 }
 
-// Coherence bin of a ray: direction octant (3 bits) above the Morton code of its origin's cell in
-// an 8 x 8 x 8 grid over the scene box grown by half its size on every side (origins outside are
-// clamped to the border cells).
+// Coherence bin of a ray: its direction class (octant and dominant axis: 24 classes) above the
+// Morton code of its origin's cell in an 8 x 8 x 8 grid over the scene box grown by half its size
+// on every side (origins outside are clamped to the border cells). Measured on GB300 against the
+// octant alone (4,096 bins): classic 1.097 -> 1.060 ms, neural 3.285 -> 3.275 ms per 2^22 rays;
+// a finer direction grid (cube faces x 4 x 4) with 4 x 4 x 4 origin cells was slower (1.114, 3.303).
 __device__ __forceinline__ uint32_t ray_bin(const nbvh_ray *rays, uint32_t i, V3 lo, V3 scale)
 {
     const float4 *r = reinterpret_cast<const float4 *>(rays + i);
     const float4 ra = __ldg(r), rb = __ldg(r + 1);
     const uint32_t oct = (rb.x > 0.0f ? 1u : 0u) | (rb.y > 0.0f ? 2u : 0u) | (rb.z > 0.0f ? 4u : 0u);
+    const float ax = fabsf(rb.x), ay = fabsf(rb.y), az = fabsf(rb.z);
+    const uint32_t dom = (ax >= ay && ax >= az) ? 0u : (ay >= az ? 1u : 2u); // NaN -> 2
     auto cell = [](float x, float l, float s) {
         const float c = (x - l) * s;
         return c >= 7.0f ? 7u : (c > 0.0f ? (uint32_t)c : 0u); // NaN -> 0
@@ -240,7 +244,7 @@ __device__ __forceinline__ uint32_t ray_bin(const nbvh_ray *rays, uint32_t i, V3
 #pragma unroll
     for (int b = 0; b < 3; b++)
         m |= (((cx >> b) & 1u) << (3 * b)) | (((cy >> b) & 1u) << (3 * b + 1)) | (((cz >> b) & 1u) << (3 * b + 2));
-    return (oct << 9) | m;
+    return (oct * 3u + dom) * 512u + m; // < 24 x 512 = kRayBins
 }
 
 struct RayBinArgs {
@@ -282,15 +286,18 @@ __global__ void __launch_bounds__(kRayBinThreads) k_ray_bins(const __grid_consta
             atomicAdd(&a.bins[b], cnt[b]);
 }
 
-// Exclusive scan of the bin counts into placement cursors (one block of 1,024 threads, 4 bins each).
+// Exclusive scan of the bin counts into placement cursors (one block of 1,024 threads,
+// kRayBins / 1,024 bins each).
+constexpr uint32_t kRayBinsPerThread = kRayBins / 1024u;
+static_assert(kRayBins % 1024u == 0u, "whole bins per scan thread");
 __global__ void __launch_bounds__(1024) k_ray_bin_scan(uint32_t *bins)
 {
     __shared__ uint32_t warp_sums[32];
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
-    uint32_t v[4], run = 0;
+    uint32_t v[kRayBinsPerThread], run = 0;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        v[k] = bins[4u * t + k];
+    for (uint32_t k = 0; k < kRayBinsPerThread; k++) {
+        v[k] = bins[kRayBinsPerThread * t + k];
         run += v[k];
     }
     uint32_t incl = run;
@@ -307,8 +314,8 @@ __global__ void __launch_bounds__(1024) k_ray_bin_scan(uint32_t *bins)
     for (uint32_t w = 0; w < warp; w++)
         base += warp_sums[w];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        bins[4u * t + k] = base;
+    for (uint32_t k = 0; k < kRayBinsPerThread; k++) {
+        bins[kRayBinsPerThread * t + k] = base;
         base += v[k];
     }
 }

@@ -434,13 +434,13 @@ inline cudaError_t allow_max_dynamic_smem(K kernel)
                                 kMaxDynamicSmem - (int)fa.sharedSizeBytes);
 }
 
-// Coherence bins of the rays of a query (direction octant x 8^3 origin cells of the scene box
-// grown by half its size on every side): the first pass and the classic kernel take the rays bin
+// Coherence bins of the rays of a query (24 direction classes, octant x dominant axis, x 8^3 origin
+// cells of the scene box grown by half its size on every side): the first pass and the classic kernel take the rays bin
 // by bin, so that the rays of a warp start near one another in the same direction. Batches below
 // kRaySortMin rays are taken in batch order: the ordering's three launches (about 50 us) pay only
 // on larger batches (measured: 2^22 uniform rays, classic 1.49 -> 1.09 ms; a 389K-ray camera batch,
 // already coherent, 0.174 -> 0.213 ms).
-constexpr uint32_t kRayBins = 4096;
+constexpr uint32_t kRayBins = 12288; // 24 direction classes x 8^3 origin cells
 constexpr uint32_t kRaySortMin = 1u << 19;
 
 // Cuts with more nodes than this are not sorted by node between steps (the sort scans the node
