@@ -81,6 +81,8 @@ struct WaveArgs {
     const uint32_t *sort_key; // sort bin of each leaf (cuts above kMaxSortNodes nodes); NULL: the node
     uint32_t n_sort_nodes;    // sort bins
     uint32_t sub_bins;        // 1: each leaf's rows in 8 bins by the octant of their segment midpoint
+    uint16_t *row_keys;       // [capacity] sort bin of each listed row, written as it is appended
+                              // (nullptr: the sort recomputes it from the row's state)
     uint32_t n_hidden_layers;
     uint32_t n;
     uint32_t n_cut_nodes;
@@ -204,6 +206,8 @@ __device__ __forceinline__ uint32_t row_bin(const WaveArgs &a, uint32_t node, V3
 
 __device__ __forceinline__ uint32_t listed_row_bin(const WaveArgs &a, const WaveList &in, uint32_t r)
 {
+    if (a.row_keys)
+        return a.row_keys[r];
     if (!a.sub_bins)
         return sort_bin(a, in.meta[r].y);
     const float4 od0 = in.od0[r], od1 = in.od1[r];
@@ -419,10 +423,14 @@ __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_co
             }
         }
         const uint32_t pos = warp_append(listed, &a.wave_counts[0]);
-        if (listed)
+        const uint32_t bin = (a.perm && listed) ? row_bin(a, s.seg_node, s.o, s.d, s.seg_mint, s.seg_maxt) : 0u;
+        if (listed) {
             store_state(a.lists[0], pos, s, stack);
+            if (a.row_keys)
+                a.row_keys[pos] = (uint16_t)bin;
+        }
         if (a.perm)
-            count_nodes(a.node_bins, listed, listed ? row_bin(a, s.seg_node, s.o, s.d, s.seg_mint, s.seg_maxt) : 0u);
+            count_nodes(a.node_bins, listed, bin);
     }
 }
 
@@ -793,11 +801,14 @@ __global__ void __launch_bounds__(decode_threads(SMEM_CUT), SMEM_CUT ? 1 : 2) k_
             }
         }
         const uint32_t pos = warp_append(keep, count_out);
-        if (keep)
+        const uint32_t bin = (a.perm && keep) ? row_bin(a, s.seg_node, s.o, s.d, s.seg_mint, s.seg_maxt) : 0u;
+        if (keep) {
             store_state(out, pos, s, stack);
+            if (a.row_keys) // the sort of this step ran before the encoder: the keys are free
+                a.row_keys[pos] = (uint16_t)bin;
+        }
         if (a.perm)
-            count_nodes(a.node_bins + ((it + 1u) & 1u) * a.n_sort_nodes, keep,
-                        keep ? row_bin(a, s.seg_node, s.o, s.d, s.seg_mint, s.seg_maxt) : 0u);
+            count_nodes(a.node_bins + ((it + 1u) & 1u) * a.n_sort_nodes, keep, bin);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -1458,6 +1469,7 @@ cudaError_t launch_wave_query(const float4 *dilated_nodes, const float4 *bounds,
     a.prec = prec;
     const bool sort = res.perm != nullptr && n_bins <= kMaxSortNodes;
     a.perm = sort ? res.perm : nullptr;
+    a.row_keys = (sort && a.n_sort_nodes <= 65536u) ? res.row_keys : nullptr;
     a.ray_order = nullptr;
     a.node_bins = res.node_bins;
     a.node_cursor = res.node_cursor;

@@ -2123,6 +2123,9 @@ uint32_t run_neural_query(const nbvh_handle *h, QueryContext &q, QueryCounters *
     res.node_bins = q.node_bins.ptr;
     res.node_cursor = q.node_cursor.ptr;
     res.sub_bins = q.node_bins.count >= 2u * kSubBins * h->neural_nodes.size();
+    // the ray-order keys are consumed by the placement before the first pass: the rows' sort bins
+    // reuse the buffer from then on
+    res.row_keys = q.ray_keys.count >= q.capacity ? q.ray_keys.ptr : nullptr;
     res.h_words = q.h_words;
     res.ev = q.ev;
     res.wait_ns = h->wait_limit_ns;

@@ -505,6 +505,10 @@ struct StepResources {
     // the rows of each leaf in kSubBins sort bins by the octant of their segment midpoint (needs
     // node_bins / node_cursor of 2 x kSubBins x the cut's nodes)
     bool sub_bins = false;
+    // [capacity] 16-bit sort bin of each listed row, written by the kernel that appends the row and
+    // read by the sort (nullptr: the sort recomputes the bins); may be the ray-order key buffer,
+    // which is free once the first pass has taken the rays
+    uint16_t *row_keys = nullptr;
     bool stall = false;            // failure-path tests: the MLP kernels wait on a barrier nothing arrives at
 };
 
