@@ -621,7 +621,7 @@ def run_ours(args):
         line["scene_config4"] = run_scene_config4(args, nb, scenes)
     if args.serve_seconds > 0:
         line["serving"] = run_serving(args, nb, scenes)
-    # the figures the benchmark spec asks for, compact, at the end of the line
+    # the headline figures (throughputs, accuracy, latencies, rooflines), compact, at the end of the line
     line["summary"] = summary_of(line)
     if rank == 0:
         print(json.dumps(line))
