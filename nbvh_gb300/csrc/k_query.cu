@@ -36,10 +36,18 @@ constexpr uint32_t kSortThreads = 1024;
 constexpr uint32_t kSortMinRows = 1u << 16;
 // Rows with at least this many (point, level) pairs to encode are sorted by octant within a leaf.
 constexpr uint32_t kSubBinMinPointLevels = 32;
-constexpr uint32_t kDefaultVisitsPerRound = 8;  // node visits of a traversal between lane refills
-// Encoder blocks per SM: all resident at once (40 registers a thread, 48 warps per SM), so each
-// block's contiguous range of rows runs in a single wave.
+// node visits of a traversal between lane refills (measured on GB300, 2^22 uniform rays: 4 -> 3.29,
+// 8 -> 3.25, 12 -> 3.24, 16 -> 3.24 ms per query)
+constexpr uint32_t kDefaultVisitsPerRound = 12;
+// Encoder blocks that fit an SM at once (the launch bound: 40 registers a thread, 48 warps per SM);
+// every launch uses at most this many per SM, so each block's contiguous range of rows runs in a
+// single wave.
 constexpr uint32_t kDefaultEncodeBlocksPerSm = 6;
+// Encoder blocks launched per SM by default, fewer than can be resident: each block then takes a
+// longer contiguous range of the sorted rows, so an SM's L1 serves fewer leaf regions at a time
+// (measured on GB300 with the rows sorted by leaf and octant, 2^22 rays: 6 blocks 3.25, 5 3.25,
+// 4 3.21, 3 3.27, 2 3.44 ms per query).
+constexpr uint32_t kEncodeBlocksLaunched = 4;
 // From step tail_step() on, the rays still listed are finished by one persistent kernel
 // (k_wave_tail) instead of one short wavefront step after another: the lists are short by then and
 // each step would cost about the same fixed 60-80 us whatever its length. The switch depends only
@@ -1234,8 +1242,9 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
     cudaError_t e = cudaSuccess;
     const uint32_t F = a.grid.n_features;
     const uint32_t enc_max = F == 2u ? encode_blocks_per_sm<2>() : encode_blocks_per_sm<4>();
+    const uint32_t enc_default = enc_max < kEncodeBlocksLaunched ? enc_max : kEncodeBlocksLaunched;
     const uint32_t enc_per_sm =
-        (r.encode_blocks_per_sm && r.encode_blocks_per_sm <= enc_max) ? r.encode_blocks_per_sm : enc_max;
+        (r.encode_blocks_per_sm && r.encode_blocks_per_sm <= enc_max) ? r.encode_blocks_per_sm : enc_default;
     const uint32_t enc_blocks = (uint32_t)num_sms * enc_per_sm;
     const uint32_t dec_blocks = (uint32_t)num_sms * (SMEM_CUT ? 1u : 2u);
     for (uint32_t it = it0; it < it1; it++) {
