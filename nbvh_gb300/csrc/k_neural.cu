@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(128) k_encode(const __grid_constant__ GridPara
         for (uint32_t k = 0; k < 8u; k++)
             dst[k] = f[k];
     } else {
-        const float2 f = encode_level(table, grid, l, p);
+        const float2 f = encode_level<true>(table, grid, l, p);
         dst[0] = f.x;
         dst[1] = f.y;
     }

@@ -39,15 +39,14 @@ constexpr uint32_t kSubBinMinPointLevels = 32;
 // node visits of a traversal between lane refills (measured on GB300, 2^22 uniform rays: 4 -> 3.29,
 // 8 -> 3.25, 12 -> 3.24, 16 -> 3.24 ms per query)
 constexpr uint32_t kDefaultVisitsPerRound = 12;
-// Encoder blocks that fit an SM at once (the launch bound: 40 registers a thread, 48 warps per SM);
-// every launch uses at most this many per SM, so each block's contiguous range of rows runs in a
-// single wave.
-constexpr uint32_t kDefaultEncodeBlocksPerSm = 6;
-// Encoder blocks launched per SM by default, fewer than can be resident: each block then takes a
-// longer contiguous range of the sorted rows, so an SM's L1 serves fewer leaf regions at a time
-// (measured on GB300 with the rows sorted by leaf and octant, 2^22 rays: 6 blocks 3.25, 5 3.25,
-// 4 3.21, 3 3.27, 2 3.44 ms per query).
-constexpr uint32_t kEncodeBlocksLaunched = 4;
+// Encoder blocks of 256 threads per SM: the launch bound (up to 64 registers a thread; the paired
+// corner gathers use 56 and spill at the 40 of a 6-block bound) and the default launch. Every launch uses at
+// most this many per SM, so each block's contiguous range of rows runs in a single wave; fewer
+// blocks than fit an SM make each block's range of the sorted rows longer, so that an SM's L1
+// serves fewer leaf regions at a time (measured on GB300 with the rows sorted by leaf and octant,
+// 2^22 rays, at a 40-register bound: 6 blocks 3.25, 5 3.25, 4 3.21, 3 3.27, 2 3.44 ms per query;
+// the 64-register bound with paired gathers then took 4 blocks from 3.22 to 3.17-3.19 ms).
+constexpr uint32_t kEncodeBlocksPerSm = 4;
 // From step tail_step() on, the rays still listed are finished by one persistent kernel
 // (k_wave_tail) instead of one short wavefront step after another: the lists are short by then and
 // each step would cost about the same fixed 60-80 us whatever its length. The switch depends only
@@ -448,17 +447,10 @@ __global__ void __launch_bounds__(kFirstThreads, 4) k_wave_first(const __grid_co
 // (src/cuda/neural/neural_bvh_module_kernels.cu:266-303): the segment ends are swapped for a
 // negative mint, then encoded into the dilated scene box. The point is computed once for all its
 // levels, so the kernel's instructions go to the gathers and their interpolation; it holds no
-// MLP state and runs at high occupancy to hide the gather latency. F = 2 (one 32-bit entry per
-// corner) runs 6 blocks of 256 threads per SM at 40 registers; the wider entries of F = 4 and 8
-// hold more gathered words and run 4.
-template <uint32_t F>
-constexpr uint32_t encode_blocks_per_sm()
-{
-    return F == 2u ? kDefaultEncodeBlocksPerSm : 4u;
-}
+// MLP state; its 4 blocks of 256 threads per SM keep many gathers in flight to hide their latency.
 
 template <uint32_t F>
-__global__ void __launch_bounds__(kEncodeThreads, encode_blocks_per_sm<F>())
+__global__ void __launch_bounds__(kEncodeThreads, kEncodeBlocksPerSm)
     k_wave_encode(const __grid_constant__ WaveArgs a, uint32_t it)
 {
     __shared__ GridParams gp;
@@ -529,19 +521,19 @@ __global__ void __launch_bounds__(kEncodeThreads, encode_blocks_per_sm<F>())
             if (vec_store) {
                 for (uint32_t l = lg * LG; l < lg * LG + LG; l += 4u) {
                     uint4 q;
-                    float2 f = encode_level(a.table, gp, l, pos);
+                    float2 f = encode_level<true>(a.table, gp, l, pos);
                     q.x = pack16(f.x, f.y);
-                    f = encode_level(a.table, gp, l + 1u, pos);
+                    f = encode_level<true>(a.table, gp, l + 1u, pos);
                     q.y = pack16(f.x, f.y);
-                    f = encode_level(a.table, gp, l + 2u, pos);
+                    f = encode_level<true>(a.table, gp, l + 2u, pos);
                     q.z = pack16(f.x, f.y);
-                    f = encode_level(a.table, gp, l + 3u, pos);
+                    f = encode_level<true>(a.table, gp, l + 3u, pos);
                     q.w = pack16(f.x, f.y);
                     *reinterpret_cast<uint4 *>(dst + l) = q;
                 }
             } else {
                 for (uint32_t l = 0; l < L; l++) {
-                    const float2 f = encode_level(a.table, gp, l, pos);
+                    const float2 f = encode_level<true>(a.table, gp, l, pos);
                     dst[l] = pack16(f.x, f.y);
                 }
             }
@@ -1241,10 +1233,9 @@ cudaError_t enqueue_steps(const WaveArgs &a, const StepResources &r, size_t dec_
 {
     cudaError_t e = cudaSuccess;
     const uint32_t F = a.grid.n_features;
-    const uint32_t enc_max = F == 2u ? encode_blocks_per_sm<2>() : encode_blocks_per_sm<4>();
-    const uint32_t enc_default = enc_max < kEncodeBlocksLaunched ? enc_max : kEncodeBlocksLaunched;
-    const uint32_t enc_per_sm =
-        (r.encode_blocks_per_sm && r.encode_blocks_per_sm <= enc_max) ? r.encode_blocks_per_sm : enc_default;
+    const uint32_t enc_per_sm = (r.encode_blocks_per_sm && r.encode_blocks_per_sm <= kEncodeBlocksPerSm)
+                                    ? r.encode_blocks_per_sm
+                                    : kEncodeBlocksPerSm;
     const uint32_t enc_blocks = (uint32_t)num_sms * enc_per_sm;
     const uint32_t dec_blocks = (uint32_t)num_sms * (SMEM_CUT ? 1u : 2u);
     for (uint32_t it = it0; it < it1; it++) {

@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(256) k_train_encode(const __grid_constant__ Gr
             *reinterpret_cast<uint4 *>(dst + 8u * l) =
                 make_uint4(pack16(f[0], f[1]), pack16(f[2], f[3]), pack16(f[4], f[5]), pack16(f[6], f[7]));
         } else {
-            const float2 f = encode_level(table, grid, l, pos);
+            const float2 f = encode_level<true>(table, grid, l, pos);
             *reinterpret_cast<uint32_t *>(dst + 2u * l) = pack16(f.x, f.y);
         }
     }

@@ -511,7 +511,7 @@ void autotune(nbvh_server *srv, uint32_t model_id)
     cudaEvent_t e0, e1;
     cuda_check(cudaEventCreate(&e0), "event");
     cuda_check(cudaEventCreate(&e1), "event");
-    const uint32_t visits[3] = {8u, 12u, 16u}, enc[2] = {4u, 6u};
+    const uint32_t visits[3] = {8u, 12u, 16u}, enc[2] = {3u, 4u};
     for (uint32_t b = kMinBucket; b <= sl.capacity; b <<= 2) {
         float best = 1e30f;
         Tuning pick;

@@ -129,8 +129,47 @@ struct MlpPrec<true> {
     }
 };
 
+// Table indices of the corners (x, y, z) and (x + 1, y, z) of one level.
+__device__ __forceinline__ void level_x_pair_index(bool hashed, uint32_t res, uint32_t size, uint32_t x, uint32_t y,
+                                                   uint32_t z, uint32_t &i0, uint32_t &i1)
+{
+    if (hashed) {
+        const uint32_t h = (y * 2654435761u) ^ (z * 805459861u);
+        i0 = (x ^ h) & (size - 1u);
+        i1 = ((x + 1u) ^ h) & (size - 1u);
+    } else {
+        const uint32_t b = y * res + z * res * res;
+        i0 = x + b;
+        i1 = x + 1u + b;
+        if (i0 >= size)
+            i0 %= size;
+        if (i1 >= size)
+            i1 %= size;
+    }
+}
+
+// Entries i0 and i1 of one level's table (`tab` = the level's first entry, 16-byte aligned: level
+// offsets are multiples of 8 entries). When both fall in one aligned pair of entries -- always for
+// an even x on a hashed level, whose hash takes x times 1, and for an even index on a dense level
+// -- one load of the pair serves both corners; otherwise the second is a load of its own.
+__device__ __forceinline__ void gather_x_pair(const uint32_t *__restrict__ tab, uint32_t i0, uint32_t i1,
+                                              uint32_t &v0, uint32_t &v1)
+{
+    const uint2 pr = __ldg(reinterpret_cast<const uint2 *>(tab + (i0 & ~1u)));
+    const bool odd = (i0 & 1u) != 0u;
+    v0 = odd ? pr.y : pr.x;
+    if ((i0 ^ i1) == 1u)
+        v1 = odd ? pr.x : pr.y;
+    else
+        v1 = __ldg(tab + i1);
+}
+
 // Features of one point at one level: 2 values, FMA accumulation over corners c = 0..7 (bit d of
 // c selects the upper corner along axis d), identical operation order to the CPU restatement.
+// PAIRS gathers the x / x + 1 corners with gather_x_pair (the same values; measured on GB300 it
+// pays in the wavefront and training encoders, 3.22 -> 3.17-3.19 ms per 2^22-ray query with the
+// wider register bound, and not in the tail kernel's 16-row tiles, 3.17 -> 3.18 ms).
+template <bool PAIRS>
 __device__ __forceinline__ float2 encode_level(const uint32_t *__restrict__ table, const GridParams &gp, uint32_t l,
                                                V3 p)
 {
@@ -142,18 +181,27 @@ __device__ __forceinline__ float2 encode_level(const uint32_t *__restrict__ tabl
     const uint32_t res = gp.res[l], size = gp.size[l], off = gp.offset[l];
     const bool hashed = gp.hashed[l] != 0u;
     uint32_t v[8];
+    if constexpr (PAIRS) {
 #pragma unroll
-    for (uint32_t c = 0; c < 8; c++) {
-        const uint32_t x = gx + (c & 1u), y = gy + ((c >> 1) & 1u), z = gz + ((c >> 2) & 1u);
-        uint32_t idx;
-        if (hashed) {
-            idx = (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (size - 1u);
-        } else {
-            idx = x + y * res + z * res * res;
-            if (idx >= size)
-                idx %= size;
+        for (uint32_t c = 0; c < 8; c += 2) {
+            uint32_t i0, i1;
+            level_x_pair_index(hashed, res, size, gx, gy + ((c >> 1) & 1u), gz + ((c >> 2) & 1u), i0, i1);
+            gather_x_pair(table + off, i0, i1, v[c], v[c + 1]);
         }
-        v[c] = __ldg(table + off + idx);
+    } else {
+#pragma unroll
+        for (uint32_t c = 0; c < 8; c++) {
+            const uint32_t x = gx + (c & 1u), y = gy + ((c >> 1) & 1u), z = gz + ((c >> 2) & 1u);
+            uint32_t idx;
+            if (hashed) {
+                idx = (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (size - 1u);
+            } else {
+                idx = x + y * res + z * res * res;
+                if (idx >= size)
+                    idx %= size;
+            }
+            v[c] = __ldg(table + off + idx);
+        }
     }
     const float wx0 = __fsub_rn(1.0f, rx), wy0 = __fsub_rn(1.0f, ry), wz0 = __fsub_rn(1.0f, rz);
     float a0 = 0.0f, a1 = 0.0f;
@@ -392,7 +440,7 @@ __device__ __forceinline__ void encode_tile_to_smem(const uint32_t *__restrict__
             float2 f[4];
 #pragma unroll
             for (uint32_t k = 0; k < 4u; k++)
-                f[k] = encode_level(table, gp, l, q[k]);
+                f[k] = encode_level<false>(table, gp, l, q[k]);
 #pragma unroll
             for (uint32_t k = 0; k < 4u; k++)
                 *reinterpret_cast<uint32_t *>(feat + (r0 + k) * ld + 2u * j) =
