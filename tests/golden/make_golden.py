@@ -108,6 +108,19 @@ def main():
             l, g = pyref.loss_and_gradient(kind, t, pr)
             lrows.append([ki, t, pr, l, g])
     out["losses"] = np.array(lrows, np.float32)
+
+    # hash-grid levels with 4 and 8 features per entry (the reference's default encoding has 4):
+    # the same 4-level geometry, own values and points (a generator of its own, so the vectors
+    # above do not move)
+    wide = np.random.default_rng(11)
+    for nf in (4, 8):
+        gridw = wide.uniform(-1, 1, (o, nf)).astype(np.float16).astype(np.float32)
+        ptsw = wide.uniform(-0.01, 1.01, (40, 3)).astype(np.float32)
+        featw = np.array([[pyref.encode_level(gridw, offs[lv], sizes[lv], res[lv], scl[lv], q) for lv in range(4)]
+                          for q in ptsw], np.float32).reshape(40, 4 * nf)
+        out["grid_values_f%d" % nf] = gridw
+        out["grid_points_f%d" % nf] = ptsw
+        out["grid_features_f%d" % nf] = featw
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", os.path.join(HERE, "golden.npz"))
 

@@ -258,11 +258,13 @@ def neural_segments(nodes, ray, dil, mint_eps, maxt_eps, lod=0, stack_size=24):
 
 
 # ---- hash-grid level (tcnn HashGrid behaviour, coherent prime hash) ----
+# grid: [entries][features]; returns the level's features (as many as the grid's columns), each
+# accumulated corner after corner.
 def encode_level(grid, offset, size, res, scale_l, p):
     pos = [fma(F(p[i]), F(scale_l), F(0.5)) for i in range(3)]
     g = [int(np.floor(x)) for x in pos]
     fr = [F(pos[i] - F(np.floor(pos[i]))) for i in range(3)]
-    a0, a1 = F(0), F(0)
+    acc = [F(0)] * grid.shape[1]
     dense = res ** 3 <= size
     for c in range(8):
         x, y, z = (g[0] + (c & 1)) & M32, (g[1] + ((c >> 1) & 1)) & M32, (g[2] + ((c >> 2) & 1)) & M32
@@ -273,9 +275,9 @@ def encode_level(grid, offset, size, res, scale_l, p):
         idx %= size
         w = F(F((fr[0] if c & 1 else F(F(1) - fr[0])) * (fr[1] if c & 2 else F(F(1) - fr[1]))) *
               (fr[2] if c & 4 else F(F(1) - fr[2])))
-        a0 = fma(w, grid[offset + idx, 0], a0)
-        a1 = fma(w, grid[offset + idx, 1], a1)
-    return a0, a1
+        for k in range(len(acc)):
+            acc[k] = fma(w, grid[offset + idx, k], acc[k])
+    return tuple(acc)
 
 
 # ---- include/cuda/neural/neural_bvh_module_common.cuh:23-58 (LocalT) ----

@@ -1,6 +1,6 @@
 """Pins the C oracle to the golden vectors of the independent Python restatement
 (tests/golden/pyref.py -> golden.npz): RNG, sin/cos, classic closest/any hit, neural segments,
-hash-grid features, LocalT decode and the composite-loss terms."""
+hash-grid features (2, 4 and 8 per entry), LocalT decode and the composite-loss terms."""
 
 import ctypes as C
 import os
@@ -56,6 +56,24 @@ def test_grid_features(oracle):
     net.grid_f16, net.weights_f16 = g16.ctypes.data, w16.ctypes.data
     feats = oracle.encode(net, G["grid_points"].reshape(-1, 1, 3))
     assert np.array_equal(feats.view(np.uint32), G["grid_features"].view(np.uint32))
+    del keep
+
+
+@pytest.mark.parametrize("nf", [4, 8])
+def test_grid_features_wide(oracle, nf):
+    """4 and 8 FP16 features per table entry: feature k of every corner accumulated in corner order."""
+    off, size, res, scl = G["grid_offsets"], G["grid_sizes"], G["grid_res"], G["grid_scale"]
+    g16 = np.ascontiguousarray(G["grid_values_f%d" % nf].astype(np.float16).view(np.uint16))
+    w16 = np.zeros(16, np.uint16)
+    net = Network()
+    net.n_levels, net.n_points, net.n_inputs, net.n_neurons, net.n_hidden_layers = 4, 1, 4 * nf, 64, 1
+    net.n_features = nf
+    keep = [off, size, res, scl, g16, w16]
+    net.level_offset, net.level_size = off.ctypes.data, size.ctypes.data
+    net.level_resolution, net.level_scale = res.ctypes.data, scl.ctypes.data
+    net.grid_f16, net.weights_f16 = g16.ctypes.data, w16.ctypes.data
+    feats = oracle.encode(net, G["grid_points_f%d" % nf].reshape(-1, 1, 3))
+    assert np.array_equal(feats.view(np.uint32), G["grid_features_f%d" % nf].view(np.uint32))
     del keep
 
 
