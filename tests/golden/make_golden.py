@@ -121,6 +121,18 @@ def main():
         out["grid_values_f%d" % nf] = gridw
         out["grid_points_f%d" % nf] = ptsw
         out["grid_features_f%d" % nf] = featw
+    # the network: 4 levels x 2 features of one point (8 inputs), 2 hidden layers of 64, FP16 weights
+    netr = np.random.default_rng(12)
+    n_w = 64 * 8 + 64 * 64 + 16 * 64
+    wts = (netr.standard_normal(n_w) * 0.3).astype(np.float16)
+    pts_n = netr.uniform(0.0, 1.0, (40, 3)).astype(np.float32)
+    mlp_out = []
+    for q in pts_n:
+        x = [v for lv in range(4) for v in pyref.encode_level(grid, offs[lv], sizes[lv], res[lv], scl[lv], q)]
+        mlp_out.append(pyref.mlp_forward(wts.astype(np.float32), 8, 2, x))
+    out["mlp_weights"] = wts.view(np.uint16)
+    out["mlp_points"] = pts_n
+    out["mlp_outputs"] = np.array(mlp_out, np.float32)
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", os.path.join(HERE, "golden.npz"))
 

@@ -6,6 +6,8 @@ contraction); fused multiply-adds are evaluated in double and rounded to float32
 file:line in the reference project.
 """
 
+import math
+
 import numpy as np
 
 F = np.float32
@@ -278,6 +280,33 @@ def encode_level(grid, offset, size, res, scale_l, p):
         for k in range(len(acc)):
             acc[k] = fma(w, grid[offset + idx, k], acc[k])
     return tuple(acc)
+
+
+# ---- tcnn FullyFusedMLP as configured at src/cuda/neural/neural_bvh_module.cu:232-238 ----
+# No biases, ReLU hidden layers, Sigmoid output padded to 16 rows. Matrices in network-first
+# parameter order, each [rows][cols] row-major: W0 [n_neurons][n_inputs], then n_hidden_layers - 1
+# times [n_neurons][n_neurons], then [16][n_neurons]. The layer inputs are FP16 values (the features
+# rounded once, every hidden activation rounded to FP32 and then to FP16); the products are summed
+# in double, input after input.
+def mlp_forward(weights, n_inputs, n_hidden_layers, x, n_neurons=64):
+    shapes = [(n_neurons, n_inputs)] + [(n_neurons, n_neurons)] * (n_hidden_layers - 1) + [(16, n_neurons)]
+    a = [float(np.float16(v)) for v in x]
+    off = 0
+    out = None
+    for m, (rows, cols) in enumerate(shapes):
+        w = weights[off:off + rows * cols].astype(np.float64).reshape(rows, cols)
+        off += rows * cols
+        nxt = []
+        for r in range(rows):
+            acc = 0.0
+            for k in range(cols):
+                acc += float(w[r, k]) * a[k]
+            nxt.append(acc)
+        if m == len(shapes) - 1:
+            out = [F(1.0 / (1.0 + math.exp(-v))) for v in nxt]
+        else:
+            a = [float(np.float16(F(v) if v > 0.0 else F(0))) for v in nxt]
+    return out
 
 
 # ---- include/cuda/neural/neural_bvh_module_common.cuh:23-58 (LocalT) ----

@@ -1,6 +1,7 @@
 """Pins the C oracle to the golden vectors of the independent Python restatement
 (tests/golden/pyref.py -> golden.npz): RNG, sin/cos, classic closest/any hit, neural segments,
-hash-grid features (2, 4 and 8 per entry), LocalT decode and the composite-loss terms."""
+hash-grid features (2, 4 and 8 per entry), the network forward, LocalT decode and the
+composite-loss terms."""
 
 import ctypes as C
 import os
@@ -74,6 +75,28 @@ def test_grid_features_wide(oracle, nf):
     net.grid_f16, net.weights_f16 = g16.ctypes.data, w16.ctypes.data
     feats = oracle.encode(net, G["grid_points_f%d" % nf].reshape(-1, 1, 3))
     assert np.array_equal(feats.view(np.uint32), G["grid_features_f%d" % nf].view(np.uint32))
+    del keep
+
+
+def test_network_forward(oracle):
+    """The network on encoded points: matrix layout and order, no biases, ReLU, the FP16 rounding of
+    the features and of every hidden activation, the sigmoid output."""
+    off, size, res, scl = G["grid_offsets"], G["grid_sizes"], G["grid_res"], G["grid_scale"]
+    g16 = np.ascontiguousarray(G["grid_values"].astype(np.float16).view(np.uint16))
+    w16 = np.ascontiguousarray(G["mlp_weights"])
+    net = Network()
+    net.n_levels, net.n_points, net.n_inputs, net.n_neurons, net.n_hidden_layers = 4, 1, 8, 64, 2
+    keep = [off, size, res, scl, g16, w16]
+    net.level_offset, net.level_size = off.ctypes.data, size.ctypes.data
+    net.level_resolution, net.level_scale = res.ctypes.data, scl.ctypes.data
+    net.grid_f16, net.weights_f16 = g16.ctypes.data, w16.ctypes.data
+    out = oracle.network_inference(net, G["mlp_points"].reshape(-1, 1, 3))
+    want = G["mlp_outputs"]
+    # both sum the products in double in the same order; the outputs agree to the last bit
+    # unless a double lands within an ulp of an FP32 / FP16 rounding boundary
+    assert np.abs(out - want).max() <= 1e-6
+    assert (out.view(np.uint32) == want.view(np.uint32)).mean() >= 0.99
+    assert want.std() > 0.01  # the outputs are not all saturated
     del keep
 
 
