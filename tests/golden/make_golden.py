@@ -133,6 +133,22 @@ def main():
     out["mlp_weights"] = wts.view(np.uint16)
     out["mlp_points"] = pts_n
     out["mlp_outputs"] = np.array(mlp_out, np.float32)
+
+    # Adam: 3 steps from step 9 with the decay starting at step 10, every step (so the first step
+    # has the full rate and the next two halve it), L2 term on
+    adr = np.random.default_rng(13)
+    p0 = adr.standard_normal(64).astype(np.float32)
+    grads = (adr.standard_normal((3, 64)) * 0.1).astype(np.float32)
+    pa, ma, va = list(p0), [F(0)] * 64, [F(0)] * 64
+    hyper = dict(lr=F(1e-2), beta1=F(0.9), beta2=F(0.999), eps=F(1e-8), l2_reg=F(1e-3), decay_start=10,
+                 decay_interval=1, decay_base=F(0.5))
+    for k in range(3):
+        pyref.adam_step(pa, ma, va, grads[k], 9 + k, **hyper)
+    out["adam_params0"] = p0
+    out["adam_grads"] = grads
+    out["adam_params3"] = np.array(pa, np.float32)
+    out["adam_m3"] = np.array(ma, np.float32)
+    out["adam_v3"] = np.array(va, np.float32)
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", os.path.join(HERE, "golden.npz"))
 

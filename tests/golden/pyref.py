@@ -309,6 +309,27 @@ def mlp_forward(weights, n_inputs, n_hidden_layers, x, n_neurons=64):
     return out
 
 
+# ---- Adam with ExponentialDecay (optimizer configured at src/cuda/neural/neural_bvh_module.cu:146-168) ----
+# Bias-corrected Adam (Kingma and Ba, Algorithm 1) with the L2 term added to the gradient; the
+# learning rate lr * base^floor((step - start) / interval) from step `start` on, folded with the
+# bias corrections into one step size in double, then FP32 arithmetic per parameter.
+def adam_step(params, m, v, grad, step, lr, beta1, beta2, eps, l2_reg, decay_start, decay_interval, decay_base):
+    lr_s = float(lr)
+    if step >= decay_start and decay_interval > 0:
+        lr_s *= math.pow(float(decay_base), float((step - decay_start) // decay_interval))
+    t = float(step) + 1.0
+    lr_t = F(lr_s * math.sqrt(1.0 - math.pow(float(beta2), t)) / (1.0 - math.pow(float(beta1), t)))
+    b1, b2, e, l2 = F(beta1), F(beta2), F(eps), F(l2_reg)
+    omb1, omb2 = F(F(1) - b1), F(F(1) - b2)
+    for i in range(len(params)):
+        w = F(params[i])
+        g = F(F(grad[i]) + F(l2 * w))
+        mi = F(F(b1 * F(m[i])) + F(omb1 * g))
+        vi = F(F(b2 * F(v[i])) + F(omb2 * F(g * g)))
+        m[i], v[i] = mi, vi
+        params[i] = F(w - F(lr_t * F(mi / F(F(np.sqrt(vi)) + e))))
+
+
 # ---- include/cuda/neural/neural_bvh_module_common.cuh:23-58 (LocalT) ----
 def decode_local_t(out_depth, mint, maxt, inside, depth_epsilon=F(0.2), fixed_depth_epsilon=F(1e-5)):
     seg_len = F(F(maxt) - F(mint))

@@ -1,6 +1,6 @@
 """Pins the C oracle to the golden vectors of the independent Python restatement
 (tests/golden/pyref.py -> golden.npz): RNG, sin/cos, classic closest/any hit, neural segments,
-hash-grid features (2, 4 and 8 per entry), the network forward, LocalT decode and the
+hash-grid features (2, 4 and 8 per entry), the network forward, Adam, LocalT decode and the
 composite-loss terms."""
 
 import ctypes as C
@@ -98,6 +98,22 @@ def test_network_forward(oracle):
     assert (out.view(np.uint32) == want.view(np.uint32)).mean() >= 0.99
     assert want.std() > 0.01  # the outputs are not all saturated
     del keep
+
+
+def test_adam(oracle):
+    """Three Adam steps across the start of the learning-rate decay, L2 term on: parameters and both
+    moments bit-identical."""
+    from types import SimpleNamespace
+    opt = SimpleNamespace(learning_rate=1e-2, beta1=0.9, beta2=0.999, epsilon=1e-8, l2_reg=1e-3, decay_start=10,
+                          decay_interval=1, decay_base=0.5)
+    cfg = SimpleNamespace(optimizer=opt)
+    p = G["adam_params0"].copy()
+    m = np.zeros_like(p)
+    v = np.zeros_like(p)
+    for k in range(3):
+        oracle.adam_step(p, m, v, G["adam_grads"][k], 9 + k, cfg)
+    for got, key in ((p, "adam_params3"), (m, "adam_m3"), (v, "adam_v3")):
+        assert np.array_equal(got.view(np.uint32), G[key].view(np.uint32)), key
 
 
 def test_decode_local_t(oracle):
