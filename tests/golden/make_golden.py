@@ -149,6 +149,19 @@ def main():
     out["adam_params3"] = np.array(pa, np.float32)
     out["adam_m3"] = np.array(ma, np.float32)
     out["adam_v3"] = np.array(va, np.float32)
+    # the neural closest-hit query on the depth-4 cut: 2 points per segment over the 4-level grid
+    # (16 inputs), 2 hidden layers, the library's default constants; the scene box is the cut's root
+    qr = np.random.default_rng(14)
+    wq = (qr.standard_normal(64 * 16 + 64 * 64 + 16 * 64) * 0.3).astype(np.float16)
+    rmn, rmx = nb.nodes_to_float(neural[:1])
+    consts = dict(node_extent_dilation=1e-4, fixed_node_dilation=1e-5, mint_eps=1e-4, maxt_eps=1e-3, points=2,
+                  distribution=0, threshold=0.5, depth_epsilon=0.2, fixed_depth_epsilon=1e-5, max_steps=1000)
+    levels = list(zip(offs, sizes, res, scl))
+    qhits = np.array([pyref.neural_query(neural, r, rmn[0], rmx[0], grid, levels, wq.astype(np.float32), 2, consts)
+                      for r in nrays], np.uint32)
+    out["query_weights"] = wq.view(np.uint16)
+    out["query_scene_box"] = np.concatenate([rmn[0], rmx[0]]).astype(np.float32)
+    out["query_hits"] = qhits
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", os.path.join(HERE, "golden.npz"))
 

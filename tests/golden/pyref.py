@@ -211,15 +211,12 @@ def dilated(nodes, i, dil):
     return mn, mx, cnt, off
 
 
-def neural_segments(nodes, ray, dil, mint_eps, maxt_eps, lod=0, stack_size=24):
-    o = [F(x) for x in ray[0:3]]
-    d = [F(x) for x in ray[4:7]]
-    rmint, rmaxt = -FLT_MAX, FLT_MAX
-    stack = [0]
-    out = []
+def next_segment(nodes, o, d, stack, rmaxt, dil, mint_eps, maxt_eps, lod=0, stack_size=24):
+    """Resumes the traversal from `stack` up to the next accepted leaf, with the traversal's current
+    depth rmaxt: (mint, maxt, node), or None once the stack is exhausted."""
+    rmint = -FLT_MAX
     while stack:
         ni = stack.pop()
-        found = None
         while True:
             bmin, bmax, cnt, off = dilated(nodes, ni, dil)
             if (0 < cnt <= 2 + lod) or off == M32:
@@ -231,12 +228,8 @@ def neural_segments(nodes, ray, dil, mint_eps, maxt_eps, lod=0, stack_size=24):
                     valid = mint < rmaxt
                     valid = valid and (maxt > maxt_eps if mint < 0 else mint > mint_eps)
                     if valid:
-                        found = (mint, maxt, ni)
-                        break
-                if not stack:
-                    break
-                ni = stack.pop()
-                continue
+                        return mint, maxt, ni
+                break
             c1, c2 = off, off + 1
             b1 = dilated(nodes, c1, dil)
             b2 = dilated(nodes, c2, dil)
@@ -245,18 +238,25 @@ def neural_segments(nodes, ray, dil, mint_eps, maxt_eps, lod=0, stack_size=24):
             if d1 > d2:
                 d1, d2, c1, c2 = d2, d1, c2, c1
             if d1 == FLT_MAX:
-                if not stack:
-                    break
-                ni = stack.pop()
-            else:
-                ni = c1
-                if d2 != FLT_MAX:
-                    stack.append(c2)
-                    assert len(stack) < stack_size
-        if found is None:
-            break
-        out.append(found)
-    return out
+                break
+            ni = c1
+            if d2 != FLT_MAX:
+                stack.append(c2)
+                assert len(stack) < stack_size
+    return None
+
+
+def neural_segments(nodes, ray, dil, mint_eps, maxt_eps, lod=0, stack_size=24):
+    """Every leaf the traversal enters, in traversal order, with no depth found yet."""
+    o = [F(x) for x in ray[0:3]]
+    d = [F(x) for x in ray[4:7]]
+    stack = [0]
+    out = []
+    while True:
+        seg = next_segment(nodes, o, d, stack, FLT_MAX, dil, mint_eps, maxt_eps, lod, stack_size)
+        if seg is None:
+            return out
+        out.append(seg)
 
 
 # ---- hash-grid level (tcnn HashGrid behaviour, coherent prime hash) ----
@@ -328,6 +328,71 @@ def adam_step(params, m, v, grad, step, lr, beta1, beta2, eps, l2_reg, decay_sta
         vi = F(F(b2 * F(v[i])) + F(omb2 * F(g * g)))
         m[i], v[i] = mi, vi
         params[i] = F(w - F(lr_t * F(mi / F(F(np.sqrt(vi)) + e))))
+
+
+# ---- the neural closest-hit query of one ray ----
+# Traversal: neural_bvh2.cuh:170-292, resumed after every network step with the current depth
+# (neural_bvh_module_common.cuh:496-550). Network input: encode_segment_from_world_po_pi and
+# encode_bvh_network_input_data (neural_bvh_module_kernels.cu:10-97, 266-303): the segment ends
+# swapped for a negative mint, mapped into the dilated scene box, points at equidistant interior
+# (distribution 0) or exterior (1) positions. Output: neural_node_traversal and
+# process_neural_bvh_traversal_step (neural_bvh_module_common.cuh:160-206,
+# path_inference_kernels.cu:61-131) without depth interpolation: visible when the first output is
+# above the threshold, LocalT depth, the hit kept when it is nearer, normal = normalize(2 n - 1).
+# The ray's tmax is the query's current depth. Returns the 12-word record: t, normal, albedo,
+# visibility, flags (bit 0 hit, bit 2 step cap), segments evaluated, 0xFFFFFFFF, 0.
+def neural_query(nodes, ray, scene_min, scene_max, grid, levels, weights, n_hidden_layers, c):
+    o = [F(x) for x in ray[0:3]]
+    d = [F(x) for x in ray[4:7]]
+    best_t = F(ray[7])
+    valid, flags, segments = False, 0, 0
+    normal, albedo, vis = [F(0)] * 3, [F(0)] * 3, F(0)
+    dilation = F(F(F(1) + F(c["node_extent_dilation"])) + F(c["fixed_node_dilation"]))
+    ext = [F(F(F(scene_max[i]) - F(scene_min[i])) * dilation) for i in range(3)]
+    center = [F(F(F(scene_max[i]) + F(scene_min[i])) * F(0.5)) for i in range(3)]
+    P = c["points"]
+    if c["distribution"] == 1:
+        delta, offset = (F(1) if P == 1 else F(F(1) / F(P - 1))), F(0)
+    else:
+        delta, offset = F(F(1) / F(P)), F(0.5)
+    seg_args = (F(c["fixed_node_dilation"]), F(c["mint_eps"]), F(c["maxt_eps"]))
+    stack = [0]
+    seg = next_segment(nodes, o, d, stack, FLT_MAX, *seg_args)
+    thr = F(c["threshold"])
+    step = 0
+    while seg is not None:
+        if step > c["max_steps"]:
+            flags |= 4
+            break
+        step += 1
+        mint, maxt, _ = seg
+        a, b = (maxt, mint) if mint < 0 else (mint, maxt)
+        epo = [F(F(F(F(o[i] + F(d[i] * a)) - center[i]) / ext[i]) + F(0.5)) for i in range(3)]
+        epi = [F(F(F(F(o[i] + F(d[i] * b)) - center[i]) / ext[i]) + F(0.5)) for i in range(3)]
+        x = []
+        for k in range(P):
+            t = F(delta * F(F(k) + offset))
+            omt = F(F(1) - t)
+            pt = [F(F(epo[i] * omt) + F(epi[i] * t)) for i in range(3)]
+            for (off, size, res, scl) in levels:
+                x.extend(encode_level(grid, off, size, res, scl, pt))
+        out = mlp_forward(weights, len(x), n_hidden_layers, x)
+        segments += 1
+        new_depth = best_t
+        if out[0] > thr:
+            de = decode_local_t(out[1], mint, maxt, mint < 0, F(c["depth_epsilon"]), F(c["fixed_depth_epsilon"]))
+            if de != FLT_MAX and de < best_t:
+                valid, best_t, new_depth, vis = True, de, de, out[0]
+                n = [F(F(out[2 + i] * F(2)) - F(1)) for i in range(3)]
+                inv = F(F(1) / F(np.sqrt(F(F(F(n[0] * n[0]) + F(n[1] * n[1])) + F(n[2] * n[2])))))
+                normal = [F(n[i] * inv) for i in range(3)]
+                albedo = [out[5], out[6], out[7]]
+        if not stack:
+            break
+        seg = next_segment(nodes, o, d, stack, new_depth, *seg_args)
+    words = [F(best_t if valid else FLT_MAX)] + normal + albedo + [F(vis if valid else 0)]
+    rec = [int(np.float32(w).view(np.uint32)) for w in words]
+    return rec + [(1 if valid else 0) | flags, segments, M32, 0]
 
 
 # ---- include/cuda/neural/neural_bvh_module_common.cuh:23-58 (LocalT) ----

@@ -1,7 +1,7 @@
 """Pins the C oracle to the golden vectors of the independent Python restatement
 (tests/golden/pyref.py -> golden.npz): RNG, sin/cos, classic closest/any hit, neural segments,
-hash-grid features (2, 4 and 8 per entry), the network forward, Adam, LocalT decode and the
-composite-loss terms."""
+hash-grid features (2, 4 and 8 per entry), the network forward, Adam, the whole neural query,
+LocalT decode and the composite-loss terms."""
 
 import ctypes as C
 import os
@@ -114,6 +114,35 @@ def test_adam(oracle):
         oracle.adam_step(p, m, v, G["adam_grads"][k], 9 + k, cfg)
     for got, key in ((p, "adam_params3"), (m, "adam_m3"), (v, "adam_v3")):
         assert np.array_equal(got.view(np.uint32), G[key].view(np.uint32)), key
+
+
+def test_neural_query(oracle):
+    """The whole neural closest-hit query of every ray (traversal resumed with the current depth,
+    segment points, features, network, visibility threshold, LocalT, nearest hit, normal and albedo):
+    all 12 record words bit-identical."""
+    from oracle.bindings import NeuralConsts
+    off, size, res, scl = G["grid_offsets"], G["grid_sizes"], G["grid_res"], G["grid_scale"]
+    g16 = np.ascontiguousarray(G["grid_values"].astype(np.float16).view(np.uint16))
+    w16 = np.ascontiguousarray(G["query_weights"])
+    net = Network()
+    net.n_levels, net.n_points, net.n_inputs, net.n_neurons, net.n_hidden_layers = 4, 2, 16, 64, 2
+    keep = [off, size, res, scl, g16, w16]
+    net.level_offset, net.level_size = off.ctypes.data, size.ctypes.data
+    net.level_resolution, net.level_scale = res.ctypes.data, scl.ctypes.data
+    net.grid_f16, net.weights_f16 = g16.ctypes.data, w16.ctypes.data
+    c = NeuralConsts()
+    c.inference_mint_epsilon, c.inference_maxt_epsilon = 1e-4, 1e-3
+    c.fixed_node_dilation, c.node_extent_dilation = 1e-5, 1e-4
+    c.primary_visibility_threshold = c.secondary_visibility_threshold = 0.5
+    c.depth_epsilon, c.fixed_depth_epsilon = 0.2, 1e-5
+    c.input_segment_points, c.segment_distribution, c.bvh_lod, c.max_traversal_steps = 2, 0, 0, 1000
+    scene = oracle.neural_scene(G["neural_nodes"], G["query_scene_box"])
+    hits = oracle.neural_query(scene, net, c, G["neural_rays"], depth=1)
+    want = G["query_hits"]
+    assert np.array_equal(hits, want), np.argwhere(hits != want)[:5]
+    assert 10 < ((want[:, 8] & 1) != 0).sum() < len(want)  # hits and misses
+    assert want[:, 9].max() >= 2  # rays that go on past a first segment
+    del keep
 
 
 def test_decode_local_t(oracle):
