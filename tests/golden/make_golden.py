@@ -162,6 +162,18 @@ def main():
     out["query_weights"] = wq.view(np.uint16)
     out["query_scene_box"] = np.concatenate([rmn[0], rmx[0]]).astype(np.float32)
     out["query_hits"] = qhits
+    # training rays on the same cut and mesh (step 3 of batches of 4,096, 4 points per segment,
+    # per-triangle albedo), with leaf-boundary sampling off and always on
+    alb = np.random.default_rng(15).uniform(0, 1, (len(f), 3)).astype(np.float32)
+    tcon = dict(node_extent_dilation=1e-4, fixed_node_dilation=1e-5, learning_mint_eps=1e-3, learning_maxt_eps=1e-3,
+                sampling_bbox_scaling=1.5, points=4, distribution=0)
+    for name, ratio in (("train0", 0.0), ("train1", 1.0)):
+        rows = [pyref.training_sample(i, 3, 4096, neural, rmn[0], rmx[0], nodes, prims, v, f, alb,
+                                      dict(tcon, leaf_boundary_sampling_ratio=ratio)) for i in range(96)]
+        out[name + "_points"] = np.array([r[0] for r in rows], np.float32)
+        out[name + "_targets"] = np.array([r[1] for r in rows], np.float32)
+        out[name + "_nodes"] = np.array([r[2] for r in rows], np.uint32)
+    out["train_albedo"] = alb
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", os.path.join(HERE, "golden.npz"))
 

@@ -395,6 +395,98 @@ def neural_query(nodes, ray, scene_min, scene_max, grid, levels, weights, n_hidd
     return rec + [(1 if valid else 0) | flags, segments, M32, 0]
 
 
+# ---- training rays: granular_sample_bvh_network_input_data (neural_bvh_module_kernels.cu:119-264)
+# with one sample per thread (no bounce continues), stack_based_sample_uniform_bvh_density and
+# sample_bbox_position (neural_bvh_module_common.cuh:635-780), labels from
+# generate_single_bvh_network_output_reference (:782-858) with LocalT depth, the geometric normal
+# (compute_its_data, include/cuda/accel/bvh.cuh:55-95) and a per-triangle albedo (0.9 without one).
+# Vector constructors draw their random components x first. Returns (points [P][3], targets [8],
+# sampled node).
+def _normalize(v):
+    inv = F(F(1) / F(np.sqrt(dot(v, v))))
+    return scale(v, inv)
+
+
+def _uniform_sphere(sx, sy):
+    sp, cp = sincos_turns(sx)
+    cos_t = F(F(sy * F(2)) - F(1))
+    sin_t = F(np.sqrt(F(F(1) - F(cos_t * cos_t))))
+    return [F(sin_t * cp), F(sin_t * sp), cos_t]
+
+
+def _cube_pos_on_face(face, u, v):
+    return [[F(1), u, v], [F(0), u, v], [u, F(1), v], [u, F(0), v], [u, v, F(1)], [u, v, F(0)]][face]
+
+
+def training_sample(i, training_step, batch_size, cut, scene_min, scene_max, bvh, prims, verts, idx, albedo, c,
+                    learned_lod=6, n_lods=7):
+    rng = Rng(lcg_seed((training_step * batch_size) & M32, 0, i))
+    direction = _uniform_sphere(rng.f(), rng.f())
+    n_learned = n_lods - learned_lod
+    lod = learned_lod + min(int(F(rng.f() * F(n_learned))), n_learned - 1)
+    dil = F(F(c["fixed_node_dilation"]) + F(rng.f() * F(c["node_extent_dilation"])))
+    sbs = F(c["sampling_bbox_scaling"])
+    ext = sub([F(x) for x in scene_max], [F(x) for x in scene_min])
+    seg, stack, o = None, [], None
+    while seg is None:
+        if not stack:  # the ray escaped: a new origin, the same direction, the traversal from the root
+            stack = [0]
+            ps = [rng.f(), rng.f(), rng.f()]
+            local = [F(F(sbs * ps[k]) - F(F(sbs - F(1)) * F(0.5))) for k in range(3)]
+            o = [F(F(local[k] * ext[k]) + F(scene_min[k])) for k in range(3)]
+        seg = next_segment(cut, o, direction, stack, FLT_MAX, dil, F(c["learning_mint_eps"]),
+                           F(c["learning_maxt_eps"]), lod)
+    mint, maxt, node = seg
+    d = direction
+    ratio = F(c["leaf_boundary_sampling_ratio"])
+    if ratio != 0 and rng.f() <= ratio:
+        f1 = min(int(F(rng.f() * F(6))), 5)
+        while True:
+            f2 = min(int(F(rng.f() * F(6))), 5)
+            if f2 != f1:
+                break
+        lp1 = _cube_pos_on_face(f1, rng.f(), rng.f())
+        lp2 = _cube_pos_on_face(f2, rng.f(), rng.f())
+        bmn, _, bmx, _ = node_box(cut, node)
+        nex = sub(bmx, bmn)
+        center = add(bmn, scale(nex, F(0.5)))
+        nex = scale(nex, F(F(1) + dil))
+        nmin = sub(center, scale(nex, F(0.5)))
+        entry = [F(nmin[k] + F(lp1[k] * nex[k])) for k in range(3)]
+        exitp = [F(nmin[k] + F(lp2[k] * nex[k])) for k in range(3)]
+        o, d = entry, _normalize(sub(exitp, entry))
+        span = sub(exitp, entry)
+        mint, maxt = F(0), F(np.sqrt(dot(span, span)))
+    # segment points (no swap for a negative mint on this path)
+    cq = dict(c, points=c["points"])
+    dilation = F(F(F(1) + F(c["node_extent_dilation"])) + F(c["fixed_node_dilation"]))
+    sext = [F(F(F(scene_max[k]) - F(scene_min[k])) * dilation) for k in range(3)]
+    center = [F(F(F(scene_max[k]) + F(scene_min[k])) * F(0.5)) for k in range(3)]
+    epo = [F(F(F(F(o[k] + F(d[k] * mint)) - center[k]) / sext[k]) + F(0.5)) for k in range(3)]
+    epi = [F(F(F(F(o[k] + F(d[k] * maxt)) - center[k]) / sext[k]) + F(0.5)) for k in range(3)]
+    P = cq["points"]
+    if c["distribution"] == 1:
+        delta, offset = (F(1) if P == 1 else F(F(1) / F(P - 1))), F(0)
+    else:
+        delta, offset = F(F(1) / F(P)), F(0.5)
+    pts = []
+    for k in range(P):
+        t = rng.f() if c["distribution"] == 2 else F(delta * F(F(k) + offset))
+        omt = F(F(1) - t)
+        pts.append([F(F(epo[j] * omt) + F(epi[j] * t)) for j in range(3)])
+    # labels from the classic BLAS on [mint, maxt]
+    t, _, _, prim = classic_intersect(bvh, prims, verts, idx, o + [mint] + d + [maxt])
+    if t == FLT_MAX:
+        return pts, [F(0)] * 8, node
+    depth = F((float(F(t - mint))) / (float(F(maxt - mint)) + 1e-3))
+    ix = idx[prim]
+    v0, v1, v2 = ([F(x) for x in verts[ix[k]]] for k in range(3))
+    n = _normalize(cross(sub(v1, v0), sub(v2, v0)))
+    nn = [F(F(n[k] + F(1)) * F(0.5)) for k in range(3)]
+    alb = [F(x) for x in albedo[prim]] if albedo is not None else [F(0.9)] * 3
+    return pts, [F(1), depth] + nn + alb, node
+
+
 # ---- include/cuda/neural/neural_bvh_module_common.cuh:23-58 (LocalT) ----
 def decode_local_t(out_depth, mint, maxt, inside, depth_epsilon=F(0.2), fixed_depth_epsilon=F(1e-5)):
     seg_len = F(F(maxt) - F(mint))

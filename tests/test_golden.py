@@ -1,7 +1,7 @@
 """Pins the C oracle to the golden vectors of the independent Python restatement
 (tests/golden/pyref.py -> golden.npz): RNG, sin/cos, classic closest/any hit, neural segments,
 hash-grid features (2, 4 and 8 per entry), the network forward, Adam, the whole neural query,
-LocalT decode and the composite-loss terms."""
+training rays with their labels, LocalT decode and the composite-loss terms."""
 
 import ctypes as C
 import os
@@ -143,6 +143,26 @@ def test_neural_query(oracle):
     assert 10 < ((want[:, 8] & 1) != 0).sum() < len(want)  # hits and misses
     assert want[:, 9].max() >= 2  # rays that go on past a first segment
     del keep
+
+
+@pytest.mark.parametrize("name,ratio", [("train0", 0.0), ("train1", 1.0)])
+def test_training_rays(oracle, name, ratio):
+    """Training rays (direction, LoD and dilation draws, origins in the scaled scene box until a leaf
+    is entered, leaf-boundary resampling, segment points) and their classic labels (visibility,
+    LocalT depth, geometric normal, albedo): bit-identical, with leaf-boundary sampling off and on."""
+    from oracle.bindings import NeuralConsts
+    c = NeuralConsts()
+    c.learning_mint_epsilon, c.learning_maxt_epsilon = 1e-3, 1e-3
+    c.fixed_node_dilation, c.node_extent_dilation = 1e-5, 1e-4
+    c.sampling_bbox_scaling, c.leaf_boundary_sampling_ratio = 1.5, ratio
+    c.input_segment_points, c.segment_distribution, c.bvh_lod, c.max_traversal_steps = 4, 0, 0, 1000
+    nscene = oracle.neural_scene(G["neural_nodes"], G["query_scene_box"])
+    cscene = oracle.classic_scene(G["bvh_nodes"], G["bvh_prims"], G["mesh_v"], G["mesh_f"])
+    pos, tgt, nodes = oracle.training_batch(nscene, cscene, G["train_albedo"], c, 3, 4096, 96)
+    assert np.array_equal(pos.view(np.uint32), G[name + "_points"].view(np.uint32))
+    assert np.array_equal(tgt.view(np.uint32), G[name + "_targets"].view(np.uint32))
+    assert np.array_equal(nodes, G[name + "_nodes"])
+    assert 10 < (tgt[:, 0] == 1).sum() < len(tgt)  # labelled hits and misses
 
 
 def test_decode_local_t(oracle):
