@@ -4,8 +4,9 @@ Workload (N-BVH inference): a 65,536-triangle fBm-displaced sphere in the unit c
 BVH2 cut at depth 10 (1,024 neural leaves), 4 stratified points per leaf segment, hash grid of 16
 levels x 2 FP16 features x 2^19 entries (resolution 16..2048), 64-wide 4-hidden-layer ReLU MLP in
 FP16, 2^22 query rays (origins uniform in the 1.5x scene box, directions uniform on the sphere).
-The network is trained on the device by the library's own optimiser on classic-labelled rays before
-timing (weights of the reference are not available). A step is one neural closest-hit query over
+The network was trained on a GB300 by the library's own optimiser on classic-labelled rays (20,000
+steps; the weights are committed under bench_data/, `--retrain` trains afresh before timing; weights
+of the reference are not available). A step is one neural closest-hit query over
 the 2^22 resident rays; the classic BVH kernel answers the same rays for the "vs classic" figure and
 judges depth / visibility.
 
