@@ -108,7 +108,9 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms during the timed region: start()
+    returns once the first sample has arrived (nvidia-smi takes a while to come up), stop() waits for
+    one more sample before ending the sampler, so the timed region lies between sampled lines."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -122,12 +124,18 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self._wait_for(1, 5.0)
         except Exception:
             self.proc = None
+
+    def _wait_for(self, count, seconds):
+        t_end = time.perf_counter() + seconds
+        while len(self.lines) < count and time.perf_counter() < t_end and self.proc.poll() is None:
+            time.sleep(0.005)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -136,6 +144,7 @@ class ClockSampler:
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self._wait_for(len(self.lines) + 1, 1.0)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
