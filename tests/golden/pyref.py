@@ -458,13 +458,12 @@ def training_sample(i, training_step, batch_size, cut, scene_min, scene_max, bvh
         span = sub(exitp, entry)
         mint, maxt = F(0), F(np.sqrt(dot(span, span)))
     # segment points (no swap for a negative mint on this path)
-    cq = dict(c, points=c["points"])
     dilation = F(F(F(1) + F(c["node_extent_dilation"])) + F(c["fixed_node_dilation"]))
     sext = [F(F(F(scene_max[k]) - F(scene_min[k])) * dilation) for k in range(3)]
     center = [F(F(F(scene_max[k]) + F(scene_min[k])) * F(0.5)) for k in range(3)]
     epo = [F(F(F(F(o[k] + F(d[k] * mint)) - center[k]) / sext[k]) + F(0.5)) for k in range(3)]
     epi = [F(F(F(F(o[k] + F(d[k] * maxt)) - center[k]) / sext[k]) + F(0.5)) for k in range(3)]
-    P = cq["points"]
+    P = c["points"]
     if c["distribution"] == 1:
         delta, offset = (F(1) if P == 1 else F(F(1) / F(P - 1))), F(0)
     else:
