@@ -1,0 +1,54 @@
+"""The GPU neural query against the golden vectors of the independent Python restatement
+(tests/golden/pyref.py, the vectors that also pin the C oracle bit for bit): the same mesh, depth-4
+cut, 4-level hash grid (2 features, 256-entry tables), 2 points per segment, 2-hidden-layer FP16
+network and default constants, on the same 120 rays. The network runs on the tensor cores, which
+sum in another order than the restatement's double sums, so the bar is the query bar: hit decisions
+equal except on threshold-borderline rays, and t, normal and albedo close on rays that hit in both."""
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import nbvh_gb300 as nb
+
+pytestmark = pytest.mark.gpu
+
+G = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden.npz"))
+
+
+def test_neural_query_against_the_restatement(built):
+    cfg = nb.default_config(**{"hashgrid.n_levels": 4, "hashgrid.n_features_per_level": 2,
+                               "hashgrid.log2_hashmap_size": 8, "hashgrid.base_resolution": 4,
+                               "hashgrid.per_level_scale": 2.0, "network.n_hidden_layers": 2,
+                               "module.input_segment_points": 2, "module.segment_distribution": 0})
+    with nb.NBVH(cfg) as h:
+        h.set_mesh(G["mesh_v"], G["mesh_f"])
+        h.build_classic()
+        h.build_neural_cut(4)
+        nodes, bbox = h.neural_bvh()
+        # the handle holds the restatement's cut, scene box and grid geometry
+        assert np.array_equal(nodes, G["neural_nodes"])
+        assert np.array_equal(bbox.view(np.uint32), G["query_scene_box"].view(np.uint32))
+        L = h.layout
+        nl = L.n_levels
+        assert list(L.level_offset[:nl]) == list(G["grid_offsets"]) and list(L.level_size[:nl]) == list(G["grid_sizes"])
+        assert list(L.level_resolution[:nl]) == list(G["grid_res"])
+        assert np.array_equal(np.array(L.level_scale[:nl], np.float32), G["grid_scale"])
+        w = G["query_weights"].view(np.float16).astype(np.float32)
+        assert L.n_network_params == len(w) and L.n_params == len(w) + G["grid_values"].size
+        h.set_params(np.concatenate([w, G["grid_values"].reshape(-1)]).astype(np.float32))
+        rays = torch.from_numpy(np.ascontiguousarray(G["neural_rays"])).cuda()
+        got = h.query_closest_neural(rays).cpu().numpy().view(np.uint32)
+    want = G["query_hits"]
+    hit_got, hit_want = (got[:, 8] & 1) != 0, (want[:, 8] & 1) != 0
+    assert 10 < hit_want.sum() < len(want)
+    # a visibility output within the network's rounding of the threshold may go either way
+    assert (hit_got != hit_want).sum() <= 2
+    both = hit_got & hit_want
+    tg, tw = got[both, 0].view(np.float32), want[both, 0].view(np.float32)
+    close = np.abs(tg - tw) <= 1e-3 * np.maximum(np.abs(tw), 1e-2)
+    assert close.mean() >= 0.97, (tg[~close], tw[~close])
+    fg, fw = got[both, 1:7].view(np.float32), want[both, 1:7].view(np.float32)
+    assert np.abs(fg - fw)[close].max() <= 1e-2  # normal and albedo
