@@ -1,9 +1,14 @@
-"""The GPU neural query against the golden vectors of the independent Python restatement
-(tests/golden/pyref.py, the vectors that also pin the C oracle bit for bit): the same mesh, depth-4
-cut, 4-level hash grid (2 features, 256-entry tables), 2 points per segment, 2-hidden-layer FP16
-network and default constants, on the same 120 rays. The network runs on the tensor cores, which
-sum in another order than the restatement's double sums, so the bar is the query bar: hit decisions
-equal except on threshold-borderline rays, and t, normal and albedo close on rays that hit in both."""
+"""The GPU kernels against the golden vectors of the independent Python restatement
+(tests/golden/pyref.py, the vectors that also pin the C oracle bit for bit), on the same mesh and
+depth-4 cut:
+
+* the neural query with a 4-level hash grid (2 features, 256-entry tables), 2 points per segment, a
+  2-hidden-layer FP16 network and the default constants, on the same 120 rays. The network runs on
+  the tensor cores, which sum in another order than the restatement's double sums, so the bar is
+  the query bar: hit decisions equal except on threshold-borderline rays, and t, normal and albedo
+  close on rays that hit in both;
+* 96 training rows of step 3 of 4,096-row batches with their classic labels, leaf-boundary sampling
+  off and on: bit-identical."""
 
 import os
 
@@ -52,3 +57,19 @@ def test_neural_query_against_the_restatement(built):
     assert close.mean() >= 0.97, (tg[~close], tw[~close])
     fg, fw = got[both, 1:7].view(np.float32), want[both, 1:7].view(np.float32)
     assert np.abs(fg - fw)[close].max() <= 1e-2  # normal and albedo
+
+
+@pytest.mark.parametrize("name,ratio", [("train0", 0.0), ("train1", 1.0)])
+def test_training_rows_against_the_restatement(built, name, ratio):
+    cfg = nb.default_config(batch_size=4096, **{"bvh.leaf_boundary_sampling_ratio": ratio})
+    with nb.NBVH(cfg) as h:
+        h.set_mesh(G["mesh_v"], G["mesh_f"], G["train_albedo"])
+        h.build_classic()
+        h.build_neural_cut(4)
+        assert np.array_equal(h.neural_bvh()[0], G["neural_nodes"])
+        pos, tgt, nodes = h.generate_training_batch(3, 96)
+        pos, tgt = pos.cpu().numpy(), tgt.cpu().numpy()
+        nodes = nodes.cpu().numpy().view(np.uint32)
+    assert np.array_equal(nodes, G[name + "_nodes"])
+    assert np.array_equal(pos.view(np.uint32), G[name + "_points"].view(np.uint32))
+    assert np.array_equal(tgt.view(np.uint32), G[name + "_targets"].view(np.uint32))
