@@ -8,7 +8,8 @@ depth-4 cut:
   the query bar: hit decisions equal except on threshold-borderline rays, and t, normal and albedo
   close on rays that hit in both;
 * 96 training rows of step 3 of 4,096-row batches with their classic labels, leaf-boundary sampling
-  off and on: bit-identical."""
+  off and on: bit-identical;
+* hash-grid features of the 4-level grid with 2, 4 and 8 features per entry: bit-identical."""
 
 import os
 
@@ -73,3 +74,21 @@ def test_training_rows_against_the_restatement(built, name, ratio):
     assert np.array_equal(nodes, G[name + "_nodes"])
     assert np.array_equal(pos.view(np.uint32), G[name + "_points"].view(np.uint32))
     assert np.array_equal(tgt.view(np.uint32), G[name + "_targets"].view(np.uint32))
+
+
+@pytest.mark.parametrize("nf", [2, 4, 8])
+def test_encoding_against_the_restatement(built, nf):
+    key = "" if nf == 2 else "_f%d" % nf
+    pts, want = G["grid_points" + key], G["grid_features" + key]
+    P = 2 if nf == 2 else 1  # 2 x 4 x 2 inputs: network inputs come in multiples of 16
+    cfg = nb.default_config(**{"hashgrid.n_levels": 4, "hashgrid.n_features_per_level": nf,
+                               "hashgrid.log2_hashmap_size": 8, "hashgrid.base_resolution": 4,
+                               "hashgrid.per_level_scale": 2.0, "module.input_segment_points": P})
+    with nb.NBVH(cfg) as h:
+        grid = G["grid_values" + key]
+        L = h.layout
+        assert L.n_grid_entries == grid.shape[0]
+        h.set_params(np.concatenate([np.zeros(L.n_network_params, np.float32), grid.reshape(-1)]))
+        n = len(pts) // P * P
+        got = h.encode(torch.from_numpy(np.ascontiguousarray(pts[:n].reshape(-1, P, 3))).cuda()).cpu().numpy()
+    assert np.array_equal(got.reshape(n, -1).view(np.uint32), want[:n].view(np.uint32))
