@@ -174,6 +174,17 @@ def main():
         out[name + "_targets"] = np.array([r[1] for r in rows], np.float32)
         out[name + "_nodes"] = np.array([r[2] for r in rows], np.uint32)
     out["train_albedo"] = alb
+
+    # a path-traced 8 x 6 frame, 2 samples per pixel, 2 bounces, ground plane and sky, on the
+    # query's network and cut
+    pp = dict(origin=[0.5, 0.45, -1.2], du=[0.7, 0.0, 0.0], dv=[0.0, -0.55, 0.0], tl=[-0.35, 0.275, 1.0], width=8,
+              height=6, spp=2, sample_base=4, sample_offset=1, seed=7, max_bounces=2, has_ground=1, ground_y=0.1,
+              ground_albedo=[0.5, 0.4, 0.3], sky_zenith=[0.3, 0.5, 0.9], sky_horizon=[0.9, 0.9, 0.8])
+    img, traced = pyref.path_trace(neural, rmn[0], rmx[0], grid, levels, wq.astype(np.float32), 2, consts, pp)
+    out["path_params"] = np.array(pp["origin"] + pp["du"] + pp["dv"] + pp["tl"] + [pp["ground_y"]] +
+                                  pp["ground_albedo"] + pp["sky_zenith"] + pp["sky_horizon"], np.float32)
+    out["path_image"] = img
+    out["path_traced"] = np.array([traced], np.uint64)
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", os.path.join(HERE, "golden.npz"))
 

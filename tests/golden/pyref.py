@@ -486,6 +486,88 @@ def training_sample(i, training_step, batch_size, cut, scene_min, scene_max, bvh
     return pts, [F(1), depth] + nn + alb, node
 
 
+# ---- the library's hybrid path tracer (k_path.cu; the Lambertian case of the reference's scatter,
+# path_inference_kernels.cu:224-429): camera rays with a per-sample jitter, one neural query per
+# bounce, an analytic ground plane and sky, cosine-weighted bounces about the normal in the
+# orthonormal basis of Duff et al. (JCGT 6(1), 2017), throughput times albedo, radiance from the
+# sky. Returns the RGB image [width * height][3] and the rays traced.
+def _cosine_sample(n, rng):
+    u1, u2 = rng.f(), rng.f()
+    sp, cp = sincos_turns(u2)
+    r, z = F(np.sqrt(u1)), F(np.sqrt(gmax(F(0), F(F(1) - u1))))
+    sign = F(1) if n[2] >= 0 else F(-1)
+    a = F(F(-1) / F(sign + n[2]))
+    c = F(F(n[0] * n[1]) * a)
+    t = [F(F(1) + F(F(F(sign * n[0]) * n[0]) * a)), F(sign * c), F(-F(sign * n[0]))]
+    b = [c, F(sign + F(F(n[1] * n[1]) * a)), F(-n[1])]
+    rc, rs = F(r * cp), F(r * sp)
+    return [F(F(F(rc * t[k]) + F(rs * b[k])) + F(z * n[k])) for k in range(3)]
+
+
+def path_trace(nodes, scene_min, scene_max, grid, levels, weights, n_hidden_layers, c, p):
+    W, Hh, spp = p["width"], p["height"], p["spp"]
+    du, dv, tl, org = ([F(x) for x in p[k]] for k in ("du", "dv", "tl", "origin"))
+    rays, ids, thr = [], [], []
+    n = W * Hh * spp
+    rad = [[F(0)] * 3 for _ in range(n)]
+    for i in range(n):
+        px, smp = i // spp, i % spp
+        x, y = px % W, px // W
+        rng = Rng(lcg_seed((p["sample_base"] + smp) & M32, p["sample_offset"], px))
+        jx, jy = rng.f(), rng.f()
+        xf, yf = F(F(F(x) + jx) / F(W)), F(F(F(y) + jy) / F(Hh))
+        d = _normalize(add(add(scale(du, xf), scale(dv, yf)), tl))
+        rays.append(org + [F(1e-4)] + d + [FLT_MAX])
+        ids.append(i)
+        thr.append([F(1), F(1), F(1), rng.state ^ ((p["seed"] * 0x9E3779B9) & M32)])
+    traced = 0
+    zen, hor, galb = ([F(x) for x in p[k]] for k in ("sky_zenith", "sky_horizon", "ground_albedo"))
+    for bounce in range(p["max_bounces"] + 1):
+        if not rays:
+            break
+        traced += len(rays)
+        nxt, nxt_ids = [], []
+        for ray, pid in zip(rays, ids):
+            h = neural_query(nodes, ray, scene_min, scene_max, grid, levels, weights, n_hidden_layers, c)
+            ro, d = ray[0:3], ray[4:7]
+            words = np.array(h[:7], np.uint32).view(np.float32)
+            t = F(words[0]) if h[8] & 1 else FLT_MAX
+            nrm, alb = [F(v) for v in words[1:4]], [F(v) for v in words[4:7]]
+            if p["has_ground"] and d[1] != 0:
+                tp = F(F(F(p["ground_y"]) - ro[1]) / d[1])
+                if tp > F(1e-4) and tp < t:
+                    t, nrm, alb = tp, [F(0), F(1), F(0)], galb
+            th = thr[pid]
+            if t == FLT_MAX:
+                w = gmax(d[1], F(0))
+                for k in range(3):
+                    rad[pid][k] = F(rad[pid][k] + F(th[k] * F(hor[k] + F(F(zen[k] - hor[k]) * w))))
+            elif bounce < p["max_bounces"]:
+                ln = F(np.sqrt(F(F(F(nrm[0] * nrm[0]) + F(nrm[1] * nrm[1])) + F(nrm[2] * nrm[2]))))
+                nrm = [F(v / ln) for v in nrm] if ln > 0 else [F(-v) for v in d]
+                if F(F(F(nrm[0] * d[0]) + F(nrm[1] * d[1])) + F(nrm[2] * d[2])) > 0:
+                    nrm = [F(-v) for v in nrm]
+                rng = Rng(th[3])
+                nd = _cosine_sample(nrm, rng)
+                for k in range(3):
+                    th[k] = F(th[k] * alb[k])
+                th[3] = rng.state
+                o = [F(F(ro[k] + F(t * d[k])) + F(F(1e-3) * nrm[k])) for k in range(3)]
+                if F(F(th[0] + th[1]) + th[2]) > 0:
+                    nxt.append(o + [F(1e-4)] + nd + [FLT_MAX])
+                    nxt_ids.append(pid)
+        rays, ids = nxt, nxt_ids
+    inv = F(F(1) / F(spp))
+    img = []
+    for px in range(W * Hh):
+        acc = [F(0)] * 3
+        for smp in range(spp):
+            for k in range(3):
+                acc[k] = F(acc[k] + rad[px * spp + smp][k])
+        img.append([F(v * inv) for v in acc])
+    return np.array(img, np.float32), traced
+
+
 # ---- include/cuda/neural/neural_bvh_module_common.cuh:23-58 (LocalT) ----
 def decode_local_t(out_depth, mint, maxt, inside, depth_epsilon=F(0.2), fixed_depth_epsilon=F(1e-5)):
     seg_len = F(F(maxt) - F(mint))

@@ -1,7 +1,8 @@
 """Pins the C oracle to the golden vectors of the independent Python restatement
 (tests/golden/pyref.py -> golden.npz): RNG, sin/cos, classic closest/any hit, neural segments,
 hash-grid features (2, 4 and 8 per entry), the network forward, Adam, the whole neural query,
-training rays with their labels, LocalT decode and the composite-loss terms."""
+training rays with their labels, a path-traced frame, LocalT decode and the composite-loss
+terms."""
 
 import ctypes as C
 import os
@@ -163,6 +164,43 @@ def test_training_rays(oracle, name, ratio):
     assert np.array_equal(tgt.view(np.uint32), G[name + "_targets"].view(np.uint32))
     assert np.array_equal(nodes, G[name + "_nodes"])
     assert 10 < (tgt[:, 0] == 1).sum() < len(tgt)  # labelled hits and misses
+
+
+def test_path_trace(oracle):
+    """A path-traced frame (camera jitter, neural hits, ground plane, sky, cosine bounces,
+    throughput, per-pixel average) on the query's network and cut: every pixel bit-identical, and
+    the same number of rays traced."""
+    from oracle.bindings import NeuralConsts, PathParams
+    off, size, res, scl = G["grid_offsets"], G["grid_sizes"], G["grid_res"], G["grid_scale"]
+    g16 = np.ascontiguousarray(G["grid_values"].astype(np.float16).view(np.uint16))
+    w16 = np.ascontiguousarray(G["query_weights"])
+    net = Network()
+    net.n_levels, net.n_points, net.n_inputs, net.n_neurons, net.n_hidden_layers = 4, 2, 16, 64, 2
+    keep = [off, size, res, scl, g16, w16]
+    net.level_offset, net.level_size = off.ctypes.data, size.ctypes.data
+    net.level_resolution, net.level_scale = res.ctypes.data, scl.ctypes.data
+    net.grid_f16, net.weights_f16 = g16.ctypes.data, w16.ctypes.data
+    c = NeuralConsts()
+    c.inference_mint_epsilon, c.inference_maxt_epsilon = 1e-4, 1e-3
+    c.fixed_node_dilation, c.node_extent_dilation = 1e-5, 1e-4
+    c.primary_visibility_threshold = c.secondary_visibility_threshold = 0.5
+    c.depth_epsilon, c.fixed_depth_epsilon = 0.2, 1e-5
+    c.input_segment_points, c.segment_distribution, c.bvh_lod, c.max_traversal_steps = 2, 0, 0, 1000
+    scene = oracle.neural_scene(G["neural_nodes"], G["query_scene_box"])
+    v = G["path_params"]
+    pp = PathParams()
+    for k in range(3):
+        pp.origin[k], pp.du[k], pp.dv[k], pp.tl[k] = v[k], v[3 + k], v[6 + k], v[9 + k]
+        pp.ground_albedo[k], pp.sky_zenith[k], pp.sky_horizon[k] = v[13 + k], v[16 + k], v[19 + k]
+    pp.width, pp.height, pp.spp, pp.sample_base, pp.sample_offset, pp.seed = 8, 6, 2, 4, 1, 7
+    pp.max_bounces, pp.has_ground, pp.ground_y = 2, 1, v[12]
+    img = np.empty((48, 4), np.float32)
+    traced = oracle.lib.orc_path_trace(C.byref(scene), C.byref(net), C.byref(c), C.byref(pp),
+                                       C.c_void_p(img.ctypes.data), C.c_int(1))
+    assert traced == int(G["path_traced"][0])
+    assert np.array_equal(img[:, :3].view(np.uint32), G["path_image"].view(np.uint32))
+    assert (G["path_image"].sum(1) > 0).sum() > 10  # lit pixels
+    del keep
 
 
 def test_decode_local_t(oracle):
