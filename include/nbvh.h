@@ -745,10 +745,11 @@ nbvh_status nbvh_debug_device_level_scales(const nbvh_config *cfg, int device, f
  *    Split larger batches into several calls.
  *  - The call cannot be captured into a CUDA graph: it reads the list lengths back to the host
  *    between steps and synchronises its stream before it returns.
- *  - The first call on each device, with that device current, looks up the buffer's device
- *    address once (setup) and keeps it for the life of the process; a first call with n = 0 does
- *    only that, so a caller can take the setup's latency before its first frame. Do not use the
- *    library across a reset of the device (cudaDeviceReset), which may move the buffer.
+ *  - The first call on each device loads the library's device code there if nothing has yet
+ *    (setup); a first call with n = 0 does only that, so a caller can take the setup's latency
+ *    before its first frame. Every call looks the buffer's address up again (no allocation), so
+ *    handles created after a reset of the device (cudaDeviceReset) find it where the reloaded
+ *    code put it; handles created before the reset are invalid, as for every call.
  *  - Each call zeroes the counters it uses before its first kernel; nothing relies on the buffer's
  *    contents from an earlier call.
  *  - There is one buffer per device, shared by every handle on it. Calls that overlap in time on

@@ -1569,27 +1569,20 @@ cudaError_t launch_copy_late(const uint32_t *late, const uint32_t *late_count, u
 
 namespace {
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
-constexpr int kNoallocMaxDevices = 64;
 } // namespace
 
+// The buffer on `device`, which the caller has made current. Its address is looked up on every
+// call (the lookup allocates nothing): a module that the runtime loads again after a device reset
+// places the buffer anew, and a handle created after the reset must not use the old address.
 cudaError_t noalloc_scratch(int device, NoallocScratch *out)
 {
-    static std::mutex mu;
-    static unsigned char *base[kNoallocMaxDevices] = {};
-    if (device < 0 || device >= kNoallocMaxDevices)
+    if (device < 0)
         return cudaErrorInvalidDevice;
-    unsigned char *p;
-    {
-        std::lock_guard<std::mutex> lock(mu);
-        if (!base[device]) {
-            void *addr = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
-            if (e != cudaSuccess)
-                return e;
-            base[device] = static_cast<unsigned char *>(addr);
-        }
-        p = base[device];
-    }
+    void *addr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (e != cudaSuccess)
+        return e;
+    unsigned char *p = static_cast<unsigned char *>(addr);
     const size_t n = kNoallocRays;
     for (int k = 0; k < 2; k++) {
         WaveList &L = out->lists[k];
